@@ -1,0 +1,344 @@
+#!/usr/bin/env python
+"""Benchmark of the SPH workpiece hot path on GB300 (one JSON line on rank 0).
+
+Workload: the interaction micro-benchmark -- 4,194,304 particles on a
+2048 x 2048 lattice (dx = 2.5 um, positions jittered +-0.05 dx, velocity
+N(0, 1 m/s), symmetric Cauchy stress N(0, 200 MPa), density 7850 kg/m^3 x
+(1 + U(-1e-3, 1e-3)), h = 1.7 dx, AISI 1045 Johnson-Cook), seeded synthetic
+data.  One step = one full leap-frog step of leap_frog::step without a tool:
+cell-list build (hash, stable sort, cell tables, reorder), predictor, EOS,
+artificial stress, neighbour sums, stress rate / continuity / momentum /
+advection, corrector, Johnson-Cook return mapping, boundary conditions and
+invalidation.  Metric: particle-steps/s (higher is better).
+
+Arms:
+  default            the CUDA library (fused kernels, CUDA-graph replay); the
+                     headline is the FP32-compensated form, the plain FP64
+                     form is reported beside it.
+  --impl reference   the reference's CPU implementation of the path (the CPU
+                     oracle restatement, all host threads) on a bounded
+                     sample of the same workload.
+Multi-GPU (--gpus N under torchrun): replicas -- every rank advances its own
+copy of the workload; no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-steps/s on 1 GB300, plain FP64 vs chosen form at <=1% force/temp error"
+UNIT = "particle-steps/s"
+
+# Algorithmic bytes per particle of the fused neighbour-sum kernel (one launch
+# processes N particles): its own record, hash, the start-of-step state it
+# corrects and the rates / state it writes; neighbour records are counted as
+# cache hits (each is read from HBM once per launch, by its owner).
+ALGO_BYTES = {
+    "fp64": dict(read=128 + 4 + (16 + 16 + 32 + 8 + 8) + 32 + 8 + 16 + 16 + 8 + 8 + 8,
+                 write=(16 + 16 + 32 + 8 + 8) + (16 + 16 + 32 + 8 + 8) + 8 + 8 + 4),
+    "fp32k": dict(read=64 + 4 + (16 + 16 + 32 + 8 + 8) + 32 + 8 + 16 + 16 + 16 + 8 + 8 + 8 + 8,
+                  write=(16 + 16 + 32 + 8 + 8) + (16 + 16 + 32 + 8 + 8) + 8 + 8 + 4),
+}
+STAGES = ["hash+histogram", "scan+scatter+rank", "reorder+predict+eos+artstress+records", "fem half step",
+          "neighbour sums+epilogue", "fem update+tool move", "contact/bc/invalidate tail"]
+# fields a caller moves per step in the end-to-end arm (the persistent state)
+E2E_FIELDS = ["pos", "vel", "h", "rho", "S", "fc", "ft", "n", "fixed", "blanked", "tool_particle", "eps_pl",
+              "eps_pl_dot", "T", "pos_t", "vel_t", "rho_t", "S_t", "T_t", "on_seg", "hash"]
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+
+    def __init__(self, index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_sample(case, max_seconds=15.0, min_steps=1):
+    """Time whole oracle steps of the workload (all host threads)."""
+    from oracle.oracle import OracleSim, num_threads
+    o = OracleSim(case.constants, case.grid, case.particles, case.dt)
+    o.step()   # warm-up (first touch, thread pool)
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        o.step()
+        n += 1
+        el = time.perf_counter() - t0
+        if n >= min_steps and el >= max_seconds:
+            break
+        if el + el / n > 2.5 * max_seconds:
+            break
+    return case.N * n / el, num_threads(), n, el
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU implementation (oracle restatement)."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from sph_fem_2d_cutting_gpu_gb300 import setups
+    from oracle.oracle import OracleSim, num_threads
+    case = setups.micro(n_side=args.n_side, seed=args.seed)
+    # bounded sample: a square sub-lattice of the workload sized for ~2 s per step
+    side = min(args.n_side, args.ref_side)
+    sub = setups.micro(n_side=side, seed=args.seed)
+    o = OracleSim(sub.constants, sub.grid, sub.particles, sub.dt)
+    for _ in range(args.warmup):
+        o.step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.step()
+    el = time.perf_counter() - t0
+    v = sub.N * args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": f"micro {case.info['n_side']}x{case.info['n_side']} lattice, dx=2.5um, h=1.7dx, "
+                               "full leap-frog step without tool", "particles": case.N,
+                   "sample_particles": sub.N},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": num_threads(), "kind": "port",
+                         "sample": f"{args.steps} whole steps of a {side}x{side} sub-lattice of the workload "
+                                   f"(reference CPU restatement, OpenMP)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_product(args):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from sph_fem_2d_cutting_gpu_gb300 import abi, setups
+    from sph_fem_2d_cutting_gpu_gb300.solver import Solver
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if dist is None:
+            return x
+        t = torch.tensor([x], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    case = setups.micro(n_side=args.n_side, seed=args.seed + rank)
+    hbm_peak, peak_kind = peaks()
+    results = {}
+    for prec_name, prec in (("fp32k", abi.SPH_PREC_FP32K), ("fp64", abi.SPH_PREC_FP64)):
+        if args.precision != "both" and args.precision != prec_name:
+            continue
+        s = Solver(case, prec, device=local)
+        stream_ptr = C.c_void_p()
+        s.lib.sph_get_stream(s.ctx, C.byref(stream_ptr))
+        ext = torch.cuda.ExternalStream(stream_ptr.value, device=torch.device("cuda", local))
+        for _ in range(args.warmup):
+            s.step()
+        s.sync()
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        clocks = Clocks(local) if rank == 0 else None
+        n0 = s.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        s.step(args.steps)
+        e1.record(ext)
+        e1.synchronize()
+        launches = s.launch_count() - n0
+        torch.cuda.synchronize()
+        barrier()
+        ck = clocks.stop() if clocks else None
+        ms = e0.elapsed_time(e1) / args.steps
+        ms = max_over_ranks(ms)
+        st = s.status()
+        # per-stage device times (same kernels, issued without the graph)
+        stage_ms = (C.c_float * 7)()
+        ns = C.c_int32()
+        s._ck(s.lib.sph_profile_steps(s.ctx, args.steps, stage_ms, C.byref(ns)), "sph_profile_steps")
+        stage = [v / args.steps for v in stage_ms]
+        res = dict(ms=ms, launches=launches / args.steps * args.steps, clocks=ck, status=st,
+                   stage_ms=dict(zip(STAGES, stage)), launches_per_step=launches / args.steps)
+        # end-to-end through the C ABI with pinned host buffers
+        if not args.no_e2e:
+            fields = {}
+            full = s.download(E2E_FIELDS)
+            for k, v in full.items():
+                t = torch.empty(v.shape, dtype=torch.float64 if v.dtype == np.float64 else torch.int32,
+                                pin_memory=True)
+                a = t.numpy()
+                a[...] = v
+                fields[k] = (t, a)
+            host_in = {k: a for k, (_, a) in fields.items()}
+            outs = {}
+            for k, v in full.items():
+                t = torch.empty(v.shape, dtype=torch.float64 if v.dtype == np.float64 else torch.int32,
+                                pin_memory=True)
+                outs[k] = (t, t.numpy())
+            host_out = {k: a for k, (_, a) in outs.items()}
+            pin_in = abi.particles_struct(host_in, s.N)
+            pin_out = abi.particles_struct(host_out, s.N)
+            nbytes = sum(a.nbytes for a in host_in.values())
+            for _ in range(max(1, args.warmup // 2)):
+                s._ck(s.lib.sph_upload_particles(s.ctx, C.byref(pin_in)), "upload")
+                s.step()
+                s._ck(s.lib.sph_download_particles(s.ctx, C.byref(pin_out)), "download")
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                s._ck(s.lib.sph_upload_particles(s.ctx, C.byref(pin_in)), "upload")
+                s.step()
+                s._ck(s.lib.sph_download_particles(s.ctx, C.byref(pin_out)), "download")
+            el = time.perf_counter() - t0
+            el = max_over_ranks(el)
+            res["e2e"] = dict(value=world * case.N * args.steps / el, unit=UNIT, h2d_bytes_per_step=nbytes,
+                              d2h_bytes_per_step=nbytes)
+        stage_interact = stage[4]
+        ab = ALGO_BYTES[prec_name]
+        algo = (ab["read"] + ab["write"]) * case.N
+        ach = algo / (stage_interact * 1e-3) / 1e9
+        res["roofline"] = {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                           "frac": ach / hbm_peak, "traffic": None,
+                           "kernel": f"k_interact{'32' if prec_name == 'fp32k' else '64'}<fused>",
+                           "algo_bytes_per_particle": ab["read"] + ab["write"], "peak_kind": peak_kind}
+        results[prec_name] = res
+        s.close()
+        del s
+        torch.cuda.empty_cache()
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return 0
+    head_name = "fp32k" if "fp32k" in results else "fp64"
+    head = results[head_name]
+    value = world * case.N / (head["ms"] * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32k" if head_name == "fp32k" else "f64",
+        "data": "synthetic (seeded): jittered lattice, random velocity/stress/density",
+        "config": {"workload": f"micro {case.info['n_side']}x{case.info['n_side']} lattice ({case.N} particles), "
+                               "dx=2.5um, h=1.7dx, cells h / 5x5 stencil, AISI 1045 JC; full leap-frog step "
+                               "without tool",
+                   "particles": case.N, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (about 3 GB of particle state per GPU)",
+                   "form": "FP32 neighbour sums with Kahan compensation, FP64 state/positions/residual"
+                           if head_name == "fp32k" else "plain FP64"},
+        "roofline": head["roofline"],
+        "clocks": head["clocks"],
+        "gpu_launches": int(round(head["launches"])),
+        "stage_ms": head["stage_ms"],
+        "status": head["status"],
+    }
+    if "e2e" in head:
+        line["e2e"] = head["e2e"]
+    if "fp64" in results and head_name != "fp64":
+        f = results["fp64"]
+        line["fp64"] = {"value": world * case.N / (f["ms"] * 1e-3), "ms_per_step": f["ms"],
+                        "stage_ms": f["stage_ms"], "roofline": f["roofline"], "clocks": f["clocks"],
+                        "e2e": f.get("e2e")}
+        line["speedup_vs_fp64"] = f["ms"] / head["ms"]
+    if not args.no_cpu:
+        v, cores, n, el = cpu_sample(case, max_seconds=args.cpu_seconds)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"{n} whole steps of the full workload in {el:.1f}s "
+                                          f"(CPU oracle restatement, OpenMP)"}
+    print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="product", choices=["product", "reference"])
+    ap.add_argument("--precision", default="both", choices=["both", "fp32k", "fp64"])
+    ap.add_argument("--n-side", type=int, default=2048)
+    ap.add_argument("--ref-side", type=int, default=1024)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_product(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,302 @@
+/*
+ * sphfem.h -- C ABI of the GB300 (sm_103a) SPH workpiece hot path.
+ *
+ * Drop-in boundary for the per-timestep path of the hybrid SPH-FEM 2D
+ * cutting solver (nyzhang1227/SPH_FEM_2D_cutting_gpu).  The reference has no
+ * plugin layer; its boundary is the set of C++ functions and methods that
+ * `leap_frog::step(particle_gpu*, grid_base*, tool_FEM*)` calls
+ * (leap_frog.cu:162-248).  Every entry point below replaces one of those
+ * calls; the replaced reference interface is cited beside each one.
+ *
+ * Conventions
+ *  - Every function returns an int status (SPH_OK == 0).  No exceptions or
+ *    process exits cross the ABI; CUDA errors map to SPH_ERR_CUDA and the
+ *    message is available from sph_last_error().
+ *  - All arithmetic state is FP64 in the caller-visible views ("double" for
+ *    the reference's float_t with USE_DOUBLE, types.h:22,57-86).  Vector
+ *    fields are interleaved exactly like the reference's double2/double4.
+ *  - One context == one CUDA device + one CUDA stream.  Calls on one context
+ *    are not thread-safe; separate contexts are independent.
+ *  - Device memory is owned by the context.  Host arrays passed in or out are
+ *    owned by the caller and copied synchronously.
+ *  - Like the reference's Green grid (grid_gpu_green.cu:152-182,204-205) the
+ *    sort swaps the particle arrays with a second buffer, so device pointers
+ *    returned by sph_get_particles() are valid only until the next sort/step.
+ */
+#ifndef SPHFEM_H
+#define SPHFEM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPHFEM_ABI_VERSION 1
+
+/* ---- return codes ------------------------------------------------------ */
+enum {
+    SPH_OK = 0,
+    SPH_ERR_INVALID = 1,   /* bad argument or size                         */
+    SPH_ERR_CUDA = 2,      /* a CUDA runtime call failed                   */
+    SPH_ERR_NO_DEVICE = 3, /* no CUDA device / wrong architecture          */
+    SPH_ERR_ALLOC = 4,     /* device or host allocation failed             */
+    SPH_ERR_STATE = 5      /* call not valid in this state (e.g. no tool)  */
+};
+
+/* ---- device status word bits (sph_status) ------------------------------- */
+#define SPH_STATUS_OUT_OF_GRID    (1u << 0) /* a particle hashed outside the cell grid (reference: UB)   */
+#define SPH_STATUS_SECANT_MAXITER (1u << 1) /* return mapping hit 100 iterations (plasticity.cuh:155)    */
+#define SPH_STATUS_NAN_BLANKED    (1u << 2) /* NaN/Inf rate -> particle blanked (actions_gpu.cu:816)      */
+#define SPH_STATUS_CONTACT_NOSEG  (1u << 3) /* inside tool, no segment found (actions_gpu.cu:188-191)     */
+#define SPH_STATUS_CONTACT_DEEP   (1u << 4) /* blanked for penetration > 2.5e-4 (actions_gpu.cu:479-492)  */
+#define SPH_STATUS_MELT_BLANKED   (1u << 5) /* T > Tmelt -> blanked (actions_gpu.cu:750-753)              */
+#define SPH_STATUS_FRIC_NAN       (1u << 6) /* NaN sliding velocity -> blanked (actions_gpu.cu:375-380)   */
+#define SPH_STATUS_CELL_OVERFLOW  (1u << 7) /* a cell held more particles than the in-cell ranker allows  */
+
+/* ---- precision of the particle path ------------------------------------ */
+enum {
+    SPH_PREC_FP64 = 0,     /* plain FP64 (reference USE_DOUBLE semantics)                         */
+    SPH_PREC_FP32K = 1     /* FP32 neighbour sums with Kahan compensation; FP64 positions, FP64
+                              return-mapping residual and FP64 FEM thermal solve                   */
+};
+
+/* ---- constant collections (constants_structs.h:18-121) ----------------- */
+typedef struct sph_phys_constants {      /* phys_constants, constants_structs.h:18-26 */
+    double E, nu, rho0, K, G, mass, mass_tool;
+} sph_phys_constants;
+
+typedef struct sph_trml_constants {      /* trml_constants, constants_structs.h:30-37 */
+    double cp, tq, k, alpha, T_init, eta;
+} sph_trml_constants;
+
+typedef struct sph_corr_constants {      /* corr_constants, constants_structs.h:41-48 */
+    double wdeltap, stresseps, xspheps, alpha, beta, eta;
+} sph_corr_constants;
+
+typedef struct sph_joco_constants {      /* joco_constants, constants_structs.h:52-66 */
+    double A, B, C, n, m, Tmelt, Tref, eps_dot_ref;
+    double tanh_a, tanh_b, tanh_c, tanh_d;
+} sph_joco_constants;
+
+typedef struct sph_tool_constants {      /* tool_constants, constants_structs.h:80-109 (no *_FRI variants) */
+    double cp, tq, k, eta, rho, T0, h, beta, mu, contact_alpha, slave_mass, hc;
+} sph_tool_constants;
+
+/* Everything the reference installs with actions_setup_* / interactions_setup_*
+ * (actions_gpu.cu:913-954, interactions_gpu.cu:476-507). */
+typedef struct sph_constants {
+    sph_phys_constants phys;
+    sph_corr_constants corr;
+    sph_joco_constants joco;
+    sph_trml_constants trml_wp;        /* workpiece: actions thermals_wp and interactions trml       */
+    sph_trml_constants trml_tool;      /* actions thermals_tool; alpha != 0 enables thermal BCs      */
+    sph_trml_constants trml_tool_sph;  /* interactions trml_tool (SPH tool particles); zero when the
+                                          reference never calls interactions_setup_thermal_constants_tool */
+    sph_tool_constants tool;
+    int32_t plastic;                   /* actions_setup_johnson_cook_constants called (m_plastic)    */
+    int32_t pad0;
+} sph_constants;
+
+/* Locked cell grid: grid_base(num_part, bbmin, bbmax, h) -> set_geometry
+ * (grid.cu:130-149).  The reference uses cell edge == h and a 5x5 stencil
+ * (cell_factor = 1, stencil = 2).  cell_factor = 2, stencil = 1 gives 2h
+ * cells with a 3x3 stencil; results then differ only by summation order. */
+typedef struct sph_grid_params {
+    double bbmin[2];
+    double bbmax[2];
+    double h;
+    int32_t cell_factor;
+    int32_t stencil;
+} sph_grid_params;
+
+/* Derived grid geometry: geom_constants (constants_structs.h:70-76). */
+typedef struct sph_geom_constants {
+    int32_t nx, ny;
+    double bbmin_x, bbmin_y, dx;
+    int32_t num_cell;
+    int32_t stencil;
+} sph_geom_constants;
+
+/* ---- particle SoA (particle_gpu, particle_gpu.h:23-83) ------------------ */
+typedef struct sph_particles {
+    int32_t N;
+    int32_t pad0;
+    double *pos, *vel;                      /* [N][2] */
+    double *h, *rho, *p;                    /* [N]    */
+    double *S, *R;                          /* [N][4] S = (Sxx, Sxy, Syy, Szz), R = (Rxx, Rxy, Ryy, 0) */
+    double *fc, *ft, *n;                    /* [N][2] */
+    double *fixed, *blanked, *tool_particle;/* [N] 0/1 flags stored as double, as the reference */
+    double *eps_pl, *eps_pl_dot, *T;        /* [N]    */
+    double *pos_t, *vel_t;                  /* [N][2] */
+    double *rho_t;                          /* [N]    */
+    double *S_t;                            /* [N][4] */
+    double *T_t;                            /* [N]    */
+    double *S_der, *v_der;                  /* [N][4] */
+    int32_t *idx, *hash, *on_seg;           /* [N]    */
+} sph_particles;
+
+/* ---- FEM tool interface segments (segment_FEM_gpu, segment_FEM_gpu.h:31-56) */
+typedef struct sph_segments {
+    int32_t n;
+    int32_t pad0;
+    double *left, *right, *normal;          /* [n][2] */
+    int32_t *marks;                         /* [n][4] element, colour, node left, node right */
+    double *heat_exchange;                  /* [n][2] (sum T*length, sum length) */
+    double *fric_heat;                      /* [n]    */
+} sph_segments;
+
+/* ---- FEM thermal system of the tool (FEM_thermal_2D_GPU, FEM_thermal_gpu.h:35-93) */
+typedef struct sph_fem {
+    int32_t n_nodes, nnz;
+    double *position;                       /* [n_nodes][2] mesh_GPU_m::position */
+    int32_t *row_ptr;                       /* [n_nodes+1] */
+    int32_t *col_ind;                       /* [nnz] */
+    double *K;                              /* [nnz] m_stiffness_matrix (after Dirichlet) */
+    double *M_inv;                          /* [n_nodes] m_mass_matrix_inverse (lumped) */
+    double *f;                              /* [n_nodes] m_f (after Dirichlet) */
+    double *T;                              /* [n_nodes] m_T */
+    double *k;                              /* [n_nodes] m_k (temperature rate) */
+} sph_fem;
+
+/* Host description of a linear-triangle tool mesh: what mesh_read produces
+ * (mesh_structure_GPU.h:37-78) before colouring and CSR construction. */
+typedef struct sph_tool_mesh {
+    int32_t n_nodes, n_elements;
+    const double *nodes;                    /* [n_nodes][2] (cm) */
+    const int32_t *elements;                /* [n_elements][3] node ids */
+    const int32_t *cutting_flags;           /* [n_elements][3] edge (a,b),(b,c),(c,a) on the contact interface */
+    const int32_t *fixed_flags;             /* [n_elements][3] edge on the fixed-temperature boundary */
+    const double *T_init;                   /* [n_nodes] initial nodal temperature, or NULL for tool.T0 */
+    double tl[2];                           /* tool_FEM ctor top-left point (segment normal reference) */
+} sph_tool_mesh;
+
+/* Rigid tool kinematics kept on the host by tool_FEM (tool_FEM.h:57-77). */
+typedef struct sph_tool_state {
+    double vel[2];
+    double tl_point_ref[2];
+    double br_point[2];
+    double ref_dist;
+    double lowest_point, right_point;
+    int32_t n_segments, n_cut_colors;
+} sph_tool_state;
+
+typedef struct sph_ctx sph_ctx;
+typedef struct sph_tool_host sph_tool_host;
+
+/* ---- host-only tool set-up (no GPU needed) -------------------------------
+ * The set-up that sph_ctx_create performs for a tool mesh, on the host only:
+ * mesh colouring and CSR pattern (mesh_structure_GPU.cu:596-780), interface
+ * segments (tool_FEM::set_up_segments_from_mesh, tool_FEM.cu:771-1039) and
+ * the assembled FEM system (FEM_thermal_gpu.cu:126-332). */
+int sph_tool_build(const sph_tool_mesh *mesh, const sph_tool_constants *tc, sph_tool_host **out);
+int sph_tool_host_info(const sph_tool_host *t, sph_tool_state *state, int32_t *n_nodes, int32_t *nnz,
+                       int32_t *n_colors);
+/* Copies into caller arrays (NULL fields skipped); sizes must match. */
+int sph_tool_host_export(const sph_tool_host *t, sph_segments *seg, sph_fem *fem);
+int sph_tool_host_destroy(sph_tool_host *t);
+
+/* ---- context ------------------------------------------------------------ */
+/* Allocates particle_gpu (particle_gpu.cu:11-104), the Green grid buffers
+ * (grid_gpu_green.cu:224-266), leap_frog snapshots (leap_frog.cu:261-271),
+ * and, with a tool mesh, sets up the interface segments
+ * (tool_FEM::set_up_segments_from_mesh, tool_FEM.cu:771-1039) and assembles
+ * the FEM thermal system (FEM_thermal_gpu.cu:584-603).  `tool` may be NULL
+ * for a tool-less run.  `host` arrays that are NULL start at zero, except
+ * on_seg which starts at 0 like the reference. */
+int sph_ctx_create(const sph_constants *c, const sph_grid_params *g,
+                   const sph_particles *host, const sph_tool_mesh *tool,
+                   double dt, int32_t precision, int32_t device, sph_ctx **out);
+int sph_ctx_destroy(sph_ctx *ctx);
+const char *sph_last_error(const sph_ctx *ctx);
+int sph_abi_version(void);
+
+int sph_set_dt(sph_ctx *ctx, double dt);                         /* global_dt */
+int sph_get_geometry(const sph_ctx *ctx, sph_geom_constants *out);
+int sph_set_constants(sph_ctx *ctx, const sph_constants *c);     /* *_setup_*_constants */
+int sph_sync(sph_ctx *ctx);
+int sph_status(sph_ctx *ctx, uint32_t *status, int32_t clear);
+/* The CUDA stream the context launches on (cudaStream_t as void*). */
+int sph_get_stream(const sph_ctx *ctx, void **stream);
+
+/* ---- particle data in and out ------------------------------------------ */
+int sph_get_particles(sph_ctx *ctx, sph_particles *dev_view);    /* device pointers (post-swap) */
+int sph_upload_particles(sph_ctx *ctx, const sph_particles *host);   /* non-NULL fields only */
+int sph_download_particles(sph_ctx *ctx, sph_particles *host);       /* non-NULL fields only */
+int sph_get_cells(sph_ctx *ctx, int32_t **cell_start, int32_t **cell_end, int32_t *num_cell); /* device */
+int sph_download_cells(sph_ctx *ctx, int32_t *cell_start, int32_t *cell_end);
+
+/* ---- grid (grid.cu, grid_gpu_green.cu) ---------------------------------- */
+int sph_update_geometry(sph_ctx *ctx);   /* grid_base::update_geometry: no-op on a locked grid (grid.cu:88-91) */
+int sph_assign_hashes(sph_ctx *ctx);     /* grid_base::assign_hashes -> compute_hashes (grid.cu:25-42,80-86) */
+int sph_sort(sph_ctx *ctx);              /* grid_gpu_green::sort -> do_sort (grid_gpu_green.cu:185-212)       */
+
+/* ---- leap-frog (leap_frog.cu:25-96) ------------------------------------- */
+int sph_init(sph_ctx *ctx);              /* init: snapshot pos, vel, S, rho, T (leap_frog.cu:25-37) */
+int sph_predict(sph_ctx *ctx);           /* predict with 0.5*dt (leap_frog.cu:45-69)                */
+int sph_correct(sph_ctx *ctx);           /* correct with dt (leap_frog.cu:71-96)                    */
+
+/* ---- per-particle actions (actions_gpu.cu) ------------------------------ */
+int sph_material_eos(sph_ctx *ctx);                    /* material_eos, :838-842 -> :222-232              */
+int sph_corrector_artificial_stress(sph_ctx *ctx);     /* corrector_artificial_stress, :844-848 -> :234-278 */
+int sph_material_stress_rate_jaumann(sph_ctx *ctx);    /* :850-854 -> :280-314                           */
+int sph_contmech_continuity(sph_ctx *ctx);             /* :856-860 -> :626-639                           */
+int sph_contmech_momentum(sph_ctx *ctx);               /* :862-866 -> :641-671                           */
+int sph_contmech_advection(sph_ctx *ctx);              /* :868-872 -> :673-687                           */
+int sph_plasticity_johnson_cook(sph_ctx *ctx);         /* :874-879 -> :689-754, plasticity.cuh:21-162    */
+int sph_perform_boundary_conditions(sph_ctx *ctx);     /* :888-892 -> :765-781                           */
+int sph_perform_boundary_conditions_thermal(sph_ctx *ctx); /* :881-886 -> :756-763                       */
+int sph_debug_invalidate(sph_ctx *ctx);                /* :907-911 -> :787-824                           */
+
+/* ---- neighbour sums (interactions_gpu.cu) ------------------------------- */
+int sph_interactions_monaghan(sph_ctx *ctx);           /* interactions_monaghan, :381-432 -> :143-379    */
+
+/* ---- FEM tool coupling -------------------------------------------------- */
+int sph_material_fric_heat_gen_fem(sph_ctx *ctx);      /* material_fric_heat_gen_FEM_v2, actions_gpu.cu:967-981 -> :345-420 */
+int sph_compute_contact_forces_fem(sph_ctx *ctx);      /* compute_contact_forces_FEM_tool_v3, actions_gpu.cu:983-999 -> :423-617 */
+int sph_segments_update(sph_ctx *ctx, double dt);      /* tool_FEM::segments_update, tool_FEM.cu:1572-1582 -> :119-139 */
+int sph_tool_update_fem(sph_ctx *ctx, double dt);      /* tool_FEM::tool_update_FEM_gpu, tool_FEM.cu:1552-1570 -> :109-117 */
+int sph_fem_reset_server(sph_ctx *ctx);                /* FEM_thermal_2D_GPU::reset_FEM_server, FEM_thermal_gpu.cu:902-921 */
+int sph_fem_apply_robin(sph_ctx *ctx);                 /* tool_FEM::apply_heat_boundary_condition -> apply_robin_bdc, :865-877 -> :342-386 */
+int sph_fem_calculate_temp_rate(sph_ctx *ctx);         /* calculate_temp_rate, :879-889 -> :443-458     */
+int sph_fem_calculate_temp(sph_ctx *ctx, double dt);   /* calculate_temp, :891-900 -> :460-468          */
+int sph_set_tool_velocity(sph_ctx *ctx, double vx, double vy);   /* tool::set_vel */
+int sph_get_tool_state(sph_ctx *ctx, sph_tool_state *out);
+int sph_get_segments(sph_ctx *ctx, sph_segments *dev_view);
+int sph_download_segments(sph_ctx *ctx, sph_segments *host);
+int sph_get_fem(sph_ctx *ctx, sph_fem *dev_view);
+int sph_download_fem(sph_ctx *ctx, sph_fem *host);
+int sph_upload_fem_state(sph_ctx *ctx, const double *T, const double *k); /* nodal T and rate, NULL = keep */
+
+/* ---- whole step ---------------------------------------------------------- */
+/* leap_frog::step(particle_gpu*, grid_base*, tool_FEM*) (leap_frog.cu:162-248),
+ * or the tool-less leap_frog::step(particle_gpu*, grid_base*) (:99-160 without
+ * the SPH-particle tool) when the context has no tool.  Runs fused kernels;
+ * the first call records a CUDA graph that later calls replay. */
+int sph_step(sph_ctx *ctx);
+int sph_run(sph_ctx *ctx, int32_t nsteps);
+/* Same step, issued as the unfused per-stage kernels in reference order. */
+int sph_step_staged(sph_ctx *ctx);
+
+/* ---- measurement hooks (output.cu:41-49 report_force; peak temperature) -- */
+int sph_reduce_force(sph_ctx *ctx, double out[2]);     /* sum over particles of fc + ft */
+int sph_reduce_max_T(sph_ctx *ctx, double *out);       /* max over non-blanked particles of T */
+
+/* ---- per-stage timing ---------------------------------------------------------
+ * Runs `nsteps` fused steps without the CUDA graph, with CUDA events on the
+ * context stream between the stages; stage_ms[k] receives the summed device
+ * time of stage k over the steps: 0 histogram/hash (previous step's tail when
+ * chained), 1 scan+scatter+rank, 2 reorder gather (+predict, EOS, artificial
+ * stress, records), 3 FEM half step, 4 neighbour sums + fused epilogue,
+ * 5 FEM rate/update + tool move, 6 contact/BC/invalidate tail (+ next
+ * histogram).  n_stages receives 7. */
+int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_stages);
+
+/* ---- kernel launch accounting ---------------------------------------------- */
+int sph_launch_count(const sph_ctx *ctx, int64_t *count);   /* kernels launched by this context */
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPHFEM_H */

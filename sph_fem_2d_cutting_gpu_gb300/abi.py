@@ -1,0 +1,241 @@
+"""ctypes mirror of include/sphfem.h and the loader of the CUDA library.
+
+The library is ``sph_fem_2d_cutting_gpu_gb300/lib/libsphfem.so`` built by
+``build.py`` for sm_103a.  There is no fallback: if the library is missing or
+does not load, ``load()`` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "lib" / "libsphfem.so"
+
+SPH_OK, SPH_ERR_INVALID, SPH_ERR_CUDA, SPH_ERR_NO_DEVICE, SPH_ERR_ALLOC, SPH_ERR_STATE = range(6)
+SPH_PREC_FP64, SPH_PREC_FP32K = 0, 1
+
+STATUS_BITS = {
+    "out_of_grid": 1 << 0,
+    "secant_maxiter": 1 << 1,
+    "nan_blanked": 1 << 2,
+    "contact_noseg": 1 << 3,
+    "contact_deep": 1 << 4,
+    "melt_blanked": 1 << 5,
+    "fric_nan": 1 << 6,
+    "cell_overflow": 1 << 7,
+}
+
+D = C.c_double
+I32 = C.c_int32
+PD = C.POINTER(C.c_double)
+PI = C.POINTER(C.c_int32)
+
+
+def _fields(names, t=D):
+    return [(n, t) for n in names]
+
+
+class PhysConstants(C.Structure):
+    _fields_ = _fields(["E", "nu", "rho0", "K", "G", "mass", "mass_tool"])
+
+
+class TrmlConstants(C.Structure):
+    _fields_ = _fields(["cp", "tq", "k", "alpha", "T_init", "eta"])
+
+
+class CorrConstants(C.Structure):
+    _fields_ = _fields(["wdeltap", "stresseps", "xspheps", "alpha", "beta", "eta"])
+
+
+class JocoConstants(C.Structure):
+    _fields_ = _fields(["A", "B", "C", "n", "m", "Tmelt", "Tref", "eps_dot_ref", "tanh_a", "tanh_b", "tanh_c",
+                        "tanh_d"])
+
+
+class ToolConstants(C.Structure):
+    _fields_ = _fields(["cp", "tq", "k", "eta", "rho", "T0", "h", "beta", "mu", "contact_alpha", "slave_mass", "hc"])
+
+
+class Constants(C.Structure):
+    _fields_ = [("phys", PhysConstants), ("corr", CorrConstants), ("joco", JocoConstants),
+                ("trml_wp", TrmlConstants), ("trml_tool", TrmlConstants), ("trml_tool_sph", TrmlConstants),
+                ("tool", ToolConstants), ("plastic", I32), ("pad0", I32)]
+
+
+class GridParams(C.Structure):
+    _fields_ = [("bbmin", D * 2), ("bbmax", D * 2), ("h", D), ("cell_factor", I32), ("stencil", I32)]
+
+
+class GeomConstants(C.Structure):
+    _fields_ = [("nx", I32), ("ny", I32), ("bbmin_x", D), ("bbmin_y", D), ("dx", D), ("num_cell", I32),
+                ("stencil", I32)]
+
+
+# (name, doubles-or-ints per particle, dtype) in sph_particles order
+PARTICLE_FIELDS = [
+    ("pos", 2, np.float64), ("vel", 2, np.float64), ("h", 1, np.float64), ("rho", 1, np.float64),
+    ("p", 1, np.float64), ("S", 4, np.float64), ("R", 4, np.float64), ("fc", 2, np.float64),
+    ("ft", 2, np.float64), ("n", 2, np.float64), ("fixed", 1, np.float64), ("blanked", 1, np.float64),
+    ("tool_particle", 1, np.float64), ("eps_pl", 1, np.float64), ("eps_pl_dot", 1, np.float64),
+    ("T", 1, np.float64), ("pos_t", 2, np.float64), ("vel_t", 2, np.float64), ("rho_t", 1, np.float64),
+    ("S_t", 4, np.float64), ("T_t", 1, np.float64), ("S_der", 4, np.float64), ("v_der", 4, np.float64),
+    ("idx", 1, np.int32), ("hash", 1, np.int32), ("on_seg", 1, np.int32),
+]
+
+
+class Particles(C.Structure):
+    _fields_ = [("N", I32), ("pad0", I32)] + [(n, PI if dt == np.int32 else PD) for n, _, dt in PARTICLE_FIELDS]
+
+
+class Segments(C.Structure):
+    _fields_ = [("n", I32), ("pad0", I32), ("left", PD), ("right", PD), ("normal", PD), ("marks", PI),
+                ("heat_exchange", PD), ("fric_heat", PD)]
+
+
+class Fem(C.Structure):
+    _fields_ = [("n_nodes", I32), ("nnz", I32), ("position", PD), ("row_ptr", PI), ("col_ind", PI), ("K", PD),
+                ("M_inv", PD), ("f", PD), ("T", PD), ("k", PD)]
+
+
+class ToolMesh(C.Structure):
+    _fields_ = [("n_nodes", I32), ("n_elements", I32), ("nodes", PD), ("elements", PI), ("cutting_flags", PI),
+                ("fixed_flags", PI), ("T_init", PD), ("tl", D * 2)]
+
+
+class ToolState(C.Structure):
+    _fields_ = [("vel", D * 2), ("tl_point_ref", D * 2), ("br_point", D * 2), ("ref_dist", D),
+                ("lowest_point", D), ("right_point", D), ("n_segments", I32), ("n_cut_colors", I32)]
+
+
+def ptr(a: np.ndarray | None):
+    """Pointer of a C-contiguous numpy array (or NULL)."""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "array must be C-contiguous"
+    t = PI if a.dtype == np.int32 else PD
+    return a.ctypes.data_as(t)
+
+
+def particles_struct(arrays: dict, N: int) -> Particles:
+    """sph_particles pointing at numpy arrays (missing fields are NULL)."""
+    s = Particles()
+    s.N = N
+    for name, w, dt in PARTICLE_FIELDS:
+        a = arrays.get(name)
+        if a is not None:
+            assert a.dtype == dt and a.size == N * w, f"field {name}: dtype/size mismatch"
+            setattr(s, name, ptr(a))
+    return s
+
+
+def empty_particles(N: int) -> dict:
+    return {name: np.zeros(N * w if w > 1 else N, dtype=dt).reshape((N, w) if w > 1 else (N,))
+            for name, w, dt in PARTICLE_FIELDS}
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load the sm_103a library; raise if it is absent (there is no CPU path)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"CUDA library not built: {LIB_PATH} (run sph_fem_2d_cutting_gpu_gb300.build.build())")
+    lib = C.CDLL(str(LIB_PATH))
+    P = C.c_void_p
+    proto = {
+        "sph_abi_version": ([], C.c_int),
+        "sph_ctx_create": ([C.POINTER(Constants), C.POINTER(GridParams), C.POINTER(Particles), C.POINTER(ToolMesh),
+                            D, I32, I32, C.POINTER(P)], C.c_int),
+        "sph_ctx_destroy": ([P], C.c_int),
+        "sph_last_error": ([P], C.c_char_p),
+        "sph_set_dt": ([P, D], C.c_int),
+        "sph_get_geometry": ([P, C.POINTER(GeomConstants)], C.c_int),
+        "sph_set_constants": ([P, C.POINTER(Constants)], C.c_int),
+        "sph_sync": ([P], C.c_int),
+        "sph_status": ([P, C.POINTER(C.c_uint32), I32], C.c_int),
+        "sph_get_stream": ([P, C.POINTER(P)], C.c_int),
+        "sph_get_particles": ([P, C.POINTER(Particles)], C.c_int),
+        "sph_upload_particles": ([P, C.POINTER(Particles)], C.c_int),
+        "sph_download_particles": ([P, C.POINTER(Particles)], C.c_int),
+        "sph_get_cells": ([P, C.POINTER(PI), C.POINTER(PI), C.POINTER(I32)], C.c_int),
+        "sph_download_cells": ([P, PI, PI], C.c_int),
+        "sph_set_tool_velocity": ([P, D, D], C.c_int),
+        "sph_get_tool_state": ([P, C.POINTER(ToolState)], C.c_int),
+        "sph_get_segments": ([P, C.POINTER(Segments)], C.c_int),
+        "sph_download_segments": ([P, C.POINTER(Segments)], C.c_int),
+        "sph_get_fem": ([P, C.POINTER(Fem)], C.c_int),
+        "sph_download_fem": ([P, C.POINTER(Fem)], C.c_int),
+        "sph_upload_fem_state": ([P, PD, PD], C.c_int),
+        "sph_segments_update": ([P, D], C.c_int),
+        "sph_tool_update_fem": ([P, D], C.c_int),
+        "sph_fem_calculate_temp": ([P, D], C.c_int),
+        "sph_run": ([P, I32], C.c_int),
+        "sph_reduce_force": ([P, PD], C.c_int),
+        "sph_reduce_max_T": ([P, PD], C.c_int),
+        "sph_launch_count": ([P, C.POINTER(C.c_int64)], C.c_int),
+        "sph_profile_steps": ([P, I32, C.POINTER(C.c_float), C.POINTER(I32)], C.c_int),
+        "sph_tool_build":([C.POINTER(ToolMesh), C.POINTER(ToolConstants), C.POINTER(P)], C.c_int),
+        "sph_tool_host_info": ([P, C.POINTER(ToolState), C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)], C.c_int),
+        "sph_tool_host_export": ([P, C.POINTER(Segments), C.POINTER(Fem)], C.c_int),
+        "sph_tool_host_destroy": ([P], C.c_int),
+    }
+    for name in STAGE_FUNCTIONS:
+        proto.setdefault(name, ([P], C.c_int))
+    for name, (args, res) in proto.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = lib
+    return lib
+
+
+def tool_model_host(case) -> dict:
+    """Host-only tool set-up (no GPU): segments, FEM system and tool state, as
+    sph_ctx_create would build them for this case."""
+    lib = load()
+    tool, keep = case.tool_struct()
+    h = C.c_void_p()
+    r = lib.sph_tool_build(C.byref(tool), C.byref(case.constants.tool), C.byref(h))
+    try:
+        if r != SPH_OK:
+            raise RuntimeError(f"sph_tool_build failed ({r})")
+        st = ToolState()
+        nn, nz, ncol = I32(), I32(), I32()
+        lib.sph_tool_host_info(h, C.byref(st), C.byref(nn), C.byref(nz), C.byref(ncol))
+        n = st.n_segments
+        seg = dict(left=np.zeros((n, 2)), right=np.zeros((n, 2)), normal=np.zeros((n, 2)),
+                   marks=np.zeros((n, 4), np.int32), heat_exchange=np.zeros((n, 2)), fric_heat=np.zeros(n))
+        fem = dict(position=np.zeros((nn.value, 2)), row_ptr=np.zeros(nn.value + 1, np.int32),
+                   col_ind=np.zeros(nz.value, np.int32), K=np.zeros(nz.value), M_inv=np.zeros(nn.value),
+                   f=np.zeros(nn.value), T=np.zeros(nn.value), k=np.zeros(nn.value))
+        s = Segments()
+        s.n = n
+        for k, v in seg.items():
+            setattr(s, k, ptr(v))
+        f = Fem()
+        f.n_nodes, f.nnz = nn.value, nz.value
+        for k, v in fem.items():
+            setattr(f, k, ptr(v))
+        if lib.sph_tool_host_export(h, C.byref(s), C.byref(f)) != SPH_OK:
+            raise RuntimeError("sph_tool_host_export failed")
+        return dict(segments=seg, fem=fem, state=st, n_colors=ncol.value, n_cut_colors=st.n_cut_colors)
+    finally:
+        if h.value:
+            lib.sph_tool_host_destroy(h)
+        del keep
+
+
+# Entry points that take only the context (the stage calls of leap_frog::step).
+STAGE_FUNCTIONS = [
+    "sph_update_geometry", "sph_assign_hashes", "sph_sort", "sph_init", "sph_predict", "sph_correct",
+    "sph_material_eos", "sph_corrector_artificial_stress", "sph_material_stress_rate_jaumann",
+    "sph_contmech_continuity", "sph_contmech_momentum", "sph_contmech_advection", "sph_plasticity_johnson_cook",
+    "sph_perform_boundary_conditions", "sph_perform_boundary_conditions_thermal", "sph_debug_invalidate",
+    "sph_interactions_monaghan", "sph_material_fric_heat_gen_fem", "sph_compute_contact_forces_fem",
+    "sph_fem_reset_server", "sph_fem_apply_robin", "sph_fem_calculate_temp_rate", "sph_step", "sph_step_staged",
+]

@@ -1,0 +1,394 @@
+// actions.cu -- per-particle kernels of the step (actions_gpu.cu, leap_frog.cu):
+// the staged form (one launch per reference call, same order and arrays) and
+// the fused contact / boundary-condition / invalidate kernel of the step.
+#include "launch.cuh"
+
+namespace sphfem {
+
+#define PARTICLE_LOOP_HEAD                                \
+    const int i = blockIdx.x * blockDim.x + threadIdx.x; \
+    if (i >= N) return;
+
+// ---- leap_frog.cu:25-37 init --------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_init(int N, SortedFields A, StepScratch W) {
+    PARTICLE_LOOP_HEAD
+    if (A.blanked[i] == 1.) return;
+    W.pos_init[i] = A.pos[i];
+    W.vel_init[i] = A.vel[i];
+    W.S_init[i] = A.S[i];
+    W.rho_init[i] = A.rho[i];
+    W.T_init[i] = A.T[i];
+}
+
+// ---- leap_frog.cu:45-96 predict (fac 0.5) / correct (fac 1) --------------------------------
+__global__ void __launch_bounds__(kBlock) k_predict_correct(int N, SortedFields A, StepScratch W, double fdt) {
+    PARTICLE_LOOP_HEAD
+    if (A.blanked[i] == 1.) return;
+    double2 p0 = W.pos_init[i], pt = A.pos_t[i], v0 = W.vel_init[i], vt = A.vel_t[i];
+    A.pos[i] = make_double2(p0.x + fdt * pt.x, p0.y + fdt * pt.y);
+    A.vel[i] = make_double2(v0.x + fdt * vt.x, v0.y + fdt * vt.y);
+    dbl4 S0 = W.S_init[i], St = A.S_t[i];
+    A.S[i] = mk4(S0.x + fdt * St.x, S0.y + fdt * St.y, S0.z + fdt * St.z, S0.w + fdt * St.w);
+    A.rho[i] = W.rho_init[i] + fdt * A.rho_t[i];
+    A.T[i] = W.T_init[i] + fdt * A.T_t[i];
+}
+
+// ---- actions_gpu.cu:222-232 do_material_eos ------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_eos(int N, KConsts K, SortedFields A, FixedFields F) {
+    PARTICLE_LOOP_HEAD
+    if (A.tool_particle[i] != 0.) return;
+    F.p[i] = eos_one(K, A.rho[i]);
+}
+
+// ---- actions_gpu.cu:234-278 do_corrector_artificial_stress ---------------------------------
+__global__ void __launch_bounds__(kBlock) k_artificial_stress(int N, KConsts K, SortedFields A, FixedFields F) {
+    PARTICLE_LOOP_HEAD
+    if (A.tool_particle[i] != 0.) return;
+    F.R[i] = artificial_stress_one(K, A.rho[i], F.p[i], A.S[i]);
+}
+
+// ---- actions_gpu.cu:280-314 do_material_stress_rate_jaumann --------------------------------
+__global__ void __launch_bounds__(kBlock) k_jaumann(int N, KConsts K, SortedFields A, FixedFields F) {
+    PARTICLE_LOOP_HEAD
+    if (A.tool_particle[i] == 1.) return;
+    A.S_t[i] = jaumann_one(K, F.v_der[i], A.S[i]);
+}
+
+// ---- actions_gpu.cu:626-639 do_contmech_continuity ------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_continuity(int N, SortedFields A, FixedFields F) {
+    PARTICLE_LOOP_HEAD
+    if (A.tool_particle[i] != 0.) return;
+    dbl4 vd = F.v_der[i];
+    A.rho_t[i] = -A.rho[i] * (vd.x + vd.w);
+}
+
+// ---- actions_gpu.cu:641-671 do_contmech_momentum --------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_momentum(int N, KConsts K, SortedFields A, FixedFields F) {
+    PARTICLE_LOOP_HEAD
+    if (A.tool_particle[i] != 0.) return;
+    const double mass = K.c.phys.mass;
+    dbl4 sd = F.S_der[i];
+    double2 fc = A.fc[i], ft = A.ft[i], vt = A.vel_t[i];
+    vt.x += sd.x + sd.y + fc.x / mass + ft.x / mass;
+    vt.y += sd.z + sd.w + fc.y / mass + ft.y / mass;
+    A.vel_t[i] = vt;
+}
+
+// ---- actions_gpu.cu:673-687 do_contmech_advection -------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_advection(int N, SortedFields A) {
+    PARTICLE_LOOP_HEAD
+    if (A.tool_particle[i] != 0.) return;
+    double2 v = A.vel[i], pt = A.pos_t[i];
+    A.pos_t[i] = make_double2(pt.x + v.x, pt.y + v.y);
+}
+
+// ---- actions_gpu.cu:689-754 do_plasticity_johnson_cook ---------------------------------------
+__global__ void __launch_bounds__(kBlock) k_plasticity(int N, KConsts K, SortedFields A, FixedFields F,
+                                                       int32_t *__restrict__ secant_iters, uint32_t *status) {
+    PARTICLE_LOOP_HEAD
+    if (A.tool_particle[i] != 0.) return;
+    if (A.blanked[i] == 1.) return;
+    dbl4 S = A.S[i];
+    double eps_pl = A.eps_pl[i], eps_pl_dot = A.eps_pl_dot[i], T = A.T[i], blanked = 0.;
+    int it = 0;
+    uint32_t st = (K.precision == SPH_PREC_FP32K)
+                      ? plasticity_one<true>(K, S, F.p[i], A.rho[i], eps_pl, eps_pl_dot, T, blanked, &it)
+                      : plasticity_one<false>(K, S, F.p[i], A.rho[i], eps_pl, eps_pl_dot, T, blanked, &it);
+    if (secant_iters) secant_iters[i] = it;
+    A.S[i] = S;
+    A.eps_pl[i] = eps_pl;
+    A.eps_pl_dot[i] = eps_pl_dot;
+    A.T[i] = T;
+    if (blanked == 1.) A.blanked[i] = 1.;
+    if (st) set_status(status, st);
+}
+
+// ---- actions_gpu.cu:345-420 do_material_fric_heat_gen_FEM_v21 --------------------------------
+__global__ void __launch_bounds__(kBlock) k_fric_heat(int N, KConsts K, SortedFields A, SegDev seg,
+                                                      const ToolDev *__restrict__ tool, uint32_t *status) {
+    PARTICLE_LOOP_HEAD
+    double T = A.T[i], blanked = A.blanked[i];
+    uint32_t st = fric_heat_one(K, tool->vel, A.vel[i], A.ft[i], A.n[i], A.fc[i], A.rho[i], A.eps_pl[i], A.on_seg[i],
+                                seg.n, T, blanked, seg.fric_heat);
+    if (T != A.T[i]) A.T[i] = T;
+    if (blanked != A.blanked[i]) A.blanked[i] = blanked;
+    if (st) set_status(status, st);
+}
+
+// ---- contact, one particle: actions_gpu.cu:423-583 (s1) ------------------------------------------
+__device__ __forceinline__ uint32_t contact_s1_one(const KConsts &K, const SegDev &seg, const ToolDev &tool,
+                                                   double2 pos, double2 vel, double2 &fc, double2 &ft, double2 &nrm,
+                                                   int &on_seg, double &blanked) {
+    int inside = 0;
+    double ddx = pos.x - tool.tl_point_ref[0], ddy = pos.y - tool.tl_point_ref[1];
+    if (sqrt(ddx * ddx + ddy * ddy) < 1.05 * tool.ref_dist) inside = inside_judgement(pos, seg.left, seg.right, seg.n);
+    if (inside == 0) {
+        fc = make_double2(0., 0.); ft = make_double2(0., 0.); nrm = make_double2(0., 0.);
+        on_seg = -1;
+        return 0u;
+    }
+    double gN = 0.;
+    double2 n_ = make_double2(0., 0.);
+    int seg_no = find_shortest_distance_v1(pos, gN, n_, seg.left, seg.right, seg.normal, seg.n);
+    on_seg = seg_no;
+    if (seg_no == -1) {
+        fc = make_double2(0., 0.); ft = make_double2(0., 0.); nrm = make_double2(0., 0.);
+        on_seg = -1;
+        return SPH_STATUS_CONTACT_NOSEG;
+    }
+    if (gN < -0.00025) {
+        blanked = 1.;
+        fc = make_double2(0., 0.); ft = make_double2(0., 0.); nrm = make_double2(0., 0.);
+        on_seg = -1;
+        return SPH_STATUS_CONTACT_DEEP;
+    }
+    const double dt = K.dt;
+    double dt2 = dt * dt;
+    double s1 = -K.c.tool.slave_mass * gN;
+    double2 fN = make_double2(s1 * n_.x / dt2 * K.c.tool.contact_alpha, s1 * n_.y / dt2 * K.c.tool.contact_alpha);
+    double vx = vel.x - tool.vel[0], vy = vel.y - tool.vel[1];
+    double vdn = vx * n_.x + vy * n_.y;
+    double vrx = vx - n_.x * vdn, vry = vy - n_.y * vdn;
+    double am = K.c.tool.contact_alpha * K.c.tool.slave_mass;
+    double kx = am * vrx / dt, ky = am * vry / dt;
+    double fy = K.c.tool.mu * sqrt(fN.x * fN.x + fN.y * fN.y);
+    double fsx = ft.x - kx, fsy = ft.y - ky;
+    double lfs = sqrt(fsx * fsx + fsy * fsy);
+    if (lfs > fy) ft = make_double2(fy * fsx / lfs, fy * fsy / lfs);
+    else ft = make_double2(fsx, fsy);
+    fc = fN;
+    nrm = n_;
+    return 0u;
+}
+
+// ---- contact, one particle: actions_gpu.cu:585-617 (s2) ------------------------------------------
+__device__ __forceinline__ void contact_s2_one(const KConsts &K, const SegDev &seg, const double *__restrict__ T_nodes,
+                                               int seg_no, double rho, double &T) {
+    int4 mk = seg.marks[seg_no];
+    double T_ = T;
+    double T_seg = 0.5 * (T_nodes[mk.z] + T_nodes[mk.w]);
+    double delta_T = T_seg - T_;
+    double length = sqrtf_d(K.c.tool.slave_mass / rho);
+    atomicAdd(&seg.heat_exchange[seg_no].x, T_ * length);
+    atomicAdd(&seg.heat_exchange[seg_no].y, length);
+    double delta_T_part = delta_T * K.c.tool.h * length / K.c.trml_wp.cp / K.c.tool.slave_mass * K.dt;
+    if (delta_T_part < 0) T += fmax(delta_T_part, delta_T);
+    else T += fmin(delta_T_part, delta_T);
+}
+
+__global__ void __launch_bounds__(kBlock) k_contact_s1(int N, KConsts K, SortedFields A, SegDev seg,
+                                                       const ToolDev *__restrict__ tool, uint32_t *status) {
+    PARTICLE_LOOP_HEAD
+    if (A.blanked[i] == 1.) return;
+    double2 fc = A.fc[i], ft = A.ft[i], nrm = A.n[i];
+    int on = A.on_seg[i];
+    double blanked = 0.;
+    uint32_t st = contact_s1_one(K, seg, *tool, A.pos[i], A.vel[i], fc, ft, nrm, on, blanked);
+    A.fc[i] = fc; A.ft[i] = ft; A.n[i] = nrm; A.on_seg[i] = on;
+    if (blanked == 1.) A.blanked[i] = 1.;
+    if (st) set_status(status, st);
+}
+
+__global__ void __launch_bounds__(kBlock) k_contact_s2(int N, KConsts K, SortedFields A, SegDev seg,
+                                                       const double *__restrict__ T_nodes) {
+    PARTICLE_LOOP_HEAD
+    if (A.blanked[i] == 1.) return;
+    int on = A.on_seg[i];
+    if (on < 0 || on >= seg.n) return;
+    double T = A.T[i];
+    contact_s2_one(K, seg, T_nodes, on, A.rho[i], T);
+    A.T[i] = T;
+}
+
+// ---- actions_gpu.cu:765-781 do_boundary_conditions ------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_bc(int N, SortedFields A) {
+    PARTICLE_LOOP_HEAD
+    if (A.tool_particle[i] != 0.) return;
+    if (A.fixed[i] != 0.) {
+        A.vel[i] = make_double2(0., 0.);
+        A.fc[i] = make_double2(0., 0.);
+        A.pos_t[i] = make_double2(0., 0.);
+        A.vel_t[i] = make_double2(0., 0.);
+    }
+}
+
+// ---- actions_gpu.cu:756-763 do_boundary_conditions_thermal ------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_bc_thermal(int N, KConsts K, SortedFields A) {
+    PARTICLE_LOOP_HEAD
+    if (A.fixed[i] == 1.) A.T[i] = K.c.trml_wp.T_init;
+}
+
+// ---- actions_gpu.cu:787-824 do_invalidate ----------------------------------------------------------
+__device__ __forceinline__ bool isnaninf(double v) { return isnan(v) || isinf(v); }
+
+__device__ __forceinline__ bool invalid_rates(double2 pt, double2 vt, dbl4 St, double rho_t, double T_t) {
+    return isnaninf(pt.x) || isnaninf(pt.y) || isnaninf(vt.x) || isnaninf(vt.y) || isnaninf(St.x) ||
+           isnaninf(St.y) || isnaninf(St.z) || isnaninf(St.w) || isnaninf(rho_t) || isnaninf(T_t);
+}
+
+__global__ void __launch_bounds__(kBlock) k_invalidate(int N, SortedFields A, uint32_t *status) {
+    PARTICLE_LOOP_HEAD
+    if (A.blanked[i] == 1.) return;
+    if (invalid_rates(A.pos_t[i], A.vel_t[i], A.S_t[i], A.rho_t[i], A.T_t[i])) {
+        A.blanked[i] = 1.;
+        set_status(status, SPH_STATUS_NAN_BLANKED);
+    }
+}
+
+// ---- fused tail of the step ----------------------------------------------------------------------
+// contact s1 + s2 (actions_gpu.cu:423-617), do_boundary_conditions,
+// do_boundary_conditions_thermal, do_invalidate (actions_gpu.cu:756-824) for
+// one particle, then (kNextHash) the next step's compute_hashes and the
+// counting-sort histogram (grid.cu:25-42) on the final state.
+template <bool kTool, bool kNextHash>
+__global__ void __launch_bounds__(kBlock) k_step_tail(int N, KConsts K, SortedFields A, SegDev seg,
+                                                      const ToolDev *__restrict__ tool,
+                                                      const double *__restrict__ T_nodes, SortScratch X,
+                                                      uint32_t *status) {
+    PARTICLE_LOOP_HEAD
+    double blanked = A.blanked[i];
+    const double tool_p = A.tool_particle[i];
+    const double fixed = A.fixed[i];
+    uint32_t st = 0;
+    double2 pos = A.pos[i];
+    if (kTool && blanked != 1.) {
+        double2 fc = A.fc[i], ft = A.ft[i], nrm = A.n[i];
+        int on = A.on_seg[i];
+        double bl = 0.;
+        st |= contact_s1_one(K, seg, *tool, pos, A.vel[i], fc, ft, nrm, on, bl);
+        if (bl == 1.) { blanked = 1.; A.blanked[i] = 1.; }
+        A.ft[i] = ft;
+        A.n[i] = nrm;
+        A.on_seg[i] = on;
+        if (tool_p == 0. && fixed != 0.) fc = make_double2(0., 0.);
+        A.fc[i] = fc;
+        if (blanked != 1. && on >= 0 && on < seg.n) {
+            double T = A.T[i];
+            contact_s2_one(K, seg, T_nodes, on, A.rho[i], T);
+            A.T[i] = T;
+        }
+    } else if (tool_p == 0. && fixed != 0.) {
+        A.fc[i] = make_double2(0., 0.);
+    }
+    if (tool_p == 0. && fixed != 0.) {
+        A.vel[i] = make_double2(0., 0.);
+        A.pos_t[i] = make_double2(0., 0.);
+        A.vel_t[i] = make_double2(0., 0.);
+    }
+    if (K.c.trml_tool.alpha != 0. && fixed == 1.) A.T[i] = K.c.trml_wp.T_init;
+    if (blanked != 1.) {
+        if (invalid_rates(A.pos_t[i], A.vel_t[i], A.S_t[i], A.rho_t[i], A.T_t[i])) {
+            blanked = 1.;
+            A.blanked[i] = 1.;
+            st |= SPH_STATUS_NAN_BLANKED;
+        }
+    }
+    if (kNextHash) {
+        int h;
+        if (blanked != 1.) {
+            const sph_geom_constants &g = K.g;
+            int ix = __double2int_rz((pos.x - g.bbmin_x) / g.dx);
+            int iy = __double2int_rz((pos.y - g.bbmin_y) / g.dx);
+            h = ix * g.ny + iy;
+            A.hash[i] = h;
+        } else {
+            h = A.hash[i];
+        }
+        int key = h;
+        if (h < 0 || h >= K.g.num_cell) {
+            key = K.g.num_cell;
+            st |= SPH_STATUS_OUT_OF_GRID;
+        }
+        X.key[i] = key;
+        X.arrival[i] = atomicAdd(X.counts + key, 1);
+    }
+    if (st) set_status(status, st);
+}
+
+// ---- measurement hooks: output.cu:41-49 report_force (sum of fc + ft); peak T ----------------------
+__global__ void __launch_bounds__(kBlock) k_reduce_force_T(int N, SortedFields A, double *__restrict__ out) {
+    __shared__ double sx[kBlock], sy[kBlock], sm[kBlock];
+    double fx = 0., fy = 0., tm = -1e300;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        double2 fc = A.fc[i], ft = A.ft[i];
+        fx += fc.x + ft.x;
+        fy += fc.y + ft.y;
+        if (A.blanked[i] != 1.) tm = fmax(tm, A.T[i]);
+    }
+    sx[threadIdx.x] = fx; sy[threadIdx.x] = fy; sm[threadIdx.x] = tm;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            sx[threadIdx.x] += sx[threadIdx.x + o];
+            sy[threadIdx.x] += sy[threadIdx.x + o];
+            sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[3 * blockIdx.x + 0] = sx[0];
+        out[3 * blockIdx.x + 1] = sy[0];
+        out[3 * blockIdx.x + 2] = sm[0];
+    }
+}
+
+// ---- host launchers --------------------------------------------------------------------------------
+#define GRID div_up(N, kBlock), kBlock, 0, s
+
+void launch_init(cudaStream_t s, int N, const SortedFields &A, const StepScratch &W) { k_init<<<GRID>>>(N, A, W); }
+void launch_predict_correct(cudaStream_t s, int N, const SortedFields &A, const StepScratch &W, double fdt) {
+    k_predict_correct<<<GRID>>>(N, A, W, fdt);
+}
+void launch_eos(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F) {
+    k_eos<<<GRID>>>(N, K, A, F);
+}
+void launch_artificial_stress(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F) {
+    k_artificial_stress<<<GRID>>>(N, K, A, F);
+}
+void launch_jaumann(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F) {
+    k_jaumann<<<GRID>>>(N, K, A, F);
+}
+void launch_continuity(cudaStream_t s, int N, const SortedFields &A, const FixedFields &F) {
+    k_continuity<<<GRID>>>(N, A, F);
+}
+void launch_momentum(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F) {
+    k_momentum<<<GRID>>>(N, K, A, F);
+}
+void launch_advection(cudaStream_t s, int N, const SortedFields &A) { k_advection<<<GRID>>>(N, A); }
+void launch_plasticity(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F,
+                       const StepScratch &W) {
+    k_plasticity<<<GRID>>>(N, K, A, F, W.secant_iters, W.status);
+}
+void launch_fric_heat(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
+                      const ToolDev *tool, uint32_t *status) {
+    k_fric_heat<<<GRID>>>(N, K, A, seg, tool, status);
+}
+void launch_contact(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
+                    const ToolDev *tool, const double *T_nodes, uint32_t *status) {
+    k_contact_s1<<<GRID>>>(N, K, A, seg, tool, status);
+    k_contact_s2<<<GRID>>>(N, K, A, seg, T_nodes);
+}
+void launch_bc(cudaStream_t s, int N, const SortedFields &A) { k_bc<<<GRID>>>(N, A); }
+void launch_bc_thermal(cudaStream_t s, int N, const KConsts &K, const SortedFields &A) {
+    k_bc_thermal<<<GRID>>>(N, K, A);
+}
+void launch_invalidate(cudaStream_t s, int N, const SortedFields &A, uint32_t *status) {
+    k_invalidate<<<GRID>>>(N, A, status);
+}
+void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
+                      const ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
+                      bool next_hash) {
+    if (K.has_tool) {
+        if (next_hash) k_step_tail<true, true><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
+        else k_step_tail<true, false><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
+    } else {
+        if (next_hash) k_step_tail<false, true><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
+        else k_step_tail<false, false><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
+    }
+}
+int reduce_blocks() { return 304; }
+void launch_reduce_force_T(cudaStream_t s, int N, const SortedFields &A, double *out) {
+    k_reduce_force_T<<<reduce_blocks(), kBlock, 0, s>>>(N, A, out);
+}
+
+}  // namespace sphfem

@@ -1,0 +1,384 @@
+// cells.cu -- cell-list build on sm_103a: hashing (grid.cu:25-42), the stable
+// key sort of grid_gpu_green (grid_gpu_green.cu:185-209) and the cell tables
+// plus reorder gather (grid_gpu_green.cu:13-115).
+//
+// The sort is a counting sort over cells rather than a radix sort: keys are
+// cell ids of a locked grid, so one histogram, one scan and one scatter give
+// every particle its cell's slot range.  The order inside a cell is then made
+// identical to thrust::sort_by_key's stable order by ranking each particle
+// among its cell-mates by original index.  The scan also yields cell_start /
+// cell_end directly.
+#include "launch.cuh"
+
+namespace sphfem {
+
+// ---- hashing: grid.cu:25-42 compute_hashes --------------------------------------
+// kHash: write hash for non-blanked particles (blanked keep their stale hash).
+// kCount: derive the sort key and take an arrival slot in the key's bucket.
+template <bool kHash, bool kCount>
+__global__ void __launch_bounds__(kBlock) k_hash_count(int N, const double2 *__restrict__ pos,
+                                                       const double *__restrict__ blanked, int32_t *__restrict__ hash,
+                                                       int32_t *__restrict__ key, int32_t *__restrict__ arrival,
+                                                       int32_t *__restrict__ counts, sph_geom_constants g,
+                                                       uint32_t *status) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    int h;
+    if (kHash && blanked[i] != 1.) {
+        double2 p = pos[i];
+        int ix = __double2int_rz((p.x - g.bbmin_x) / g.dx);
+        int iy = __double2int_rz((p.y - g.bbmin_y) / g.dx);
+        h = ix * g.ny + iy;
+        hash[i] = h;
+    } else {
+        h = hash[i];
+    }
+    if (kCount) {
+        int k = h;
+        if (h < 0 || h >= g.num_cell) {
+            k = g.num_cell;
+            set_status(status, SPH_STATUS_OUT_OF_GRID);
+        }
+        key[i] = k;
+        arrival[i] = atomicAdd(counts + k, 1);
+    }
+}
+
+// ---- exclusive scan of the per-cell counts -----------------------------------------
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int *smem_warp, int &total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) smem_warp[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int nw = blockDim.x >> 5;
+        int s = (lane < nw) ? smem_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < nw) smem_warp[lane] = s;
+    }
+    __syncthreads();
+    int warp_prefix = (wid > 0) ? smem_warp[wid - 1] : 0;
+    total = smem_warp[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return warp_prefix + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const int32_t *__restrict__ in, int n,
+                                                              int32_t *__restrict__ block_sums) {
+    __shared__ int sw[32];
+    int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++)
+        if (base + k < n) s += in[base + k];
+    int total;
+    block_exclusive_scan(s, sw, total);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(int32_t *__restrict__ block_sums, int nb) {
+    __shared__ int sw[32];
+    int carry = 0;
+    for (int base = 0; base < nb; base += blockDim.x) {
+        int i = base + threadIdx.x;
+        int v = (i < nb) ? block_sums[i] : 0;
+        int total;
+        int ex = block_exclusive_scan(v, sw, total);
+        if (i < nb) block_sums[i] = carry + ex;
+        carry += total;
+    }
+}
+
+// Writes offsets[0..n] (n = num_cell + 1 buckets, offsets[n] = N) and the
+// reference's cell tables: cell_start = first slot or -1 when empty; cell_end
+// = one past the last slot, left untouched for empty cells (stale, as the
+// reference leaves it).
+__global__ void __launch_bounds__(kScanThreads) k_scan_down(const int32_t *__restrict__ counts, int n,
+                                                            const int32_t *__restrict__ block_sums,
+                                                            int32_t *__restrict__ offsets,
+                                                            int32_t *__restrict__ cell_start,
+                                                            int32_t *__restrict__ cell_end, int num_cell) {
+    __shared__ int sw[32];
+    int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        v[k] = (base + k < n) ? counts[base + k] : 0;
+        s += v[k];
+    }
+    int total;
+    int ex = block_exclusive_scan(s, sw, total) + block_sums[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        int c = base + k;
+        if (c < n) {
+            offsets[c] = ex;
+            if (c < num_cell) {
+                if (v[k] > 0) {
+                    cell_start[c] = ex;
+                    cell_end[c] = ex + v[k];
+                } else {
+                    cell_start[c] = -1;
+                }
+            }
+            if (c == n - 1) offsets[n] = ex + v[k];
+        }
+        ex += v[k];
+    }
+}
+
+// ---- scatter into the cell's slot range (arbitrary order inside the cell) -------------
+__global__ void __launch_bounds__(kBlock) k_scatter(int N, const int32_t *__restrict__ key,
+                                                    const int32_t *__restrict__ arrival,
+                                                    const int32_t *__restrict__ offsets, int32_t *__restrict__ slots) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    slots[offsets[key[i]] + arrival[i]] = i;
+}
+
+// ---- stable order inside each cell: rank by original index -------------------------------
+// perm[k] = original index of the particle that lands at sorted position k
+// (the reference's particles->idx after sort_by_key).
+__global__ void __launch_bounds__(kBlock) k_rank(int N, const int32_t *__restrict__ key,
+                                                 const int32_t *__restrict__ offsets,
+                                                 const int32_t *__restrict__ slots, int32_t *__restrict__ perm,
+                                                 uint32_t *status) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    int i = slots[s];
+    int c = key[i];
+    int cs = offsets[c], ce = offsets[c + 1];
+    if (ce - cs > kCellRankCap && s == cs) set_status(status, SPH_STATUS_CELL_OVERFLOW);
+    int rank = 0;
+    for (int t = cs; t < ce; t++) rank += (__ldg(slots + t) < i) ? 1 : 0;
+    perm[cs + rank] = i;
+}
+
+// ---- reorder gather (grid_gpu_green.cu:55-113) ----------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_gather_plain(int N, const int32_t *__restrict__ perm, SortedFields A,
+                                                         SortedFields B) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    int i = perm[k];
+    B.pos[k] = A.pos[i];
+    B.vel[k] = A.vel[i];
+    B.fc[k] = A.fc[i];
+    B.ft[k] = A.ft[i];
+    B.h[k] = A.h[i];
+    B.n[k] = A.n[i];
+    B.rho[k] = A.rho[i];
+    B.S[k] = A.S[i];
+    B.eps_pl[k] = A.eps_pl[i];
+    B.eps_pl_dot[k] = A.eps_pl_dot[i];
+    B.T[k] = A.T[i];
+    B.fixed[k] = A.fixed[i];
+    B.blanked[k] = A.blanked[i];
+    B.tool_particle[k] = A.tool_particle[i];
+    B.pos_t[k] = A.pos_t[i];
+    B.vel_t[k] = A.vel_t[i];
+    B.rho_t[k] = A.rho_t[i];
+    B.S_t[k] = A.S_t[i];
+    B.T_t[k] = A.T_t[i];
+    B.on_seg[k] = A.on_seg[i];
+    B.hash[k] = A.hash[i];
+}
+
+// ---- neighbour records ----------------------------------------------------------------
+// FP64 record: (x, y, vx, vy) (sA, sB, sC, Rxx) (Rxy, Ryy, h, rho) (c, vol, T, flags)
+// with sA = (Sxx-p)/rho^2, sB = Sxy/rho^2, sC = (Syy-p)/rho^2 (interactions_gpu.cu:278-281),
+// c = sqrtf(K/rho) (:294-295), vol = mass/rho (:250).
+__device__ __forceinline__ void write_record64(dbl4 *__restrict__ rec, int k, const KConsts &K, double2 pos,
+                                               double2 vel, dbl4 S, dbl4 R, double p, double h, double rho,
+                                               double T, double blanked, double tool, int row) {
+    double rho21 = 1. / (rho * rho);
+    dbl4 r0 = mk4(pos.x, pos.y, vel.x, vel.y);
+    dbl4 r1 = mk4((S.x - p) * rho21, S.y * rho21, (S.z - p) * rho21, R.x);
+    dbl4 r2 = mk4(R.y, R.z, h, rho);
+    int flags = (row & kRowMask) | (blanked == 1. ? kFlagBlanked : 0) | (tool == 1. ? kFlagTool : 0);
+    dbl4 r3 = mk4(sqrtf_d(K.c.phys.K / rho), K.c.phys.mass / rho, T, __longlong_as_double((long long)flags));
+    rec[4 * k + 0] = r0;
+    rec[4 * k + 1] = r1;
+    rec[4 * k + 2] = r2;
+    rec[4 * k + 3] = r3;
+}
+
+// FP32 record: (xr, yr, flags|row, h) (vx, vy, rho, c) (sA, sB, sC, vol) (Rxx, Rxy, Ryy, T)
+// xr, yr = offset of the particle from its cell's lower-left corner; the first
+// 16 bytes are all the candidate test needs.
+__device__ __forceinline__ void write_record32(float4 *__restrict__ rec, int k, const KConsts &K, double2 pos,
+                                               double2 vel, dbl4 S, dbl4 R, double p, double h, double rho,
+                                               double T, double blanked, double tool, int hash) {
+    const sph_geom_constants &g = K.g;
+    int ci = 0, cj = 0;
+    if (hash >= 0 && hash < g.num_cell) { ci = hash / g.ny; cj = hash - ci * g.ny; }
+    double xr = pos.x - (g.bbmin_x + (double)ci * g.dx);
+    double yr = pos.y - (g.bbmin_y + (double)cj * g.dx);
+    double rho21 = 1. / (rho * rho);
+    int flags = (cj & kRowMask) | (blanked == 1. ? kFlagBlanked : 0) | (tool == 1. ? kFlagTool : 0);
+    rec[4 * k + 0] = make_float4((float)xr, (float)yr, __int_as_float(flags), (float)h);
+    rec[4 * k + 1] = make_float4((float)vel.x, (float)vel.y, (float)rho, sqrtf((float)(K.c.phys.K / rho)));
+    rec[4 * k + 2] = make_float4((float)((S.x - p) * rho21), (float)(S.y * rho21), (float)((S.z - p) * rho21),
+                                 (float)(K.c.phys.mass / rho));
+    rec[4 * k + 3] = make_float4((float)R.x, (float)R.y, (float)R.z, (float)T);
+}
+
+// Staged path helper: records from the particle arrays as they are now
+// (interactions_monaghan reads pos, vel, S, R, h, rho, p, T, tool, blanked).
+__global__ void __launch_bounds__(kBlock) k_build_records(int N, KConsts K, SortedFields A, FixedFields F,
+                                                          dbl4 *__restrict__ rec64, float4 *__restrict__ rec32) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    double tool = A.tool_particle[k];
+    double thermal_alpha = (tool == 0.) ? K.c.trml_wp.alpha : K.c.trml_tool_sph.alpha;
+    double T = (thermal_alpha != 0.) ? A.T[k] : 0.;
+    int hash = A.hash[k];
+    if (rec64) {
+        int row = 0;
+        if (hash >= 0 && hash < K.g.num_cell) row = hash - (hash / K.g.ny) * K.g.ny;
+        write_record64(rec64, k, K, A.pos[k], A.vel[k], A.S[k], F.R[k], F.p[k], A.h[k], A.rho[k], T, A.blanked[k],
+                       tool, row);
+    } else {
+        write_record32(rec32, k, K, A.pos[k], A.vel[k], A.S[k], F.R[k], F.p[k], A.h[k], A.rho[k], T, A.blanked[k],
+                       tool, hash);
+    }
+}
+
+// Fused reorder: gather (grid_gpu_green.cu:55-113) + init snapshot (the sorted
+// state itself, leap_frog.cu:25-37) + predict (leap_frog.cu:45-69) +
+// do_material_eos (actions_gpu.cu:222-232) + do_corrector_artificial_stress
+// (actions_gpu.cu:234-278) + the neighbour record of the predicted state.
+// The sorted arrays B keep the start-of-step state (the reference's *_init
+// snapshots); the predicted values live only in the records and in p / R.
+template <bool kF32>
+__global__ void __launch_bounds__(kBlock) k_gather_fused(int N, const int32_t *__restrict__ perm, KConsts K,
+                                                         SortedFields A, SortedFields B, FixedFields F,
+                                                         dbl4 *__restrict__ rec64, float4 *__restrict__ rec32) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    int i = perm[k];
+    F.idx[k] = i;
+    double2 pos = A.pos[i], vel = A.vel[i];
+    dbl4 S = A.S[i];
+    double rho = A.rho[i], T = A.T[i], h = A.h[i];
+    double blanked = A.blanked[i], tool = A.tool_particle[i];
+    double2 pos_t = A.pos_t[i], vel_t = A.vel_t[i];
+    double rho_t = A.rho_t[i], T_t = A.T_t[i];
+    dbl4 S_t = A.S_t[i];
+    int hash = A.hash[i];
+    B.pos[k] = pos;
+    B.vel[k] = vel;
+    B.fc[k] = A.fc[i];
+    B.ft[k] = A.ft[i];
+    B.h[k] = h;
+    B.n[k] = A.n[i];
+    B.rho[k] = rho;
+    B.S[k] = S;
+    B.eps_pl[k] = A.eps_pl[i];
+    B.eps_pl_dot[k] = A.eps_pl_dot[i];
+    B.T[k] = T;
+    B.fixed[k] = A.fixed[i];
+    B.blanked[k] = blanked;
+    B.tool_particle[k] = tool;
+    B.pos_t[k] = pos_t;
+    B.vel_t[k] = vel_t;
+    B.rho_t[k] = rho_t;
+    B.S_t[k] = S_t;
+    B.T_t[k] = T_t;
+    B.on_seg[k] = A.on_seg[i];
+    B.hash[k] = hash;
+    // predict (half step) for active particles
+    if (blanked != 1.) {
+        const double hdt = 0.5 * K.dt;
+        pos.x = pos.x + hdt * pos_t.x;
+        pos.y = pos.y + hdt * pos_t.y;
+        vel.x = vel.x + hdt * vel_t.x;
+        vel.y = vel.y + hdt * vel_t.y;
+        S.x = S.x + hdt * S_t.x;
+        S.y = S.y + hdt * S_t.y;
+        S.z = S.z + hdt * S_t.z;
+        S.w = S.w + hdt * S_t.w;
+        rho = rho + hdt * rho_t;
+        T = T + hdt * T_t;
+    }
+    double p = F.p[k];
+    dbl4 R = F.R[k];
+    if (tool == 0.) {
+        p = eos_one(K, rho);
+        R = artificial_stress_one(K, rho, p, S);
+        F.p[k] = p;
+        F.R[k] = R;
+    }
+    double thermal_alpha = (tool == 0.) ? K.c.trml_wp.alpha : K.c.trml_tool_sph.alpha;
+    double Tn = (thermal_alpha != 0.) ? T : 0.;
+    if (!kF32) {
+        int row = 0;
+        if (hash >= 0 && hash < K.g.num_cell) row = hash - (hash / K.g.ny) * K.g.ny;
+        write_record64(rec64, k, K, pos, vel, S, R, p, h, rho, Tn, blanked, tool, row);
+    } else {
+        write_record32(rec32, k, K, pos, vel, S, R, p, h, rho, Tn, blanked, tool, hash);
+    }
+}
+
+// ---- host launchers ---------------------------------------------------------------------
+void launch_hash(cudaStream_t s, int N, const SortedFields &A, sph_geom_constants g) {
+    k_hash_count<true, false><<<div_up(N, kBlock), kBlock, 0, s>>>(N, A.pos, A.blanked, A.hash, nullptr, nullptr,
+                                                                     nullptr, g, nullptr);
+}
+
+void launch_count(cudaStream_t s, int N, const SortedFields &A, const SortScratch &X, sph_geom_constants g,
+                  uint32_t *status, bool with_hash) {
+    cudaMemsetAsync(X.counts, 0, sizeof(int32_t) * (size_t)(g.num_cell + 1), s);
+    if (with_hash)
+        k_hash_count<true, true><<<div_up(N, kBlock), kBlock, 0, s>>>(N, A.pos, A.blanked, A.hash, X.key, X.arrival,
+                                                                       X.counts, g, status);
+    else
+        k_hash_count<false, true><<<div_up(N, kBlock), kBlock, 0, s>>>(N, A.pos, A.blanked, A.hash, X.key, X.arrival,
+                                                                        X.counts, g, status);
+}
+
+int scan_blocks(int num_cell) { return div_up(num_cell + 1, kScanTile); }
+
+void launch_sort_rest(cudaStream_t s, int N, const SortScratch &X, sph_geom_constants g, int32_t *perm,
+                      uint32_t *status) {
+    const int n = g.num_cell + 1;
+    const int nb = scan_blocks(g.num_cell);
+    k_scan_reduce<<<nb, kScanThreads, 0, s>>>(X.counts, n, X.block_sums);
+    k_scan_top<<<1, 1024, 0, s>>>(X.block_sums, nb);
+    k_scan_down<<<nb, kScanThreads, 0, s>>>(X.counts, n, X.block_sums, X.offsets, X.cell_start, X.cell_end, g.num_cell);
+    k_scatter<<<div_up(N, kBlock), kBlock, 0, s>>>(N, X.key, X.arrival, X.offsets, X.slots);
+    k_rank<<<div_up(N, kBlock), kBlock, 0, s>>>(N, X.key, X.offsets, X.slots, perm, status);
+}
+
+void launch_gather_plain(cudaStream_t s, int N, const int32_t *perm, const SortedFields &A, const SortedFields &B) {
+    k_gather_plain<<<div_up(N, kBlock), kBlock, 0, s>>>(N, perm, A, B);
+}
+
+void launch_gather_fused(cudaStream_t s, int N, const int32_t *perm, const KConsts &K, const SortedFields &A,
+                         const SortedFields &B, const FixedFields &F, const StepScratch &W) {
+    if (K.precision == SPH_PREC_FP32K)
+        k_gather_fused<true><<<div_up(N, kBlock), kBlock, 0, s>>>(N, perm, K, A, B, F, W.rec64, W.rec32);
+    else
+        k_gather_fused<false><<<div_up(N, kBlock), kBlock, 0, s>>>(N, perm, K, A, B, F, W.rec64, W.rec32);
+}
+
+void launch_build_records(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F,
+                          const StepScratch &W) {
+    k_build_records<<<div_up(N, kBlock), kBlock, 0, s>>>(N, K, A, F, K.precision == SPH_PREC_FP32K ? nullptr : W.rec64,
+                                                         W.rec32);
+}
+
+}  // namespace sphfem

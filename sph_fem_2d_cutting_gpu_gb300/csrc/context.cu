@@ -1,0 +1,1005 @@
+// context.cu -- the C ABI (include/sphfem.h): context, data movement, the
+// stage entry points that mirror the calls of leap_frog::step
+// (leap_frog.cu:162-248) and the fused, graph-captured step.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "launch.cuh"
+#include "toolsetup.h"
+
+using namespace sphfem;
+
+struct sph_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int N = 0;
+    KConsts K{};
+    sph_grid_params grid{};
+    SortedFields buf[2]{};
+    int cur = 0;                         // buf[cur] holds the particle state
+    FixedFields F{};
+    SortScratch X{};
+    StepScratch W{};
+    bool counts_valid = false;           // X.key/arrival/counts match the current state
+    // tool
+    bool has_tool = false;
+    ToolModelHost tool_host;
+    SegDev seg{};
+    FemDev fem{};
+    ToolDev *tool_dev = nullptr;
+    double *fem_T_old = nullptr, *fem_f_temp = nullptr, *fem_K_temp = nullptr;
+    // graphs, one per buffer parity
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int64_t graph_launches[2] = {0, 0};
+    bool use_graph = true;
+    int64_t launches = 0;
+    double *h_reduce = nullptr;          // pinned
+    std::vector<void *> allocs;
+    std::string err;
+};
+
+namespace {
+
+const char *g_no_ctx = "no context";
+
+int fail(sph_ctx *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                       \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess)                                                                         \
+            return fail(ctx, SPH_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));         \
+    } while (0)
+
+#define CK_LAUNCH()                                                                                    \
+    do {                                                                                               \
+        cudaError_t e_ = cudaGetLastError();                                                           \
+        if (e_ != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T>
+int dalloc(sph_ctx *ctx, T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)p, sizeof(T) * count);
+    if (e != cudaSuccess) return fail(ctx, SPH_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    ctx->allocs.push_back((void *)*p);
+    return SPH_OK;
+}
+
+#define DALLOC(p, n)                          \
+    do {                                      \
+        int r_ = dalloc(ctx, &(p), (n));      \
+        if (r_ != SPH_OK) return r_;          \
+    } while (0)
+
+void geometry_from(const sph_grid_params &g, sph_geom_constants &out) {
+    // grid.cu:130-149 set_geometry (locked grid); cell edge = h * cell_factor
+    double bbmin_x = g.bbmin[0] - 1e-6, bbmin_y = g.bbmin[1] - 1e-6;
+    double bbmax_x = g.bbmax[0] + 1e-6, bbmax_y = g.bbmax[1] + 1e-6;
+    double kernel_width = 2.;
+    double dx = g.h * kernel_width / 2. * (double)g.cell_factor;
+    unsigned int nx = (unsigned int)ceil((bbmax_x - bbmin_x) / dx);
+    unsigned int ny = (unsigned int)ceil((bbmax_y - bbmin_y) / dx);
+    out.nx = (int)nx;
+    out.ny = (int)ny;
+    out.bbmin_x = bbmin_x;
+    out.bbmin_y = bbmin_y;
+    out.dx = dx;
+    out.num_cell = (int)(nx * ny);
+    out.stencil = g.stencil;
+}
+
+void derive(KConsts &K) {
+    K.c0sq = 0.;
+    K.inv_wdeltap = 1. / K.c.corr.wdeltap;
+    K.eta2 = K.c.corr.eta * K.c.corr.eta;
+}
+
+void invalidate_graphs(sph_ctx *ctx) {
+    for (int p = 0; p < 2; p++)
+        if (ctx->graph[p]) {
+            cudaGraphExecDestroy(ctx->graph[p]);
+            ctx->graph[p] = nullptr;
+        }
+}
+
+// Field descriptors for upload/download of the caller-visible view.
+struct FieldDesc {
+    size_t off_view;      // offset of the double*/int* member in sph_particles
+    int width;            // 8-byte (or 4-byte for ints) words per particle
+    bool is_int;
+};
+
+sph_particles view_of(const sph_ctx *ctx) {
+    const SortedFields &A = ctx->buf[ctx->cur];
+    sph_particles v;
+    std::memset(&v, 0, sizeof(v));
+    v.N = ctx->N;
+    v.pos = (double *)A.pos; v.vel = (double *)A.vel; v.h = A.h; v.rho = A.rho; v.p = ctx->F.p;
+    v.S = (double *)A.S; v.R = (double *)ctx->F.R; v.fc = (double *)A.fc; v.ft = (double *)A.ft; v.n = (double *)A.n;
+    v.fixed = A.fixed; v.blanked = A.blanked; v.tool_particle = A.tool_particle;
+    v.eps_pl = A.eps_pl; v.eps_pl_dot = A.eps_pl_dot; v.T = A.T;
+    v.pos_t = (double *)A.pos_t; v.vel_t = (double *)A.vel_t; v.rho_t = A.rho_t; v.S_t = (double *)A.S_t; v.T_t = A.T_t;
+    v.S_der = (double *)ctx->F.S_der; v.v_der = (double *)ctx->F.v_der;
+    v.idx = ctx->F.idx; v.hash = A.hash; v.on_seg = A.on_seg;
+    return v;
+}
+
+const FieldDesc kFields[] = {
+    {offsetof(sph_particles, pos), 2, false},   {offsetof(sph_particles, vel), 2, false},
+    {offsetof(sph_particles, h), 1, false},     {offsetof(sph_particles, rho), 1, false},
+    {offsetof(sph_particles, p), 1, false},     {offsetof(sph_particles, S), 4, false},
+    {offsetof(sph_particles, R), 4, false},     {offsetof(sph_particles, fc), 2, false},
+    {offsetof(sph_particles, ft), 2, false},    {offsetof(sph_particles, n), 2, false},
+    {offsetof(sph_particles, fixed), 1, false}, {offsetof(sph_particles, blanked), 1, false},
+    {offsetof(sph_particles, tool_particle), 1, false}, {offsetof(sph_particles, eps_pl), 1, false},
+    {offsetof(sph_particles, eps_pl_dot), 1, false},    {offsetof(sph_particles, T), 1, false},
+    {offsetof(sph_particles, pos_t), 2, false}, {offsetof(sph_particles, vel_t), 2, false},
+    {offsetof(sph_particles, rho_t), 1, false}, {offsetof(sph_particles, S_t), 4, false},
+    {offsetof(sph_particles, T_t), 1, false},   {offsetof(sph_particles, S_der), 4, false},
+    {offsetof(sph_particles, v_der), 4, false}, {offsetof(sph_particles, idx), 1, true},
+    {offsetof(sph_particles, hash), 1, true},   {offsetof(sph_particles, on_seg), 1, true},
+};
+
+template <class M>
+M member(const sph_particles &v, size_t off) {
+    return *(const M *)((const char *)&v + off);
+}
+
+int alloc_sorted(sph_ctx *ctx, SortedFields &S, int N) {
+    DALLOC(S.pos, N); DALLOC(S.vel, N); DALLOC(S.fc, N); DALLOC(S.ft, N); DALLOC(S.n, N);
+    DALLOC(S.h, N); DALLOC(S.rho, N); DALLOC(S.eps_pl, N); DALLOC(S.eps_pl_dot, N); DALLOC(S.T, N);
+    DALLOC(S.fixed, N); DALLOC(S.blanked, N); DALLOC(S.tool_particle, N); DALLOC(S.S, N);
+    DALLOC(S.pos_t, N); DALLOC(S.vel_t, N); DALLOC(S.rho_t, N); DALLOC(S.T_t, N); DALLOC(S.S_t, N);
+    DALLOC(S.on_seg, N); DALLOC(S.hash, N);
+    return SPH_OK;
+}
+
+int zero_all(sph_ctx *ctx) {
+    sph_particles v = view_of(ctx);
+    for (const FieldDesc &fd : kFields) {
+        void *dst = member<void *>(v, fd.off_view);
+        size_t bytes = (size_t)ctx->N * fd.width * (fd.is_int ? 4 : 8);
+        CK(cudaMemsetAsync(dst, 0, bytes, ctx->stream));
+    }
+    return SPH_OK;
+}
+
+// ---- staged FEM helpers ----------------------------------------------------------------
+int ensure_fem_temp(sph_ctx *ctx) {
+    if (ctx->fem_T_old) return SPH_OK;
+    DALLOC(ctx->fem_T_old, ctx->fem.n_nodes);
+    DALLOC(ctx->fem_f_temp, ctx->fem.n_nodes);
+    DALLOC(ctx->fem_K_temp, ctx->fem.nnz);
+    return SPH_OK;
+}
+
+#define REQUIRE_CTX() \
+    if (!ctx) return SPH_ERR_INVALID;
+#define REQUIRE_TOOL() \
+    if (!ctx->has_tool) return fail(ctx, SPH_ERR_STATE, "context has no tool");
+
+SortedFields &CUR(sph_ctx *ctx) { return ctx->buf[ctx->cur]; }
+
+// The fused step body (everything after the histogram of the current state).
+int issue_fused_body(sph_ctx *ctx, int64_t &n) {
+    const int N = ctx->N;
+    cudaStream_t s = ctx->stream;
+    SortedFields &A = ctx->buf[ctx->cur];
+    SortedFields &B = ctx->buf[1 - ctx->cur];
+    launch_sort_rest(s, N, ctx->X, ctx->K.g, ctx->F.idx, ctx->W.status);
+    n += 5;
+    launch_gather_fused(s, N, ctx->F.idx, ctx->K, A, B, ctx->F, ctx->W);
+    n += 1;
+    if (ctx->has_tool) {
+        launch_fem_half(s, ctx->fem, 0.5 * ctx->K.dt);
+        n += 1;
+    }
+    launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, ctx->seg, ctx->tool_dev, true);
+    n += 1;
+    if (ctx->has_tool) {
+        launch_fem_rate_update(s, ctx->K, ctx->fem, ctx->seg, ctx->K.dt);
+        launch_tool_move(s, ctx->seg, ctx->fem, ctx->tool_dev, ctx->K.dt, 3);
+        n += 2;
+    }
+    CK(cudaMemsetAsync(ctx->X.counts, 0, sizeof(int32_t) * (size_t)(ctx->K.g.num_cell + 1), s));
+    launch_step_tail(s, N, ctx->K, B, ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->X, ctx->W.status, true);
+    n += 1;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+}  // namespace
+
+struct sph_tool_host {
+    ToolModelHost m;
+    std::string err;
+};
+
+extern "C" {
+
+int sph_abi_version(void) { return SPHFEM_ABI_VERSION; }
+
+// ---- host-only tool set-up ------------------------------------------------------------------
+int sph_tool_build(const sph_tool_mesh *mesh, const sph_tool_constants *tc, sph_tool_host **out) {
+    if (!mesh || !tc || !out) return SPH_ERR_INVALID;
+    sph_tool_host *t = new sph_tool_host();
+    *out = t;
+    return build_tool_model(*mesh, *tc, t->m, t->err);
+}
+
+int sph_tool_host_info(const sph_tool_host *t, sph_tool_state *st, int32_t *n_nodes, int32_t *nnz,
+                       int32_t *n_colors) {
+    if (!t) return SPH_ERR_INVALID;
+    const ToolModelHost &M = t->m;
+    if (st) {
+        std::memset(st, 0, sizeof(*st));
+        for (int a = 0; a < 2; a++) {
+            st->tl_point_ref[a] = M.tl_point_ref[a];
+            st->br_point[a] = M.br_point[a];
+        }
+        st->ref_dist = M.ref_dist;
+        st->lowest_point = M.lowest_point;
+        st->right_point = M.right_point;
+        st->n_segments = M.n_seg;
+        st->n_cut_colors = M.n_cut_colors;
+    }
+    if (n_nodes) *n_nodes = M.n_nodes;
+    if (nnz) *nnz = (int32_t)M.col_ind.size();
+    if (n_colors) *n_colors = M.n_colors;
+    return SPH_OK;
+}
+
+int sph_tool_host_export(const sph_tool_host *t, sph_segments *seg, sph_fem *fem) {
+    if (!t) return SPH_ERR_INVALID;
+    const ToolModelHost &M = t->m;
+    if (seg) {
+        if (seg->n != M.n_seg) return SPH_ERR_INVALID;
+        const size_t n = (size_t)M.n_seg;
+        if (seg->left) std::memcpy(seg->left, M.left.data(), 16 * n);
+        if (seg->right) std::memcpy(seg->right, M.right.data(), 16 * n);
+        if (seg->normal) std::memcpy(seg->normal, M.normal.data(), 16 * n);
+        if (seg->marks) std::memcpy(seg->marks, M.marks.data(), 16 * n);
+        if (seg->heat_exchange) std::memset(seg->heat_exchange, 0, 16 * n);
+        if (seg->fric_heat) std::memset(seg->fric_heat, 0, 8 * n);
+    }
+    if (fem) {
+        if (fem->n_nodes != M.n_nodes || fem->nnz != (int32_t)M.col_ind.size()) return SPH_ERR_INVALID;
+        const size_t nn = (size_t)M.n_nodes, nz = M.col_ind.size();
+        if (fem->position) std::memcpy(fem->position, M.pos.data(), 16 * nn);
+        if (fem->row_ptr) std::memcpy(fem->row_ptr, M.row_ptr.data(), 4 * (nn + 1));
+        if (fem->col_ind) std::memcpy(fem->col_ind, M.col_ind.data(), 4 * nz);
+        if (fem->K) std::memcpy(fem->K, M.K.data(), 8 * nz);
+        if (fem->M_inv) std::memcpy(fem->M_inv, M.M_inv.data(), 8 * nn);
+        if (fem->f) std::memcpy(fem->f, M.f.data(), 8 * nn);
+        if (fem->T) std::memcpy(fem->T, M.T.data(), 8 * nn);
+        if (fem->k) std::memset(fem->k, 0, 8 * nn);
+    }
+    return SPH_OK;
+}
+
+int sph_tool_host_destroy(sph_tool_host *t) {
+    if (!t) return SPH_ERR_INVALID;
+    delete t;
+    return SPH_OK;
+}
+
+const char *sph_last_error(const sph_ctx *ctx) { return ctx ? ctx->err.c_str() : g_no_ctx; }
+
+int sph_ctx_destroy(sph_ctx *ctx) {
+    if (!ctx) return SPH_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    invalidate_graphs(ctx);
+    for (void *p : ctx->allocs) cudaFree(p);
+    if (ctx->tool_dev) cudaFree(ctx->tool_dev);
+    if (ctx->h_reduce) cudaFreeHost(ctx->h_reduce);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return SPH_OK;
+}
+
+int sph_ctx_create(const sph_constants *c, const sph_grid_params *g, const sph_particles *host,
+                   const sph_tool_mesh *tool, double dt, int32_t precision, int32_t device, sph_ctx **out) {
+    if (!c || !g || !host || !out) return SPH_ERR_INVALID;
+    *out = nullptr;
+    if (host->N <= 0) return SPH_ERR_INVALID;
+    if (precision != SPH_PREC_FP64 && precision != SPH_PREC_FP32K) return SPH_ERR_INVALID;
+    if (g->cell_factor < 1 || g->stencil < 1 || !(g->h > 0)) return SPH_ERR_INVALID;
+    if ((double)g->stencil * (double)g->cell_factor < 2.0) return SPH_ERR_INVALID;   // stencil must cover 2h
+    sph_ctx *ctx = new sph_ctx();
+    ctx->device = device;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device) {
+        delete ctx;
+        return SPH_ERR_NO_DEVICE;
+    }
+    cudaDeviceProp prop;
+    if (cudaSetDevice(device) != cudaSuccess || cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+        delete ctx;
+        return SPH_ERR_NO_DEVICE;
+    }
+    if (!(prop.major == 10 && prop.minor == 3)) {   // built for sm_103a only
+        delete ctx;
+        return SPH_ERR_NO_DEVICE;
+    }
+    *out = ctx;   // from here on errors are reported through ctx (caller destroys)
+    CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    const int N = host->N;
+    ctx->N = N;
+    ctx->grid = *g;
+    ctx->K.c = *c;
+    geometry_from(*g, ctx->K.g);
+    if (ctx->K.g.nx <= 0 || ctx->K.g.ny <= 0 || (int64_t)ctx->K.g.nx * ctx->K.g.ny > (int64_t)1 << 30)
+        return fail(ctx, SPH_ERR_INVALID, "grid geometry out of range");
+    ctx->K.dt = dt;
+    ctx->K.precision = precision;
+    derive(ctx->K);
+    // particle arrays (particle_gpu ctor, particle_gpu.cu:11-104) and the Green buffer
+    for (int b = 0; b < 2; b++) {
+        int r = alloc_sorted(ctx, ctx->buf[b], N);
+        if (r) return r;
+    }
+    DALLOC(ctx->F.p, N); DALLOC(ctx->F.R, N); DALLOC(ctx->F.S_der, N); DALLOC(ctx->F.v_der, N); DALLOC(ctx->F.idx, N);
+    const int nc = ctx->K.g.num_cell;
+    DALLOC(ctx->X.key, N); DALLOC(ctx->X.arrival, N); DALLOC(ctx->X.slots, N);
+    DALLOC(ctx->X.counts, (size_t)nc + 1); DALLOC(ctx->X.offsets, (size_t)nc + 2);
+    DALLOC(ctx->X.block_sums, (size_t)scan_blocks(nc) + 1);
+    DALLOC(ctx->X.cell_start, nc); DALLOC(ctx->X.cell_end, nc);
+    if (precision == SPH_PREC_FP32K) DALLOC(ctx->W.rec32, (size_t)4 * N);
+    else DALLOC(ctx->W.rec64, (size_t)4 * N);
+    DALLOC(ctx->W.pos_init, N); DALLOC(ctx->W.vel_init, N); DALLOC(ctx->W.S_init, N);
+    DALLOC(ctx->W.rho_init, N); DALLOC(ctx->W.T_init, N);
+    DALLOC(ctx->W.secant_iters, N); DALLOC(ctx->W.status, 1);
+    DALLOC(ctx->W.reduce, (size_t)3 * reduce_blocks());
+    CK(cudaMallocHost((void **)&ctx->h_reduce, sizeof(double) * 3 * reduce_blocks()));
+    int r = zero_all(ctx);
+    if (r) return r;
+    for (int b = 0; b < 2; b++) CK(cudaMemsetAsync(ctx->buf[b].hash, 0, sizeof(int32_t) * N, ctx->stream));
+    CK(cudaMemsetAsync(ctx->W.status, 0, sizeof(uint32_t), ctx->stream));
+    CK(cudaMemsetAsync(ctx->W.secant_iters, 0, sizeof(int32_t) * N, ctx->stream));
+    CK(cudaMemsetAsync(ctx->X.cell_end, 0, sizeof(int32_t) * nc, ctx->stream));
+    CK(cudaMemsetAsync(ctx->X.cell_start, 0xff, sizeof(int32_t) * nc, ctx->stream));
+    {   // idx = 0..N-1 (thrust::sequence, particle_gpu.cu:56-57)
+        std::vector<int32_t> seq(N);
+        for (int i = 0; i < N; i++) seq[i] = i;
+        CK(cudaMemcpyAsync(ctx->F.idx, seq.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    r = sph_upload_particles(ctx, host);
+    if (r) return r;
+    // tool
+    CK(cudaMalloc((void **)&ctx->tool_dev, sizeof(ToolDev)));
+    ToolDev td{};
+    if (tool) {
+        r = build_tool_model(*tool, c->tool, ctx->tool_host, ctx->err);
+        if (r) return r;
+        ToolModelHost &M = ctx->tool_host;
+        ctx->has_tool = true;
+        ctx->K.has_tool = 1;
+        SegDev &S = ctx->seg;
+        S.n = M.n_seg;
+        DALLOC(S.left, M.n_seg); DALLOC(S.right, M.n_seg); DALLOC(S.normal, M.n_seg); DALLOC(S.marks, M.n_seg);
+        DALLOC(S.heat_exchange, M.n_seg); DALLOC(S.fric_heat, M.n_seg);
+        CK(cudaMemcpy(S.left, M.left.data(), sizeof(double) * 2 * M.n_seg, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(S.right, M.right.data(), sizeof(double) * 2 * M.n_seg, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(S.normal, M.normal.data(), sizeof(double) * 2 * M.n_seg, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(S.marks, M.marks.data(), sizeof(int4) * M.n_seg, cudaMemcpyHostToDevice));
+        CK(cudaMemset(S.heat_exchange, 0, sizeof(double2) * M.n_seg));
+        CK(cudaMemset(S.fric_heat, 0, sizeof(double) * M.n_seg));
+        FemDev &Fm = ctx->fem;
+        Fm.n_nodes = M.n_nodes;
+        Fm.nnz = (int)M.col_ind.size();
+        DALLOC(Fm.position, M.n_nodes); DALLOC(Fm.row_ptr, M.n_nodes + 1); DALLOC(Fm.col_ind, Fm.nnz);
+        DALLOC(Fm.diag, M.n_nodes); DALLOC(Fm.K, Fm.nnz); DALLOC(Fm.M_inv, M.n_nodes); DALLOC(Fm.f, M.n_nodes);
+        DALLOC(Fm.T, M.n_nodes); DALLOC(Fm.k, M.n_nodes); DALLOC(Fm.T_half, M.n_nodes);
+        DALLOC(Fm.node_seg_ptr, M.n_nodes + 1); DALLOC(Fm.node_seg, M.node_seg.size());
+        CK(cudaMemcpy(Fm.position, M.pos.data(), sizeof(double) * 2 * M.n_nodes, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(Fm.row_ptr, M.row_ptr.data(), sizeof(int) * (M.n_nodes + 1), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(Fm.col_ind, M.col_ind.data(), sizeof(int) * Fm.nnz, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(Fm.diag, M.diag.data(), sizeof(int) * M.n_nodes, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(Fm.K, M.K.data(), sizeof(double) * Fm.nnz, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(Fm.M_inv, M.M_inv.data(), sizeof(double) * M.n_nodes, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(Fm.f, M.f.data(), sizeof(double) * M.n_nodes, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(Fm.T, M.T.data(), sizeof(double) * M.n_nodes, cudaMemcpyHostToDevice));
+        CK(cudaMemset(Fm.k, 0, sizeof(double) * M.n_nodes));
+        CK(cudaMemcpy(Fm.T_half, M.T.data(), sizeof(double) * M.n_nodes, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(Fm.node_seg_ptr, M.node_seg_ptr.data(), sizeof(int) * (M.n_nodes + 1), cudaMemcpyHostToDevice));
+        if (!M.node_seg.empty())
+            CK(cudaMemcpy(Fm.node_seg, M.node_seg.data(), sizeof(int) * M.node_seg.size(), cudaMemcpyHostToDevice));
+        td.tl_point_ref[0] = M.tl_point_ref[0]; td.tl_point_ref[1] = M.tl_point_ref[1];
+        td.br_point[0] = M.br_point[0]; td.br_point[1] = M.br_point[1];
+        td.ref_dist = M.ref_dist; td.lowest_point = M.lowest_point; td.right_point = M.right_point;
+    }
+    CK(cudaMemcpy(ctx->tool_dev, &td, sizeof(ToolDev), cudaMemcpyHostToDevice));
+    CK(cudaDeviceSynchronize());
+    return SPH_OK;
+}
+
+int sph_set_dt(sph_ctx *ctx, double dt) {
+    REQUIRE_CTX();
+    ctx->K.dt = dt;
+    invalidate_graphs(ctx);
+    return SPH_OK;
+}
+
+int sph_get_geometry(const sph_ctx *ctx, sph_geom_constants *out) {
+    if (!ctx || !out) return SPH_ERR_INVALID;
+    *out = ctx->K.g;
+    return SPH_OK;
+}
+
+int sph_set_constants(sph_ctx *ctx, const sph_constants *c) {
+    REQUIRE_CTX();
+    if (!c) return SPH_ERR_INVALID;
+    ctx->K.c = *c;
+    derive(ctx->K);
+    invalidate_graphs(ctx);
+    return SPH_OK;
+}
+
+int sph_sync(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaGetLastError());
+    return SPH_OK;
+}
+
+int sph_status(sph_ctx *ctx, uint32_t *status, int32_t clear) {
+    REQUIRE_CTX();
+    if (!status) return SPH_ERR_INVALID;
+    CK(cudaMemcpyAsync(status, ctx->W.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    if (clear) CK(cudaMemsetAsync(ctx->W.status, 0, sizeof(uint32_t), ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+int sph_get_stream(const sph_ctx *ctx, void **stream) {
+    if (!ctx || !stream) return SPH_ERR_INVALID;
+    *stream = (void *)ctx->stream;
+    return SPH_OK;
+}
+
+int sph_launch_count(const sph_ctx *ctx, int64_t *count) {
+    if (!ctx || !count) return SPH_ERR_INVALID;
+    *count = ctx->launches;
+    return SPH_OK;
+}
+
+int sph_get_particles(sph_ctx *ctx, sph_particles *dev_view) {
+    REQUIRE_CTX();
+    if (!dev_view) return SPH_ERR_INVALID;
+    *dev_view = view_of(ctx);
+    return SPH_OK;
+}
+
+int sph_upload_particles(sph_ctx *ctx, const sph_particles *host) {
+    REQUIRE_CTX();
+    if (!host || host->N != ctx->N) return fail(ctx, SPH_ERR_INVALID, "upload: particle count mismatch");
+    sph_particles v = view_of(ctx);
+    for (const FieldDesc &fd : kFields) {
+        const void *src = member<const void *>(*host, fd.off_view);
+        if (!src) continue;
+        void *dst = member<void *>(v, fd.off_view);
+        CK(cudaMemcpyAsync(dst, src, (size_t)ctx->N * fd.width * (fd.is_int ? 4 : 8), cudaMemcpyHostToDevice,
+                           ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->counts_valid = false;
+    return SPH_OK;
+}
+
+int sph_download_particles(sph_ctx *ctx, sph_particles *host) {
+    REQUIRE_CTX();
+    if (!host || host->N != ctx->N) return fail(ctx, SPH_ERR_INVALID, "download: particle count mismatch");
+    sph_particles v = view_of(ctx);
+    for (const FieldDesc &fd : kFields) {
+        void *dst = member<void *>(*host, fd.off_view);
+        if (!dst) continue;
+        const void *src = member<void *>(v, fd.off_view);
+        CK(cudaMemcpyAsync(dst, src, (size_t)ctx->N * fd.width * (fd.is_int ? 4 : 8), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+int sph_get_cells(sph_ctx *ctx, int32_t **cell_start, int32_t **cell_end, int32_t *num_cell) {
+    REQUIRE_CTX();
+    if (cell_start) *cell_start = ctx->X.cell_start;
+    if (cell_end) *cell_end = ctx->X.cell_end;
+    if (num_cell) *num_cell = ctx->K.g.num_cell;
+    return SPH_OK;
+}
+
+int sph_download_cells(sph_ctx *ctx, int32_t *cell_start, int32_t *cell_end) {
+    REQUIRE_CTX();
+    size_t b = sizeof(int32_t) * (size_t)ctx->K.g.num_cell;
+    if (cell_start) CK(cudaMemcpyAsync(cell_start, ctx->X.cell_start, b, cudaMemcpyDeviceToHost, ctx->stream));
+    if (cell_end) CK(cudaMemcpyAsync(cell_end, ctx->X.cell_end, b, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+// ---- grid ------------------------------------------------------------------------------------
+int sph_update_geometry(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    return SPH_OK;   // locked grid (grid.cu:88-91)
+}
+
+int sph_assign_hashes(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    launch_hash(ctx->stream, ctx->N, CUR(ctx), ctx->K.g);
+    ctx->launches += 1;
+    ctx->counts_valid = false;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+int sph_sort(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    const int N = ctx->N;
+    launch_count(ctx->stream, N, CUR(ctx), ctx->X, ctx->K.g, ctx->W.status, false);
+    launch_sort_rest(ctx->stream, N, ctx->X, ctx->K.g, ctx->F.idx, ctx->W.status);
+    launch_gather_plain(ctx->stream, N, ctx->F.idx, CUR(ctx), ctx->buf[1 - ctx->cur]);
+    ctx->launches += 7;
+    CK_LAUNCH();
+    ctx->cur = 1 - ctx->cur;   // double_buffer swap (grid_gpu_green.cu:152-182)
+    ctx->counts_valid = false;
+    return SPH_OK;
+}
+
+// ---- leap frog --------------------------------------------------------------------------------
+int sph_init(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    launch_init(ctx->stream, ctx->N, CUR(ctx), ctx->W);
+    ctx->launches++;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+int sph_predict(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    launch_predict_correct(ctx->stream, ctx->N, CUR(ctx), ctx->W, 0.5 * ctx->K.dt);
+    ctx->launches++;
+    ctx->counts_valid = false;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+int sph_correct(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    launch_predict_correct(ctx->stream, ctx->N, CUR(ctx), ctx->W, ctx->K.dt);
+    ctx->launches++;
+    ctx->counts_valid = false;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+// ---- actions ----------------------------------------------------------------------------------
+#define STAGE(name, call)                 \
+    int name(sph_ctx *ctx) {              \
+        REQUIRE_CTX();                    \
+        call;                             \
+        ctx->launches++;                  \
+        ctx->counts_valid = false;        \
+        CK_LAUNCH();                      \
+        return SPH_OK;                    \
+    }
+
+STAGE(sph_material_eos, launch_eos(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->F))
+STAGE(sph_corrector_artificial_stress, launch_artificial_stress(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->F))
+STAGE(sph_material_stress_rate_jaumann, launch_jaumann(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->F))
+STAGE(sph_contmech_continuity, launch_continuity(ctx->stream, ctx->N, CUR(ctx), ctx->F))
+STAGE(sph_contmech_momentum, launch_momentum(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->F))
+STAGE(sph_contmech_advection, launch_advection(ctx->stream, ctx->N, CUR(ctx)))
+STAGE(sph_perform_boundary_conditions, launch_bc(ctx->stream, ctx->N, CUR(ctx)))
+STAGE(sph_debug_invalidate, launch_invalidate(ctx->stream, ctx->N, CUR(ctx), ctx->W.status))
+
+int sph_perform_boundary_conditions_thermal(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    if (ctx->K.c.trml_tool.alpha == 0.) return SPH_OK;   // m_thermal off (actions_gpu.cu:881-886)
+    launch_bc_thermal(ctx->stream, ctx->N, ctx->K, CUR(ctx));
+    ctx->launches++;
+    ctx->counts_valid = false;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+int sph_plasticity_johnson_cook(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    if (!ctx->K.c.plastic) return SPH_OK;   // m_plastic off (actions_gpu.cu:874-879)
+    launch_plasticity(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->F, ctx->W);
+    ctx->launches++;
+    ctx->counts_valid = false;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+int sph_interactions_monaghan(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    launch_build_records(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->F, ctx->W);
+    launch_interactions(ctx->stream, ctx->N, ctx->K, ctx->X.offsets, CUR(ctx), ctx->F, ctx->W, ctx->seg,
+                        ctx->tool_dev, false);
+    ctx->launches += 2;
+    ctx->counts_valid = false;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+// ---- tool -------------------------------------------------------------------------------------
+int sph_material_fric_heat_gen_fem(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    launch_fric_heat(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->seg, ctx->tool_dev, ctx->W.status);
+    ctx->launches++;
+    ctx->counts_valid = false;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+int sph_compute_contact_forces_fem(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    launch_contact(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->W.status);
+    ctx->launches += 2;
+    ctx->counts_valid = false;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+int sph_segments_update(sph_ctx *ctx, double dt) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    launch_tool_move(ctx->stream, ctx->seg, ctx->fem, ctx->tool_dev, dt, 1);
+    ctx->launches++;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+int sph_tool_update_fem(sph_ctx *ctx, double dt) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    launch_tool_move(ctx->stream, ctx->seg, ctx->fem, ctx->tool_dev, dt, 2);
+    ctx->launches++;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+int sph_fem_reset_server(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    int r = ensure_fem_temp(ctx);
+    if (r) return r;
+    launch_fem_reset(ctx->stream, ctx->fem, ctx->fem_T_old, ctx->fem_f_temp, ctx->fem_K_temp);
+    ctx->launches++;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+int sph_fem_apply_robin(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    int r = ensure_fem_temp(ctx);
+    if (r) return r;
+    launch_fem_robin(ctx->stream, ctx->K, ctx->fem, ctx->seg, ctx->fem_f_temp, ctx->fem_K_temp);
+    ctx->launches++;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+int sph_fem_calculate_temp_rate(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    int r = ensure_fem_temp(ctx);
+    if (r) return r;
+    launch_fem_rate(ctx->stream, ctx->fem, ctx->fem_f_temp, ctx->fem_K_temp);
+    ctx->launches++;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+int sph_fem_calculate_temp(sph_ctx *ctx, double dt) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    int r = ensure_fem_temp(ctx);
+    if (r) return r;
+    launch_fem_temp(ctx->stream, ctx->fem, ctx->fem_T_old, dt);
+    ctx->launches++;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+int sph_set_tool_velocity(sph_ctx *ctx, double vx, double vy) {
+    REQUIRE_CTX();
+    double v[2] = {vx, vy};
+    CK(cudaMemcpyAsync(ctx->tool_dev, v, sizeof(v), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+int sph_get_tool_state(sph_ctx *ctx, sph_tool_state *out) {
+    REQUIRE_CTX();
+    if (!out) return SPH_ERR_INVALID;
+    ToolDev td;
+    CK(cudaMemcpyAsync(&td, ctx->tool_dev, sizeof(td), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    std::memset(out, 0, sizeof(*out));
+    for (int a = 0; a < 2; a++) {
+        out->vel[a] = td.vel[a];
+        out->tl_point_ref[a] = td.tl_point_ref[a];
+        out->br_point[a] = td.br_point[a];
+    }
+    out->ref_dist = td.ref_dist;
+    out->lowest_point = td.lowest_point;
+    out->right_point = td.right_point;
+    out->n_segments = ctx->seg.n;
+    out->n_cut_colors = ctx->tool_host.n_cut_colors;
+    return SPH_OK;
+}
+
+int sph_get_segments(sph_ctx *ctx, sph_segments *v) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    if (!v) return SPH_ERR_INVALID;
+    v->n = ctx->seg.n;
+    v->left = (double *)ctx->seg.left;
+    v->right = (double *)ctx->seg.right;
+    v->normal = (double *)ctx->seg.normal;
+    v->marks = (int32_t *)ctx->seg.marks;
+    v->heat_exchange = (double *)ctx->seg.heat_exchange;
+    v->fric_heat = ctx->seg.fric_heat;
+    return SPH_OK;
+}
+
+int sph_download_segments(sph_ctx *ctx, sph_segments *h) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    if (!h || h->n != ctx->seg.n) return fail(ctx, SPH_ERR_INVALID, "download_segments: size mismatch");
+    const size_t n = (size_t)ctx->seg.n;
+    cudaStream_t s = ctx->stream;
+    if (h->left) CK(cudaMemcpyAsync(h->left, ctx->seg.left, 16 * n, cudaMemcpyDeviceToHost, s));
+    if (h->right) CK(cudaMemcpyAsync(h->right, ctx->seg.right, 16 * n, cudaMemcpyDeviceToHost, s));
+    if (h->normal) CK(cudaMemcpyAsync(h->normal, ctx->seg.normal, 16 * n, cudaMemcpyDeviceToHost, s));
+    if (h->marks) CK(cudaMemcpyAsync(h->marks, ctx->seg.marks, 16 * n, cudaMemcpyDeviceToHost, s));
+    if (h->heat_exchange) CK(cudaMemcpyAsync(h->heat_exchange, ctx->seg.heat_exchange, 16 * n, cudaMemcpyDeviceToHost, s));
+    if (h->fric_heat) CK(cudaMemcpyAsync(h->fric_heat, ctx->seg.fric_heat, 8 * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return SPH_OK;
+}
+
+int sph_get_fem(sph_ctx *ctx, sph_fem *v) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    if (!v) return SPH_ERR_INVALID;
+    v->n_nodes = ctx->fem.n_nodes;
+    v->nnz = ctx->fem.nnz;
+    v->position = (double *)ctx->fem.position;
+    v->row_ptr = ctx->fem.row_ptr;
+    v->col_ind = ctx->fem.col_ind;
+    v->K = ctx->fem.K;
+    v->M_inv = ctx->fem.M_inv;
+    v->f = ctx->fem.f;
+    v->T = ctx->fem.T;
+    v->k = ctx->fem.k;
+    return SPH_OK;
+}
+
+int sph_download_fem(sph_ctx *ctx, sph_fem *h) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    if (!h || h->n_nodes != ctx->fem.n_nodes || h->nnz != ctx->fem.nnz)
+        return fail(ctx, SPH_ERR_INVALID, "download_fem: size mismatch");
+    const size_t nn = (size_t)ctx->fem.n_nodes, nz = (size_t)ctx->fem.nnz;
+    cudaStream_t s = ctx->stream;
+    if (h->position) CK(cudaMemcpyAsync(h->position, ctx->fem.position, 16 * nn, cudaMemcpyDeviceToHost, s));
+    if (h->row_ptr) CK(cudaMemcpyAsync(h->row_ptr, ctx->fem.row_ptr, 4 * (nn + 1), cudaMemcpyDeviceToHost, s));
+    if (h->col_ind) CK(cudaMemcpyAsync(h->col_ind, ctx->fem.col_ind, 4 * nz, cudaMemcpyDeviceToHost, s));
+    if (h->K) CK(cudaMemcpyAsync(h->K, ctx->fem.K, 8 * nz, cudaMemcpyDeviceToHost, s));
+    if (h->M_inv) CK(cudaMemcpyAsync(h->M_inv, ctx->fem.M_inv, 8 * nn, cudaMemcpyDeviceToHost, s));
+    if (h->f) CK(cudaMemcpyAsync(h->f, ctx->fem.f, 8 * nn, cudaMemcpyDeviceToHost, s));
+    if (h->T) CK(cudaMemcpyAsync(h->T, ctx->fem.T, 8 * nn, cudaMemcpyDeviceToHost, s));
+    if (h->k) CK(cudaMemcpyAsync(h->k, ctx->fem.k, 8 * nn, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return SPH_OK;
+}
+
+int sph_upload_fem_state(sph_ctx *ctx, const double *T, const double *k) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    const size_t nn = (size_t)ctx->fem.n_nodes;
+    if (T) CK(cudaMemcpyAsync(ctx->fem.T, T, 8 * nn, cudaMemcpyHostToDevice, ctx->stream));
+    if (k) CK(cudaMemcpyAsync(ctx->fem.k, k, 8 * nn, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+// ---- whole step -------------------------------------------------------------------------------
+int sph_step(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    cudaStream_t s = ctx->stream;
+    if (!ctx->counts_valid) {
+        launch_count(s, ctx->N, CUR(ctx), ctx->X, ctx->K.g, ctx->W.status, true);
+        ctx->launches += 1;
+        CK_LAUNCH();
+    }
+    const int p = ctx->cur;
+    if (ctx->use_graph) {
+        if (!ctx->graph[p]) {
+            cudaGraph_t g = nullptr;
+            CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            int64_t n = 0;
+            int r = issue_fused_body(ctx, n);
+            cudaError_t e = cudaStreamEndCapture(s, &g);
+            if (r) {
+                if (g) cudaGraphDestroy(g);
+                return r;
+            }
+            if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&ctx->graph[p], g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
+            ctx->graph_launches[p] = n;
+        }
+        CK(cudaGraphLaunch(ctx->graph[p], s));
+        ctx->launches += ctx->graph_launches[p];
+    } else {
+        int64_t n = 0;
+        int r = issue_fused_body(ctx, n);
+        if (r) return r;
+        ctx->launches += n;
+    }
+    ctx->cur = 1 - ctx->cur;
+    ctx->counts_valid = true;
+    return SPH_OK;
+}
+
+int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_stages) {
+    REQUIRE_CTX();
+    constexpr int kStages = 7;
+    if (!stage_ms || nsteps < 1) return SPH_ERR_INVALID;
+    if (n_stages) *n_stages = kStages;
+    cudaStream_t s = ctx->stream;
+    const int N = ctx->N;
+    cudaEvent_t ev[kStages + 1];
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    for (int k = 0; k < kStages; k++) stage_ms[k] = 0.f;
+    for (int step = 0; step < nsteps; step++) {
+        SortedFields &A = ctx->buf[ctx->cur];
+        SortedFields &B = ctx->buf[1 - ctx->cur];
+        CK(cudaEventRecord(ev[0], s));
+        if (!ctx->counts_valid) {
+            launch_count(s, N, A, ctx->X, ctx->K.g, ctx->W.status, true);
+            ctx->launches++;
+        }
+        CK(cudaEventRecord(ev[1], s));
+        launch_sort_rest(s, N, ctx->X, ctx->K.g, ctx->F.idx, ctx->W.status);
+        CK(cudaEventRecord(ev[2], s));
+        launch_gather_fused(s, N, ctx->F.idx, ctx->K, A, B, ctx->F, ctx->W);
+        CK(cudaEventRecord(ev[3], s));
+        if (ctx->has_tool) launch_fem_half(s, ctx->fem, 0.5 * ctx->K.dt);
+        CK(cudaEventRecord(ev[4], s));
+        launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, ctx->seg, ctx->tool_dev, true);
+        CK(cudaEventRecord(ev[5], s));
+        if (ctx->has_tool) {
+            launch_fem_rate_update(s, ctx->K, ctx->fem, ctx->seg, ctx->K.dt);
+            launch_tool_move(s, ctx->seg, ctx->fem, ctx->tool_dev, ctx->K.dt, 3);
+        }
+        CK(cudaEventRecord(ev[6], s));
+        CK(cudaMemsetAsync(ctx->X.counts, 0, sizeof(int32_t) * (size_t)(ctx->K.g.num_cell + 1), s));
+        launch_step_tail(s, N, ctx->K, B, ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->X, ctx->W.status, true);
+        CK(cudaEventRecord(ev[7], s));
+        CK_LAUNCH();
+        ctx->launches += 8 + (ctx->has_tool ? 3 : 0);
+        CK(cudaEventSynchronize(ev[7]));
+        for (int k = 0; k < kStages; k++) {
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+            stage_ms[k] += ms;
+        }
+        ctx->cur = 1 - ctx->cur;
+        ctx->counts_valid = true;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    return SPH_OK;
+}
+
+int sph_run(sph_ctx *ctx, int32_t nsteps) {
+    REQUIRE_CTX();
+    for (int i = 0; i < nsteps; i++) {
+        int r = sph_step(ctx);
+        if (r) return r;
+    }
+    return SPH_OK;
+}
+
+int sph_step_staged(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    int r;
+#define RUN(x)            \
+    if ((r = (x)) != SPH_OK) return r;
+    const double dt = ctx->K.dt;
+    RUN(sph_update_geometry(ctx));
+    RUN(sph_assign_hashes(ctx));
+    RUN(sph_sort(ctx));
+    RUN(sph_init(ctx));
+    if (ctx->has_tool) RUN(sph_fem_reset_server(ctx));
+    RUN(sph_predict(ctx));
+    if (ctx->has_tool) RUN(sph_fem_calculate_temp(ctx, 0.5 * dt));
+    RUN(sph_material_eos(ctx));
+    RUN(sph_corrector_artificial_stress(ctx));
+    RUN(sph_interactions_monaghan(ctx));
+    RUN(sph_material_stress_rate_jaumann(ctx));
+    RUN(sph_contmech_continuity(ctx));
+    RUN(sph_contmech_momentum(ctx));
+    RUN(sph_contmech_advection(ctx));
+    RUN(sph_correct(ctx));
+    if (ctx->has_tool) {
+        RUN(sph_material_fric_heat_gen_fem(ctx));
+        RUN(sph_fem_apply_robin(ctx));
+        RUN(sph_fem_calculate_temp_rate(ctx));
+        RUN(sph_fem_calculate_temp(ctx, dt));
+    }
+    RUN(sph_plasticity_johnson_cook(ctx));
+    if (ctx->has_tool) {
+        RUN(sph_segments_update(ctx, dt));
+        RUN(sph_tool_update_fem(ctx, dt));
+        RUN(sph_compute_contact_forces_fem(ctx));
+    }
+    RUN(sph_perform_boundary_conditions(ctx));
+    RUN(sph_perform_boundary_conditions_thermal(ctx));
+    RUN(sph_debug_invalidate(ctx));
+#undef RUN
+    return SPH_OK;
+}
+
+// ---- measurement hooks --------------------------------------------------------------------------
+static int reduce_force_T(sph_ctx *ctx, double out[3]) {
+    launch_reduce_force_T(ctx->stream, ctx->N, CUR(ctx), ctx->W.reduce);
+    ctx->launches++;
+    CK_LAUNCH();
+    const int nb = reduce_blocks();
+    CK(cudaMemcpyAsync(ctx->h_reduce, ctx->W.reduce, sizeof(double) * 3 * nb, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    double fx = 0., fy = 0., tm = -1e300;
+    for (int b = 0; b < nb; b++) {
+        fx += ctx->h_reduce[3 * b];
+        fy += ctx->h_reduce[3 * b + 1];
+        tm = std::fmax(tm, ctx->h_reduce[3 * b + 2]);
+    }
+    out[0] = fx;
+    out[1] = fy;
+    out[2] = tm;
+    return SPH_OK;
+}
+
+int sph_reduce_force(sph_ctx *ctx, double out[2]) {
+    REQUIRE_CTX();
+    if (!out) return SPH_ERR_INVALID;
+    double r3[3];
+    int r = reduce_force_T(ctx, r3);
+    if (r) return r;
+    out[0] = r3[0];
+    out[1] = r3[1];
+    return SPH_OK;
+}
+
+int sph_reduce_max_T(sph_ctx *ctx, double *out) {
+    REQUIRE_CTX();
+    if (!out) return SPH_ERR_INVALID;
+    double r3[3];
+    int r = reduce_force_T(ctx, r3);
+    if (r) return r;
+    *out = r3[2];
+    return SPH_OK;
+}
+
+}  // extern "C"

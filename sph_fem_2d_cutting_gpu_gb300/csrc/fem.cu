@@ -1,0 +1,164 @@
+// fem.cu -- explicit FEM thermal update of the tool and the rigid tool motion
+// (FEM_thermal_gpu.cu:342-468,865-921; tool_FEM.cu:109-139,1552-1582).
+//
+// The reference copies K -> K_temp and f -> f_temp every step
+// (reset_FEM_server), adds the Robin terms of every contact segment with
+// atomics in six colour launches (apply_robin_bdc) and then runs a
+// one-thread-per-row SpMV.  Here each node gathers the Robin terms of the
+// (at most a few) segments that end on it, in a fixed order, and applies them
+// inside its own SpMV row: the same arithmetic without the per-step matrix
+// copy, without atomics and without the colour launches.
+#include "launch.cuh"
+
+namespace sphfem {
+
+// Robin terms of node i (FEM_thermal_gpu.cu:342-386): rhs and diagonal additions.
+__device__ __forceinline__ void robin_terms(const KConsts &K, const FemDev &F, const SegDev &seg, int i, double &df,
+                                            double &dk) {
+    df = 0.;
+    dk = 0.;
+    for (int t = F.node_seg_ptr[i]; t < F.node_seg_ptr[i + 1]; t++) {
+        int s = F.node_seg[t];
+        double2 hx = seg.heat_exchange[s];
+        if (hx.y == 0) continue;
+        double T_cont_particle = hx.x / hx.y;
+        double fric_eng = seg.fric_heat[s];
+        double2 l = seg.left[s], r = seg.right[s];
+        double ddx = l.x - r.x, ddy = l.y - r.y;
+        double dist = sqrtf_d(ddx * ddx + ddy * ddy);
+        df += 0.5 * K.c.tool.h * dist * T_cont_particle + 0.5 * fric_eng;
+        dk += K.c.tool.h * (0.5 * dist);
+    }
+}
+
+// calculate_temp(0.5*dt) at the start of the step (FEM_thermal_gpu.cu:460-468,
+// with T_old == T right after reset_FEM_server): T_half = 0.5 dt k + T.
+__global__ void __launch_bounds__(kBlock) k_fem_half(FemDev F, double hdt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F.n_nodes) return;
+    F.T_half[i] = hdt * F.k[i] + F.T[i];
+}
+
+// apply_robin_bdc + calculate_temp_rate + calculate_temp(dt), one row per
+// thread (FEM_thermal_gpu.cu:342-386,443-468).  Reads T_half, writes k and T.
+__global__ void __launch_bounds__(kBlock) k_fem_rate_update(KConsts K, FemDev F, SegDev seg, double dt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F.n_nodes) return;
+    double df, dk;
+    robin_terms(K, F, seg, i, df, dk);
+    double buffer = 0.;
+    for (int t = F.row_ptr[i]; t < F.row_ptr[i + 1]; t++) {
+        int c = F.col_ind[t];
+        double kij = F.K[t];
+        if (c == i) kij += dk;
+        buffer += kij * F.T_half[c];
+    }
+    double k = F.M_inv[i] * ((F.f[i] + df) - buffer);
+    F.k[i] = k;
+    F.T[i] = dt * k + F.T[i];
+}
+
+// Staged forms: the reference's separate calls.  K_temp / f_temp hold the
+// per-step copies that reset_FEM_server makes.
+__global__ void __launch_bounds__(kBlock) k_fem_reset(FemDev F, double *__restrict__ T_old,
+                                                      double *__restrict__ f_temp, double *__restrict__ K_temp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < F.n_nodes) {
+        T_old[i] = F.T[i];
+        f_temp[i] = F.f[i];
+    }
+    if (i < F.nnz) K_temp[i] = F.K[i];
+}
+
+__global__ void __launch_bounds__(kBlock) k_fem_robin(KConsts K, FemDev F, SegDev seg, double *__restrict__ f_temp,
+                                                      double *__restrict__ K_temp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F.n_nodes) return;
+    double df, dk;
+    robin_terms(K, F, seg, i, df, dk);
+    f_temp[i] += df;
+    K_temp[F.diag[i]] += dk;
+}
+
+__global__ void __launch_bounds__(kBlock) k_fem_rate(FemDev F, const double *__restrict__ f_temp,
+                                                     const double *__restrict__ K_temp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F.n_nodes) return;
+    double buffer = 0.;
+    for (int t = F.row_ptr[i]; t < F.row_ptr[i + 1]; t++) buffer += K_temp[t] * F.T[F.col_ind[t]];
+    F.k[i] = F.M_inv[i] * (f_temp[i] - buffer);
+}
+
+__global__ void __launch_bounds__(kBlock) k_fem_temp(FemDev F, const double *__restrict__ T_old, double dt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F.n_nodes) return;
+    F.T[i] = dt * F.k[i] + T_old[i];
+}
+
+// tool_FEM.cu:119-139 do_segments_update (flank_retreat == 0 without wear).
+__device__ __forceinline__ void segment_move(const SegDev &seg, int s, const double *vel, double dt) {
+    double2 l = seg.left[s], r = seg.right[s];
+    double dy = __dadd_rn(__dmul_rn(vel[1], dt), 0.);
+    seg.left[s] = make_double2(add_mul_rn(l.x, vel[0], dt), __dadd_rn(l.y, dy));
+    seg.right[s] = make_double2(add_mul_rn(r.x, vel[0], dt), __dadd_rn(r.y, dy));
+    seg.heat_exchange[s] = make_double2(0., 0.);
+    seg.fric_heat[s] = 0.;
+}
+
+// tool_FEM.cu:109-117 do_tool_update_FEM_gpu + the host bookkeeping of
+// tool_update_FEM_gpu (tool_FEM.cu:1555-1559), kept on the device.
+__device__ __forceinline__ void node_move(const FemDev &F, int i, const double *vel, double dt) {
+    double2 p = F.position[i];
+    double dy = __dadd_rn(__dmul_rn(vel[1], dt), 0.);
+    F.position[i] = make_double2(add_mul_rn(p.x, vel[0], dt), __dadd_rn(p.y, dy));
+}
+
+__device__ __forceinline__ void tool_state_move(ToolDev *tool, double dt) {
+    const double vx = tool->vel[0], vy = tool->vel[1];
+    tool->tl_point_ref[0] = add_mul_rn(tool->tl_point_ref[0], vx, dt);
+    tool->tl_point_ref[1] = add_mul_rn(tool->tl_point_ref[1], vy, dt);
+    tool->br_point[0] = add_mul_rn(tool->br_point[0], vx, dt);
+    tool->br_point[1] = add_mul_rn(tool->br_point[1], vy, dt);
+    tool->lowest_point = add_mul_rn(tool->lowest_point, vy, dt);
+    tool->right_point = add_mul_rn(tool->right_point, vx, dt);
+}
+
+// what = 1: segments only; 2: nodes + tool state only; 3: both (fused step).
+__global__ void __launch_bounds__(kBlock) k_tool_move(SegDev seg, FemDev F, ToolDev *tool, double dt, int what) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double vel[2] = {tool->vel[0], tool->vel[1]};
+    if ((what & 1) && i < seg.n) segment_move(seg, i, vel, dt);
+    if ((what & 2) && i < F.n_nodes) node_move(F, i, vel, dt);
+    __syncthreads();
+    if ((what & 2) && i == 0) tool_state_move(tool, dt);
+}
+
+// ---- host launchers ---------------------------------------------------------------------------
+void launch_fem_half(cudaStream_t s, const FemDev &F, double hdt) {
+    k_fem_half<<<div_up(F.n_nodes, kBlock), kBlock, 0, s>>>(F, hdt);
+}
+void launch_fem_rate_update(cudaStream_t s, const KConsts &K, const FemDev &F, const SegDev &seg, double dt) {
+    k_fem_rate_update<<<div_up(F.n_nodes, kBlock), kBlock, 0, s>>>(K, F, seg, dt);
+}
+void launch_fem_reset(cudaStream_t s, const FemDev &F, double *T_old, double *f_temp, double *K_temp) {
+    k_fem_reset<<<div_up(F.nnz > F.n_nodes ? F.nnz : F.n_nodes, kBlock), kBlock, 0, s>>>(F, T_old, f_temp, K_temp);
+}
+void launch_fem_robin(cudaStream_t s, const KConsts &K, const FemDev &F, const SegDev &seg, double *f_temp,
+                      double *K_temp) {
+    k_fem_robin<<<div_up(F.n_nodes, kBlock), kBlock, 0, s>>>(K, F, seg, f_temp, K_temp);
+}
+void launch_fem_rate(cudaStream_t s, const FemDev &F, const double *f_temp, const double *K_temp) {
+    k_fem_rate<<<div_up(F.n_nodes, kBlock), kBlock, 0, s>>>(F, f_temp, K_temp);
+}
+void launch_fem_temp(cudaStream_t s, const FemDev &F, const double *T_old, double dt) {
+    k_fem_temp<<<div_up(F.n_nodes, kBlock), kBlock, 0, s>>>(F, T_old, dt);
+}
+void launch_tool_move(cudaStream_t s, const SegDev &seg, const FemDev &F, ToolDev *tool, double dt, int what) {
+    int n = 0;
+    if (what & 1) n = seg.n;
+    if ((what & 2) && F.n_nodes > n) n = F.n_nodes;
+    if (n < 1) n = 1;
+    k_tool_move<<<div_up(n, kBlock), kBlock, 0, s>>>(seg, F, tool, dt, what);
+}
+
+}  // namespace sphfem

@@ -1,0 +1,376 @@
+// interactions.cu -- neighbour sums of do_interactions_monaghan
+// (interactions_gpu.cu:143-379: velocity gradient, stress divergence with
+// Gray-Monaghan artificial stress, Monaghan artificial viscosity, XSPH and
+// Brookshaw heat conduction) on sm_103a.
+//
+// One thread per particle in sorted order.  Neighbours are visited column by
+// column: the cells (ii, gj-R .. gj+R) of one grid column are consecutive
+// keys, so their particles form one contiguous slot range [offsets[c0],
+// offsets[c1+1]) -- the reference's visiting order (ii outer, jj inner,
+// sorted order inside a cell) without per-cell bookkeeping.
+//
+// Out-of-support candidates are skipped: in the reference they run the full
+// body with W = dW = 0 and add exact zeros (interactions_gpu.cu:230-337), so
+// skipping them changes no sum.  Per-neighbour quotients that depend only on
+// the neighbour ((S-p)/rho^2, mass/rho, sqrtf(K/rho)) come precomputed in the
+// neighbour record; constant factors (mass, -eps*mass, 2*alpha) are applied
+// once after the loop.  These reassociations change results by O(1e-16)
+// relative.
+//
+// Fused mode adds, per particle, the rest of the particle chain up to the
+// return mapping: do_material_stress_rate_jaumann, do_contmech_continuity /
+// _momentum / _advection (actions_gpu.cu:280-314,626-687), correct
+// (leap_frog.cu:71-96), do_material_fric_heat_gen_FEM_v21
+// (actions_gpu.cu:345-420) and do_plasticity_johnson_cook
+// (actions_gpu.cu:689-754).  Correct writes the start-of-step arrays in
+// place (only this thread touches them); neighbours read the predicted state
+// from the records, so there is no read/write race.
+#include "launch.cuh"
+
+namespace sphfem {
+
+struct Sums64 {
+    double vd0, vd1, vd2, vd3;     // v_der
+    double sd0, sd1, sd2, sd3;     // S_der / mass
+    double vt0, vt1;               // vel_t / (-mass)
+    double xt0, xt1;               // pos_t / (eps*mass)
+    double tl;                     // T_lapl / 2
+};
+
+// Kahan-compensated FP32 accumulator.
+struct KahanF {
+    float s, c;
+    __device__ __forceinline__ void add(float v) {
+        float y = v - c;
+        float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
+// ---- per-particle epilogue shared by both precisions (fused mode) ---------------------
+// vd, sd (= S_der), vt (= vel_t from viscosity), xt (= pos_t from XSPH), T_t.
+__device__ __forceinline__ void fused_epilogue(int k, const KConsts &K, const SortedFields &B, const FixedFields &F,
+                                               const SegDev &seg, const ToolDev *__restrict__ tool,
+                                               int32_t *__restrict__ secant_iters, uint32_t *status, bool is_tool,
+                                               double2 vel_pred, double rho_pred, dbl4 vd, dbl4 sd,
+                                               double2 vt, double2 xt, bool thermal, double T_t_new) {
+    const double dt = K.dt;
+    const double mass = K.c.phys.mass;
+    dbl4 S0 = B.S[k];
+    dbl4 St = B.S_t[k];
+    double2 pos_t, vel_t;
+    double rho_t = B.rho_t[k];
+    if (!is_tool) {
+        const double hdt = 0.5 * dt;
+        dbl4 Sp = mk4(S0.x + hdt * St.x, S0.y + hdt * St.y, S0.z + hdt * St.z, S0.w + hdt * St.w);
+        St = jaumann_one(K, vd, Sp);                                  // actions_gpu.cu:280-314
+        rho_t = -rho_pred * (vd.x + vd.w);                            // actions_gpu.cu:626-639
+        double2 fc = B.fc[k], ft = B.ft[k];
+        vel_t.x = vt.x + (((sd.x + sd.y) + fc.x / mass) + ft.x / mass);   // actions_gpu.cu:641-671
+        vel_t.y = vt.y + (((sd.z + sd.w) + fc.y / mass) + ft.y / mass);
+        pos_t.x = xt.x + vel_pred.x;                                  // actions_gpu.cu:673-687
+        pos_t.y = xt.y + vel_pred.y;
+    } else {
+        vel_t = vt;
+        pos_t = xt;
+    }
+    double T_t = thermal ? T_t_new : B.T_t[k];
+    B.pos_t[k] = pos_t;
+    B.vel_t[k] = vel_t;
+    B.S_t[k] = St;
+    B.rho_t[k] = rho_t;
+    B.T_t[k] = T_t;
+    // correct (leap_frog.cu:71-96)
+    double2 pos = B.pos[k], vel = B.vel[k];
+    pos.x = pos.x + dt * pos_t.x;
+    pos.y = pos.y + dt * pos_t.y;
+    vel.x = vel.x + dt * vel_t.x;
+    vel.y = vel.y + dt * vel_t.y;
+    dbl4 S = mk4(S0.x + dt * St.x, S0.y + dt * St.y, S0.z + dt * St.z, S0.w + dt * St.w);
+    double rho = B.rho[k] + dt * rho_t;
+    double T = B.T[k] + dt * T_t;
+    B.pos[k] = pos;
+    B.vel[k] = vel;
+    B.rho[k] = rho;
+    double blanked = 0.;
+    uint32_t st = 0;
+    // friction heat (actions_gpu.cu:345-420), tool runs only
+    if (K.has_tool) st |= fric_heat_one(K, tool->vel, vel, B.ft[k], B.n[k], B.fc[k], rho, B.eps_pl[k], B.on_seg[k],
+                                        seg.n, T, blanked, seg.fric_heat);
+    // return mapping (actions_gpu.cu:689-754)
+    if (K.c.plastic && !is_tool && blanked != 1.) {
+        double eps_pl = B.eps_pl[k], eps_pl_dot = B.eps_pl_dot[k];
+        int it = 0;
+        if (K.precision == SPH_PREC_FP32K)
+            st |= plasticity_one<true>(K, S, F.p[k], rho, eps_pl, eps_pl_dot, T, blanked, &it);
+        else
+            st |= plasticity_one<false>(K, S, F.p[k], rho, eps_pl, eps_pl_dot, T, blanked, &it);
+        B.eps_pl[k] = eps_pl;
+        B.eps_pl_dot[k] = eps_pl_dot;
+        if (secant_iters) secant_iters[k] = it;
+    }
+    B.S[k] = S;
+    B.T[k] = T;
+    if (blanked == 1.) B.blanked[k] = 1.;
+    if (st) set_status(status, st);
+}
+
+// ---- FP64 ---------------------------------------------------------------------------
+template <bool kFused>
+__global__ void __launch_bounds__(kBlock) k_interact64(int N, KConsts K, const int32_t *__restrict__ offsets,
+                                                       const dbl4 *__restrict__ rec, SortedFields B, FixedFields F,
+                                                       SegDev seg, const ToolDev *__restrict__ tool,
+                                                       int32_t *__restrict__ secant_iters, uint32_t *status) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const dbl4 i3 = rec[4 * k + 3];
+    const int fi = (int)__double_as_longlong(i3.w);
+    if (fi & kFlagBlanked) return;
+    const bool tool_i = (fi & kFlagTool) != 0;
+    const dbl4 i0 = rec[4 * k + 0], i1 = rec[4 * k + 1], i2 = rec[4 * k + 2];
+    const double xi = i0.x, yi = i0.y, vix = i0.z, viy = i0.w;
+    const double sAi = i1.x, sBi = i1.y, sCi = i1.z, Rxxi = i1.w;
+    const double Rxyi = i2.x, Ryyi = i2.y, hi = i2.z, rhoi = i2.w;
+    const double ci = i3.x, Ti = i3.z;
+    const double thermal_alpha = (!tool_i) ? K.c.trml_wp.alpha : K.c.trml_tool_sph.alpha;
+    const bool thermal = thermal_alpha != 0.;
+    const double h1 = 1 / hi;
+    const double fourh2 = 4 * hi * hi;
+    const double fac = kPiFac * h1 * h1;
+    const double alpha = K.c.corr.alpha, beta = K.c.corr.beta, eta2 = K.eta2, inv_wdp = K.inv_wdeltap;
+
+    Sums64 a = {};
+    const int hash = B.hash[k];
+    const sph_geom_constants &g = K.g;
+    if (hash >= 0 && hash < g.num_cell) {
+        const int gi = hash / g.ny, gj = hash - gi * g.ny, R = g.stencil;
+        const int lo_i = max(gi - R, 0), hi_i = min(gi + R + 1, g.nx);
+        const int lo_j = max(gj - R, 0), hi_j = min(gj + R + 1, g.ny);
+        for (int ii = lo_i; ii < hi_i; ii++) {
+            const int c0 = ii * g.ny + lo_j, c1 = ii * g.ny + hi_j;   // cells [c0, c1)
+            const int j0 = __ldg(offsets + c0), j1 = __ldg(offsets + c1);
+            for (int j = j0; j < j1; j++) {
+                const dbl4 n0 = rec[4 * j + 0];
+                const double dx = xi - n0.x, dy = yi - n0.y;
+                const double rr2 = dx * dx + dy * dy;
+                if (rr2 >= fourh2 || rr2 < 1e-8) continue;
+                const dbl4 n3 = rec[4 * j + 3];
+                const int fj = (int)__double_as_longlong(n3.w);
+                if (fj & kFlagBlanked) continue;
+                // cubic spline (kernels.cuh:25-65)
+                const double rad = sqrtf_d(rr2);
+                const double q = rad * h1;
+                double val, der;
+                if (q > 1) {
+                    const double t = 2 - q, t2 = t * t;
+                    val = 0.25 * t2 * t2 * t2;
+                    der = -0.75 * t2 * h1 / rad;
+                } else {
+                    val = 1 - 1.5 * q * q * (1 - 0.5 * q);
+                    der = -3.0 * q * (1 - 0.75 * q) * h1 / rad;
+                }
+                const double w = val * fac;
+                const double dwf = der * fac;
+                const double wx = dwf * dx, wy = dwf * dy;
+                const double volj = n3.y;
+                if (!tool_i && !(fj & kFlagTool)) {
+                    const dbl4 n1 = rec[4 * j + 1];
+                    const dbl4 n2 = rec[4 * j + 2];
+                    const double dvx = n0.z - vix, dvy = n0.w - viy;
+                    const double tx = wx * volj, ty = wy * volj;
+                    a.vd0 += dvx * tx;
+                    a.vd1 += dvx * ty;
+                    a.vd2 += dvy * tx;
+                    a.vd3 += dvy * ty;
+                    double fab = w * inv_wdp;
+                    fab *= fab;
+                    fab *= fab;
+                    const double ax = (sAi + n1.x) + fab * (Rxxi + n1.w);
+                    const double ay = (sBi + n1.y) + fab * (Rxyi + n2.x);
+                    const double az = (sCi + n1.z) + fab * (Ryyi + n2.y);
+                    a.sd0 += ax * wx;
+                    a.sd1 += ay * wy;
+                    a.sd2 += ay * wx;
+                    a.sd3 += az * wy;
+                    const double vijposij = -(dvx * dx + dvy * dy);
+                    const double irho = 1. / (0.5 * (rhoi + n2.w));
+                    if (vijposij < 0.) {
+                        const double cij = 0.5 * (ci + n3.x);
+                        const double hij = 0.5 * (hi + n2.z);
+                        const double muij = (hij * vijposij) / (rr2 + eta2 * hij * hij);
+                        const double piij = (-alpha * cij * muij + beta * muij * muij) * irho;
+                        a.vt0 += piij * wx;
+                        a.vt1 += piij * wy;
+                    }
+                    const double wr = w * irho;
+                    a.xt0 += wr * dvx;
+                    a.xt1 += wr * dvy;
+                }
+                if (thermal) a.tl += volj * (Ti - n3.z) * dwf;   // Brookshaw, (e.dW)/r == dW/dr
+            }
+        }
+    }
+    const double mass = K.c.phys.mass;
+    const dbl4 vd = mk4(a.vd0, a.vd1, a.vd2, a.vd3);
+    const dbl4 sd = mk4(mass * a.sd0, mass * a.sd1, mass * a.sd2, mass * a.sd3);
+    const double2 vt = make_double2(-mass * a.vt0, -mass * a.vt1);
+    const double xs = K.c.corr.xspheps * mass;
+    const double2 xt = make_double2(xs * a.xt0, xs * a.xt1);
+    const double T_t = thermal_alpha * (2.0 * a.tl);
+    if (!kFused) {
+        F.S_der[k] = sd;
+        F.v_der[k] = vd;
+        B.pos_t[k] = xt;
+        B.vel_t[k] = vt;
+        if (thermal) B.T_t[k] = T_t;
+    } else {
+        fused_epilogue(k, K, B, F, seg, tool, secant_iters, status, tool_i, make_double2(vix, viy), rhoi, vd, sd, vt,
+                       xt, thermal, T_t);
+    }
+}
+
+// ---- FP32 with Kahan-compensated sums --------------------------------------------------
+template <bool kFused>
+__global__ void __launch_bounds__(kBlock) k_interact32(int N, KConsts K, const int32_t *__restrict__ offsets,
+                                                       const float4 *__restrict__ rec, SortedFields B, FixedFields F,
+                                                       SegDev seg, const ToolDev *__restrict__ tool,
+                                                       int32_t *__restrict__ secant_iters, uint32_t *status) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const float4 i0 = rec[4 * k + 0];
+    const int fi = __float_as_int(i0.z);
+    if (fi & kFlagBlanked) return;
+    const bool tool_i = (fi & kFlagTool) != 0;
+    const float4 i1 = rec[4 * k + 1], i2 = rec[4 * k + 2], i3 = rec[4 * k + 3];
+    const float xri = i0.x, yri = i0.y, hi = i0.w;
+    const float vix = i1.x, viy = i1.y, rhoi = i1.z, ci = i1.w;
+    const float sAi = i2.x, sBi = i2.y, sCi = i2.z;
+    const float Rxxi = i3.x, Rxyi = i3.y, Ryyi = i3.z, Ti = i3.w;
+    const double thermal_alpha = (!tool_i) ? K.c.trml_wp.alpha : K.c.trml_tool_sph.alpha;
+    const bool thermal = thermal_alpha != 0.;
+    const float h1 = 1.f / hi;
+    const float fourh2 = 4.f * hi * hi;
+    const float fac = (float)kPiFac * h1 * h1;
+    const float alpha = (float)K.c.corr.alpha, beta = (float)K.c.corr.beta, eta2 = (float)K.eta2;
+    const float inv_wdp = (float)K.inv_wdeltap;
+    const float cell = (float)K.g.dx;
+
+    KahanF vd0 = {}, vd1 = {}, vd2 = {}, vd3 = {}, sd0 = {}, sd1 = {}, sd2 = {}, sd3 = {};
+    KahanF vt0 = {}, vt1 = {}, xt0 = {}, xt1 = {}, tl = {};
+    const int hash = B.hash[k];
+    const sph_geom_constants &g = K.g;
+    if (hash >= 0 && hash < g.num_cell) {
+        const int gi = hash / g.ny, gj = hash - gi * g.ny, R = g.stencil;
+        const int lo_i = max(gi - R, 0), hi_i = min(gi + R + 1, g.nx);
+        const int lo_j = max(gj - R, 0), hi_j = min(gj + R + 1, g.ny);
+        for (int ii = lo_i; ii < hi_i; ii++) {
+            const int c0 = ii * g.ny + lo_j, c1 = ii * g.ny + hi_j;
+            const int j0 = __ldg(offsets + c0), j1 = __ldg(offsets + c1);
+            const float dxc = (float)(gi - ii) * cell;
+            for (int j = j0; j < j1; j++) {
+                const float4 n0 = rec[4 * j + 0];
+                const int fj = __float_as_int(n0.z);
+                const float dyc = (float)(gj - (fj & kRowMask)) * cell;
+                const float dx = dxc + (xri - n0.x), dy = dyc + (yri - n0.y);
+                const float rr2 = dx * dx + dy * dy;
+                if (rr2 >= fourh2 || rr2 < 1e-8f) continue;
+                if (fj & kFlagBlanked) continue;
+                const float rad = sqrtf(rr2);
+                const float q = rad * h1;
+                float val, der;
+                if (q > 1.f) {
+                    const float t = 2.f - q, t2 = t * t;
+                    val = 0.25f * t2 * t2 * t2;
+                    der = -0.75f * t2 * h1 / rad;
+                } else {
+                    val = 1.f - 1.5f * q * q * (1.f - 0.5f * q);
+                    der = -3.0f * q * (1.f - 0.75f * q) * h1 / rad;
+                }
+                const float w = val * fac;
+                const float dwf = der * fac;
+                const float wx = dwf * dx, wy = dwf * dy;
+                const float4 n2 = rec[4 * j + 2];
+                const float volj = n2.w;
+                if (!tool_i && !(fj & kFlagTool)) {
+                    const float4 n1 = rec[4 * j + 1];
+                    const float4 n3 = rec[4 * j + 3];
+                    const float dvx = n1.x - vix, dvy = n1.y - viy;
+                    const float tx = wx * volj, ty = wy * volj;
+                    vd0.add(dvx * tx);
+                    vd1.add(dvx * ty);
+                    vd2.add(dvy * tx);
+                    vd3.add(dvy * ty);
+                    float fab = w * inv_wdp;
+                    fab *= fab;
+                    fab *= fab;
+                    const float ax = (sAi + n2.x) + fab * (Rxxi + n3.x);
+                    const float ay = (sBi + n2.y) + fab * (Rxyi + n3.y);
+                    const float az = (sCi + n2.z) + fab * (Ryyi + n3.z);
+                    sd0.add(ax * wx);
+                    sd1.add(ay * wy);
+                    sd2.add(ay * wx);
+                    sd3.add(az * wy);
+                    const float vijposij = -(dvx * dx + dvy * dy);
+                    const float irho = 1.f / (0.5f * (rhoi + n1.z));
+                    if (vijposij < 0.f) {
+                        const float cij = 0.5f * (ci + n1.w);
+                        const float hij = 0.5f * (hi + n0.w);
+                        const float muij = (hij * vijposij) / (rr2 + eta2 * hij * hij);
+                        const float piij = (-alpha * cij * muij + beta * muij * muij) * irho;
+                        vt0.add(piij * wx);
+                        vt1.add(piij * wy);
+                    }
+                    const float wr = w * irho;
+                    xt0.add(wr * dvx);
+                    xt1.add(wr * dvy);
+                }
+                if (thermal) {
+                    const float4 n3 = rec[4 * j + 3];
+                    tl.add(volj * (Ti - n3.w) * dwf);
+                }
+            }
+        }
+    }
+    const double mass = K.c.phys.mass;
+    const dbl4 vd = mk4(vd0.s, vd1.s, vd2.s, vd3.s);
+    const dbl4 sd = mk4(mass * sd0.s, mass * sd1.s, mass * sd2.s, mass * sd3.s);
+    const double2 vt = make_double2(-mass * vt0.s, -mass * vt1.s);
+    const double xs = K.c.corr.xspheps * mass;
+    const double2 xt = make_double2(xs * xt0.s, xs * xt1.s);
+    const double T_t = thermal_alpha * (2.0 * (double)tl.s);
+    if (!kFused) {
+        F.S_der[k] = sd;
+        F.v_der[k] = vd;
+        B.pos_t[k] = xt;
+        B.vel_t[k] = vt;
+        if (thermal) B.T_t[k] = T_t;
+    } else {
+        // the predicted velocity / density the FP64 path reads from its record
+        const double hdt = 0.5 * K.dt;
+        double2 v0 = B.vel[k], vt_old = B.vel_t[k];
+        double2 vel_pred = make_double2(v0.x + hdt * vt_old.x, v0.y + hdt * vt_old.y);
+        double rho_pred = B.rho[k] + hdt * B.rho_t[k];
+        fused_epilogue(k, K, B, F, seg, tool, secant_iters, status, tool_i, vel_pred, rho_pred, vd, sd, vt, xt,
+                       thermal, T_t);
+    }
+}
+
+void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const SortedFields &B,
+                         const FixedFields &F, const StepScratch &W, const SegDev &seg, const ToolDev *tool,
+                         bool fused) {
+    const int grid = div_up(N, kBlock);
+    if (K.precision == SPH_PREC_FP32K) {
+        if (fused)
+            k_interact32<true><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec32, B, F, seg, tool, W.secant_iters, W.status);
+        else
+            k_interact32<false><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec32, B, F, seg, tool, W.secant_iters, W.status);
+    } else {
+        if (fused)
+            k_interact64<true><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec64, B, F, seg, tool, W.secant_iters, W.status);
+        else
+            k_interact64<false><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec64, B, F, seg, tool, W.secant_iters, W.status);
+    }
+}
+
+}  // namespace sphfem

@@ -1,0 +1,62 @@
+// launch.cuh -- host-side launchers of the device kernels (one stream each).
+#pragma once
+
+#include "common.cuh"
+#include "physics.cuh"
+#include "state.cuh"
+
+namespace sphfem {
+
+// cells.cu
+void launch_hash(cudaStream_t s, int N, const SortedFields &A, sph_geom_constants g);
+void launch_count(cudaStream_t s, int N, const SortedFields &A, const SortScratch &X, sph_geom_constants g,
+                  uint32_t *status, bool with_hash);
+int scan_blocks(int num_cell);
+void launch_sort_rest(cudaStream_t s, int N, const SortScratch &X, sph_geom_constants g, int32_t *perm,
+                      uint32_t *status);
+void launch_gather_plain(cudaStream_t s, int N, const int32_t *perm, const SortedFields &A, const SortedFields &B);
+void launch_gather_fused(cudaStream_t s, int N, const int32_t *perm, const KConsts &K, const SortedFields &A,
+                         const SortedFields &B, const FixedFields &F, const StepScratch &W);
+void launch_build_records(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F,
+                          const StepScratch &W);
+
+// interactions.cu
+void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const SortedFields &B,
+                         const FixedFields &F, const StepScratch &W, const SegDev &seg, const ToolDev *tool,
+                         bool fused);
+
+// actions.cu
+void launch_init(cudaStream_t s, int N, const SortedFields &A, const StepScratch &W);
+void launch_predict_correct(cudaStream_t s, int N, const SortedFields &A, const StepScratch &W, double fdt);
+void launch_eos(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F);
+void launch_artificial_stress(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F);
+void launch_jaumann(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F);
+void launch_continuity(cudaStream_t s, int N, const SortedFields &A, const FixedFields &F);
+void launch_momentum(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F);
+void launch_advection(cudaStream_t s, int N, const SortedFields &A);
+void launch_plasticity(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F,
+                       const StepScratch &W);
+void launch_fric_heat(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
+                      const ToolDev *tool, uint32_t *status);
+void launch_contact(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
+                    const ToolDev *tool, const double *T_nodes, uint32_t *status);
+void launch_bc(cudaStream_t s, int N, const SortedFields &A);
+void launch_bc_thermal(cudaStream_t s, int N, const KConsts &K, const SortedFields &A);
+void launch_invalidate(cudaStream_t s, int N, const SortedFields &A, uint32_t *status);
+void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
+                      const ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
+                      bool next_hash);
+int reduce_blocks();
+void launch_reduce_force_T(cudaStream_t s, int N, const SortedFields &A, double *out);
+
+// fem.cu
+void launch_fem_half(cudaStream_t s, const FemDev &F, double hdt);
+void launch_fem_rate_update(cudaStream_t s, const KConsts &K, const FemDev &F, const SegDev &seg, double dt);
+void launch_fem_reset(cudaStream_t s, const FemDev &F, double *T_old, double *f_temp, double *K_temp);
+void launch_fem_robin(cudaStream_t s, const KConsts &K, const FemDev &F, const SegDev &seg, double *f_temp,
+                      double *K_temp);
+void launch_fem_rate(cudaStream_t s, const FemDev &F, const double *f_temp, const double *K_temp);
+void launch_fem_temp(cudaStream_t s, const FemDev &F, const double *T_old, double dt);
+void launch_tool_move(cudaStream_t s, const SegDev &seg, const FemDev &F, ToolDev *tool, double dt, int what);
+
+}  // namespace sphfem

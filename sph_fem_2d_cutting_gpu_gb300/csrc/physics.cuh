@@ -1,0 +1,318 @@
+// physics.cuh -- per-particle device functions of the SPH workpiece path.
+// Each function cites the reference kernel it restates.  They are shared by
+// the staged kernels (one launch per reference call) and the fused step.
+#pragma once
+
+#include <cfloat>
+
+#include "common.cuh"
+
+namespace sphfem {
+
+// ---- kernels.cuh:25-65 cubic_spline (reference form, FP64) -------------------
+__device__ __forceinline__ void cubic_spline(double xij, double yij, double hi, double &w, double &wx, double &wy) {
+    w = 0.; wx = 0.; wy = 0.;
+    double rr2 = xij * xij + yij * yij;
+    double h1 = 1 / hi;
+    double fourh2 = 4 * hi * hi;
+    if (rr2 >= fourh2 || rr2 < 1e-8) return;
+    double der, val;
+    double rad = sqrtf_d(rr2);
+    double q = rad * h1;
+    double fac = kPiFac * h1 * h1;
+    if (q > 1) {
+        double t = 2 - q;
+        double t2 = t * t;
+        val = 0.25 * t2 * t2 * t2;
+        der = -0.75 * t2 * h1 / rad;
+    } else {
+        val = 1 - 1.5 * q * q * (1 - 0.5 * q);
+        der = -3.0 * q * (1 - 0.75 * q) * h1 / rad;
+    }
+    w = val * fac;
+    wx = der * xij * fac;
+    wy = der * yij * fac;
+}
+
+// ---- plasticity.cuh:21-39 sigma_yield ----------------------------------------
+// Term_C depends only on the temperature, which is constant during one return
+// mapping, so callers may pass it precomputed (identical arithmetic).
+__device__ __forceinline__ double jc_term_c(const sph_joco_constants &jc, double t) {
+    double theta = (t - jc.Tref) / (jc.Tmelt - jc.Tref);
+    if (theta > 1.) theta = 1.;
+    return 1.0 - pow(theta, jc.m);
+}
+
+__device__ __forceinline__ double sigma_yield_tc(const sph_joco_constants &jc, double eps_pl, double eps_pl_dot,
+                                                 double term_c) {
+    double Term_A = jc.A + jc.B * pow(eps_pl, jc.n);
+    double Term_B;
+    double eps_dot = eps_pl_dot / jc.eps_dot_ref;
+    if (eps_dot > 1.0) Term_B = 1.0 + jc.C * log(eps_dot);
+    else Term_B = pow((1.0 + eps_dot), jc.C);
+    return Term_A * Term_B * term_c;
+}
+
+__device__ __forceinline__ double sigma_yield(const sph_joco_constants &jc, double eps_pl, double eps_pl_dot, double t) {
+    return sigma_yield_tc(jc, eps_pl, eps_pl_dot, jc_term_c(jc, t));
+}
+
+// Same flow stress with the rate/strain terms in FP32 (powf/logf).  Used by the
+// FP32-compensated mode, where only the secant residual stays in FP64.
+__device__ __forceinline__ double sigma_yield_tc_f32(const sph_joco_constants &jc, double eps_pl, double eps_pl_dot,
+                                                     double term_c) {
+    float Term_A = (float)jc.A + (float)jc.B * powf((float)eps_pl, (float)jc.n);
+    float Term_B;
+    float eps_dot = (float)(eps_pl_dot / jc.eps_dot_ref);
+    if (eps_dot > 1.0f) Term_B = 1.0f + (float)jc.C * logf(eps_dot);
+    else Term_B = powf(1.0f + eps_dot, (float)jc.C);
+    return (double)(Term_A * Term_B) * term_c;
+}
+
+// ---- plasticity.cuh:117-162 opt_fun + solve_secant ----------------------------
+// Returns delta_lambda; *iters = iterations used, negative when the 100
+// iteration cap was hit (plasticity.cuh:155-158).
+template <bool kF32Yield>
+__device__ __forceinline__ double solve_secant(const sph_joco_constants &jc, double init, double tol,
+                                              double norm_Strial, double eps_pl_init, double term_c, double delta_t,
+                                              double mu, int *iters) {
+    const double s23 = sqrt(2.0 / 3.0);
+    auto opt_fun = [&](double dl) {
+        double eq = eps_pl_init + s23 * fmax(dl, 0.);
+        double eqd = s23 * fmax(dl, 0.) / delta_t;
+        double sY = kF32Yield ? sigma_yield_tc_f32(jc, eq, eqd, term_c) : sigma_yield_tc(jc, eq, eqd, term_c);
+        return norm_Strial - 2 * mu * dl - s23 * sY;
+    };
+    double delta_lambda = init;
+    double delta_lambda_old = delta_lambda;
+    int iter = 0;
+    const int max_iter = 100;
+    while (true) {
+        double g = opt_fun(delta_lambda);
+        double delta_lambda_1 = delta_lambda * 1.01;
+        double g_1 = opt_fun(delta_lambda_1);
+        double slope = (g - g_1) / (delta_lambda - delta_lambda_1);
+        delta_lambda_old = delta_lambda;
+        delta_lambda = delta_lambda - g / slope;
+        if (delta_lambda < 0.) delta_lambda = -0.1 * delta_lambda;
+        if (fabs(delta_lambda - delta_lambda_old) < tol) { *iters = iter + 1; return delta_lambda; }
+        if (iter > max_iter) { *iters = -(iter + 1); return delta_lambda; }
+        iter++;
+    }
+}
+
+// ---- actions_gpu.cu:689-754 do_plasticity_johnson_cook (one particle) --------
+// Reads/writes the particle's S, eps_pl, eps_pl_dot, T, blanked.  Returns
+// status bits.  `iters_out` receives the secant iteration count (0 if elastic).
+template <bool kF32Yield>
+__device__ __forceinline__ uint32_t plasticity_one(const KConsts &K, dbl4 &S, double p, double rho,
+                                                   double &eps_pl, double &eps_pl_dot, double &T, double &blanked,
+                                                   int *iters_out) {
+    const sph_joco_constants &jc = K.c.joco;
+    const double mu = K.c.phys.G;
+    const double dt = K.dt;
+    double Sxx = S.x, Syy = S.z, Szz = S.w, Sxy = S.y;
+    double norm_Strial = sqrtf_d(Sxx * Sxx + Syy * Syy + Szz * Szz + 2. * Sxy * Sxy);
+    double cxx = Sxx - p, cyy = Syy - p, czz = Szz - p, cxy = Sxy;
+    double svm = sqrtf_d((cxx * cxx + cyy * cyy + czz * czz) - cxx * cyy - cxx * czz - cyy * czz + 3.0 * cxy * cxy);
+    double term_c = jc_term_c(jc, T);
+    double sigma_Y = kF32Yield ? sigma_yield_tc_f32(jc, eps_pl, eps_pl_dot, term_c)
+                               : sigma_yield_tc(jc, eps_pl, eps_pl_dot, term_c);
+    *iters_out = 0;
+    if (svm < sigma_Y) {
+        eps_pl_dot = 0.;
+        return 0u;
+    }
+    int it = 0;
+    double delta_lambda = solve_secant<kF32Yield>(jc, fmax(eps_pl_dot * dt * sqrt(2. / 3.), 1e-8), 1e-6, norm_Strial,
+                                                  eps_pl, term_c, dt, mu, &it);
+    uint32_t st = 0;
+    if (it < 0) { st |= SPH_STATUS_SECANT_MAXITER; it = -it; }
+    *iters_out = it;
+    double eps_pl_new = eps_pl + sqrtf_d(2.0 / 3.0) * fmaxf_d(delta_lambda, 0.);
+    double eps_pl_dot_new = sqrtf_d(2.0 / 3.0) * fmaxf_d(delta_lambda, 0.) / dt;
+    double eps_old = eps_pl;
+    eps_pl = eps_pl_new;
+    eps_pl_dot = eps_pl_dot_new;
+    S.x = Sxx - Sxx / norm_Strial * delta_lambda * 2. * mu;
+    S.z = Syy - Syy / norm_Strial * delta_lambda * 2. * mu;
+    S.w = Szz - Szz / norm_Strial * delta_lambda * 2. * mu;
+    S.y = Sxy - Sxy / norm_Strial * delta_lambda * 2. * mu;
+    if (K.c.trml_wp.tq != 0.) {
+        double delta_eps_pl = eps_pl_new - eps_old;
+        double sY = kF32Yield ? sigma_yield_tc_f32(jc, eps_pl_new, eps_pl_dot_new, term_c)
+                              : sigma_yield_tc(jc, eps_pl_new, eps_pl_dot_new, term_c);
+        T += K.c.trml_wp.tq / (K.c.trml_wp.cp * rho) * delta_eps_pl * sY;
+    }
+    if (T > jc.Tmelt) {
+        T = jc.Tmelt;
+        blanked = 1.;
+        st |= SPH_STATUS_MELT_BLANKED;
+    }
+    return st;
+}
+
+// ---- actions_gpu.cu:345-420 do_material_fric_heat_gen_FEM_v21 (one particle) --
+// WEAR_NODE_SHIFT statistics are not part of the path.  Returns status bits.
+// A segment id outside [0, n_seg) (the reference only ever stores -1 or a
+// valid id) is treated like -1, so caller-uploaded data cannot index out of range.
+__device__ __forceinline__ uint32_t fric_heat_one(const KConsts &K, const double *vel_tool, double2 vel, double2 ft,
+                                                  double2 nrm, double2 fc, double rho, double eps_pl, int seg,
+                                                  int n_seg, double &T, double &blanked,
+                                                  double *__restrict__ fric_heat) {
+    (void)fc; (void)rho;
+    if (blanked == 1.) return 0u;
+    if (eps_pl > 20.) return 0u;
+    double f_fric_mag = sqrtf_d(ft.x * ft.x + ft.y * ft.y);
+    if (seg < 0 || seg >= n_seg) return 0u;
+    const double partition_wp = K.c.tool.beta;
+    double vdx = vel.x - vel_tool[0], vdy = vel.y - vel_tool[1];
+    double vdn = vdx * nrm.x + vdy * nrm.y;
+    double vrx = vdx - vdn * nrm.x, vry = vdy - vdn * nrm.y;
+    double v_rel_mag = sqrtf_d(vrx * vrx + vry * vry);
+    double value = K.c.tool.eta * f_fric_mag * v_rel_mag;
+    if (isnan(v_rel_mag)) {
+        blanked = 1.;
+        return SPH_STATUS_FRIC_NAN;
+    }
+    if (v_rel_mag > 0.03) return 0u;
+    double T_buffer = T + value * (1 - partition_wp) * K.dt / K.c.trml_wp.cp / K.c.phys.mass;
+    if (T_buffer > 1550.) {
+        T = 1550.;
+    } else {
+        T = T_buffer;
+        atomicAdd(fric_heat + seg, value * partition_wp);
+    }
+    return 0u;
+}
+
+// ---- actions_gpu.cu:222-232 do_material_eos ----------------------------------
+__device__ __forceinline__ double eos_one(const KConsts &K, double rho) {
+    double c0 = sqrtf_d(K.c.phys.K / K.c.phys.rho0);
+    return c0 * c0 * (rho - K.c.phys.rho0);
+}
+
+// ---- actions_gpu.cu:234-278 do_corrector_artificial_stress (+ stress_angle :45-49)
+__device__ __forceinline__ dbl4 artificial_stress_one(const KConsts &K, double rho, double p, dbl4 S) {
+    double eps = K.c.corr.stresseps;
+    double sxx = S.x - p, sxy = S.y, syy = S.z - p;
+    double rhoi21 = 1. / (rho * rho);
+    double numer = 2. * sxy;
+    double denom = sxx - syy + 0.;
+    double theta = 0.5 * (double)sph_atan2f((float)numer, (float)denom);
+    double cos_theta = (double)sph_cosf((float)theta);
+    double sin_theta = (double)sph_sinf((float)theta);
+    double cos_theta2 = cos_theta * cos_theta;
+    double sin_theta2 = sin_theta * sin_theta;
+    double rot_sxx = cos_theta2 * sxx + 2.0 * cos_theta * sin_theta * sxy + sin_theta2 * syy;
+    double rot_syy = sin_theta2 * sxx - 2.0 * cos_theta * sin_theta * sxy + cos_theta2 * syy;
+    double rot_rxx = 0., rot_ryy = 0.;
+    if (rot_sxx > 0) rot_rxx = -eps * rot_sxx * rhoi21;
+    if (rot_syy > 0) rot_ryy = -eps * rot_syy * rhoi21;
+    return mk4(cos_theta2 * rot_rxx + sin_theta2 * rot_ryy, cos_theta * sin_theta * (rot_rxx - rot_ryy),
+                        sin_theta2 * rot_rxx + cos_theta2 * rot_ryy, 0.);
+}
+
+// ---- actions_gpu.cu:280-314 do_material_stress_rate_jaumann -------------------
+// S_t = 2G (epsdot - tr/3 I) + Omega S + S Omega^T (Belytschko 3.7.9); the GLM
+// column-major products reduce to these element formulas.
+__device__ __forceinline__ dbl4 jaumann_one(const KConsts &K, dbl4 vd, dbl4 S) {
+    double G = K.c.phys.G;
+    double vx_x = vd.x, vx_y = vd.y, vy_x = vd.z, vy_y = vd.w;
+    double e01 = 0.5 * (vx_y + vy_x);
+    double om10 = 0.5 * (vx_y - vy_x);
+    double om01 = 0.5 * (vy_x - vx_y);
+    double tr = vx_x + vy_y + 0.;
+    double s = (1. / 3.) * tr;
+    double twoG = 2. * G;
+    dbl4 r;
+    r.x = (twoG * (vx_x - s) + om10 * S.y) + S.y * om10;
+    r.y = (twoG * (e01 - 0.) + om01 * S.x) + S.z * om10;
+    r.z = (twoG * (vy_y - s) + om01 * S.y) + S.y * om01;
+    r.w = (twoG * (0. - s) + 0.) + 0.;
+    return r;
+}
+
+// ---- actions_gpu.cu:33-43 find_max / find_min -----------------------------------
+__device__ __forceinline__ double find_max(double a, double b) { return (a >= b) ? a : b; }
+__device__ __forceinline__ double find_min(double a, double b) { return (a >= b) ? b : a; }
+
+// ---- actions_gpu.cu:51-63 on_segment_mesh -----------------------------------------
+__device__ __forceinline__ int on_segment_mesh(double2 left, double2 right, double2 point) {
+    if (point.y <= fmaxf_d(left.y, right.y) && point.y >= fminf_d(left.y, right.y)) {
+        if (left.x == right.x && point.x < left.x) return 1;
+        if (fabs(left.y - right.y) != 0) {
+            double x_on_seg = right.x + (left.x - right.x) / (left.y - right.y) * (point.y - right.y);
+            if (x_on_seg > point.x && x_on_seg != left.x) return 1;
+        } else {
+            if (point.x <= fmax(left.x, right.x)) return 1;
+        }
+    }
+    return 0;
+}
+
+// ---- actions_gpu.cu:83-93 inside_judgement (ray casting towards +x) ------------
+__device__ __forceinline__ int inside_judgement(double2 qp, const double2 *__restrict__ left,
+                                                const double2 *__restrict__ right, int num_seg) {
+    int intersections = 0;
+    for (int i = 0; i < num_seg; i++) intersections += on_segment_mesh(__ldg(left + i), __ldg(right + i), qp);
+    return (intersections % 2 == 0) ? 0 : 1;
+}
+
+// ---- actions_gpu.cu:139-220 find_shortest_distance_v1 ------------------------------
+__device__ __forceinline__ int find_shortest_distance_v1(double2 qp, double &dN, double2 &n_re,
+                                                         const double2 *__restrict__ left,
+                                                         const double2 *__restrict__ right,
+                                                         const double2 *__restrict__ n, int num_seg) {
+    int seg = -1;
+    double depth = FLT_MAX;
+    const double limit_value = 2.5e-4;
+    for (int i = 0; i < num_seg; i++) {
+        double2 L = __ldg(left + i), Rr = __ldg(right + i);
+        double ymax = find_max(L.y, Rr.y), ymin = find_min(L.y, Rr.y);
+        double xmax = find_max(L.x, Rr.x), xmin = find_min(L.x, Rr.x);
+        if (qp.x > xmin - 0.0008 && qp.x < xmax + 0.0008 && qp.y > ymin - 0.0008 && qp.y < ymax + 0.0008) {
+            double2 ni = __ldg(n + i);
+            double d = (qp.x - L.x) * ni.x + (qp.y - L.y) * ni.y;
+            if (d >= 0. && d < depth) {
+                double intersec_x = qp.x - d * ni.x;
+                double intersec_y = qp.y - d * ni.y;
+                if (intersec_y <= ymax && intersec_y >= ymin && intersec_x <= xmax && intersec_x >= xmin) {
+                    depth = d;
+                    seg = i;
+                }
+            }
+        }
+    }
+    if (seg != -1 && depth <= limit_value) {
+        double2 ns = __ldg(n + seg);
+        n_re = make_double2(-ns.x, -ns.y);
+        dN = -depth;
+    } else {
+        depth = FLT_MAX;
+        for (int i = 0; i < num_seg; i++) {
+            double2 Rr = __ldg(right + i);
+            double d_trial = sqrtf_d((qp.x - Rr.x) * (qp.x - Rr.x) + (qp.y - Rr.y) * (qp.y - Rr.y));
+            if (d_trial < depth) { depth = d_trial; seg = i; }
+        }
+        if (seg == -1) return seg;
+        double2 ns = __ldg(n + seg);
+        double2 rs = __ldg(right + seg);
+        double nsx = ns.x, nsy = ns.y;
+        for (int j = 0; j < num_seg; j++) {
+            double2 Lj = __ldg(left + j);
+            if (Lj.y == rs.y && Lj.x == rs.x) {
+                double2 nj = __ldg(n + j);
+                nsx = (nj.x + ns.x) / 2.;
+                nsy = (nj.y + ns.y) / 2.;
+                break;
+            }
+        }
+        double n_length = sqrtf_d(nsx * nsx + nsy * nsy);
+        n_re = make_double2(-nsx / n_length, -nsy / n_length);
+        dN = -1.0 * depth;
+    }
+    return seg;
+}
+
+}  // namespace sphfem

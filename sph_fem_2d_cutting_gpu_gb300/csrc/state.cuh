@@ -1,0 +1,80 @@
+// state.cuh -- device-side layout of the particle state and step scratch.
+#pragma once
+
+#include "common.cuh"
+
+namespace sphfem {
+
+// The 20 fields reordered by the Green sort (grid_gpu_green.cu:55-113) plus
+// the sort keys; two copies, swapped after each sort like the reference.
+struct SortedFields {
+    double2 *pos, *vel, *fc, *ft, *n;
+    double *h, *rho, *eps_pl, *eps_pl_dot, *T, *fixed, *blanked, *tool_particle;
+    dbl4 *S;
+    double2 *pos_t, *vel_t;
+    double *rho_t, *T_t;
+    dbl4 *S_t;
+    int32_t *on_seg;
+    int32_t *hash;
+};
+
+// Arrays that are not reordered by the sort (particle_gpu fields the Green
+// buffer does not carry: p, R, S_der, v_der, idx).
+struct FixedFields {
+    double *p;
+    dbl4 *R;
+    dbl4 *S_der, *v_der;
+    int32_t *idx;
+};
+
+// Scratch of the counting sort.
+struct SortScratch {
+    int32_t *key;        // [N] sort key of each particle (hash, or num_cell when out of range)
+    int32_t *arrival;    // [N] arrival slot inside its cell (atomic counter value)
+    int32_t *counts;     // [num_cell+1] particles per cell (last = out-of-grid bucket)
+    int32_t *offsets;    // [num_cell+2] exclusive scan of counts
+    int32_t *slots;      // [N] particle ids grouped by cell, arbitrary order inside a cell
+    int32_t *block_sums; // scan partials
+    int32_t *cell_start, *cell_end;   // grid_gpu_green m_cell_start / m_cell_end
+};
+
+// Packed neighbour record: what a neighbour contributes to the pair sums.
+// FP64: 16 doubles = 128 B; FP32K: 16 floats = 64 B (positions as offsets
+// from the particle's cell corner; the last word packs the cell row and flags).
+constexpr int kRecWords = 16;
+enum : int { kFlagBlanked = 1 << 30, kFlagTool = 1 << 29, kRowMask = (1 << 29) - 1 };
+
+// Interface segments (segment_FEM_gpu, segment_FEM_gpu.h:31-56).
+struct SegDev {
+    int n;
+    double2 *left, *right, *normal;
+    int4 *marks;              // element, colour, node left, node right
+    double2 *heat_exchange;   // (sum T*length, sum length)
+    double *fric_heat;
+};
+
+// FEM thermal system of the tool (FEM_thermal_2D_GPU, FEM_thermal_gpu.h:35-93).
+// K, f are the assembled (post-Dirichlet) m_stiffness_matrix / m_f; the Robin
+// terms of apply_robin_bdc are added on the fly from the segments touching a
+// node (node_seg_ptr / node_seg), so no K_temp/f_temp copy is made per step.
+struct FemDev {
+    int n_nodes, nnz;
+    double2 *position;
+    int32_t *row_ptr, *col_ind, *diag;   // diag[i] = CSR slot of (i,i)
+    double *K, *M_inv, *f, *T, *k;
+    double *T_half;                      // T after calculate_temp(0.5 dt)
+    int32_t *node_seg_ptr, *node_seg;    // segments whose left/right node is this node
+};
+
+struct StepScratch {
+    dbl4 *rec64;      // [N][4] FP64 records
+    float4 *rec32;       // [N][4] FP32 records
+    double2 *pos_init, *vel_init;   // leap_frog snapshots (staged path)
+    dbl4 *S_init;
+    double *rho_init, *T_init;
+    int32_t *secant_iters;          // [N] secant iterations of the last JC pass (0 = elastic)
+    uint32_t *status;               // device status word
+    double *reduce;                 // reduction scratch
+};
+
+}  // namespace sphfem

@@ -1,0 +1,215 @@
+"""Scenario set-ups in the reference's unit system (cm, g, microsecond; stress
+in Mbar = 100 GPa; temperature in K), following the template of
+setup_ref_cut_FEM_tool_no_wear_thermal_paper (benchmarks_NZ.cpp:51-367).
+
+Workloads:
+  * ``ti64_cut``     -- Ti6Al4V orthogonal cut, 200 x 60 particles, dx = 5 um,
+                        tool mesh of about 2,000 nodes (rake 0, clearance 7 deg,
+                        edge radius 5 um), 70 m/min, uncut chip thickness 80 um.
+  * ``micro``        -- 2048 x 2048 jittered lattice with dx = 2.5 um, random
+                        velocity / stress / density, no tool.
+  * ``aisi1045_cut`` -- AISI 1045 cut, 1600 x 400 particles, dx = 2.5 um, tool
+                        mesh of about 20,000 nodes (rake -6, clearance 5 deg,
+                        edge radius 20 um), 120 m/min, 100 um.
+Unit conversions: 1 m/s = 1e-4 cm/us; 1 MPa = 1e-5 Mbar; 1 J/(kg K) = 1e-8
+(g cm^2/us^2)/(g K); 1 W/(m K) = 1e-13 bomb units.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+from .tool_mesh import mesh_tool
+
+MPMIN_TO_CMUS = 1.0 / 60.0 * 1e-4      # m/min -> cm/us
+
+
+def wdeltap(hdx: float, dx: float) -> float:
+    """Cubic-spline value at one particle spacing (benchmarks_NZ.cpp:131-136)."""
+    h1 = 1.0 / (hdx * dx)
+    q = dx * h1
+    fac = 10 * (1.0 / math.pi) / 7.0 * h1 * h1
+    return fac * (1 - 1.5 * q * q * (1 - 0.5 * q))
+
+
+@dataclass
+class Material:
+    E: float
+    nu: float
+    rho0: float
+    A: float
+    B: float
+    C: float
+    n: float
+    m: float
+    Tmelt: float
+    Tref: float = 300.0
+    eps_dot_ref: float = 1e-6
+    cp: float = 0.0
+    k: float = 0.0
+    tq: float = 0.9
+    eta: float = 0.9
+
+
+TI64 = Material(E=1.138, nu=0.342, rho0=4.43, A=0.00862, B=0.00331, C=0.012, n=0.34, m=0.8, Tmelt=1836.0,
+                cp=526e-8, k=6.8e-13)
+# AISI 1045: Johnson-Cook from the workload description; thermal data (not in
+# the reference) cp = 486 J/(kg K), k = 49.8 W/(m K).
+AISI1045 = Material(E=2.0, nu=0.3, rho0=7.85, A=0.005531, B=0.006008, C=0.0134, n=0.234, m=1.0, Tmelt=1733.0,
+                    cp=486e-8, k=49.8e-13)
+
+
+def make_constants(mat: Material, dx: float, hdx: float, mu: float = 0.35, plastic: bool = True,
+                   thermal: bool = True) -> abi.Constants:
+    c = abi.Constants()
+    G = mat.E / (2.0 * (1.0 + mat.nu))
+    c.phys.E, c.phys.nu, c.phys.rho0 = mat.E, mat.nu, mat.rho0
+    c.phys.G = G
+    c.phys.K = 2.0 * G * (1 + mat.nu) / (3 * (1 - 2 * mat.nu))
+    c.phys.mass = dx * dx * mat.rho0
+    rho_tool = 15.25
+    c.phys.mass_tool = dx * dx * rho_tool
+    c.joco.A, c.joco.B, c.joco.C, c.joco.n, c.joco.m = mat.A, mat.B, mat.C, mat.n, mat.m
+    c.joco.Tmelt, c.joco.Tref, c.joco.eps_dot_ref = mat.Tmelt, mat.Tref, mat.eps_dot_ref
+    if thermal:
+        c.trml_wp.cp, c.trml_wp.tq, c.trml_wp.k = mat.cp, mat.tq, mat.k
+        c.trml_wp.alpha = mat.k / (mat.rho0 * mat.cp)
+        c.trml_wp.eta, c.trml_wp.T_init = mat.eta, mat.Tref
+        # tool thermal constants of the reference set-up (benchmarks_NZ.cpp:118-122)
+        c.trml_tool.cp, c.trml_tool.k = 15e-8, 59e-13
+        c.trml_tool.alpha = c.trml_tool.k / (rho_tool * c.trml_tool.cp)
+        c.trml_tool.T_init = mat.Tref
+    c.corr.alpha, c.corr.beta, c.corr.eta = 1.0, 1.0, 0.1
+    c.corr.xspheps, c.corr.stresseps = 0.5, 0.3
+    c.corr.wdeltap = wdeltap(hdx, dx)
+    # tool constants (benchmarks_NZ.cpp:194-205)
+    t = c.tool
+    t.cp, t.tq, t.k, t.eta, t.rho, t.T0 = 292e-8, 0.9, 88e-13, 1.0, 15.25, mat.Tref
+    t.h, t.beta, t.mu, t.contact_alpha, t.slave_mass = 2e-10, 0.5, mu, 0.02, c.phys.mass
+    c.plastic = 1 if plastic else 0
+    return c
+
+
+@dataclass
+class Case:
+    name: str
+    constants: abi.Constants
+    grid: abi.GridParams
+    particles: dict            # numpy arrays by sph_particles field name
+    N: int
+    dt: float
+    tool_mesh: dict | None = None
+    tool_speed: float = 0.0
+    feed: float = 0.0
+    steps: int = 0
+    info: dict = field(default_factory=dict)
+
+    def tool_struct(self):
+        if self.tool_mesh is None:
+            return None, []
+        m = self.tool_mesh
+        keep = [m["nodes"], m["elements"], m["cutting_flags"], m["fixed_flags"]]
+        s = abi.ToolMesh()
+        s.n_nodes = len(m["nodes"])
+        s.n_elements = len(m["elements"])
+        s.nodes = abi.ptr(m["nodes"])
+        s.elements = abi.ptr(m["elements"])
+        s.cutting_flags = abi.ptr(m["cutting_flags"])
+        s.fixed_flags = abi.ptr(m["fixed_flags"])
+        s.T_init = None
+        s.tl[0], s.tl[1] = float(m["tl"][0]), float(m["tl"][1])
+        return s, keep
+
+
+def grid_params(bbmin, bbmax, h, cell_factor=1, stencil=2) -> abi.GridParams:
+    g = abi.GridParams()
+    g.bbmin[0], g.bbmin[1] = bbmin
+    g.bbmax[0], g.bbmax[1] = bbmax
+    g.h = h
+    g.cell_factor = cell_factor
+    g.stencil = stencil
+    return g
+
+
+def micro(n_side: int = 2048, dx: float = 2.5e-4, hdx: float = 1.7, seed: int = 0, cell_factor: int = 1,
+          stencil: int = 2) -> Case:
+    """Interaction micro-benchmark: jittered n_side x n_side lattice, no tool."""
+    rng = np.random.default_rng(seed)
+    N = n_side * n_side
+    P = abi.empty_particles(N)
+    i, j = np.meshgrid(np.arange(n_side), np.arange(n_side), indexing="ij")
+    pos = np.stack([i.ravel() * dx, j.ravel() * dx], 1)
+    pos += rng.uniform(-0.05 * dx, 0.05 * dx, size=pos.shape)
+    P["pos"][:] = pos
+    P["vel"][:] = rng.normal(0.0, 1e-4, size=(N, 2))             # N(0, 1 m/s)
+    sxx, sxy, syy, szz = (rng.normal(0.0, 0.002, size=N) for _ in range(4))   # N(0, 200 MPa)
+    P["S"][:] = np.stack([sxx, sxy, syy, szz], 1)
+    mat = AISI1045
+    P["rho"][:] = mat.rho0 * (1.0 + rng.uniform(-1e-3, 1e-3, size=N))
+    P["h"][:] = hdx * dx
+    P["T"][:] = 300.0
+    P["on_seg"][:] = -1
+    c = make_constants(mat, dx, hdx)
+    h = hdx * dx
+    lo = pos.min(0) - 1e-8
+    hi = pos.max(0) + 1e-8
+    # margin of two smoothing lengths so the one step stays inside the grid
+    g = grid_params((lo[0] - 2 * h, lo[1] - 2 * h), (hi[0] + 2 * h, hi[1] + 2 * h), h, cell_factor, stencil)
+    dt = 0.3 * hdx * dx / (math.sqrt(c.phys.K / c.phys.rho0))
+    return Case("micro", c, g, P, N, dt, info=dict(n_side=n_side, dx=dx, hdx=hdx, seed=seed))
+
+
+def cutting(name: str, mat: Material, nx: int, ny: int, dx: float, hdx: float, speed_mpmin: float, feed: float,
+            rake: float, clearance: float, r: float, mu: float, s_min: float, s_max: float, tool_size: float,
+            cfl: float = 0.3, steps: int = 0, cell_factor: int = 1, stencil: int = 2) -> Case:
+    """Orthogonal cut following benchmarks_NZ.cpp:51-367 (lattice, fixed
+    boundaries, tool placement at the target feed, locked grid, CFL step)."""
+    lo_x, lo_y = 0.005, 0.0
+    hi_y = lo_y + (ny - 1) * dx
+    N = nx * ny
+    i, j = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    pos = np.stack([i.ravel() * dx + lo_x, j.ravel() * dx + lo_y], 1)
+    min_x, min_y = pos.min(0)
+    max_x, max_y = pos.max(0)
+    P = abi.empty_particles(N)
+    P["pos"][:] = pos
+    P["rho"][:] = mat.rho0
+    P["h"][:] = hdx * dx
+    P["T"][:] = mat.Tref
+    fixed = (pos[:, 1] < min_y + 0.5 * dx)
+    fixed |= (pos[:, 0] < min_x + dx / 2) & (pos[:, 1] < min_y + 0.5 * (hi_y - lo_y))
+    fixed |= pos[:, 0] > max_x - dx
+    P["fixed"][:] = fixed.astype(np.float64)
+    P["on_seg"][:] = 0
+    c = make_constants(mat, dx, hdx, mu=mu)
+    vel_tool = speed_mpmin * MPMIN_TO_CMUS
+    tl = (-tool_size, hi_y + 0.5 * tool_size)
+    mesh = mesh_tool(tl, tool_size, tool_size, rake, clearance, r, s_min=s_min, s_max=s_max)
+    bbmin = pos.min(0) - 1e-8
+    bbmax = pos.max(0) + 1e-8 + np.array([300 * dx, 500 * dx])
+    bbmax[1] = max(bbmax[1], hi_y + (max_x + dx) - lo_x)
+    g = grid_params(tuple(bbmin), tuple(bbmax), hdx * dx, cell_factor, stencil)
+    dt = cfl * hdx * dx / (math.sqrt(c.phys.K / c.phys.rho0) + math.sqrt(vel_tool))   # benchmarks_NZ.cpp:360
+    case = Case(name, c, g, P, N, dt, tool_mesh=mesh, tool_speed=vel_tool, feed=feed, steps=steps,
+                info=dict(nx=nx, ny=ny, dx=dx, hdx=hdx, lo_x=lo_x, hi_y=hi_y, rake=rake, clearance=clearance, r=r,
+                          nodes=len(mesh["nodes"]), elements=len(mesh["elements"])))
+    return case
+
+
+def ti64_cut(steps: int = 2000, **kw) -> Case:
+    return cutting("ti64_cut", TI64, 200, 60, 5e-4, 1.7, 70.0, 0.008, 0.0, 7.0, 5e-4, 0.35,
+                   s_min=1.0e-4, s_max=3.0e-3, tool_size=0.06, steps=steps, **kw)
+
+
+def aisi1045_cut(steps: int = 20000, **kw) -> Case:
+    return cutting("aisi1045_cut", AISI1045, 1600, 400, 2.5e-4, 1.7, 120.0, 0.01, -6.0, 5.0, 2e-3, 0.35,
+                   s_min=7e-5, s_max=2.5e-3, tool_size=0.2, steps=steps, **kw)
+
+
+def small_cut(nx: int = 40, ny: int = 16, steps: int = 20, **kw) -> Case:
+    """A few hundred particles and a coarse tool: sizes the CPU oracle finishes in seconds."""
+    return cutting("small_cut", TI64, nx, ny, 5e-4, 1.7, 300.0, 0.002, 0.0, 7.0, 5e-4, 0.35,
+                   s_min=2e-4, s_max=2.5e-3, tool_size=0.015, steps=steps, **kw)

@@ -1,0 +1,200 @@
+"""Python host mirror of the reference's step interface over the C ABI.
+
+``Solver`` owns one ``sph_ctx``.  Its methods carry the names of the calls
+that ``leap_frog::step`` makes (leap_frog.cu:162-248) and raise ``SphError``
+on any non-zero status, so host code (and the parity tests) read like the
+reference's call sequence.  All compute runs in the sm_103a library; there is
+no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .setups import Case
+
+
+class SphError(RuntimeError):
+    pass
+
+
+class Solver:
+    def __init__(self, case: Case, precision: int = abi.SPH_PREC_FP64, device: int = 0, place_tool: bool = True):
+        self.lib = abi.load()
+        self.case = case
+        self.N = case.N
+        self._keep = []
+        host = abi.particles_struct(case.particles, case.N)
+        tool, keep = case.tool_struct()
+        self._keep += keep
+        ctx = C.c_void_p()
+        r = self.lib.sph_ctx_create(C.byref(case.constants), C.byref(case.grid), C.byref(host),
+                                    C.byref(tool) if tool is not None else None, case.dt, precision, device,
+                                    C.byref(ctx))
+        self.ctx = ctx
+        if r != abi.SPH_OK:
+            msg = self.lib.sph_last_error(ctx).decode() if ctx.value else ""
+            if ctx.value:
+                self.lib.sph_ctx_destroy(ctx)
+                self.ctx = C.c_void_p()
+            raise SphError(f"sph_ctx_create failed ({r}): {msg}")
+        self.has_tool = tool is not None
+        if self.has_tool and place_tool:
+            self.place_tool()
+
+    # ---- plumbing -------------------------------------------------------------------------
+    def _ck(self, r: int, what: str):
+        if r != abi.SPH_OK:
+            raise SphError(f"{what} failed ({r}): {self.lib.sph_last_error(self.ctx).decode()}")
+
+    def call(self, name: str, *args):
+        self._ck(getattr(self.lib, name)(self.ctx, *args), name)
+
+    def close(self):
+        if getattr(self, "ctx", None) is not None and self.ctx.value:
+            self.lib.sph_ctx_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        self.call("sph_sync")
+
+    def status(self, clear: bool = True) -> int:
+        s = C.c_uint32()
+        self._ck(self.lib.sph_status(self.ctx, C.byref(s), 1 if clear else 0), "sph_status")
+        return s.value
+
+    def geometry(self) -> abi.GeomConstants:
+        g = abi.GeomConstants()
+        self._ck(self.lib.sph_get_geometry(self.ctx, C.byref(g)), "sph_get_geometry")
+        return g
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        self._ck(self.lib.sph_launch_count(self.ctx, C.byref(n)), "sph_launch_count")
+        return n.value
+
+    # ---- data movement ----------------------------------------------------------------------
+    def download(self, fields=None) -> dict:
+        out = abi.empty_particles(self.N)
+        if fields is not None:
+            out = {k: v for k, v in out.items() if k in fields}
+        s = abi.particles_struct(out, self.N)
+        self._ck(self.lib.sph_download_particles(self.ctx, C.byref(s)), "sph_download_particles")
+        return out
+
+    def upload(self, arrays: dict):
+        arrays = {k: np.ascontiguousarray(v) for k, v in arrays.items()}
+        s = abi.particles_struct(arrays, self.N)
+        self._ck(self.lib.sph_upload_particles(self.ctx, C.byref(s)), "sph_upload_particles")
+
+    def cells(self):
+        g = self.geometry()
+        cs = np.zeros(g.num_cell, np.int32)
+        ce = np.zeros(g.num_cell, np.int32)
+        self._ck(self.lib.sph_download_cells(self.ctx, abi.ptr(cs), abi.ptr(ce)), "sph_download_cells")
+        return cs, ce
+
+    def tool_state(self) -> abi.ToolState:
+        t = abi.ToolState()
+        self._ck(self.lib.sph_get_tool_state(self.ctx, C.byref(t)), "sph_get_tool_state")
+        return t
+
+    def segments(self) -> dict:
+        n = self.tool_state().n_segments
+        out = dict(left=np.zeros((n, 2)), right=np.zeros((n, 2)), normal=np.zeros((n, 2)),
+                   marks=np.zeros((n, 4), np.int32), heat_exchange=np.zeros((n, 2)), fric_heat=np.zeros(n))
+        s = abi.Segments()
+        s.n = n
+        for k, v in out.items():
+            setattr(s, k, abi.ptr(v))
+        self._ck(self.lib.sph_download_segments(self.ctx, C.byref(s)), "sph_download_segments")
+        return out
+
+    def fem(self) -> dict:
+        f = abi.Fem()
+        self._ck(self.lib.sph_get_fem(self.ctx, C.byref(f)), "sph_get_fem")
+        nn, nz = f.n_nodes, f.nnz
+        out = dict(position=np.zeros((nn, 2)), row_ptr=np.zeros(nn + 1, np.int32), col_ind=np.zeros(nz, np.int32),
+                   K=np.zeros(nz), M_inv=np.zeros(nn), f=np.zeros(nn), T=np.zeros(nn), k=np.zeros(nn))
+        h = abi.Fem()
+        h.n_nodes, h.nnz = nn, nz
+        for k, v in out.items():
+            setattr(h, k, abi.ptr(v))
+        self._ck(self.lib.sph_download_fem(self.ctx, C.byref(h)), "sph_download_fem")
+        return out
+
+    def upload_fem_state(self, T=None, k=None):
+        self._ck(self.lib.sph_upload_fem_state(self.ctx, abi.ptr(None if T is None else np.ascontiguousarray(T)),
+                                               abi.ptr(None if k is None else np.ascontiguousarray(k))),
+                 "sph_upload_fem_state")
+
+    # ---- tool ---------------------------------------------------------------------------
+    def set_vel(self, vx: float, vy: float):
+        self._ck(self.lib.sph_set_tool_velocity(self.ctx, vx, vy), "sph_set_tool_velocity")
+
+    def move_tool(self, dt: float):
+        """segments_update + tool_update_FEM_gpu with the current velocity."""
+        self._ck(self.lib.sph_segments_update(self.ctx, dt), "sph_segments_update")
+        self._ck(self.lib.sph_tool_update_fem(self.ctx, dt), "sph_tool_update_fem")
+
+    def place_tool(self):
+        """Tool placement of benchmarks_NZ.cpp:247-267."""
+        case = self.case
+        dx = case.info["dx"]
+        v = case.tool_speed
+        ts = self.tool_state()
+        distance = ts.right_point - case.info["lo_x"] + dx * 0.01
+        time = distance / v
+        self.set_vel(v, 0.0)
+        self.move_tool(-time)
+        ts = self.tool_state()
+        current_feed = case.info["hi_y"] - ts.lowest_point
+        dist_to_target = abs(current_feed - case.feed)
+        correction_time = dist_to_target / v
+        sign = 1.0 if current_feed > case.feed else -1.0
+        self.set_vel(0.0, v)
+        self.move_tool(correction_time * sign)
+        self.set_vel(v, 0.0)
+
+    # ---- the step and its stages -------------------------------------------------------------
+    def step(self, n: int = 1):
+        """leap_frog::step (fused kernels, CUDA-graph replay)."""
+        if n == 1:
+            self.call("sph_step")
+        else:
+            self._ck(self.lib.sph_run(self.ctx, n), "sph_run")
+
+    def step_staged(self):
+        """leap_frog::step issued as the reference's separate calls."""
+        self.call("sph_step_staged")
+
+    def reduce_force(self):
+        out = np.zeros(2)
+        self._ck(self.lib.sph_reduce_force(self.ctx, abi.ptr(out)), "sph_reduce_force")
+        return out
+
+    def max_T(self) -> float:
+        out = np.zeros(1)
+        self._ck(self.lib.sph_reduce_max_T(self.ctx, abi.ptr(out)), "sph_reduce_max_T")
+        return float(out[0])
+
+    def __getattr__(self, name):
+        # stage calls by their reference names: update_geometry, assign_hashes, sort,
+        # material_eos, interactions_monaghan, ... -> sph_<name>(ctx)
+        if name.startswith("_"):
+            raise AttributeError(name)
+        full = "sph_" + name
+        if full in abi.STAGE_FUNCTIONS:
+            return lambda: self.call(full)
+        raise AttributeError(name)
+
+    def fem_calculate_temp(self, dt: float):
+        self._ck(self.lib.sph_fem_calculate_temp(self.ctx, dt), "sph_fem_calculate_temp")
