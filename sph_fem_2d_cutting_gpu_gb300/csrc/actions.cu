@@ -290,9 +290,8 @@ __global__ void __launch_bounds__(kBlock) k_step_tail(int N, KConsts K, SortedFi
             int ix = __double2int_rz((pos.x - g.bbmin_x) / g.dx);
             int iy = __double2int_rz((pos.y - g.bbmin_y) / g.dx);
             h = ix * g.ny + iy;
-            A.hash[i] = h;
         } else {
-            h = A.hash[i];
+            h = A.hash[i];   // blanked particles keep their stale hash
         }
         int key = h;
         if (h < 0 || h >= K.g.num_cell) {
@@ -301,6 +300,7 @@ __global__ void __launch_bounds__(kBlock) k_step_tail(int N, KConsts K, SortedFi
         }
         X.key[i] = key;
         X.arrival[i] = atomicAdd(X.counts + key, 1);
+        X.hash_next[i] = h;   // the visible hash array changes only at the next sort
     }
     if (st) set_status(status, st);
 }

@@ -19,8 +19,8 @@ template <bool kHash, bool kCount>
 __global__ void __launch_bounds__(kBlock) k_hash_count(int N, const double2 *__restrict__ pos,
                                                        const double *__restrict__ blanked, int32_t *__restrict__ hash,
                                                        int32_t *__restrict__ key, int32_t *__restrict__ arrival,
-                                                       int32_t *__restrict__ counts, sph_geom_constants g,
-                                                       uint32_t *status) {
+                                                       int32_t *__restrict__ counts, int32_t *__restrict__ hash_next,
+                                                       sph_geom_constants g, uint32_t *status) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     int h;
@@ -41,6 +41,7 @@ __global__ void __launch_bounds__(kBlock) k_hash_count(int N, const double2 *__r
         }
         key[i] = k;
         arrival[i] = atomicAdd(counts + k, 1);
+        hash_next[i] = h;
     }
 }
 
@@ -263,9 +264,11 @@ __global__ void __launch_bounds__(kBlock) k_build_records(int N, KConsts K, Sort
 // (actions_gpu.cu:234-278) + the neighbour record of the predicted state.
 // The sorted arrays B keep the start-of-step state (the reference's *_init
 // snapshots); the predicted values live only in the records and in p / R.
+// hash_src: the hashes the histogram pass took (compute_hashes of this step).
 template <bool kF32>
 __global__ void __launch_bounds__(kBlock) k_gather_fused(int N, const int32_t *__restrict__ perm, KConsts K,
                                                          SortedFields A, SortedFields B, FixedFields F,
+                                                         const int32_t *__restrict__ hash_src,
                                                          dbl4 *__restrict__ rec64, float4 *__restrict__ rec32) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= N) return;
@@ -278,7 +281,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused(int N, const int32_t *_
     double2 pos_t = A.pos_t[i], vel_t = A.vel_t[i];
     double rho_t = A.rho_t[i], T_t = A.T_t[i];
     dbl4 S_t = A.S_t[i];
-    int hash = A.hash[i];
+    int hash = hash_src[i];
     B.pos[k] = pos;
     B.vel[k] = vel;
     B.fc[k] = A.fc[i];
@@ -336,7 +339,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused(int N, const int32_t *_
 // ---- host launchers ---------------------------------------------------------------------
 void launch_hash(cudaStream_t s, int N, const SortedFields &A, sph_geom_constants g) {
     k_hash_count<true, false><<<div_up(N, kBlock), kBlock, 0, s>>>(N, A.pos, A.blanked, A.hash, nullptr, nullptr,
-                                                                     nullptr, g, nullptr);
+                                                                     nullptr, nullptr, g, nullptr);
 }
 
 void launch_count(cudaStream_t s, int N, const SortedFields &A, const SortScratch &X, sph_geom_constants g,
@@ -344,10 +347,10 @@ void launch_count(cudaStream_t s, int N, const SortedFields &A, const SortScratc
     cudaMemsetAsync(X.counts, 0, sizeof(int32_t) * (size_t)(g.num_cell + 1), s);
     if (with_hash)
         k_hash_count<true, true><<<div_up(N, kBlock), kBlock, 0, s>>>(N, A.pos, A.blanked, A.hash, X.key, X.arrival,
-                                                                       X.counts, g, status);
+                                                                       X.counts, X.hash_next, g, status);
     else
         k_hash_count<false, true><<<div_up(N, kBlock), kBlock, 0, s>>>(N, A.pos, A.blanked, A.hash, X.key, X.arrival,
-                                                                        X.counts, g, status);
+                                                                        X.counts, X.hash_next, g, status);
 }
 
 int scan_blocks(int num_cell) { return div_up(num_cell + 1, kScanTile); }
@@ -368,11 +371,11 @@ void launch_gather_plain(cudaStream_t s, int N, const int32_t *perm, const Sorte
 }
 
 void launch_gather_fused(cudaStream_t s, int N, const int32_t *perm, const KConsts &K, const SortedFields &A,
-                         const SortedFields &B, const FixedFields &F, const StepScratch &W) {
+                         const SortedFields &B, const FixedFields &F, const StepScratch &W, const int32_t *hash_src) {
     if (K.precision == SPH_PREC_FP32K)
-        k_gather_fused<true><<<div_up(N, kBlock), kBlock, 0, s>>>(N, perm, K, A, B, F, W.rec64, W.rec32);
+        k_gather_fused<true><<<div_up(N, kBlock), kBlock, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec64, W.rec32);
     else
-        k_gather_fused<false><<<div_up(N, kBlock), kBlock, 0, s>>>(N, perm, K, A, B, F, W.rec64, W.rec32);
+        k_gather_fused<false><<<div_up(N, kBlock), kBlock, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec64, W.rec32);
 }
 
 void launch_build_records(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F,

@@ -196,7 +196,7 @@ int issue_fused_body(sph_ctx *ctx, int64_t &n) {
     SortedFields &B = ctx->buf[1 - ctx->cur];
     launch_sort_rest(s, N, ctx->X, ctx->K.g, ctx->F.idx, ctx->W.status);
     n += 5;
-    launch_gather_fused(s, N, ctx->F.idx, ctx->K, A, B, ctx->F, ctx->W);
+    launch_gather_fused(s, N, ctx->F.idx, ctx->K, A, B, ctx->F, ctx->W, ctx->X.hash_next);
     n += 1;
     if (ctx->has_tool) {
         launch_fem_half(s, ctx->fem, 0.5 * ctx->K.dt);
@@ -349,7 +349,7 @@ int sph_ctx_create(const sph_constants *c, const sph_grid_params *g, const sph_p
     }
     DALLOC(ctx->F.p, N); DALLOC(ctx->F.R, N); DALLOC(ctx->F.S_der, N); DALLOC(ctx->F.v_der, N); DALLOC(ctx->F.idx, N);
     const int nc = ctx->K.g.num_cell;
-    DALLOC(ctx->X.key, N); DALLOC(ctx->X.arrival, N); DALLOC(ctx->X.slots, N);
+    DALLOC(ctx->X.key, N); DALLOC(ctx->X.arrival, N); DALLOC(ctx->X.slots, N); DALLOC(ctx->X.hash_next, N);
     DALLOC(ctx->X.counts, (size_t)nc + 1); DALLOC(ctx->X.offsets, (size_t)nc + 2);
     DALLOC(ctx->X.block_sums, (size_t)scan_blocks(nc) + 1);
     DALLOC(ctx->X.cell_start, nc); DALLOC(ctx->X.cell_end, nc);
@@ -883,7 +883,7 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
         CK(cudaEventRecord(ev[1], s));
         launch_sort_rest(s, N, ctx->X, ctx->K.g, ctx->F.idx, ctx->W.status);
         CK(cudaEventRecord(ev[2], s));
-        launch_gather_fused(s, N, ctx->F.idx, ctx->K, A, B, ctx->F, ctx->W);
+        launch_gather_fused(s, N, ctx->F.idx, ctx->K, A, B, ctx->F, ctx->W, ctx->X.hash_next);
         CK(cudaEventRecord(ev[3], s));
         if (ctx->has_tool) launch_fem_half(s, ctx->fem, 0.5 * ctx->K.dt);
         CK(cudaEventRecord(ev[4], s));

@@ -16,7 +16,7 @@ void launch_sort_rest(cudaStream_t s, int N, const SortScratch &X, sph_geom_cons
                       uint32_t *status);
 void launch_gather_plain(cudaStream_t s, int N, const int32_t *perm, const SortedFields &A, const SortedFields &B);
 void launch_gather_fused(cudaStream_t s, int N, const int32_t *perm, const KConsts &K, const SortedFields &A,
-                         const SortedFields &B, const FixedFields &F, const StepScratch &W);
+                         const SortedFields &B, const FixedFields &F, const StepScratch &W, const int32_t *hash_src);
 void launch_build_records(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F,
                           const StepScratch &W);
 

@@ -30,6 +30,8 @@ struct FixedFields {
 // Scratch of the counting sort.
 struct SortScratch {
     int32_t *key;        // [N] sort key of each particle (hash, or num_cell when out of range)
+    int32_t *hash_next;  // [N] raw hash taken by the histogram pass (the fused step keeps the
+                         //     visible hash array as the reference leaves it until the next sort)
     int32_t *arrival;    // [N] arrival slot inside its cell (atomic counter value)
     int32_t *counts;     // [num_cell+1] particles per cell (last = out-of-grid bucket)
     int32_t *offsets;    // [num_cell+2] exclusive scan of counts
