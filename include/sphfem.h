@@ -292,6 +292,35 @@ int sph_reduce_max_T(sph_ctx *ctx, double *out);       /* max over non-blanked p
  * histogram).  n_stages receives 7. */
 int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_stages);
 
+/* ---- cell-list build that allocates nothing ------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * when they need a cell list: a host application whose own memory manager
+ * owns all device memory, a latency-critical loop that cannot afford an
+ * allocation's synchronisation, a recovery path that must work when device
+ * memory is exhausted.
+ *
+ * Computes the same results as sph_assign_hashes + sph_sort
+ * (compute_hashes + stable sort_by_key + cell tables, grid.cu:25-42,
+ * grid_gpu_green.cu:13-115,185-209) for device arrays the caller owns:
+ *  - pos [n][2], blanked [n]: inputs;
+ *  - hash [n]: in/out; recomputed for non-blanked particles, kept (stale)
+ *    for blanked ones;
+ *  - perm [n]: sorted position -> original index;
+ *  - hash_sorted [n]: optional (NULL to skip);
+ *  - cell_start / cell_end [g->num_cell]: cell_end is left untouched for
+ *    empty cells.
+ * Scratch is a fixed file-scope device array (about 5.2 MB held by every GPU
+ * that loads the library).  Limits: n <= 262144 particles and
+ * g->num_cell <= 262143 cells; larger sizes return SPH_ERR_INVALID with a
+ * message in err (err_len bytes, may be NULL).  The first call on a device
+ * looks up the array's address there; make it before any stream capture.
+ * All calls share the scratch, so calls that overlap on the GPU race:
+ * serialise them.  Work is queued on `stream` (cudaStream_t, NULL = default
+ * stream); the call does not synchronise. */
+int sph_cells_build_noalloc(const double *pos, const double *blanked, int32_t *hash, int32_t n,
+                            const sph_geom_constants *g, int32_t *perm, int32_t *hash_sorted,
+                            int32_t *cell_start, int32_t *cell_end, void *stream, char *err, int32_t err_len);
+
 /* ---- kernel launch accounting ---------------------------------------------- */
 int sph_launch_count(const sph_ctx *ctx, int64_t *count);   /* kernels launched by this context */
 

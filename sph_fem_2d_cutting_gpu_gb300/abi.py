@@ -178,7 +178,9 @@ def load() -> C.CDLL:
         "sph_reduce_force": ([P, PD], C.c_int),
         "sph_reduce_max_T": ([P, PD], C.c_int),
         "sph_launch_count": ([P, C.POINTER(C.c_int64)], C.c_int),
-        "sph_profile_steps": ([P, I32, C.POINTER(C.c_float), C.POINTER(I32)], C.c_int),
+        "sph_cells_build_noalloc": ([P, P, P, I32, C.POINTER(GeomConstants), P, P, P, P, P, C.c_char_p, I32],
+                                    C.c_int),
+        "sph_profile_steps":([P, I32, C.POINTER(C.c_float), C.POINTER(I32)], C.c_int),
         "sph_tool_build":([C.POINTER(ToolMesh), C.POINTER(ToolConstants), C.POINTER(P)], C.c_int),
         "sph_tool_host_info": ([P, C.POINTER(ToolState), C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)], C.c_int),
         "sph_tool_host_export": ([P, C.POINTER(Segments), C.POINTER(Fem)], C.c_int),

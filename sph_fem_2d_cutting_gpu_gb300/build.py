@@ -23,7 +23,7 @@ LIB = LIBDIR / "libsphfem.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
                      "-Xptxas", "-warn-spills"]
-SOURCES = ["cells.cu", "interactions.cu", "actions.cu", "fem.cu", "context.cu", "toolsetup.cpp"]
+SOURCES = ["cells.cu", "interactions.cu", "actions.cu", "fem.cu", "context.cu", "toolsetup.cpp", "noalloc.cu"]
 HEADERS = ["common.cuh", "physics.cuh", "state.cuh", "launch.cuh", "toolsetup.h"]
 
 
