@@ -282,6 +282,47 @@ int sph_step_staged(sph_ctx *ctx);
 int sph_reduce_force(sph_ctx *ctx, double out[2]);     /* sum over particles of fc + ft */
 int sph_reduce_max_T(sph_ctx *ctx, double *out);       /* max over non-blanked particles of T */
 
+/* ---- batched multi-case runs ------------------------------------------------------
+ * Many independent cutting cases advanced together: every case keeps its own
+ * particles, FEM tool, tool velocity and time step; they share the material
+ * and corrector constants, the smoothing length (cell geometry) and the
+ * precision form, which must be SPH_PREC_FP32K.  Each case is moved to its own
+ * strip of one global cell grid (x offset, gaps wider than the stencil), so
+ * every step stage runs as one launch over all cases and one CUDA graph per
+ * step replays them all.  The tool of each case must already be placed
+ * (positions in the case's own frame).  No counterpart call in the reference:
+ * it runs one case per process (mfree_gpu.cpp:141-381). */
+typedef struct sph_case_desc {
+    const sph_particles *host;      /* particles of this case (case frame)            */
+    const sph_tool_mesh *tool;      /* tool mesh of this case (case frame, placed)    */
+    double dt;                      /* time step of this case                         */
+    double tool_vel[2];             /* tool velocity (tool::set_vel)                  */
+    double bbmin[2], bbmax[2];      /* this case's locked grid box (case frame)       */
+} sph_case_desc;
+
+/* `cell` gives the shared h, cell_factor and stencil; its bbmin/bbmax are
+ * ignored (each case brings its own box).  Case k is moved by offset_k so
+ * that its box starts at its own column range of the global grid and its
+ * bottom lines up with the others; with cells of the same edge, a particle
+ * sees the cells it sees in a single-case context on that box.  A particle
+ * that leaves its case box stays in the global grid (a single-case grid sends
+ * it to the overflow bucket); cases whose particles stay in their boxes do
+ * not interact (the gap between cases is wider than the stencil). */
+int sph_batch_create(const sph_constants *c, const sph_grid_params *cell, int32_t n_cases,
+                     const sph_case_desc *cases, int32_t precision, int32_t device, sph_ctx **out);
+/* Particle range [first, first+count) of case k in the concatenated arrays
+ * before the first sort (cases are concatenated in order), the offset added
+ * to the case's positions (x, y), and its first segment / FEM node and counts. */
+int sph_batch_case_info(const sph_ctx *ctx, int32_t k, int32_t *first, int32_t *count, double offset[2],
+                        int32_t *seg_first, int32_t *seg_count, int32_t *node_first, int32_t *node_count);
+int sph_batch_n_cases(const sph_ctx *ctx, int32_t *n_cases);
+/* Per case k: out[3k], out[3k+1] = sum of fc + ft over the case's particles
+ * (report_force, output.cu:41-49), out[3k+2] = max T over its non-blanked
+ * particles.  Works on single-case contexts too (n_cases = 1). */
+int sph_batch_reduce(sph_ctx *ctx, double *out);
+/* Case of every particle of the current (caller-visible) order, [N]. */
+int sph_batch_case_of_particles(sph_ctx *ctx, int32_t *case_of);
+
 /* ---- per-stage timing ---------------------------------------------------------
  * Runs `nsteps` fused steps without the CUDA graph, with CUDA events on the
  * context stream between the stages; stage_ms[k] receives the summed device

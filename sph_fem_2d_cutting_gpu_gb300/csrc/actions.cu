@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(kBlock) k_fric_heat(int N, KConsts K, SortedFi
                                                       const ToolDev *__restrict__ tool, uint32_t *status) {
     PARTICLE_LOOP_HEAD
     double T = A.T[i], blanked = A.blanked[i];
-    uint32_t st = fric_heat_one(K, tool->vel, A.vel[i], A.ft[i], A.n[i], A.fc[i], A.rho[i], A.eps_pl[i], A.on_seg[i],
+    uint32_t st = fric_heat_one(K, K.dt, tool->vel, A.vel[i], A.ft[i], A.n[i], A.fc[i], A.rho[i], A.eps_pl[i], A.on_seg[i],
                                 seg.n, T, blanked, seg.fric_heat);
     if (T != A.T[i]) A.T[i] = T;
     if (blanked != A.blanked[i]) A.blanked[i] = blanked;
@@ -116,7 +116,8 @@ __global__ void __launch_bounds__(kBlock) k_fric_heat(int N, KConsts K, SortedFi
 }
 
 // ---- contact, one particle: actions_gpu.cu:423-583 (s1) ------------------------------------------
-__device__ __forceinline__ uint32_t contact_s1_one(const KConsts &K, const SegDev &seg, const ToolDev &tool,
+// seg: the segments of the particle's case; on_seg comes back as an index into them.
+__device__ __forceinline__ uint32_t contact_s1_one(const KConsts &K, double dt, const SegDev &seg, const ToolDev &tool,
                                                    double2 pos, double2 vel, double2 &fc, double2 &ft, double2 &nrm,
                                                    int &on_seg, double &blanked) {
     int inside = 0;
@@ -142,7 +143,6 @@ __device__ __forceinline__ uint32_t contact_s1_one(const KConsts &K, const SegDe
         on_seg = -1;
         return SPH_STATUS_CONTACT_DEEP;
     }
-    const double dt = K.dt;
     double dt2 = dt * dt;
     double s1 = -K.c.tool.slave_mass * gN;
     double2 fN = make_double2(s1 * n_.x / dt2 * K.c.tool.contact_alpha, s1 * n_.y / dt2 * K.c.tool.contact_alpha);
@@ -162,8 +162,8 @@ __device__ __forceinline__ uint32_t contact_s1_one(const KConsts &K, const SegDe
 }
 
 // ---- contact, one particle: actions_gpu.cu:585-617 (s2) ------------------------------------------
-__device__ __forceinline__ void contact_s2_one(const KConsts &K, const SegDev &seg, const double *__restrict__ T_nodes,
-                                               int seg_no, double rho, double &T) {
+__device__ __forceinline__ void contact_s2_one(const KConsts &K, double dt, const SegDev &seg,
+                                               const double *__restrict__ T_nodes, int seg_no, double rho, double &T) {
     int4 mk = seg.marks[seg_no];
     double T_ = T;
     double T_seg = 0.5 * (T_nodes[mk.z] + T_nodes[mk.w]);
@@ -171,7 +171,7 @@ __device__ __forceinline__ void contact_s2_one(const KConsts &K, const SegDev &s
     double length = sqrtf_d(K.c.tool.slave_mass / rho);
     atomicAdd(&seg.heat_exchange[seg_no].x, T_ * length);
     atomicAdd(&seg.heat_exchange[seg_no].y, length);
-    double delta_T_part = delta_T * K.c.tool.h * length / K.c.trml_wp.cp / K.c.tool.slave_mass * K.dt;
+    double delta_T_part = delta_T * K.c.tool.h * length / K.c.trml_wp.cp / K.c.tool.slave_mass * dt;
     if (delta_T_part < 0) T += fmax(delta_T_part, delta_T);
     else T += fmin(delta_T_part, delta_T);
 }
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(kBlock) k_contact_s1(int N, KConsts K, SortedF
     double2 fc = A.fc[i], ft = A.ft[i], nrm = A.n[i];
     int on = A.on_seg[i];
     double blanked = 0.;
-    uint32_t st = contact_s1_one(K, seg, *tool, A.pos[i], A.vel[i], fc, ft, nrm, on, blanked);
+    uint32_t st = contact_s1_one(K, K.dt, seg, *tool, A.pos[i], A.vel[i], fc, ft, nrm, on, blanked);
     A.fc[i] = fc; A.ft[i] = ft; A.n[i] = nrm; A.on_seg[i] = on;
     if (blanked == 1.) A.blanked[i] = 1.;
     if (st) set_status(status, st);
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(kBlock) k_contact_s2(int N, KConsts K, SortedF
     int on = A.on_seg[i];
     if (on < 0 || on >= seg.n) return;
     double T = A.T[i];
-    contact_s2_one(K, seg, T_nodes, on, A.rho[i], T);
+    contact_s2_one(K, K.dt, seg, T_nodes, on, A.rho[i], T);
     A.T[i] = T;
 }
 
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(kBlock) k_bc_thermal(int N, KConsts K, SortedF
 }
 
 // ---- actions_gpu.cu:787-824 do_invalidate ----------------------------------------------------------
-__device__ __forceinline__ bool isnaninf(double v) { return isnan(v) || isinf(v); }
+__device__ __forceinline__ bool isnaninf(double v) { return is_nan_or_inf(v); }
 
 __device__ __forceinline__ bool invalid_rates(double2 pt, double2 vt, dbl4 St, double rho_t, double T_t) {
     return isnaninf(pt.x) || isnaninf(pt.y) || isnaninf(vt.x) || isnaninf(vt.y) || isnaninf(St.x) ||
@@ -246,46 +246,54 @@ __global__ void __launch_bounds__(kBlock) k_step_tail(int N, KConsts K, SortedFi
                                                       const double *__restrict__ T_nodes, SortScratch X,
                                                       uint32_t *status) {
     PARTICLE_LOOP_HEAD
-    double blanked = A.blanked[i];
-    const double tool_p = A.tool_particle[i];
-    const double fixed = A.fixed[i];
+    bool blanked = flag_is_one(A.blanked[i]);
+    const bool bc_fixed = !flag_nonzero(A.tool_particle[i]) && flag_nonzero(A.fixed[i]);   // do_boundary_conditions
+    const bool bc_thermal = K.thermal_bc && flag_is_one(A.fixed[i]);                         // ..._thermal
     uint32_t st = 0;
     double2 pos = A.pos[i];
-    if (kTool && blanked != 1.) {
+    if (kTool && !blanked) {
+        // the particle's case: its tool, time step and interface segments
+        const ToolDev &tc = tool[case_of_hash(K, A.hash[i])];
+        SegDev cs = seg;
+        cs.left += tc.seg_first;
+        cs.right += tc.seg_first;
+        cs.normal += tc.seg_first;
+        cs.n = tc.seg_count;
         double2 fc = A.fc[i], ft = A.ft[i], nrm = A.n[i];
         int on = A.on_seg[i];
         double bl = 0.;
-        st |= contact_s1_one(K, seg, *tool, pos, A.vel[i], fc, ft, nrm, on, bl);
-        if (bl == 1.) { blanked = 1.; A.blanked[i] = 1.; }
+        st |= contact_s1_one(K, tc.dt, cs, tc, pos, A.vel[i], fc, ft, nrm, on, bl);
+        if (on >= 0) on += tc.seg_first;   // global segment id
+        if (flag_is_one(bl)) { blanked = true; A.blanked[i] = 1.; }
         A.ft[i] = ft;
         A.n[i] = nrm;
         A.on_seg[i] = on;
-        if (tool_p == 0. && fixed != 0.) fc = make_double2(0., 0.);
+        if (bc_fixed) fc = make_double2(0., 0.);
         A.fc[i] = fc;
-        if (blanked != 1. && on >= 0 && on < seg.n) {
+        if (!blanked && on >= 0 && on < seg.n) {
             double T = A.T[i];
-            contact_s2_one(K, seg, T_nodes, on, A.rho[i], T);
+            contact_s2_one(K, tc.dt, seg, T_nodes, on, A.rho[i], T);
             A.T[i] = T;
         }
-    } else if (tool_p == 0. && fixed != 0.) {
+    } else if (bc_fixed) {
         A.fc[i] = make_double2(0., 0.);
     }
-    if (tool_p == 0. && fixed != 0.) {
+    if (bc_fixed) {
         A.vel[i] = make_double2(0., 0.);
         A.pos_t[i] = make_double2(0., 0.);
         A.vel_t[i] = make_double2(0., 0.);
     }
-    if (K.c.trml_tool.alpha != 0. && fixed == 1.) A.T[i] = K.c.trml_wp.T_init;
-    if (blanked != 1.) {
+    if (bc_thermal) A.T[i] = K.c.trml_wp.T_init;
+    if (!blanked) {
         if (invalid_rates(A.pos_t[i], A.vel_t[i], A.S_t[i], A.rho_t[i], A.T_t[i])) {
-            blanked = 1.;
+            blanked = true;
             A.blanked[i] = 1.;
             st |= SPH_STATUS_NAN_BLANKED;
         }
     }
     if (kNextHash) {
         int h;
-        if (blanked != 1.) {
+        if (!blanked) {
             const sph_geom_constants &g = K.g;
             int ix = __double2int_rz((pos.x - g.bbmin_x) / g.dx);
             int iy = __double2int_rz((pos.y - g.bbmin_y) / g.dx);
@@ -329,6 +337,43 @@ __global__ void __launch_bounds__(kBlock) k_reduce_force_T(int N, SortedFields A
         out[3 * blockIdx.x + 0] = sx[0];
         out[3 * blockIdx.x + 1] = sy[0];
         out[3 * blockIdx.x + 2] = sm[0];
+    }
+}
+
+// Per-case sums of fc + ft and max T of non-blanked particles, one block per
+// case over its contiguous particle range.  With `offsets` (the state is in
+// cell order; cases own disjoint column ranges, so whole cases are contiguous)
+// case k spans cells [cell_bound[k], cell_bound[k+1]); otherwise particles
+// [part_bound[k], part_bound[k+1]) (the concatenation order of the upload).
+__global__ void __launch_bounds__(kBlock) k_reduce_cases(SortedFields A, const int32_t *__restrict__ offsets,
+                                                         const int32_t *__restrict__ cell_bound,
+                                                         const int32_t *__restrict__ part_bound,
+                                                         double *__restrict__ out) {
+    __shared__ double sx[kBlock], sy[kBlock], sm[kBlock];
+    const int k = blockIdx.x;
+    const int b = offsets ? offsets[cell_bound[k]] : part_bound[k];
+    const int e = offsets ? offsets[cell_bound[k + 1]] : part_bound[k + 1];
+    double fx = 0., fy = 0., tm = -1e300;
+    for (int i = b + threadIdx.x; i < e; i += blockDim.x) {
+        double2 fc = A.fc[i], ft = A.ft[i];
+        fx += fc.x + ft.x;
+        fy += fc.y + ft.y;
+        if (A.blanked[i] != 1.) tm = fmax(tm, A.T[i]);
+    }
+    sx[threadIdx.x] = fx; sy[threadIdx.x] = fy; sm[threadIdx.x] = tm;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            sx[threadIdx.x] += sx[threadIdx.x + o];
+            sy[threadIdx.x] += sy[threadIdx.x + o];
+            sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[3 * k + 0] = sx[0];
+        out[3 * k + 1] = sy[0];
+        out[3 * k + 2] = sm[0];
     }
 }
 
@@ -389,6 +434,10 @@ void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedField
 int reduce_blocks() { return 304; }
 void launch_reduce_force_T(cudaStream_t s, int N, const SortedFields &A, double *out) {
     k_reduce_force_T<<<reduce_blocks(), kBlock, 0, s>>>(N, A, out);
+}
+void launch_reduce_cases(cudaStream_t s, int n_cases, const SortedFields &A, const int32_t *offsets,
+                         const int32_t *cell_bound, const int32_t *part_bound, double *out) {
+    k_reduce_cases<<<n_cases, kBlock, 0, s>>>(A, offsets, cell_bound, part_bound, out);
 }
 
 }  // namespace sphfem

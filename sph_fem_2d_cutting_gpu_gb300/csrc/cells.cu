@@ -336,6 +336,95 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused(int N, const int32_t *_
     }
 }
 
+// FP32-compensated form of the fused reorder: the same gather, with the
+// predictor, EOS and artificial stress of the predicted state evaluated in
+// FP32 (positions and density stay FP64: rho - rho0 is a small difference,
+// FP32 would lose its leading digits) and written into the FP32 record.
+__global__ void __launch_bounds__(kBlock) k_gather_fused32(int N, const int32_t *__restrict__ perm, KConsts K,
+                                                           SortedFields A, SortedFields B, FixedFields F,
+                                                           const int32_t *__restrict__ hash_src,
+                                                           float4 *__restrict__ rec, const ToolDev *__restrict__ tools) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    int i = perm[k];
+    F.idx[k] = i;
+    const double2 pos = A.pos[i], vel = A.vel[i], pos_t = A.pos_t[i], vel_t = A.vel_t[i];
+    const dbl4 S = A.S[i], S_t = A.S_t[i];
+    const double rho = A.rho[i], T = A.T[i], h = A.h[i], rho_t = A.rho_t[i], T_t = A.T_t[i];
+    const double blanked = A.blanked[i], tool = A.tool_particle[i];
+    const int hash = hash_src[i];
+    B.pos[k] = pos;
+    B.vel[k] = vel;
+    B.fc[k] = A.fc[i];
+    B.ft[k] = A.ft[i];
+    B.h[k] = h;
+    B.n[k] = A.n[i];
+    B.rho[k] = rho;
+    B.S[k] = S;
+    B.eps_pl[k] = A.eps_pl[i];
+    B.eps_pl_dot[k] = A.eps_pl_dot[i];
+    B.T[k] = T;
+    B.fixed[k] = A.fixed[i];
+    B.blanked[k] = blanked;
+    B.tool_particle[k] = tool;
+    B.pos_t[k] = pos_t;
+    B.vel_t[k] = vel_t;
+    B.rho_t[k] = rho_t;
+    B.S_t[k] = S_t;
+    B.T_t[k] = T_t;
+    B.on_seg[k] = A.on_seg[i];
+    B.hash[k] = hash;
+    const bool is_blanked = flag_is_one(blanked), is_tool = flag_nonzero(tool);
+    // predictor (leap_frog.cu:45-69)
+    double2 pp = pos;
+    double rp = rho;
+    float vx = (float)vel.x, vy = (float)vel.y;
+    float4 Sp = make_float4((float)S.x, (float)S.y, (float)S.z, (float)S.w);
+    float Tp = (float)T;
+    if (!is_blanked) {
+        const ToolDev &tc = tools[case_of_hash(K, hash)];   // time step of the particle's case
+        const double hdt = tc.hdt;
+        const float hdtf = tc.hdtf;
+        pp.x = pos.x + hdt * pos_t.x;
+        pp.y = pos.y + hdt * pos_t.y;
+        rp = rho + hdt * rho_t;
+        vx = fmaf(hdtf, (float)vel_t.x, vx);
+        vy = fmaf(hdtf, (float)vel_t.y, vy);
+        Sp.x = fmaf(hdtf, (float)S_t.x, Sp.x);
+        Sp.y = fmaf(hdtf, (float)S_t.y, Sp.y);
+        Sp.z = fmaf(hdtf, (float)S_t.z, Sp.z);
+        Sp.w = fmaf(hdtf, (float)S_t.w, Sp.w);
+        Tp = fmaf(hdtf, (float)T_t, Tp);
+    }
+    const float rhof = (float)rp;
+    float p;
+    float4 R;
+    if (!is_tool) {
+        p = (float)(K.c0sq * (rp - K.c.phys.rho0));                 // do_material_eos
+        R = artificial_stress_f32(K.f.stresseps, rhof, p, Sp);
+        F.p[k] = (double)p;
+        F.R[k] = mk4(R.x, R.y, R.z, 0.);
+    } else {
+        p = (float)F.p[k];
+        dbl4 Rd = F.R[k];
+        R = make_float4((float)Rd.x, (float)Rd.y, (float)Rd.z, 0.f);
+    }
+    const float thermal_alpha = is_tool ? K.f.alpha_tool_sph : K.f.alpha_wp;
+    const float Tn = (thermal_alpha != 0.f) ? Tp : 0.f;
+    // record: (xr, yr, flags|row, h) (vx, vy, rho, c) (sA, sB, sC, m/rho) (Rxx, Rxy, Ryy, T)
+    const sph_geom_constants &g = K.g;
+    int ci = 0, cj = 0;
+    if (hash >= 0 && hash < g.num_cell) { ci = hash / g.ny; cj = hash - ci * g.ny; }
+    const float xr = (float)(pp.x - (g.bbmin_x + (double)ci * g.dx));
+    const float yr = (float)(pp.y - (g.bbmin_y + (double)cj * g.dx));
+    const int flags = (cj & kRowMask) | (is_blanked ? kFlagBlanked : 0) | (is_tool ? kFlagTool : 0);
+    const float rho21 = 1.f / (rhof * rhof);
+    rec[4 * k + 0] = make_float4(xr, yr, __int_as_float(flags), (float)h);
+    rec[4 * k + 1] = make_float4(vx, vy, rhof, sqrtf(K.f.K_bulk / rhof));
+    rec[4 * k + 2] = make_float4((Sp.x - p) * rho21, Sp.y * rho21, (Sp.z - p) * rho21, K.f.mass / rhof);
+    rec[4 * k + 3] = make_float4(R.x, R.y, R.z, Tn);
+}
+
 // ---- host launchers ---------------------------------------------------------------------
 void launch_hash(cudaStream_t s, int N, const SortedFields &A, sph_geom_constants g) {
     k_hash_count<true, false><<<div_up(N, kBlock), kBlock, 0, s>>>(N, A.pos, A.blanked, A.hash, nullptr, nullptr,
@@ -371,9 +460,10 @@ void launch_gather_plain(cudaStream_t s, int N, const int32_t *perm, const Sorte
 }
 
 void launch_gather_fused(cudaStream_t s, int N, const int32_t *perm, const KConsts &K, const SortedFields &A,
-                         const SortedFields &B, const FixedFields &F, const StepScratch &W, const int32_t *hash_src) {
+                         const SortedFields &B, const FixedFields &F, const StepScratch &W, const int32_t *hash_src,
+                         const ToolDev *tool) {
     if (K.precision == SPH_PREC_FP32K)
-        k_gather_fused<true><<<div_up(N, kBlock), kBlock, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec64, W.rec32);
+        k_gather_fused32<<<div_up(N, kBlock), kBlock, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec32, tool);
     else
         k_gather_fused<false><<<div_up(N, kBlock), kBlock, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec64, W.rec32);
 }

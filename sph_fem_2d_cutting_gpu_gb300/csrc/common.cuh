@@ -16,8 +16,23 @@ __host__ __device__ __forceinline__ dbl4 mk4(double x, double y, double z, doubl
 }
 
 constexpr int kBlock = 256;          // particle kernels
+constexpr int kPairChunk = 32;       // in-support neighbours collected per pass of the pair loops
+constexpr int kMaxStencil = 3;       // the pair list packs the column offset in 3 bits
 constexpr int kCellRankCap = 4096;   // cells larger than this are ranked by the slow path
 constexpr double kPiFac = 0.454728408833987;   // PI_FAC, kernels.cuh:19 (10/(7 pi))
+
+struct JcF32 {   // Johnson-Cook constants in FP32 (plasticity.cuh:21-39)
+    float A, B, C, n, m, Tref, inv_dT, inv_epsdot_ref, Tmelt;
+};
+
+// FP32 copies of the constants the FP32-compensated kernels use, computed
+// once on the host: on GB300 a per-thread double->float conversion or double
+// division runs on the narrow FP64 pipe in every warp.
+struct KF32 {
+    float mass, inv_mass, xs_mass, alpha, beta, eta2, inv_wdp, cell, G, K_bulk, c0sq, stresseps;
+    float dt, hdt, inv_dt, tq_over_cp, alpha_wp, alpha_tool_sph, T_init;
+    JcF32 jc;
+};
 
 // Every constant a kernel needs, passed by value (lands in the kernel
 // parameter bank; no __constant__ symbol, so CUDA graphs capture it as is).
@@ -29,19 +44,57 @@ struct KConsts {
     double c0sq;          // (sqrtf(K/rho0))^2 of do_material_eos (actions_gpu.cu:228-230)
     double inv_wdeltap;   // 1/wdeltap (interactions_gpu.cu:269)
     double eta2;          // eta*eta (interactions_gpu.cu:301)
+    double inv_dx;        // 1/cell edge
     int32_t has_tool;
     int32_t precision;
+    int32_t thermal_bc;   // m_thermal: thermals_tool.alpha != 0 (actions_gpu.cu:938-944)
+    int32_t n_cases;      // 1, or the number of cases of a batched context
+    KF32 f;
+    // batched contexts: case of every grid column / FEM node / segment (NULL: one case)
+    const uint16_t *case_of_col;
+    const uint16_t *case_of_node;
+    const uint16_t *case_of_seg;
 };
+
+// Case of a particle from its cell hash (its grid column).
+__device__ __forceinline__ int case_of_hash(const KConsts &K, int hash) {
+    if (!K.case_of_col) return 0;
+    int ix = hash / K.g.ny;
+    ix = ix < 0 ? 0 : (ix >= K.g.nx ? K.g.nx - 1 : ix);
+    return K.case_of_col[ix];
+}
+
+// ---- flags stored as double 0/1 (particle_gpu.h:41-43), tested on the integer
+// pipe: GB300's FP64 pipe is narrow and a double compare occupies it.
+__device__ __forceinline__ bool flag_is_one(double v) {            // v == 1.
+    return __double_as_longlong(v) == 0x3FF0000000000000LL;
+}
+__device__ __forceinline__ bool flag_nonzero(double v) {           // v != 0. (NaN counts as non-zero)
+    return (__double_as_longlong(v) << 1) != 0;
+}
+__device__ __forceinline__ bool is_nan_or_inf(double v) {          // isnan(v) || isinf(v)
+    return (__double_as_longlong(v) & 0x7FF0000000000000LL) == 0x7FF0000000000000LL;
+}
+
+// compute_hashes' cell index (int)((x - bbmin)/dx) (grid.cu:36-39).
+__device__ __forceinline__ int cell_coord(double x, double bbmin, double dx) {
+    return __double2int_rz((x - bbmin) / dx);
+}
 
 // Device copy of the rigid tool kinematics that tool_FEM keeps on the host
 // (tool_FEM.h:57-77); updated by the tool-move kernel so a captured CUDA graph
 // needs no host round trip.
+// In a batched context there is one per case, with the case's time step and
+// its range of interface segments.
 struct ToolDev {
     double vel[2];
     double tl_point_ref[2];
     double br_point[2];
     double ref_dist;
     double lowest_point, right_point;
+    double dt, hdt;                 // time step of the case and half of it
+    float dtf, hdtf, inv_dtf;       // the same in FP32
+    int32_t seg_first, seg_count;   // the case's interface segments
 };
 
 // ---- float narrowings of the reference (double argument -> float call) ------

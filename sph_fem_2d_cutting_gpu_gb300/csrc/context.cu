@@ -1,6 +1,7 @@
 // context.cu -- the C ABI (include/sphfem.h): context, data movement, the
 // stage entry points that mirror the calls of leap_frog::step
 // (leap_frog.cu:162-248) and the fused, graph-captured step.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -37,6 +38,14 @@ struct sph_ctx {
     bool use_graph = true;
     int64_t launches = 0;
     double *h_reduce = nullptr;          // pinned
+    bool in_cell_order = false;          // the state is in the order of the last sort (X.offsets)
+    // batched contexts (one case otherwise): per-case ranges and offsets
+    std::vector<int32_t> case_first, case_count, case_seg_first, case_seg_count, case_node_first, case_node_count;
+    std::vector<double> case_offset;                 // [n_cases][2]
+    std::vector<uint16_t> case_of_col_h;             // [nx]
+    int32_t *case_cell_bound = nullptr;              // [n_cases + 1] first cell of each case's columns
+    int32_t *case_part_bound = nullptr;              // [n_cases + 1] prefix of case particle counts
+    double *case_reduce = nullptr;                   // [n_cases][3]
     std::vector<void *> allocs;
     std::string err;
 };
@@ -97,9 +106,46 @@ void geometry_from(const sph_grid_params &g, sph_geom_constants &out) {
 }
 
 void derive(KConsts &K) {
-    K.c0sq = 0.;
+    double c0 = (double)sqrtf((float)(K.c.phys.K / K.c.phys.rho0));   // actions_gpu.cu:228 (float sqrt)
+    K.c0sq = c0 * c0;
     K.inv_wdeltap = 1. / K.c.corr.wdeltap;
     K.eta2 = K.c.corr.eta * K.c.corr.eta;
+    K.inv_dx = 1. / K.g.dx;
+    K.thermal_bc = (K.c.trml_tool.alpha != 0.) ? 1 : 0;
+    KF32 &f = K.f;
+    f.mass = (float)K.c.phys.mass;
+    f.inv_mass = (float)(1.0 / K.c.phys.mass);
+    f.xs_mass = (float)K.c.corr.xspheps * f.mass;
+    f.alpha = (float)K.c.corr.alpha;
+    f.beta = (float)K.c.corr.beta;
+    f.eta2 = (float)K.eta2;
+    f.inv_wdp = (float)K.inv_wdeltap;
+    f.cell = (float)K.g.dx;
+    f.G = (float)K.c.phys.G;
+    f.K_bulk = (float)K.c.phys.K;
+    f.c0sq = (float)K.c0sq;
+    f.stresseps = (float)K.c.corr.stresseps;
+    f.dt = (float)K.dt;
+    f.hdt = (float)(0.5 * K.dt);
+    f.inv_dt = (float)(1.0 / K.dt);
+    f.tq_over_cp = K.c.trml_wp.cp != 0. ? (float)(K.c.trml_wp.tq / K.c.trml_wp.cp) : 0.f;
+    f.alpha_wp = (float)K.c.trml_wp.alpha;
+    f.alpha_tool_sph = (float)K.c.trml_tool_sph.alpha;
+    f.T_init = (float)K.c.trml_wp.T_init;
+    const sph_joco_constants &jc = K.c.joco;
+    f.jc.A = (float)jc.A; f.jc.B = (float)jc.B; f.jc.C = (float)jc.C; f.jc.n = (float)jc.n; f.jc.m = (float)jc.m;
+    f.jc.Tref = (float)jc.Tref;
+    f.jc.inv_dT = (float)(1.0 / (jc.Tmelt - jc.Tref));
+    f.jc.inv_epsdot_ref = (float)(1.0 / jc.eps_dot_ref);
+    f.jc.Tmelt = (float)jc.Tmelt;
+}
+
+void set_case_dt(ToolDev &td, double dt) {
+    td.dt = dt;
+    td.hdt = 0.5 * dt;
+    td.dtf = (float)dt;
+    td.hdtf = (float)(0.5 * dt);
+    td.inv_dtf = (float)(1.0 / dt);
 }
 
 void invalidate_graphs(sph_ctx *ctx) {
@@ -185,6 +231,9 @@ int ensure_fem_temp(sph_ctx *ctx) {
     if (!ctx) return SPH_ERR_INVALID;
 #define REQUIRE_TOOL() \
     if (!ctx->has_tool) return fail(ctx, SPH_ERR_STATE, "context has no tool");
+// Calls that take one time step or one tool for the whole context.
+#define REQUIRE_SINGLE_CASE() \
+    if (ctx->K.n_cases > 1) return fail(ctx, SPH_ERR_STATE, "batched context: only the fused step runs per case");
 
 SortedFields &CUR(sph_ctx *ctx) { return ctx->buf[ctx->cur]; }
 
@@ -196,17 +245,17 @@ int issue_fused_body(sph_ctx *ctx, int64_t &n) {
     SortedFields &B = ctx->buf[1 - ctx->cur];
     launch_sort_rest(s, N, ctx->X, ctx->K.g, ctx->F.idx, ctx->W.status);
     n += 5;
-    launch_gather_fused(s, N, ctx->F.idx, ctx->K, A, B, ctx->F, ctx->W, ctx->X.hash_next);
+    launch_gather_fused(s, N, ctx->F.idx, ctx->K, A, B, ctx->F, ctx->W, ctx->X.hash_next, ctx->tool_dev);
     n += 1;
     if (ctx->has_tool) {
-        launch_fem_half(s, ctx->fem, 0.5 * ctx->K.dt);
+        launch_fem_half(s, ctx->K, ctx->fem, ctx->tool_dev);
         n += 1;
     }
     launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, ctx->seg, ctx->tool_dev, true);
     n += 1;
     if (ctx->has_tool) {
-        launch_fem_rate_update(s, ctx->K, ctx->fem, ctx->seg, ctx->K.dt);
-        launch_tool_move(s, ctx->seg, ctx->fem, ctx->tool_dev, ctx->K.dt, 3);
+        launch_fem_rate_update(s, ctx->K, ctx->fem, ctx->seg, ctx->tool_dev);
+        launch_tool_move(s, ctx->K, ctx->seg, ctx->fem, ctx->tool_dev, ctx->K.dt, 3, true);
         n += 2;
     }
     CK(cudaMemsetAsync(ctx->X.counts, 0, sizeof(int32_t) * (size_t)(ctx->K.g.num_cell + 1), s));
@@ -306,14 +355,22 @@ int sph_ctx_destroy(sph_ctx *ctx) {
     return SPH_OK;
 }
 
-int sph_ctx_create(const sph_constants *c, const sph_grid_params *g, const sph_particles *host,
-                   const sph_tool_mesh *tool, double dt, int32_t precision, int32_t device, sph_ctx **out) {
-    if (!c || !g || !host || !out) return SPH_ERR_INVALID;
-    *out = nullptr;
-    if (host->N <= 0) return SPH_ERR_INVALID;
-    if (precision != SPH_PREC_FP64 && precision != SPH_PREC_FP32K) return SPH_ERR_INVALID;
+}  // extern "C"
+
+namespace {
+
+int check_cell_params(const sph_grid_params *g) {
     if (g->cell_factor < 1 || g->stencil < 1 || !(g->h > 0)) return SPH_ERR_INVALID;
     if ((double)g->stencil * (double)g->cell_factor < 2.0) return SPH_ERR_INVALID;   // stencil must cover 2h
+    if (g->stencil > kMaxStencil) return SPH_ERR_INVALID;
+    return SPH_OK;
+}
+
+// Device checks, particle / sort / scratch allocation (particle_gpu ctor,
+// particle_gpu.cu:11-104, and the Green grid buffers) for N particles on the
+// cell geometry `geo`.  On SPH_OK or a context-reported error *out is set.
+int ctx_begin(const sph_constants *c, const sph_grid_params *g, const sph_geom_constants &geo, int N, double dt,
+              int32_t precision, int32_t device, sph_ctx **out) {
     sph_ctx *ctx = new sph_ctx();
     ctx->device = device;
     int ndev = 0;
@@ -332,15 +389,15 @@ int sph_ctx_create(const sph_constants *c, const sph_grid_params *g, const sph_p
     }
     *out = ctx;   // from here on errors are reported through ctx (caller destroys)
     CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
-    const int N = host->N;
     ctx->N = N;
     ctx->grid = *g;
     ctx->K.c = *c;
-    geometry_from(*g, ctx->K.g);
-    if (ctx->K.g.nx <= 0 || ctx->K.g.ny <= 0 || (int64_t)ctx->K.g.nx * ctx->K.g.ny > (int64_t)1 << 30)
+    ctx->K.g = geo;
+    if (geo.nx <= 0 || geo.ny <= 0 || (int64_t)geo.nx * geo.ny > (int64_t)1 << 30)
         return fail(ctx, SPH_ERR_INVALID, "grid geometry out of range");
     ctx->K.dt = dt;
     ctx->K.precision = precision;
+    ctx->K.n_cases = 1;
     derive(ctx->K);
     // particle arrays (particle_gpu ctor, particle_gpu.cu:11-104) and the Green buffer
     for (int b = 0; b < 2; b++) {
@@ -373,14 +430,14 @@ int sph_ctx_create(const sph_constants *c, const sph_grid_params *g, const sph_p
         CK(cudaMemcpyAsync(ctx->F.idx, seq.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
     }
-    r = sph_upload_particles(ctx, host);
-    if (r) return r;
-    // tool
-    CK(cudaMalloc((void **)&ctx->tool_dev, sizeof(ToolDev)));
-    ToolDev td{};
-    if (tool) {
-        r = build_tool_model(*tool, c->tool, ctx->tool_host, ctx->err);
-        if (r) return r;
+    return SPH_OK;
+}
+
+// Uploads the tool model ctx->tool_host (segments, FEM system, node ->
+// segment lists) and the per-case kinematic states `tds` (one per case).
+int ctx_upload_tool(sph_ctx *ctx, bool with_model, const std::vector<ToolDev> &tds) {
+    CK(cudaMalloc((void **)&ctx->tool_dev, sizeof(ToolDev) * tds.size()));
+    if (with_model) {
         ToolModelHost &M = ctx->tool_host;
         ctx->has_tool = true;
         ctx->K.has_tool = 1;
@@ -414,19 +471,117 @@ int sph_ctx_create(const sph_constants *c, const sph_grid_params *g, const sph_p
         CK(cudaMemcpy(Fm.node_seg_ptr, M.node_seg_ptr.data(), sizeof(int) * (M.n_nodes + 1), cudaMemcpyHostToDevice));
         if (!M.node_seg.empty())
             CK(cudaMemcpy(Fm.node_seg, M.node_seg.data(), sizeof(int) * M.node_seg.size(), cudaMemcpyHostToDevice));
-        td.tl_point_ref[0] = M.tl_point_ref[0]; td.tl_point_ref[1] = M.tl_point_ref[1];
-        td.br_point[0] = M.br_point[0]; td.br_point[1] = M.br_point[1];
-        td.ref_dist = M.ref_dist; td.lowest_point = M.lowest_point; td.right_point = M.right_point;
     }
-    CK(cudaMemcpy(ctx->tool_dev, &td, sizeof(ToolDev), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->tool_dev, tds.data(), sizeof(ToolDev) * tds.size(), cudaMemcpyHostToDevice));
     CK(cudaDeviceSynchronize());
     return SPH_OK;
 }
 
+// Kinematic state of a tool model (tool_FEM.h:57-77) on case slots
+// [seg_first, seg_first + seg_count).
+ToolDev tool_state_of(const ToolModelHost &M, double dt, int seg_first) {
+    ToolDev td{};
+    td.tl_point_ref[0] = M.tl_point_ref[0]; td.tl_point_ref[1] = M.tl_point_ref[1];
+    td.br_point[0] = M.br_point[0]; td.br_point[1] = M.br_point[1];
+    td.ref_dist = M.ref_dist; td.lowest_point = M.lowest_point; td.right_point = M.right_point;
+    td.seg_first = seg_first;
+    td.seg_count = M.n_seg;
+    set_case_dt(td, dt);
+    return td;
+}
+
+// Appends tool model `b` to `a` (block-diagonal FEM system, shifted node,
+// element, nonzero and segment ids).
+void append_tool_model(ToolModelHost &a, const ToolModelHost &b) {
+    const int no = a.n_nodes, ne = a.n_elements, nz = (int)a.col_ind.size(), ns = a.n_seg;
+    const int nsl = (int)a.node_seg.size();
+    a.pos.insert(a.pos.end(), b.pos.begin(), b.pos.end());
+    for (const Int4 &e : b.elements) a.elements.push_back({e.x + no, e.y + no, e.z + no, e.w});
+    if (a.row_ptr.empty()) a.row_ptr.push_back(0);
+    for (size_t i = 1; i < b.row_ptr.size(); i++) a.row_ptr.push_back(b.row_ptr[i] + nz);
+    for (int c : b.col_ind) a.col_ind.push_back(c + no);
+    for (int d : b.diag) a.diag.push_back(d + nz);
+    a.K.insert(a.K.end(), b.K.begin(), b.K.end());
+    a.M.insert(a.M.end(), b.M.begin(), b.M.end());
+    a.M_inv.insert(a.M_inv.end(), b.M_inv.begin(), b.M_inv.end());
+    a.f.insert(a.f.end(), b.f.begin(), b.f.end());
+    a.T.insert(a.T.end(), b.T.begin(), b.T.end());
+    a.left.insert(a.left.end(), b.left.begin(), b.left.end());
+    a.right.insert(a.right.end(), b.right.begin(), b.right.end());
+    a.normal.insert(a.normal.end(), b.normal.begin(), b.normal.end());
+    for (const Int4 &m : b.marks) a.marks.push_back({m.x + ne, m.y, m.z + no, m.w + no});
+    if (a.node_seg_ptr.empty()) a.node_seg_ptr.push_back(0);
+    for (size_t i = 1; i < b.node_seg_ptr.size(); i++) a.node_seg_ptr.push_back(b.node_seg_ptr[i] + nsl);
+    for (int s : b.node_seg) a.node_seg.push_back(s + ns);
+    a.n_nodes += b.n_nodes;
+    a.n_elements += b.n_elements;
+    a.n_seg += b.n_seg;
+    a.n_colors = std::max(a.n_colors, b.n_colors);
+    a.n_cut_colors = std::max(a.n_cut_colors, b.n_cut_colors);
+}
+
+// Uploads the per-case reduction bounds (cells of each case's columns and the
+// upload order's particle ranges) from the host case tables.
+int finish_cases(sph_ctx *ctx, const std::vector<int32_t> &cell_bound) {
+    const int n = (int)ctx->case_first.size();
+    std::vector<int32_t> part_bound(n + 1, 0);
+    for (int k = 0; k < n; k++) part_bound[k + 1] = part_bound[k] + ctx->case_count[k];
+    DALLOC(ctx->case_cell_bound, (size_t)n + 1);
+    DALLOC(ctx->case_part_bound, (size_t)n + 1);
+    DALLOC(ctx->case_reduce, (size_t)3 * n);
+    CK(cudaMemcpy(ctx->case_cell_bound, cell_bound.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->case_part_bound, part_bound.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice));
+    return SPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sph_ctx_create(const sph_constants *c, const sph_grid_params *g, const sph_particles *host,
+                   const sph_tool_mesh *tool, double dt, int32_t precision, int32_t device, sph_ctx **out) {
+    if (!c || !g || !host || !out) return SPH_ERR_INVALID;
+    *out = nullptr;
+    if (host->N <= 0) return SPH_ERR_INVALID;
+    if (precision != SPH_PREC_FP64 && precision != SPH_PREC_FP32K) return SPH_ERR_INVALID;
+    if (check_cell_params(g)) return SPH_ERR_INVALID;
+    sph_geom_constants geo;
+    geometry_from(*g, geo);
+    int r = ctx_begin(c, g, geo, host->N, dt, precision, device, out);
+    sph_ctx *ctx = *out;
+    if (r) return r;
+    r = sph_upload_particles(ctx, host);
+    if (r) return r;
+    if (tool) {
+        r = build_tool_model(*tool, c->tool, ctx->tool_host, ctx->err);
+        if (r) return r;
+    }
+    std::vector<ToolDev> tds(1, tool ? tool_state_of(ctx->tool_host, dt, 0) : ToolDev{});
+    if (!tool) set_case_dt(tds[0], dt);
+    r = ctx_upload_tool(ctx, tool != nullptr, tds);
+    if (r) return r;
+    ctx->case_first = {0};
+    ctx->case_count = {ctx->N};
+    ctx->case_offset = {0., 0.};
+    ctx->case_seg_first = {0};
+    ctx->case_seg_count = {ctx->seg.n};
+    ctx->case_node_first = {0};
+    ctx->case_node_count = {ctx->fem.n_nodes};
+    return finish_cases(ctx, {0, ctx->K.g.num_cell});
+}
+
 int sph_set_dt(sph_ctx *ctx, double dt) {
     REQUIRE_CTX();
+    REQUIRE_SINGLE_CASE();
     ctx->K.dt = dt;
+    derive(ctx->K);
     invalidate_graphs(ctx);
+    ToolDev td;
+    CK(cudaMemcpyAsync(&td, ctx->tool_dev, sizeof(ToolDev), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    set_case_dt(td, dt);
+    CK(cudaMemcpyAsync(ctx->tool_dev, &td, sizeof(ToolDev), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     return SPH_OK;
 }
 
@@ -494,6 +649,7 @@ int sph_upload_particles(sph_ctx *ctx, const sph_particles *host) {
     }
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->counts_valid = false;
+    ctx->in_cell_order = false;
     return SPH_OK;
 }
 
@@ -554,6 +710,7 @@ int sph_sort(sph_ctx *ctx) {
     CK_LAUNCH();
     ctx->cur = 1 - ctx->cur;   // double_buffer swap (grid_gpu_green.cu:152-182)
     ctx->counts_valid = false;
+    ctx->in_cell_order = true;
     return SPH_OK;
 }
 
@@ -568,6 +725,7 @@ int sph_init(sph_ctx *ctx) {
 
 int sph_predict(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_SINGLE_CASE();
     launch_predict_correct(ctx->stream, ctx->N, CUR(ctx), ctx->W, 0.5 * ctx->K.dt);
     ctx->launches++;
     ctx->counts_valid = false;
@@ -577,6 +735,7 @@ int sph_predict(sph_ctx *ctx) {
 
 int sph_correct(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_SINGLE_CASE();
     launch_predict_correct(ctx->stream, ctx->N, CUR(ctx), ctx->W, ctx->K.dt);
     ctx->launches++;
     ctx->counts_valid = false;
@@ -616,6 +775,7 @@ int sph_perform_boundary_conditions_thermal(sph_ctx *ctx) {
 
 int sph_plasticity_johnson_cook(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_SINGLE_CASE();
     if (!ctx->K.c.plastic) return SPH_OK;   // m_plastic off (actions_gpu.cu:874-879)
     launch_plasticity(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->F, ctx->W);
     ctx->launches++;
@@ -626,6 +786,7 @@ int sph_plasticity_johnson_cook(sph_ctx *ctx) {
 
 int sph_interactions_monaghan(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_SINGLE_CASE();
     launch_build_records(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->F, ctx->W);
     launch_interactions(ctx->stream, ctx->N, ctx->K, ctx->X.offsets, CUR(ctx), ctx->F, ctx->W, ctx->seg,
                         ctx->tool_dev, false);
@@ -638,6 +799,7 @@ int sph_interactions_monaghan(sph_ctx *ctx) {
 // ---- tool -------------------------------------------------------------------------------------
 int sph_material_fric_heat_gen_fem(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_SINGLE_CASE();
     REQUIRE_TOOL();
     launch_fric_heat(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->seg, ctx->tool_dev, ctx->W.status);
     ctx->launches++;
@@ -648,6 +810,7 @@ int sph_material_fric_heat_gen_fem(sph_ctx *ctx) {
 
 int sph_compute_contact_forces_fem(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_SINGLE_CASE();
     REQUIRE_TOOL();
     launch_contact(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->W.status);
     ctx->launches += 2;
@@ -658,8 +821,9 @@ int sph_compute_contact_forces_fem(sph_ctx *ctx) {
 
 int sph_segments_update(sph_ctx *ctx, double dt) {
     REQUIRE_CTX();
+    REQUIRE_SINGLE_CASE();
     REQUIRE_TOOL();
-    launch_tool_move(ctx->stream, ctx->seg, ctx->fem, ctx->tool_dev, dt, 1);
+    launch_tool_move(ctx->stream, ctx->K, ctx->seg, ctx->fem, ctx->tool_dev, dt, 1, false);
     ctx->launches++;
     CK_LAUNCH();
     return SPH_OK;
@@ -667,8 +831,9 @@ int sph_segments_update(sph_ctx *ctx, double dt) {
 
 int sph_tool_update_fem(sph_ctx *ctx, double dt) {
     REQUIRE_CTX();
+    REQUIRE_SINGLE_CASE();
     REQUIRE_TOOL();
-    launch_tool_move(ctx->stream, ctx->seg, ctx->fem, ctx->tool_dev, dt, 2);
+    launch_tool_move(ctx->stream, ctx->K, ctx->seg, ctx->fem, ctx->tool_dev, dt, 2, false);
     ctx->launches++;
     CK_LAUNCH();
     return SPH_OK;
@@ -709,6 +874,7 @@ int sph_fem_calculate_temp_rate(sph_ctx *ctx) {
 
 int sph_fem_calculate_temp(sph_ctx *ctx, double dt) {
     REQUIRE_CTX();
+    REQUIRE_SINGLE_CASE();
     REQUIRE_TOOL();
     int r = ensure_fem_temp(ctx);
     if (r) return r;
@@ -720,6 +886,7 @@ int sph_fem_calculate_temp(sph_ctx *ctx, double dt) {
 
 int sph_set_tool_velocity(sph_ctx *ctx, double vx, double vy) {
     REQUIRE_CTX();
+    REQUIRE_SINGLE_CASE();
     double v[2] = {vx, vy};
     CK(cudaMemcpyAsync(ctx->tool_dev, v, sizeof(v), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -859,6 +1026,7 @@ int sph_step(sph_ctx *ctx) {
     }
     ctx->cur = 1 - ctx->cur;
     ctx->counts_valid = true;
+    ctx->in_cell_order = true;
     return SPH_OK;
 }
 
@@ -883,15 +1051,15 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
         CK(cudaEventRecord(ev[1], s));
         launch_sort_rest(s, N, ctx->X, ctx->K.g, ctx->F.idx, ctx->W.status);
         CK(cudaEventRecord(ev[2], s));
-        launch_gather_fused(s, N, ctx->F.idx, ctx->K, A, B, ctx->F, ctx->W, ctx->X.hash_next);
+        launch_gather_fused(s, N, ctx->F.idx, ctx->K, A, B, ctx->F, ctx->W, ctx->X.hash_next, ctx->tool_dev);
         CK(cudaEventRecord(ev[3], s));
-        if (ctx->has_tool) launch_fem_half(s, ctx->fem, 0.5 * ctx->K.dt);
+        if (ctx->has_tool) launch_fem_half(s, ctx->K, ctx->fem, ctx->tool_dev);
         CK(cudaEventRecord(ev[4], s));
         launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, ctx->seg, ctx->tool_dev, true);
         CK(cudaEventRecord(ev[5], s));
         if (ctx->has_tool) {
-            launch_fem_rate_update(s, ctx->K, ctx->fem, ctx->seg, ctx->K.dt);
-            launch_tool_move(s, ctx->seg, ctx->fem, ctx->tool_dev, ctx->K.dt, 3);
+            launch_fem_rate_update(s, ctx->K, ctx->fem, ctx->seg, ctx->tool_dev);
+            launch_tool_move(s, ctx->K, ctx->seg, ctx->fem, ctx->tool_dev, ctx->K.dt, 3, true);
         }
         CK(cudaEventRecord(ev[6], s));
         CK(cudaMemsetAsync(ctx->X.counts, 0, sizeof(int32_t) * (size_t)(ctx->K.g.num_cell + 1), s));
@@ -907,6 +1075,7 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
         }
         ctx->cur = 1 - ctx->cur;
         ctx->counts_valid = true;
+        ctx->in_cell_order = true;
     }
     for (auto &e : ev) cudaEventDestroy(e);
     return SPH_OK;
@@ -923,6 +1092,7 @@ int sph_run(sph_ctx *ctx, int32_t nsteps) {
 
 int sph_step_staged(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_SINGLE_CASE();
     int r;
 #define RUN(x)            \
     if ((r = (x)) != SPH_OK) return r;
@@ -999,6 +1169,233 @@ int sph_reduce_max_T(sph_ctx *ctx, double *out) {
     int r = reduce_force_T(ctx, r3);
     if (r) return r;
     *out = r3[2];
+    return SPH_OK;
+}
+
+// ---- batched multi-case contexts ------------------------------------------------------------------
+int sph_batch_create(const sph_constants *c, const sph_grid_params *cell, int32_t n_cases,
+                     const sph_case_desc *cases, int32_t precision, int32_t device, sph_ctx **out) {
+    if (!c || !cell || !cases || !out || n_cases < 1 || n_cases > 65535) return SPH_ERR_INVALID;
+    *out = nullptr;
+    if (precision != SPH_PREC_FP32K) return SPH_ERR_INVALID;   // per-case time steps live in the FP32K path
+    if (check_cell_params(cell)) return SPH_ERR_INVALID;
+    const bool with_tool = cases[0].tool != nullptr;
+    int64_t n_total = 0;
+    for (int k = 0; k < n_cases; k++) {
+        const sph_case_desc &d = cases[k];
+        if (!d.host || d.host->N <= 0 || !(d.dt > 0)) return SPH_ERR_INVALID;
+        if ((d.tool != nullptr) != with_tool) return SPH_ERR_INVALID;
+        if (!(d.bbmax[0] > d.bbmin[0]) || !(d.bbmax[1] > d.bbmin[1])) return SPH_ERR_INVALID;
+        n_total += d.host->N;
+    }
+    if (n_total > (int64_t)1 << 30) return SPH_ERR_INVALID;
+    // layout: case k gets columns [col0[k], col0[k] + nx_k) of one global
+    // grid, gaps of stencil + 1 columns between cases, bottoms aligned
+    const double gx0 = cases[0].bbmin[0], gy0 = cases[0].bbmin[1];
+    const int gap = cell->stencil + 1;
+    std::vector<int> col0(n_cases), ncol(n_cases);
+    std::vector<double> offs(2 * (size_t)n_cases);
+    sph_geom_constants geo;
+    geometry_from(*cell, geo);   // dx and stencil; extents set below
+    int cols = 0, rows = 0;
+    for (int k = 0; k < n_cases; k++) {
+        sph_grid_params gk = *cell;
+        for (int a = 0; a < 2; a++) {
+            gk.bbmin[a] = cases[k].bbmin[a];
+            gk.bbmax[a] = cases[k].bbmax[a];
+        }
+        sph_geom_constants ck;
+        geometry_from(gk, ck);
+        if (k) cols += gap;
+        col0[k] = cols;
+        ncol[k] = ck.nx;
+        cols += ck.nx;
+        rows = std::max(rows, ck.ny);
+        offs[2 * k] = (gx0 + (double)col0[k] * geo.dx) - cases[k].bbmin[0];
+        offs[2 * k + 1] = gy0 - cases[k].bbmin[1];
+        if ((int64_t)cols * std::max(rows, 1) > (int64_t)1 << 30) return SPH_ERR_INVALID;
+    }
+    geo.nx = cols;
+    geo.ny = rows;
+    geo.bbmin_x = gx0 - 1e-6;
+    geo.bbmin_y = gy0 - 1e-6;
+    geo.num_cell = cols * rows;
+    sph_grid_params g = *cell;
+    g.bbmin[0] = gx0;
+    g.bbmin[1] = gy0;
+    g.bbmax[0] = gx0 + (double)cols * geo.dx - 2e-6;
+    g.bbmax[1] = gy0 + (double)rows * geo.dx - 2e-6;
+    int r = ctx_begin(c, &g, geo, (int)n_total, cases[0].dt, precision, device, out);
+    sph_ctx *ctx = *out;
+    if (r) return r;
+    ctx->K.n_cases = n_cases;
+    // tool models, each moved by its case offset and appended
+    std::vector<ToolDev> tds(n_cases);
+    ctx->case_seg_first.assign(n_cases, 0);
+    ctx->case_seg_count.assign(n_cases, 0);
+    ctx->case_node_first.assign(n_cases, 0);
+    ctx->case_node_count.assign(n_cases, 0);
+    for (int k = 0; k < n_cases; k++) {
+        const sph_case_desc &d = cases[k];
+        ToolDev td{};
+        if (with_tool) {
+            const sph_tool_mesh &m = *d.tool;
+            if (m.n_nodes <= 0 || !m.nodes) return fail(ctx, SPH_ERR_INVALID, "batch: empty tool mesh");
+            std::vector<double> nodes(2 * (size_t)m.n_nodes);
+            for (int i = 0; i < m.n_nodes; i++) {
+                nodes[2 * i] = m.nodes[2 * i] + offs[2 * k];
+                nodes[2 * i + 1] = m.nodes[2 * i + 1] + offs[2 * k + 1];
+            }
+            sph_tool_mesh mk = m;
+            mk.nodes = nodes.data();
+            mk.tl[0] = m.tl[0] + offs[2 * k];
+            mk.tl[1] = m.tl[1] + offs[2 * k + 1];
+            ToolModelHost Mk;
+            r = build_tool_model(mk, c->tool, Mk, ctx->err);
+            if (r) return r;
+            ctx->case_seg_first[k] = ctx->tool_host.n_seg;
+            ctx->case_seg_count[k] = Mk.n_seg;
+            ctx->case_node_first[k] = ctx->tool_host.n_nodes;
+            ctx->case_node_count[k] = Mk.n_nodes;
+            td = tool_state_of(Mk, d.dt, ctx->tool_host.n_seg);
+            append_tool_model(ctx->tool_host, Mk);
+        } else {
+            set_case_dt(td, d.dt);
+        }
+        td.vel[0] = d.tool_vel[0];
+        td.vel[1] = d.tool_vel[1];
+        tds[k] = td;
+    }
+    // particles, concatenated in case order and moved by the case offsets
+    const int N = (int)n_total;
+    ctx->case_first.assign(n_cases, 0);
+    ctx->case_count.assign(n_cases, 0);
+    ctx->case_offset = offs;
+    {
+        int first = 0;
+        for (int k = 0; k < n_cases; k++) {
+            ctx->case_first[k] = first;
+            ctx->case_count[k] = cases[k].host->N;
+            first += cases[k].host->N;
+        }
+    }
+    sph_particles cat;
+    std::memset(&cat, 0, sizeof(cat));
+    cat.N = N;
+    std::vector<std::vector<char>> store;
+    for (const FieldDesc &fd : kFields) {
+        if (fd.off_view == offsetof(sph_particles, idx) || fd.off_view == offsetof(sph_particles, hash)) continue;
+        bool any = false;
+        for (int k = 0; k < n_cases; k++) any |= member<const void *>(*cases[k].host, fd.off_view) != nullptr;
+        if (!any) continue;
+        const size_t esz = (size_t)fd.width * (fd.is_int ? 4 : 8);
+        store.emplace_back((size_t)N * esz, 0);
+        char *dst = store.back().data();
+        for (int k = 0; k < n_cases; k++) {
+            const char *src = member<const char *>(*cases[k].host, fd.off_view);
+            char *at = dst + (size_t)ctx->case_first[k] * esz;
+            const size_t nk = (size_t)cases[k].host->N;
+            if (src) std::memcpy(at, src, nk * esz);
+            if (fd.off_view == offsetof(sph_particles, pos)) {
+                double *p = (double *)at;
+                for (size_t i = 0; i < nk; i++) {
+                    p[2 * i] += offs[2 * k];
+                    p[2 * i + 1] += offs[2 * k + 1];
+                }
+            } else if (fd.off_view == offsetof(sph_particles, on_seg) && src) {
+                int32_t *q = (int32_t *)at;
+                for (size_t i = 0; i < nk; i++)
+                    if (q[i] >= 0) q[i] += ctx->case_seg_first[k];
+            }
+        }
+        *(void **)((char *)&cat + fd.off_view) = (void *)dst;
+    }
+    r = sph_upload_particles(ctx, &cat);
+    if (r) return r;
+    r = ctx_upload_tool(ctx, with_tool, tds);
+    if (r) return r;
+    // case tables: columns split in the middle of each gap; nodes; segments
+    ctx->case_of_col_h.assign(cols, 0);
+    std::vector<int32_t> cell_bound(n_cases + 1);
+    for (int k = 0; k < n_cases; k++) {
+        int b = k ? col0[k] - (gap + 1) / 2 : 0;
+        int e = (k + 1 < n_cases) ? col0[k + 1] - (gap + 1) / 2 : cols;
+        for (int ix = b; ix < e; ix++) ctx->case_of_col_h[ix] = (uint16_t)k;
+        cell_bound[k] = b * rows;
+        if (k + 1 == n_cases) cell_bound[k + 1] = cols * rows;
+    }
+    uint16_t *d_col = nullptr, *d_node = nullptr, *d_seg = nullptr;
+    DALLOC(d_col, (size_t)cols);
+    CK(cudaMemcpy(d_col, ctx->case_of_col_h.data(), sizeof(uint16_t) * cols, cudaMemcpyHostToDevice));
+    ctx->K.case_of_col = d_col;
+    if (with_tool) {
+        std::vector<uint16_t> cn(ctx->tool_host.n_nodes), cs(ctx->tool_host.n_seg);
+        for (int k = 0; k < n_cases; k++) {
+            for (int i = 0; i < ctx->case_node_count[k]; i++) cn[ctx->case_node_first[k] + i] = (uint16_t)k;
+            for (int i = 0; i < ctx->case_seg_count[k]; i++) cs[ctx->case_seg_first[k] + i] = (uint16_t)k;
+        }
+        DALLOC(d_node, cn.size());
+        DALLOC(d_seg, cs.size());
+        CK(cudaMemcpy(d_node, cn.data(), sizeof(uint16_t) * cn.size(), cudaMemcpyHostToDevice));
+        if (!cs.empty()) CK(cudaMemcpy(d_seg, cs.data(), sizeof(uint16_t) * cs.size(), cudaMemcpyHostToDevice));
+        ctx->K.case_of_node = d_node;
+        ctx->K.case_of_seg = d_seg;
+    }
+    return finish_cases(ctx, cell_bound);
+}
+
+int sph_batch_n_cases(const sph_ctx *ctx, int32_t *n_cases) {
+    if (!ctx || !n_cases) return SPH_ERR_INVALID;
+    *n_cases = ctx->K.n_cases;
+    return SPH_OK;
+}
+
+int sph_batch_case_info(const sph_ctx *ctx, int32_t k, int32_t *first, int32_t *count, double offset[2],
+                        int32_t *seg_first, int32_t *seg_count, int32_t *node_first, int32_t *node_count) {
+    if (!ctx || k < 0 || k >= (int32_t)ctx->case_first.size()) return SPH_ERR_INVALID;
+    if (first) *first = ctx->case_first[k];
+    if (count) *count = ctx->case_count[k];
+    if (offset) {
+        offset[0] = ctx->case_offset[2 * k];
+        offset[1] = ctx->case_offset[2 * k + 1];
+    }
+    if (seg_first) *seg_first = ctx->case_seg_first[k];
+    if (seg_count) *seg_count = ctx->case_seg_count[k];
+    if (node_first) *node_first = ctx->case_node_first[k];
+    if (node_count) *node_count = ctx->case_node_count[k];
+    return SPH_OK;
+}
+
+int sph_batch_reduce(sph_ctx *ctx, double *out) {
+    REQUIRE_CTX();
+    if (!out) return SPH_ERR_INVALID;
+    const int n = (int)ctx->case_first.size();
+    launch_reduce_cases(ctx->stream, n, CUR(ctx), ctx->in_cell_order ? ctx->X.offsets : nullptr,
+                        ctx->case_cell_bound, ctx->case_part_bound, ctx->case_reduce);
+    ctx->launches++;
+    CK_LAUNCH();
+    CK(cudaMemcpyAsync(out, ctx->case_reduce, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+int sph_batch_case_of_particles(sph_ctx *ctx, int32_t *case_of) {
+    REQUIRE_CTX();
+    if (!case_of) return SPH_ERR_INVALID;
+    const int n = (int)ctx->case_first.size();
+    if (!ctx->in_cell_order || n == 1) {
+        for (int k = 0; k < n; k++)
+            for (int i = 0; i < ctx->case_count[k]; i++) case_of[ctx->case_first[k] + i] = k;
+        return SPH_OK;
+    }
+    CK(cudaMemcpyAsync(case_of, CUR(ctx).hash, sizeof(int32_t) * ctx->N, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const int nx = ctx->K.g.nx, ny = ctx->K.g.ny;
+    for (int i = 0; i < ctx->N; i++) {   // the device's case_of_hash
+        int ix = case_of[i] / ny;
+        ix = ix < 0 ? 0 : (ix >= nx ? nx - 1 : ix);
+        case_of[i] = ctx->case_of_col_h[ix];
+    }
     return SPH_OK;
 }
 

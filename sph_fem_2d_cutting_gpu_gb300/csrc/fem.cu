@@ -33,17 +33,24 @@ __device__ __forceinline__ void robin_terms(const KConsts &K, const FemDev &F, c
 
 // calculate_temp(0.5*dt) at the start of the step (FEM_thermal_gpu.cu:460-468,
 // with T_old == T right after reset_FEM_server): T_half = 0.5 dt k + T.
-__global__ void __launch_bounds__(kBlock) k_fem_half(FemDev F, double hdt) {
+// Time step of the case a node belongs to (one case unless batched).
+__device__ __forceinline__ const ToolDev &node_case(const KConsts &K, const ToolDev *tool, int i) {
+    return tool[K.case_of_node ? K.case_of_node[i] : 0];
+}
+
+__global__ void __launch_bounds__(kBlock) k_fem_half(KConsts K, FemDev F, const ToolDev *__restrict__ tool) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.n_nodes) return;
-    F.T_half[i] = hdt * F.k[i] + F.T[i];
+    F.T_half[i] = node_case(K, tool, i).hdt * F.k[i] + F.T[i];
 }
 
 // apply_robin_bdc + calculate_temp_rate + calculate_temp(dt), one row per
 // thread (FEM_thermal_gpu.cu:342-386,443-468).  Reads T_half, writes k and T.
-__global__ void __launch_bounds__(kBlock) k_fem_rate_update(KConsts K, FemDev F, SegDev seg, double dt) {
+__global__ void __launch_bounds__(kBlock) k_fem_rate_update(KConsts K, FemDev F, SegDev seg,
+                                                            const ToolDev *__restrict__ tool) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.n_nodes) return;
+    const double dt = node_case(K, tool, i).dt;
     double df, dk;
     robin_terms(K, F, seg, i, df, dk);
     double buffer = 0.;
@@ -123,22 +130,30 @@ __device__ __forceinline__ void tool_state_move(ToolDev *tool, double dt) {
     tool->right_point = add_mul_rn(tool->right_point, vx, dt);
 }
 
-// what = 1: segments only; 2: nodes + tool state only; 3: both (fused step).
-__global__ void __launch_bounds__(kBlock) k_tool_move(SegDev seg, FemDev F, ToolDev *tool, double dt, int what) {
+// what = 1: segments only; 2: nodes + tool state only; 3: both.  With
+// per_case the velocity and time step of each segment's / node's case are
+// used (the fused step, batched or not); otherwise case 0 with `dt`.
+__global__ void __launch_bounds__(kBlock) k_tool_move(KConsts K, SegDev seg, FemDev F, ToolDev *tool, double dt,
+                                                      int what, int per_case) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double vel[2] = {tool->vel[0], tool->vel[1]};
-    if ((what & 1) && i < seg.n) segment_move(seg, i, vel, dt);
-    if ((what & 2) && i < F.n_nodes) node_move(F, i, vel, dt);
-    __syncthreads();
-    if ((what & 2) && i == 0) tool_state_move(tool, dt);
+    if ((what & 1) && i < seg.n) {
+        const ToolDev &tc = tool[(per_case && K.case_of_seg) ? K.case_of_seg[i] : 0];
+        segment_move(seg, i, tc.vel, per_case ? tc.dt : dt);
+    }
+    if ((what & 2) && i < F.n_nodes) {
+        const ToolDev &tc = tool[(per_case && K.case_of_node) ? K.case_of_node[i] : 0];
+        node_move(F, i, tc.vel, per_case ? tc.dt : dt);
+    }
+    if ((what & 2) && i < (per_case ? K.n_cases : 1)) tool_state_move(tool + i, per_case ? tool[i].dt : dt);
 }
 
 // ---- host launchers ---------------------------------------------------------------------------
-void launch_fem_half(cudaStream_t s, const FemDev &F, double hdt) {
-    k_fem_half<<<div_up(F.n_nodes, kBlock), kBlock, 0, s>>>(F, hdt);
+void launch_fem_half(cudaStream_t s, const KConsts &K, const FemDev &F, const ToolDev *tool) {
+    k_fem_half<<<div_up(F.n_nodes, kBlock), kBlock, 0, s>>>(K, F, tool);
 }
-void launch_fem_rate_update(cudaStream_t s, const KConsts &K, const FemDev &F, const SegDev &seg, double dt) {
-    k_fem_rate_update<<<div_up(F.n_nodes, kBlock), kBlock, 0, s>>>(K, F, seg, dt);
+void launch_fem_rate_update(cudaStream_t s, const KConsts &K, const FemDev &F, const SegDev &seg,
+                            const ToolDev *tool) {
+    k_fem_rate_update<<<div_up(F.n_nodes, kBlock), kBlock, 0, s>>>(K, F, seg, tool);
 }
 void launch_fem_reset(cudaStream_t s, const FemDev &F, double *T_old, double *f_temp, double *K_temp) {
     k_fem_reset<<<div_up(F.nnz > F.n_nodes ? F.nnz : F.n_nodes, kBlock), kBlock, 0, s>>>(F, T_old, f_temp, K_temp);
@@ -153,12 +168,12 @@ void launch_fem_rate(cudaStream_t s, const FemDev &F, const double *f_temp, cons
 void launch_fem_temp(cudaStream_t s, const FemDev &F, const double *T_old, double dt) {
     k_fem_temp<<<div_up(F.n_nodes, kBlock), kBlock, 0, s>>>(F, T_old, dt);
 }
-void launch_tool_move(cudaStream_t s, const SegDev &seg, const FemDev &F, ToolDev *tool, double dt, int what) {
-    int n = 0;
-    if (what & 1) n = seg.n;
+void launch_tool_move(cudaStream_t s, const KConsts &K, const SegDev &seg, const FemDev &F, ToolDev *tool, double dt,
+                      int what, bool per_case) {
+    int n = per_case ? K.n_cases : 1;
+    if ((what & 1) && seg.n > n) n = seg.n;
     if ((what & 2) && F.n_nodes > n) n = F.n_nodes;
-    if (n < 1) n = 1;
-    k_tool_move<<<div_up(n, kBlock), kBlock, 0, s>>>(seg, F, tool, dt, what);
+    k_tool_move<<<div_up(n, kBlock), kBlock, 0, s>>>(K, seg, F, tool, dt, what, per_case ? 1 : 0);
 }
 
 }  // namespace sphfem

@@ -96,7 +96,7 @@ __device__ __forceinline__ void fused_epilogue(int k, const KConsts &K, const So
     double blanked = 0.;
     uint32_t st = 0;
     // friction heat (actions_gpu.cu:345-420), tool runs only
-    if (K.has_tool) st |= fric_heat_one(K, tool->vel, vel, B.ft[k], B.n[k], B.fc[k], rho, B.eps_pl[k], B.on_seg[k],
+    if (K.has_tool) st |= fric_heat_one(K, K.dt, tool->vel, vel, B.ft[k], B.n[k], B.fc[k], rho, B.eps_pl[k], B.on_seg[k],
                                         seg.n, T, blanked, seg.fric_heat);
     // return mapping (actions_gpu.cu:689-754)
     if (K.c.plastic && !is_tool && blanked != 1.) {
@@ -113,6 +113,88 @@ __device__ __forceinline__ void fused_epilogue(int k, const KConsts &K, const So
     B.S[k] = S;
     B.T[k] = T;
     if (blanked == 1.) B.blanked[k] = 1.;
+    if (st) set_status(status, st);
+}
+
+// FP32-compensated epilogue: the rates (Jaumann, continuity, momentum,
+// advection) and the return mapping in FP32; the corrector keeps positions
+// and density in FP64.  vd, sd, vt, xt as in the FP64 epilogue.
+__device__ __forceinline__ void fused_epilogue32(int k, const KConsts &K, const SortedFields &B,
+                                                 const FixedFields &F, const SegDev &seg,
+                                                 const ToolDev *__restrict__ tool, int32_t *__restrict__ secant_iters,
+                                                 uint32_t *status, bool is_tool, float2 vel_pred, float rho_pred,
+                                                 float4 vd, float4 sd, float2 vt, float2 xt, bool thermal, float T_t_new) {
+    const ToolDev &tc = tool[case_of_hash(K, B.hash[k])];   // the particle's case (time step, tool)
+    const double dt = tc.dt;
+    const float dtf = tc.dtf, hdtf = tc.hdtf;
+    const float inv_mass = K.f.inv_mass;
+    const dbl4 S0d = B.S[k];
+    float4 S0 = make_float4((float)S0d.x, (float)S0d.y, (float)S0d.z, (float)S0d.w);
+    float4 St;
+    float2 pos_t, vel_t;
+    double rho_t;
+    if (!is_tool) {
+        const dbl4 Sto = B.S_t[k];
+        float4 Sp = make_float4(fmaf(hdtf, (float)Sto.x, S0.x), fmaf(hdtf, (float)Sto.y, S0.y),
+                                fmaf(hdtf, (float)Sto.z, S0.z), fmaf(hdtf, (float)Sto.w, S0.w));
+        St = jaumann_f32(K.f.G, vd, Sp);
+        rho_t = (double)(-rho_pred * (vd.x + vd.w));
+        const double2 fc = B.fc[k], ft = B.ft[k];
+        vel_t.x = vt.x + ((sd.x + sd.y) + ((float)fc.x + (float)ft.x) * inv_mass);
+        vel_t.y = vt.y + ((sd.z + sd.w) + ((float)fc.y + (float)ft.y) * inv_mass);
+        pos_t.x = xt.x + vel_pred.x;
+        pos_t.y = xt.y + vel_pred.y;
+        B.S_t[k] = mk4(St.x, St.y, St.z, St.w);
+        B.rho_t[k] = rho_t;
+    } else {
+        const dbl4 Sto = B.S_t[k];
+        St = make_float4((float)Sto.x, (float)Sto.y, (float)Sto.z, (float)Sto.w);
+        rho_t = B.rho_t[k];
+        vel_t = vt;
+        pos_t = xt;
+    }
+    const float T_t = thermal ? T_t_new : (float)B.T_t[k];
+    const double2 pos_t_d = make_double2(pos_t.x, pos_t.y);
+    B.pos_t[k] = pos_t_d;
+    B.vel_t[k] = make_double2(vel_t.x, vel_t.y);
+    if (thermal) B.T_t[k] = (double)T_t;
+    // corrector (leap_frog.cu:71-96)
+    double2 pos = B.pos[k];
+    pos.x = pos.x + dt * pos_t_d.x;
+    pos.y = pos.y + dt * pos_t_d.y;
+    B.pos[k] = pos;
+    const double2 v0 = B.vel[k];
+    const float2 vel = make_float2(fmaf(dtf, vel_t.x, (float)v0.x), fmaf(dtf, vel_t.y, (float)v0.y));
+    B.vel[k] = make_double2(vel.x, vel.y);
+    float4 S = make_float4(fmaf(dtf, St.x, S0.x), fmaf(dtf, St.y, S0.y), fmaf(dtf, St.z, S0.z), fmaf(dtf, St.w, S0.w));
+    const double rho = B.rho[k] + dt * rho_t;
+    B.rho[k] = rho;
+    float T = fmaf(dtf, T_t, (float)B.T[k]);
+    uint32_t st = 0;
+    bool blanked = false;
+    if (K.has_tool) {   // friction heat (actions_gpu.cu:345-420) for particles in contact
+        const int on = B.on_seg[k];
+        if (on >= 0 && on < seg.n) {
+            double Td = (double)T, bl = 0.;
+            st |= fric_heat_one(K, dt, tc.vel, make_double2(vel.x, vel.y), B.ft[k], B.n[k], B.fc[k], rho,
+                                B.eps_pl[k], on, seg.n, Td, bl, seg.fric_heat);
+            T = (float)Td;
+            blanked = flag_is_one(bl);
+        }
+    }
+    if (K.c.plastic && !is_tool && !blanked) {   // return mapping (actions_gpu.cu:689-754)
+        const JcF32 &j = K.f.jc;
+        float eps_pl = (float)B.eps_pl[k], eps_pl_dot = (float)B.eps_pl_dot[k];
+        int it = 0;
+        st |= plasticity_f32(K, j, dtf, tc.inv_dtf, S, (float)F.p[k], (float)rho, eps_pl, eps_pl_dot, T, blanked,
+                             &it);
+        B.eps_pl[k] = (double)eps_pl;
+        B.eps_pl_dot[k] = (double)eps_pl_dot;
+        if (secant_iters) secant_iters[k] = it;
+    }
+    B.S[k] = mk4(S.x, S.y, S.z, S.w);
+    B.T[k] = (double)T;
+    if (blanked) B.blanked[k] = 1.;
     if (st) set_status(status, st);
 }
 
@@ -143,18 +225,45 @@ __global__ void __launch_bounds__(kBlock) k_interact64(int N, KConsts K, const i
     Sums64 a = {};
     const int hash = B.hash[k];
     const sph_geom_constants &g = K.g;
+    __shared__ int s_list[kPairChunk][kBlock];
+    int ii = 0, hi_i = 0, lo_j = 0, hi_j = 0, jc = 0, j1 = 0;
+    bool done = true;
     if (hash >= 0 && hash < g.num_cell) {
         const int gi = hash / g.ny, gj = hash - gi * g.ny, R = g.stencil;
-        const int lo_i = max(gi - R, 0), hi_i = min(gi + R + 1, g.nx);
-        const int lo_j = max(gj - R, 0), hi_j = min(gj + R + 1, g.ny);
-        for (int ii = lo_i; ii < hi_i; ii++) {
-            const int c0 = ii * g.ny + lo_j, c1 = ii * g.ny + hi_j;   // cells [c0, c1)
-            const int j0 = __ldg(offsets + c0), j1 = __ldg(offsets + c1);
-            for (int j = j0; j < j1; j++) {
+        ii = max(gi - R, 0);
+        hi_i = min(gi + R + 1, g.nx);
+        lo_j = max(gj - R, 0);
+        hi_j = min(gj + R + 1, g.ny);
+        jc = __ldg(offsets + ii * g.ny + lo_j);
+        j1 = __ldg(offsets + ii * g.ny + hi_j);
+        done = false;
+    }
+    while (!done) {
+        // phase 1: collect the next in-support candidates (columns ii, cells lo_j..hi_j)
+        int cnt = 0;
+        while (cnt < kPairChunk) {
+            if (jc < j1) {
+                const dbl4 n0 = rec[4 * jc + 0];
+                const double dx = xi - n0.x, dy = yi - n0.y;
+                const double rr2 = dx * dx + dy * dy;
+                if (rr2 < fourh2 && rr2 >= 1e-8) s_list[cnt++][threadIdx.x] = jc;
+                jc++;
+            } else {
+                if (++ii >= hi_i) {
+                    done = true;
+                    break;
+                }
+                jc = __ldg(offsets + ii * g.ny + lo_j);
+                j1 = __ldg(offsets + ii * g.ny + hi_j);
+            }
+        }
+        // phase 2: pair body over the list, lanes in step
+        for (int t = 0; t < cnt; t++) {
+            const int j = s_list[t][threadIdx.x];
+            {
                 const dbl4 n0 = rec[4 * j + 0];
                 const double dx = xi - n0.x, dy = yi - n0.y;
                 const double rr2 = dx * dx + dy * dy;
-                if (rr2 >= fourh2 || rr2 < 1e-8) continue;
                 const dbl4 n3 = rec[4 * j + 3];
                 const int fj = (int)__double_as_longlong(n3.w);
                 if (fj & kFlagBlanked) continue;
@@ -247,54 +356,110 @@ __global__ void __launch_bounds__(kBlock) k_interact32(int N, KConsts K, const i
     const float vix = i1.x, viy = i1.y, rhoi = i1.z, ci = i1.w;
     const float sAi = i2.x, sBi = i2.y, sCi = i2.z;
     const float Rxxi = i3.x, Rxyi = i3.y, Ryyi = i3.z, Ti = i3.w;
-    const double thermal_alpha = (!tool_i) ? K.c.trml_wp.alpha : K.c.trml_tool_sph.alpha;
-    const bool thermal = thermal_alpha != 0.;
+    const float thermal_alpha = (!tool_i) ? K.f.alpha_wp : K.f.alpha_tool_sph;
+    const bool thermal = thermal_alpha != 0.f;
     const float h1 = 1.f / hi;
     const float fourh2 = 4.f * hi * hi;
     const float fac = (float)kPiFac * h1 * h1;
-    const float alpha = (float)K.c.corr.alpha, beta = (float)K.c.corr.beta, eta2 = (float)K.eta2;
-    const float inv_wdp = (float)K.inv_wdeltap;
-    const float cell = (float)K.g.dx;
+    const float alpha = K.f.alpha, beta = K.f.beta, eta2 = K.f.eta2;
+    const float inv_wdp = K.f.inv_wdp;
+    const float cell = K.f.cell;
 
     KahanF vd0 = {}, vd1 = {}, vd2 = {}, vd3 = {}, sd0 = {}, sd1 = {}, sd2 = {}, sd3 = {};
     KahanF vt0 = {}, vt1 = {}, xt0 = {}, xt1 = {}, tl = {};
     const int hash = B.hash[k];
     const sph_geom_constants &g = K.g;
+    __shared__ int s_list[kPairChunk][kBlock];
+    int gi = 0, gj = 0, ii = 0, hi_i = 0, lo_j = 0, hi_j = 0, j = 0, j1 = 0;
+    const int R = g.stencil;
+    bool done = true;
     if (hash >= 0 && hash < g.num_cell) {
-        const int gi = hash / g.ny, gj = hash - gi * g.ny, R = g.stencil;
-        const int lo_i = max(gi - R, 0), hi_i = min(gi + R + 1, g.nx);
-        const int lo_j = max(gj - R, 0), hi_j = min(gj + R + 1, g.ny);
-        for (int ii = lo_i; ii < hi_i; ii++) {
-            const int c0 = ii * g.ny + lo_j, c1 = ii * g.ny + hi_j;
-            const int j0 = __ldg(offsets + c0), j1 = __ldg(offsets + c1);
-            const float dxc = (float)(gi - ii) * cell;
-            for (int j = j0; j < j1; j++) {
+        gi = hash / g.ny;
+        gj = hash - gi * g.ny;
+        ii = max(gi - R, 0);
+        hi_i = min(gi + R + 1, g.nx);
+        lo_j = max(gj - R, 0);
+        hi_j = min(gj + R + 1, g.ny);
+        j = __ldg(offsets + ii * g.ny + lo_j);
+        j1 = __ldg(offsets + ii * g.ny + hi_j);
+        done = false;
+    }
+    while (!done) {
+        // phase 1: collect the next in-support, active neighbours (column offset packed in 3 bits);
+        // four candidates per round keep four loads in flight
+        int cnt = 0;
+        while (cnt < kPairChunk) {
+            if (j + 4 <= j1 && cnt <= kPairChunk - 4) {
+                float4 n[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) n[u] = rec[4 * (j + u)];
+                const float dxc = (float)(gi - ii) * cell;
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int fj = __float_as_int(n[u].z);
+                    const float dx = dxc + (xri - n[u].x);
+                    const float dy = (float)(gj - (fj & kRowMask)) * cell + (yri - n[u].y);
+                    const float rr2 = dx * dx + dy * dy;
+                    if (rr2 < fourh2 && rr2 >= 1e-8f && !(fj & kFlagBlanked))
+                        s_list[cnt++][threadIdx.x] = ((j + u) << 3) | (gi - ii + R);
+                }
+                j += 4;
+            } else if (j < j1) {
                 const float4 n0 = rec[4 * j + 0];
                 const int fj = __float_as_int(n0.z);
-                const float dyc = (float)(gj - (fj & kRowMask)) * cell;
-                const float dx = dxc + (xri - n0.x), dy = dyc + (yri - n0.y);
+                const float dx = (float)(gi - ii) * cell + (xri - n0.x);
+                const float dy = (float)(gj - (fj & kRowMask)) * cell + (yri - n0.y);
                 const float rr2 = dx * dx + dy * dy;
-                if (rr2 >= fourh2 || rr2 < 1e-8f) continue;
-                if (fj & kFlagBlanked) continue;
-                const float rad = sqrtf(rr2);
-                const float q = rad * h1;
+                if (rr2 < fourh2 && rr2 >= 1e-8f && !(fj & kFlagBlanked)) s_list[cnt++][threadIdx.x] = (j << 3) | (gi - ii + R);
+                j++;
+            } else {
+                if (++ii >= hi_i) {
+                    done = true;
+                    break;
+                }
+                j = __ldg(offsets + ii * g.ny + lo_j);
+                j1 = __ldg(offsets + ii * g.ny + hi_j);
+            }
+        }
+        // phase 2: the pair body over the collected list, lanes in step; the
+        // next neighbour's record is fetched while the current one is computed
+        float4 p0, p1, p2, p3;
+        int pe = 0;
+        if (cnt > 0) {
+            pe = s_list[0][threadIdx.x];
+            const int jp = pe >> 3;
+            p0 = rec[4 * jp + 0]; p1 = rec[4 * jp + 1]; p2 = rec[4 * jp + 2]; p3 = rec[4 * jp + 3];
+        }
+        for (int t = 0; t < cnt; t++) {
+            const int e = pe;
+            const float4 n0 = p0, n1 = p1, n2 = p2, n3 = p3;
+            if (t + 1 < cnt) {
+                pe = s_list[t + 1][threadIdx.x];
+                const int jp = pe >> 3;
+                p0 = rec[4 * jp + 0]; p1 = rec[4 * jp + 1]; p2 = rec[4 * jp + 2]; p3 = rec[4 * jp + 3];
+            }
+            {
+                const int fj = __float_as_int(n0.z);
+                const float dx = (float)((e & 7) - R) * cell + (xri - n0.x);
+                const float dy = (float)(gj - (fj & kRowMask)) * cell + (yri - n0.y);
+                const float rr2 = dx * dx + dy * dy;
+                // FP32 form: hardware reciprocal square root instead of sqrt and division
+                const float inv_r = rsqrtf(rr2);
+                const float q = rr2 * inv_r * h1;
                 float val, der;
                 if (q > 1.f) {
                     const float t = 2.f - q, t2 = t * t;
                     val = 0.25f * t2 * t2 * t2;
-                    der = -0.75f * t2 * h1 / rad;
+                    der = -0.75f * t2 * h1 * inv_r;
                 } else {
                     val = 1.f - 1.5f * q * q * (1.f - 0.5f * q);
-                    der = -3.0f * q * (1.f - 0.75f * q) * h1 / rad;
+                    der = -3.0f * q * (1.f - 0.75f * q) * h1 * inv_r;
                 }
                 const float w = val * fac;
                 const float dwf = der * fac;
                 const float wx = dwf * dx, wy = dwf * dy;
-                const float4 n2 = rec[4 * j + 2];
                 const float volj = n2.w;
                 if (!tool_i && !(fj & kFlagTool)) {
-                    const float4 n1 = rec[4 * j + 1];
-                    const float4 n3 = rec[4 * j + 3];
                     const float dvx = n1.x - vix, dvy = n1.y - viy;
                     const float tx = wx * volj, ty = wy * volj;
                     vd0.add(dvx * tx);
@@ -312,11 +477,11 @@ __global__ void __launch_bounds__(kBlock) k_interact32(int N, KConsts K, const i
                     sd2.add(ay * wx);
                     sd3.add(az * wy);
                     const float vijposij = -(dvx * dx + dvy * dy);
-                    const float irho = 1.f / (0.5f * (rhoi + n1.z));
+                    const float irho = __fdividef(2.f, rhoi + n1.z);
                     if (vijposij < 0.f) {
                         const float cij = 0.5f * (ci + n1.w);
                         const float hij = 0.5f * (hi + n0.w);
-                        const float muij = (hij * vijposij) / (rr2 + eta2 * hij * hij);
+                        const float muij = __fdividef(hij * vijposij, rr2 + eta2 * hij * hij);
                         const float piij = (-alpha * cij * muij + beta * muij * muij) * irho;
                         vt0.add(piij * wx);
                         vt1.add(piij * wy);
@@ -325,34 +490,27 @@ __global__ void __launch_bounds__(kBlock) k_interact32(int N, KConsts K, const i
                     xt0.add(wr * dvx);
                     xt1.add(wr * dvy);
                 }
-                if (thermal) {
-                    const float4 n3 = rec[4 * j + 3];
-                    tl.add(volj * (Ti - n3.w) * dwf);
-                }
+                if (thermal) tl.add(volj * (Ti - n3.w) * dwf);
             }
         }
     }
-    const double mass = K.c.phys.mass;
-    const dbl4 vd = mk4(vd0.s, vd1.s, vd2.s, vd3.s);
-    const dbl4 sd = mk4(mass * sd0.s, mass * sd1.s, mass * sd2.s, mass * sd3.s);
-    const double2 vt = make_double2(-mass * vt0.s, -mass * vt1.s);
-    const double xs = K.c.corr.xspheps * mass;
-    const double2 xt = make_double2(xs * xt0.s, xs * xt1.s);
-    const double T_t = thermal_alpha * (2.0 * (double)tl.s);
+    const float mass = K.f.mass;
+    const float xs = K.f.xs_mass;
+    const float4 vd = make_float4(vd0.s, vd1.s, vd2.s, vd3.s);
+    const float4 sd = make_float4(mass * sd0.s, mass * sd1.s, mass * sd2.s, mass * sd3.s);
+    const float2 vt = make_float2(-mass * vt0.s, -mass * vt1.s);
+    const float2 xt = make_float2(xs * xt0.s, xs * xt1.s);
+    const float T_t = thermal_alpha * (2.0f * tl.s);
     if (!kFused) {
-        F.S_der[k] = sd;
-        F.v_der[k] = vd;
-        B.pos_t[k] = xt;
-        B.vel_t[k] = vt;
-        if (thermal) B.T_t[k] = T_t;
+        F.S_der[k] = mk4(sd.x, sd.y, sd.z, sd.w);
+        F.v_der[k] = mk4(vd.x, vd.y, vd.z, vd.w);
+        B.pos_t[k] = make_double2(xt.x, xt.y);
+        B.vel_t[k] = make_double2(vt.x, vt.y);
+        if (thermal) B.T_t[k] = (double)T_t;
     } else {
-        // the predicted velocity / density the FP64 path reads from its record
-        const double hdt = 0.5 * K.dt;
-        double2 v0 = B.vel[k], vt_old = B.vel_t[k];
-        double2 vel_pred = make_double2(v0.x + hdt * vt_old.x, v0.y + hdt * vt_old.y);
-        double rho_pred = B.rho[k] + hdt * B.rho_t[k];
-        fused_epilogue(k, K, B, F, seg, tool, secant_iters, status, tool_i, vel_pred, rho_pred, vd, sd, vt, xt,
-                       thermal, T_t);
+        // predicted velocity and density from this particle's record
+        fused_epilogue32(k, K, B, F, seg, tool, secant_iters, status, tool_i, make_float2(vix, viy), rhoi, vd, sd,
+                         vt, xt, thermal, T_t);
     }
 }
 

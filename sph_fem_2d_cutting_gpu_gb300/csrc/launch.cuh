@@ -16,7 +16,8 @@ void launch_sort_rest(cudaStream_t s, int N, const SortScratch &X, sph_geom_cons
                       uint32_t *status);
 void launch_gather_plain(cudaStream_t s, int N, const int32_t *perm, const SortedFields &A, const SortedFields &B);
 void launch_gather_fused(cudaStream_t s, int N, const int32_t *perm, const KConsts &K, const SortedFields &A,
-                         const SortedFields &B, const FixedFields &F, const StepScratch &W, const int32_t *hash_src);
+                         const SortedFields &B, const FixedFields &F, const StepScratch &W, const int32_t *hash_src,
+                         const ToolDev *tool);
 void launch_build_records(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F,
                           const StepScratch &W);
 
@@ -48,15 +49,19 @@ void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedField
                       bool next_hash);
 int reduce_blocks();
 void launch_reduce_force_T(cudaStream_t s, int N, const SortedFields &A, double *out);
+void launch_reduce_cases(cudaStream_t s, int n_cases, const SortedFields &A, const int32_t *offsets,
+                         const int32_t *cell_bound, const int32_t *part_bound, double *out);
 
 // fem.cu
-void launch_fem_half(cudaStream_t s, const FemDev &F, double hdt);
-void launch_fem_rate_update(cudaStream_t s, const KConsts &K, const FemDev &F, const SegDev &seg, double dt);
+void launch_fem_half(cudaStream_t s, const KConsts &K, const FemDev &F, const ToolDev *tool);
+void launch_fem_rate_update(cudaStream_t s, const KConsts &K, const FemDev &F, const SegDev &seg,
+                            const ToolDev *tool);
 void launch_fem_reset(cudaStream_t s, const FemDev &F, double *T_old, double *f_temp, double *K_temp);
 void launch_fem_robin(cudaStream_t s, const KConsts &K, const FemDev &F, const SegDev &seg, double *f_temp,
                       double *K_temp);
 void launch_fem_rate(cudaStream_t s, const FemDev &F, const double *f_temp, const double *K_temp);
 void launch_fem_temp(cudaStream_t s, const FemDev &F, const double *T_old, double dt);
-void launch_tool_move(cudaStream_t s, const SegDev &seg, const FemDev &F, ToolDev *tool, double dt, int what);
+void launch_tool_move(cudaStream_t s, const KConsts &K, const SegDev &seg, const FemDev &F, ToolDev *tool, double dt,
+                      int what, bool per_case);
 
 }  // namespace sphfem

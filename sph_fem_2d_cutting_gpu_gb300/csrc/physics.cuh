@@ -156,9 +156,9 @@ __device__ __forceinline__ uint32_t plasticity_one(const KConsts &K, dbl4 &S, do
 // WEAR_NODE_SHIFT statistics are not part of the path.  Returns status bits.
 // A segment id outside [0, n_seg) (the reference only ever stores -1 or a
 // valid id) is treated like -1, so caller-uploaded data cannot index out of range.
-__device__ __forceinline__ uint32_t fric_heat_one(const KConsts &K, const double *vel_tool, double2 vel, double2 ft,
-                                                  double2 nrm, double2 fc, double rho, double eps_pl, int seg,
-                                                  int n_seg, double &T, double &blanked,
+__device__ __forceinline__ uint32_t fric_heat_one(const KConsts &K, double dt, const double *vel_tool, double2 vel,
+                                                  double2 ft, double2 nrm, double2 fc, double rho, double eps_pl,
+                                                  int seg, int n_seg, double &T, double &blanked,
                                                   double *__restrict__ fric_heat) {
     (void)fc; (void)rho;
     if (blanked == 1.) return 0u;
@@ -176,7 +176,7 @@ __device__ __forceinline__ uint32_t fric_heat_one(const KConsts &K, const double
         return SPH_STATUS_FRIC_NAN;
     }
     if (v_rel_mag > 0.03) return 0u;
-    double T_buffer = T + value * (1 - partition_wp) * K.dt / K.c.trml_wp.cp / K.c.phys.mass;
+    double T_buffer = T + value * (1 - partition_wp) * dt / K.c.trml_wp.cp / K.c.phys.mass;
     if (T_buffer > 1550.) {
         T = 1550.;
     } else {
@@ -231,6 +231,109 @@ __device__ __forceinline__ dbl4 jaumann_one(const KConsts &K, dbl4 vd, dbl4 S) {
     r.z = (twoG * (vy_y - s) + om01 * S.y) + S.y * om01;
     r.w = (twoG * (0. - s) + 0.) + 0.;
     return r;
+}
+
+// ============================================================================
+// FP32 forms used by SPH_PREC_FP32K.  Same formulas as above in single
+// precision; only the return-mapping residual is evaluated in FP64.
+// ============================================================================
+
+// actions_gpu.cu:234-278 in FP32
+__device__ __forceinline__ float4 artificial_stress_f32(float stresseps, float rho, float p, float4 S) {
+    float sxx = S.x - p, sxy = S.y, syy = S.z - p;
+    float rhoi21 = 1.f / (rho * rho);
+    float theta = 0.5f * atan2f(2.f * sxy, sxx - syy);
+    float cs, sn;
+    sincosf(theta, &sn, &cs);
+    float cs2 = cs * cs, sn2 = sn * sn;
+    float rot_sxx = cs2 * sxx + 2.f * cs * sn * sxy + sn2 * syy;
+    float rot_syy = sn2 * sxx - 2.f * cs * sn * sxy + cs2 * syy;
+    float rxx = rot_sxx > 0.f ? -stresseps * rot_sxx * rhoi21 : 0.f;
+    float ryy = rot_syy > 0.f ? -stresseps * rot_syy * rhoi21 : 0.f;
+    return make_float4(cs2 * rxx + sn2 * ryy, cs * sn * (rxx - ryy), sn2 * rxx + cs2 * ryy, 0.f);
+}
+
+// actions_gpu.cu:280-314 in FP32
+__device__ __forceinline__ float4 jaumann_f32(float G, float4 vd, float4 S) {
+    float om10 = 0.5f * (vd.y - vd.z);
+    float om01 = -om10;
+    float e01 = 0.5f * (vd.y + vd.z);
+    float s = (1.f / 3.f) * (vd.x + vd.w);
+    float twoG = 2.f * G;
+    return make_float4(twoG * (vd.x - s) + 2.f * om10 * S.y, twoG * e01 + om01 * S.x + S.z * om10,
+                       twoG * (vd.w - s) + 2.f * om01 * S.y, -twoG * s);
+}
+
+__device__ __forceinline__ float jc_term_c_f32(const JcF32 &j, float T) {
+    float theta = fminf((T - j.Tref) * j.inv_dT, 1.f);
+    return 1.f - powf(theta, j.m);
+}
+
+__device__ __forceinline__ float sigma_yield_f32(const JcF32 &j, float eps, float epsd, float term_c) {
+    float eps_dot = epsd * j.inv_epsdot_ref;
+    float term_b = (eps_dot > 1.f) ? 1.f + j.C * logf(eps_dot) : powf(1.f + eps_dot, j.C);
+    return (j.A + j.B * powf(eps, j.n)) * term_b * term_c;
+}
+
+// actions_gpu.cu:689-754 + plasticity.cuh:117-162 in FP32 with the secant
+// residual g(dl) = |S_trial| - 2 mu dl - sqrt(2/3) sigma_Y in FP64.
+__device__ __forceinline__ uint32_t plasticity_f32(const KConsts &K, const JcF32 &j, float dt, float inv_dt, float4 &S,
+                                                   float p, float rho, float &eps_pl, float &eps_pl_dot, float &T,
+                                                   bool &blanked, int *iters_out) {
+    const float mu = K.f.G;
+    const float s23 = 0.816496580927726f;   // sqrt(2/3)
+    float norm = sqrtf(S.x * S.x + S.z * S.z + S.w * S.w + 2.f * S.y * S.y);
+    float cxx = S.x - p, cyy = S.z - p, czz = S.w - p, cxy = S.y;
+    float svm = sqrtf((cxx * cxx + cyy * cyy + czz * czz) - cxx * cyy - cxx * czz - cyy * czz + 3.f * cxy * cxy);
+    float term_c = jc_term_c_f32(j, T);
+    float sY = sigma_yield_f32(j, eps_pl, eps_pl_dot, term_c);
+    *iters_out = 0;
+    if (svm < sY) {
+        eps_pl_dot = 0.f;
+        return 0u;
+    }
+    const double norm_d = (double)norm, two_mu = 2.0 * K.c.phys.G, s23d = 0.816496580927726;
+    auto residual = [&](float dl) {   // FP64 residual
+        float dlp = fmaxf(dl, 0.f);
+        float sy = sigma_yield_f32(j, eps_pl + s23 * dlp, s23 * dlp * inv_dt, term_c);
+        return norm_d - two_mu * (double)dl - s23d * (double)sy;
+    };
+    float dl = fmaxf(eps_pl_dot * dt * s23, 1e-8f), dl_old;
+    int iter = 0;
+    uint32_t st = 0;
+    while (true) {
+        double g = residual(dl);
+        float dl1 = dl * 1.01f;
+        double g1 = residual(dl1);
+        float slope = (float)(g - g1) / (dl - dl1);
+        dl_old = dl;
+        dl = dl - (float)g / slope;
+        if (dl < 0.f) dl = -0.1f * dl;
+        if (fabsf(dl - dl_old) < 1e-6f) { iter++; break; }
+        if (iter > 100) { st |= SPH_STATUS_SECANT_MAXITER; iter++; break; }
+        iter++;
+    }
+    *iters_out = iter;
+    float dlp = fmaxf(dl, 0.f);
+    float eps_new = eps_pl + s23 * dlp;
+    float epsd_new = s23 * dlp * inv_dt;
+    float f = dl * 2.f * mu / norm;
+    S.x -= S.x * f;
+    S.y -= S.y * f;
+    S.z -= S.z * f;
+    S.w -= S.w * f;
+    if (K.c.trml_wp.tq != 0.) {
+        float sy_new = sigma_yield_f32(j, eps_new, epsd_new, term_c);
+        T += K.f.tq_over_cp / rho * (eps_new - eps_pl) * sy_new;
+    }
+    eps_pl = eps_new;
+    eps_pl_dot = epsd_new;
+    if (T > j.Tmelt) {
+        T = j.Tmelt;
+        blanked = true;
+        st |= SPH_STATUS_MELT_BLANKED;
+    }
+    return st;
 }
 
 // ---- actions_gpu.cu:33-43 find_max / find_min -----------------------------------
