@@ -109,6 +109,11 @@ class ToolState(C.Structure):
                 ("lowest_point", D), ("right_point", D), ("n_segments", I32), ("n_cut_colors", I32)]
 
 
+class CaseDesc(C.Structure):
+    _fields_ = [("host", C.POINTER(Particles)), ("tool", C.POINTER(ToolMesh)), ("dt", D), ("tool_vel", D * 2),
+                ("bbmin", D * 2), ("bbmax", D * 2)]
+
+
 def ptr(a: np.ndarray | None):
     """Pointer of a C-contiguous numpy array (or NULL)."""
     if a is None:
@@ -185,6 +190,12 @@ def load() -> C.CDLL:
         "sph_tool_host_info": ([P, C.POINTER(ToolState), C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)], C.c_int),
         "sph_tool_host_export": ([P, C.POINTER(Segments), C.POINTER(Fem)], C.c_int),
         "sph_tool_host_destroy": ([P], C.c_int),
+        "sph_batch_create": ([C.POINTER(Constants), C.POINTER(GridParams), I32, C.POINTER(CaseDesc), I32, I32,
+                              C.POINTER(P)], C.c_int),
+        "sph_batch_case_info": ([P, I32, PI, PI, PD, PI, PI, PI, PI], C.c_int),
+        "sph_batch_n_cases": ([P, PI], C.c_int),
+        "sph_batch_reduce": ([P, PD], C.c_int),
+        "sph_batch_case_of_particles": ([P, PI], C.c_int),
     }
     for name in STAGE_FUNCTIONS:
         proto.setdefault(name, ([P], C.c_int))

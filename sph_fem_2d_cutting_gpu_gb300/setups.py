@@ -11,6 +11,11 @@ Workloads:
   * ``aisi1045_cut`` -- AISI 1045 cut, 1600 x 400 particles, dx = 2.5 um, tool
                         mesh of about 20,000 nodes (rake -6, clearance 5 deg,
                         edge radius 20 um), 120 m/min, 100 um.
+  * ``batched_sweep`` -- independent AISI 1045 cuts of uneven sizes (particle
+                        counts log-uniform in [20k, 300k], height 0.5 mm,
+                        speed U(30, 300) m/min, uncut chip thickness
+                        U(20, 150) um, rake U(-10, 15) deg, tools of 2,000 to
+                        8,000 nodes) for the batched context.
 Unit conversions: 1 m/s = 1e-4 cm/us; 1 MPa = 1e-5 Mbar; 1 J/(kg K) = 1e-8
 (g cm^2/us^2)/(g K); 1 W/(m K) = 1e-13 bomb units.
 """
@@ -213,3 +218,59 @@ def small_cut(nx: int = 40, ny: int = 16, steps: int = 20, **kw) -> Case:
     """A few hundred particles and a coarse tool: sizes the CPU oracle finishes in seconds."""
     return cutting("small_cut", TI64, nx, ny, 5e-4, 1.7, 300.0, 0.002, 0.0, 7.0, 5e-4, 0.35,
                    s_min=2e-4, s_max=2.5e-3, tool_size=0.015, steps=steps, **kw)
+
+
+def placed(case: Case, preload_dx: float = 0.0) -> Case:
+    """Copy of a cutting case whose tool mesh is already at its start position.
+
+    The placement of benchmarks_NZ.cpp:247-267 moves the tool left until its
+    right point is 0.01 dx left of the workpiece, then vertically to the
+    target uncut chip thickness.  Here the two moves are applied to the mesh
+    nodes (and the mesh's top-left reference point) on the host, as one
+    translation, so the case needs no tool moves on the device (batched
+    contexts take placed tools).  ``preload_dx`` moves the tool that many dx
+    further in the cutting direction (contact from the first step)."""
+    import copy
+    assert case.tool_mesh is not None
+    st = abi.tool_model_host(case)["state"]
+    dx = case.info["dx"]
+    shift_x = -(st.right_point - case.info["lo_x"] + dx * 0.01) + preload_dx * dx
+    current_feed = case.info["hi_y"] - st.lowest_point
+    sign = 1.0 if current_feed > case.feed else -1.0
+    shift_y = sign * abs(current_feed - case.feed)
+    out = copy.copy(case)
+    m = dict(case.tool_mesh)
+    m["nodes"] = np.ascontiguousarray(case.tool_mesh["nodes"] + np.array([shift_x, shift_y]))
+    m["tl"] = (case.tool_mesh["tl"][0] + shift_x, case.tool_mesh["tl"][1] + shift_y)
+    out.tool_mesh = m
+    out.info = dict(case.info, placed_shift=(shift_x, shift_y))
+    return out
+
+
+def _tool_size_for(nodes: float) -> float:
+    """Tool edge length (cm) whose graded mesh (s_min 1 um, s_max 30 um, edge
+    radius 20 um) has about `nodes` nodes; piecewise linear fit of measured
+    counts."""
+    return float(np.interp(nodes, [2600.0, 3700.0, 6400.0, 8000.0], [0.03, 0.06, 0.10, 0.115]))
+
+
+def batched_sweep(n_cases: int = 64, seed: int = 0, n_min: int = 20_000, n_max: int = 300_000,
+                  dx: float = 2.5e-4, height: float = 0.05, steps: int = 5000, cell_factor: int = 1,
+                  stencil: int = 2) -> list[Case]:
+    """Independent AISI 1045 cuts of uneven sizes (placed tools), drawn from `seed`."""
+    rng = np.random.default_rng(seed)
+    ny = int(round(height / dx))
+    cases = []
+    for k in range(n_cases):
+        count = math.exp(rng.uniform(math.log(n_min), math.log(n_max)))
+        nx = max(8, int(round(count / ny)))
+        speed = rng.uniform(30.0, 300.0)
+        feed = rng.uniform(20e-4, 150e-4)
+        rake = rng.uniform(-10.0, 15.0)
+        target_nodes = rng.uniform(2000.0, 8000.0)
+        size = _tool_size_for(max(target_nodes, 2600.0))
+        c = cutting(f"sweep{k}", AISI1045, nx, ny, dx, 1.7, speed, feed, rake, 5.0, 2e-3, 0.35,
+                    s_min=1e-4, s_max=3e-3, tool_size=size, steps=steps, cell_factor=cell_factor, stencil=stencil)
+        c.info.update(speed_mpmin=speed, target_nodes=target_nodes, case_index=k, seed=seed)
+        cases.append(placed(c))
+    return cases

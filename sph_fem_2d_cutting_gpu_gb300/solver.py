@@ -41,8 +41,11 @@ class Solver:
                 self.ctx = C.c_void_p()
             raise SphError(f"sph_ctx_create failed ({r}): {msg}")
         self.has_tool = tool is not None
-        if self.has_tool and place_tool:
-            self.place_tool()
+        if self.has_tool:
+            if place_tool:
+                self.place_tool()
+            else:   # tool already placed (setups.placed): cutting velocity only
+                self.set_vel(case.tool_speed, 0.0)
 
     # ---- plumbing -------------------------------------------------------------------------
     def _ck(self, r: int, what: str):
@@ -198,3 +201,117 @@ class Solver:
 
     def fem_calculate_temp(self, dt: float):
         self._ck(self.lib.sph_fem_calculate_temp(self.ctx, dt), "sph_fem_calculate_temp")
+
+
+class Batch:
+    """Many independent cases in one batched context (sph_batch_create).
+
+    Every case keeps its own particles, FEM tool, tool velocity and time step;
+    one fused step advances all of them.  Tools must be placed already
+    (``setups.placed``).  Results come back per case in the case's own frame."""
+
+    def __init__(self, cases: list[Case], precision: int = abi.SPH_PREC_FP32K, device: int = 0):
+        self.lib = abi.load()
+        self.cases = cases
+        self.n_cases = len(cases)
+        self._keep = []
+        descs = (abi.CaseDesc * self.n_cases)()
+        hosts = []
+        for k, case in enumerate(cases):
+            host = abi.particles_struct(case.particles, case.N)
+            hosts.append(host)
+            tool, keep = case.tool_struct()
+            self._keep += keep + [tool]
+            d = descs[k]
+            d.host = C.pointer(host)
+            d.tool = C.pointer(tool) if tool is not None else None
+            d.dt = case.dt
+            d.tool_vel[0], d.tool_vel[1] = case.tool_speed, 0.0
+            d.bbmin[0], d.bbmin[1] = case.grid.bbmin[0], case.grid.bbmin[1]
+            d.bbmax[0], d.bbmax[1] = case.grid.bbmax[0], case.grid.bbmax[1]
+        self._keep += hosts
+        c0 = cases[0]
+        ctx = C.c_void_p()
+        r = self.lib.sph_batch_create(C.byref(c0.constants), C.byref(c0.grid), self.n_cases, descs, precision,
+                                      device, C.byref(ctx))
+        self.ctx = ctx
+        if r != abi.SPH_OK:
+            msg = self.lib.sph_last_error(ctx).decode() if ctx.value else ""
+            if ctx.value:
+                self.lib.sph_ctx_destroy(ctx)
+                self.ctx = C.c_void_p()
+            raise SphError(f"sph_batch_create failed ({r}): {msg}")
+        self.N = sum(c.N for c in cases)
+        self.info = [self.case_info(k) for k in range(self.n_cases)]
+
+    def _ck(self, r: int, what: str):
+        if r != abi.SPH_OK:
+            raise SphError(f"{what} failed ({r}): {self.lib.sph_last_error(self.ctx).decode()}")
+
+    def close(self):
+        if getattr(self, "ctx", None) is not None and self.ctx.value:
+            self.lib.sph_ctx_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def case_info(self, k: int) -> dict:
+        first, count, sf, sc, nf, nc = (C.c_int32() for _ in range(6))
+        off = np.zeros(2)
+        self._ck(self.lib.sph_batch_case_info(self.ctx, k, C.byref(first), C.byref(count), abi.ptr(off),
+                                              C.byref(sf), C.byref(sc), C.byref(nf), C.byref(nc)),
+                 "sph_batch_case_info")
+        return dict(first=first.value, count=count.value, offset=off, seg_first=sf.value, seg_count=sc.value,
+                    node_first=nf.value, node_count=nc.value)
+
+    def step(self, n: int = 1):
+        self._ck(self.lib.sph_run(self.ctx, n), "sph_run")
+
+    def sync(self):
+        self._ck(self.lib.sph_sync(self.ctx), "sph_sync")
+
+    def status(self, clear: bool = True) -> int:
+        s = C.c_uint32()
+        self._ck(self.lib.sph_status(self.ctx, C.byref(s), 1 if clear else 0), "sph_status")
+        return s.value
+
+    def reduce(self) -> np.ndarray:
+        """[n_cases, 3]: force x, force y (sum of fc + ft), max T of non-blanked particles."""
+        out = np.zeros((self.n_cases, 3))
+        self._ck(self.lib.sph_batch_reduce(self.ctx, abi.ptr(out)), "sph_batch_reduce")
+        return out
+
+    def download_cases(self, fields=None) -> list[dict]:
+        """Per-case particle arrays in the current order, positions in the case frame."""
+        out = abi.empty_particles(self.N)
+        if fields is not None:
+            out = {k: v for k, v in out.items() if k in fields}
+        s = abi.particles_struct(out, self.N)
+        self._ck(self.lib.sph_download_particles(self.ctx, C.byref(s)), "sph_download_particles")
+        case_of = np.zeros(self.N, np.int32)
+        self._ck(self.lib.sph_batch_case_of_particles(self.ctx, abi.ptr(case_of)), "sph_batch_case_of_particles")
+        res = []
+        for k in range(self.n_cases):
+            sel = case_of == k
+            d = {name: a[sel] for name, a in out.items()}
+            if "pos" in d:
+                d["pos"] = d["pos"] - self.info[k]["offset"]
+            if "on_seg" in d:
+                o = d["on_seg"]
+                d["on_seg"] = np.where(o >= 0, o - self.info[k]["seg_first"], o).astype(np.int32)
+            res.append(d)
+        return res
+
+    def fem_T(self) -> list[np.ndarray]:
+        f = abi.Fem()
+        self._ck(self.lib.sph_get_fem(self.ctx, C.byref(f)), "sph_get_fem")
+        T = np.zeros(f.n_nodes)
+        h = abi.Fem()
+        h.n_nodes, h.nnz = f.n_nodes, f.nnz
+        h.T = abi.ptr(T)
+        self._ck(self.lib.sph_download_fem(self.ctx, C.byref(h)), "sph_download_fem")
+        return [T[i["node_first"]:i["node_first"] + i["node_count"]] for i in self.info]
