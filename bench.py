@@ -211,6 +211,110 @@ def run_batched(args, local, max_over_ranks, barrier):
     return out
 
 
+def run_learned(args, local):
+    """The learned warm start on the AISI 1045 cut (640,000 particles, tool of
+    about 13,000 nodes, edge placement): log the plain FP32K return mappings
+    until `learned_records` states, train the MLP on 90 % of them, score it on
+    the held-out 10 %, then time the plain and the warm-started FP32K step and
+    the plain FP64 step from the logged state."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from sph_fem_2d_cutting_gpu_gb300 import abi, learned, setups
+    from sph_fem_2d_cutting_gpu_gb300.solver import Solver
+
+    def timed(s, steps):
+        stream_ptr = C.c_void_p()
+        s.lib.sph_get_stream(s.ctx, C.byref(stream_ptr))
+        ext = torch.cuda.ExternalStream(stream_ptr.value, device=torch.device("cuda", local))
+        s.step(args.warmup)
+        s.sync()
+        s.jc_stats(True, reset=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        s.step(steps)
+        e1.record(ext)
+        e1.synchronize()
+        calls, iters = s.jc_stats(True, reset=True)
+        return e0.elapsed_time(e1) / steps, calls, iters
+
+    case = setups.placed(setups.aisi1045_cut(), mode="edge")
+    s = Solver(case, abi.SPH_PREC_FP32K, device=local, place_tool=False)
+    s.jc_log_enable(args.learned_records)
+    t0 = time.perf_counter()
+    logged = 0
+    while logged < args.learned_max_steps:
+        s.step(500)
+        logged += 500
+        if s.jc_log_read(0)[1] >= args.learned_records:
+            break
+    rec, offered = s.jc_log_read()
+    log_s = time.perf_counter() - t0
+    s.jc_log_enable(0)
+    n_logged = len(rec)
+    rec = learned.valid_records(rec)
+    x, t = learned.features(rec, case.constants)
+    rng = np.random.default_rng(args.seed)
+    perm = rng.permutation(len(t))
+    n_ho = max(1, len(t) // 10)
+    ho, tr = perm[:n_ho], perm[n_ho:]
+    m = learned.Mlp(device=local, seed=args.seed)
+    m.fit_norm(x[tr], t[tr])
+    t0 = time.perf_counter()
+    losses = m.train(x[tr], t[tr], epochs=args.learned_epochs, batch=8192, lr=2e-3, seed=args.seed)
+    train_s = time.perf_counter() - t0
+    dl_max = rec[ho, learned.NORM] / np.float32(2.0 * case.constants.phys.G)
+    dl_true = rec[ho, learned.DL]
+    dl_mlp = np.minimum(np.exp(m.predict(x[ho])) * dl_max, dl_max)
+    dl_ref = np.maximum(rec[ho, learned.EPSD] * rec[ho, learned.DT] * np.float32(np.sqrt(2.0 / 3.0)),
+                        np.float32(1e-8))
+    err_mlp = np.abs(dl_mlp - dl_true) / dl_true
+    err_ref = np.abs(dl_ref - dl_true) / dl_true
+    # timed windows from the logged state: plain FP32K, warm-started FP32K
+    ms_plain, c_plain, it_plain = timed(s, args.steps)
+    s.attach_mlp(m)
+    ms_warm, c_warm, it_warm = timed(s, args.steps)
+    F32, T32 = s.reduce_force(), s.max_T()
+    P = s.download()
+    fem_T = s.fem()
+    steps_done = logged + 2 * (args.warmup + args.steps)
+    s.close()
+    m.close()
+    # plain FP64 from the same state (tool translated by the distance it moved)
+    c64 = setups.moved(case, case.tool_speed * case.dt * steps_done)
+    s64 = Solver(c64, abi.SPH_PREC_FP64, device=local, place_tool=False)
+    s64.upload(P)
+    s64.upload_fem_state(T=fem_T["T"], k=fem_T["k"])
+    ms_64, c_64, it_64 = timed(s64, args.steps)
+    s64.close()
+    torch.cuda.empty_cache()
+    return {
+        "workload": "AISI 1045 cut 1600x400 (640,000 particles), tool of "
+                    f"{case.info['nodes']} nodes, rake -6 deg, 120 m/min, edge placement",
+        "records_logged": int(n_logged), "records_offered": int(offered), "records_usable": int(len(rec)),
+        "steps_logged": logged,
+        "log_s": log_s, "train_samples": int(len(tr)), "train_epochs": args.learned_epochs,
+        "train_s": train_s, "train_loss": [float(v) for v in losses],
+        "heldout": {"samples": int(n_ho),
+                    "median_rel_err_mlp": float(np.median(err_mlp)),
+                    "p90_rel_err_mlp": float(np.quantile(err_mlp, 0.9)),
+                    "median_rel_err_reference_start": float(np.median(err_ref)),
+                    "p90_rel_err_reference_start": float(np.quantile(err_ref, 0.9)),
+                    "logged_iters_per_return": float(rec[:, learned.ITERS].mean())},
+        "timed_steps": args.steps,
+        "fp32k_plain": {"value": case.N / (ms_plain * 1e-3), "ms_per_step": ms_plain, "returns": c_plain,
+                        "iters_per_return": it_plain / max(c_plain, 1)},
+        "fp32k_mlp": {"value": case.N / (ms_warm * 1e-3), "ms_per_step": ms_warm, "returns": c_warm,
+                      "iters_per_return": it_warm / max(c_warm, 1)},
+        "fp64_plain": {"value": case.N / (ms_64 * 1e-3), "ms_per_step": ms_64, "returns": c_64,
+                       "iters_per_return": it_64 / max(c_64, 1)},
+        "speedup_mlp_vs_fp64": ms_64 / ms_warm,
+        "unit": UNIT,
+    }
+
+
 def run_product(args):
     import ctypes as C
 
@@ -326,6 +430,9 @@ def run_product(args):
     if args.batched_cases > 0:
         batched = run_batched(args, local, max_over_ranks, barrier)
         torch.cuda.empty_cache()
+    learned_line = None
+    if args.learned_records > 0 and rank == 0:
+        learned_line = run_learned(args, local)
 
     if rank != 0:
         if dist is not None:
@@ -363,6 +470,8 @@ def run_product(args):
     if batched is not None:
         batched["value"] *= world
         line["batched_sweep"] = batched
+    if learned_line is not None:
+        line["learned_warm_start"] = learned_line
     if not args.no_cpu:
         v, cores, n, el = cpu_sample(case, max_seconds=args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -388,6 +497,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--batched-cases", type=int, default=64, help="cases of the batched sweep (0: skip)")
+    ap.add_argument("--learned-records", type=int, default=10_000_000,
+                    help="return-mapping states logged for the learned warm start (0: skip)")
+    ap.add_argument("--learned-max-steps", type=int, default=20_000)
+    ap.add_argument("--learned-epochs", type=int, default=3)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -53,6 +53,7 @@ enum {
 #define SPH_STATUS_MELT_BLANKED   (1u << 5) /* T > Tmelt -> blanked (actions_gpu.cu:750-753)              */
 #define SPH_STATUS_FRIC_NAN       (1u << 6) /* NaN sliding velocity -> blanked (actions_gpu.cu:375-380)   */
 #define SPH_STATUS_CELL_OVERFLOW  (1u << 7) /* a cell held more particles than the in-cell ranker allows  */
+#define SPH_STATUS_MMA_TIMEOUT    (1u << 8) /* a tensor-core wait of the learned warm start gave up (1 s)  */
 
 /* ---- precision of the particle path ------------------------------------ */
 enum {
@@ -322,6 +323,53 @@ int sph_batch_n_cases(const sph_ctx *ctx, int32_t *n_cases);
 int sph_batch_reduce(sph_ctx *ctx, double *out);
 /* Case of every particle of the current (caller-visible) order, [N]. */
 int sph_batch_case_of_particles(sph_ctx *ctx, int32_t *case_of);
+
+/* ---- learned warm start of the return mapping -----------------------------------
+ * No counterpart in the reference.  A 4-64-64-64-1 SiLU MLP (BF16 weights,
+ * FP32 accumulation, tensor-core layers) predicts the plastic-multiplier
+ * increment of a yielding trial state from x = (log(svm / A), eps_pl,
+ * log(1 + eps_pl_dot / eps_dot_ref), (T - Tref) / (Tmelt - Tref)); its target
+ * is t = log(2 G dl / |dev S_trial|).  Attached to an FP32K context, the
+ * prediction replaces the reference's start dl0 = max(eps_pl_dot dt sqrt(2/3),
+ * 1e-8) of the secant return mapping (actions_gpu.cu:724, plasticity.cuh:128-
+ * 162), which still runs to the reference tolerance.
+ * Parameter vector (SPH_MLP_NPARAMS floats): W1 [64][4], b1 [64], W2 [64][64],
+ * b2 [64], W3 [64][64], b3 [64], W4 [64], b4 (W row-major [out][in]).  Inputs
+ * and target are standardised with `norm` before the network.  Losses are
+ * 0.5 (y - t)^2 in standardised units, averaged over the samples. */
+#define SPH_MLP_NPARAMS 8705
+typedef struct sph_mlp sph_mlp;
+typedef struct sph_mlp_norm {
+    float x_mean[4], x_std[4];
+    float y_mean, y_std;
+} sph_mlp_norm;
+
+int sph_mlp_create(int32_t device, uint64_t seed, sph_mlp **out);       /* uniform(+-1/sqrt(fan_in)) init */
+int sph_mlp_destroy(sph_mlp *m);
+const char *sph_mlp_last_error(const sph_mlp *m);
+int sph_mlp_get_params(sph_mlp *m, float *params, sph_mlp_norm *norm);  /* NULL outputs skipped */
+int sph_mlp_set_params(sph_mlp *m, const float *params, const sph_mlp_norm *norm);
+int sph_mlp_fit_norm(sph_mlp *m, const float *x, const float *t, int64_t n);   /* moments of the data */
+int sph_mlp_predict(sph_mlp *m, const float *x, int64_t n, float *y);  /* host x [n][4] -> host y [n] */
+/* Gradient of the mean loss over the n samples (host in/out; grad [SPH_MLP_NPARAMS]). */
+int sph_mlp_gradients(sph_mlp *m, const float *x, const float *t, int64_t n, float *grad, float *loss);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the gradient of these n samples. */
+int sph_mlp_adam_step(sph_mlp *m, const float *x, const float *t, int64_t n, float lr, float *loss);
+/* Minibatch Adam over `epochs` shuffled passes (seeded); epoch_loss [epochs] = mean loss of each pass. */
+int sph_mlp_train(sph_mlp *m, const float *x, const float *t, int64_t n, int32_t epochs, int32_t batch, float lr,
+                  uint64_t seed, float *epoch_loss);
+
+/* Return-mapping log: every yielding return mapping of the fused step appends
+ * (svm, eps_pl, eps_pl_dot, T, |dev S_trial|, dl, secant iterations, dt) as 8
+ * floats while fewer than `capacity` records are held; capacity 0 turns it off. */
+int sph_jc_log_enable(sph_ctx *ctx, int64_t capacity);
+int sph_jc_log_read(sph_ctx *ctx, float *records, int64_t max_records, int64_t *n_offered);
+/* Counters of return mappings and secant iterations (enable 1/0; out[2] may
+ * be NULL; reset zeroes them after the read). */
+int sph_jc_stats(sph_ctx *ctx, int32_t enable, int64_t *out, int32_t reset);
+/* Copies the network into the context and starts the return mappings of the
+ * fused FP32K step from its prediction; NULL detaches. */
+int sph_mlp_attach(sph_ctx *ctx, const sph_mlp *m);
 
 /* ---- per-stage timing ---------------------------------------------------------
  * Runs `nsteps` fused steps without the CUDA graph, with CUDA events on the

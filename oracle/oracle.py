@@ -73,6 +73,9 @@ def load() -> C.CDLL:
         "orc_fem_calculate_temp_rate": ([F, PD, PD], None),
         "orc_fem_calculate_temp": ([F, PD, D], None),
         "orc_step": ([P, PI, PI, G, K, D, S, F, T, I], C.c_uint32),
+        "orc_mlp_eval": ([PD, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int64, I, PD,
+                          PD, PD], I),
+        "orc_mlp_adam": ([C.POINTER(C.c_float)] * 4 + [C.c_int64, C.c_float], I),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -267,3 +270,42 @@ def set_threads(n: int):
 
 def num_threads() -> int:
     return int(load().orc_num_threads())
+
+
+# ---- learned warm start (mlp_oracle.cpp) --------------------------------------------------------
+MLP_NPARAMS = 8705
+
+
+def _fptr(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def norm_array(norm) -> np.ndarray:
+    """sph_mlp_norm (or a 10-vector) as float32 [x_mean(4), x_std(4), y_mean, y_std]."""
+    if isinstance(norm, np.ndarray):
+        return np.ascontiguousarray(norm, np.float32)
+    return np.array(list(norm.x_mean) + list(norm.x_std) + [norm.y_mean, norm.y_std], np.float32)
+
+
+def mlp_eval(params, norm, x, t=None, bf16=True, grad=False):
+    """Returns (y, grad or None, loss or None) of the MLP oracle."""
+    lib = load()
+    p = np.ascontiguousarray(params, np.float64)
+    nm = norm_array(norm)
+    x = np.ascontiguousarray(x, np.float32)
+    n = x.shape[0]
+    tt = None if t is None else np.ascontiguousarray(t, np.float32)
+    y = np.zeros(n)
+    g = np.zeros(MLP_NPARAMS) if grad else None
+    loss = np.zeros(1) if tt is not None else None
+    r = lib.orc_mlp_eval(abi.ptr(p), _fptr(nm), _fptr(x), _fptr(tt), n, 1 if bf16 else 0, abi.ptr(y),
+                         abi.ptr(g) if g is not None else None, abi.ptr(loss) if loss is not None else None)
+    assert r == 0
+    return y, g, (None if loss is None else float(loss[0]))
+
+
+def mlp_adam(params, m1, m2, grad, t, lr):
+    """One FP32 Adam step in place (oracle of the GPU update)."""
+    arrs = [np.ascontiguousarray(a, np.float32) for a in (params, m1, m2, grad)]
+    load().orc_mlp_adam(*[_fptr(a) for a in arrs], int(t), float(lr))
+    return arrs[0], arrs[1], arrs[2]

@@ -31,6 +31,7 @@ D = C.c_double
 I32 = C.c_int32
 PD = C.POINTER(C.c_double)
 PI = C.POINTER(C.c_int32)
+PF = C.POINTER(C.c_float)
 
 
 def _fields(names, t=D):
@@ -109,6 +110,14 @@ class ToolState(C.Structure):
                 ("lowest_point", D), ("right_point", D), ("n_segments", I32), ("n_cut_colors", I32)]
 
 
+class MlpNorm(C.Structure):
+    _fields_ = [("x_mean", C.c_float * 4), ("x_std", C.c_float * 4), ("y_mean", C.c_float), ("y_std", C.c_float)]
+
+
+MLP_NPARAMS = 8705
+JC_LOG_WIDTH = 8
+
+
 class CaseDesc(C.Structure):
     _fields_ = [("host", C.POINTER(Particles)), ("tool", C.POINTER(ToolMesh)), ("dt", D), ("tool_vel", D * 2),
                 ("bbmin", D * 2), ("bbmax", D * 2)]
@@ -119,7 +128,9 @@ def ptr(a: np.ndarray | None):
     if a is None:
         return None
     assert a.flags["C_CONTIGUOUS"], "array must be C-contiguous"
-    t = PI if a.dtype == np.int32 else PD
+    t = {np.dtype(np.int32): PI, np.dtype(np.float32): PF, np.dtype(np.int64): C.POINTER(C.c_int64)}.get(a.dtype, PD)
+    if t is PD:
+        assert a.dtype == np.float64, f"unsupported dtype {a.dtype}"
     return a.ctypes.data_as(t)
 
 
@@ -196,6 +207,20 @@ def load() -> C.CDLL:
         "sph_batch_n_cases": ([P, PI], C.c_int),
         "sph_batch_reduce": ([P, PD], C.c_int),
         "sph_batch_case_of_particles": ([P, PI], C.c_int),
+        "sph_mlp_create": ([I32, C.c_uint64, C.POINTER(P)], C.c_int),
+        "sph_mlp_destroy": ([P], C.c_int),
+        "sph_mlp_last_error": ([P], C.c_char_p),
+        "sph_mlp_get_params": ([P, PF, C.POINTER(MlpNorm)], C.c_int),
+        "sph_mlp_set_params": ([P, PF, C.POINTER(MlpNorm)], C.c_int),
+        "sph_mlp_fit_norm": ([P, PF, PF, C.c_int64], C.c_int),
+        "sph_mlp_predict": ([P, PF, C.c_int64, PF], C.c_int),
+        "sph_mlp_gradients": ([P, PF, PF, C.c_int64, PF, PF], C.c_int),
+        "sph_mlp_adam_step": ([P, PF, PF, C.c_int64, C.c_float, PF], C.c_int),
+        "sph_mlp_train": ([P, PF, PF, C.c_int64, I32, I32, C.c_float, C.c_uint64, PF], C.c_int),
+        "sph_jc_log_enable": ([P, C.c_int64], C.c_int),
+        "sph_jc_log_read": ([P, PF, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
+        "sph_jc_stats": ([P, I32, C.POINTER(C.c_int64), I32], C.c_int),
+        "sph_mlp_attach": ([P, P], C.c_int),
     }
     for name in STAGE_FUNCTIONS:
         proto.setdefault(name, ([P], C.c_int))

@@ -54,7 +54,41 @@ struct KConsts {
     const uint16_t *case_of_col;
     const uint16_t *case_of_node;
     const uint16_t *case_of_seg;
+    // return mapping: state log, statistics and the learned warm start (NULL: off)
+    float *jc_log;                        // [jc_log_cap][kJcLogWidth]
+    unsigned long long *jc_log_count;     // records offered (may exceed the capacity)
+    long long jc_log_cap;
+    unsigned long long *jc_stats;         // [0] return mappings, [1] secant iterations
+    int32_t *jc_list;                     // yielding particles deferred to the warm-started return mapping
+    int32_t *jc_list_count;
 };
+
+// One logged return mapping: trial von Mises stress, equivalent plastic
+// strain and its rate before the step, temperature, |dev S_trial|, the
+// converged plastic-multiplier increment, secant iterations, time step.
+constexpr int kJcLogWidth = 8;
+
+__device__ __forceinline__ void jc_log_record(const KConsts &K, float svm, float eps, float epsd, float T, float norm,
+                                              float dl, int iters, float dt) {
+    if (!K.jc_log) return;
+    unsigned long long at = atomicAdd(K.jc_log_count, 1ull);
+    if ((long long)at >= K.jc_log_cap) return;
+    float4 *r = (float4 *)(K.jc_log + at * kJcLogWidth);
+    r[0] = make_float4(svm, eps, epsd, T);
+    r[1] = make_float4(norm, dl, (float)iters, dt);
+}
+
+// Return-mapping counters, aggregated over the active lanes of the warp.
+__device__ __forceinline__ void jc_count(const KConsts &K, int iters) {
+    if (!K.jc_stats) return;
+    const unsigned mask = __activemask();
+    const unsigned n = __popc(mask);
+    const unsigned it = __reduce_add_sync(mask, (unsigned)iters);
+    if ((threadIdx.x & 31) == __ffs(mask) - 1) {
+        atomicAdd(K.jc_stats, (unsigned long long)n);
+        atomicAdd(K.jc_stats + 1, (unsigned long long)it);
+    }
+}
 
 // Case of a particle from its cell hash (its grid column).
 __device__ __forceinline__ int case_of_hash(const KConsts &K, int hash) {

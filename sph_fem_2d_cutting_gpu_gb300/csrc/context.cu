@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "launch.cuh"
+#include "mlp_host.h"
 #include "toolsetup.h"
 
 using namespace sphfem;
@@ -46,6 +47,17 @@ struct sph_ctx {
     int32_t *case_cell_bound = nullptr;              // [n_cases + 1] first cell of each case's columns
     int32_t *case_part_bound = nullptr;              // [n_cases + 1] prefix of case particle counts
     double *case_reduce = nullptr;                   // [n_cases][3]
+    // return-mapping log / statistics / learned warm start
+    int num_sms = 0;
+    float *jc_log = nullptr;
+    unsigned long long *jc_log_count = nullptr;
+    int64_t jc_log_cap = 0;
+    unsigned long long *jc_stats = nullptr;
+    int32_t *jc_list = nullptr, *jc_list_count = nullptr;
+    float *mlp_params = nullptr;
+    uint16_t *mlp_wb = nullptr;
+    MlpDev mlp{};
+    bool mlp_on = false;
     std::vector<void *> allocs;
     std::string err;
 };
@@ -237,6 +249,12 @@ int ensure_fem_temp(sph_ctx *ctx) {
 
 SortedFields &CUR(sph_ctx *ctx) { return ctx->buf[ctx->cur]; }
 
+// CTAs of the warm-started return mapping: persistent, about 4 per SM.
+int jc_warm_grid(const sph_ctx *ctx) {
+    int tiles = (ctx->N + 127) / 128;
+    return std::max(1, std::min(tiles, 4 * std::max(ctx->num_sms, 1)));
+}
+
 // The fused step body (everything after the histogram of the current state).
 int issue_fused_body(sph_ctx *ctx, int64_t &n) {
     const int N = ctx->N;
@@ -251,8 +269,14 @@ int issue_fused_body(sph_ctx *ctx, int64_t &n) {
         launch_fem_half(s, ctx->K, ctx->fem, ctx->tool_dev);
         n += 1;
     }
+    if (ctx->mlp_on) CK(cudaMemsetAsync(ctx->jc_list_count, 0, sizeof(int32_t), s));
     launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, ctx->seg, ctx->tool_dev, true);
     n += 1;
+    if (ctx->mlp_on) {
+        launch_jc_warm(s, jc_warm_grid(ctx), ctx->K, B, ctx->F, ctx->tool_dev, ctx->mlp, ctx->W.secant_iters,
+                       ctx->W.status);
+        n += 1;
+    }
     if (ctx->has_tool) {
         launch_fem_rate_update(s, ctx->K, ctx->fem, ctx->seg, ctx->tool_dev);
         launch_tool_move(s, ctx->K, ctx->seg, ctx->fem, ctx->tool_dev, ctx->K.dt, 3, true);
@@ -388,6 +412,7 @@ int ctx_begin(const sph_constants *c, const sph_grid_params *g, const sph_geom_c
         return SPH_ERR_NO_DEVICE;
     }
     *out = ctx;   // from here on errors are reported through ctx (caller destroys)
+    ctx->num_sms = prop.multiProcessorCount;
     CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     ctx->N = N;
     ctx->grid = *g;
@@ -416,6 +441,8 @@ int ctx_begin(const sph_constants *c, const sph_grid_params *g, const sph_geom_c
     DALLOC(ctx->W.rho_init, N); DALLOC(ctx->W.T_init, N);
     DALLOC(ctx->W.secant_iters, N); DALLOC(ctx->W.status, 1);
     DALLOC(ctx->W.reduce, (size_t)3 * reduce_blocks());
+    DALLOC(ctx->jc_stats, 2);
+    CK(cudaMemset(ctx->jc_stats, 0, 2 * sizeof(unsigned long long)));
     CK(cudaMallocHost((void **)&ctx->h_reduce, sizeof(double) * 3 * reduce_blocks()));
     int r = zero_all(ctx);
     if (r) return r;
@@ -1055,7 +1082,13 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
         CK(cudaEventRecord(ev[3], s));
         if (ctx->has_tool) launch_fem_half(s, ctx->K, ctx->fem, ctx->tool_dev);
         CK(cudaEventRecord(ev[4], s));
+        if (ctx->mlp_on) CK(cudaMemsetAsync(ctx->jc_list_count, 0, sizeof(int32_t), s));
         launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, ctx->seg, ctx->tool_dev, true);
+        if (ctx->mlp_on) {
+            launch_jc_warm(s, jc_warm_grid(ctx), ctx->K, B, ctx->F, ctx->tool_dev, ctx->mlp, ctx->W.secant_iters,
+                           ctx->W.status);
+            ctx->launches++;
+        }
         CK(cudaEventRecord(ev[5], s));
         if (ctx->has_tool) {
             launch_fem_rate_update(s, ctx->K, ctx->fem, ctx->seg, ctx->tool_dev);
@@ -1396,6 +1429,94 @@ int sph_batch_case_of_particles(sph_ctx *ctx, int32_t *case_of) {
         ix = ix < 0 ? 0 : (ix >= nx ? nx - 1 : ix);
         case_of[i] = ctx->case_of_col_h[ix];
     }
+    return SPH_OK;
+}
+
+// ---- return-mapping log, statistics, learned warm start -------------------------------------------
+int sph_jc_log_enable(sph_ctx *ctx, int64_t capacity) {
+    REQUIRE_CTX();
+    if (capacity < 0) return SPH_ERR_INVALID;
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->jc_log) {
+        cudaFree(ctx->jc_log);
+        ctx->allocs.erase(std::find(ctx->allocs.begin(), ctx->allocs.end(), (void *)ctx->jc_log));
+        ctx->jc_log = nullptr;
+    }
+    if (!ctx->jc_log_count) DALLOC(ctx->jc_log_count, 1);
+    CK(cudaMemset(ctx->jc_log_count, 0, sizeof(unsigned long long)));
+    ctx->jc_log_cap = capacity;
+    if (capacity > 0) DALLOC(ctx->jc_log, (size_t)capacity * kJcLogWidth);
+    ctx->K.jc_log = ctx->jc_log;
+    ctx->K.jc_log_count = ctx->jc_log_count;
+    ctx->K.jc_log_cap = capacity;
+    invalidate_graphs(ctx);
+    return SPH_OK;
+}
+
+int sph_jc_log_read(sph_ctx *ctx, float *records, int64_t max_records, int64_t *n_offered) {
+    REQUIRE_CTX();
+    unsigned long long n = 0;
+    if (ctx->jc_log_count) {
+        CK(cudaMemcpyAsync(&n, ctx->jc_log_count, sizeof(n), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    if (n_offered) *n_offered = (int64_t)n;
+    const int64_t held = std::min<int64_t>((int64_t)n, ctx->jc_log_cap);
+    const int64_t m = std::min<int64_t>(held, max_records);
+    if (records && m > 0) {
+        CK(cudaMemcpyAsync(records, ctx->jc_log, sizeof(float) * kJcLogWidth * (size_t)m, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    return SPH_OK;
+}
+
+int sph_jc_stats(sph_ctx *ctx, int32_t enable, int64_t *out, int32_t reset) {
+    REQUIRE_CTX();
+    unsigned long long h[2] = {0, 0};
+    CK(cudaMemcpyAsync(h, ctx->jc_stats, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    if (reset) CK(cudaMemsetAsync(ctx->jc_stats, 0, sizeof(h), ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (out) {
+        out[0] = (int64_t)h[0];
+        out[1] = (int64_t)h[1];
+    }
+    unsigned long long *want = enable ? ctx->jc_stats : nullptr;
+    if (ctx->K.jc_stats != want) {
+        ctx->K.jc_stats = want;
+        invalidate_graphs(ctx);
+    }
+    return SPH_OK;
+}
+
+int sph_mlp_attach(sph_ctx *ctx, const sph_mlp *m) {
+    REQUIRE_CTX();
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (!m) {
+        ctx->mlp_on = false;
+        ctx->K.jc_list = nullptr;
+        ctx->K.jc_list_count = nullptr;
+        invalidate_graphs(ctx);
+        return SPH_OK;
+    }
+    if (ctx->K.precision != SPH_PREC_FP32K)
+        return fail(ctx, SPH_ERR_STATE, "the learned warm start runs in the FP32K return mapping");
+    if (m->device != ctx->device) return fail(ctx, SPH_ERR_INVALID, "network on another device");
+    CK(mlp_configure());
+    if (!ctx->mlp_params) {
+        DALLOC(ctx->mlp_params, kMlpParams);
+        DALLOC(ctx->mlp_wb, kMlpWb);
+        DALLOC(ctx->jc_list, ctx->N);
+        DALLOC(ctx->jc_list_count, 1);
+    }
+    CK(cudaStreamSynchronize(m->stream));
+    CK(cudaMemcpy(ctx->mlp_params, m->params, sizeof(float) * kMlpParams, cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(ctx->mlp_wb, m->wb, sizeof(uint16_t) * kMlpWb, cudaMemcpyDeviceToDevice));
+    ctx->mlp = mlp_view(m, ctx->mlp_params, ctx->mlp_wb);
+    ctx->mlp_on = true;
+    ctx->K.jc_list = ctx->jc_list;
+    ctx->K.jc_list_count = ctx->jc_list_count;
+    invalidate_graphs(ctx);
     return SPH_OK;
 }
 

@@ -186,10 +186,26 @@ __device__ __forceinline__ void fused_epilogue32(int k, const KConsts &K, const 
         const JcF32 &j = K.f.jc;
         float eps_pl = (float)B.eps_pl[k], eps_pl_dot = (float)B.eps_pl_dot[k];
         int it = 0;
-        st |= plasticity_f32(K, j, dtf, tc.inv_dtf, S, (float)F.p[k], (float)rho, eps_pl, eps_pl_dot, T, blanked,
-                             &it);
-        B.eps_pl[k] = (double)eps_pl;
-        B.eps_pl_dot[k] = (double)eps_pl_dot;
+        if (K.jc_list) {
+            // learned warm start: the trial state is stored below and a yielding
+            // particle finishes its return mapping in k_jc_warm
+            JcTrial tr;
+            if (jc_trial_f32(j, S, (float)F.p[k], eps_pl, eps_pl_dot, T, tr)) {
+                const unsigned mask = __activemask();
+                const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+                int base = 0;
+                if (lane == leader) base = atomicAdd(K.jc_list_count, __popc(mask));
+                base = __shfl_sync(mask, base, leader);
+                K.jc_list[base + __popc(mask & ((1u << lane) - 1u))] = k;
+            } else {
+                B.eps_pl_dot[k] = 0.;
+            }
+        } else {
+            st |= plasticity_f32(K, j, dtf, tc.inv_dtf, S, (float)F.p[k], (float)rho, eps_pl, eps_pl_dot, T,
+                                 blanked, &it);
+            B.eps_pl[k] = (double)eps_pl;
+            B.eps_pl_dot[k] = (double)eps_pl_dot;
+        }
         if (secant_iters) secant_iters[k] = it;
     }
     B.S[k] = mk4(S.x, S.y, S.z, S.w);

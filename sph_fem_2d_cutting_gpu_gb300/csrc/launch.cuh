@@ -64,4 +64,19 @@ void launch_fem_temp(cudaStream_t s, const FemDev &F, const double *T_old, doubl
 void launch_tool_move(cudaStream_t s, const KConsts &K, const SegDev &seg, const FemDev &F, ToolDev *tool, double dt,
                       int what, bool per_case);
 
+// mlp.cu
+size_t mlp_fwd_smem();
+size_t mlp_train_smem();
+cudaError_t mlp_configure();
+void launch_mlp_predict(cudaStream_t s, const MlpDev &m, const float *x, int64_t n, float *y, uint32_t *status,
+                        int grid);
+void launch_jc_warm(cudaStream_t s, int grid, const KConsts &K, const SortedFields &B, const FixedFields &F,
+                    const ToolDev *tool, const MlpDev &m, int32_t *secant_iters, uint32_t *status);
+void launch_mlp_grad(cudaStream_t s, int grid, const MlpDev &m, const float *x, const float *t, const int32_t *idx,
+                     int64_t nb, float *part, uint32_t *status);
+void launch_mlp_reduce_adam(cudaStream_t s, const float *part, int nparts, float *grad_out, float *loss_out,
+                            float *params, float *m1, float *m2, uint16_t *wb, float lr, float beta1, float beta2,
+                            float eps, float c1, float c2, bool adam);
+void launch_mlp_refresh_wb(cudaStream_t s, const float *params, uint16_t *wb);
+
 }  // namespace sphfem

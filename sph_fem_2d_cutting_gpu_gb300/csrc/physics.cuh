@@ -129,6 +129,9 @@ __device__ __forceinline__ uint32_t plasticity_one(const KConsts &K, dbl4 &S, do
     uint32_t st = 0;
     if (it < 0) { st |= SPH_STATUS_SECANT_MAXITER; it = -it; }
     *iters_out = it;
+    jc_log_record(K, (float)svm, (float)eps_pl, (float)eps_pl_dot, (float)T, (float)norm_Strial, (float)delta_lambda,
+                  it, (float)dt);
+    jc_count(K, it);
     double eps_pl_new = eps_pl + sqrtf_d(2.0 / 3.0) * fmaxf_d(delta_lambda, 0.);
     double eps_pl_dot_new = sqrtf_d(2.0 / 3.0) * fmaxf_d(delta_lambda, 0.) / dt;
     double eps_old = eps_pl;
@@ -275,30 +278,40 @@ __device__ __forceinline__ float sigma_yield_f32(const JcF32 &j, float eps, floa
     return (j.A + j.B * powf(eps, j.n)) * term_b * term_c;
 }
 
-// actions_gpu.cu:689-754 + plasticity.cuh:117-162 in FP32 with the secant
-// residual g(dl) = |S_trial| - 2 mu dl - sqrt(2/3) sigma_Y in FP64.
-__device__ __forceinline__ uint32_t plasticity_f32(const KConsts &K, const JcF32 &j, float dt, float inv_dt, float4 &S,
-                                                   float p, float rho, float &eps_pl, float &eps_pl_dot, float &T,
-                                                   bool &blanked, int *iters_out) {
+// Trial state of the FP32 return mapping (actions_gpu.cu:689-720): deviatoric
+// norm, von Mises stress of the Cauchy stress S - p I, thermal softening term
+// and yield stress at the state before the step.  Returns true if yielding.
+struct JcTrial {
+    float norm, svm, term_c;
+};
+
+__device__ __forceinline__ bool jc_trial_f32(const JcF32 &j, const float4 &S, float p, float eps_pl, float eps_pl_dot,
+                                             float T, JcTrial &tr) {
+    tr.norm = sqrtf(S.x * S.x + S.z * S.z + S.w * S.w + 2.f * S.y * S.y);
+    float cxx = S.x - p, cyy = S.z - p, czz = S.w - p, cxy = S.y;
+    tr.svm = sqrtf((cxx * cxx + cyy * cyy + czz * czz) - cxx * cyy - cxx * czz - cyy * czz + 3.f * cxy * cxy);
+    tr.term_c = jc_term_c_f32(j, T);
+    float sY = sigma_yield_f32(j, eps_pl, eps_pl_dot, tr.term_c);
+    return !(tr.svm < sY);
+}
+
+// Radial return from a yielding trial state (actions_gpu.cu:720-754,
+// plasticity.cuh:117-162) in FP32 with the secant residual
+// g(dl) = |S_trial| - 2 mu dl - sqrt(2/3) sigma_Y in FP64, started from dl_init.
+// The stopping rule (|dl - dl_old| < 1e-6, at most 101 iterations) is the
+// reference's, so any start converges to the same tolerance.
+__device__ __forceinline__ uint32_t jc_return_f32(const KConsts &K, const JcF32 &j, float dt, float inv_dt, float4 &S,
+                                                  float rho, float &eps_pl, float &eps_pl_dot, float &T, bool &blanked,
+                                                  int *iters_out, const JcTrial &tr, float dl_init) {
     const float mu = K.f.G;
     const float s23 = 0.816496580927726f;   // sqrt(2/3)
-    float norm = sqrtf(S.x * S.x + S.z * S.z + S.w * S.w + 2.f * S.y * S.y);
-    float cxx = S.x - p, cyy = S.z - p, czz = S.w - p, cxy = S.y;
-    float svm = sqrtf((cxx * cxx + cyy * cyy + czz * czz) - cxx * cyy - cxx * czz - cyy * czz + 3.f * cxy * cxy);
-    float term_c = jc_term_c_f32(j, T);
-    float sY = sigma_yield_f32(j, eps_pl, eps_pl_dot, term_c);
-    *iters_out = 0;
-    if (svm < sY) {
-        eps_pl_dot = 0.f;
-        return 0u;
-    }
-    const double norm_d = (double)norm, two_mu = 2.0 * K.c.phys.G, s23d = 0.816496580927726;
+    const double norm_d = (double)tr.norm, two_mu = 2.0 * K.c.phys.G, s23d = 0.816496580927726;
     auto residual = [&](float dl) {   // FP64 residual
         float dlp = fmaxf(dl, 0.f);
-        float sy = sigma_yield_f32(j, eps_pl + s23 * dlp, s23 * dlp * inv_dt, term_c);
+        float sy = sigma_yield_f32(j, eps_pl + s23 * dlp, s23 * dlp * inv_dt, tr.term_c);
         return norm_d - two_mu * (double)dl - s23d * (double)sy;
     };
-    float dl = fmaxf(eps_pl_dot * dt * s23, 1e-8f), dl_old;
+    float dl = dl_init, dl_old;
     int iter = 0;
     uint32_t st = 0;
     while (true) {
@@ -314,16 +327,18 @@ __device__ __forceinline__ uint32_t plasticity_f32(const KConsts &K, const JcF32
         iter++;
     }
     *iters_out = iter;
+    jc_log_record(K, tr.svm, eps_pl, eps_pl_dot, T, tr.norm, dl, iter, dt);
+    jc_count(K, iter);
     float dlp = fmaxf(dl, 0.f);
     float eps_new = eps_pl + s23 * dlp;
     float epsd_new = s23 * dlp * inv_dt;
-    float f = dl * 2.f * mu / norm;
+    float f = dl * 2.f * mu / tr.norm;
     S.x -= S.x * f;
     S.y -= S.y * f;
     S.z -= S.z * f;
     S.w -= S.w * f;
     if (K.c.trml_wp.tq != 0.) {
-        float sy_new = sigma_yield_f32(j, eps_new, epsd_new, term_c);
+        float sy_new = sigma_yield_f32(j, eps_new, epsd_new, tr.term_c);
         T += K.f.tq_over_cp / rho * (eps_new - eps_pl) * sy_new;
     }
     eps_pl = eps_new;
@@ -334,6 +349,25 @@ __device__ __forceinline__ uint32_t plasticity_f32(const KConsts &K, const JcF32
         st |= SPH_STATUS_MELT_BLANKED;
     }
     return st;
+}
+
+// The reference's start dl0 = max(eps_pl_dot dt sqrt(2/3), 1e-8) (actions_gpu.cu:724).
+__device__ __forceinline__ float jc_default_start(float eps_pl_dot, float dt) {
+    return fmaxf(eps_pl_dot * dt * 0.816496580927726f, 1e-8f);
+}
+
+// actions_gpu.cu:689-754 + plasticity.cuh:117-162 in FP32 (trial + return).
+__device__ __forceinline__ uint32_t plasticity_f32(const KConsts &K, const JcF32 &j, float dt, float inv_dt, float4 &S,
+                                                   float p, float rho, float &eps_pl, float &eps_pl_dot, float &T,
+                                                   bool &blanked, int *iters_out) {
+    JcTrial tr;
+    *iters_out = 0;
+    if (!jc_trial_f32(j, S, p, eps_pl, eps_pl_dot, T, tr)) {
+        eps_pl_dot = 0.f;
+        return 0u;
+    }
+    return jc_return_f32(K, j, dt, inv_dt, S, rho, eps_pl, eps_pl_dot, T, blanked, iters_out, tr,
+                         jc_default_start(eps_pl_dot, dt));
 }
 
 // ---- actions_gpu.cu:33-43 find_max / find_min -----------------------------------

@@ -79,4 +79,20 @@ struct StepScratch {
     double *reduce;                 // reduction scratch
 };
 
+// The learned warm start of the return mapping: a 4-64-64-64-1 SiLU MLP.
+// Parameters in FP32 (layout kMlp* offsets); BF16 copies of the four weight
+// matrices feed the tensor cores.  Features and target are standardised with
+// the training set's moments.
+constexpr int kMlpIn = 4, kMlpH = 64;
+constexpr int kMlpOffW1 = 0, kMlpOffB1 = 256, kMlpOffW2 = 320, kMlpOffB2 = 4416, kMlpOffW3 = 4480,
+              kMlpOffB3 = 8576, kMlpOffW4 = 8640, kMlpOffB4 = 8704, kMlpParams = 8705;
+// BF16 weight copies: W1 [64][4], W2 [64][64], W3 [64][64], W4 [64]
+constexpr int kMlpWbW1 = 0, kMlpWbW2 = 256, kMlpWbW3 = 4352, kMlpWbW4 = 8448, kMlpWb = 8512;
+
+struct MlpDev {
+    const float *params;      // [kMlpParams] FP32 (biases are read from here)
+    const uint16_t *wb;       // [kMlpWb] BF16 bit patterns of the weights
+    float x_mean[4], x_inv_std[4], y_mean, y_std;
+};
+
 }  // namespace sphfem

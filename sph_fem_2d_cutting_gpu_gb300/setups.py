@@ -220,30 +220,44 @@ def small_cut(nx: int = 40, ny: int = 16, steps: int = 20, **kw) -> Case:
                    s_min=2e-4, s_max=2.5e-3, tool_size=0.015, steps=steps, **kw)
 
 
-def placed(case: Case, preload_dx: float = 0.0) -> Case:
+def placed(case: Case, preload_dx: float = 0.0, mode: str = "reference") -> Case:
     """Copy of a cutting case whose tool mesh is already at its start position.
 
-    The placement of benchmarks_NZ.cpp:247-267 moves the tool left until its
-    right point is 0.01 dx left of the workpiece, then vertically to the
-    target uncut chip thickness.  Here the two moves are applied to the mesh
-    nodes (and the mesh's top-left reference point) on the host, as one
-    translation, so the case needs no tool moves on the device (batched
-    contexts take placed tools).  ``preload_dx`` moves the tool that many dx
-    further in the cutting direction (contact from the first step)."""
+    mode "reference": the placement of benchmarks_NZ.cpp:247-267 -- the tool
+    moves left until its right point (largest node x) is 0.01 dx left of the
+    workpiece, then vertically to the target uncut chip thickness.  With a
+    negative rake angle the right point is the top of the rake face, above
+    the workpiece, and the cutting edge starts far from the workpiece.
+    mode "edge": after the vertical move, the rightmost node at or below the
+    workpiece top is put 0.01 dx left of the workpiece, so every rake angle
+    starts in contact.
+    The moves are applied to the mesh nodes (and the mesh's top-left
+    reference point) on the host, as one translation, so the case needs no
+    tool moves on the device (batched contexts take placed tools).
+    ``preload_dx`` moves the tool that many dx further in the cutting
+    direction (contact from the first step)."""
     import copy
     assert case.tool_mesh is not None
     st = abi.tool_model_host(case)["state"]
     dx = case.info["dx"]
-    shift_x = -(st.right_point - case.info["lo_x"] + dx * 0.01) + preload_dx * dx
     current_feed = case.info["hi_y"] - st.lowest_point
     sign = 1.0 if current_feed > case.feed else -1.0
     shift_y = sign * abs(current_feed - case.feed)
+    nodes = case.tool_mesh["nodes"]
+    if mode == "reference":
+        shift_x = -(st.right_point - case.info["lo_x"] + dx * 0.01)
+    elif mode == "edge":
+        band = nodes[:, 1] + shift_y <= case.info["hi_y"] + 1e-12
+        shift_x = case.info["lo_x"] - dx * 0.01 - float(nodes[band, 0].max())
+    else:
+        raise ValueError(mode)
+    shift_x += preload_dx * dx
     out = copy.copy(case)
     m = dict(case.tool_mesh)
-    m["nodes"] = np.ascontiguousarray(case.tool_mesh["nodes"] + np.array([shift_x, shift_y]))
+    m["nodes"] = np.ascontiguousarray(nodes + np.array([shift_x, shift_y]))
     m["tl"] = (case.tool_mesh["tl"][0] + shift_x, case.tool_mesh["tl"][1] + shift_y)
     out.tool_mesh = m
-    out.info = dict(case.info, placed_shift=(shift_x, shift_y))
+    out.info = dict(case.info, placed_shift=(shift_x, shift_y), placement=mode)
     return out
 
 
@@ -272,5 +286,18 @@ def batched_sweep(n_cases: int = 64, seed: int = 0, n_min: int = 20_000, n_max: 
         c = cutting(f"sweep{k}", AISI1045, nx, ny, dx, 1.7, speed, feed, rake, 5.0, 2e-3, 0.35,
                     s_min=1e-4, s_max=3e-3, tool_size=size, steps=steps, cell_factor=cell_factor, stencil=stencil)
         c.info.update(speed_mpmin=speed, target_nodes=target_nodes, case_index=k, seed=seed)
-        cases.append(placed(c))
+        cases.append(placed(c, mode="edge"))
     return cases
+
+
+def moved(case: Case, shift_x: float, shift_y: float = 0.0) -> Case:
+    """Copy of a placed case with its tool mesh translated by (shift_x,
+    shift_y): the tool of a run restarted from a state in which the tool has
+    advanced (the rigid motion of tool_FEM.cu:109-139 as one translation)."""
+    import copy
+    out = copy.copy(case)
+    m = dict(case.tool_mesh)
+    m["nodes"] = np.ascontiguousarray(case.tool_mesh["nodes"] + np.array([shift_x, shift_y]))
+    m["tl"] = (case.tool_mesh["tl"][0] + shift_x, case.tool_mesh["tl"][1] + shift_y)
+    out.tool_mesh = m
+    return out

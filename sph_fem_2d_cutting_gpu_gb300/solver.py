@@ -189,6 +189,33 @@ class Solver:
         self._ck(self.lib.sph_reduce_max_T(self.ctx, abi.ptr(out)), "sph_reduce_max_T")
         return float(out[0])
 
+    # ---- return-mapping log / statistics / learned warm start -------------------------------
+    def jc_log_enable(self, capacity: int):
+        self._ck(self.lib.sph_jc_log_enable(self.ctx, capacity), "sph_jc_log_enable")
+
+    def jc_log_read(self, max_records: int | None = None):
+        """(records [n, 8] float32, number of return mappings offered to the log)."""
+        n = C.c_int64()
+        self._ck(self.lib.sph_jc_log_read(self.ctx, None, 0, C.byref(n)), "sph_jc_log_read")
+        m = n.value if max_records is None else min(n.value, max_records)
+        rec = np.zeros((m, abi.JC_LOG_WIDTH), np.float32)
+        if m:
+            self._ck(self.lib.sph_jc_log_read(self.ctx, abi.ptr(rec), m, C.byref(n)), "sph_jc_log_read")
+            held = min(n.value, m)
+            rec = rec[:held]
+        return rec, n.value
+
+    def jc_stats(self, enable: bool = True, reset: bool = False):
+        """(return mappings, secant iterations) counted since the last reset."""
+        out = np.zeros(2, np.int64)
+        self._ck(self.lib.sph_jc_stats(self.ctx, 1 if enable else 0, abi.ptr(out), 1 if reset else 0),
+                 "sph_jc_stats")
+        return int(out[0]), int(out[1])
+
+    def attach_mlp(self, mlp):
+        """Start the FP32K return mappings from the network's prediction (None detaches)."""
+        self._ck(self.lib.sph_mlp_attach(self.ctx, mlp.h if mlp is not None else None), "sph_mlp_attach")
+
     def __getattr__(self, name):
         # stage calls by their reference names: update_geometry, assign_hashes, sort,
         # material_eos, interactions_monaghan, ... -> sph_<name>(ctx)
