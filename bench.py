@@ -136,10 +136,10 @@ def run_reference(args):
         return 0
     from sph_fem_2d_cutting_gpu_gb300 import setups
     from oracle.oracle import OracleSim, num_threads
-    case = setups.micro(n_side=args.n_side, seed=args.seed)
+    case = setups.micro(n_side=args.n_side, seed=args.seed, cell_factor=args.cell_factor, stencil=args.stencil)
     # bounded sample: a square sub-lattice of the workload sized for ~2 s per step
     side = min(args.n_side, args.ref_side)
-    sub = setups.micro(n_side=side, seed=args.seed)
+    sub = setups.micro(n_side=side, seed=args.seed, cell_factor=args.cell_factor, stencil=args.stencil)
     o = OracleSim(sub.constants, sub.grid, sub.particles, sub.dt)
     for _ in range(args.warmup):
         o.step()
@@ -152,8 +152,10 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": f"micro {case.info['n_side']}x{case.info['n_side']} lattice, dx=2.5um, h=1.7dx, "
-                               "full leap-frog step without tool", "particles": case.N,
+        "config": {"workload": f"micro {case.info['n_side']}x{case.info['n_side']} lattice ({case.N} particles), "
+                               f"dx=2.5um, h=1.7dx, cells {args.cell_factor}h / "
+                               f"{2 * args.stencil + 1}x{2 * args.stencil + 1} stencil, AISI 1045 JC; full "
+                               "leap-frog step without tool", "particles": case.N,
                    "sample_particles": sub.N},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": num_threads(), "kind": "port",
                          "sample": f"{args.steps} whole steps of a {side}x{side} sub-lattice of the workload "
@@ -174,10 +176,19 @@ def run_batched(args, local, max_over_ranks, barrier):
     from sph_fem_2d_cutting_gpu_gb300 import abi, setups
     from sph_fem_2d_cutting_gpu_gb300.solver import Batch
 
+    from sph_fem_2d_cutting_gpu_gb300 import tune
+
     t0 = time.perf_counter()
     cases = setups.batched_sweep(n_cases=args.batched_cases, seed=args.seed)
-    b = Batch(cases, abi.SPH_PREC_FP32K, device=local)
     setup_s = time.perf_counter() - t0
+    tuned, table = None, None
+    if not args.no_tune:
+        tuned, table = tune.autotune(lambda cs: Batch(cs, abi.SPH_PREC_FP32K, device=local), cases,
+                                     warmup=args.warmup, steps=max(3, args.steps // 2))
+        cases = [tune.with_geometry(c, tuned["cell_factor"], tuned["stencil"]) for c in cases]
+    b = Batch(cases, abi.SPH_PREC_FP32K, device=local)
+    if tuned is not None:
+        tune.set_variant(b, tuned["variant"])
     stream_ptr = C.c_void_p()
     b.lib.sph_get_stream(b.ctx, C.byref(stream_ptr))
     ext = torch.cuda.ExternalStream(stream_ptr.value, device=torch.device("cuda", local))
@@ -204,6 +215,7 @@ def run_batched(args, local, max_over_ranks, barrier):
            "fem_nodes": nodes, "launches_per_step": (n1.value - n0.value) / args.steps,
            "stage_ms": dict(zip(STAGES, [v / args.steps for v in stage_ms])), "status": st,
            "setup_s": setup_s, "dtype": "f32k",
+           "autotune": None if tuned is None else {"best": tuned, "table": table},
            "workload": f"{b.n_cases} AISI 1045 cuts, counts log-uniform 20k-300k (height 0.5 mm, dx 2.5 um), "
                        "speed U(30,300) m/min, uncut chip U(20,150) um, rake U(-10,15) deg, own FEM tool each; "
                        "one fused step over all cases, CUDA-graph replay"}
@@ -342,7 +354,9 @@ def run_product(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    case = setups.micro(n_side=args.n_side, seed=args.seed + rank)
+    # cells of 2h with a 3x3 stencil, as the micro-benchmark specifies
+    case = setups.micro(n_side=args.n_side, seed=args.seed + rank, cell_factor=args.cell_factor,
+                        stencil=args.stencil)
     hbm_peak, peak_kind = peaks()
     results = {}
     for prec_name, prec in (("fp32k", abi.SPH_PREC_FP32K), ("fp64", abi.SPH_PREC_FP64)):
@@ -352,6 +366,20 @@ def run_product(args):
         stream_ptr = C.c_void_p()
         s.lib.sph_get_stream(s.ctx, C.byref(stream_ptr))
         ext = torch.cuda.ExternalStream(stream_ptr.value, device=torch.device("cuda", local))
+        variant_table = None
+        if prec == abi.SPH_PREC_FP32K and not args.no_tune:
+            # launch shape of the neighbour sums: timed on this workload (the state it
+            # advances is restored afterwards, so the timed run starts from step 0)
+            from sph_fem_2d_cutting_gpu_gb300 import tune
+            P0 = s.download()
+            variant_table = []
+            for v in range(len(tune.launch_variants())):
+                tune.set_variant(s, v)
+                variant_table.append(tune._time_steps(s, 2, 4))
+            best_v = min(range(len(variant_table)), key=lambda v: variant_table[v])
+            tune.set_variant(s, best_v)
+            s.upload(P0)
+            del P0
         for _ in range(args.warmup):
             s.step()
         s.sync()
@@ -379,6 +407,11 @@ def run_product(args):
         stage = [v / args.steps for v in stage_ms]
         res = dict(ms=ms, launches=launches / args.steps * args.steps, clocks=ck, status=st,
                    stage_ms=dict(zip(STAGES, stage)), launches_per_step=launches / args.steps)
+        if variant_table is not None:
+            from sph_fem_2d_cutting_gpu_gb300 import tune
+            shapes = tune.launch_variants()
+            res["launch_tuning"] = {"chosen": {"block": shapes[best_v][0], "min_blocks": shapes[best_v][1]},
+                                    "ms_per_step": {f"{b}x{m}": t for (b, m), t in zip(shapes, variant_table)}}
         # end-to-end through the C ABI with pinned host buffers
         if not args.no_e2e:
             fields = {}
@@ -447,8 +480,9 @@ def run_product(args):
         "vs_baseline": None, "dtype": "f32k" if head_name == "fp32k" else "f64",
         "data": "synthetic (seeded): jittered lattice, random velocity/stress/density",
         "config": {"workload": f"micro {case.info['n_side']}x{case.info['n_side']} lattice ({case.N} particles), "
-                               "dx=2.5um, h=1.7dx, cells h / 5x5 stencil, AISI 1045 JC; full leap-frog step "
-                               "without tool",
+                               f"dx=2.5um, h=1.7dx, cells {args.cell_factor}h / "
+                               f"{2 * args.stencil + 1}x{2 * args.stencil + 1} stencil, AISI 1045 JC; full "
+                               "leap-frog step without tool",
                    "particles": case.N, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (about 3 GB of particle state per GPU)",
                    "form": "FP32 neighbour sums with Kahan compensation, FP64 state/positions/residual"
@@ -459,6 +493,8 @@ def run_product(args):
         "stage_ms": head["stage_ms"],
         "status": head["status"],
     }
+    if "launch_tuning" in head:
+        line["launch_tuning"] = head["launch_tuning"]
     if "e2e" in head:
         line["e2e"] = head["e2e"]
     if "fp64" in results and head_name != "fp64":
@@ -501,6 +537,9 @@ def main():
                     help="return-mapping states logged for the learned warm start (0: skip)")
     ap.add_argument("--learned-max-steps", type=int, default=20_000)
     ap.add_argument("--learned-epochs", type=int, default=3)
+    ap.add_argument("--no-tune", action="store_true", help="no launch-shape / cell-geometry autotuning")
+    ap.add_argument("--cell-factor", type=int, default=2, help="micro workload: cell edge in h")
+    ap.add_argument("--stencil", type=int, default=1, help="micro workload: stencil half-width in cells")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

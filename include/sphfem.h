@@ -371,6 +371,19 @@ int sph_jc_stats(sph_ctx *ctx, int32_t enable, int64_t *out, int32_t reset);
  * fused FP32K step from its prediction; NULL detaches. */
 int sph_mlp_attach(sph_ctx *ctx, const sph_mlp *m);
 
+/* ---- launch shapes -------------------------------------------------------------
+ * No counterpart in the reference (its launches are fixed at 256 threads).
+ * The fused FP32K neighbour-sum kernel is compiled for several launch shapes
+ * (threads per block, minimum resident blocks per SM); an autotuner times the
+ * step with each and sets the fastest.  Variant 0 is the default. */
+typedef struct sph_launch_config {
+    int32_t interact_variant;
+} sph_launch_config;
+/* *n: in, capacity of block/min_blocks (may be NULL); out, number of variants. */
+int sph_launch_variants(int32_t *n, int32_t *block, int32_t *min_blocks);
+int sph_set_launch_config(sph_ctx *ctx, const sph_launch_config *cfg);
+int sph_get_launch_config(const sph_ctx *ctx, sph_launch_config *cfg);
+
 /* ---- per-stage timing ---------------------------------------------------------
  * Runs `nsteps` fused steps without the CUDA graph, with CUDA events on the
  * context stream between the stages; stage_ms[k] receives the summed device

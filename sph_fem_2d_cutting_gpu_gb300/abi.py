@@ -118,6 +118,10 @@ MLP_NPARAMS = 8705
 JC_LOG_WIDTH = 8
 
 
+class LaunchConfig(C.Structure):
+    _fields_ = [("interact_variant", I32)]
+
+
 class CaseDesc(C.Structure):
     _fields_ = [("host", C.POINTER(Particles)), ("tool", C.POINTER(ToolMesh)), ("dt", D), ("tool_vel", D * 2),
                 ("bbmin", D * 2), ("bbmax", D * 2)]
@@ -221,6 +225,9 @@ def load() -> C.CDLL:
         "sph_jc_log_read": ([P, PF, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
         "sph_jc_stats": ([P, I32, C.POINTER(C.c_int64), I32], C.c_int),
         "sph_mlp_attach": ([P, P], C.c_int),
+        "sph_launch_variants": ([PI, PI, PI], C.c_int),
+        "sph_set_launch_config": ([P, C.POINTER(LaunchConfig)], C.c_int),
+        "sph_get_launch_config": ([P, C.POINTER(LaunchConfig)], C.c_int),
     }
     for name in STAGE_FUNCTIONS:
         proto.setdefault(name, ([P], C.c_int))

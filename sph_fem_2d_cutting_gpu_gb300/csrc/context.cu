@@ -58,6 +58,7 @@ struct sph_ctx {
     uint16_t *mlp_wb = nullptr;
     MlpDev mlp{};
     bool mlp_on = false;
+    int interact_variant = 0;            // launch shape of the fused FP32K neighbour sums
     std::vector<void *> allocs;
     std::string err;
 };
@@ -270,7 +271,8 @@ int issue_fused_body(sph_ctx *ctx, int64_t &n) {
         n += 1;
     }
     if (ctx->mlp_on) CK(cudaMemsetAsync(ctx->jc_list_count, 0, sizeof(int32_t), s));
-    launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, ctx->seg, ctx->tool_dev, true);
+    launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, ctx->seg, ctx->tool_dev, true,
+                        ctx->interact_variant);
     n += 1;
     if (ctx->mlp_on) {
         launch_jc_warm(s, jc_warm_grid(ctx), ctx->K, B, ctx->F, ctx->tool_dev, ctx->mlp, ctx->W.secant_iters,
@@ -1083,7 +1085,8 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
         if (ctx->has_tool) launch_fem_half(s, ctx->K, ctx->fem, ctx->tool_dev);
         CK(cudaEventRecord(ev[4], s));
         if (ctx->mlp_on) CK(cudaMemsetAsync(ctx->jc_list_count, 0, sizeof(int32_t), s));
-        launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, ctx->seg, ctx->tool_dev, true);
+        launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, ctx->seg, ctx->tool_dev, true,
+                            ctx->interact_variant);
         if (ctx->mlp_on) {
             launch_jc_warm(s, jc_warm_grid(ctx), ctx->K, B, ctx->F, ctx->tool_dev, ctx->mlp, ctx->W.secant_iters,
                            ctx->W.status);
@@ -1517,6 +1520,39 @@ int sph_mlp_attach(sph_ctx *ctx, const sph_mlp *m) {
     ctx->K.jc_list = ctx->jc_list;
     ctx->K.jc_list_count = ctx->jc_list_count;
     invalidate_graphs(ctx);
+    return SPH_OK;
+}
+
+// ---- launch shapes (autotuning) -------------------------------------------------------------------
+int sph_launch_variants(int32_t *n, int32_t *block, int32_t *min_blocks) {
+    if (!n) return SPH_ERR_INVALID;
+    const int nv = interact_variant_count();
+    for (int v = 0; v < nv && (block || min_blocks); v++) {
+        int b, m;
+        interact_variant_shape(v, &b, &m);
+        if (v < *n) {
+            if (block) block[v] = b;
+            if (min_blocks) min_blocks[v] = m;
+        }
+    }
+    *n = nv;
+    return SPH_OK;
+}
+
+int sph_set_launch_config(sph_ctx *ctx, const sph_launch_config *cfg) {
+    REQUIRE_CTX();
+    if (!cfg || cfg->interact_variant < 0 || cfg->interact_variant >= interact_variant_count())
+        return fail(ctx, SPH_ERR_INVALID, "unknown launch variant");
+    if (cfg->interact_variant != ctx->interact_variant) {
+        ctx->interact_variant = cfg->interact_variant;
+        invalidate_graphs(ctx);
+    }
+    return SPH_OK;
+}
+
+int sph_get_launch_config(const sph_ctx *ctx, sph_launch_config *cfg) {
+    if (!ctx || !cfg) return SPH_ERR_INVALID;
+    cfg->interact_variant = ctx->interact_variant;
     return SPH_OK;
 }
 

@@ -356,8 +356,10 @@ __global__ void __launch_bounds__(kBlock) k_interact64(int N, KConsts K, const i
 }
 
 // ---- FP32 with Kahan-compensated sums --------------------------------------------------
-template <bool kFused>
-__global__ void __launch_bounds__(kBlock) k_interact32(int N, KConsts K, const int32_t *__restrict__ offsets,
+// kB threads per block, at least kMinB resident blocks per SM (a register
+// budget for the compiler): the launch shapes the autotuner chooses from.
+template <bool kFused, int kB = kBlock, int kMinB = 1>
+__global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, const int32_t *__restrict__ offsets,
                                                        const float4 *__restrict__ rec, SortedFields B, FixedFields F,
                                                        SegDev seg, const ToolDev *__restrict__ tool,
                                                        int32_t *__restrict__ secant_iters, uint32_t *status) {
@@ -385,7 +387,7 @@ __global__ void __launch_bounds__(kBlock) k_interact32(int N, KConsts K, const i
     KahanF vt0 = {}, vt1 = {}, xt0 = {}, xt1 = {}, tl = {};
     const int hash = B.hash[k];
     const sph_geom_constants &g = K.g;
-    __shared__ int s_list[kPairChunk][kBlock];
+    __shared__ int s_list[kPairChunk][kB];
     int gi = 0, gj = 0, ii = 0, hi_i = 0, lo_j = 0, hi_j = 0, j = 0, j1 = 0;
     const int R = g.stencil;
     bool done = true;
@@ -530,14 +532,38 @@ __global__ void __launch_bounds__(kBlock) k_interact32(int N, KConsts K, const i
     }
 }
 
+// Launch shapes of the fused FP32K neighbour-sum kernel: (threads per block,
+// minimum resident blocks per SM).  Variant 0 is the default.
+const int kInteractVariants[][2] = {{256, 1}, {256, 3}, {128, 4}, {128, 6}, {512, 1}, {64, 8}};
+
+int interact_variant_count() { return (int)(sizeof(kInteractVariants) / sizeof(kInteractVariants[0])); }
+void interact_variant_shape(int v, int *block, int *min_blocks) {
+    *block = kInteractVariants[v][0];
+    *min_blocks = kInteractVariants[v][1];
+}
+
+template <int kB, int kMinB>
+static void launch_i32(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const SortedFields &B,
+                       const FixedFields &F, const StepScratch &W, const SegDev &seg, const ToolDev *tool) {
+    k_interact32<true, kB, kMinB><<<div_up(N, kB), kB, 0, s>>>(N, K, offsets, W.rec32, B, F, seg, tool,
+                                                                 W.secant_iters, W.status);
+}
+
 void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const SortedFields &B,
                          const FixedFields &F, const StepScratch &W, const SegDev &seg, const ToolDev *tool,
-                         bool fused) {
+                         bool fused, int variant) {
     const int grid = div_up(N, kBlock);
     if (K.precision == SPH_PREC_FP32K) {
-        if (fused)
-            k_interact32<true><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec32, B, F, seg, tool, W.secant_iters, W.status);
-        else
+        if (fused) {
+            switch (variant) {
+                case 1: launch_i32<256, 3>(s, N, K, offsets, B, F, W, seg, tool); break;
+                case 2: launch_i32<128, 4>(s, N, K, offsets, B, F, W, seg, tool); break;
+                case 3: launch_i32<128, 6>(s, N, K, offsets, B, F, W, seg, tool); break;
+                case 4: launch_i32<512, 1>(s, N, K, offsets, B, F, W, seg, tool); break;
+                case 5: launch_i32<64, 8>(s, N, K, offsets, B, F, W, seg, tool); break;
+                default: launch_i32<256, 1>(s, N, K, offsets, B, F, W, seg, tool); break;
+            }
+        } else
             k_interact32<false><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec32, B, F, seg, tool, W.secant_iters, W.status);
     } else {
         if (fused)

@@ -24,7 +24,9 @@ void launch_build_records(cudaStream_t s, int N, const KConsts &K, const SortedF
 // interactions.cu
 void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const SortedFields &B,
                          const FixedFields &F, const StepScratch &W, const SegDev &seg, const ToolDev *tool,
-                         bool fused);
+                         bool fused, int variant = 0);
+int interact_variant_count();
+void interact_variant_shape(int v, int *block, int *min_blocks);
 
 // actions.cu
 void launch_init(cudaStream_t s, int N, const SortedFields &A, const StepScratch &W);

@@ -192,6 +192,13 @@ __device__ void load_small(MlpSmall &s, const MlpDev &m) {
 // W [64 out][64 in] as the B operand of X W^T (rows n = out, K = in), or
 // transposed (rows n = in, K = out) as the B operand of dZ W.
 __device__ void load_weight(unsigned char *dst, const uint16_t *w, bool transpose) {
+    if (!transpose) {   // 8 consecutive inputs of one output = one 16-byte core-matrix row
+        for (int i = threadIdx.x; i < kMlpH * kMlpH / 8; i += blockDim.x) {
+            const int o = i >> 3, k8 = (i & 7) * 8;
+            *(uint4 *)(dst + cm_off(o, k8, 64)) = *(const uint4 *)(w + o * kMlpH + k8);
+        }
+        return;
+    }
     for (int i = threadIdx.x; i < kMlpH * kMlpH; i += blockDim.x) {
         int o = i >> 6, in = i & 63;
         int n = transpose ? in : o, k = transpose ? o : in;

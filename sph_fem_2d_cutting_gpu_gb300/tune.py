@@ -1,0 +1,85 @@
+"""Autotuner of the fused step's launch shape and cell geometry.
+
+Candidates: every compiled launch shape of the FP32K neighbour-sum kernel
+(``sph_launch_variants``: threads per block, minimum resident blocks per SM)
+times every cell geometry in ``CELL_GEOMETRIES`` (cell edge = h x factor,
+stencil half-width in cells; both cover the 2h kernel support).  Each
+candidate is timed on the workload itself with CUDA events over whole fused
+steps after a warm-up; the fastest is returned with the full table.  The
+state a trial advances is thrown away (each geometry gets a fresh context),
+so tuning does not change the run that follows.
+"""
+from __future__ import annotations
+
+import copy
+import ctypes as C
+import time
+
+from . import abi
+
+CELL_GEOMETRIES = [(1, 2), (2, 1)]
+
+
+def launch_variants():
+    lib = abi.load()
+    n = C.c_int32(0)
+    lib.sph_launch_variants(C.byref(n), None, None)
+    blk = (C.c_int32 * n.value)()
+    mb = (C.c_int32 * n.value)()
+    cap = C.c_int32(n.value)
+    lib.sph_launch_variants(C.byref(cap), blk, mb)
+    return [(blk[i], mb[i]) for i in range(n.value)]
+
+
+def set_variant(obj, v: int):
+    cfg = abi.LaunchConfig()
+    cfg.interact_variant = v
+    obj._ck(obj.lib.sph_set_launch_config(obj.ctx, C.byref(cfg)), "sph_set_launch_config")
+
+
+def _time_steps(obj, warmup: int, steps: int) -> float:
+    import torch
+    stream_ptr = C.c_void_p()
+    obj.lib.sph_get_stream(obj.ctx, C.byref(stream_ptr))
+    dev = torch.cuda.current_device()
+    ext = torch.cuda.ExternalStream(stream_ptr.value, device=torch.device("cuda", dev))
+    obj.step(warmup)
+    obj.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    obj.step(steps)
+    e1.record(ext)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def with_geometry(case, factor: int, stencil: int):
+    c = copy.copy(case)
+    g = abi.GridParams()
+    C.pointer(g)[0] = case.grid
+    g.cell_factor, g.stencil = factor, stencil
+    c.grid = g
+    return c
+
+
+def autotune(make, cases, warmup: int = 3, steps: int = 10, geometries=None, variants=None):
+    """Times every (geometry, launch variant) on contexts built by
+    ``make(cases_with_geometry)`` (a Solver or Batch factory) and returns
+    (best dict, table).  ``cases`` is a case or a list of cases."""
+    geometries = geometries or CELL_GEOMETRIES
+    all_v = launch_variants()
+    variants = list(range(len(all_v))) if variants is None else variants
+    table = []
+    t0 = time.perf_counter()
+    for factor, stencil in geometries:
+        cs = [with_geometry(c, factor, stencil) for c in cases] if isinstance(cases, list) else \
+            with_geometry(cases, factor, stencil)
+        obj = make(cs)
+        for v in variants:
+            set_variant(obj, v)
+            ms = _time_steps(obj, warmup, steps)
+            table.append(dict(cell_factor=factor, stencil=stencil, variant=v, block=all_v[v][0],
+                              min_blocks=all_v[v][1], ms_per_step=ms))
+        obj.close()
+    best = min(table, key=lambda r: r["ms_per_step"])
+    return dict(best, tune_s=time.perf_counter() - t0), table

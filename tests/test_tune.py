@@ -1,0 +1,63 @@
+"""Launch shapes and the autotuner."""
+import numpy as np
+import pytest
+
+from sph_fem_2d_cutting_gpu_gb300 import abi, setups, tune
+from sph_fem_2d_cutting_gpu_gb300.solver import Solver
+from conftest import rel_err
+
+
+def test_launch_variants_listed(lib):
+    v = tune.launch_variants()
+    assert v[0] == (256, 1)
+    assert len(v) >= 4 and len(set(v)) == len(v)
+    for block, min_blocks in v:
+        assert block % 32 == 0 and block * min_blocks <= 2048
+
+
+def test_with_geometry_copies_grid():
+    c = setups.small_cut()
+    c2 = tune.with_geometry(c, 2, 1)
+    assert (c2.grid.cell_factor, c2.grid.stencil) == (2, 1)
+    assert (c.grid.cell_factor, c.grid.stencil) == (1, 2)
+    assert c2.grid.bbmin[0] == c.grid.bbmin[0]
+
+
+def run_variants(case, steps, fields):
+    out = []
+    for v in range(len(tune.launch_variants())):
+        s = Solver(case, abi.SPH_PREC_FP32K, place_tool=False)
+        tune.set_variant(s, v)
+        s.step(steps)
+        out.append(s.download(fields))
+        s.close()
+    return out
+
+
+@pytest.mark.gpu
+def test_launch_variants_bit_identical_without_tool(lib):
+    # each particle's sums run in one thread in the same order whatever the
+    # launch shape: without a tool (no segment atomics) results are bit-identical
+    runs = run_variants(setups.micro(n_side=128, seed=3), 3, ["pos", "vel", "S", "rho", "T", "eps_pl"])
+    for v, P in enumerate(runs[1:], 1):
+        for f in P:
+            assert np.array_equal(P[f], runs[0][f]), (v, f)
+
+
+@pytest.mark.gpu
+def test_launch_variants_agree_with_tool(lib):
+    # with a tool the friction heat of a segment is an FP64 atomic sum whose
+    # order follows the launch shape: agreement to rounding
+    case = setups.placed(setups.small_cut(nx=48, ny=20), preload_dx=0.3)
+    runs = run_variants(case, 40, ["pos", "vel", "S", "T", "eps_pl", "fc", "ft"])
+    for v, P in enumerate(runs[1:], 1):
+        for f in P:
+            assert rel_err(P[f], runs[0][f]) < 1e-6, (v, f)
+
+
+@pytest.mark.gpu
+def test_autotune_returns_fastest(lib):
+    case = setups.micro(n_side=256)
+    best, table = tune.autotune(lambda c: Solver(c, abi.SPH_PREC_FP32K), case, warmup=3, steps=5)
+    assert len(table) == len(tune.CELL_GEOMETRIES) * len(tune.launch_variants())
+    assert best["ms_per_step"] == min(r["ms_per_step"] for r in table)
