@@ -410,8 +410,10 @@ def run_product(args):
         if variant_table is not None:
             from sph_fem_2d_cutting_gpu_gb300 import tune
             shapes = tune.launch_variants()
-            res["launch_tuning"] = {"chosen": {"block": shapes[best_v][0], "min_blocks": shapes[best_v][1]},
-                                    "ms_per_step": {f"{b}x{m}": t for (b, m), t in zip(shapes, variant_table)}}
+            res["launch_tuning"] = {"chosen": {"block": shapes[best_v][0], "min_blocks": shapes[best_v][1],
+                                               "staged_records": shapes[best_v][2]},
+                                    "ms_per_step": {f"{b}x{m}" + (f"s{c}" if c else ""): t
+                                                    for (b, m, c), t in zip(shapes, variant_table)}}
         # end-to-end through the C ABI with pinned host buffers
         if not args.no_e2e:
             fields = {}

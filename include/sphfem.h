@@ -54,6 +54,7 @@ enum {
 #define SPH_STATUS_FRIC_NAN       (1u << 6) /* NaN sliding velocity -> blanked (actions_gpu.cu:375-380)   */
 #define SPH_STATUS_CELL_OVERFLOW  (1u << 7) /* a cell held more particles than the in-cell ranker allows  */
 #define SPH_STATUS_MMA_TIMEOUT    (1u << 8) /* a tensor-core wait of the learned warm start gave up (1 s)  */
+#define SPH_STATUS_COPY_TIMEOUT   (1u << 9) /* a staged neighbour copy did not complete in 1 s (global loads used) */
 
 /* ---- precision of the particle path ------------------------------------ */
 enum {
@@ -374,13 +375,15 @@ int sph_mlp_attach(sph_ctx *ctx, const sph_mlp *m);
 /* ---- launch shapes -------------------------------------------------------------
  * No counterpart in the reference (its launches are fixed at 256 threads).
  * The fused FP32K neighbour-sum kernel is compiled for several launch shapes
- * (threads per block, minimum resident blocks per SM); an autotuner times the
- * step with each and sets the fastest.  Variant 0 is the default. */
+ * (threads per block, minimum resident blocks per SM, and the number of
+ * neighbour records a block stages in shared memory -- 0 for global loads);
+ * an autotuner times the step with each and sets the fastest.  Variant 0 is
+ * the default. */
 typedef struct sph_launch_config {
     int32_t interact_variant;
 } sph_launch_config;
-/* *n: in, capacity of block/min_blocks (may be NULL); out, number of variants. */
-int sph_launch_variants(int32_t *n, int32_t *block, int32_t *min_blocks);
+/* *n: in, capacity of the output arrays (each may be NULL); out, number of variants. */
+int sph_launch_variants(int32_t *n, int32_t *block, int32_t *min_blocks, int32_t *staged_records);
 int sph_set_launch_config(sph_ctx *ctx, const sph_launch_config *cfg);
 int sph_get_launch_config(const sph_ctx *ctx, sph_launch_config *cfg);
 

@@ -25,6 +25,8 @@ STATUS_BITS = {
     "melt_blanked": 1 << 5,
     "fric_nan": 1 << 6,
     "cell_overflow": 1 << 7,
+    "mma_timeout": 1 << 8,
+    "copy_timeout": 1 << 9,
 }
 
 D = C.c_double
@@ -225,7 +227,7 @@ def load() -> C.CDLL:
         "sph_jc_log_read": ([P, PF, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
         "sph_jc_stats": ([P, I32, C.POINTER(C.c_int64), I32], C.c_int),
         "sph_mlp_attach": ([P, P], C.c_int),
-        "sph_launch_variants": ([PI, PI, PI], C.c_int),
+        "sph_launch_variants": ([PI, PI, PI, PI], C.c_int),
         "sph_set_launch_config": ([P, C.POINTER(LaunchConfig)], C.c_int),
         "sph_get_launch_config": ([P, C.POINTER(LaunchConfig)], C.c_int),
     }

@@ -122,7 +122,13 @@ __device__ __forceinline__ uint32_t contact_s1_one(const KConsts &K, double dt, 
                                                    int &on_seg, double &blanked) {
     int inside = 0;
     double ddx = pos.x - tool.tl_point_ref[0], ddy = pos.y - tool.tl_point_ref[1];
-    if (sqrt(ddx * ddx + ddy * ddy) < 1.05 * tool.ref_dist) inside = inside_judgement(pos, seg.left, seg.right, seg.n);
+    // A segment counts a crossing only if the particle's y lies in its float-rounded
+    // y-range (on_segment_mesh); float rounding is monotone, so a particle outside the
+    // rounded y-range of all segments has no crossing and the scan is skipped.
+    // (the y test first: both tests are pure, and it spares most particles the FP64 sqrt)
+    if (pos.y <= (double)(float)tool.seg_ymax && pos.y >= (double)(float)tool.seg_ymin &&
+        sqrt(ddx * ddx + ddy * ddy) < 1.05 * tool.ref_dist)
+        inside = inside_judgement(pos, seg.left, seg.right, seg.n);
     if (inside == 0) {
         fc = make_double2(0., 0.); ft = make_double2(0., 0.); nrm = make_double2(0., 0.);
         on_seg = -1;
@@ -295,8 +301,8 @@ __global__ void __launch_bounds__(kBlock) k_step_tail(int N, KConsts K, SortedFi
         int h;
         if (!blanked) {
             const sph_geom_constants &g = K.g;
-            int ix = __double2int_rz((pos.x - g.bbmin_x) / g.dx);
-            int iy = __double2int_rz((pos.y - g.bbmin_y) / g.dx);
+            int ix = cell_coord(pos.x, g.bbmin_x, g.dx, K.f.inv_cell);
+            int iy = cell_coord(pos.y, g.bbmin_y, g.dx, K.f.inv_cell);
             h = ix * g.ny + iy;
         } else {
             h = A.hash[i];   // blanked particles keep their stale hash

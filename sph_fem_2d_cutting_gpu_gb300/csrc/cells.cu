@@ -20,14 +20,14 @@ __global__ void __launch_bounds__(kBlock) k_hash_count(int N, const double2 *__r
                                                        const double *__restrict__ blanked, int32_t *__restrict__ hash,
                                                        int32_t *__restrict__ key, int32_t *__restrict__ arrival,
                                                        int32_t *__restrict__ counts, int32_t *__restrict__ hash_next,
-                                                       sph_geom_constants g, uint32_t *status) {
+                                                       sph_geom_constants g, float inv_dxf, uint32_t *status) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     int h;
     if (kHash && blanked[i] != 1.) {
         double2 p = pos[i];
-        int ix = __double2int_rz((p.x - g.bbmin_x) / g.dx);
-        int iy = __double2int_rz((p.y - g.bbmin_y) / g.dx);
+        int ix = cell_coord(p.x, g.bbmin_x, g.dx, inv_dxf);
+        int iy = cell_coord(p.y, g.bbmin_y, g.dx, inv_dxf);
         h = ix * g.ny + iy;
         hash[i] = h;
     } else {
@@ -428,7 +428,8 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused32(int N, const int32_t 
 // ---- host launchers ---------------------------------------------------------------------
 void launch_hash(cudaStream_t s, int N, const SortedFields &A, sph_geom_constants g) {
     k_hash_count<true, false><<<div_up(N, kBlock), kBlock, 0, s>>>(N, A.pos, A.blanked, A.hash, nullptr, nullptr,
-                                                                     nullptr, nullptr, g, nullptr);
+                                                                     nullptr, nullptr, g, (float)(1.0 / g.dx),
+                                                                     nullptr);
 }
 
 void launch_count(cudaStream_t s, int N, const SortedFields &A, const SortScratch &X, sph_geom_constants g,
@@ -436,10 +437,10 @@ void launch_count(cudaStream_t s, int N, const SortedFields &A, const SortScratc
     cudaMemsetAsync(X.counts, 0, sizeof(int32_t) * (size_t)(g.num_cell + 1), s);
     if (with_hash)
         k_hash_count<true, true><<<div_up(N, kBlock), kBlock, 0, s>>>(N, A.pos, A.blanked, A.hash, X.key, X.arrival,
-                                                                       X.counts, X.hash_next, g, status);
+                                                                       X.counts, X.hash_next, g, (float)(1.0 / g.dx), status);
     else
         k_hash_count<false, true><<<div_up(N, kBlock), kBlock, 0, s>>>(N, A.pos, A.blanked, A.hash, X.key, X.arrival,
-                                                                        X.counts, X.hash_next, g, status);
+                                                                        X.counts, X.hash_next, g, (float)(1.0 / g.dx), status);
 }
 
 int scan_blocks(int num_cell) { return div_up(num_cell + 1, kScanTile); }

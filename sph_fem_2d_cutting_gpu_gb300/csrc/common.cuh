@@ -31,6 +31,7 @@ struct JcF32 {   // Johnson-Cook constants in FP32 (plasticity.cuh:21-39)
 struct KF32 {
     float mass, inv_mass, xs_mass, alpha, beta, eta2, inv_wdp, cell, G, K_bulk, c0sq, stresseps;
     float dt, hdt, inv_dt, tq_over_cp, alpha_wp, alpha_tool_sph, T_init;
+    float inv_cell;   // (float)(1 / cell edge), for cell_coord
     JcF32 jc;
 };
 
@@ -110,9 +111,23 @@ __device__ __forceinline__ bool is_nan_or_inf(double v) {          // isnan(v) |
     return (__double_as_longlong(v) & 0x7FF0000000000000LL) == 0x7FF0000000000000LL;
 }
 
-// compute_hashes' cell index (int)((x - bbmin)/dx) (grid.cu:36-39).
-__device__ __forceinline__ int cell_coord(double x, double bbmin, double dx) {
-    return __double2int_rz((x - bbmin) / dx);
+// compute_hashes' cell index (int)((x - bbmin)/dx) (grid.cu:36-39), bit for bit.
+// The quotient is first formed in FP32 with inv_dxf = (float)(1/dx): against the
+// FP64 quotient its error is below 3*2^-24 relative (three FP32 roundings and the
+// FP64 division's own), so when its fractional part is more than 2.5e-7*q away
+// from an integer both truncate to the same cell and the FP64 division -- a long
+// sequence on GB300's narrow FP64 pipe -- is skipped.  Negative, huge or
+// non-finite offsets take the FP64 division.
+__device__ __forceinline__ int cell_coord(double x, double bbmin, double dx, float inv_dxf) {
+    const double a = x - bbmin;
+    if (a >= 0.) {
+        const float qf = (float)a * inv_dxf;
+        const float t = truncf(qf);
+        const float fr = qf - t;
+        const float m = 2.5e-7f * qf + 1e-30f;
+        if (fr > m && fr < 1.f - m) return (int)t;
+    }
+    return __double2int_rz(a / dx);
 }
 
 // Device copy of the rigid tool kinematics that tool_FEM keeps on the host
@@ -129,6 +144,7 @@ struct ToolDev {
     double dt, hdt;                 // time step of the case and half of it
     float dtf, hdtf, inv_dtf;       // the same in FP32
     int32_t seg_first, seg_count;   // the case's interface segments
+    double seg_ymin, seg_ymax;      // y-range of those segments (moved with them)
 };
 
 // ---- float narrowings of the reference (double argument -> float call) ------

@@ -134,6 +134,7 @@ void derive(KConsts &K) {
     f.eta2 = (float)K.eta2;
     f.inv_wdp = (float)K.inv_wdeltap;
     f.cell = (float)K.g.dx;
+    f.inv_cell = (float)(1.0 / K.g.dx);
     f.G = (float)K.c.phys.G;
     f.K_bulk = (float)K.c.phys.K;
     f.c0sq = (float)K.c0sq;
@@ -515,6 +516,13 @@ ToolDev tool_state_of(const ToolModelHost &M, double dt, int seg_first) {
     td.ref_dist = M.ref_dist; td.lowest_point = M.lowest_point; td.right_point = M.right_point;
     td.seg_first = seg_first;
     td.seg_count = M.n_seg;
+    td.seg_ymin = INFINITY;
+    td.seg_ymax = -INFINITY;
+    for (int s = 0; s < M.n_seg; s++)
+        for (double y : {M.left[2 * s + 1], M.right[2 * s + 1]}) {
+            td.seg_ymin = std::min(td.seg_ymin, y);
+            td.seg_ymax = std::max(td.seg_ymax, y);
+        }
     set_case_dt(td, dt);
     return td;
 }
@@ -1524,16 +1532,15 @@ int sph_mlp_attach(sph_ctx *ctx, const sph_mlp *m) {
 }
 
 // ---- launch shapes (autotuning) -------------------------------------------------------------------
-int sph_launch_variants(int32_t *n, int32_t *block, int32_t *min_blocks) {
+int sph_launch_variants(int32_t *n, int32_t *block, int32_t *min_blocks, int32_t *staged_records) {
     if (!n) return SPH_ERR_INVALID;
     const int nv = interact_variant_count();
-    for (int v = 0; v < nv && (block || min_blocks); v++) {
-        int b, m;
-        interact_variant_shape(v, &b, &m);
-        if (v < *n) {
-            if (block) block[v] = b;
-            if (min_blocks) min_blocks[v] = m;
-        }
+    for (int v = 0; v < nv && v < *n; v++) {
+        int b, m, st;
+        interact_variant_shape(v, &b, &m, &st);
+        if (block) block[v] = b;
+        if (min_blocks) min_blocks[v] = m;
+        if (staged_records) staged_records[v] = st;
     }
     *n = nv;
     return SPH_OK;

@@ -145,6 +145,11 @@ __global__ void __launch_bounds__(kBlock) k_tool_move(KConsts K, SegDev seg, Fem
         node_move(F, i, tc.vel, per_case ? tc.dt : dt);
     }
     if ((what & 2) && i < (per_case ? K.n_cases : 1)) tool_state_move(tool + i, per_case ? tool[i].dt : dt);
+    if ((what & 1) && i < (per_case ? K.n_cases : 1)) {   // the segments' y-range, with segment_move's arithmetic
+        const double dy = __dadd_rn(__dmul_rn(tool[i].vel[1], per_case ? tool[i].dt : dt), 0.);
+        tool[i].seg_ymin = __dadd_rn(tool[i].seg_ymin, dy);
+        tool[i].seg_ymax = __dadd_rn(tool[i].seg_ymax, dy);
+    }
 }
 
 // ---- host launchers ---------------------------------------------------------------------------

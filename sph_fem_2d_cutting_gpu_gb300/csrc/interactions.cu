@@ -25,6 +25,7 @@
 // (actions_gpu.cu:689-754).  Correct writes the start-of-step arrays in
 // place (only this thread touches them); neighbours read the predicted state
 // from the records, so there is no read/write race.
+#include "async.cuh"
 #include "launch.cuh"
 
 namespace sphfem {
@@ -356,14 +357,84 @@ __global__ void __launch_bounds__(kBlock) k_interact64(int N, KConsts K, const i
 }
 
 // ---- FP32 with Kahan-compensated sums --------------------------------------------------
+// Staged blocks: the records of the block's cells and their stencil halo,
+// one contiguous run per grid column (cells are column-major in the sorted
+// order), copied into shared memory by the bulk-copy engine before the pair
+// loops.  Staged only when all of the block's particles lie in one grid column
+// and the region holds at most `cap` records; otherwise global loads.
+struct StageHdr {
+    int staged, ix, r_lo, r_hi, c_lo;
+    int delta[2 * kMaxStencil + 1];   // shared slot minus global record index, per column
+};
+
+__device__ __forceinline__ void stage_issue(int N, int kB, const KConsts &K, const int32_t *__restrict__ offsets,
+                                            const float4 *__restrict__ rec, const SortedFields &B, int cap,
+                                            float4 *srec, StageHdr &h, uint32_t mbar) {
+    const sph_geom_constants &g = K.g;
+    const int R = g.stencil;
+    const int b0 = blockIdx.x * kB;
+    const int hf = B.hash[b0], hl = B.hash[min(b0 + kB, N) - 1];
+    h.staged = 0;
+    if (hf < 0 || hl >= g.num_cell || hl < hf) return;
+    const int ix = hf / g.ny;
+    if (hl / g.ny != ix) return;
+    const int r_lo = max(hf - ix * g.ny - R, 0), r_hi = min(hl - ix * g.ny + R, g.ny - 1);
+    const int c_lo = max(ix - R, 0), c_hi = min(ix + R, g.nx - 1);
+    int total = 0, start[2 * kMaxStencil + 1], len[2 * kMaxStencil + 1];
+    for (int c = c_lo; c <= c_hi; c++) {
+        start[c - c_lo] = __ldg(offsets + c * g.ny + r_lo);
+        len[c - c_lo] = __ldg(offsets + c * g.ny + r_hi + 1) - start[c - c_lo];
+        h.delta[c - c_lo] = total - start[c - c_lo];
+        total += len[c - c_lo];
+    }
+    if (total <= 0 || total > cap) return;
+    mbar_init(mbar);
+    mbar_arrive_expect_tx(mbar, (uint32_t)total * 64u);
+    for (int c = c_lo; c <= c_hi; c++)
+        if (len[c - c_lo] > 0)
+            bulk_g2s(smem_u32(srec + 4 * (start[c - c_lo] + h.delta[c - c_lo])), rec + 4 * (size_t)start[c - c_lo],
+                     (uint32_t)len[c - c_lo] * 64u, mbar);
+    h.staged = 1;
+    h.ix = ix;
+    h.r_lo = r_lo;
+    h.r_hi = r_hi;
+    h.c_lo = c_lo;
+}
+
 // kB threads per block, at least kMinB resident blocks per SM (a register
 // budget for the compiler): the launch shapes the autotuner chooses from.
-template <bool kFused, int kB = kBlock, int kMinB = 1>
+// kStaged: neighbour records from shared memory (dynamic: cap records + the
+// pair lists).
+template <bool kFused, int kB = kBlock, int kMinB = 1, bool kStaged = false>
 __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, const int32_t *__restrict__ offsets,
                                                        const float4 *__restrict__ rec, SortedFields B, FixedFields F,
                                                        SegDev seg, const ToolDev *__restrict__ tool,
-                                                       int32_t *__restrict__ secant_iters, uint32_t *status) {
+                                                       int32_t *__restrict__ secant_iters, uint32_t *status,
+                                                       int cap) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int (*s_list)[kB];
+    const float4 *nrec = rec;   // where the neighbour records are read from
+    __shared__ StageHdr s_hdr;
+    __shared__ alignas(8) unsigned long long s_mbar;
+    bool staged = false;
+    if constexpr (kStaged) {
+        extern __shared__ __align__(128) float4 s_dyn[];
+        s_list = (int (*)[kB])(s_dyn + 4 * cap);
+        if (threadIdx.x == 0) stage_issue(N, kB, K, offsets, rec, B, cap, s_dyn, s_hdr, smem_u32(&s_mbar));
+        __syncthreads();
+        if (s_hdr.staged) {
+            staged = mbar_wait(smem_u32(&s_mbar), 0);
+            if (staged) {
+                nrec = s_dyn;
+            } else {   // copies late: report, wait once more (bounded) for them, use global loads
+                if (threadIdx.x == 0) set_status(status, SPH_STATUS_COPY_TIMEOUT);
+                mbar_wait(smem_u32(&s_mbar), 0);
+            }
+        }
+    } else {
+        __shared__ int s_list_st[kPairChunk][kB];
+        s_list = s_list_st;
+    }
     if (k >= N) return;
     const float4 i0 = rec[4 * k + 0];
     const int fi = __float_as_int(i0.z);
@@ -387,7 +458,6 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
     KahanF vt0 = {}, vt1 = {}, xt0 = {}, xt1 = {}, tl = {};
     const int hash = B.hash[k];
     const sph_geom_constants &g = K.g;
-    __shared__ int s_list[kPairChunk][kB];
     int gi = 0, gj = 0, ii = 0, hi_i = 0, lo_j = 0, hi_j = 0, j = 0, j1 = 0;
     const int R = g.stencil;
     bool done = true;
@@ -402,6 +472,17 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
         j1 = __ldg(offsets + ii * g.ny + hi_j);
         done = false;
     }
+    // a particle whose stencil lies inside the staged region reads shared memory
+    // (slot = global index + per-column delta); any other uses global loads
+    bool use_s = false;
+    if constexpr (kStaged) {
+        use_s = staged && !done && gi == s_hdr.ix && lo_j >= s_hdr.r_lo && hi_j - 1 <= s_hdr.r_hi;
+        if (use_s) {
+            j += s_hdr.delta[ii - s_hdr.c_lo];
+            j1 += s_hdr.delta[ii - s_hdr.c_lo];
+        }
+    }
+    const float4 *__restrict__ nb = use_s ? nrec : rec;
     while (!done) {
         // phase 1: collect the next in-support, active neighbours (column offset packed in 3 bits);
         // four candidates per round keep four loads in flight
@@ -410,7 +491,7 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
             if (j + 4 <= j1 && cnt <= kPairChunk - 4) {
                 float4 n[4];
 #pragma unroll
-                for (int u = 0; u < 4; u++) n[u] = rec[4 * (j + u)];
+                for (int u = 0; u < 4; u++) n[u] = nb[4 * (j + u)];
                 const float dxc = (float)(gi - ii) * cell;
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
@@ -423,7 +504,7 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
                 }
                 j += 4;
             } else if (j < j1) {
-                const float4 n0 = rec[4 * j + 0];
+                const float4 n0 = nb[4 * j + 0];
                 const int fj = __float_as_int(n0.z);
                 const float dx = (float)(gi - ii) * cell + (xri - n0.x);
                 const float dy = (float)(gj - (fj & kRowMask)) * cell + (yri - n0.y);
@@ -437,6 +518,12 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
                 }
                 j = __ldg(offsets + ii * g.ny + lo_j);
                 j1 = __ldg(offsets + ii * g.ny + hi_j);
+                if constexpr (kStaged) {
+                    if (use_s) {
+                        j += s_hdr.delta[ii - s_hdr.c_lo];
+                        j1 += s_hdr.delta[ii - s_hdr.c_lo];
+                    }
+                }
             }
         }
         // phase 2: the pair body over the collected list, lanes in step; the
@@ -446,7 +533,7 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
         if (cnt > 0) {
             pe = s_list[0][threadIdx.x];
             const int jp = pe >> 3;
-            p0 = rec[4 * jp + 0]; p1 = rec[4 * jp + 1]; p2 = rec[4 * jp + 2]; p3 = rec[4 * jp + 3];
+            p0 = nb[4 * jp + 0]; p1 = nb[4 * jp + 1]; p2 = nb[4 * jp + 2]; p3 = nb[4 * jp + 3];
         }
         for (int t = 0; t < cnt; t++) {
             const int e = pe;
@@ -454,7 +541,7 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
             if (t + 1 < cnt) {
                 pe = s_list[t + 1][threadIdx.x];
                 const int jp = pe >> 3;
-                p0 = rec[4 * jp + 0]; p1 = rec[4 * jp + 1]; p2 = rec[4 * jp + 2]; p3 = rec[4 * jp + 3];
+                p0 = nb[4 * jp + 0]; p1 = nb[4 * jp + 1]; p2 = nb[4 * jp + 2]; p3 = nb[4 * jp + 3];
             }
             {
                 const int fj = __float_as_int(n0.z);
@@ -533,20 +620,33 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
 }
 
 // Launch shapes of the fused FP32K neighbour-sum kernel: (threads per block,
-// minimum resident blocks per SM).  Variant 0 is the default.
-const int kInteractVariants[][2] = {{256, 1}, {256, 3}, {128, 4}, {128, 6}, {512, 1}, {64, 8}};
+// minimum resident blocks per SM, staged records: 0 = global loads).
+// Variant 0 is the default.
+const int kInteractVariants[][3] = {{256, 1, 0},   {256, 3, 0},   {128, 4, 0},  {128, 6, 0},  {512, 1, 0},
+                                    {64, 8, 0},    {128, 3, 640}, {128, 2, 1024}, {64, 6, 384}, {256, 2, 1024}};
 
 int interact_variant_count() { return (int)(sizeof(kInteractVariants) / sizeof(kInteractVariants[0])); }
-void interact_variant_shape(int v, int *block, int *min_blocks) {
+void interact_variant_shape(int v, int *block, int *min_blocks, int *staged) {
     *block = kInteractVariants[v][0];
     *min_blocks = kInteractVariants[v][1];
+    *staged = kInteractVariants[v][2];
 }
 
-template <int kB, int kMinB>
+template <int kB, int kMinB, bool kStaged>
 static void launch_i32(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const SortedFields &B,
-                       const FixedFields &F, const StepScratch &W, const SegDev &seg, const ToolDev *tool) {
-    k_interact32<true, kB, kMinB><<<div_up(N, kB), kB, 0, s>>>(N, K, offsets, W.rec32, B, F, seg, tool,
-                                                                 W.secant_iters, W.status);
+                       const FixedFields &F, const StepScratch &W, const SegDev &seg, const ToolDev *tool, int cap) {
+    size_t smem = 0;
+    if (kStaged) {
+        smem = (size_t)cap * 64 + sizeof(int) * kPairChunk * kB;
+        static bool configured = false;   // opt in above 48 KB of dynamic shared memory, once
+        if (!configured) {
+            cudaFuncSetAttribute(k_interact32<true, kB, kMinB, kStaged>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+            configured = true;
+        }
+    }
+    k_interact32<true, kB, kMinB, kStaged><<<div_up(N, kB), kB, smem, s>>>(N, K, offsets, W.rec32, B, F, seg, tool,
+                                                                           W.secant_iters, W.status, cap);
 }
 
 void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const SortedFields &B,
@@ -556,15 +656,20 @@ void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t 
     if (K.precision == SPH_PREC_FP32K) {
         if (fused) {
             switch (variant) {
-                case 1: launch_i32<256, 3>(s, N, K, offsets, B, F, W, seg, tool); break;
-                case 2: launch_i32<128, 4>(s, N, K, offsets, B, F, W, seg, tool); break;
-                case 3: launch_i32<128, 6>(s, N, K, offsets, B, F, W, seg, tool); break;
-                case 4: launch_i32<512, 1>(s, N, K, offsets, B, F, W, seg, tool); break;
-                case 5: launch_i32<64, 8>(s, N, K, offsets, B, F, W, seg, tool); break;
-                default: launch_i32<256, 1>(s, N, K, offsets, B, F, W, seg, tool); break;
+                case 1: launch_i32<256, 3, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+                case 2: launch_i32<128, 4, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+                case 3: launch_i32<128, 6, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+                case 4: launch_i32<512, 1, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+                case 5: launch_i32<64, 8, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+                case 6: launch_i32<128, 3, true>(s, N, K, offsets, B, F, W, seg, tool, 640); break;
+                case 7: launch_i32<128, 2, true>(s, N, K, offsets, B, F, W, seg, tool, 1024); break;
+                case 8: launch_i32<64, 6, true>(s, N, K, offsets, B, F, W, seg, tool, 384); break;
+                case 9: launch_i32<256, 2, true>(s, N, K, offsets, B, F, W, seg, tool, 1024); break;
+                default: launch_i32<256, 1, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
             }
         } else
-            k_interact32<false><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec32, B, F, seg, tool, W.secant_iters, W.status);
+            k_interact32<false><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec32, B, F, seg, tool, W.secant_iters, W.status,
+                                                        0);
     } else {
         if (fused)
             k_interact64<true><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec64, B, F, seg, tool, W.secant_iters, W.status);

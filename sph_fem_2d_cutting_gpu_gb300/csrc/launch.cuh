@@ -26,7 +26,7 @@ void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t 
                          const FixedFields &F, const StepScratch &W, const SegDev &seg, const ToolDev *tool,
                          bool fused, int variant = 0);
 int interact_variant_count();
-void interact_variant_shape(int v, int *block, int *min_blocks);
+void interact_variant_shape(int v, int *block, int *min_blocks, int *staged);
 
 // actions.cu
 void launch_init(cudaStream_t s, int N, const SortedFields &A, const StepScratch &W);

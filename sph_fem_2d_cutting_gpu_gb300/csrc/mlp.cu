@@ -17,6 +17,7 @@
 // and an orderly exit that still frees TMEM).
 #include <cuda_bf16.h>
 
+#include "async.cuh"
 #include "launch.cuh"
 
 namespace sphfem {
@@ -25,15 +26,12 @@ namespace {
 constexpr int kTile = 128;                 // samples per tile = threads per CTA
 constexpr uint32_t kTmemCols = 256;        // training: [0,64) layer, [64,192) stacked dW
 constexpr uint32_t kTmemColsFwd = 64;      // inference
-constexpr unsigned long long kWaitNs = 1000000000ull;   // 1 s
 
 // Instruction descriptor of tcgen05.mma kind::f16: D F32 (bits 4-5 = 1), A and
 // B BF16 (bits 7-9, 10-12 = 1), both K-major, N>>3 at bit 17, M>>4 at bit 24.
 constexpr uint32_t idesc_bf16(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 // Byte offset of element (row r, column k) of a K-major BF16 operand with kt
 // columns: 8x8 core matrices of 8 rows x 16 bytes (128 contiguous bytes);
@@ -77,34 +75,6 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t mbar) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(1) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-// Bounded wait for the phase `parity` of the mbarrier to complete.
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-    const unsigned long long t0 = global_ns();
-    for (uint32_t it = 0; it < (1u << 26); it++) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(mbar), "r"(parity)
-            : "memory");
-        if (done) return true;
-        if ((it & 63) == 63 && global_ns() - t0 > kWaitNs) return false;
-    }
-    return false;
-}
 
 // Whole warp: allocate `ncols` TMEM columns, address written to smem slot.
 __device__ __forceinline__ void tmem_alloc(uint32_t slot_saddr, uint32_t ncols) {

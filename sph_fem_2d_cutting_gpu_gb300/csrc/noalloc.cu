@@ -62,14 +62,14 @@ __host__ __device__ inline ScratchView carve(int32_t *base) {
 __global__ void __launch_bounds__(kBlock) k_na_hash_count(int n, const double2 *__restrict__ pos,
                                                           const double *__restrict__ blanked,
                                                           int32_t *__restrict__ hash, sph_geom_constants g,
-                                                          ScratchView X) {
+                                                          float inv_dxf, ScratchView X) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int h;
     if (blanked[i] != 1.) {
         double2 p = pos[i];
-        int ix = __double2int_rz((p.x - g.bbmin_x) / g.dx);
-        int iy = __double2int_rz((p.y - g.bbmin_y) / g.dx);
+        int ix = cell_coord(p.x, g.bbmin_x, g.dx, inv_dxf);
+        int iy = cell_coord(p.y, g.bbmin_y, g.dx, inv_dxf);
         h = ix * g.ny + iy;
         hash[i] = h;
     } else {
@@ -205,7 +205,7 @@ extern "C" int sph_cells_build_noalloc(const double *pos, const double *blanked,
     cudaError_t e = cudaMemsetAsync(X.counts, 0, sizeof(int32_t) * (size_t)buckets, s);
     if (e == cudaSuccess) {
         const int grid = div_up(n, kBlock);
-        k_na_hash_count<<<grid, kBlock, 0, s>>>(n, (const double2 *)pos, blanked, hash, *g, X);
+        k_na_hash_count<<<grid, kBlock, 0, s>>>(n, (const double2 *)pos, blanked, hash, *g, (float)(1.0 / g->dx), X);
         k_na_scan<<<1, 1024, 0, s>>>(buckets, g->num_cell, X, cell_start, cell_end);
         k_na_scatter<<<grid, kBlock, 0, s>>>(n, X);
         k_na_rank<<<grid, kBlock, 0, s>>>(n, X, hash, perm, hash_sorted);

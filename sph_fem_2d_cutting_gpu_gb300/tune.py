@@ -1,7 +1,8 @@
 """Autotuner of the fused step's launch shape and cell geometry.
 
 Candidates: every compiled launch shape of the FP32K neighbour-sum kernel
-(``sph_launch_variants``: threads per block, minimum resident blocks per SM)
+(``sph_launch_variants``: threads per block, minimum resident blocks per SM,
+neighbour records staged in shared memory)
 times every cell geometry in ``CELL_GEOMETRIES`` (cell edge = h x factor,
 stencil half-width in cells; both cover the 2h kernel support).  Each
 candidate is timed on the workload itself with CUDA events over whole fused
@@ -21,14 +22,16 @@ CELL_GEOMETRIES = [(1, 2), (2, 1)]
 
 
 def launch_variants():
+    """[(threads per block, min blocks per SM, staged records)] of the compiled shapes."""
     lib = abi.load()
     n = C.c_int32(0)
-    lib.sph_launch_variants(C.byref(n), None, None)
+    lib.sph_launch_variants(C.byref(n), None, None, None)
     blk = (C.c_int32 * n.value)()
     mb = (C.c_int32 * n.value)()
+    st = (C.c_int32 * n.value)()
     cap = C.c_int32(n.value)
-    lib.sph_launch_variants(C.byref(cap), blk, mb)
-    return [(blk[i], mb[i]) for i in range(n.value)]
+    lib.sph_launch_variants(C.byref(cap), blk, mb, st)
+    return [(blk[i], mb[i], st[i]) for i in range(n.value)]
 
 
 def set_variant(obj, v: int):
@@ -79,7 +82,7 @@ def autotune(make, cases, warmup: int = 3, steps: int = 10, geometries=None, var
             set_variant(obj, v)
             ms = _time_steps(obj, warmup, steps)
             table.append(dict(cell_factor=factor, stencil=stencil, variant=v, block=all_v[v][0],
-                              min_blocks=all_v[v][1], ms_per_step=ms))
+                              min_blocks=all_v[v][1], staged=all_v[v][2], ms_per_step=ms))
         obj.close()
     best = min(table, key=lambda r: r["ms_per_step"])
     return dict(best, tune_s=time.perf_counter() - t0), table

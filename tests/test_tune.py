@@ -9,10 +9,13 @@ from conftest import rel_err
 
 def test_launch_variants_listed(lib):
     v = tune.launch_variants()
-    assert v[0] == (256, 1)
+    assert v[0] == (256, 1, 0)
     assert len(v) >= 4 and len(set(v)) == len(v)
-    for block, min_blocks in v:
+    assert any(c > 0 for _, _, c in v)
+    for block, min_blocks, staged in v:
         assert block % 32 == 0 and block * min_blocks <= 2048
+        # staged records + pair lists fit the 227 KB a block may use
+        assert staged * 64 + 32 * block * 4 <= 227 * 1024
 
 
 def test_with_geometry_copies_grid():
