@@ -49,6 +49,11 @@ ALGO_BYTES = {
     "fp32k": dict(read=64 + 4 + (16 + 16 + 32 + 8 + 8) + 32 + 8 + 16 + 16 + 16 + 8 + 8 + 8 + 8,
                   write=(16 + 16 + 32 + 8 + 8) + (16 + 16 + 32 + 8 + 8) + 8 + 8 + 4),
 }
+# DRAM bytes (read + write) per particle of one full-size launch of the fused
+# neighbour sums, from ncu on the 2048x2048 micro workload with 2h cells
+# (dram__bytes_read.sum 991,403,264 + dram__bytes_write.sum 706,622,464 for
+# 4,194,304 particles, k_interact32<fused, 64x8>; one-pass capture).
+NCU_TRAFFIC_PER_PARTICLE = {"fp32k": (991_403_264 + 706_622_464) / 4_194_304}
 STAGES = ["hash+histogram", "scan+scatter+rank", "reorder+predict+eos+artstress+records", "fem half step",
           "neighbour sums+epilogue", "fem update+tool move", "contact/bc/invalidate tail"]
 # fields a caller moves per step in the end-to-end arm (the persistent state)
@@ -380,13 +385,15 @@ def run_product(args):
             tune.set_variant(s, best_v)
             s.upload(P0)
             del P0
+        # clock samples (every 200 ms) span the loaded period around the timed steps:
+        # warm-up, timed steps, stage profile and the end-to-end loop
+        clocks = Clocks(local) if rank == 0 else None
         for _ in range(args.warmup):
             s.step()
         s.sync()
         torch.cuda.synchronize()
         barrier()
         torch.cuda.synchronize()
-        clocks = Clocks(local) if rank == 0 else None
         n0 = s.launch_count()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(ext)
@@ -396,7 +403,6 @@ def run_product(args):
         launches = s.launch_count() - n0
         torch.cuda.synchronize()
         barrier()
-        ck = clocks.stop() if clocks else None
         ms = e0.elapsed_time(e1) / args.steps
         ms = max_over_ranks(ms)
         st = s.status()
@@ -405,7 +411,7 @@ def run_product(args):
         ns = C.c_int32()
         s._ck(s.lib.sph_profile_steps(s.ctx, args.steps, stage_ms, C.byref(ns)), "sph_profile_steps")
         stage = [v / args.steps for v in stage_ms]
-        res = dict(ms=ms, launches=launches / args.steps * args.steps, clocks=ck, status=st,
+        res = dict(ms=ms, launches=launches / args.steps * args.steps, status=st,
                    stage_ms=dict(zip(STAGES, stage)), launches_per_step=launches / args.steps)
         if variant_table is not None:
             from sph_fem_2d_cutting_gpu_gb300 import tune
@@ -448,12 +454,15 @@ def run_product(args):
             el = max_over_ranks(el)
             res["e2e"] = dict(value=world * case.N * args.steps / el, unit=UNIT, h2d_bytes_per_step=nbytes,
                               d2h_bytes_per_step=nbytes)
+        res["clocks"] = clocks.stop() if clocks else None
         stage_interact = stage[4]
         ab = ALGO_BYTES[prec_name]
         algo = (ab["read"] + ab["write"]) * case.N
         ach = algo / (stage_interact * 1e-3) / 1e9
         res["roofline"] = {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
-                           "frac": ach / hbm_peak, "traffic": None,
+                           "frac": ach / hbm_peak,
+                           "traffic": (NCU_TRAFFIC_PER_PARTICLE[prec_name] * case.N
+                                       if prec_name in NCU_TRAFFIC_PER_PARTICLE and args.cell_factor == 2 else None),
                            "kernel": f"k_interact{'32' if prec_name == 'fp32k' else '64'}<fused>",
                            "algo_bytes_per_particle": ab["read"] + ab["write"], "peak_kind": peak_kind}
         results[prec_name] = res
