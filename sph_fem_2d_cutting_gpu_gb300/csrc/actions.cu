@@ -125,8 +125,14 @@ __device__ __forceinline__ uint32_t contact_s1_one(const KConsts &K, double dt, 
     // A segment counts a crossing only if the particle's y lies in its float-rounded
     // y-range (on_segment_mesh); float rounding is monotone, so a particle outside the
     // rounded y-range of all segments has no crossing and the scan is skipped.
-    // (the y test first: both tests are pure, and it spares most particles the FP64 sqrt)
+    // Likewise right of every segment: a crossing lies right of the segments' largest
+    // x only by the float rounding of the y-range, which moves the interpolated
+    // crossing by at most |dx/dy| * |y| * 2^-24 (bounded here with 2^-22 and an
+    // absolute 1e-12).  (These tests first: all tests are pure, and they spare most
+    // particles the FP64 sqrt.)
     if (pos.y <= (double)(float)tool.seg_ymax && pos.y >= (double)(float)tool.seg_ymin &&
+        pos.x <= tool.seg_xmax + tool.seg_dxdy * fmax(fabs(tool.seg_ymin), fabs(tool.seg_ymax)) * 2.384185791015625e-7 +
+                     1e-12 &&
         sqrt(ddx * ddx + ddy * ddy) < 1.05 * tool.ref_dist)
         inside = inside_judgement(pos, seg.left, seg.right, seg.n);
     if (inside == 0) {

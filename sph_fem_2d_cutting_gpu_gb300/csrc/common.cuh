@@ -145,6 +145,8 @@ struct ToolDev {
     float dtf, hdtf, inv_dtf;       // the same in FP32
     int32_t seg_first, seg_count;   // the case's interface segments
     double seg_ymin, seg_ymax;      // y-range of those segments (moved with them)
+    double seg_xmax;                // largest x of their end points (moved with them)
+    double seg_dxdy;                // largest |dx/dy| of a non-horizontal segment
 };
 
 // ---- float narrowings of the reference (double argument -> float call) ------

@@ -518,11 +518,15 @@ ToolDev tool_state_of(const ToolModelHost &M, double dt, int seg_first) {
     td.seg_count = M.n_seg;
     td.seg_ymin = INFINITY;
     td.seg_ymax = -INFINITY;
-    for (int s = 0; s < M.n_seg; s++)
-        for (double y : {M.left[2 * s + 1], M.right[2 * s + 1]}) {
-            td.seg_ymin = std::min(td.seg_ymin, y);
-            td.seg_ymax = std::max(td.seg_ymax, y);
-        }
+    td.seg_xmax = -INFINITY;
+    td.seg_dxdy = 0.;
+    for (int s = 0; s < M.n_seg; s++) {
+        const double lx = M.left[2 * s], ly = M.left[2 * s + 1], rx = M.right[2 * s], ry = M.right[2 * s + 1];
+        td.seg_ymin = std::min({td.seg_ymin, ly, ry});
+        td.seg_ymax = std::max({td.seg_ymax, ly, ry});
+        td.seg_xmax = std::max({td.seg_xmax, lx, rx});
+        if (ly != ry) td.seg_dxdy = std::max(td.seg_dxdy, 1.01 * std::fabs(lx - rx) / std::fabs(ly - ry));
+    }
     set_case_dt(td, dt);
     return td;
 }

@@ -146,9 +146,11 @@ __global__ void __launch_bounds__(kBlock) k_tool_move(KConsts K, SegDev seg, Fem
     }
     if ((what & 2) && i < (per_case ? K.n_cases : 1)) tool_state_move(tool + i, per_case ? tool[i].dt : dt);
     if ((what & 1) && i < (per_case ? K.n_cases : 1)) {   // the segments' y-range, with segment_move's arithmetic
-        const double dy = __dadd_rn(__dmul_rn(tool[i].vel[1], per_case ? tool[i].dt : dt), 0.);
+        const double dtc = per_case ? tool[i].dt : dt;
+        const double dy = __dadd_rn(__dmul_rn(tool[i].vel[1], dtc), 0.);
         tool[i].seg_ymin = __dadd_rn(tool[i].seg_ymin, dy);
         tool[i].seg_ymax = __dadd_rn(tool[i].seg_ymax, dy);
+        tool[i].seg_xmax = add_mul_rn(tool[i].seg_xmax, tool[i].vel[0], dtc);
     }
 }
 

@@ -205,13 +205,40 @@ struct FwdSmem {
 
 // Forward pass of this CTA's tile; xn = standardised features of this
 // thread's row.  Returns the standardised output, or sets *timeout.
+// 16 columns [c0, c0+16) of row r of a K-major 64-column operand (BF16).
+__device__ __forceinline__ void store_row16(unsigned char *base, int r, int c0, const float *v) {
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const float *w = v + 8 * h;
+        *(uint4 *)(base + cm_off(r, c0 + 8 * h, 64)) =
+            make_uint4(pack_bf16x2(w[0], w[1]), pack_bf16x2(w[2], w[3]), pack_bf16x2(w[4], w[5]),
+                       pack_bf16x2(w[6], w[7]));
+    }
+}
+
+// Forward pass of this CTA's tile; xn = standardised features of this
+// thread's row.  Returns the standardised output, or sets *timeout.  The
+// activations go 16 columns at a time (TMEM load, SiLU, store) in a rolled
+// loop: the code stays small enough for the instruction cache of a short,
+// latency-bound launch.
 __device__ float forward_tile(FwdSmem &sh, uint32_t tmem, uint32_t &phase, const float *xn, bool &timeout) {
     const uint32_t mbar = smem_u32(&sh.mbar);
     const int r = threadIdx.x;
-    float v[kMlpH];
-    layer1(sh.small, xn, v, nullptr);
-    store_row64(sh.act, r, v);
-    float y = 0.f;
+    const uint32_t trow = tmem + (((uint32_t)threadIdx.x >> 5) * 32u << 16);
+    float v[16];
+#pragma unroll 1
+    for (int c0 = 0; c0 < kMlpH; c0 += 16) {   // layer 1 on the CUDA cores
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            float acc = sh.small.b1[c0 + q];
+#pragma unroll
+            for (int c = 0; c < kMlpIn; c++) acc = fmaf(sh.small.w1[(c0 + q) * kMlpIn + c], xn[c], acc);
+            v[q] = siluf_(acc);
+        }
+        store_row16(sh.act, r, c0, v);
+    }
+    float y = sh.small.b4;
+#pragma unroll 1
     for (int layer = 0; layer < 2; layer++) {
         fence_async_smem();
         tc_fence_before();
@@ -228,18 +255,18 @@ __device__ float forward_tile(FwdSmem &sh, uint32_t tmem, uint32_t &phase, const
             return 0.f;
         }
         tc_fence_after();
-        tmem_row64(tmem, 0, v);
         const float *b = layer == 0 ? sh.small.b2 : sh.small.b3;
-        if (layer == 0) {
+#pragma unroll 1
+        for (int c0 = 0; c0 < kMlpH; c0 += 16) {
+            tmem_ld16(trow + c0, v);
+            if (layer == 0) {   // the MMA has read act: overwrite it with A2 (next MMA after the barrier)
 #pragma unroll
-            for (int j = 0; j < kMlpH; j++) v[j] = siluf_(v[j] + b[j]);
-            tc_fence_before();
-            __syncthreads();   // every row read before the next MMA overwrites TMEM; act is free (MMA done)
-            store_row64(sh.act, r, v);
-        } else {
-            y = sh.small.b4;
+                for (int q = 0; q < 16; q++) v[q] = siluf_(v[q] + b[c0 + q]);
+                store_row16(sh.act, r, c0, v);
+            } else {
 #pragma unroll
-            for (int j = 0; j < kMlpH; j++) y = fmaf(sh.small.w4[j], siluf_(v[j] + b[j]), y);
+                for (int q = 0; q < 16; q++) y = fmaf(sh.small.w4[c0 + q], siluf_(v[q] + b[c0 + q]), y);
+            }
         }
     }
     tc_fence_before();
