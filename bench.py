@@ -452,8 +452,29 @@ def run_product(args):
                 s._ck(s.lib.sph_download_particles(s.ctx, C.byref(pin_out)), "download")
             el = time.perf_counter() - t0
             el = max_over_ranks(el)
+            e2e_sync = dict(value=world * case.N * args.steps / el, unit=UNIT, h2d_bytes_per_step=nbytes,
+                            d2h_bytes_per_step=nbytes, api="sph_upload_particles + sph_step + sph_download_particles")
+            # pipelined: each step's state in and result out, the upload of the next state
+            # overlapping the download of the last result (sph_*_particles_async)
+
+            def pipelined(n):
+                s.upload_async(pin_in)
+                for k in range(n):
+                    s.step()
+                    s.download_async(pin_out)
+                    if k + 1 < n:
+                        s.upload_async(pin_in)
+                s.sync()
+
+            pipelined(max(2, args.warmup))
+            barrier()
+            t0 = time.perf_counter()
+            pipelined(args.steps)
+            el = max_over_ranks(time.perf_counter() - t0)
             res["e2e"] = dict(value=world * case.N * args.steps / el, unit=UNIT, h2d_bytes_per_step=nbytes,
-                              d2h_bytes_per_step=nbytes)
+                              d2h_bytes_per_step=nbytes,
+                              api="sph_upload_particles_async + sph_step + sph_download_particles_async")
+            res["e2e_sync"] = e2e_sync
         res["clocks"] = clocks.stop() if clocks else None
         stage_interact = stage[4]
         ab = ALGO_BYTES[prec_name]
@@ -508,6 +529,7 @@ def run_product(args):
         line["launch_tuning"] = head["launch_tuning"]
     if "e2e" in head:
         line["e2e"] = head["e2e"]
+        line["e2e_sync"] = head["e2e_sync"]
     if "fp64" in results and head_name != "fp64":
         f = results["fp64"]
         line["fp64"] = {"value": world * case.N / (f["ms"] * 1e-3), "ms_per_step": f["ms"],

@@ -280,6 +280,19 @@ int sph_run(sph_ctx *ctx, int32_t nsteps);
 /* Same step, issued as the unfused per-stage kernels in reference order. */
 int sph_step_staged(sph_ctx *ctx);
 
+/* ---- pipelined host I/O ------------------------------------------------------------
+ * No counterpart in the reference.  For callers that feed a state in and read the
+ * result out every step: the copies run on the context's own copy streams and return
+ * at once, so the upload of the next state (into the particle buffer the last step
+ * read, free once that step has finished) overlaps the download of the last result.
+ * Every later call on the context -- the step included -- first waits for them;
+ * sph_sync waits for everything.  Host arrays must stay untouched until then and be
+ * page-locked for the copies to overlap.
+ * sph_upload_particles_async takes the state fields only: p, R, S_der, v_der and idx
+ * are recomputed by the step and must be NULL. */
+int sph_upload_particles_async(sph_ctx *ctx, const sph_particles *host);
+int sph_download_particles_async(sph_ctx *ctx, sph_particles *host);
+
 /* ---- measurement hooks (output.cu:41-49 report_force; peak temperature) -- */
 int sph_reduce_force(sph_ctx *ctx, double out[2]);     /* sum over particles of fc + ft */
 int sph_reduce_max_T(sph_ctx *ctx, double *out);       /* max over non-blanked particles of T */

@@ -228,6 +228,8 @@ def load() -> C.CDLL:
         "sph_jc_stats": ([P, I32, C.POINTER(C.c_int64), I32], C.c_int),
         "sph_mlp_attach": ([P, P], C.c_int),
         "sph_launch_variants": ([PI, PI, PI, PI], C.c_int),
+        "sph_upload_particles_async": ([P, C.POINTER(Particles)], C.c_int),
+        "sph_download_particles_async": ([P, C.POINTER(Particles)], C.c_int),
         "sph_set_launch_config": ([P, C.POINTER(LaunchConfig)], C.c_int),
         "sph_get_launch_config": ([P, C.POINTER(LaunchConfig)], C.c_int),
     }

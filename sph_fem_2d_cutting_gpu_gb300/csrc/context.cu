@@ -59,6 +59,12 @@ struct sph_ctx {
     MlpDev mlp{};
     bool mlp_on = false;
     int interact_variant = 0;            // launch shape of the fused FP32K neighbour sums
+    // pipelined host I/O: uploads into the free particle buffer and downloads run on
+    // their own streams; the compute stream joins them before its next launch
+    cudaStream_t io_up = nullptr, io_down = nullptr;
+    cudaEvent_t ev_compute = nullptr, ev_up = nullptr, ev_down = nullptr;
+    bool up_pending = false, down_pending = false;
+    int down_buf = -1;
     std::vector<void *> allocs;
     std::string err;
 };
@@ -92,6 +98,30 @@ int dalloc(sph_ctx *ctx, T **p, size_t count) {
     cudaError_t e = cudaMalloc((void **)p, sizeof(T) * count);
     if (e != cudaSuccess) return fail(ctx, SPH_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
     ctx->allocs.push_back((void *)*p);
+    return SPH_OK;
+}
+
+// Makes the compute stream wait for pending asynchronous uploads / downloads.
+int join_io(sph_ctx *ctx) {
+    if (ctx->up_pending) {
+        CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_up, 0));
+        ctx->up_pending = false;
+    }
+    if (ctx->down_pending) {
+        CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_down, 0));
+        ctx->down_pending = false;
+        ctx->down_buf = -1;
+    }
+    return SPH_OK;
+}
+
+int ensure_io(sph_ctx *ctx) {
+    if (ctx->io_up) return SPH_OK;
+    CK(cudaStreamCreateWithFlags(&ctx->io_up, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&ctx->io_down, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&ctx->ev_compute, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->ev_up, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ctx->ev_down, cudaEventDisableTiming));
     return SPH_OK;
 }
 
@@ -177,8 +207,8 @@ struct FieldDesc {
     bool is_int;
 };
 
-sph_particles view_of(const sph_ctx *ctx) {
-    const SortedFields &A = ctx->buf[ctx->cur];
+sph_particles view_of_buf(const sph_ctx *ctx, int b) {
+    const SortedFields &A = ctx->buf[b];
     sph_particles v;
     std::memset(&v, 0, sizeof(v));
     v.N = ctx->N;
@@ -191,6 +221,8 @@ sph_particles view_of(const sph_ctx *ctx) {
     v.idx = ctx->F.idx; v.hash = A.hash; v.on_seg = A.on_seg;
     return v;
 }
+
+sph_particles view_of(const sph_ctx *ctx) { return view_of_buf(ctx, ctx->cur); }
 
 const FieldDesc kFields[] = {
     {offsetof(sph_particles, pos), 2, false},   {offsetof(sph_particles, vel), 2, false},
@@ -241,8 +273,12 @@ int ensure_fem_temp(sph_ctx *ctx) {
     return SPH_OK;
 }
 
-#define REQUIRE_CTX() \
-    if (!ctx) return SPH_ERR_INVALID;
+#define REQUIRE_CTX()                            \
+    if (!ctx) return SPH_ERR_INVALID;            \
+    {                                            \
+        int jr_ = join_io(ctx);                  \
+        if (jr_ != SPH_OK) return jr_;           \
+    }
 #define REQUIRE_TOOL() \
     if (!ctx->has_tool) return fail(ctx, SPH_ERR_STATE, "context has no tool");
 // Calls that take one time step or one tool for the whole context.
@@ -373,6 +409,15 @@ int sph_ctx_destroy(sph_ctx *ctx) {
     if (!ctx) return SPH_ERR_INVALID;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->io_up) {
+        cudaStreamSynchronize(ctx->io_up);
+        cudaStreamSynchronize(ctx->io_down);
+        cudaStreamDestroy(ctx->io_up);
+        cudaStreamDestroy(ctx->io_down);
+        cudaEventDestroy(ctx->ev_compute);
+        cudaEventDestroy(ctx->ev_up);
+        cudaEventDestroy(ctx->ev_down);
+    }
     invalidate_graphs(ctx);
     for (void *p : ctx->allocs) cudaFree(p);
     if (ctx->tool_dev) cudaFree(ctx->tool_dev);
@@ -645,6 +690,10 @@ int sph_sync(sph_ctx *ctx) {
     REQUIRE_CTX();
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->io_up) {
+        CK(cudaStreamSynchronize(ctx->io_up));
+        CK(cudaStreamSynchronize(ctx->io_down));
+    }
     CK(cudaGetLastError());
     return SPH_OK;
 }
@@ -706,6 +755,56 @@ int sph_download_particles(sph_ctx *ctx, sph_particles *host) {
                            ctx->stream));
     }
     CK(cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+// ---- pipelined host I/O ------------------------------------------------------------------------
+int sph_upload_particles_async(sph_ctx *ctx, const sph_particles *host) {
+    if (!ctx) return SPH_ERR_INVALID;
+    if (!host || host->N != ctx->N) return fail(ctx, SPH_ERR_INVALID, "upload: particle count mismatch");
+    if (host->p || host->R || host->S_der || host->v_der || host->idx)
+        return fail(ctx, SPH_ERR_INVALID, "async upload: p, R, S_der, v_der, idx are recomputed by the step");
+    int r = ensure_io(ctx);
+    if (r) return r;
+    const int tgt = 1 - ctx->cur;   // the buffer the last step read: free once it has finished
+    CK(cudaEventRecord(ctx->ev_compute, ctx->stream));
+    CK(cudaStreamWaitEvent(ctx->io_up, ctx->ev_compute, 0));
+    if (ctx->down_pending && ctx->down_buf == tgt) CK(cudaStreamWaitEvent(ctx->io_up, ctx->ev_down, 0));
+    const sph_particles v = view_of_buf(ctx, tgt);
+    for (const FieldDesc &fd : kFields) {
+        const void *src = member<const void *>(*host, fd.off_view);
+        if (!src) continue;
+        void *dst = member<void *>(v, fd.off_view);
+        CK(cudaMemcpyAsync(dst, src, (size_t)ctx->N * fd.width * (fd.is_int ? 4 : 8), cudaMemcpyHostToDevice,
+                           ctx->io_up));
+    }
+    CK(cudaEventRecord(ctx->ev_up, ctx->io_up));
+    ctx->up_pending = true;
+    ctx->cur = tgt;
+    ctx->counts_valid = false;
+    ctx->in_cell_order = false;
+    return SPH_OK;
+}
+
+int sph_download_particles_async(sph_ctx *ctx, sph_particles *host) {
+    if (!ctx) return SPH_ERR_INVALID;
+    if (!host || host->N != ctx->N) return fail(ctx, SPH_ERR_INVALID, "download: particle count mismatch");
+    int r = ensure_io(ctx);
+    if (r) return r;
+    CK(cudaEventRecord(ctx->ev_compute, ctx->stream));
+    CK(cudaStreamWaitEvent(ctx->io_down, ctx->ev_compute, 0));
+    if (ctx->up_pending) CK(cudaStreamWaitEvent(ctx->io_down, ctx->ev_up, 0));
+    const sph_particles v = view_of(ctx);
+    for (const FieldDesc &fd : kFields) {
+        void *dst = member<void *>(*host, fd.off_view);
+        if (!dst) continue;
+        const void *src = member<void *>(v, fd.off_view);
+        CK(cudaMemcpyAsync(dst, src, (size_t)ctx->N * fd.width * (fd.is_int ? 4 : 8), cudaMemcpyDeviceToHost,
+                           ctx->io_down));
+    }
+    CK(cudaEventRecord(ctx->ev_down, ctx->io_down));
+    ctx->down_pending = true;
+    ctx->down_buf = ctx->cur;
     return SPH_OK;
 }
 

@@ -98,6 +98,15 @@ class Solver:
         s = abi.particles_struct(arrays, self.N)
         self._ck(self.lib.sph_upload_particles(self.ctx, C.byref(s)), "sph_upload_particles")
 
+    # ---- pipelined host I/O (sph_upload_particles_async / sph_download_particles_async) --------
+    def upload_async(self, struct: abi.Particles):
+        """Queue the upload of a particles struct of page-locked arrays (the arrays
+        must stay alive and unchanged until ``sync``)."""
+        self._ck(self.lib.sph_upload_particles_async(self.ctx, C.byref(struct)), "sph_upload_particles_async")
+
+    def download_async(self, struct: abi.Particles):
+        self._ck(self.lib.sph_download_particles_async(self.ctx, C.byref(struct)), "sph_download_particles_async")
+
     def cells(self):
         g = self.geometry()
         cs = np.zeros(g.num_cell, np.int32)
