@@ -20,8 +20,10 @@ struct sph_ctx {
     int N = 0;
     KConsts K{};
     sph_grid_params grid{};
-    SortedFields buf[2]{};
+    SortedFields buf[3]{};               // the third only once pipelined I/O is used
+    int nbuf = 2;
     int cur = 0;                         // buf[cur] holds the particle state
+    int last_in = -1;                    // the buffer the last step read
     FixedFields F{};
     SortScratch X{};
     StepScratch W{};
@@ -34,8 +36,8 @@ struct sph_ctx {
     ToolDev *tool_dev = nullptr;
     double *fem_T_old = nullptr, *fem_f_temp = nullptr, *fem_K_temp = nullptr;
     // graphs, one per buffer parity
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    int64_t graph_launches[2] = {0, 0};
+    cudaGraphExec_t graph[3][3] = {};    // [input buffer][output buffer]
+    int64_t graph_launches[3][3] = {};
     bool use_graph = true;
     int64_t launches = 0;
     double *h_reduce = nullptr;          // pinned
@@ -59,12 +61,12 @@ struct sph_ctx {
     MlpDev mlp{};
     bool mlp_on = false;
     int interact_variant = 0;            // launch shape of the fused FP32K neighbour sums
-    // pipelined host I/O: uploads into the free particle buffer and downloads run on
-    // their own streams; the compute stream joins them before its next launch
+    // pipelined host I/O: uploads into a free particle buffer and downloads run on
+    // their own streams, ordered per buffer by events; a step waits only for the
+    // copies into its input and out of its output buffer
     cudaStream_t io_up = nullptr, io_down = nullptr;
-    cudaEvent_t ev_compute = nullptr, ev_up = nullptr, ev_down = nullptr;
-    bool up_pending = false, down_pending = false;
-    int down_buf = -1;
+    cudaEvent_t ev_used[3] = {}, ev_up[3] = {}, ev_down[3] = {}, ev_fixed = nullptr;
+    bool up_pending[3] = {}, down_pending[3] = {}, fixed_pending = false;
     std::vector<void *> allocs;
     std::string err;
 };
@@ -101,28 +103,47 @@ int dalloc(sph_ctx *ctx, T **p, size_t count) {
     return SPH_OK;
 }
 
-// Makes the compute stream wait for pending asynchronous uploads / downloads.
-int join_io(sph_ctx *ctx) {
-    if (ctx->up_pending) {
-        CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_up, 0));
-        ctx->up_pending = false;
+// Makes the compute stream wait for the pending copies into (upload) / out of
+// (download) buffer b, or for every pending copy with b < 0.
+int wait_io(sph_ctx *ctx, int b) {
+    for (int i = 0; i < 3; i++) {
+        if (b >= 0 && i != b) continue;
+        if (ctx->up_pending[i]) {
+            CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_up[i], 0));
+            ctx->up_pending[i] = false;
+        }
+        if (ctx->down_pending[i]) {
+            CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_down[i], 0));
+            ctx->down_pending[i] = false;
+        }
     }
-    if (ctx->down_pending) {
-        CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_down, 0));
-        ctx->down_pending = false;
-        ctx->down_buf = -1;
+    if (ctx->fixed_pending) {   // downloads of p, R, S_der, v_der, idx (written by every step)
+        CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_fixed, 0));
+        ctx->fixed_pending = false;
     }
     return SPH_OK;
 }
 
-int ensure_io(sph_ctx *ctx) {
-    if (ctx->io_up) return SPH_OK;
-    CK(cudaStreamCreateWithFlags(&ctx->io_up, cudaStreamNonBlocking));
-    CK(cudaStreamCreateWithFlags(&ctx->io_down, cudaStreamNonBlocking));
-    CK(cudaEventCreateWithFlags(&ctx->ev_compute, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&ctx->ev_up, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&ctx->ev_down, cudaEventDisableTiming));
+int join_io(sph_ctx *ctx) { return wait_io(ctx, -1); }
+
+// After compute that used buffers a and b: mark the point on the compute stream.
+int mark_used(sph_ctx *ctx, int a, int b) {
+    if (!ctx->io_up) return SPH_OK;
+    CK(cudaEventRecord(ctx->ev_used[a], ctx->stream));
+    if (b != a) CK(cudaEventRecord(ctx->ev_used[b], ctx->stream));
     return SPH_OK;
+}
+
+// The buffer a step (or sort) reading buf[cur] writes: one whose copies are not
+// in flight if there is one, else the lowest other index (the step then waits).
+int pick_out(const sph_ctx *ctx) {
+    int fallback = -1;
+    for (int b = 0; b < ctx->nbuf; b++) {
+        if (b == ctx->cur) continue;
+        if (fallback < 0) fallback = b;
+        if (!ctx->up_pending[b] && !ctx->down_pending[b]) return b;
+    }
+    return fallback;
 }
 
 #define DALLOC(p, n)                          \
@@ -193,11 +214,12 @@ void set_case_dt(ToolDev &td, double dt) {
 }
 
 void invalidate_graphs(sph_ctx *ctx) {
-    for (int p = 0; p < 2; p++)
-        if (ctx->graph[p]) {
-            cudaGraphExecDestroy(ctx->graph[p]);
-            ctx->graph[p] = nullptr;
-        }
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++)
+            if (ctx->graph[a][b]) {
+                cudaGraphExecDestroy(ctx->graph[a][b]);
+                ctx->graph[a][b] = nullptr;
+            }
 }
 
 // Field descriptors for upload/download of the caller-visible view.
@@ -264,6 +286,25 @@ int zero_all(sph_ctx *ctx) {
     return SPH_OK;
 }
 
+// Copy streams, per-buffer events and the third particle buffer of pipelined I/O.
+int ensure_io(sph_ctx *ctx) {
+    if (ctx->io_up) return SPH_OK;
+    int r = alloc_sorted(ctx, ctx->buf[2], ctx->N);
+    if (r) return r;
+    ctx->nbuf = 3;
+    CK(cudaStreamCreateWithFlags(&ctx->io_up, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&ctx->io_down, cudaStreamNonBlocking));
+    for (int b = 0; b < 3; b++) {
+        CK(cudaEventCreateWithFlags(&ctx->ev_used[b], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ctx->ev_up[b], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ctx->ev_down[b], cudaEventDisableTiming));
+    }
+    CK(cudaEventCreateWithFlags(&ctx->ev_fixed, cudaEventDisableTiming));
+    // the buffers' last users are whatever the compute stream has queued so far
+    for (int b = 0; b < 3; b++) CK(cudaEventRecord(ctx->ev_used[b], ctx->stream));
+    return SPH_OK;
+}
+
 // ---- staged FEM helpers ----------------------------------------------------------------
 int ensure_fem_temp(sph_ctx *ctx) {
     if (ctx->fem_T_old) return SPH_OK;
@@ -293,12 +334,13 @@ int jc_warm_grid(const sph_ctx *ctx) {
     return std::max(1, std::min(tiles, 4 * std::max(ctx->num_sms, 1)));
 }
 
-// The fused step body (everything after the histogram of the current state).
-int issue_fused_body(sph_ctx *ctx, int64_t &n) {
+// The fused step body (everything after the histogram of the current state),
+// reading buf[cur] and writing buf[w].
+int issue_fused_body(sph_ctx *ctx, int64_t &n, int w) {
     const int N = ctx->N;
     cudaStream_t s = ctx->stream;
     SortedFields &A = ctx->buf[ctx->cur];
-    SortedFields &B = ctx->buf[1 - ctx->cur];
+    SortedFields &B = ctx->buf[w];
     launch_sort_rest(s, N, ctx->X, ctx->K.g, ctx->F.idx, ctx->W.status);
     n += 5;
     launch_gather_fused(s, N, ctx->F.idx, ctx->K, A, B, ctx->F, ctx->W, ctx->X.hash_next, ctx->tool_dev);
@@ -414,9 +456,12 @@ int sph_ctx_destroy(sph_ctx *ctx) {
         cudaStreamSynchronize(ctx->io_down);
         cudaStreamDestroy(ctx->io_up);
         cudaStreamDestroy(ctx->io_down);
-        cudaEventDestroy(ctx->ev_compute);
-        cudaEventDestroy(ctx->ev_up);
-        cudaEventDestroy(ctx->ev_down);
+        for (int b = 0; b < 3; b++) {
+            cudaEventDestroy(ctx->ev_used[b]);
+            cudaEventDestroy(ctx->ev_up[b]);
+            cudaEventDestroy(ctx->ev_down[b]);
+        }
+        cudaEventDestroy(ctx->ev_fixed);
     }
     invalidate_graphs(ctx);
     for (void *p : ctx->allocs) cudaFree(p);
@@ -766,11 +811,13 @@ int sph_upload_particles_async(sph_ctx *ctx, const sph_particles *host) {
         return fail(ctx, SPH_ERR_INVALID, "async upload: p, R, S_der, v_der, idx are recomputed by the step");
     int r = ensure_io(ctx);
     if (r) return r;
-    const int tgt = 1 - ctx->cur;   // the buffer the last step read: free once it has finished
-    CK(cudaEventRecord(ctx->ev_compute, ctx->stream));
-    CK(cudaStreamWaitEvent(ctx->io_up, ctx->ev_compute, 0));
-    if (ctx->down_pending && ctx->down_buf == tgt) CK(cudaStreamWaitEvent(ctx->io_up, ctx->ev_down, 0));
-    const sph_particles v = view_of_buf(ctx, tgt);
+    // a buffer neither holding the current state nor read by the last queued step
+    int t = -1;
+    for (int b = 0; b < 3 && t < 0; b++)
+        if (b != ctx->cur && b != ctx->last_in) t = b;
+    CK(cudaStreamWaitEvent(ctx->io_up, ctx->ev_used[t], 0));                  // its last compute user
+    if (ctx->down_pending[t]) CK(cudaStreamWaitEvent(ctx->io_up, ctx->ev_down[t], 0));   // a download out of it
+    const sph_particles v = view_of_buf(ctx, t);
     for (const FieldDesc &fd : kFields) {
         const void *src = member<const void *>(*host, fd.off_view);
         if (!src) continue;
@@ -778,9 +825,9 @@ int sph_upload_particles_async(sph_ctx *ctx, const sph_particles *host) {
         CK(cudaMemcpyAsync(dst, src, (size_t)ctx->N * fd.width * (fd.is_int ? 4 : 8), cudaMemcpyHostToDevice,
                            ctx->io_up));
     }
-    CK(cudaEventRecord(ctx->ev_up, ctx->io_up));
-    ctx->up_pending = true;
-    ctx->cur = tgt;
+    CK(cudaEventRecord(ctx->ev_up[t], ctx->io_up));
+    ctx->up_pending[t] = true;
+    ctx->cur = t;
     ctx->counts_valid = false;
     ctx->in_cell_order = false;
     return SPH_OK;
@@ -791,10 +838,15 @@ int sph_download_particles_async(sph_ctx *ctx, sph_particles *host) {
     if (!host || host->N != ctx->N) return fail(ctx, SPH_ERR_INVALID, "download: particle count mismatch");
     int r = ensure_io(ctx);
     if (r) return r;
-    CK(cudaEventRecord(ctx->ev_compute, ctx->stream));
-    CK(cudaStreamWaitEvent(ctx->io_down, ctx->ev_compute, 0));
-    if (ctx->up_pending) CK(cudaStreamWaitEvent(ctx->io_down, ctx->ev_up, 0));
-    const sph_particles v = view_of(ctx);
+    const int src_b = ctx->cur;
+    const bool fixed = host->p || host->R || host->S_der || host->v_der || host->idx;
+    CK(cudaStreamWaitEvent(ctx->io_down, ctx->ev_used[src_b], 0));            // the step that wrote it
+    if (fixed) {                                                              // p, R, ...: the last step
+        CK(cudaEventRecord(ctx->ev_fixed, ctx->stream));
+        CK(cudaStreamWaitEvent(ctx->io_down, ctx->ev_fixed, 0));
+    }
+    if (ctx->up_pending[src_b]) CK(cudaStreamWaitEvent(ctx->io_down, ctx->ev_up[src_b], 0));
+    const sph_particles v = view_of_buf(ctx, src_b);
     for (const FieldDesc &fd : kFields) {
         void *dst = member<void *>(*host, fd.off_view);
         if (!dst) continue;
@@ -802,9 +854,12 @@ int sph_download_particles_async(sph_ctx *ctx, sph_particles *host) {
         CK(cudaMemcpyAsync(dst, src, (size_t)ctx->N * fd.width * (fd.is_int ? 4 : 8), cudaMemcpyDeviceToHost,
                            ctx->io_down));
     }
-    CK(cudaEventRecord(ctx->ev_down, ctx->io_down));
-    ctx->down_pending = true;
-    ctx->down_buf = ctx->cur;
+    CK(cudaEventRecord(ctx->ev_down[src_b], ctx->io_down));
+    ctx->down_pending[src_b] = true;
+    if (fixed) {
+        CK(cudaEventRecord(ctx->ev_fixed, ctx->io_down));
+        ctx->fixed_pending = true;
+    }
     return SPH_OK;
 }
 
@@ -845,10 +900,14 @@ int sph_sort(sph_ctx *ctx) {
     const int N = ctx->N;
     launch_count(ctx->stream, N, CUR(ctx), ctx->X, ctx->K.g, ctx->W.status, false);
     launch_sort_rest(ctx->stream, N, ctx->X, ctx->K.g, ctx->F.idx, ctx->W.status);
-    launch_gather_plain(ctx->stream, N, ctx->F.idx, CUR(ctx), ctx->buf[1 - ctx->cur]);
+    const int w = pick_out(ctx);
+    launch_gather_plain(ctx->stream, N, ctx->F.idx, CUR(ctx), ctx->buf[w]);
     ctx->launches += 7;
     CK_LAUNCH();
-    ctx->cur = 1 - ctx->cur;   // double_buffer swap (grid_gpu_green.cu:152-182)
+    int rm = mark_used(ctx, ctx->cur, w);
+    if (rm) return rm;
+    ctx->last_in = ctx->cur;
+    ctx->cur = w;   // double_buffer swap (grid_gpu_green.cu:152-182)
     ctx->counts_valid = false;
     ctx->in_cell_order = true;
     return SPH_OK;
@@ -1131,8 +1190,13 @@ int sph_upload_fem_state(sph_ctx *ctx, const double *T, const double *k) {
 
 // ---- whole step -------------------------------------------------------------------------------
 int sph_step(sph_ctx *ctx) {
-    REQUIRE_CTX();
+    if (!ctx) return SPH_ERR_INVALID;
     cudaStream_t s = ctx->stream;
+    const int w = pick_out(ctx);
+    // only the copies into the input, out of (or into) the output, and of the derived fields
+    int r0 = wait_io(ctx, ctx->cur);
+    if (r0 == SPH_OK) r0 = wait_io(ctx, w);
+    if (r0) return r0;
     if (!ctx->counts_valid) {
         launch_count(s, ctx->N, CUR(ctx), ctx->X, ctx->K.g, ctx->W.status, true);
         ctx->launches += 1;
@@ -1140,31 +1204,34 @@ int sph_step(sph_ctx *ctx) {
     }
     const int p = ctx->cur;
     if (ctx->use_graph) {
-        if (!ctx->graph[p]) {
+        if (!ctx->graph[p][w]) {
             cudaGraph_t g = nullptr;
             CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
             int64_t n = 0;
-            int r = issue_fused_body(ctx, n);
+            int r = issue_fused_body(ctx, n, w);
             cudaError_t e = cudaStreamEndCapture(s, &g);
             if (r) {
                 if (g) cudaGraphDestroy(g);
                 return r;
             }
             if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
-            e = cudaGraphInstantiate(&ctx->graph[p], g, 0);
+            e = cudaGraphInstantiate(&ctx->graph[p][w], g, 0);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
-            ctx->graph_launches[p] = n;
+            ctx->graph_launches[p][w] = n;
         }
-        CK(cudaGraphLaunch(ctx->graph[p], s));
-        ctx->launches += ctx->graph_launches[p];
+        CK(cudaGraphLaunch(ctx->graph[p][w], s));
+        ctx->launches += ctx->graph_launches[p][w];
     } else {
         int64_t n = 0;
-        int r = issue_fused_body(ctx, n);
+        int r = issue_fused_body(ctx, n, w);
         if (r) return r;
         ctx->launches += n;
     }
-    ctx->cur = 1 - ctx->cur;
+    int r1 = mark_used(ctx, p, w);
+    if (r1) return r1;
+    ctx->last_in = p;
+    ctx->cur = w;
     ctx->counts_valid = true;
     ctx->in_cell_order = true;
     return SPH_OK;
@@ -1181,8 +1248,9 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
     for (auto &e : ev) CK(cudaEventCreate(&e));
     for (int k = 0; k < kStages; k++) stage_ms[k] = 0.f;
     for (int step = 0; step < nsteps; step++) {
+        const int w = pick_out(ctx);
         SortedFields &A = ctx->buf[ctx->cur];
-        SortedFields &B = ctx->buf[1 - ctx->cur];
+        SortedFields &B = ctx->buf[w];
         CK(cudaEventRecord(ev[0], s));
         if (!ctx->counts_valid) {
             launch_count(s, N, A, ctx->X, ctx->K.g, ctx->W.status, true);
@@ -1220,7 +1288,10 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
             CK(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
             stage_ms[k] += ms;
         }
-        ctx->cur = 1 - ctx->cur;
+        int rm = mark_used(ctx, ctx->cur, w);
+        if (rm) return rm;
+        ctx->last_in = ctx->cur;
+        ctx->cur = w;
         ctx->counts_valid = true;
         ctx->in_cell_order = true;
     }

@@ -38,18 +38,25 @@ def test_pipelined_steps_equal_synchronous(lib, precision):
     s.upload(state)
     s.step()
     want = s.download(STATE)
-    # pipelined: three requests on the same input state
+    # pipelined: six requests on the same input state (the three particle buffers
+    # rotate twice)
     src, keep_in = pinned_like(state)
-    outs = [pinned_like(state) for _ in range(3)]
+    outs = [pinned_like(state) for _ in range(6)]
     pin_in = abi.particles_struct(src, case.N)
     pin_out = [abi.particles_struct(o, case.N) for o, _ in outs]
     s.upload_async(pin_in)
-    for k in range(3):
+    for k in range(6):
         s.step()
         s.download_async(pin_out[k])
-        if k < 2:
+        if k < 5:
             s.upload_async(pin_in)
     s.sync()
+    # and a synchronous step afterwards still sees consistent state
+    s.upload(state)
+    s.step()
+    again = s.download(STATE)
+    for f in STATE:
+        assert np.array_equal(again[f], want[f]), f
     for o, _ in outs:
         for f in STATE:
             assert np.array_equal(o[f], want[f]), f
