@@ -228,6 +228,41 @@ def run_batched(args, local, max_over_ranks, barrier):
     return out
 
 
+def run_accuracy(case, mlp, steps, every, local):
+    """Cutting force (sum of fc + ft) and peak temperature of the FP32K form, with
+    and without the warm start, against the plain FP64 form over `steps` steps of
+    the same run (checkpoints every `every` steps).  The FP64 form is the oracle
+    here: it matches the CPU restatement of the reference to 1e-10 per step."""
+    import numpy as np
+
+    from sph_fem_2d_cutting_gpu_gb300 import abi
+    from sph_fem_2d_cutting_gpu_gb300.solver import Solver
+
+    hist = {}
+    for name, prec, net in (("fp64", abi.SPH_PREC_FP64, None), ("fp32k", abi.SPH_PREC_FP32K, None),
+                            ("fp32k_mlp", abi.SPH_PREC_FP32K, mlp)):
+        s = Solver(case, prec, device=local, place_tool=False)
+        if net is not None:
+            s.attach_mlp(net)
+        h = []
+        for _ in range(steps // every):
+            s.step(every)
+            h.append((s.reduce_force(), s.max_T()))
+        hist[name] = h
+        s.close()
+    F0 = np.array([f for f, _ in hist["fp64"]])
+    T0 = np.array([t for _, t in hist["fp64"]])
+    fmax = float(np.linalg.norm(F0, axis=1).max())
+    rise = max(float(T0.max()) - 300.0, 1.0)
+    out = {"steps": steps, "every": every, "peak_force_fp64": fmax, "peak_T_fp64": float(T0.max())}
+    for name in ("fp32k", "fp32k_mlp"):
+        F = np.array([f for f, _ in hist[name]])
+        T = np.array([t for _, t in hist[name]])
+        out[name] = {"force_err_of_peak": float(np.linalg.norm(F - F0, axis=1).max() / fmax),
+                     "peak_T_err_of_rise": float(np.abs(T - T0).max() / rise)}
+    return out
+
+
 def run_learned(args, local):
     """The learned warm start on the AISI 1045 cut (640,000 particles, tool of
     about 13,000 nodes, edge placement): log the plain FP32K return mappings
@@ -298,7 +333,6 @@ def run_learned(args, local):
     fem_T = s.fem()
     steps_done = logged + 2 * (args.warmup + args.steps)
     s.close()
-    m.close()
     # plain FP64 from the same state (tool translated by the distance it moved)
     c64 = setups.moved(case, case.tool_speed * case.dt * steps_done)
     s64 = Solver(c64, abi.SPH_PREC_FP64, device=local, place_tool=False)
@@ -307,7 +341,13 @@ def run_learned(args, local):
     ms_64, c_64, it_64 = timed(s64, args.steps)
     s64.close()
     torch.cuda.empty_cache()
+    accuracy = None
+    if args.accuracy_steps > 0:
+        accuracy = run_accuracy(case, m, args.accuracy_steps, args.accuracy_every, local)
+    m.close()
+    torch.cuda.empty_cache()
     return {
+        "accuracy_vs_fp64": accuracy,
         "workload": "AISI 1045 cut 1600x400 (640,000 particles), tool of "
                     f"{case.info['nodes']} nodes, rake -6 deg, 120 m/min, edge placement",
         "records_logged": int(n_logged), "records_offered": int(offered), "records_usable": int(len(rec)),
@@ -570,6 +610,9 @@ def main():
                     help="return-mapping states logged for the learned warm start (0: skip)")
     ap.add_argument("--learned-max-steps", type=int, default=20_000)
     ap.add_argument("--learned-epochs", type=int, default=3)
+    ap.add_argument("--accuracy-steps", type=int, default=4000,
+                    help="AISI 1045 cut: FP32K (+ warm start) against FP64 over this many steps (0: skip)")
+    ap.add_argument("--accuracy-every", type=int, default=500)
     ap.add_argument("--no-tune", action="store_true", help="no launch-shape / cell-geometry autotuning")
     ap.add_argument("--cell-factor", type=int, default=2, help="micro workload: cell edge in h")
     ap.add_argument("--stencil", type=int, default=1, help="micro workload: stencil half-width in cells")
