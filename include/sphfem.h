@@ -280,6 +280,20 @@ int sph_run(sph_ctx *ctx, int32_t nsteps);
 /* Same step, issued as the unfused per-stage kernels in reference order. */
 int sph_step_staged(sph_ctx *ctx);
 
+/* ---- output in the reference's formats ---------------------------------------------
+ * Legacy-ASCII VTK as vtk_writer.cu writes it: particles (vtk_writer.cu:11-220:
+ * non-blanked particles as vertex cells with Temperature, on_seg,
+ * EquivAccumPlasticStrain, Velocity, fc and ft x 1e5, normal, SvM) and the FEM
+ * tool (vtk_writer.cu:304-366: nodes, triangles, nodal temperature; with tl_ref
+ * the tool moved back by its travel since its top-left point was at tl_ref,
+ * vtk_writer.cu:518-587).  Vertex cells index the written points (the
+ * reference indexes the full particle array, which points past the POINTS list
+ * once particles are blanked).  sph_append_force_log appends the line
+ * "%.9g %.9g\n" of sph_reduce_force (mfree_gpu.cpp:336-338). */
+int sph_write_vtk_particles(sph_ctx *ctx, const char *path);
+int sph_write_vtk_tool(sph_ctx *ctx, const char *path, const double *tl_ref);
+int sph_append_force_log(sph_ctx *ctx, const char *path);
+
 /* ---- pipelined host I/O ------------------------------------------------------------
  * No counterpart in the reference.  For callers that feed a state in and read the
  * result out every step: the copies run on the context's own copy streams and return

@@ -1737,4 +1737,121 @@ int sph_get_launch_config(const sph_ctx *ctx, sph_launch_config *cfg) {
     return SPH_OK;
 }
 
+// ---- output in the reference's formats (vtk_writer.cu, mfree_gpu.cpp) ------------------------------
+namespace {
+int write_fail(sph_ctx *ctx, FILE *fp, const std::string &what) {
+    if (fp) fclose(fp);
+    return fail(ctx, SPH_ERR_INVALID, what);
+}
+}  // namespace
+
+int sph_write_vtk_particles(sph_ctx *ctx, const char *path) {
+    REQUIRE_CTX();
+    if (!path) return SPH_ERR_INVALID;
+    const int n = ctx->N;
+    std::vector<double> pos(2 * (size_t)n), vel(2 * (size_t)n), fc(2 * (size_t)n), ft(2 * (size_t)n),
+        nrm(2 * (size_t)n), S(4 * (size_t)n), p(n), T(n), eps(n), blanked(n);
+    std::vector<int32_t> on_seg(n);
+    sph_particles h;
+    std::memset(&h, 0, sizeof(h));
+    h.N = n;
+    h.pos = pos.data(); h.vel = vel.data(); h.fc = fc.data(); h.ft = ft.data(); h.n = nrm.data();
+    h.S = S.data(); h.p = p.data(); h.T = T.data(); h.eps_pl = eps.data(); h.blanked = blanked.data();
+    h.on_seg = on_seg.data();
+    int r = sph_download_particles(ctx, &h);
+    if (r) return r;
+    FILE *fp = fopen(path, "w");
+    if (!fp) return fail(ctx, SPH_ERR_INVALID, std::string("cannot open ") + path);
+    int m = 0;
+    for (int i = 0; i < n; i++) m += blanked[i] != 1.;
+    // vtk_writer.cu:11-220: points of the non-blanked particles, one vertex cell each
+    fprintf(fp, "# vtk DataFile Version 2.0\nmfree iwf\nASCII\n\nDATASET UNSTRUCTURED_GRID\nPOINTS %d float\n", m);
+    for (int i = 0; i < n; i++)
+        if (blanked[i] != 1.) fprintf(fp, "%f %f %f\n", pos[2 * i], pos[2 * i + 1], 0.);
+    fprintf(fp, "\nCELLS %d %d\n", m, 2 * m);
+    for (int k = 0; k < m; k++) fprintf(fp, "%d %d\n", 1, k);   // vertex k of the POINTS list
+    fprintf(fp, "\nCELL_TYPES %d\n", m);
+    for (int k = 0; k < m; k++) fprintf(fp, "%d\n", 1);
+    fprintf(fp, "\nPOINT_DATA %d\n", m);
+    fprintf(fp, "SCALARS Temperature float 1\nLOOKUP_TABLE default\n");
+    for (int i = 0; i < n; i++)
+        if (blanked[i] != 1.) fprintf(fp, "%f\n", T[i]);
+    fprintf(fp, "\nSCALARS on_seg int 1\nLOOKUP_TABLE default\n");
+    for (int i = 0; i < n; i++)
+        if (blanked[i] != 1.) fprintf(fp, "%d\n", on_seg[i]);
+    fprintf(fp, "\nSCALARS EquivAccumPlasticStrain float 1\nLOOKUP_TABLE default\n");
+    for (int i = 0; i < n; i++)
+        if (blanked[i] != 1.) fprintf(fp, "%f\n", eps[i]);
+    fprintf(fp, "\nVECTORS Velocity float\n");
+    for (int i = 0; i < n; i++)
+        if (blanked[i] != 1.) fprintf(fp, "%f %f %f\n", vel[2 * i], vel[2 * i + 1], 0.);
+    fprintf(fp, "\nVECTORS fc float\n");
+    for (int i = 0; i < n; i++)
+        if (blanked[i] != 1.) fprintf(fp, "%2f %2f %2f\n", 100000 * fc[2 * i], 100000 * fc[2 * i + 1], 0.);
+    fprintf(fp, "\nVECTORS ft float\n");
+    for (int i = 0; i < n; i++)
+        if (blanked[i] != 1.) fprintf(fp, "%f %f %f\n", 100000 * ft[2 * i], 100000 * ft[2 * i + 1], 0.);
+    fprintf(fp, "\nVECTORS normal float\n");
+    for (int i = 0; i < n; i++)
+        if (blanked[i] != 1.) fprintf(fp, "%f %f %f\n", nrm[2 * i], nrm[2 * i + 1], 0.);
+    fprintf(fp, "\nSCALARS SvM float 1\nLOOKUP_TABLE default\n");
+    for (int i = 0; i < n; i++) {
+        if (blanked[i] == 1.) continue;
+        const double cxx = S[4 * i] - p[i], cyy = S[4 * i + 2] - p[i], czz = S[4 * i + 3] - p[i], cxy = S[4 * i + 1];
+        const double svm2 = (cxx * cxx + cyy * cyy + czz * czz) - cxx * cyy - cxx * czz - cyy * czz + 3.0 * cxy * cxy;
+        fprintf(fp, "%f\n", svm2 > 0 ? std::sqrt(svm2) : 0.);
+    }
+    fprintf(fp, "\n");
+    if (fclose(fp) != 0) return fail(ctx, SPH_ERR_INVALID, std::string("cannot write ") + path);
+    return SPH_OK;
+}
+
+int sph_write_vtk_tool(sph_ctx *ctx, const char *path, const double *tl_ref) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    if (!path) return SPH_ERR_INVALID;
+    const ToolModelHost &M = ctx->tool_host;
+    const int nn = ctx->fem.n_nodes;
+    std::vector<double> position(2 * (size_t)nn), T(nn);
+    CK(cudaMemcpyAsync(position.data(), ctx->fem.position, 16 * (size_t)nn, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(T.data(), ctx->fem.T, 8 * (size_t)nn, cudaMemcpyDeviceToHost, ctx->stream));
+    double shift[2] = {0., 0.};
+    if (tl_ref) {   // vtk_writer.cu:518-587: the tool moved back by its travel since tl_ref
+        ToolDev td;
+        CK(cudaMemcpyAsync(&td, ctx->tool_dev, sizeof(td), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        shift[0] = td.tl_point_ref[0] - tl_ref[0];
+        shift[1] = td.tl_point_ref[1] - tl_ref[1];
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    FILE *fp = fopen(path, "w");
+    if (!fp) return fail(ctx, SPH_ERR_INVALID, std::string("cannot open ") + path);
+    // vtk_writer.cu:304-366: nodes, triangles, nodal temperature
+    fprintf(fp, "# vtk DataFile Version 2.0\nmfree iwf\nASCII\n\nDATASET UNSTRUCTURED_GRID\nPOINTS %d float\n", nn);
+    for (int i = 0; i < nn; i++) fprintf(fp, "%f %f %f\n", position[2 * i] - shift[0], position[2 * i + 1] - shift[1], 0.);
+    const int ne = M.n_elements;
+    fprintf(fp, "\nCELLS %d %d\n", ne, 4 * ne);
+    for (int e = 0; e < ne; e++) fprintf(fp, "3 %d %d %d\n", M.elements[e].x, M.elements[e].y, M.elements[e].z);
+    fprintf(fp, "\nCELL_TYPES %d\n", ne);
+    for (int e = 0; e < ne; e++) fprintf(fp, "5\n");
+    fprintf(fp, "POINT_DATA %d\nSCALARS temperature float 1\nLOOKUP_TABLE default\n", nn);
+    for (int i = 0; i < nn; i++) fprintf(fp, "%f\n", T[i]);
+    fprintf(fp, "\n");
+    if (fclose(fp) != 0) return fail(ctx, SPH_ERR_INVALID, std::string("cannot write ") + path);
+    return SPH_OK;
+}
+
+int sph_append_force_log(sph_ctx *ctx, const char *path) {
+    REQUIRE_CTX();
+    if (!path) return SPH_ERR_INVALID;
+    double f[2];
+    int r = sph_reduce_force(ctx, f);
+    if (r) return r;
+    FILE *fp = fopen(path, "a");
+    if (!fp) return fail(ctx, SPH_ERR_INVALID, std::string("cannot open ") + path);
+    fprintf(fp, "%.9g %.9g\n", f[0], f[1]);   // mfree_gpu.cpp:336-338
+    if (fclose(fp) != 0) return write_fail(ctx, nullptr, std::string("cannot write ") + path);
+    return SPH_OK;
+}
+
 }  // extern "C"

@@ -98,6 +98,21 @@ class Solver:
         s = abi.particles_struct(arrays, self.N)
         self._ck(self.lib.sph_upload_particles(self.ctx, C.byref(s)), "sph_upload_particles")
 
+    # ---- output in the reference's formats (vtk_writer.cu, mfree_gpu.cpp) ------------------------
+    def write_vtk(self, path: str):
+        """Particles as legacy-ASCII VTK (vtk_writer_write(particle_gpu*, step))."""
+        self._ck(self.lib.sph_write_vtk_particles(self.ctx, str(path).encode()), "sph_write_vtk_particles")
+
+    def write_vtk_tool(self, path: str, tl_ref=None):
+        """The FEM tool as legacy-ASCII VTK (vtk_writer_write_FEM_tool); with tl_ref,
+        moved back to where its top-left point was tl_ref (vtk_writer_write_tool_org)."""
+        ref = None if tl_ref is None else np.ascontiguousarray(tl_ref, np.float64)
+        self._ck(self.lib.sph_write_vtk_tool(self.ctx, str(path).encode(), abi.ptr(ref)), "sph_write_vtk_tool")
+
+    def append_force_log(self, path: str):
+        """One line 'fx fy' of the cutting force (the reference's force log)."""
+        self._ck(self.lib.sph_append_force_log(self.ctx, str(path).encode()), "sph_append_force_log")
+
     # ---- pipelined host I/O (sph_upload_particles_async / sph_download_particles_async) --------
     def upload_async(self, struct: abi.Particles):
         """Queue the upload of a particles struct of page-locked arrays (the arrays

@@ -251,3 +251,124 @@ def mesh_tool(tl, length, height, rake_deg, clearance_deg, r, s_min, s_max, grad
             flags_fix[e, k] = 1
     return dict(nodes=np.ascontiguousarray(nodes, np.float64), elements=np.ascontiguousarray(tri, np.int32),
                 cutting_flags=flags_cut, fixed_flags=flags_fix, tl=np.array(o["tl"], float), outline=o)
+
+
+# ---- Abaqus .inp meshes (mesh_structure_GPU.cu:784-1257 mesh_read) ---------------------------------
+def _ints(line: str):
+    return [int(t) for t in line.replace(" ", "").split(",") if t.strip()]
+
+
+def _edge_flags(tri, nodes_in_set):
+    """Edge flags of boundary elements: edge (a,b) -> 0, (b,c) -> 1, (c,a) -> 2 is
+    flagged when both of its nodes are in the node set."""
+    a, b, c = (int(v) in nodes_in_set for v in tri)
+    return [int(a and b), int(b and c), int(c and a)]
+
+
+def _correct_full(flags, elements, boundary, full):
+    """Elements with all three edges flagged (mesh_structure_GPU.cu:862-890): the
+    edge opposite a node that no other boundary element shares is unflagged."""
+    for e in full:
+        others = [b for b in boundary if b != e]
+        for k, opp in ((0, 1), (1, 2), (2, 0)):
+            node = elements[e][k]
+            if not any(node in elements[b][:3] for b in others):
+                flags[e][opp] = 0
+
+
+def read_inp(path: str, scale: float = 0.01, tl=(0.0, 0.0)) -> dict:
+    """Tool mesh from an Abaqus-style .inp file, as mesh_read reads it: '*Node'
+    lines 'id, x, y' (coordinates times `scale`, 1/100 in the reference), an
+    'Element' header and lines 'id, n1, n2, n3' (1-based), node sets ('Nset')
+    and element sets ('Elset') named 'CuttingEdge' and 'FixedBoundary', 'End'.
+    Lines containing '#' are skipped.  Returns the dict ``mesh_tool`` returns
+    (nodes, elements, cutting_flags, fixed_flags, tl); `tl` is the tool's
+    top-left reference point (tool_FEM ctor), not part of the file."""
+    nodes, elements = [], []
+    cut_nodes, fix_nodes = set(), set()
+    cut_elems, fix_elems = [], []
+    mode = None
+    with open(path) as f:
+        for line in f:
+            if "#" in line:
+                continue
+            if "*Node" in line:
+                mode = "node"
+                continue
+            if "Element" in line:
+                mode = "elem"
+                continue
+            if "CuttingEdge" in line and "Nset" in line:
+                mode = "cut_nodes"
+                continue
+            if "CuttingEdge" in line and "Elset" in line:
+                mode = "cut_elems"
+                continue
+            if "FixedBoundary" in line and "Nset" in line:
+                mode = "fix_nodes"
+                continue
+            if "FixedBoundary" in line and "Elset" in line:
+                mode = "fix_elems"
+                continue
+            if "End" in line:
+                break
+            if not line.strip():
+                continue
+            if mode == "node":
+                t = [s for s in line.split(",")]
+                nodes.append((float(t[1]) * scale, float(t[2]) * scale))
+            elif mode == "elem":
+                v = _ints(line)
+                elements.append([v[1] - 1, v[2] - 1, v[3] - 1])
+            elif mode == "cut_nodes":
+                cut_nodes.update(v - 1 for v in _ints(line))
+            elif mode == "cut_elems":
+                cut_elems += [v - 1 for v in _ints(line)]
+            elif mode == "fix_nodes":
+                fix_nodes.update(v - 1 for v in _ints(line))
+            elif mode == "fix_elems":
+                fix_elems += [v - 1 for v in _ints(line)]
+    n_el = len(elements)
+    cut = [[0, 0, 0] for _ in range(n_el)]
+    fix = [[0, 0, 0] for _ in range(n_el)]
+    for flags, boundary, in_set in ((cut, cut_elems, cut_nodes), (fix, fix_elems, fix_nodes)):
+        full = []
+        for e in boundary:
+            flags[e] = _edge_flags(elements[e], in_set)
+            if all(flags[e]):
+                full.append(e)
+        _correct_full(flags, elements, boundary, full)
+    return dict(nodes=np.ascontiguousarray(nodes, np.float64), elements=np.ascontiguousarray(elements, np.int32),
+                cutting_flags=np.ascontiguousarray(cut, np.int32), fixed_flags=np.ascontiguousarray(fix, np.int32),
+                tl=np.array(tl, float))
+
+
+def write_inp(mesh: dict, path: str, scale: float = 0.01):
+    """Writes a mesh in the layout ``read_inp`` reads (coordinates divided by
+    `scale`); the boundary sets are the nodes and elements of flagged edges."""
+    nodes, el = mesh["nodes"], mesh["elements"]
+    with open(path, "w") as f:
+        f.write("*Heading\n*Node\n")
+        for i, (x, y) in enumerate(nodes):
+            f.write(f"{i + 1}, {x / scale:.17g}, {y / scale:.17g}\n")
+        f.write("*Element, type=CPS3\n")
+        for i, (a, b, c) in enumerate(el):
+            f.write(f"{i + 1}, {a + 1}, {b + 1}, {c + 1}\n")
+        for name, key in (("CuttingEdge", "cutting_flags"), ("FixedBoundary", "fixed_flags")):
+            fl = mesh[key]
+            elems = [i for i in range(len(el)) if fl[i].any()]
+            nds = set()
+            for i in elems:
+                a, b, c = el[i]
+                for k, (p, q) in enumerate(((a, b), (b, c), (c, a))):
+                    if fl[i][k]:
+                        nds.update((int(p), int(q)))
+            f.write(f"*Nset, nset={name}\n")
+            ids = sorted(n + 1 for n in nds)
+            for k in range(0, len(ids), 16):
+                f.write(", ".join(str(v) for v in ids[k:k + 16]) + "\n")
+            f.write(f"*Elset, elset={name}\n")
+            ids = [i + 1 for i in elems]
+            for k in range(0, len(ids), 16):
+                f.write(", ".join(str(v) for v in ids[k:k + 16]) + "\n")
+        f.write("*End Part\n")
