@@ -54,6 +54,14 @@ ALGO_BYTES = {
 # (dram__bytes_read.sum 991,403,264 + dram__bytes_write.sum 706,622,464 for
 # 4,194,304 particles, k_interact32<fused, 64x8>; one-pass capture).
 NCU_TRAFFIC_PER_PARTICLE = {"fp32k": (991_403_264 + 706_622_464) / 4_194_304}
+# Floating-point work per particle of the fused neighbour sums, from ncu's SASS
+# instruction counters (dadd + dmul + 2 dfma; fadd + fmul + 2 ffma) on the
+# 512x512 micro workload with 2h cells (262,144 particles): k_interact64 executes
+# 1,401,475,197 FP64 flops, k_interact32 1,454,251,763 FP32 flops.
+NCU_FLOPS_PER_PARTICLE = {"fp64": 1_401_475_197 / 262_144, "fp32k": 1_454_251_763 / 262_144}
+# Nominal GB300 rates (no measured figure exists for these pipes): FP64 1.25 TFLOP/s;
+# FP32 152 SMs x 128 lanes x 2 flops x 2.07 GHz = 80.5 TFLOP/s.
+NOMINAL_TFLOPS = {"fp64": 1.25, "fp32k": 80.5}
 STAGES = ["hash+histogram", "scan+scatter+rank", "reorder+predict+eos+artstress+records", "fem half step",
           "neighbour sums+epilogue", "fem update+tool move", "contact/bc/invalidate tail"]
 # fields a caller moves per step in the end-to-end arm (the persistent state)
@@ -520,6 +528,11 @@ def run_product(args):
         ab = ALGO_BYTES[prec_name]
         algo = (ab["read"] + ab["write"]) * case.N
         ach = algo / (stage_interact * 1e-3) / 1e9
+        fl = NCU_FLOPS_PER_PARTICLE[prec_name] * case.N / (stage_interact * 1e-3) / 1e12
+        res["compute"] = {"pipe": "fp64" if prec_name == "fp64" else "fp32", "achieved": fl,
+                          "peak": NOMINAL_TFLOPS[prec_name], "unit": "TFLOP/s",
+                          "frac": fl / NOMINAL_TFLOPS[prec_name], "peak_kind": "nominal",
+                          "flops_per_particle": NCU_FLOPS_PER_PARTICLE[prec_name]}
         res["roofline"] = {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
                            "frac": ach / hbm_peak,
                            "traffic": (NCU_TRAFFIC_PER_PARTICLE[prec_name] * case.N
@@ -531,6 +544,29 @@ def run_product(args):
         del s
         torch.cuda.empty_cache()
 
+    # the same micro workload on the reference's cell geometry (cells of h, 5x5)
+    alt = None
+    if args.cell_factor == 2 and not args.no_alt_geometry:
+        alt = {}
+        hc = setups.micro(n_side=args.n_side, seed=args.seed + rank, cell_factor=1, stencil=2)
+        for prec_name, prec in (("fp32k", abi.SPH_PREC_FP32K), ("fp64", abi.SPH_PREC_FP64)):
+            if args.precision != "both" and args.precision != prec_name:
+                continue
+            s = Solver(hc, prec, device=local)
+            stream_ptr = C.c_void_p()
+            s.lib.sph_get_stream(s.ctx, C.byref(stream_ptr))
+            ext = torch.cuda.ExternalStream(stream_ptr.value, device=torch.device("cuda", local))
+            s.step(args.warmup)
+            s.sync()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            s.step(args.steps)
+            e1.record(ext)
+            e1.synchronize()
+            ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+            alt[prec_name] = {"value": world * hc.N / (ms * 1e-3), "ms_per_step": ms}
+            s.close()
+            torch.cuda.empty_cache()
     batched = None
     if args.batched_cases > 0:
         batched = run_batched(args, local, max_over_ranks, barrier)
@@ -560,6 +596,7 @@ def run_product(args):
                    "form": "FP32 neighbour sums with Kahan compensation, FP64 state/positions/residual"
                            if head_name == "fp32k" else "plain FP64"},
         "roofline": head["roofline"],
+        "compute": head["compute"],
         "clocks": head["clocks"],
         "gpu_launches": int(round(head["launches"])),
         "stage_ms": head["stage_ms"],
@@ -573,9 +610,13 @@ def run_product(args):
     if "fp64" in results and head_name != "fp64":
         f = results["fp64"]
         line["fp64"] = {"value": world * case.N / (f["ms"] * 1e-3), "ms_per_step": f["ms"],
-                        "stage_ms": f["stage_ms"], "roofline": f["roofline"], "clocks": f["clocks"],
+                        "stage_ms": f["stage_ms"], "roofline": f["roofline"], "compute": f["compute"],
+                        "clocks": f["clocks"],
                         "e2e": f.get("e2e")}
         line["speedup_vs_fp64"] = f["ms"] / head["ms"]
+    if alt:
+        line["micro_cells_h"] = dict(alt, workload="the same micro workload with cells of h / 5x5 stencil "
+                                                   "(the reference's geometry), default launch shape")
     if batched is not None:
         batched["value"] *= world
         line["batched_sweep"] = batched
@@ -615,6 +656,7 @@ def main():
     ap.add_argument("--accuracy-every", type=int, default=500)
     ap.add_argument("--no-tune", action="store_true", help="no launch-shape / cell-geometry autotuning")
     ap.add_argument("--cell-factor", type=int, default=2, help="micro workload: cell edge in h")
+    ap.add_argument("--no-alt-geometry", action="store_true", help="skip the cells-of-h micro line")
     ap.add_argument("--stencil", type=int, default=1, help="micro workload: stencil half-width in cells")
     args = ap.parse_args()
     if args.warmup < 3:
