@@ -280,6 +280,14 @@ int sph_run(sph_ctx *ctx, int32_t nsteps);
 /* Same step, issued as the unfused per-stage kernels in reference order. */
 int sph_step_staged(sph_ctx *ctx);
 
+/* ---- wear log: tool_wear::eval_usui (tool_wear.cu:14-54) ---------------------------
+ * Usui wear rate K exp(alpha/T) p |v_r| over the particles in contact (p = |fc| /
+ * (2 pi h), v_r = v - v*n with the component-wise product of the reference, and
+ * its in-contact test on fc.x, fc.y, ft.x, fc.y): out = {min, max, mean}, 0 when
+ * no particle is in contact; *accum_wear (if given) += dt * mean. */
+int sph_eval_usui(sph_ctx *ctx, double K_usui, double alpha, const double tool_vel[2], double dt, double out[3],
+                  double *accum_wear);
+
 /* ---- output in the reference's formats ---------------------------------------------
  * Legacy-ASCII VTK as vtk_writer.cu writes it: particles (vtk_writer.cu:11-220:
  * non-blanked particles as vertex cells with Temperature, on_seg,

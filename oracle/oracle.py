@@ -309,3 +309,21 @@ def mlp_adam(params, m1, m2, grad, t, lr):
     arrs = [np.ascontiguousarray(a, np.float32) for a in (params, m1, m2, grad)]
     load().orc_mlp_adam(*[_fptr(a) for a in arrs], int(t), float(lr))
     return arrs[0], arrs[1], arrs[2]
+
+
+# ---- tool_wear::eval_usui (tool_wear.cu:14-54) ---------------------------------------------------
+def eval_usui(P: dict, K_usui: float, alpha: float, tool_vel):
+    """(min, max, mean) Usui wear rate over the particles in contact, restated with
+    the reference's in-contact test (fc.x, fc.y, ft.x, fc.y) and its component-wise
+    v - v*n."""
+    fc, ft, v, n, h, T = P["fc"], P["ft"], P["vel"], P["n"], P["h"], P["T"]
+    inc = (np.abs(fc[:, 0]) > 0) | (np.abs(fc[:, 1]) > 0) | (np.abs(ft[:, 0]) > 0) | (np.abs(fc[:, 1]) > 0)
+    if not inc.any():
+        return 0.0, 0.0, 0.0
+    vv = v[inc] - np.asarray(tool_vel)[None, :]
+    vr = vv - vv * n[inc]
+    vmag = np.sqrt((vr ** 2).sum(1))
+    fmag = np.sqrt((fc[inc] ** 2).sum(1))
+    p = fmag / (2 * h[inc] * np.pi)
+    w = K_usui * np.exp(alpha / T[inc]) * p * vmag
+    return float(w.min()), float(w.max()), float(w.mean())

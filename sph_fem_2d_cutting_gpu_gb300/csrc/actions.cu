@@ -389,6 +389,49 @@ __global__ void __launch_bounds__(kBlock) k_reduce_cases(SortedFields A, const i
     }
 }
 
+// tool_wear::eval_usui (tool_wear.cu:14-54) per particle, reduced per block:
+// in-contact particles (|fc.x|, |fc.y|, |ft.x| or -- as the reference tests it --
+// |fc.y| again nonzero) contribute K exp(alpha/T) p |v_r| with p = |fc| / (2 pi h)
+// and v_r = v - v*n (component-wise product, as glm's vec2 * vec2).
+// out[4 * block + 0..3] = min, max, sum, count.
+__global__ void __launch_bounds__(kBlock) k_usui(int N, SortedFields A, double K_usui, double alpha, double vtx,
+                                                 double vty, double *__restrict__ out) {
+    __shared__ double smin[kBlock], smax[kBlock], ssum[kBlock], scnt[kBlock];
+    double mn = 1.7976931348623157e308, mx = 0., sm = 0., cnt = 0.;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        const double2 fc = A.fc[i], ft = A.ft[i];
+        if (!(fabs(fc.x) > 0. || fabs(fc.y) > 0. || fabs(ft.x) > 0. || fabs(fc.y) > 0.)) continue;
+        const double2 v0 = A.vel[i], n = A.n[i];
+        const double vx = v0.x - vtx, vy = v0.y - vty;
+        const double rx = vx - vx * n.x, ry = vy - vy * n.y;
+        const double vmag = sqrt(rx * rx + ry * ry);
+        const double fmag = sqrt(fc.x * fc.x + fc.y * fc.y);
+        const double p = fmag / (2. * A.h[i] * 3.14159265358979323846);
+        const double w = K_usui * exp(alpha / A.T[i]) * p * vmag;
+        mn = fmin(mn, w);
+        mx = fmax(mx, w);
+        sm += w;
+        cnt += 1.;
+    }
+    smin[threadIdx.x] = mn; smax[threadIdx.x] = mx; ssum[threadIdx.x] = sm; scnt[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + o]);
+            smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + o]);
+            ssum[threadIdx.x] += ssum[threadIdx.x + o];
+            scnt[threadIdx.x] += scnt[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[4 * blockIdx.x + 0] = smin[0];
+        out[4 * blockIdx.x + 1] = smax[0];
+        out[4 * blockIdx.x + 2] = ssum[0];
+        out[4 * blockIdx.x + 3] = scnt[0];
+    }
+}
+
 // ---- host launchers --------------------------------------------------------------------------------
 #define GRID div_up(N, kBlock), kBlock, 0, s
 
@@ -446,6 +489,10 @@ void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedField
 int reduce_blocks() { return 304; }
 void launch_reduce_force_T(cudaStream_t s, int N, const SortedFields &A, double *out) {
     k_reduce_force_T<<<reduce_blocks(), kBlock, 0, s>>>(N, A, out);
+}
+void launch_usui(cudaStream_t s, int N, const SortedFields &A, double K_usui, double alpha, double vtx, double vty,
+                 double *out) {
+    k_usui<<<reduce_blocks(), kBlock, 0, s>>>(N, A, K_usui, alpha, vtx, vty, out);
 }
 void launch_reduce_cases(cudaStream_t s, int n_cases, const SortedFields &A, const int32_t *offsets,
                          const int32_t *cell_bound, const int32_t *part_bound, double *out) {

@@ -61,6 +61,7 @@ struct sph_ctx {
     MlpDev mlp{};
     bool mlp_on = false;
     int interact_variant = 0;            // launch shape of the fused FP32K neighbour sums
+    double *usui_scratch = nullptr;      // per-block partials of sph_eval_usui
     // pipelined host I/O: uploads into a free particle buffer and downloads run on
     // their own streams, ordered per buffer by events; a step waits only for the
     // copies into its input and out of its output buffer
@@ -1851,6 +1852,35 @@ int sph_append_force_log(sph_ctx *ctx, const char *path) {
     if (!fp) return fail(ctx, SPH_ERR_INVALID, std::string("cannot open ") + path);
     fprintf(fp, "%.9g %.9g\n", f[0], f[1]);   // mfree_gpu.cpp:336-338
     if (fclose(fp) != 0) return write_fail(ctx, nullptr, std::string("cannot write ") + path);
+    return SPH_OK;
+}
+
+// ---- tool_wear::eval_usui (tool_wear.cu:14-54) --------------------------------------------------
+int sph_eval_usui(sph_ctx *ctx, double K_usui, double alpha, const double tool_vel[2], double dt, double out[3],
+                  double *accum_wear) {
+    REQUIRE_CTX();
+    if (!tool_vel || !out) return SPH_ERR_INVALID;
+    const int nb = reduce_blocks();
+    std::vector<double> h(4 * (size_t)nb);
+    double *dev = nullptr;
+    if (!ctx->usui_scratch) DALLOC(ctx->usui_scratch, 4 * (size_t)nb);
+    dev = ctx->usui_scratch;
+    launch_usui(ctx->stream, ctx->N, CUR(ctx), K_usui, alpha, tool_vel[0], tool_vel[1], dev);
+    ctx->launches++;
+    CK_LAUNCH();
+    CK(cudaMemcpyAsync(h.data(), dev, sizeof(double) * 4 * nb, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    double mn = 1.7976931348623157e308, mx = 0., sm = 0., cnt = 0.;
+    for (int b = 0; b < nb; b++) {
+        mn = std::fmin(mn, h[4 * b]);
+        mx = std::fmax(mx, h[4 * b + 1]);
+        sm += h[4 * b + 2];
+        cnt += h[4 * b + 3];
+    }
+    out[0] = cnt == 0. ? 0. : mn;
+    out[1] = mx;
+    out[2] = cnt == 0. ? 0. : sm / cnt;
+    if (accum_wear) *accum_wear += dt * out[2];
     return SPH_OK;
 }
 

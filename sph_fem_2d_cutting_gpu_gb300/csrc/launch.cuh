@@ -50,6 +50,8 @@ void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedField
                       const ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
                       bool next_hash);
 int reduce_blocks();
+void launch_usui(cudaStream_t s, int N, const SortedFields &A, double K_usui, double alpha, double vtx, double vty,
+                 double *out);
 void launch_reduce_force_T(cudaStream_t s, int N, const SortedFields &A, double *out);
 void launch_reduce_cases(cudaStream_t s, int n_cases, const SortedFields &A, const int32_t *offsets,
                          const int32_t *cell_bound, const int32_t *part_bound, double *out);

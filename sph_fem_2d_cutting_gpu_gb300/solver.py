@@ -98,6 +98,17 @@ class Solver:
         s = abi.particles_struct(arrays, self.N)
         self._ck(self.lib.sph_upload_particles(self.ctx, C.byref(s)), "sph_upload_particles")
 
+    def eval_usui(self, K_usui: float, alpha: float, dt: float = 0.0, tool_vel=None):
+        """tool_wear::eval_usui: (min, max, mean) Usui wear rate of the particles in
+        contact; the accumulated wear (dt * mean per call) is kept on the object."""
+        vt = np.array([self.case.tool_speed, 0.0] if tool_vel is None else tool_vel, np.float64)
+        out = np.zeros(3)
+        acc = np.array([getattr(self, "accum_wear", 0.0)])
+        self._ck(self.lib.sph_eval_usui(self.ctx, K_usui, alpha, abi.ptr(vt), dt, abi.ptr(out), abi.ptr(acc)),
+                 "sph_eval_usui")
+        self.accum_wear = float(acc[0])
+        return tuple(out)
+
     # ---- output in the reference's formats (vtk_writer.cu, mfree_gpu.cpp) ------------------------
     def write_vtk(self, path: str):
         """Particles as legacy-ASCII VTK (vtk_writer_write(particle_gpu*, step))."""

@@ -91,3 +91,18 @@ def test_vtk_particles_tool_and_force_log(lib, tmp_path):
     rows = [list(map(float, l.split())) for l in open(tmp_path / "force")]
     assert len(rows) == 3 and all(len(r) == 2 for r in rows)
     s.close()
+
+
+def test_usui_wear_log_matches_oracle(lib):
+    from oracle.oracle import eval_usui
+    case = setups.placed(setups.small_cut(), preload_dx=0.3)
+    s = Solver(case, abi.SPH_PREC_FP64, place_tool=False)
+    s.step(15)
+    K_usui, alpha = 1e-8, -2500.0
+    got = s.eval_usui(K_usui, alpha, dt=case.dt)
+    P = s.download(["fc", "ft", "vel", "n", "h", "T"])
+    want = eval_usui(P, K_usui, alpha, (case.tool_speed, 0.0))
+    assert want[1] > 0, "no particle in contact"
+    assert np.allclose(got, want, rtol=1e-12, atol=0)
+    assert np.isclose(s.accum_wear, case.dt * want[2], rtol=1e-12)
+    s.close()
