@@ -280,6 +280,46 @@ int sph_run(sph_ctx *ctx, int32_t nsteps);
 /* Same step, issued as the unfused per-stage kernels in reference order. */
 int sph_step_staged(sph_ctx *ctx);
 
+/* ---- rigid tool (the reference's SPH-tool mode) --------------------------------------
+ * leap_frog::step(particle_gpu*, grid_base*) with a global `tool` (leap_frog.cu:
+ * 99-160): a rigid polygon tool of up to five segments and an optional fillet
+ * (tool.cpp, tool_gpu.cu), penalty contact with LS-DYNA friction
+ * (do_compute_contact_forces, tool_gpu.cu:142-198), friction heat
+ * (do_material_fric_heat_gen, actions_gpu.cu:316-343, when trml_wp.eta != 0),
+ * tool particles moved with the tool (update_tool_particles, tool_gpu.cu:201-213)
+ * and the segments moved on the host every step (tool::update_tool,
+ * tool.cpp).  Segment i runs left -> right with outward normal n, the line
+ * y = a x + b (x = b when vertical) through its end points; with a fillet the
+ * tool has five segments and the fillet replaces segment 2 in the distance
+ * search.  The penalty uses phys.mass and tool.contact_alpha.  A context has
+ * either a FEM tool or a rigid tool. */
+#define SPH_RIGID_MAX_SEG 5
+typedef struct sph_rigid_tool {
+    int32_t n_seg, has_fillet;
+    double left[SPH_RIGID_MAX_SEG][2], right[SPH_RIGID_MAX_SEG][2], n[SPH_RIGID_MAX_SEG][2];
+    double la[SPH_RIGID_MAX_SEG], lb[SPH_RIGID_MAX_SEG];
+    int32_t vertical[SPH_RIGID_MAX_SEG], pad0;
+    double fillet_p[2], fillet_r, fillet_t1, fillet_t2;   /* centre, radius, angle range */
+    double vel[2];
+    double mu;                                           /* Coulomb friction; 0: none */
+} sph_rigid_tool;
+
+int sph_set_rigid_tool(sph_ctx *ctx, const sph_rigid_tool *tool);   /* NULL removes it */
+int sph_get_rigid_tool(sph_ctx *ctx, sph_rigid_tool *tool);
+/* Staged calls of the rigid-tool step: tool_gpu_update_tool (segments and tool
+ * particles by vel * dt), compute_contact_forces, material_fric_heat_gen. */
+int sph_rigid_tool_update(sph_ctx *ctx);
+int sph_compute_contact_forces(sph_ctx *ctx);
+int sph_material_fric_heat_gen(sph_ctx *ctx);
+
+/* Thermal conduction model of the neighbour sums: SPH_THERMAL_BROOKSHAW (the
+ * reference's default, interactions_gpu.cu:143-379) or SPH_THERMAL_PSE
+ * (do_interactions_heat_pse, interactions_gpu.cu:84-140; FP64 contexts only). */
+#define SPH_THERMAL_BROOKSHAW 0
+#define SPH_THERMAL_PSE 1
+int sph_set_thermal_model(sph_ctx *ctx, int32_t model);
+int sph_interactions_heat_pse(sph_ctx *ctx);
+
 /* ---- wear log: tool_wear::eval_usui (tool_wear.cu:14-54) ---------------------------
  * Usui wear rate K exp(alpha/T) p |v_r| over the particles in contact (p = |fc| /
  * (2 pi h), v_r = v - v*n with the component-wise product of the reference, and

@@ -39,6 +39,7 @@ def load() -> C.CDLL:
     S = C.POINTER(abi.Segments)
     F = C.POINTER(abi.Fem)
     T = C.POINTER(abi.ToolState)
+    R = C.POINTER(abi.RigidTool)
     PD, PI, D, I = abi.PD, abi.PI, C.c_double, C.c_int
     sig = {
         "orc_num_threads": ([], I),
@@ -73,6 +74,13 @@ def load() -> C.CDLL:
         "orc_fem_calculate_temp_rate": ([F, PD, PD], None),
         "orc_fem_calculate_temp": ([F, PD, D], None),
         "orc_step": ([P, PI, PI, G, K, D, S, F, T, I], C.c_uint32),
+        "orc_interactions_monaghan_pse_build": ([P, PI, PI, G, K], None),
+        "orc_rigid_move": ([R, D], None),
+        "orc_rigid_move_particles": ([P, PD, D], None),
+        "orc_contact_rigid": ([P, R, K, D], None),
+        "orc_fric_heat_rigid": ([P, K, PD, D], None),
+        "orc_interactions_heat_pse": ([P, PI, PI, G, K], None),
+        "orc_step_rigid": ([P, PI, PI, G, K, D, R, I], C.c_uint32),
         "orc_mlp_eval": ([PD, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int64, I, PD,
                           PD, PD], I),
         "orc_mlp_adam": ([C.POINTER(C.c_float)] * 4 + [C.c_int64, C.c_float], I),
@@ -105,7 +113,7 @@ class OracleSim:
     tool, the interface segments, FEM system and tool kinematics."""
 
     def __init__(self, constants: abi.Constants, grid: abi.GridParams, particles: dict, dt: float,
-                 tool: dict | None = None):
+                 tool: dict | None = None, rigid: abi.RigidTool | None = None, pse: bool = False):
         self.lib = load()
         self.C = constants
         self.grid = grid
@@ -124,6 +132,12 @@ class OracleSim:
             C.memmove(C.byref(self.ts), C.byref(st), C.sizeof(abi.ToolState))
             self.n_colors = int(tool.get("n_cut_colors", 6))
             self.tool = True
+        # rigid (SPH-mode) tool and the thermal solver of leap_frog::step(particles, grid)
+        self.rigid = None
+        if rigid is not None:
+            self.rigid = abi.RigidTool()
+            C.memmove(C.byref(self.rigid), C.byref(rigid), C.sizeof(abi.RigidTool))
+        self.pse = bool(pse)
 
     def pstruct(self):
         return abi.particles_struct(self.P, self.N)
@@ -138,6 +152,10 @@ class OracleSim:
 
     def step(self) -> int:
         p = self.pstruct()
+        if self.rigid is not None or self.pse:
+            return self.lib.orc_step_rigid(C.byref(p), abi.ptr(self.cell_start), abi.ptr(self.cell_end),
+                                           C.byref(self.g), C.byref(self.C), self.dt,
+                                           C.byref(self.rigid) if self.rigid is not None else None, int(self.pse))
         if self.tool:
             s, f = self.sstruct(), self.fstruct()
             return self.lib.orc_step(C.byref(p), abi.ptr(self.cell_start), abi.ptr(self.cell_end), C.byref(self.g),
@@ -165,8 +183,29 @@ class OracleSim:
 
     def interactions_monaghan(self):
         p = self.pstruct()
-        self.lib.orc_interactions_monaghan(C.byref(p), abi.ptr(self.cell_start), abi.ptr(self.cell_end),
+        fn = self.lib.orc_interactions_monaghan_pse_build if self.pse else self.lib.orc_interactions_monaghan
+        fn(C.byref(p), abi.ptr(self.cell_start), abi.ptr(self.cell_end), C.byref(self.g), C.byref(self.C))
+
+    def interactions_heat_pse(self):
+        p = self.pstruct()
+        self.lib.orc_interactions_heat_pse(C.byref(p), abi.ptr(self.cell_start), abi.ptr(self.cell_end),
                                            C.byref(self.g), C.byref(self.C))
+
+    # rigid tool (tool_gpu.cu, actions_gpu.cu:316-343)
+    def rigid_tool_update(self):
+        p = self.pstruct()
+        self.lib.orc_rigid_move(C.byref(self.rigid), self.dt)
+        vel = np.array(self.rigid.vel[:], dtype=np.float64)
+        self.lib.orc_rigid_move_particles(C.byref(p), abi.ptr(vel), self.dt)
+
+    def compute_contact_forces(self):
+        p = self.pstruct()
+        self.lib.orc_contact_rigid(C.byref(p), C.byref(self.rigid), C.byref(self.C), self.dt)
+
+    def material_fric_heat_gen(self):
+        p = self.pstruct()
+        vel = np.array(self.rigid.vel[:], dtype=np.float64)
+        self.lib.orc_fric_heat_rigid(C.byref(p), C.byref(self.C), abi.ptr(vel), self.dt)
 
     def material_stress_rate_jaumann(self):
         p = self.pstruct()

@@ -431,19 +431,24 @@ void orc_corrector_artificial_stress(sph_particles *P, const sph_constants *C) {
     }
 }
 
-// interactions_gpu.cu:143-379 do_interactions_monaghan (Brookshaw on, SURFACE off)
-// with unhash/hash (:75-82); cell stencil generalised to g->stencil cells per side.
-void orc_interactions_monaghan(sph_particles *P, const int32_t *cell_start, const int32_t *cell_end,
-                               const sph_geom_constants *g, const sph_constants *C) {
+// interactions_gpu.cu:143-379 do_interactions_monaghan (SURFACE off) with
+// unhash/hash (:75-82); cell stencil generalised to g->stencil cells per side.
+// pse == 0: the Brookshaw build (types.h:122).  pse != 0: the
+// Thermal_Conduction_PSE build -- tool particles return before any write
+// (:156-158) and the Brookshaw sum is compiled out (T_t comes from
+// interactions_heat_pse).
+static void monaghan_impl(sph_particles *P, const int32_t *cell_start, const int32_t *cell_end,
+                          const sph_geom_constants *g, const sph_constants *C, int pse) {
     const int N = P->N;
     const int R = g->stencil;
 #pragma omp parallel for schedule(dynamic, 256)
     for (int pidx = 0; pidx < N; pidx++) {
         if (P->blanked[pidx] == 1.) continue;
         double is_tool_particle_i = P->tool_particle[pidx];
+        if (pse && is_tool_particle_i == 1.) continue;
         double mass = C->phys.mass;
         double K = C->phys.K;
-        double thermal_alpha = (is_tool_particle_i == 0.) ? C->trml_wp.alpha : C->trml_tool_sph.alpha;
+        double thermal_alpha = pse ? 0. : ((is_tool_particle_i == 0.) ? C->trml_wp.alpha : C->trml_tool_sph.alpha);
         double wdeltap = C->corr.wdeltap, alpha = C->corr.alpha, beta = C->corr.beta,
                eta = C->corr.eta, eps = C->corr.xspheps;
         int nx = g->nx, ny = g->ny;
@@ -536,6 +541,16 @@ void orc_interactions_monaghan(sph_particles *P, const int32_t *cell_start, cons
         P->vel_t[2 * pidx] = vt[0]; P->vel_t[2 * pidx + 1] = vt[1];
         if (thermal_alpha != 0.) P->T_t[pidx] = thermal_alpha * T_lapl;
     }
+}
+
+void orc_interactions_monaghan(sph_particles *P, const int32_t *cell_start, const int32_t *cell_end,
+                               const sph_geom_constants *g, const sph_constants *C) {
+    monaghan_impl(P, cell_start, cell_end, g, C, 0);
+}
+
+void orc_interactions_monaghan_pse_build(sph_particles *P, const int32_t *cell_start, const int32_t *cell_end,
+                                         const sph_geom_constants *g, const sph_constants *C) {
+    monaghan_impl(P, cell_start, cell_end, g, C, 1);
 }
 
 // actions_gpu.cu:280-314 do_material_stress_rate_jaumann (GLM column-major 3x3
@@ -935,6 +950,264 @@ uint32_t orc_step(sph_particles *P, int32_t *cell_start, int32_t *cell_end, cons
         orc_tool_update(F, ts, dt);
         st |= orc_contact_s1(P, Sg, C, ts->tl_point_ref, ts->ref_dist, ts->vel, dt);
         orc_contact_s2(P, Sg, C, F->T, dt);
+    }
+    orc_boundary_conditions(P);
+    orc_boundary_conditions_thermal(P, C);
+    if (orc_invalidate(P) > 0) st |= SPH_STATUS_NAN_BLANKED;
+    return st;
+}
+
+
+// ---- rigid (SPH-mode) tool ---------------------------------------------------------------
+// geometric_primitives.cpp:58-75 line(p1, p2)
+static void rigid_line(const double *p1, const double *p2, double &a, double &b, int32_t &vertical) {
+    double detM = p1[0] * 1. - 1. * p2[0];
+    if (fabs(detM) < 1e-12) {
+        vertical = 1;
+        a = DBL_MAX;
+        b = p1[0];
+        return;
+    }
+    vertical = 0;
+    a = (p1[1] * 1. - 1. * p2[1]) / detM;
+    b = (p2[1] * p1[0] - p2[0] * p1[1]) / detM;
+}
+
+// tool.cpp:202-212 tool::update_tool: segment ends and fillet centre move by
+// dt * velocity, the lines are rebuilt, the normals stay.
+void orc_rigid_move(sph_rigid_tool *t, double dt) {
+    for (int i = 0; i < t->n_seg; i++) {
+        for (int a = 0; a < 2; a++) {
+            t->left[i][a] += dt * t->vel[a];
+            t->right[i][a] += dt * t->vel[a];
+        }
+        rigid_line(t->left[i], t->right[i], t->la[i], t->lb[i], t->vertical[i]);
+    }
+    if (t->has_fillet) {
+        t->fillet_p[0] += dt * t->vel[0];
+        t->fillet_p[1] += dt * t->vel[1];
+    }
+}
+
+// tool_gpu.cu:205-216 update_tool_particles
+void orc_rigid_move_particles(sph_particles *P, const double vel[2], double dt) {
+    for (int i = 0; i < P->N; i++) {
+        if (P->tool_particle[i] == 0.) continue;
+        P->pos[2 * i] += dt * vel[0];
+        P->pos[2 * i + 1] += dt * vel[1];
+    }
+}
+
+// tool_gpu.cu:24-31 myatan2
+static double rigid_myatan2(double y, double x) {
+    double t = atan2(y, x);
+    return (t > 0.) ? t : t + 2 * M_PI;
+}
+
+// tool_gpu.cu:33-58 circle_segment_distance
+static double rigid_fillet_distance(const sph_rigid_tool *t, double qx, double qy) {
+    double Ax = t->fillet_p[0], Ay = t->fillet_p[1], r = t->fillet_r;
+    double Cx = Ax + r * (qx - Ax) / sqrt((qx - Ax) * (qx - Ax) + (qy - Ay) * (qy - Ay));
+    double Cy = Ay + r * (qy - Ay) / sqrt((qx - Ax) * (qx - Ax) + (qy - Ay) * (qy - Ay));
+    double th = rigid_myatan2(Ay - Cy, Ax - Cx);
+    bool valid = th > fmin(t->fillet_t1, t->fillet_t2) && th < fmax(t->fillet_t1, t->fillet_t2);
+    if (!valid) return FLT_MAX;
+    return sqrt((Cx - qx) * (Cx - qx) + (Cy - qy) * (Cy - qy));
+}
+
+// tool_gpu.cu:60-76 segment_closest_point
+static void rigid_closest(const sph_rigid_tool *t, int i, double qx, double qy, double &px, double &py) {
+    if (t->vertical[i]) {
+        px = t->lb[i];
+        py = qy;
+        return;
+    }
+    double bb = -1, cc = t->lb[i], aa = t->la[i];
+    px = (bb * (bb * qx - aa * qy) - aa * cc) / (aa * aa + bb * bb);
+    py = (aa * (-bb * qx + aa * qy) - bb * cc) / (aa * aa + bb * bb);
+}
+
+// glm::normalize: v * inversesqrt(dot(v, v)), inversesqrt(x) = 1 / sqrt(x)
+static void rigid_normalize(double x, double y, double &nx, double &ny) {
+    double inv = 1. / sqrt(x * x + y * y);
+    nx = x * inv;
+    ny = y * inv;
+}
+
+// tool_gpu.cu:82-134 establish_contact (a fillet exists iff there are 5 segments)
+static bool rigid_establish_contact(const sph_rigid_tool *t, double qx, double qy, double cp[2], double n[2]) {
+    bool has_fillet = t->n_seg == SPH_RIGID_MAX_SEG;
+    bool in = true;
+    for (int i = 0; i < t->n_seg; i++)
+        in = in && ((t->left[i][0] - qx) * t->n[i][0] + (t->left[i][1] - qy) * t->n[i][1] < 0.);
+    if (has_fillet) {
+        double dx = t->fillet_p[0] - qx, dy = t->fillet_p[1] - qy;
+        in = in || sqrt(dx * dx + dy * dy) < t->fillet_r;
+    }
+    if (!in) return false;
+    double depth = FLT_MAX;
+    for (int i = 0; i < t->n_seg; i++) {
+        double d;
+        if (t->vertical[i]) {
+            d = fabs(t->left[i][0] - qx);
+            if (d < depth) {
+                depth = d;
+                rigid_normalize(t->left[i][0] - qx, 0., n[0], n[1]);
+                cp[0] = t->left[i][0];
+                cp[1] = qy;
+            }
+        } else if (has_fillet && i == 2) {
+            d = rigid_fillet_distance(t, qx, qy);
+            if (d < depth) {
+                depth = d;
+                rigid_normalize(qx - t->fillet_p[0], qy - t->fillet_p[1], n[0], n[1]);
+                cp[0] = t->fillet_p[0] + n[0] * t->fillet_r;
+                cp[1] = t->fillet_p[1] + n[1] * t->fillet_r;
+            }
+        } else {
+            double px, py;
+            rigid_closest(t, i, qx, qy, px, py);
+            d = sqrt((px - qx) * (px - qx) + (py - qy) * (py - qy));
+            if (d < depth) {
+                depth = d;
+                n[0] = -t->n[i][0];
+                n[1] = -t->n[i][1];
+                cp[0] = px;
+                cp[1] = py;
+            }
+        }
+    }
+    return true;
+}
+
+// tool_gpu.cu:146-202 do_compute_contact_forces (penalty with slave_mass =
+// phys.mass, contact_alpha of the tool constants; LS-DYNA friction).  Blanked
+// particles are not skipped, as in the reference.
+void orc_contact_rigid(sph_particles *P, const sph_rigid_tool *t, const sph_constants *C, double dt) {
+    const double ms = C->phys.mass, alpha = C->tool.contact_alpha;
+    for (int i = 0; i < P->N; i++) {
+        if (P->tool_particle[i] != 0.) continue;
+        double xs[2] = {P->pos[2 * i], P->pos[2 * i + 1]}, vs[2] = {P->vel[2 * i], P->vel[2 * i + 1]};
+        double xm[2] = {0., 0.}, n[2] = {0., 0.};
+        if (!rigid_establish_contact(t, xs[0], xs[1], xm, n)) {
+            for (int a = 0; a < 2; a++) P->fc[2 * i + a] = P->ft[2 * i + a] = P->n[2 * i + a] = 0.;
+            continue;
+        }
+        double dt2 = dt * dt;
+        double gN = (xs[0] - xm[0]) * n[0] + (xs[1] - xm[1]) * n[1];
+        double fN[2], fT[2] = {0., 0.};
+        for (int a = 0; a < 2; a++) fN[a] = -ms * gN * n[a] / dt2 * alpha;
+        if (t->mu != 0.) {
+            double v[2] = {vs[0] - t->vel[0], vs[1] - t->vel[1]};
+            double vr[2] = {v[0] - v[0] * n[0], v[1] - v[1] * n[1]};
+            double fricold[2] = {P->ft[2 * i], P->ft[2 * i + 1]};
+            double kdeltae[2] = {alpha * ms * vr[0] / dt, alpha * ms * vr[1] / dt};
+            double fy = t->mu * sqrt(fN[0] * fN[0] + fN[1] * fN[1]);
+            double fstar[2] = {fricold[0] - kdeltae[0], fricold[1] - kdeltae[1]};
+            double ls = sqrt(fstar[0] * fstar[0] + fstar[1] * fstar[1]);
+            if (ls > fy) {
+                fT[0] = fy * fstar[0] / ls;
+                fT[1] = fy * fstar[1] / ls;
+            } else {
+                fT[0] = fstar[0];
+                fT[1] = fstar[1];
+            }
+        }
+        for (int a = 0; a < 2; a++) {
+            P->fc[2 * i + a] = fN[a];
+            P->ft[2 * i + a] = fT[a];
+            P->n[2 * i + a] = n[a];
+        }
+    }
+}
+
+// actions_gpu.cu:316-343 do_material_fric_heat_gen (launched only when
+// thermals_wp.eta != 0, actions_gpu.cu:955-965); blanked particles are not skipped.
+void orc_fric_heat_rigid(sph_particles *P, const sph_constants *C, const double vel_tool[2], double dt) {
+    if (C->trml_wp.eta == 0.) return;
+    for (int i = 0; i < P->N; i++) {
+        if (P->tool_particle[i] != 0.) continue;
+        double fx = P->ft[2 * i], fy = P->ft[2 * i + 1];
+        double f = sqrtf_d(fx * fx + fy * fy);
+        if (f == 0.) continue;
+        double nx = P->n[2 * i], ny = P->n[2 * i + 1];
+        double vdx = P->vel[2 * i] - vel_tool[0], vdy = P->vel[2 * i + 1] - vel_tool[1];
+        double vdn = vdx * nx + vdy * ny;
+        double vrx = vdx - vdn * nx, vry = vdy - vdn * ny;
+        double v = sqrtf_d(vrx * vrx + vry * vry);
+        P->T[i] += C->trml_wp.eta * dt * f * v / (C->trml_wp.cp * C->phys.mass);
+    }
+}
+
+// interactions_gpu.cu:84-140 do_interactions_heat_pse with kernels.cuh:67-84
+// lapl_pse, over the 5x5 block of cells of edge h (launched only when
+// thermals_workpiece.alpha != 0, :434-435).  alpha by the tool flag (the
+// reference binds its tool-flag texture over N ints of an N-double array, so
+// its second half of particles reads flag 0; the intended flag is used here).
+void orc_interactions_heat_pse(sph_particles *P, const int32_t *cell_start, const int32_t *cell_end,
+                               const sph_geom_constants *g, const sph_constants *C) {
+    if (C->trml_wp.alpha == 0.) return;
+    const int N = P->N, nx = g->nx, ny = g->ny;
+    const double mass = C->phys.mass;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int pidx = 0; pidx < N; pidx++) {
+        if (P->blanked[pidx] == 1.) continue;
+        double pix = P->pos[2 * pidx], piy = P->pos[2 * pidx + 1], hi = P->h[pidx], Ti = P->T[pidx];
+        int hashi = P->hash[pidx];
+        double alpha = (P->tool_particle[pidx] == 1.) ? C->trml_tool_sph.alpha : C->trml_wp.alpha;
+        double T_ti = 0.;
+        if (hashi >= 0 && hashi < g->num_cell) {
+            int gi = hashi / ny, gj = hashi - gi * ny;
+            int low_i = gi - 2 < 0 ? 0 : gi - 2, low_j = gj - 2 < 0 ? 0 : gj - 2;
+            int high_i = gi + 3 > nx ? nx : gi + 3, high_j = gj + 3 > ny ? ny : gj + 3;
+            for (int ii = low_i; ii < high_i; ii++)
+                for (int jj = low_j; jj < high_j; jj++) {
+                    int idx = ii * ny + jj;
+                    int c_start = cell_start[idx], c_end = cell_end[idx];
+                    if (c_start == -1) continue;
+                    for (int iter = c_start; iter < c_end; iter++) {
+                        double xij = pix - P->pos[2 * iter], yij = piy - P->pos[2 * iter + 1];
+                        double xx = sqrt(xij * xij + yij * yij);
+                        double h2 = hi * hi, h4 = h2 * h2;
+                        double w2 = +4. / (h4 * M_PI) * exp(-xx * xx / (h2));
+                        T_ti += (P->T[iter] - Ti) * w2 * mass / P->rho[iter];
+                    }
+                }
+        }
+        P->T_t[pidx] = alpha * T_ti;
+    }
+}
+
+// leap_frog.cu:99-160 leap_frog::step(particle_gpu*, grid_base*) with an SPH
+// (rigid) tool t (NULL: no tool); pse selects the Thermal_Conduction_PSE
+// build.  Returns SPH_STATUS_* bits observed during the step.
+uint32_t orc_step_rigid(sph_particles *P, int32_t *cell_start, int32_t *cell_end, const sph_geom_constants *g,
+                        const sph_constants *C, double dt, sph_rigid_tool *t, int pse) {
+    const int N = P->N;
+    uint32_t st = 0;
+    std::vector<double> pos_init(2 * (size_t)N), vel_init(2 * (size_t)N), S_init(4 * (size_t)N), rho_init(N), T_init(N);
+    orc_compute_hashes(P, g);
+    if (orc_sort_green(P, cell_start, cell_end, g->num_cell) > 0) st |= SPH_STATUS_OUT_OF_GRID;
+    orc_init(P, pos_init.data(), vel_init.data(), S_init.data(), rho_init.data(), T_init.data());
+    orc_predict(P, pos_init.data(), vel_init.data(), S_init.data(), rho_init.data(), T_init.data(), dt);
+    orc_material_eos(P, C);
+    orc_corrector_artificial_stress(P, C);
+    monaghan_impl(P, cell_start, cell_end, g, C, pse);
+    if (pse) orc_interactions_heat_pse(P, cell_start, cell_end, g, C);
+    orc_material_stress_rate_jaumann(P, C);
+    orc_contmech_continuity(P);
+    orc_contmech_momentum(P, C);
+    orc_contmech_advection(P);
+    orc_correct(P, pos_init.data(), vel_init.data(), S_init.data(), rho_init.data(), T_init.data(), dt);
+    if (t) orc_fric_heat_rigid(P, C, t->vel, dt);
+    if (C->plastic) {
+        int64_t its = 0;
+        if (orc_plasticity_johnson_cook(P, C, dt, &its) > 0) st |= SPH_STATUS_SECANT_MAXITER;
+    }
+    if (t) {
+        orc_rigid_move(t, dt);
+        orc_rigid_move_particles(P, t->vel, dt);
+        orc_contact_rigid(P, t, C, dt);
     }
     orc_boundary_conditions(P);
     orc_boundary_conditions_thermal(P, C);

@@ -15,6 +15,8 @@ LIB_PATH = Path(__file__).resolve().parent / "lib" / "libsphfem.so"
 
 SPH_OK, SPH_ERR_INVALID, SPH_ERR_CUDA, SPH_ERR_NO_DEVICE, SPH_ERR_ALLOC, SPH_ERR_STATE = range(6)
 SPH_PREC_FP64, SPH_PREC_FP32K = 0, 1
+SPH_THERMAL_BROOKSHAW, SPH_THERMAL_PSE = 0, 1
+SPH_RIGID_MAX_SEG = 5
 
 STATUS_BITS = {
     "out_of_grid": 1 << 0,
@@ -122,6 +124,16 @@ JC_LOG_WIDTH = 8
 
 class LaunchConfig(C.Structure):
     _fields_ = [("interact_variant", I32)]
+
+
+class RigidTool(C.Structure):
+    """sph_rigid_tool: the segments of a rigid tool outline (tool_gpu.h) and its fillet."""
+    _fields_ = [("n_seg", I32), ("has_fillet", I32),
+                ("left", (D * 2) * SPH_RIGID_MAX_SEG), ("right", (D * 2) * SPH_RIGID_MAX_SEG),
+                ("n", (D * 2) * SPH_RIGID_MAX_SEG), ("la", D * SPH_RIGID_MAX_SEG), ("lb", D * SPH_RIGID_MAX_SEG),
+                ("vertical", I32 * SPH_RIGID_MAX_SEG), ("pad0", I32),
+                ("fillet_p", D * 2), ("fillet_r", D), ("fillet_t1", D), ("fillet_t2", D),
+                ("vel", D * 2), ("mu", D)]
 
 
 class CaseDesc(C.Structure):
@@ -236,6 +248,9 @@ def load() -> C.CDLL:
         "sph_download_particles_async": ([P, C.POINTER(Particles)], C.c_int),
         "sph_set_launch_config": ([P, C.POINTER(LaunchConfig)], C.c_int),
         "sph_get_launch_config": ([P, C.POINTER(LaunchConfig)], C.c_int),
+        "sph_set_rigid_tool": ([P, C.POINTER(RigidTool)], C.c_int),
+        "sph_get_rigid_tool": ([P, C.POINTER(RigidTool)], C.c_int),
+        "sph_set_thermal_model": ([P, I32], C.c_int),
     }
     for name in STAGE_FUNCTIONS:
         proto.setdefault(name, ([P], C.c_int))
@@ -291,4 +306,5 @@ STAGE_FUNCTIONS = [
     "sph_perform_boundary_conditions", "sph_perform_boundary_conditions_thermal", "sph_debug_invalidate",
     "sph_interactions_monaghan", "sph_material_fric_heat_gen_fem", "sph_compute_contact_forces_fem",
     "sph_fem_reset_server", "sph_fem_apply_robin", "sph_fem_calculate_temp_rate", "sph_step", "sph_step_staged",
+    "sph_rigid_tool_update", "sph_compute_contact_forces", "sph_material_fric_heat_gen", "sph_interactions_heat_pse",
 ]

@@ -2,6 +2,7 @@
 // the staged form (one launch per reference call, same order and arrays) and
 // the fused contact / boundary-condition / invalidate kernel of the step.
 #include "launch.cuh"
+#include "rigid.cuh"
 
 namespace sphfem {
 
@@ -247,12 +248,51 @@ __global__ void __launch_bounds__(kBlock) k_invalidate(int N, SortedFields A, ui
     }
 }
 
+// ---- rigid (SPH-mode) tool: tool_gpu.cu, actions_gpu.cu:316-343 ----------------------------------
+// tool::update_tool (tool.cpp:202-212) on the device copy of the tool.
+__global__ void k_rigid_move(sph_rigid_tool *t, double dt) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) rigid_move(*t, dt);
+}
+
+// tool_gpu.cu:205-216 update_tool_particles
+__global__ void __launch_bounds__(kBlock) k_rigid_move_particles(int N, SortedFields A,
+                                                                 const sph_rigid_tool *__restrict__ t, double dt) {
+    PARTICLE_LOOP_HEAD
+    if (!flag_nonzero(A.tool_particle[i])) return;
+    double2 pos = A.pos[i];
+    pos.x += dt * t->vel[0];
+    pos.y += dt * t->vel[1];
+    A.pos[i] = pos;
+}
+
+// tool_gpu.cu:146-202 do_compute_contact_forces (no blanked test, as there)
+__global__ void __launch_bounds__(kBlock) k_contact_rigid(int N, KConsts K, SortedFields A, double dt) {
+    PARTICLE_LOOP_HEAD
+    if (flag_nonzero(A.tool_particle[i])) return;
+    double2 fc, ft = A.ft[i], nrm;
+    rigid_contact_one(K, *K.rigid, dt, A.pos[i], A.vel[i], fc, ft, nrm);
+    A.fc[i] = fc;
+    A.ft[i] = ft;
+    A.n[i] = nrm;
+}
+
+// actions_gpu.cu:316-343 do_material_fric_heat_gen (no blanked test, as there)
+__global__ void __launch_bounds__(kBlock) k_fric_heat_rigid(int N, KConsts K, SortedFields A, double dt) {
+    PARTICLE_LOOP_HEAD
+    if (flag_nonzero(A.tool_particle[i])) return;
+    double T = A.T[i];
+    rigid_fric_heat_one(K, dt, K.rigid->vel, A.vel[i], A.ft[i], A.n[i], T);
+    if (T != A.T[i]) A.T[i] = T;
+}
+
 // ---- fused tail of the step ----------------------------------------------------------------------
-// contact s1 + s2 (actions_gpu.cu:423-617), do_boundary_conditions,
-// do_boundary_conditions_thermal, do_invalidate (actions_gpu.cu:756-824) for
-// one particle, then (kNextHash) the next step's compute_hashes and the
-// counting-sort histogram (grid.cu:25-42) on the final state.
-template <bool kTool, bool kNextHash>
+// The tool's contact for one particle -- kMode 1: FEM tool, contact s1 + s2
+// (actions_gpu.cu:423-617); kMode 2: rigid tool, update_tool_particles and
+// do_compute_contact_forces (tool_gpu.cu:146-216); kMode 0: no tool -- then
+// do_boundary_conditions, do_boundary_conditions_thermal, do_invalidate
+// (actions_gpu.cu:756-824) and (kNextHash) the next step's compute_hashes and
+// the counting-sort histogram (grid.cu:25-42) on the final state.
+template <int kMode, bool kNextHash>
 __global__ void __launch_bounds__(kBlock) k_step_tail(int N, KConsts K, SortedFields A, SegDev seg,
                                                       const ToolDev *__restrict__ tool,
                                                       const double *__restrict__ T_nodes, SortScratch X,
@@ -263,7 +303,7 @@ __global__ void __launch_bounds__(kBlock) k_step_tail(int N, KConsts K, SortedFi
     const bool bc_thermal = K.thermal_bc && flag_is_one(A.fixed[i]);                         // ..._thermal
     uint32_t st = 0;
     double2 pos = A.pos[i];
-    if (kTool && !blanked) {
+    if (kMode == 1 && !blanked) {
         // the particle's case: its tool, time step and interface segments
         const ToolDev &tc = tool[case_of_hash(K, A.hash[i])];
         SegDev cs = seg;
@@ -286,6 +326,20 @@ __global__ void __launch_bounds__(kBlock) k_step_tail(int N, KConsts K, SortedFi
             double T = A.T[i];
             contact_s2_one(K, tc.dt, seg, T_nodes, on, A.rho[i], T);
             A.T[i] = T;
+        }
+    } else if (kMode == 2) {
+        const sph_rigid_tool &rt = *K.rigid;
+        if (flag_nonzero(A.tool_particle[i])) {   // update_tool_particles, blanked or not
+            pos.x += K.dt * rt.vel[0];
+            pos.y += K.dt * rt.vel[1];
+            A.pos[i] = pos;
+        } else {                                  // contact, blanked or not
+            double2 fc, ft = A.ft[i], nrm;
+            rigid_contact_one(K, rt, K.dt, pos, A.vel[i], fc, ft, nrm);
+            A.ft[i] = ft;
+            A.n[i] = nrm;
+            if (bc_fixed) fc = make_double2(0., 0.);
+            A.fc[i] = fc;
         }
     } else if (bc_fixed) {
         A.fc[i] = make_double2(0., 0.);
@@ -479,12 +533,25 @@ void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedField
                       const ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
                       bool next_hash) {
     if (K.has_tool) {
-        if (next_hash) k_step_tail<true, true><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
-        else k_step_tail<true, false><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
+        if (next_hash) k_step_tail<1, true><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
+        else k_step_tail<1, false><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
+    } else if (K.rigid) {
+        if (next_hash) k_step_tail<2, true><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
+        else k_step_tail<2, false><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
     } else {
-        if (next_hash) k_step_tail<false, true><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
-        else k_step_tail<false, false><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
+        if (next_hash) k_step_tail<0, true><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
+        else k_step_tail<0, false><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
     }
+}
+void launch_rigid_move(cudaStream_t s, sph_rigid_tool *t, double dt) { k_rigid_move<<<1, 32, 0, s>>>(t, dt); }
+void launch_rigid_move_particles(cudaStream_t s, int N, const SortedFields &A, const sph_rigid_tool *t, double dt) {
+    k_rigid_move_particles<<<GRID>>>(N, A, t, dt);
+}
+void launch_contact_rigid(cudaStream_t s, int N, const KConsts &K, const SortedFields &A) {
+    k_contact_rigid<<<GRID>>>(N, K, A, K.dt);
+}
+void launch_fric_heat_rigid(cudaStream_t s, int N, const KConsts &K, const SortedFields &A) {
+    k_fric_heat_rigid<<<GRID>>>(N, K, A, K.dt);
 }
 int reduce_blocks() { return 304; }
 void launch_reduce_force_T(cudaStream_t s, int N, const SortedFields &A, double *out) {

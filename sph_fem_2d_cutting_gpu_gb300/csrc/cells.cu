@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(kBlock) k_build_records(int N, KConsts K, Sort
     if (k >= N) return;
     double tool = A.tool_particle[k];
     double thermal_alpha = (tool == 0.) ? K.c.trml_wp.alpha : K.c.trml_tool_sph.alpha;
-    double T = (thermal_alpha != 0.) ? A.T[k] : 0.;
+    double T = (thermal_alpha != 0. || K.thermal_pse) ? A.T[k] : 0.;   // PSE reads every neighbour's T
     int hash = A.hash[k];
     if (rec64) {
         int row = 0;
@@ -326,7 +326,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused(int N, const int32_t *_
         F.R[k] = R;
     }
     double thermal_alpha = (tool == 0.) ? K.c.trml_wp.alpha : K.c.trml_tool_sph.alpha;
-    double Tn = (thermal_alpha != 0.) ? T : 0.;
+    double Tn = (thermal_alpha != 0. || K.thermal_pse) ? T : 0.;   // PSE reads every neighbour's T
     if (!kF32) {
         int row = 0;
         if (hash >= 0 && hash < K.g.num_cell) row = hash - (hash / K.g.ny) * K.g.ny;

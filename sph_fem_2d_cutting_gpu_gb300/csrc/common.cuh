@@ -62,6 +62,9 @@ struct KConsts {
     unsigned long long *jc_stats;         // [0] return mappings, [1] secant iterations
     int32_t *jc_list;                     // yielding particles deferred to the warm-started return mapping
     int32_t *jc_list_count;
+    // rigid tool (device copy, moved every step) and the PSE conduction switch
+    sph_rigid_tool *rigid;
+    int32_t thermal_pse;
 };
 
 // One logged return mapping: trial von Mises stress, equivalent plastic

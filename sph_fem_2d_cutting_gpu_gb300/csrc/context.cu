@@ -62,6 +62,7 @@ struct sph_ctx {
     bool mlp_on = false;
     int interact_variant = 0;            // launch shape of the fused FP32K neighbour sums
     double *usui_scratch = nullptr;      // per-block partials of sph_eval_usui
+    sph_rigid_tool *rigid_dev = nullptr; // the rigid tool, moved on the device every step (NULL: none)
     // pipelined host I/O: uploads into a free particle buffer and downloads run on
     // their own streams, ordered per buffer by events; a step waits only for the
     // copies into its input and out of its output buffer
@@ -335,6 +336,10 @@ int jc_warm_grid(const sph_ctx *ctx) {
     return std::max(1, std::min(tiles, 4 * std::max(ctx->num_sms, 1)));
 }
 
+// The PSE conduction sum runs in this step (interactions_heat_pse returns at
+// once without workpiece conduction, interactions_gpu.cu:434-435).
+bool pse_active(const sph_ctx *ctx) { return ctx->K.thermal_pse && ctx->K.c.trml_wp.alpha != 0.; }
+
 // The fused step body (everything after the histogram of the current state),
 // reading buf[cur] and writing buf[w].
 int issue_fused_body(sph_ctx *ctx, int64_t &n, int w) {
@@ -350,6 +355,10 @@ int issue_fused_body(sph_ctx *ctx, int64_t &n, int w) {
         launch_fem_half(s, ctx->K, ctx->fem, ctx->tool_dev);
         n += 1;
     }
+    if (pse_active(ctx)) {
+        launch_heat_pse(s, N, ctx->K, ctx->X.offsets, ctx->W, B);
+        n += 1;
+    }
     if (ctx->mlp_on) CK(cudaMemsetAsync(ctx->jc_list_count, 0, sizeof(int32_t), s));
     launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, ctx->seg, ctx->tool_dev, true,
                         ctx->interact_variant);
@@ -363,6 +372,10 @@ int issue_fused_body(sph_ctx *ctx, int64_t &n, int w) {
         launch_fem_rate_update(s, ctx->K, ctx->fem, ctx->seg, ctx->tool_dev);
         launch_tool_move(s, ctx->K, ctx->seg, ctx->fem, ctx->tool_dev, ctx->K.dt, 3, true);
         n += 2;
+    }
+    if (ctx->K.rigid) {
+        launch_rigid_move(s, ctx->K.rigid, ctx->K.dt);
+        n += 1;
     }
     CK(cudaMemsetAsync(ctx->X.counts, 0, sizeof(int32_t) * (size_t)(ctx->K.g.num_cell + 1), s));
     launch_step_tail(s, N, ctx->K, B, ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->X, ctx->W.status, true);
@@ -1263,6 +1276,7 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
         launch_gather_fused(s, N, ctx->F.idx, ctx->K, A, B, ctx->F, ctx->W, ctx->X.hash_next, ctx->tool_dev);
         CK(cudaEventRecord(ev[3], s));
         if (ctx->has_tool) launch_fem_half(s, ctx->K, ctx->fem, ctx->tool_dev);
+        if (pse_active(ctx)) launch_heat_pse(s, N, ctx->K, ctx->X.offsets, ctx->W, B);
         CK(cudaEventRecord(ev[4], s));
         if (ctx->mlp_on) CK(cudaMemsetAsync(ctx->jc_list_count, 0, sizeof(int32_t), s));
         launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, ctx->seg, ctx->tool_dev, true,
@@ -1277,12 +1291,13 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
             launch_fem_rate_update(s, ctx->K, ctx->fem, ctx->seg, ctx->tool_dev);
             launch_tool_move(s, ctx->K, ctx->seg, ctx->fem, ctx->tool_dev, ctx->K.dt, 3, true);
         }
+        if (ctx->K.rigid) launch_rigid_move(s, ctx->K.rigid, ctx->K.dt);
         CK(cudaEventRecord(ev[6], s));
         CK(cudaMemsetAsync(ctx->X.counts, 0, sizeof(int32_t) * (size_t)(ctx->K.g.num_cell + 1), s));
         launch_step_tail(s, N, ctx->K, B, ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->X, ctx->W.status, true);
         CK(cudaEventRecord(ev[7], s));
         CK_LAUNCH();
-        ctx->launches += 8 + (ctx->has_tool ? 3 : 0);
+        ctx->launches += 8 + (ctx->has_tool ? 3 : 0) + (pse_active(ctx) ? 1 : 0) + (ctx->K.rigid ? 1 : 0);
         CK(cudaEventSynchronize(ev[7]));
         for (int k = 0; k < kStages; k++) {
             float ms = 0.f;
@@ -1326,6 +1341,7 @@ int sph_step_staged(sph_ctx *ctx) {
     RUN(sph_material_eos(ctx));
     RUN(sph_corrector_artificial_stress(ctx));
     RUN(sph_interactions_monaghan(ctx));
+    if (ctx->K.thermal_pse) RUN(sph_interactions_heat_pse(ctx));
     RUN(sph_material_stress_rate_jaumann(ctx));
     RUN(sph_contmech_continuity(ctx));
     RUN(sph_contmech_momentum(ctx));
@@ -1337,11 +1353,16 @@ int sph_step_staged(sph_ctx *ctx) {
         RUN(sph_fem_calculate_temp_rate(ctx));
         RUN(sph_fem_calculate_temp(ctx, dt));
     }
+    if (ctx->K.rigid) RUN(sph_material_fric_heat_gen(ctx));
     RUN(sph_plasticity_johnson_cook(ctx));
     if (ctx->has_tool) {
         RUN(sph_segments_update(ctx, dt));
         RUN(sph_tool_update_fem(ctx, dt));
         RUN(sph_compute_contact_forces_fem(ctx));
+    }
+    if (ctx->K.rigid) {
+        RUN(sph_rigid_tool_update(ctx));
+        RUN(sph_compute_contact_forces(ctx));
     }
     RUN(sph_perform_boundary_conditions(ctx));
     RUN(sph_perform_boundary_conditions_thermal(ctx));
@@ -1881,6 +1902,112 @@ int sph_eval_usui(sph_ctx *ctx, double K_usui, double alpha, const double tool_v
     out[1] = mx;
     out[2] = cnt == 0. ? 0. : sm / cnt;
     if (accum_wear) *accum_wear += dt * out[2];
+    return SPH_OK;
+}
+
+
+// ---- rigid (SPH-mode) tool and PSE conduction: leap_frog.cu:99-160 --------------------------------
+int sph_set_rigid_tool(sph_ctx *ctx, const sph_rigid_tool *tool) {
+    REQUIRE_CTX();
+    REQUIRE_SINGLE_CASE();
+    if (!tool) {   // remove it (the allocation stays with the context)
+        if (ctx->K.rigid) {
+            ctx->K.rigid = nullptr;
+            invalidate_graphs(ctx);
+        }
+        return SPH_OK;
+    }
+    if (ctx->has_tool) return fail(ctx, SPH_ERR_STATE, "context has a FEM tool");
+    if (tool->n_seg < 1 || tool->n_seg > SPH_RIGID_MAX_SEG)
+        return fail(ctx, SPH_ERR_INVALID, "rigid tool: 1..5 segments");
+    // tool_gpu.cu:83: a fillet exists exactly when the outline has 5 segments
+    if ((tool->has_fillet != 0) != (tool->n_seg == SPH_RIGID_MAX_SEG))
+        return fail(ctx, SPH_ERR_INVALID, "rigid tool: a fillet goes with 5 segments, and 5 segments with a fillet");
+    if (!ctx->rigid_dev) DALLOC(ctx->rigid_dev, 1);
+    CK(cudaMemcpyAsync(ctx->rigid_dev, tool, sizeof(sph_rigid_tool), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->K.rigid != ctx->rigid_dev) {
+        ctx->K.rigid = ctx->rigid_dev;
+        invalidate_graphs(ctx);
+    }
+    return SPH_OK;
+}
+
+int sph_get_rigid_tool(sph_ctx *ctx, sph_rigid_tool *tool) {
+    REQUIRE_CTX();
+    if (!tool) return SPH_ERR_INVALID;
+    if (!ctx->K.rigid) return fail(ctx, SPH_ERR_STATE, "context has no rigid tool");
+    CK(cudaMemcpyAsync(tool, ctx->K.rigid, sizeof(sph_rigid_tool), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+// tool_gpu.cu:266-305 tool_gpu_update_tool: segments and fillet (tool.cpp:202-212),
+// then the tool particles (update_tool_particles), by the context's time step.
+int sph_rigid_tool_update(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    if (!ctx->K.rigid) return fail(ctx, SPH_ERR_STATE, "context has no rigid tool");
+    launch_rigid_move(ctx->stream, ctx->K.rigid, ctx->K.dt);
+    launch_rigid_move_particles(ctx->stream, ctx->N, CUR(ctx), ctx->K.rigid, ctx->K.dt);
+    ctx->launches += 2;
+    ctx->counts_valid = false;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+// tool_gpu.cu:307-313 compute_contact_forces
+int sph_compute_contact_forces(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    if (!ctx->K.rigid) return fail(ctx, SPH_ERR_STATE, "context has no rigid tool");
+    launch_contact_rigid(ctx->stream, ctx->N, ctx->K, CUR(ctx));
+    ctx->launches++;
+    ctx->counts_valid = false;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+// actions_gpu.cu:955-965 material_fric_heat_gen (off while thermals_wp.eta == 0)
+int sph_material_fric_heat_gen(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    if (!ctx->K.rigid) return fail(ctx, SPH_ERR_STATE, "context has no rigid tool");
+    if (ctx->K.c.trml_wp.eta == 0.) return SPH_OK;
+    launch_fric_heat_rigid(ctx->stream, ctx->N, ctx->K, CUR(ctx));
+    ctx->launches++;
+    ctx->counts_valid = false;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+// types.h:11-13,122-123: the thermal solver of the build, Brookshaw or PSE.  PSE
+// sums over the reference's 5x5 block of cells of edge h, so it needs the
+// reference's cell geometry (cell_factor 1), and is evaluated in FP64.
+int sph_set_thermal_model(sph_ctx *ctx, int32_t model) {
+    REQUIRE_CTX();
+    if (model != SPH_THERMAL_BROOKSHAW && model != SPH_THERMAL_PSE)
+        return fail(ctx, SPH_ERR_INVALID, "unknown thermal model");
+    const int32_t pse = model == SPH_THERMAL_PSE ? 1 : 0;
+    if (pse) {
+        if (ctx->K.precision != SPH_PREC_FP64) return fail(ctx, SPH_ERR_STATE, "PSE conduction needs an FP64 context");
+        if (ctx->grid.cell_factor != 1) return fail(ctx, SPH_ERR_STATE, "PSE conduction needs cells of edge h");
+        if (ctx->K.n_cases > 1) return fail(ctx, SPH_ERR_STATE, "PSE conduction: single-case contexts only");
+    }
+    if (pse != ctx->K.thermal_pse) {
+        ctx->K.thermal_pse = pse;
+        invalidate_graphs(ctx);
+    }
+    return SPH_OK;
+}
+
+// interactions_gpu.cu:434-462 interactions_heat_pse on the current state
+int sph_interactions_heat_pse(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    if (!ctx->K.thermal_pse) return fail(ctx, SPH_ERR_STATE, "thermal model is not PSE");
+    if (ctx->K.c.trml_wp.alpha == 0.) return SPH_OK;
+    launch_build_records(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->F, ctx->W);
+    launch_heat_pse(ctx->stream, ctx->N, ctx->K, ctx->X.offsets, ctx->W, CUR(ctx));
+    ctx->launches += 2;
+    ctx->counts_valid = false;
+    CK_LAUNCH();
     return SPH_OK;
 }
 

@@ -27,6 +27,7 @@
 // from the records, so there is no read/write race.
 #include "async.cuh"
 #include "launch.cuh"
+#include "rigid.cuh"
 
 namespace sphfem {
 
@@ -48,6 +49,16 @@ struct KahanF {
         s = t;
     }
 };
+
+// A particle blanked before the step skips the neighbour sums, the corrector and
+// the return mapping, but the rigid tool's do_material_fric_heat_gen
+// (actions_gpu.cu:316-343) has no blanked test and still heats it.
+__device__ __forceinline__ void rigid_heat_blanked(int k, const KConsts &K, const SortedFields &B) {
+    if (!K.rigid || K.c.trml_wp.eta == 0. || flag_nonzero(B.tool_particle[k])) return;
+    double T = B.T[k];
+    rigid_fric_heat_one(K, K.dt, K.rigid->vel, B.vel[k], B.ft[k], B.n[k], T);
+    if (T != B.T[k]) B.T[k] = T;
+}
 
 // ---- per-particle epilogue shared by both precisions (fused mode) ---------------------
 // vd, sd (= S_der), vt (= vel_t from viscosity), xt (= pos_t from XSPH), T_t.
@@ -72,6 +83,9 @@ __device__ __forceinline__ void fused_epilogue(int k, const KConsts &K, const So
         vel_t.y = vt.y + (((sd.z + sd.w) + fc.y / mass) + ft.y / mass);
         pos_t.x = xt.x + vel_pred.x;                                  // actions_gpu.cu:673-687
         pos_t.y = xt.y + vel_pred.y;
+    } else if (K.thermal_pse) {   // PSE build: tool particles leave the sums unwritten
+        vel_t = B.vel_t[k];
+        pos_t = B.pos_t[k];
     } else {
         vel_t = vt;
         pos_t = xt;
@@ -99,6 +113,8 @@ __device__ __forceinline__ void fused_epilogue(int k, const KConsts &K, const So
     // friction heat (actions_gpu.cu:345-420), tool runs only
     if (K.has_tool) st |= fric_heat_one(K, K.dt, tool->vel, vel, B.ft[k], B.n[k], B.fc[k], rho, B.eps_pl[k], B.on_seg[k],
                                         seg.n, T, blanked, seg.fric_heat);
+    else if (K.rigid && !is_tool && K.c.trml_wp.eta != 0.)   // actions_gpu.cu:316-343
+        rigid_fric_heat_one(K, dt, K.rigid->vel, vel, B.ft[k], B.n[k], T);
     // return mapping (actions_gpu.cu:689-754)
     if (K.c.plastic && !is_tool && blanked != 1.) {
         double eps_pl = B.eps_pl[k], eps_pl_dot = B.eps_pl_dot[k];
@@ -182,6 +198,10 @@ __device__ __forceinline__ void fused_epilogue32(int k, const KConsts &K, const 
             T = (float)Td;
             blanked = flag_is_one(bl);
         }
+    } else if (K.rigid && !is_tool && K.c.trml_wp.eta != 0.) {   // actions_gpu.cu:316-343
+        double Td = (double)T;
+        rigid_fric_heat_one(K, dt, K.rigid->vel, make_double2(vel.x, vel.y), B.ft[k], B.n[k], Td);
+        T = (float)Td;
     }
     if (K.c.plastic && !is_tool && !blanked) {   // return mapping (actions_gpu.cu:689-754)
         const JcF32 &j = K.f.jc;
@@ -225,15 +245,19 @@ __global__ void __launch_bounds__(kBlock) k_interact64(int N, KConsts K, const i
     if (k >= N) return;
     const dbl4 i3 = rec[4 * k + 3];
     const int fi = (int)__double_as_longlong(i3.w);
-    if (fi & kFlagBlanked) return;
+    if (fi & kFlagBlanked) {
+        if (kFused) rigid_heat_blanked(k, K, B);
+        return;
+    }
     const bool tool_i = (fi & kFlagTool) != 0;
+    const bool pse_tool = K.thermal_pse && tool_i;   // PSE build: tool particles return at once
     const dbl4 i0 = rec[4 * k + 0], i1 = rec[4 * k + 1], i2 = rec[4 * k + 2];
     const double xi = i0.x, yi = i0.y, vix = i0.z, viy = i0.w;
     const double sAi = i1.x, sBi = i1.y, sCi = i1.z, Rxxi = i1.w;
     const double Rxyi = i2.x, Ryyi = i2.y, hi = i2.z, rhoi = i2.w;
     const double ci = i3.x, Ti = i3.z;
     const double thermal_alpha = (!tool_i) ? K.c.trml_wp.alpha : K.c.trml_tool_sph.alpha;
-    const bool thermal = thermal_alpha != 0.;
+    const bool thermal = thermal_alpha != 0. && !K.thermal_pse;   // Brookshaw build only
     const double h1 = 1 / hi;
     const double fourh2 = 4 * hi * hi;
     const double fac = kPiFac * h1 * h1;
@@ -245,7 +269,7 @@ __global__ void __launch_bounds__(kBlock) k_interact64(int N, KConsts K, const i
     __shared__ int s_list[kPairChunk][kBlock];
     int ii = 0, hi_i = 0, lo_j = 0, hi_j = 0, jc = 0, j1 = 0;
     bool done = true;
-    if (hash >= 0 && hash < g.num_cell) {
+    if (hash >= 0 && hash < g.num_cell && !pse_tool) {
         const int gi = hash / g.ny, gj = hash - gi * g.ny, R = g.stencil;
         ii = max(gi - R, 0);
         hi_i = min(gi + R + 1, g.nx);
@@ -345,6 +369,7 @@ __global__ void __launch_bounds__(kBlock) k_interact64(int N, KConsts K, const i
     const double2 xt = make_double2(xs * a.xt0, xs * a.xt1);
     const double T_t = thermal_alpha * (2.0 * a.tl);
     if (!kFused) {
+        if (pse_tool) return;
         F.S_der[k] = sd;
         F.v_der[k] = vd;
         B.pos_t[k] = xt;
@@ -438,7 +463,10 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
     if (k >= N) return;
     const float4 i0 = rec[4 * k + 0];
     const int fi = __float_as_int(i0.z);
-    if (fi & kFlagBlanked) return;
+    if (fi & kFlagBlanked) {
+        if (kFused) rigid_heat_blanked(k, K, B);
+        return;
+    }
     const bool tool_i = (fi & kFlagTool) != 0;
     const float4 i1 = rec[4 * k + 1], i2 = rec[4 * k + 2], i3 = rec[4 * k + 3];
     const float xri = i0.x, yri = i0.y, hi = i0.w;
@@ -647,6 +675,52 @@ static void launch_i32(cudaStream_t s, int N, const KConsts &K, const int32_t *o
     }
     k_interact32<true, kB, kMinB, kStaged><<<div_up(N, kB), kB, smem, s>>>(N, K, offsets, W.rec32, B, F, seg, tool,
                                                                            W.secant_iters, W.status, cap);
+}
+
+// ---- interactions_gpu.cu:84-140 do_interactions_heat_pse (FP64) --------------------------
+// T_t = alpha * sum_j (T_j - T_i) W2(r_ij, h_i) m / rho_j over every particle of
+// the 5x5 block of cells of edge h around the particle's cell (no support
+// cut-off, blanked neighbours included), W2 = 4 / (h^4 pi) exp(-|r|^2 / h^2)
+// (kernels.cuh:67-84).  Reads the predicted state from the FP64 records; the
+// block's columns are contiguous slot ranges as in the neighbour sums.
+__global__ void __launch_bounds__(kBlock) k_heat_pse64(int N, KConsts K, const int32_t *__restrict__ offsets,
+                                                       const dbl4 *__restrict__ rec,
+                                                       const int32_t *__restrict__ hashes, double *__restrict__ T_t) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const dbl4 i3 = rec[4 * k + 3];
+    const int fi = (int)__double_as_longlong(i3.w);
+    if (fi & kFlagBlanked) return;
+    const dbl4 i0 = rec[4 * k + 0], i2 = rec[4 * k + 2];
+    const double xi = i0.x, yi = i0.y, hi = i2.z, Ti = i3.z;
+    const double alpha = (fi & kFlagTool) ? K.c.trml_tool_sph.alpha : K.c.trml_wp.alpha;
+    const double mass = K.c.phys.mass;
+    const double h2 = hi * hi, h4 = h2 * h2;
+    const double c = 4. / (h4 * kRigidPi);
+    double sum = 0.;
+    const int hash = hashes[k];
+    const sph_geom_constants &g = K.g;
+    if (hash >= 0 && hash < g.num_cell) {
+        const int gi = hash / g.ny, gj = hash - gi * g.ny;
+        const int lo_i = max(gi - 2, 0), hi_i = min(gi + 3, g.nx);
+        const int lo_j = max(gj - 2, 0), hi_j = min(gj + 3, g.ny);
+        for (int ii = lo_i; ii < hi_i; ii++) {
+            const int j1 = __ldg(offsets + ii * g.ny + hi_j);
+            for (int j = __ldg(offsets + ii * g.ny + lo_j); j < j1; j++) {
+                const dbl4 n0 = rec[4 * j + 0];
+                const double xij = xi - n0.x, yij = yi - n0.y;
+                const double xx = sqrt(xij * xij + yij * yij);
+                const double w2 = c * exp(-xx * xx / h2);
+                sum += (rec[4 * j + 3].z - Ti) * w2 * mass / rec[4 * j + 2].w;
+            }
+        }
+    }
+    T_t[k] = alpha * sum;
+}
+
+void launch_heat_pse(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const StepScratch &W,
+                     const SortedFields &B) {
+    k_heat_pse64<<<div_up(N, kBlock), kBlock, 0, s>>>(N, K, offsets, W.rec64, B.hash, B.T_t);
 }
 
 void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const SortedFields &B,

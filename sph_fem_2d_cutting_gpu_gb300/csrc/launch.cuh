@@ -25,6 +25,8 @@ void launch_build_records(cudaStream_t s, int N, const KConsts &K, const SortedF
 void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const SortedFields &B,
                          const FixedFields &F, const StepScratch &W, const SegDev &seg, const ToolDev *tool,
                          bool fused, int variant = 0);
+void launch_heat_pse(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const StepScratch &W,
+                     const SortedFields &B);
 int interact_variant_count();
 void interact_variant_shape(int v, int *block, int *min_blocks, int *staged);
 
@@ -49,6 +51,10 @@ void launch_invalidate(cudaStream_t s, int N, const SortedFields &A, uint32_t *s
 void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
                       const ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
                       bool next_hash);
+void launch_rigid_move(cudaStream_t s, sph_rigid_tool *t, double dt);
+void launch_rigid_move_particles(cudaStream_t s, int N, const SortedFields &A, const sph_rigid_tool *t, double dt);
+void launch_contact_rigid(cudaStream_t s, int N, const KConsts &K, const SortedFields &A);
+void launch_fric_heat_rigid(cudaStream_t s, int N, const KConsts &K, const SortedFields &A);
 int reduce_blocks();
 void launch_usui(cudaStream_t s, int N, const SortedFields &A, double K_usui, double alpha, double vtx, double vty,
                  double *out);

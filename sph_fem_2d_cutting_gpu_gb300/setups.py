@@ -11,6 +11,10 @@ Workloads:
   * ``aisi1045_cut`` -- AISI 1045 cut, 1600 x 400 particles, dx = 2.5 um, tool
                         mesh of about 20,000 nodes (rake -6, clearance 5 deg,
                         edge radius 20 um), 120 m/min, 100 um.
+  * ``ref_cut``      -- the reference's SPH-tool cut (setup_ref_cut,
+                        benchmarks.cpp:247-530): Ti6Al4V, workpiece 1.95 mm
+                        long and 3 x feed high, rigid tool with optional
+                        edge radius, sampled with thermal-only tool particles.
   * ``batched_sweep`` -- independent AISI 1045 cuts of uneven sizes (particle
                         counts log-uniform in [20k, 300k], height 0.5 mm,
                         speed U(30, 300) m/min, uncut chip thickness
@@ -27,6 +31,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import abi
+from .rigid_tool import RigidTool
 from .tool_mesh import mesh_tool
 
 MPMIN_TO_CMUS = 1.0 / 60.0 * 1e-4      # m/min -> cm/us
@@ -111,6 +116,7 @@ class Case:
     feed: float = 0.0
     steps: int = 0
     info: dict = field(default_factory=dict)
+    rigid: RigidTool | None = None     # rigid (SPH-mode) tool instead of a FEM tool
 
     def tool_struct(self):
         if self.tool_mesh is None:
@@ -301,3 +307,97 @@ def moved(case: Case, shift_x: float, shift_y: float = 0.0) -> Case:
     m["tl"] = (case.tool_mesh["tl"][0] + shift_x, case.tool_mesh["tl"][1] + shift_y)
     out.tool_mesh = m
     return out
+
+
+# Ti6Al4V of setup_ref_cut (benchmarks.cpp:263-287, Johnson 85)
+TI64_REF = Material(E=1.1, nu=0.35, rho0=4.429998, A=0.0085200, B=0.0033890, C=0.02754, n=0.148, m=0.5961,
+                    Tmelt=1836.0, cp=580e-8, k=7.3e-13)
+
+
+def ref_cut(ny: int = 10, rake: float = 0.0, clear: float = 7.0, chamfer: float = 5e-4, speed: float = 0.0,
+            feed: float = 0.002, length: float = 0.195, sample_tool: bool = True, preload_dx: float = 0.0,
+            steps: int = 0, cell_factor: int = 1, stencil: int = 2) -> Case:
+    """setup_ref_cut (benchmarks.cpp:247-530): Ti6Al4V workpiece of ny rows and
+    3 x feed height (length 1.95 mm in the reference; shorter here for small
+    cases), a rigid tool of rake / clearance angle (degrees) and edge radius
+    `chamfer` placed at the workpiece front and the target feed, and the tool
+    sampled with particles that take part in heat conduction only.  speed in
+    cm/us (0: the reference's 500 m/min).  preload_dx moves the tool that many
+    particle spacings into the workpiece (0 in the reference)."""
+    mat = TI64_REF
+    hi_y, lo_x = 0.060, 0.005
+    hi_x = lo_x + length
+    lo_y = hi_y - 3 * feed
+    dy = (hi_y - lo_y) / (ny - 1)
+    dx = dy
+    nx = int((hi_x - lo_x) / dx)
+    hdx = 1.5
+    c = make_constants(mat, dx, hdx, mu=0.35)
+    rho_tool = 15.25
+    c.phys.mass_tool = dx * dx * rho_tool
+    c.joco.tanh_a, c.joco.tanh_b, c.joco.tanh_c, c.joco.tanh_d = 1.1, 0.4, 12.0, 1.0
+    # tool thermal constants (benchmarks.cpp:303-309); the same for the SPH tool's
+    # conduction and for the thermal boundary switch
+    for t in (c.trml_tool, c.trml_tool_sph):
+        t.cp, t.tq, t.k, t.eta = 292e-8, 0.0, 88e-13, 0.0
+        t.alpha = t.k / (rho_tool * t.cp)
+        t.T_init = mat.Tref
+    c.tool.contact_alpha = 0.075           # benchmarks.cpp:414
+    c.tool.slave_mass = c.phys.mass
+    # workpiece lattice and its fixed boundaries (benchmarks.cpp:326-374)
+    i, j = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    pos = np.stack([i.ravel() * dx + lo_x, j.ravel() * dx + lo_y], 1)
+    min_x, min_y = pos.min(0)
+    max_x, max_y = pos.max(0)
+    fixed = pos[:, 1] < min_y + 0.5 * dx
+    fixed |= (pos[:, 0] < min_x + dx / 2) & (pos[:, 1] < min_y + 0.5 * (hi_y - lo_y))
+    fixed |= pos[:, 0] > max_x - dx
+    vel_tool = 83.333328 * 1e-5 if speed == 0.0 else speed
+    # tool from Ruettimann's FEM simulations, moved to the workpiece front and the
+    # target feed (benchmarks.cpp:378-412)
+    nudge = 0.004
+    tl = (-0.05 + nudge, 0.0986074)
+    tool = RigidTool.from_angles(tl, -0.0086824 - -0.05, 0.0986074 - 0.0555074, rake, clear, chamfer, 0.35)
+    distance = tool.front - lo_x
+    tool.vel = (vel_tool, 0.0)
+    tool.update(-(distance / vel_tool))
+    current_feed = hi_y - tool.low()
+    correction_time = abs(current_feed - feed) / vel_tool
+    sign = 1.0 if current_feed > feed else -1.0
+    tool.vel = (0.0, vel_tool)
+    tool.update(correction_time * sign)
+    tool.vel = (vel_tool, 0.0)
+    if preload_dx:
+        tool.update(preload_dx * dx / vel_tool)
+    n_wp = nx * ny
+    # tool particles (benchmarks.cpp:418-450)
+    tpos = tool.sample(dx) if sample_tool else np.zeros((0, 2))
+    n_tool = len(tpos)
+    N = n_wp + n_tool
+    P = abi.empty_particles(N)
+    P["pos"][:n_wp] = pos
+    P["pos"][n_wp:] = tpos
+    P["rho"][:n_wp] = mat.rho0
+    P["rho"][n_wp:] = rho_tool
+    P["h"][:] = hdx * dx
+    P["T"][:] = mat.Tref
+    P["fixed"][:n_wp] = fixed.astype(np.float64)
+    if n_tool:
+        tfix = (tpos[:, 0] < tpos[:, 0].min() + dx / 2) | (tpos[:, 1] > tpos[:, 1].max() - dx / 2)
+        P["fixed"][n_wp:] = tfix.astype(np.float64)
+    P["tool_particle"][n_wp:] = 1.0
+    P["on_seg"][:] = -1
+    # domain (benchmarks.cpp:456-487)
+    allpos = P["pos"]
+    bbmin = allpos.min(0) - 1e-8
+    bbmax = allpos.max(0) + 1e-8
+    tx0, tx1, ty0, ty1 = tool.safe_bb(1e-3)
+    bbmin = np.minimum(bbmin, [tx0, ty0])
+    bbmax = np.array([max(bbmax[0], tx1) + 10 * dx, max(bbmax[1], ty1)])
+    bbmax[1] = max(bbmax[1], hi_y + hi_x - lo_x)
+    g = grid_params(tuple(bbmin), tuple(bbmax), hdx * dx, cell_factor, stencil)
+    dt = 0.32 * hdx * dx / (math.sqrt(c.phys.K / c.phys.rho0) + math.sqrt(vel_tool))   # benchmarks.cpp:518
+    return Case("ref_cut", c, g, P, N, dt, tool_speed=vel_tool, feed=feed, steps=steps,
+                info=dict(nx=nx, ny=ny, dx=dx, hdx=hdx, n_workpiece=n_wp, n_tool=n_tool, rake=rake, clear=clear,
+                          chamfer=chamfer, lo_x=lo_x, hi_y=hi_y, usui_K=7.8 / 100, usui_alpha=2500.0),
+                rigid=tool)

@@ -46,6 +46,8 @@ class Solver:
                 self.place_tool()
             else:   # tool already placed (setups.placed): cutting velocity only
                 self.set_vel(case.tool_speed, 0.0)
+        if case.rigid is not None:
+            self.set_rigid_tool(case.rigid.to_struct())
 
     # ---- plumbing -------------------------------------------------------------------------
     def _ck(self, r: int, what: str):
@@ -203,6 +205,19 @@ class Solver:
         self.set_vel(v, 0.0)
 
     # ---- the step and its stages -------------------------------------------------------------
+    # ---- rigid (SPH-mode) tool and thermal model (leap_frog.cu:99-160) -------------------------
+    def set_rigid_tool(self, tool: abi.RigidTool | None):
+        self._ck(self.lib.sph_set_rigid_tool(self.ctx, C.byref(tool) if tool is not None else None),
+                 "sph_set_rigid_tool")
+
+    def rigid_tool(self) -> abi.RigidTool:
+        t = abi.RigidTool()
+        self._ck(self.lib.sph_get_rigid_tool(self.ctx, C.byref(t)), "sph_get_rigid_tool")
+        return t
+
+    def set_thermal_model(self, model: int):
+        self._ck(self.lib.sph_set_thermal_model(self.ctx, int(model)), "sph_set_thermal_model")
+
     def step(self, n: int = 1):
         """leap_frog::step (fused kernels, CUDA-graph replay)."""
         if n == 1:
