@@ -9,9 +9,14 @@
 //
 // Parity pins: cubic_spline and the Johnson-Cook secant return mapping are
 // checked against the reference's own kernels.cuh / plasticity.cuh compiled
-// on the host (oracle/ref_pin.cpp, golden vectors in tests/golden/).  The rest
-// of the path is pinned by analytic known-answer tests only; the reference
-// has no tests, golden vectors or fixtures of its own.
+// on the host (oracle/ref_pin.cpp, golden vectors in tests/golden/); the
+// rigid tool's outline, fillet, placement and particle sampling (the host
+// set-up the rigid-tool functions below consume) against the reference's own
+// tool.cpp / geometric_primitives.cpp (oracle/ref_tool_pin.cpp).  The device
+// kernels of tool_gpu.cu cannot be built for the host (kernel-launch syntax),
+// so the rigid contact below, like the rest of the path, is pinned by analytic
+// known-answer tests only; the reference has no tests, golden vectors or
+// fixtures of its own.
 //
 // Semantics kept from the reference on purpose:
 //  - float narrowings: sqrtf/fmaxf/fminf of double arguments round the

@@ -229,3 +229,23 @@ def _points_and_fillet(tl, tr, br, bl, r: float):
     t1 = _myatan2(p[1] - trc[1], p[0] - trc[0])
     t2 = _myatan2(p[1] - blc[1], p[0] - blc[0])
     return [tl, tr, trc, blc, bl], Fillet(r, t1, t2, p)
+
+
+def place(tool: RigidTool, lo_x: float, hi_y: float, feed: float, vel_tool: float, preload_time: float = 0.0):
+    """setup_ref_cut's placement (benchmarks.cpp:388-412): move the tool front
+    to the workpiece front lo_x, then vertically until its lowest point is
+    `feed` below the workpiece top hi_y; leave it moving at (vel_tool, 0).
+    preload_time > 0 moves it further along x (0 in the reference)."""
+    distance = tool.front - lo_x
+    time = distance / vel_tool
+    tool.vel = (vel_tool, 0.0)
+    tool.update(-time)
+    current_feed = hi_y - tool.low()
+    correction_time = abs(current_feed - feed) / vel_tool
+    sign = 1.0 if current_feed > feed else -1.0
+    tool.vel = (0.0, vel_tool)
+    tool.update(correction_time * sign)
+    tool.vel = (vel_tool, 0.0)
+    if preload_time != 0.0:
+        tool.update(preload_time)
+    return tool

@@ -32,6 +32,7 @@ import numpy as np
 
 from . import abi
 from .rigid_tool import RigidTool
+from .rigid_tool import place as place_rigid
 from .tool_mesh import mesh_tool
 
 MPMIN_TO_CMUS = 1.0 / 60.0 * 1e-4      # m/min -> cm/us
@@ -309,6 +310,11 @@ def moved(case: Case, shift_x: float, shift_y: float = 0.0) -> Case:
     return out
 
 
+# tool of setup_ref_cut, from Ruettimann's FEM simulations (benchmarks.cpp:384-390)
+REF_CUT_TOOL_TL = (-0.05 + 0.004, 0.0986074)
+REF_CUT_TOOL_LENGTH = -0.0086824 - -0.05
+REF_CUT_TOOL_HEIGHT = 0.0986074 - 0.0555074
+
 # Ti6Al4V of setup_ref_cut (benchmarks.cpp:263-287, Johnson 85)
 TI64_REF = Material(E=1.1, nu=0.35, rho0=4.429998, A=0.0085200, B=0.0033890, C=0.02754, n=0.148, m=0.5961,
                     Tmelt=1836.0, cp=580e-8, k=7.3e-13)
@@ -355,20 +361,9 @@ def ref_cut(ny: int = 10, rake: float = 0.0, clear: float = 7.0, chamfer: float 
     vel_tool = 83.333328 * 1e-5 if speed == 0.0 else speed
     # tool from Ruettimann's FEM simulations, moved to the workpiece front and the
     # target feed (benchmarks.cpp:378-412)
-    nudge = 0.004
-    tl = (-0.05 + nudge, 0.0986074)
-    tool = RigidTool.from_angles(tl, -0.0086824 - -0.05, 0.0986074 - 0.0555074, rake, clear, chamfer, 0.35)
-    distance = tool.front - lo_x
-    tool.vel = (vel_tool, 0.0)
-    tool.update(-(distance / vel_tool))
-    current_feed = hi_y - tool.low()
-    correction_time = abs(current_feed - feed) / vel_tool
-    sign = 1.0 if current_feed > feed else -1.0
-    tool.vel = (0.0, vel_tool)
-    tool.update(correction_time * sign)
-    tool.vel = (vel_tool, 0.0)
-    if preload_dx:
-        tool.update(preload_dx * dx / vel_tool)
+    tl = REF_CUT_TOOL_TL
+    tool = RigidTool.from_angles(tl, REF_CUT_TOOL_LENGTH, REF_CUT_TOOL_HEIGHT, rake, clear, chamfer, 0.35)
+    place_rigid(tool, lo_x, hi_y, feed, vel_tool, preload_dx * dx / vel_tool)
     n_wp = nx * ny
     # tool particles (benchmarks.cpp:418-450)
     tpos = tool.sample(dx) if sample_tool else np.zeros((0, 2))

@@ -247,3 +247,39 @@ def test_ref_cut_setup_matches_reference_placement():
         assert P["fixed"][tp].sum() > 0
         assert abs(t.vel[0] - 83.333328e-5) < 1e-18 and t.vel[1] == 0.0
         assert Line.through((0.0, 0.0), (0.0, 1.0)).vertical
+
+
+# ---- pinned to the reference's own tool.cpp / geometric_primitives.cpp ------------------------------
+GOLDEN_TOOL = __import__("pathlib").Path(__file__).resolve().parent / "golden" / "ref_tool_pin.npz"
+
+
+def test_tool_geometry_matches_reference_golden():
+    """RigidTool.from_angles + place + sample reproduce the reference's host
+    geometry bit for bit (fixture from tests/golden/make_tool_golden.py)."""
+    from sph_fem_2d_cutting_gpu_gb300.rigid_tool import place
+    g = np.load(GOLDEN_TOOL)
+    rows = g["inputs"]
+    for k, r in enumerate(rows):
+        tlx, tly, length, height, rake, clear, rad, mu, vel, lo_x, hi_y, feed, dx, pre = r
+        t = RigidTool.from_angles((tlx, tly), length, height, rake, clear, rad, mu)
+        place(t, lo_x, hi_y, feed, vel, pre)
+        segs = np.array([[*s.left, *s.right, *s.n, s.line.a, s.line.b, 1.0 if s.line.vertical else 0.0]
+                         for s in t.segments])
+        ref = g[f"segs_{k}"]
+        assert segs.shape == ref.shape, k
+        # -0.0 and 0.0 print the same way; compare values
+        assert np.array_equal(segs, ref), (k, np.argwhere(segs != ref))
+        fr = g[f"fillet_{k}"]
+        if t.fillet is None:
+            assert np.isnan(fr).all(), k
+        else:
+            f = t.fillet
+            assert np.array_equal([f.p[0], f.p[1], f.r, f.t1, f.t2], fr), k
+        assert np.array_equal([t.low(), t.front], g[f"scalars_{k}"]), k
+        assert np.array_equal(t.safe_bb(0.1 * dx), g[f"bb_{k}"]), k
+        smp = t.sample(dx)
+        assert np.array_equal(smp, g[f"samples_{k}"]), (k, len(smp), len(g[f"samples_{k}"]))
+        # the packed struct the device moves carries the same outline
+        st = t.to_struct()
+        for i, s in enumerate(t.segments):
+            assert (st.la[i], st.lb[i]) == (s.line.a, s.line.b)
