@@ -236,6 +236,65 @@ def run_batched(args, local, max_over_ranks, barrier):
     return out
 
 
+def run_rigid(args, local):
+    """The reference's SPH-tool cut (setup_ref_cut with mfree_gpu.cpp's default
+    arguments: rake 0, clearance 4.5 deg, edge radius 3.5 um, uncut chip 100 um,
+    300 in the reference's speed unit) at ny = 30 rows -- the reference's own
+    size -- and at larger ny: leap_frog::step(particles, grid) with the rigid
+    tool, the Brookshaw build, FP64 and FP32K, plus the PSE build in FP64; the
+    CPU oracle's whole-step time beside each size."""
+    import ctypes as C
+
+    import torch
+
+    from sph_fem_2d_cutting_gpu_gb300 import abi, setups
+    from sph_fem_2d_cutting_gpu_gb300.solver import Solver
+    from oracle.oracle import OracleSim, num_threads
+
+    speed = 83.333328e-5 / 200 * 300
+    rows = []
+    for ny in args.rigid_ny:
+        case = setups.ref_cut(ny=ny, rake=0.0, clear=4.5, chamfer=0.00035, speed=speed, feed=0.01)
+        row = {"ny": ny, "particles": case.N, "workpiece": case.info["n_workpiece"], "tool": case.info["n_tool"]}
+        for name, prec, pse in (("fp64", abi.SPH_PREC_FP64, False), ("fp32k", abi.SPH_PREC_FP32K, False),
+                                ("fp64_pse", abi.SPH_PREC_FP64, True)):
+            s = Solver(case, prec, device=local)
+            if pse:
+                s.set_thermal_model(abi.SPH_THERMAL_PSE)
+            sp = C.c_void_p()
+            s.lib.sph_get_stream(s.ctx, C.byref(sp))
+            ext = torch.cuda.ExternalStream(sp.value, device=torch.device("cuda", local))
+            s.step(args.warmup)
+            s.sync()
+            n0 = s.launch_count()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            s.step(args.steps)
+            e1.record(ext)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            row[name] = {"ms_per_step": ms, "value": case.N / (ms * 1e-3),
+                         "launches_per_step": (s.launch_count() - n0) / args.steps, "status": s.status()}
+            s.close()
+        if not args.no_cpu:
+            o = OracleSim(case.constants, case.grid, case.particles, case.dt, rigid=case.rigid.to_struct())
+            o.step()
+            t0, n = time.perf_counter(), 0
+            while n < 1 or (time.perf_counter() - t0 < args.cpu_seconds / 4 and n < 200):
+                o.step()
+                n += 1
+            el = time.perf_counter() - t0
+            row["cpu_oracle"] = {"value": case.N * n / el, "ms_per_step": 1e3 * el / n, "steps": n,
+                                 "cores": num_threads()}
+            row["fp64_vs_cpu"] = row["cpu_oracle"]["ms_per_step"] / row["fp64"]["ms_per_step"]
+        rows.append(row)
+        torch.cuda.empty_cache()
+    return {"unit": UNIT, "rows": rows,
+            "workload": "setup_ref_cut (benchmarks.cpp:247-530) with mfree_gpu.cpp's default arguments: Ti6Al4V, "
+                        "workpiece 1.95 mm x 0.3 mm, rigid tool (rake 0, clearance 4.5 deg, r 3.5 um) sampled "
+                        "with thermal tool particles, 1.25e-3 cm/us; ny rows (30: the reference's size)"}
+
+
 def run_accuracy(case, mlp, steps, every, local):
     """Cutting force (sum of fc + ft) and peak temperature of the FP32K form, with
     and without the warm start, against the plain FP64 form over `steps` steps of
@@ -574,6 +633,10 @@ def run_product(args):
     learned_line = None
     if args.learned_records > 0 and rank == 0:
         learned_line = run_learned(args, local)
+    rigid_line = None
+    if args.rigid_ny and rank == 0:
+        rigid_line = run_rigid(args, local)
+        torch.cuda.empty_cache()
 
     if rank != 0:
         if dist is not None:
@@ -622,6 +685,8 @@ def run_product(args):
         line["batched_sweep"] = batched
     if learned_line is not None:
         line["learned_warm_start"] = learned_line
+    if rigid_line is not None:
+        line["rigid_tool_cut"] = rigid_line
     if not args.no_cpu:
         v, cores, n, el = cpu_sample(case, max_seconds=args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -658,6 +723,8 @@ def main():
     ap.add_argument("--cell-factor", type=int, default=2, help="micro workload: cell edge in h")
     ap.add_argument("--no-alt-geometry", action="store_true", help="skip the cells-of-h micro line")
     ap.add_argument("--stencil", type=int, default=1, help="micro workload: stencil half-width in cells")
+    ap.add_argument("--rigid-ny", type=int, nargs="*", default=[30, 240],
+                    help="rows of the rigid-tool cut sizes to time (none: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
