@@ -236,6 +236,59 @@ def run_batched(args, local, max_over_ranks, barrier):
     return out
 
 
+def run_small_cut(args, local):
+    """The small plain-method case (Ti6Al4V cut, 200 x 60 = 12,000 particles, FEM
+    tool of about 2,000 nodes, 70 m/min, 80 um): per-step time of the fused,
+    graph-replayed step in FP64 and FP32K, and the CPU oracle's step beside it.
+    At this size the step is latency- and launch-bound, not HBM-bound."""
+    import ctypes as C
+
+    import torch
+
+    from sph_fem_2d_cutting_gpu_gb300 import abi, setups
+    from sph_fem_2d_cutting_gpu_gb300.solver import Solver
+    from oracle.oracle import OracleSim, num_threads
+
+    case = setups.ti64_cut()
+    row = {"particles": case.N, "fem_nodes": case.info["nodes"]}
+    for name, prec in (("fp64", abi.SPH_PREC_FP64), ("fp32k", abi.SPH_PREC_FP32K)):
+        s = Solver(case, prec, device=local)
+        sp = C.c_void_p()
+        s.lib.sph_get_stream(s.ctx, C.byref(sp))
+        ext = torch.cuda.ExternalStream(sp.value, device=torch.device("cuda", local))
+        s.step(args.warmup)
+        s.sync()
+        n0 = s.launch_count()
+        steps = max(args.steps, 50)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        s.step(steps)
+        e1.record(ext)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        row[name] = {"ms_per_step": ms, "value": case.N / (ms * 1e-3),
+                     "launches_per_step": (s.launch_count() - n0) / steps, "status": s.status()}
+        if prec == abi.SPH_PREC_FP64 and not args.no_cpu:
+            P = s.download()
+            ts = s.tool_state()
+            tool = dict(segments=s.segments(), fem=s.fem(), state=ts, n_cut_colors=ts.n_cut_colors)
+            o = OracleSim(case.constants, case.grid, P, case.dt, tool=tool)
+            o.step()
+            t0, n = time.perf_counter(), 0
+            while n < 1 or (time.perf_counter() - t0 < 2.0 and n < 500):
+                o.step()
+                n += 1
+            el = time.perf_counter() - t0
+            row["cpu_oracle"] = {"value": case.N * n / el, "ms_per_step": 1e3 * el / n, "steps": n,
+                                 "cores": num_threads()}
+        s.close()
+    if "cpu_oracle" in row:
+        row["fp64_vs_cpu"] = row["cpu_oracle"]["ms_per_step"] / row["fp64"]["ms_per_step"]
+    row["workload"] = ("Ti6Al4V orthogonal cut, 200 x 60 particles (dx 5 um, h 1.7 dx), FEM tool of about 2,000 "
+                       "nodes (rake 0, clearance 7 deg, r 5 um), 70 m/min, uncut chip 80 um")
+    return row
+
+
 def run_rigid(args, local):
     """The reference's SPH-tool cut (setup_ref_cut with mfree_gpu.cpp's default
     arguments: rake 0, clearance 4.5 deg, edge radius 3.5 um, uncut chip 100 um,
@@ -633,6 +686,10 @@ def run_product(args):
     learned_line = None
     if args.learned_records > 0 and rank == 0:
         learned_line = run_learned(args, local)
+    small_line = None
+    if not args.no_small and rank == 0:
+        small_line = run_small_cut(args, local)
+        torch.cuda.empty_cache()
     rigid_line = None
     if args.rigid_ny and rank == 0:
         rigid_line = run_rigid(args, local)
@@ -687,6 +744,8 @@ def run_product(args):
         line["learned_warm_start"] = learned_line
     if rigid_line is not None:
         line["rigid_tool_cut"] = rigid_line
+    if small_line is not None:
+        line["ti64_cut_small"] = small_line
     if not args.no_cpu:
         v, cores, n, el = cpu_sample(case, max_seconds=args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -723,6 +782,7 @@ def main():
     ap.add_argument("--cell-factor", type=int, default=2, help="micro workload: cell edge in h")
     ap.add_argument("--no-alt-geometry", action="store_true", help="skip the cells-of-h micro line")
     ap.add_argument("--stencil", type=int, default=1, help="micro workload: stencil half-width in cells")
+    ap.add_argument("--no-small", action="store_true", help="skip the 12,000-particle Ti6Al4V cut line")
     ap.add_argument("--rigid-ny", type=int, nargs="*", default=[30, 240],
                     help="rows of the rigid-tool cut sizes to time (none: skip)")
     args = ap.parse_args()

@@ -532,6 +532,9 @@ void launch_invalidate(cudaStream_t s, int N, const SortedFields &A, uint32_t *s
 void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
                       const ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
                       bool next_hash) {
+    const int tb = fp64_block(N);   // the contact search is FP64 work: spread small systems over all SMs
+#undef GRID
+#define GRID div_up(N, tb), tb, 0, s
     if (K.has_tool) {
         if (next_hash) k_step_tail<1, true><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
         else k_step_tail<1, false><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
@@ -543,6 +546,8 @@ void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedField
         else k_step_tail<0, false><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
     }
 }
+#undef GRID
+#define GRID div_up(N, kBlock), kBlock, 0, s
 void launch_rigid_move(cudaStream_t s, sph_rigid_tool *t, double dt) { k_rigid_move<<<1, 32, 0, s>>>(t, dt); }
 void launch_rigid_move_particles(cudaStream_t s, int N, const SortedFields &A, const sph_rigid_tool *t, double dt) {
     k_rigid_move_particles<<<GRID>>>(N, A, t, dt);

@@ -463,10 +463,11 @@ void launch_gather_plain(cudaStream_t s, int N, const int32_t *perm, const Sorte
 void launch_gather_fused(cudaStream_t s, int N, const int32_t *perm, const KConsts &K, const SortedFields &A,
                          const SortedFields &B, const FixedFields &F, const StepScratch &W, const int32_t *hash_src,
                          const ToolDev *tool) {
+    const int tb = fp64_block(N);   // EOS and artificial stress per particle: spread small systems
     if (K.precision == SPH_PREC_FP32K)
-        k_gather_fused32<<<div_up(N, kBlock), kBlock, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec32, tool);
+        k_gather_fused32<<<div_up(N, tb), tb, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec32, tool);
     else
-        k_gather_fused<false><<<div_up(N, kBlock), kBlock, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec64, W.rec32);
+        k_gather_fused<false><<<div_up(N, tb), tb, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec64, W.rec32);
 }
 
 void launch_build_records(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F,

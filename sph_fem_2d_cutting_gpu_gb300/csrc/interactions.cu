@@ -236,8 +236,8 @@ __device__ __forceinline__ void fused_epilogue32(int k, const KConsts &K, const 
 }
 
 // ---- FP64 ---------------------------------------------------------------------------
-template <bool kFused>
-__global__ void __launch_bounds__(kBlock) k_interact64(int N, KConsts K, const int32_t *__restrict__ offsets,
+template <bool kFused, int kB = kBlock>
+__global__ void __launch_bounds__(kB) k_interact64(int N, KConsts K, const int32_t *__restrict__ offsets,
                                                        const dbl4 *__restrict__ rec, SortedFields B, FixedFields F,
                                                        SegDev seg, const ToolDev *__restrict__ tool,
                                                        int32_t *__restrict__ secant_iters, uint32_t *status) {
@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(kBlock) k_interact64(int N, KConsts K, const i
     Sums64 a = {};
     const int hash = B.hash[k];
     const sph_geom_constants &g = K.g;
-    __shared__ int s_list[kPairChunk][kBlock];
+    __shared__ int s_list[kPairChunk][kB];
     int ii = 0, hi_i = 0, lo_j = 0, hi_j = 0, jc = 0, j1 = 0;
     bool done = true;
     if (hash >= 0 && hash < g.num_cell && !pse_tool) {
@@ -677,13 +677,33 @@ static void launch_i32(cudaStream_t s, int N, const KConsts &K, const int32_t *o
                                                                            W.secant_iters, W.status, cap);
 }
 
+// Threads per block of the FP64 per-particle kernels: the largest of 256, 128,
+// 64 that still gives every SM two blocks, else 32.  The FP64 pipe is narrow, so
+// a small system (the reference's own cases are 7k-12k particles) must spread
+// over all SMs rather than fill a few.  Results do not depend on it: each
+// particle's sums run in one thread in the same order.
+int fp64_block(int N) {
+    static int sms[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int &n = sms[dev & 63];
+    if (!n) {
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 152;
+    }
+    for (int kb : {256, 128, 64})
+        if (div_up(N, kb) >= 2 * n) return kb;
+    return 32;
+}
+
 // ---- interactions_gpu.cu:84-140 do_interactions_heat_pse (FP64) --------------------------
 // T_t = alpha * sum_j (T_j - T_i) W2(r_ij, h_i) m / rho_j over every particle of
 // the 5x5 block of cells of edge h around the particle's cell (no support
 // cut-off, blanked neighbours included), W2 = 4 / (h^4 pi) exp(-|r|^2 / h^2)
 // (kernels.cuh:67-84).  Reads the predicted state from the FP64 records; the
 // block's columns are contiguous slot ranges as in the neighbour sums.
-__global__ void __launch_bounds__(kBlock) k_heat_pse64(int N, KConsts K, const int32_t *__restrict__ offsets,
+template <int kB>
+__global__ void __launch_bounds__(kB) k_heat_pse64(int N, KConsts K, const int32_t *__restrict__ offsets,
                                                        const dbl4 *__restrict__ rec,
                                                        const int32_t *__restrict__ hashes, double *__restrict__ T_t) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -694,9 +714,9 @@ __global__ void __launch_bounds__(kBlock) k_heat_pse64(int N, KConsts K, const i
     const dbl4 i0 = rec[4 * k + 0], i2 = rec[4 * k + 2];
     const double xi = i0.x, yi = i0.y, hi = i2.z, Ti = i3.z;
     const double alpha = (fi & kFlagTool) ? K.c.trml_tool_sph.alpha : K.c.trml_wp.alpha;
-    const double mass = K.c.phys.mass;
     const double h2 = hi * hi, h4 = h2 * h2;
     const double c = 4. / (h4 * kRigidPi);
+    const double inv_h2 = 1. / h2;
     double sum = 0.;
     const int hash = hashes[k];
     const sph_geom_constants &g = K.g;
@@ -707,11 +727,13 @@ __global__ void __launch_bounds__(kBlock) k_heat_pse64(int N, KConsts K, const i
         for (int ii = lo_i; ii < hi_i; ii++) {
             const int j1 = __ldg(offsets + ii * g.ny + hi_j);
             for (int j = __ldg(offsets + ii * g.ny + lo_j); j < j1; j++) {
-                const dbl4 n0 = rec[4 * j + 0];
+                const dbl4 n0 = rec[4 * j + 0], n3 = rec[4 * j + 3];
                 const double xij = xi - n0.x, yij = yi - n0.y;
-                const double xx = sqrt(xij * xij + yij * yij);
-                const double w2 = c * exp(-xx * xx / h2);
-                sum += (rec[4 * j + 3].z - Ti) * w2 * mass / rec[4 * j + 2].w;
+                // |r|^2 / h^2 as a product with 1/h^2; n3.y = m / rho_j.  Both differ
+                // from the reference's sqrt-square, division and m / rho_j order by
+                // rounding only (relative 1e-16 per term).
+                const double w2 = c * exp(-(xij * xij + yij * yij) * inv_h2);
+                sum += (n3.z - Ti) * w2 * n3.y;
             }
         }
     }
@@ -720,7 +742,12 @@ __global__ void __launch_bounds__(kBlock) k_heat_pse64(int N, KConsts K, const i
 
 void launch_heat_pse(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const StepScratch &W,
                      const SortedFields &B) {
-    k_heat_pse64<<<div_up(N, kBlock), kBlock, 0, s>>>(N, K, offsets, W.rec64, B.hash, B.T_t);
+    switch (fp64_block(N)) {
+        case 32: k_heat_pse64<32><<<div_up(N, 32), 32, 0, s>>>(N, K, offsets, W.rec64, B.hash, B.T_t); break;
+        case 64: k_heat_pse64<64><<<div_up(N, 64), 64, 0, s>>>(N, K, offsets, W.rec64, B.hash, B.T_t); break;
+        case 128: k_heat_pse64<128><<<div_up(N, 128), 128, 0, s>>>(N, K, offsets, W.rec64, B.hash, B.T_t); break;
+        default: k_heat_pse64<256><<<div_up(N, 256), 256, 0, s>>>(N, K, offsets, W.rec64, B.hash, B.T_t); break;
+    }
 }
 
 void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const SortedFields &B,
@@ -745,10 +772,27 @@ void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t 
             k_interact32<false><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec32, B, F, seg, tool, W.secant_iters, W.status,
                                                         0);
     } else {
-        if (fused)
-            k_interact64<true><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec64, B, F, seg, tool, W.secant_iters, W.status);
-        else
-            k_interact64<false><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec64, B, F, seg, tool, W.secant_iters, W.status);
+        const int kb = fp64_block(N);
+        const int g64 = div_up(N, kb);
+#define I64(F, B) k_interact64<F, B><<<g64, B, 0, s>>>(N, K, offsets, W.rec64, B_, F_, seg, tool, W.secant_iters, W.status)
+        const SortedFields &B_ = B;
+        const FixedFields &F_ = F;
+        if (fused) {
+            switch (kb) {
+                case 32: I64(true, 32); break;
+                case 64: I64(true, 64); break;
+                case 128: I64(true, 128); break;
+                default: I64(true, 256); break;
+            }
+        } else {
+            switch (kb) {
+                case 32: I64(false, 32); break;
+                case 64: I64(false, 64); break;
+                case 128: I64(false, 128); break;
+                default: I64(false, 256); break;
+            }
+        }
+#undef I64
     }
 }
 

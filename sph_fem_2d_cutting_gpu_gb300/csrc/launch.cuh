@@ -28,6 +28,7 @@ void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t 
 void launch_heat_pse(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const StepScratch &W,
                      const SortedFields &B);
 int interact_variant_count();
+int fp64_block(int N);   // threads per block of the FP64 per-particle kernels for N particles
 void interact_variant_shape(int v, int *block, int *min_blocks, int *staged);
 
 // actions.cu
