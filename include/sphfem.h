@@ -181,6 +181,10 @@ typedef struct sph_tool_state {
     double ref_dist;
     double lowest_point, right_point;
     int32_t n_segments, n_cut_colors;
+    /* wear (WEAR_NODE_SHIFT): flank_retreat (tool_FEM.cu:19) is added to the y
+     * motion of nodes and segments every step; flank_contact (tool_FEM.cu:20) is
+     * lowest_point after the last tool update.  Both 0 / lowest_point without wear. */
+    double flank_retreat, flank_contact;
 } sph_tool_state;
 
 typedef struct sph_ctx sph_ctx;
@@ -196,6 +200,9 @@ int sph_tool_host_info(const sph_tool_host *t, sph_tool_state *state, int32_t *n
                        int32_t *n_colors);
 /* Copies into caller arrays (NULL fields skipped); sizes must match. */
 int sph_tool_host_export(const sph_tool_host *t, sph_segments *seg, sph_fem *fem);
+/* Wear layers of the host tool model (layer[e][0]: layer 1, layer[e][1]: layer 2;
+ * mesh_structure_GPU.cu:1063-1148). */
+int sph_tool_host_layers(const sph_tool_host *t, int32_t *layer);
 int sph_tool_host_destroy(sph_tool_host *t);
 
 /* ---- context ------------------------------------------------------------ */
@@ -471,6 +478,53 @@ int sph_get_launch_config(const sph_ctx *ctx, sph_launch_config *cfg);
  * 5 FEM rate/update + tool move, 6 contact/BC/invalidate tail (+ next
  * histogram).  n_stages receives 7. */
 int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_stages);
+
+/* ---- tool wear by nodal shift (WEAR_NODE_SHIFT) --------------------------------
+ * The reference's wear path of the FEM-tool step (types.h:25):
+ *  - every step the segment statistics are reset (segments_wear_rate_reset,
+ *    tool_FEM.cu:1595-1609) and the friction-heat kernel adds, per contact
+ *    segment, the count, contact pressure, sliding speed, segment temperature
+ *    and sliding force of its particles (actions_gpu.cu:401-419);
+ *  - once wear is switched on (the reference's `wear_pro`, mfree_gpu.cpp:300),
+ *    wear_adjustment (actions_gpu.cu:1009-1020) runs after the return mapping:
+ *    the elements of the two cutting-edge layers leave the lumped mass and
+ *    stiffness (mesh_retreat_wear, FEM_thermal_gpu.cu:923-936), the cutting-edge
+ *    nodes move along the segment normals by the Usui rake/flank wear
+ *    (do_nodal_shift_wear_smooth_temp with RESTRICT_WEAR_TEMP and
+ *    USE_USUI_RAKE_FLANK, tool_FEM.cu:299-432), the layers return at the new
+ *    node positions (mesh_resume_wear), the segments follow the nodes
+ *    (do_segment_wear_update, tool_FEM.cu:520-545), the flank correction sets
+ *    flank_retreat (do_correct_flank_contact, tool_FEM.cu:559-587) and the
+ *    lumped inverse mass is rebuilt (FEM_thermal_gpu.cu:326-331,838-844).
+ * The gmsh remesh of the reference's main loop is not part of this (no gmsh).
+ * Single-case contexts with a FEM tool only. */
+typedef struct sph_wear_constants {   /* constants_structs.h:113-119 */
+    double A, B, C, D;                /* flank: A, B; rake (|n.x| > 0.85): C, D */
+} sph_wear_constants;
+
+#define SPH_WEAR_OFF 0          /* build without WEAR_NODE_SHIFT */
+#define SPH_WEAR_ACCUMULATE 1   /* WEAR_NODE_SHIFT, wear_pro false: segment statistics only */
+#define SPH_WEAR_SHIFT 2        /* WEAR_NODE_SHIFT, wear_pro true: statistics + wear_adjustment each step */
+
+int sph_set_wear(sph_ctx *ctx, int32_t mode, const sph_wear_constants *wc);
+
+/* Host view of the wear state (any pointer may be NULL to skip that field). */
+typedef struct sph_wear_state {
+    int32_t n_elements, n_seg;
+    int32_t *elements;        /* [n_elements][4] node a, b, c, colour (mesh_GPU_m::node_num) */
+    int32_t *layer;           /* [n_elements][2] cutting_boundary_layer: layer 1, layer 2 */
+    double *M;                /* [n_nodes] lumped mass (m_mass_matrix, after Dirichlet) */
+    double *phys_para;        /* [n_seg][4] count, sum pressure, sum sliding speed, sum segment T */
+    double *sliding_force;    /* [n_seg] */
+    double *wear_nodes;       /* [n_seg] wear rate of the segment (left + right) / dt */
+} sph_wear_state;
+int sph_download_wear(sph_ctx *ctx, sph_wear_state *host);
+int sph_upload_wear(sph_ctx *ctx, const sph_wear_state *host);   /* M, phys_para, sliding_force, wear_nodes */
+
+/* Stage entry points: m_tool->segments_wear_rate_reset() (leap_frog.cu:183-186)
+ * and wear_adjustment(m_tool) (leap_frog.cu:224-229). */
+int sph_segments_wear_rate_reset(sph_ctx *ctx);
+int sph_wear_adjustment(sph_ctx *ctx);
 
 /* ---- cell-list build that allocates nothing ------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc

@@ -40,6 +40,8 @@ def load() -> C.CDLL:
     F = C.POINTER(abi.Fem)
     T = C.POINTER(abi.ToolState)
     R = C.POINTER(abi.RigidTool)
+    Wp = C.POINTER(abi.WearState)
+    Wc = C.POINTER(abi.WearConstants)
     PD, PI, D, I = abi.PD, abi.PI, C.c_double, C.c_int
     sig = {
         "orc_num_threads": ([], I),
@@ -81,6 +83,12 @@ def load() -> C.CDLL:
         "orc_fric_heat_rigid": ([P, K, PD, D], None),
         "orc_interactions_heat_pse": ([P, PI, PI, G, K], None),
         "orc_step_rigid": ([P, PI, PI, G, K, D, R, I], C.c_uint32),
+        "orc_wear_layers": ([I, PI, PI, I, PI], None),
+        "orc_wear_reset": ([Wp], None),
+        "orc_wear_adjustment": ([F, S, T, Wp, K, Wc, D], None),
+        "orc_fric_heat_gen_fem_wear": ([P, S, K, PD, D, PD, Wp], I),
+        "orc_segments_update_flank": ([S, PD, D, D], None),
+        "orc_step_wear": ([P, PI, PI, G, K, D, S, F, T, I, Wp, Wc, I], C.c_uint32),
         "orc_mlp_eval": ([PD, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int64, I, PD,
                           PD, PD], I),
         "orc_mlp_adam": ([C.POINTER(C.c_float)] * 4 + [C.c_int64, C.c_float], I),
@@ -113,7 +121,8 @@ class OracleSim:
     tool, the interface segments, FEM system and tool kinematics."""
 
     def __init__(self, constants: abi.Constants, grid: abi.GridParams, particles: dict, dt: float,
-                 tool: dict | None = None, rigid: abi.RigidTool | None = None, pse: bool = False):
+                 tool: dict | None = None, rigid: abi.RigidTool | None = None, pse: bool = False,
+                 wear: dict | None = None):
         self.lib = load()
         self.C = constants
         self.grid = grid
@@ -138,12 +147,34 @@ class OracleSim:
             self.rigid = abi.RigidTool()
             C.memmove(C.byref(self.rigid), C.byref(rigid), C.sizeof(abi.RigidTool))
         self.pse = bool(pse)
+        # wear by nodal shift: dict(mode, constants, elements, layer, M) (statistics start at zero)
+        self.wear_mode = 0
+        if wear is not None:
+            ns = len(self.seg["fric_heat"])
+            self.wear = dict(elements=np.ascontiguousarray(wear["elements"], np.int32).copy(),
+                             layer=np.ascontiguousarray(wear["layer"], np.int32).copy(),
+                             M=np.ascontiguousarray(wear["M"], np.float64).copy(),
+                             phys_para=np.zeros((ns, 4)), sliding_force=np.zeros(ns), wear_nodes=np.zeros(ns))
+            self.wear_mode = int(wear["mode"])
+            self.wear_c = abi.WearConstants()
+            c = wear.get("constants")
+            if c is not None:
+                C.memmove(C.byref(self.wear_c), C.byref(c), C.sizeof(abi.WearConstants))
 
     def pstruct(self):
         return abi.particles_struct(self.P, self.N)
 
     def sstruct(self):
         return _struct_from(self.seg, abi.Segments, "n", len(self.seg["fric_heat"]))
+
+    def wstruct(self):
+        w = self.wear
+        s = abi.WearState()
+        s.n_elements = len(w["elements"])
+        s.n_seg = len(w["sliding_force"])
+        for k in ("elements", "layer", "M", "phys_para", "sliding_force", "wear_nodes"):
+            setattr(s, k, abi.ptr(w[k]))
+        return s
 
     def fstruct(self):
         f = _struct_from(self.fem, abi.Fem, "n_nodes", len(self.fem["T"]))
@@ -158,6 +189,12 @@ class OracleSim:
                                            C.byref(self.rigid) if self.rigid is not None else None, int(self.pse))
         if self.tool:
             s, f = self.sstruct(), self.fstruct()
+            if self.wear_mode:
+                w = self.wstruct()
+                return self.lib.orc_step_wear(C.byref(p), abi.ptr(self.cell_start), abi.ptr(self.cell_end),
+                                              C.byref(self.g), C.byref(self.C), self.dt, C.byref(s), C.byref(f),
+                                              C.byref(self.ts), self.n_colors, C.byref(w), C.byref(self.wear_c),
+                                              self.wear_mode)
             return self.lib.orc_step(C.byref(p), abi.ptr(self.cell_start), abi.ptr(self.cell_end), C.byref(self.g),
                                      C.byref(self.C), self.dt, C.byref(s), C.byref(f), C.byref(self.ts),
                                      self.n_colors)
@@ -250,12 +287,26 @@ class OracleSim:
 
     def material_fric_heat_gen_fem(self) -> int:
         p, s = self.pstruct(), self.sstruct()
+        if self.wear_mode:
+            w = self.wstruct()
+            return self.lib.orc_fric_heat_gen_fem_wear(C.byref(p), C.byref(s), C.byref(self.C), self.ts.vel, self.dt,
+                                                       abi.ptr(self.fem["T"]), C.byref(w))
         return self.lib.orc_fric_heat_gen_fem(C.byref(p), C.byref(s), C.byref(self.C), self.ts.vel, self.dt)
 
     def move_tool(self, dt: float):
         s, f = self.sstruct(), self.fstruct()
-        self.lib.orc_segments_update(C.byref(s), self.ts.vel, dt)
+        self.lib.orc_segments_update_flank(C.byref(s), self.ts.vel, dt, self.ts.flank_retreat)
         self.lib.orc_tool_update(C.byref(f), C.byref(self.ts), dt)
+
+    # wear by nodal shift (leap_frog.cu:183-186,224-229)
+    def segments_wear_rate_reset(self):
+        w = self.wstruct()
+        self.lib.orc_wear_reset(C.byref(w))
+
+    def wear_adjustment(self):
+        f, s, w = self.fstruct(), self.sstruct(), self.wstruct()
+        self.lib.orc_wear_adjustment(C.byref(f), C.byref(s), C.byref(self.ts), C.byref(w), C.byref(self.C),
+                                     C.byref(self.wear_c), self.dt)
 
     # leap-frog snapshots (leap_frog.cu:25-96)
     def init(self):

@@ -718,8 +718,10 @@ int orc_invalidate(sph_particles *P) {
 
 // actions_gpu.cu:345-420 do_material_fric_heat_gen_FEM_v21 (WEAR_NODE_SHIFT off).
 // fric_heat is accumulated in particle index order.  Returns NaN-blanked count.
-int orc_fric_heat_gen_fem(sph_particles *P, sph_segments *Sg, const sph_constants *C, const double vel_tool[2],
-                          double dt) {
+// WEAR_NODE_SHIFT statistics (actions_gpu.cu:401-419) when W != NULL:
+// T_nodes = the FEM temperature at that point of the step.
+static int fric_heat_impl(sph_particles *P, sph_segments *Sg, const sph_constants *C, const double vel_tool[2],
+                          double dt, const double *T_nodes, sph_wear_state *W) {
     const int N = P->N;
     int nanb = 0;
     for (int pidx = 0; pidx < N; pidx++) {
@@ -742,7 +744,6 @@ int orc_fric_heat_gen_fem(sph_particles *P, sph_segments *Sg, const sph_constant
         double f_normal = sqrtf_d(fcx * fcx + fcy * fcy);
         double rho_ = P->rho[pidx];
         double length = sqrtf_d(C->tool.slave_mass / rho_);
-        (void)f_normal; (void)length;
         if (v_rel_mag > 0.03) continue;
         double T_buffer = P->T[pidx] + value * (1 - partition_wp) * dt / C->trml_wp.cp / C->phys.mass;
         if (T_buffer > 1550.) {
@@ -752,8 +753,31 @@ int orc_fric_heat_gen_fem(sph_particles *P, sph_segments *Sg, const sph_constant
             P->T[pidx] = T_buffer;
             Sg->fric_heat[seg] += value * partition_wp;
         }
+        if (W) {
+            int left_no = Sg->marks[4 * seg + 2], right_no = Sg->marks[4 * seg + 3];
+            double T_seg = 0.5 * (T_nodes[left_no] + T_nodes[right_no]);
+            double vel_tool_norm = sqrt(vel_tool[0] * vel_tool[0] + vel_tool[1] * vel_tool[1]);
+            if (v_rel_mag > 0.008) continue;
+            else if (v_rel_mag > vel_tool_norm * 8.0 && fabs(ny) > 0.5) continue;
+            double pressure_trial = f_normal / length;
+            W->phys_para[4 * seg + 0] += 1.;
+            W->phys_para[4 * seg + 1] += pressure_trial;
+            W->phys_para[4 * seg + 2] += v_rel_mag;
+            W->phys_para[4 * seg + 3] += T_seg;
+            W->sliding_force[seg] += f_fric_mag / length;
+        }
     }
     return nanb;
+}
+
+int orc_fric_heat_gen_fem(sph_particles *P, sph_segments *Sg, const sph_constants *C, const double vel_tool[2],
+                          double dt) {
+    return fric_heat_impl(P, Sg, C, vel_tool, dt, nullptr, nullptr);
+}
+
+int orc_fric_heat_gen_fem_wear(sph_particles *P, sph_segments *Sg, const sph_constants *C, const double vel_tool[2],
+                               double dt, const double *T_nodes, sph_wear_state *W) {
+    return fric_heat_impl(P, Sg, C, vel_tool, dt, T_nodes, W);
 }
 
 // actions_gpu.cu:423-583 do_compute_contact_forces_FEM_tool_v3_s1.
@@ -841,29 +865,35 @@ void orc_contact_s2(sph_particles *P, sph_segments *Sg, const sph_constants *C, 
 }
 
 // tool_FEM.cu:119-139 do_segments_update (flank_retreat == 0 without wear)
-void orc_segments_update(sph_segments *Sg, const double vel[2], double dt) {
+// (y + vel.y dt + flank_retreat, left to right; flank_retreat is 0 without wear)
+void orc_segments_update_flank(sph_segments *Sg, const double vel[2], double dt, double flank_retreat) {
     for (int i = 0; i < Sg->n; i++) {
         double lx = Sg->left[2 * i], ly = Sg->left[2 * i + 1], rx = Sg->right[2 * i], ry = Sg->right[2 * i + 1];
         Sg->left[2 * i] = lx + vel[0] * dt;
-        Sg->left[2 * i + 1] = ly + (vel[1] * dt + 0.);
+        Sg->left[2 * i + 1] = ly + vel[1] * dt + flank_retreat;
         Sg->right[2 * i] = rx + vel[0] * dt;
-        Sg->right[2 * i + 1] = ry + (vel[1] * dt + 0.);
+        Sg->right[2 * i + 1] = ry + vel[1] * dt + flank_retreat;
         Sg->heat_exchange[2 * i] = 0; Sg->heat_exchange[2 * i + 1] = 0;
         Sg->fric_heat[i] = 0.;
     }
 }
 
+void orc_segments_update(sph_segments *Sg, const double vel[2], double dt) { orc_segments_update_flank(Sg, vel, dt, 0.); }
+
 // tool_FEM.cu:109-117 do_tool_update_FEM_gpu and the host bookkeeping of
 // tool_FEM::tool_update_FEM_gpu (:1552-1559)
+// (position.y += vel.y dt + flank_retreat, tool_FEM.cu:115; flank_contact =
+// lowest_point afterwards, tool_FEM.cu:1567-1569)
 void orc_tool_update(sph_fem *F, sph_tool_state *ts, double dt) {
     for (int i = 0; i < F->n_nodes; i++) {
         F->position[2 * i] += ts->vel[0] * dt;
-        F->position[2 * i + 1] += ts->vel[1] * dt + 0.;
+        F->position[2 * i + 1] += ts->vel[1] * dt + ts->flank_retreat;
     }
     ts->tl_point_ref[0] += ts->vel[0] * dt; ts->tl_point_ref[1] += ts->vel[1] * dt;
     ts->br_point[0] += ts->vel[0] * dt; ts->br_point[1] += ts->vel[1] * dt;
     ts->lowest_point += ts->vel[1] * dt;
     ts->right_point += ts->vel[0] * dt;
+    ts->flank_contact = ts->lowest_point;
 }
 
 // FEM_thermal_gpu.cu:902-921 reset_FEM_server: T_old = T, f_temp = f, K_temp = K
@@ -911,14 +941,149 @@ void orc_fem_calculate_temp(sph_fem *F, const double *T_old, double dt) {
     for (int idx = 0; idx < F->n_nodes; idx++) F->T[idx] = dt * F->k[idx] + T_old[idx];
 }
 
+// ---- tool wear by nodal shift (WEAR_NODE_SHIFT) -----------------------------------------
+// mesh_structure_GPU.cu:1063-1148: layer 1 = elements with a cutting edge
+// (cutting_boundary_elements); layer 2 = every other element with a node on the
+// cutting edge (CuttingEdgeNum) or a node of a layer-1 element.
+void orc_wear_layers(int n_elements, const int32_t *elements, const int32_t *cutting_flags, int n_nodes,
+                     int32_t *layer) {
+    std::vector<char> edge_node(n_nodes, 0), l1_node(n_nodes, 0);
+    for (int e = 0; e < n_elements; e++) {
+        const int32_t *el = elements + 3 * e, *cf = cutting_flags + 3 * e;
+        const int pairs[3][2] = {{el[0], el[1]}, {el[1], el[2]}, {el[2], el[0]}};
+        layer[2 * e] = layer[2 * e + 1] = 0;
+        for (int a = 0; a < 3; a++)
+            if (cf[a]) {
+                edge_node[pairs[a][0]] = edge_node[pairs[a][1]] = 1;
+                layer[2 * e] = 1;
+            }
+    }
+    for (int e = 0; e < n_elements; e++)
+        if (layer[2 * e])
+            for (int a = 0; a < 3; a++) l1_node[elements[3 * e + a]] = 1;
+    for (int e = 0; e < n_elements; e++) {
+        if (layer[2 * e]) continue;
+        for (int a = 0; a < 3; a++) {
+            const int nd = elements[3 * e + a];
+            if (edge_node[nd] || l1_node[nd]) layer[2 * e + 1] = 1;
+        }
+    }
+}
+
+// tool_FEM.cu:1595-1609 segments_wear_rate_reset
+void orc_wear_reset(sph_wear_state *W) {
+    for (int s = 0; s < W->n_seg; s++) {
+        for (int c = 0; c < 4; c++) W->phys_para[4 * s + c] = 0.;
+        W->sliding_force[s] = 0.;
+        W->wear_nodes[s] = 0.;
+    }
+}
+
+// FEM_thermal_gpu.cu:71-109: lumped mass m and stiffness ke of a linear triangle,
+// ke = w 3 k |det J| B^T B with B = J^-T grad_ref (the glm::inverse of the
+// transposed Jacobian written out).
+static void p1_element_ref(const double *pos, const int32_t *el, const sph_tool_constants &tc, double &m,
+                           double ke[3][3]) {
+    const double weights = 1. / 3. * 0.5;
+    const double c0x = pos[2 * el[0]], c0y = pos[2 * el[0] + 1];
+    const double J0x = pos[2 * el[1]] - c0x, J0y = pos[2 * el[1] + 1] - c0y;   // jacobian[0]
+    const double J1x = pos[2 * el[2]] - c0x, J1y = pos[2 * el[2] + 1] - c0y;   // jacobian[1]
+    const double determinant = fabs(J0x * J1y - J1x * J0y);
+    m = weights * tc.cp * tc.rho * determinant;
+    // transpose(J) has rows J0, J1; its inverse: (1 / det) [[J1y, -J0y], [-J1x, J0x]]
+    const double d = J0x * J1y - J0y * J1x;
+    const double iT[2][2] = {{J1y / d, -J0y / d}, {-J1x / d, J0x / d}};
+    const double G[3][2] = {{-1., -1.}, {1., 0.}, {0., 1.}};
+    double B[3][2];
+    for (int a = 0; a < 3; a++) {
+        B[a][0] = iT[0][0] * G[a][0] + iT[0][1] * G[a][1];
+        B[a][1] = iT[1][0] * G[a][0] + iT[1][1] * G[a][1];
+    }
+    const double value = tc.k * determinant;
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) ke[a][b] = weights * 3. * value * (B[a][0] * B[b][0] + B[a][1] * B[b][1]);
+}
+
+// do_mesh_adjustment_wear (FEM_thermal_gpu.cu:476-577) over every layer element,
+// sign -1 (mesh_retreat_wear) or +1 (mesh_resume_wear).
+static void mesh_adjust(sph_fem *F, sph_wear_state *W, const sph_tool_constants &tc, double sign) {
+    for (int e = 0; e < W->n_elements; e++) {
+        if (W->layer[2 * e] == 0 && W->layer[2 * e + 1] == 0) continue;
+        const int32_t *el = W->elements + 4 * e;
+        double m, ke[3][3];
+        p1_element_ref(F->position, el, tc, m, ke);
+        for (int a = 0; a < 3; a++) {
+            W->M[el[a]] += sign * m;
+            for (int k = F->row_ptr[el[a]]; k < F->row_ptr[el[a] + 1]; k++)
+                for (int b = 0; b < 3; b++)
+                    if (F->col_ind[k] == el[b]) F->K[k] += sign * ke[b][a];
+        }
+    }
+}
+
+// actions_gpu.cu:1009-1020 wear_adjustment: retreat, nodal shift
+// (do_nodal_shift_wear_smooth_temp, tool_FEM.cu:299-432, RESTRICT_WEAR_TEMP and
+// USE_USUI_RAKE_FLANK), resume, do_segment_wear_update (tool_FEM.cu:520-545),
+// do_correct_flank_contact over the first 512 segments (tool_FEM.cu:559-587) and
+// the lumped inverse mass.  Segments in index order.
+void orc_wear_adjustment(sph_fem *F, sph_segments *Sg, sph_tool_state *ts, sph_wear_state *W,
+                         const sph_constants *C, const sph_wear_constants *wc, double dt) {
+    const sph_tool_constants &tc = C->tool;
+    mesh_adjust(F, W, tc, -1.);
+    for (int s = 0; s < Sg->n; s++) {
+        const double *w = W->phys_para + 4 * s;
+        if (w[0] == 0.) continue;
+        const int left = Sg->marks[4 * s + 2], right = Sg->marks[4 * s + 3];
+        double pressure = w[1] / w[0];
+        double vel = w[2] / w[0];
+        double Tl = F->T[left], Tr = F->T[right];
+        if (vel > 0.008) continue;
+        Tl = fmin(Tl, 1350.);
+        Tr = fmin(Tr, 1350.);
+        vel = fmin(vel, 0.008);
+        pressure = fmin(pressure, 0.04);
+        const double nx = Sg->normal[2 * s], ny = Sg->normal[2 * s + 1];
+        double wl, wr;
+        if (fabs(nx) > 0.85) {
+            wl = dt * wc->C * pressure * vel * exp(-wc->D / Tl);
+            wr = dt * wc->C * pressure * vel * exp(-wc->D / Tr);
+        } else {
+            wl = dt * wc->A * pressure * vel * exp(-wc->B / Tl);
+            wr = dt * wc->A * pressure * vel * exp(-wc->B / Tr);
+        }
+        W->wear_nodes[s] = (wl + wr) / dt;
+        F->position[2 * left] += nx * wl;
+        F->position[2 * left + 1] += ny * wl;
+        F->position[2 * right] += nx * wr;
+        F->position[2 * right + 1] += ny * wr;
+    }
+    mesh_adjust(F, W, tc, 1.);
+    double mn = FLT_MAX;
+    for (int s = 0; s < Sg->n; s++) {
+        const int l = Sg->marks[4 * s + 2], r = Sg->marks[4 * s + 3];
+        const double lx = F->position[2 * l], ly = F->position[2 * l + 1];
+        const double rx = F->position[2 * r], ry = F->position[2 * r + 1];
+        Sg->left[2 * s] = lx; Sg->left[2 * s + 1] = ly;
+        Sg->right[2 * s] = rx; Sg->right[2 * s + 1] = ry;
+        const double dx = rx - lx, dy = ry - ly;
+        const double inv = 1. / sqrt(dy * dy + (-dx) * (-dx));
+        Sg->normal[2 * s] = dy * inv;
+        Sg->normal[2 * s + 1] = -dx * inv;
+        if (s < 512) mn = fmin(mn, ly);
+    }
+    ts->flank_retreat = ts->flank_contact - mn;
+    for (int i = 0; i < F->n_nodes; i++) F->M_inv[i] = 1. / W->M[i];
+}
+
 // leap_frog.cu:162-248 leap_frog::step(particle_gpu*, grid_base*, tool_FEM*) with
 // WEAR_NODE_SHIFT off; without a tool (Sg == NULL) the tool calls are skipped
 // (leap_frog.cu:99-160 with no SPH tool).  cell_start/cell_end persist between
 // calls (cell_end of empty cells stays stale as in the reference).
 // Returns SPH_STATUS_* bits observed during the step.
-uint32_t orc_step(sph_particles *P, int32_t *cell_start, int32_t *cell_end, const sph_geom_constants *g,
-                  const sph_constants *C, double dt, sph_segments *Sg, sph_fem *F, sph_tool_state *ts,
-                  int n_colors) {
+uint32_t orc_step_wear(sph_particles *P, int32_t *cell_start, int32_t *cell_end, const sph_geom_constants *g,
+                       const sph_constants *C, double dt, sph_segments *Sg, sph_fem *F, sph_tool_state *ts,
+                       int n_colors, sph_wear_state *W, const sph_wear_constants *wc, int wear_mode) {
+    if (!W) wear_mode = 0;
     const int N = P->N;
     uint32_t st = 0;
     std::vector<double> pos_init(2 * (size_t)N), vel_init(2 * (size_t)N), S_init(4 * (size_t)N), rho_init(N), T_init(N);
@@ -929,6 +1094,7 @@ uint32_t orc_step(sph_particles *P, int32_t *cell_start, int32_t *cell_end, cons
     if (Sg) {
         T_old.resize(F->n_nodes); f_temp.resize(F->n_nodes); K_temp.resize(F->nnz);
         orc_fem_reset_server(F, T_old.data(), f_temp.data(), K_temp.data());
+        if (wear_mode) orc_wear_reset(W);
     }
     orc_predict(P, pos_init.data(), vel_init.data(), S_init.data(), rho_init.data(), T_init.data(), dt);
     if (Sg) orc_fem_calculate_temp(F, T_old.data(), 0.5 * dt);
@@ -941,7 +1107,7 @@ uint32_t orc_step(sph_particles *P, int32_t *cell_start, int32_t *cell_end, cons
     orc_contmech_advection(P);
     orc_correct(P, pos_init.data(), vel_init.data(), S_init.data(), rho_init.data(), T_init.data(), dt);
     if (Sg) {
-        if (orc_fric_heat_gen_fem(P, Sg, C, ts->vel, dt) > 0) st |= SPH_STATUS_FRIC_NAN;
+        if (fric_heat_impl(P, Sg, C, ts->vel, dt, F->T, wear_mode ? W : nullptr) > 0) st |= SPH_STATUS_FRIC_NAN;
         orc_fem_apply_robin(F, Sg, C, n_colors, K_temp.data(), f_temp.data());
         orc_fem_calculate_temp_rate(F, K_temp.data(), f_temp.data());
         orc_fem_calculate_temp(F, T_old.data(), dt);
@@ -950,8 +1116,9 @@ uint32_t orc_step(sph_particles *P, int32_t *cell_start, int32_t *cell_end, cons
         int64_t its = 0;
         if (orc_plasticity_johnson_cook(P, C, dt, &its) > 0) st |= SPH_STATUS_SECANT_MAXITER;
     }
+    if (Sg && wear_mode == 2) orc_wear_adjustment(F, Sg, ts, W, C, wc, dt);
     if (Sg) {
-        orc_segments_update(Sg, ts->vel, dt);
+        orc_segments_update_flank(Sg, ts->vel, dt, ts->flank_retreat);
         orc_tool_update(F, ts, dt);
         st |= orc_contact_s1(P, Sg, C, ts->tl_point_ref, ts->ref_dist, ts->vel, dt);
         orc_contact_s2(P, Sg, C, F->T, dt);
@@ -1218,6 +1385,13 @@ uint32_t orc_step_rigid(sph_particles *P, int32_t *cell_start, int32_t *cell_end
     orc_boundary_conditions_thermal(P, C);
     if (orc_invalidate(P) > 0) st |= SPH_STATUS_NAN_BLANKED;
     return st;
+}
+
+
+uint32_t orc_step(sph_particles *P, int32_t *cell_start, int32_t *cell_end, const sph_geom_constants *g,
+                  const sph_constants *C, double dt, sph_segments *Sg, sph_fem *F, sph_tool_state *ts,
+                  int n_colors) {
+    return orc_step_wear(P, cell_start, cell_end, g, C, dt, Sg, F, ts, n_colors, nullptr, nullptr, 0);
 }
 
 }  // extern "C"

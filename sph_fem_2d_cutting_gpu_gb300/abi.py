@@ -17,6 +17,7 @@ SPH_OK, SPH_ERR_INVALID, SPH_ERR_CUDA, SPH_ERR_NO_DEVICE, SPH_ERR_ALLOC, SPH_ERR
 SPH_PREC_FP64, SPH_PREC_FP32K = 0, 1
 SPH_THERMAL_BROOKSHAW, SPH_THERMAL_PSE = 0, 1
 SPH_RIGID_MAX_SEG = 5
+SPH_WEAR_OFF, SPH_WEAR_ACCUMULATE, SPH_WEAR_SHIFT = 0, 1, 2
 
 STATUS_BITS = {
     "out_of_grid": 1 << 0,
@@ -111,7 +112,8 @@ class ToolMesh(C.Structure):
 
 class ToolState(C.Structure):
     _fields_ = [("vel", D * 2), ("tl_point_ref", D * 2), ("br_point", D * 2), ("ref_dist", D),
-                ("lowest_point", D), ("right_point", D), ("n_segments", I32), ("n_cut_colors", I32)]
+                ("lowest_point", D), ("right_point", D), ("n_segments", I32), ("n_cut_colors", I32),
+                ("flank_retreat", D), ("flank_contact", D)]
 
 
 class MlpNorm(C.Structure):
@@ -124,6 +126,16 @@ JC_LOG_WIDTH = 8
 
 class LaunchConfig(C.Structure):
     _fields_ = [("interact_variant", I32)]
+
+
+class WearConstants(C.Structure):
+    """sph_wear_constants (constants_structs.h:113-119): flank A, B; rake C, D."""
+    _fields_ = _fields(["A", "B", "C", "D"])
+
+
+class WearState(C.Structure):
+    _fields_ = [("n_elements", I32), ("n_seg", I32), ("elements", PI), ("layer", PI), ("M", PD),
+                ("phys_para", PD), ("sliding_force", PD), ("wear_nodes", PD)]
 
 
 class RigidTool(C.Structure):
@@ -251,6 +263,10 @@ def load() -> C.CDLL:
         "sph_set_rigid_tool": ([P, C.POINTER(RigidTool)], C.c_int),
         "sph_get_rigid_tool": ([P, C.POINTER(RigidTool)], C.c_int),
         "sph_set_thermal_model": ([P, I32], C.c_int),
+        "sph_set_wear": ([P, I32, C.POINTER(WearConstants)], C.c_int),
+        "sph_download_wear": ([P, C.POINTER(WearState)], C.c_int),
+        "sph_upload_wear": ([P, C.POINTER(WearState)], C.c_int),
+        "sph_tool_host_layers": ([P, PI], C.c_int),
     }
     for name in STAGE_FUNCTIONS:
         proto.setdefault(name, ([P], C.c_int))
@@ -307,4 +323,5 @@ STAGE_FUNCTIONS = [
     "sph_interactions_monaghan", "sph_material_fric_heat_gen_fem", "sph_compute_contact_forces_fem",
     "sph_fem_reset_server", "sph_fem_apply_robin", "sph_fem_calculate_temp_rate", "sph_step", "sph_step_staged",
     "sph_rigid_tool_update", "sph_compute_contact_forces", "sph_material_fric_heat_gen", "sph_interactions_heat_pse",
+    "sph_segments_wear_rate_reset", "sph_wear_adjustment",
 ]

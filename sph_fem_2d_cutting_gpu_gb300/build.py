@@ -24,8 +24,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
                      "-Xptxas", "-warn-spills"]
 SOURCES = ["cells.cu", "interactions.cu", "actions.cu", "fem.cu", "context.cu", "toolsetup.cpp", "noalloc.cu", "mlp.cu",
-           "mlp_host.cu"]
-HEADERS = ["common.cuh", "physics.cuh", "state.cuh", "launch.cuh", "toolsetup.h", "mlp_host.h", "rigid.cuh", "async.cuh"]
+           "mlp_host.cu", "wear.cu"]
+HEADERS = ["common.cuh", "physics.cuh", "state.cuh", "launch.cuh", "toolsetup.h", "mlp_host.h", "rigid.cuh", "async.cuh", "p1elem.h"]
 
 
 def nvcc() -> str:

@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(kBlock) k_fric_heat(int N, KConsts K, SortedFi
     PARTICLE_LOOP_HEAD
     double T = A.T[i], blanked = A.blanked[i];
     uint32_t st = fric_heat_one(K, K.dt, tool->vel, A.vel[i], A.ft[i], A.n[i], A.fc[i], A.rho[i], A.eps_pl[i], A.on_seg[i],
-                                seg.n, T, blanked, seg.fric_heat);
+                                seg.n, T, blanked, seg.fric_heat, seg.wear);
     if (T != A.T[i]) A.T[i] = T;
     if (blanked != A.blanked[i]) A.blanked[i] = blanked;
     if (st) set_status(status, st);

@@ -150,6 +150,17 @@ struct ToolDev {
     double seg_ymin, seg_ymax;      // y-range of those segments (moved with them)
     double seg_xmax;                // largest x of their end points (moved with them)
     double seg_dxdy;                // largest |dx/dy| of a non-horizontal segment
+    double flank_retreat;           // wear: added to the y motion of nodes and segments (tool_FEM.cu:19)
+    double flank_contact;           // wear: lowest_point after the last tool update (tool_FEM.cu:20)
+};
+
+// Per-segment wear statistics gathered by the friction-heat kernel
+// (WEAR_NODE_SHIFT, actions_gpu.cu:401-419); pp == NULL: not gathered.
+struct WearAcc {
+    dbl4 *pp;                 // count, sum contact pressure, sum sliding speed, sum segment T
+    double *sf;               // sum sliding force / length
+    const int4 *marks;        // segment nodes (z: left, w: right)
+    const double *T_nodes;    // FEM nodal temperature when the friction heat runs
 };
 
 // ---- float narrowings of the reference (double argument -> float call) ------

@@ -63,6 +63,12 @@ struct sph_ctx {
     int interact_variant = 0;            // launch shape of the fused FP32K neighbour sums
     double *usui_scratch = nullptr;      // per-block partials of sph_eval_usui
     sph_rigid_tool *rigid_dev = nullptr; // the rigid tool, moved on the device every step (NULL: none)
+    // wear by nodal shift (WEAR_NODE_SHIFT): SPH_WEAR_* mode, device layer data
+    int wear_mode = SPH_WEAR_OFF;
+    bool wear_ready = false;
+    WearDev wear{};
+    dbl4 *wear_pp = nullptr;             // per-segment statistics (seg.wear points here while wear is on)
+    double *wear_sf = nullptr;
     // pipelined host I/O: uploads into a free particle buffer and downloads run on
     // their own streams, ordered per buffer by events; a step waits only for the
     // copies into its input and out of its output buffer
@@ -359,8 +365,13 @@ int issue_fused_body(sph_ctx *ctx, int64_t &n, int w) {
         launch_heat_pse(s, N, ctx->K, ctx->X.offsets, ctx->W, B);
         n += 1;
     }
+    SegDev sw = ctx->seg;
+    if (ctx->wear_mode != SPH_WEAR_OFF) {   // segments_wear_rate_reset (leap_frog.cu:183-186)
+        launch_wear_reset(s, ctx->seg);
+        sw.wear.T_nodes = ctx->fem.T_half;  // the friction heat sees the half-step FEM temperature
+    }
     if (ctx->mlp_on) CK(cudaMemsetAsync(ctx->jc_list_count, 0, sizeof(int32_t), s));
-    launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, ctx->seg, ctx->tool_dev, true,
+    launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, sw, ctx->tool_dev, true,
                         ctx->interact_variant);
     n += 1;
     if (ctx->mlp_on) {
@@ -370,8 +381,13 @@ int issue_fused_body(sph_ctx *ctx, int64_t &n, int w) {
     }
     if (ctx->has_tool) {
         launch_fem_rate_update(s, ctx->K, ctx->fem, ctx->seg, ctx->tool_dev);
+        n += 1;
+        if (ctx->wear_mode == SPH_WEAR_SHIFT) {   // wear_adjustment (leap_frog.cu:224-229)
+            launch_wear_adjustment(s, ctx->K, ctx->fem, ctx->seg, ctx->wear, ctx->tool_dev, ctx->K.dt);
+            n += 5;
+        }
         launch_tool_move(s, ctx->K, ctx->seg, ctx->fem, ctx->tool_dev, ctx->K.dt, 3, true);
-        n += 2;
+        n += 1;
     }
     if (ctx->K.rigid) {
         launch_rigid_move(s, ctx->K.rigid, ctx->K.dt);
@@ -418,6 +434,8 @@ int sph_tool_host_info(const sph_tool_host *t, sph_tool_state *st, int32_t *n_no
         st->right_point = M.right_point;
         st->n_segments = M.n_seg;
         st->n_cut_colors = M.n_cut_colors;
+        st->flank_retreat = 0.;
+        st->flank_contact = M.lowest_point;
     }
     if (n_nodes) *n_nodes = M.n_nodes;
     if (nnz) *nnz = (int32_t)M.col_ind.size();
@@ -449,6 +467,15 @@ int sph_tool_host_export(const sph_tool_host *t, sph_segments *seg, sph_fem *fem
         if (fem->f) std::memcpy(fem->f, M.f.data(), 8 * nn);
         if (fem->T) std::memcpy(fem->T, M.T.data(), 8 * nn);
         if (fem->k) std::memset(fem->k, 0, 8 * nn);
+    }
+    return SPH_OK;
+}
+
+int sph_tool_host_layers(const sph_tool_host *t, int32_t *layer) {
+    if (!t || !layer) return SPH_ERR_INVALID;
+    for (int e = 0; e < t->m.n_elements; e++) {
+        layer[2 * e] = t->m.layer[e].x;
+        layer[2 * e + 1] = t->m.layer[e].y;
     }
     return SPH_OK;
 }
@@ -618,6 +645,8 @@ ToolDev tool_state_of(const ToolModelHost &M, double dt, int seg_first) {
     td.tl_point_ref[0] = M.tl_point_ref[0]; td.tl_point_ref[1] = M.tl_point_ref[1];
     td.br_point[0] = M.br_point[0]; td.br_point[1] = M.br_point[1];
     td.ref_dist = M.ref_dist; td.lowest_point = M.lowest_point; td.right_point = M.right_point;
+    td.flank_retreat = 0.;
+    td.flank_contact = M.lowest_point;   // as after a tool update (tool_FEM.cu:1567-1569)
     td.seg_first = seg_first;
     td.seg_count = M.n_seg;
     td.seg_ymin = INFINITY;
@@ -1014,7 +1043,9 @@ int sph_material_fric_heat_gen_fem(sph_ctx *ctx) {
     REQUIRE_CTX();
     REQUIRE_SINGLE_CASE();
     REQUIRE_TOOL();
-    launch_fric_heat(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->seg, ctx->tool_dev, ctx->W.status);
+    SegDev sw = ctx->seg;
+    sw.wear.T_nodes = ctx->fem.T;   // after calculate_temp(0.5 dt) in the staged sequence
+    launch_fric_heat(ctx->stream, ctx->N, ctx->K, CUR(ctx), sw, ctx->tool_dev, ctx->W.status);
     ctx->launches++;
     ctx->counts_valid = false;
     CK_LAUNCH();
@@ -1123,6 +1154,8 @@ int sph_get_tool_state(sph_ctx *ctx, sph_tool_state *out) {
     out->right_point = td.right_point;
     out->n_segments = ctx->seg.n;
     out->n_cut_colors = ctx->tool_host.n_cut_colors;
+    out->flank_retreat = td.flank_retreat;
+    out->flank_contact = td.flank_contact;
     return SPH_OK;
 }
 
@@ -1336,6 +1369,7 @@ int sph_step_staged(sph_ctx *ctx) {
     RUN(sph_sort(ctx));
     RUN(sph_init(ctx));
     if (ctx->has_tool) RUN(sph_fem_reset_server(ctx));
+    if (ctx->wear_mode != SPH_WEAR_OFF) RUN(sph_segments_wear_rate_reset(ctx));
     RUN(sph_predict(ctx));
     if (ctx->has_tool) RUN(sph_fem_calculate_temp(ctx, 0.5 * dt));
     RUN(sph_material_eos(ctx));
@@ -1355,6 +1389,7 @@ int sph_step_staged(sph_ctx *ctx) {
     }
     if (ctx->K.rigid) RUN(sph_material_fric_heat_gen(ctx));
     RUN(sph_plasticity_johnson_cook(ctx));
+    if (ctx->wear_mode == SPH_WEAR_SHIFT) RUN(sph_wear_adjustment(ctx));
     if (ctx->has_tool) {
         RUN(sph_segments_update(ctx, dt));
         RUN(sph_tool_update_fem(ctx, dt));
@@ -2008,6 +2043,161 @@ int sph_interactions_heat_pse(sph_ctx *ctx) {
     ctx->launches += 2;
     ctx->counts_valid = false;
     CK_LAUNCH();
+    return SPH_OK;
+}
+
+
+// ---- tool wear by nodal shift (WEAR_NODE_SHIFT) ---------------------------------------------------
+namespace {
+// Device layer data and per-segment statistics, allocated on first use.
+int wear_setup(sph_ctx *ctx) {
+    if (ctx->wear_ready) return SPH_OK;
+    const ToolModelHost &M = ctx->tool_host;
+    SegDev &S = ctx->seg;
+    FemDev &Fm = ctx->fem;
+    WearDev &W = ctx->wear;
+    DALLOC(ctx->wear_pp, S.n);
+    DALLOC(ctx->wear_sf, S.n);
+    DALLOC(S.wear_rate, S.n);
+    DALLOC(Fm.M, Fm.n_nodes);
+    int32_t *node = nullptr, *adj_ptr = nullptr;
+    int4 *adj = nullptr, *slot = nullptr, *elements = nullptr;
+    DALLOC(node, M.wear_node.size());
+    DALLOC(adj_ptr, M.wear_adj_ptr.size());
+    DALLOC(adj, M.wear_adj.size());
+    DALLOC(slot, M.wear_slot.size());
+    DALLOC(elements, M.elements.size());
+    DALLOC(W.seg_delta, S.n);
+    CK(cudaMemsetAsync(ctx->wear_pp, 0, sizeof(dbl4) * S.n, ctx->stream));
+    CK(cudaMemsetAsync(ctx->wear_sf, 0, sizeof(double) * S.n, ctx->stream));
+    CK(cudaMemsetAsync(S.wear_rate, 0, sizeof(double) * S.n, ctx->stream));
+    CK(cudaMemsetAsync(W.seg_delta, 0, sizeof(dbl4) * S.n, ctx->stream));
+    CK(cudaMemcpyAsync(Fm.M, M.M.data(), sizeof(double) * Fm.n_nodes, cudaMemcpyHostToDevice, ctx->stream));
+    if (!M.wear_node.empty()) {
+        CK(cudaMemcpyAsync(node, M.wear_node.data(), sizeof(int32_t) * M.wear_node.size(), cudaMemcpyHostToDevice,
+                           ctx->stream));
+        CK(cudaMemcpyAsync(adj, M.wear_adj.data(), sizeof(int4) * M.wear_adj.size(), cudaMemcpyHostToDevice,
+                           ctx->stream));
+        CK(cudaMemcpyAsync(slot, M.wear_slot.data(), sizeof(int4) * M.wear_slot.size(), cudaMemcpyHostToDevice,
+                           ctx->stream));
+    }
+    CK(cudaMemcpyAsync(adj_ptr, M.wear_adj_ptr.data(), sizeof(int32_t) * M.wear_adj_ptr.size(),
+                       cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(elements, M.elements.data(), sizeof(int4) * M.elements.size(), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    W.n_nodes = (int)M.wear_node.size();
+    W.node = node;
+    W.adj_ptr = adj_ptr;
+    W.adj = adj;
+    W.slot = slot;
+    W.elements = elements;
+    S.wear.marks = S.marks;
+    ctx->wear_ready = true;
+    return SPH_OK;
+}
+}  // namespace
+
+int sph_set_wear(sph_ctx *ctx, int32_t mode, const sph_wear_constants *wc) {
+    REQUIRE_CTX();
+    REQUIRE_SINGLE_CASE();
+    REQUIRE_TOOL();
+    if (mode != SPH_WEAR_OFF && mode != SPH_WEAR_ACCUMULATE && mode != SPH_WEAR_SHIFT)
+        return fail(ctx, SPH_ERR_INVALID, "unknown wear mode");
+    if (mode == SPH_WEAR_SHIFT && !wc) return fail(ctx, SPH_ERR_INVALID, "nodal shift needs the wear constants");
+    if (mode != SPH_WEAR_OFF) {
+        int r = wear_setup(ctx);
+        if (r) return r;
+    }
+    WearDev &W = ctx->wear;
+    bool changed = mode != ctx->wear_mode;
+    if (wc && (wc->A != W.A || wc->B != W.B || wc->C != W.C || wc->D != W.D)) {
+        W.A = wc->A; W.B = wc->B; W.C = wc->C; W.D = wc->D;
+        changed = true;
+    }
+    ctx->wear_mode = mode;
+    // the friction heat gathers the statistics only while wear is on
+    const bool on = mode != SPH_WEAR_OFF;
+    ctx->seg.wear.pp = on ? ctx->wear_pp : nullptr;
+    ctx->seg.wear.sf = on ? ctx->wear_sf : nullptr;
+    if (changed) invalidate_graphs(ctx);
+    return SPH_OK;
+}
+
+int sph_segments_wear_rate_reset(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    if (ctx->wear_mode == SPH_WEAR_OFF) return fail(ctx, SPH_ERR_STATE, "wear is off");
+    launch_wear_reset(ctx->stream, ctx->seg);
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+int sph_wear_adjustment(sph_ctx *ctx) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    if (ctx->wear_mode != SPH_WEAR_SHIFT) return fail(ctx, SPH_ERR_STATE, "nodal-shift wear is off");
+    launch_wear_adjustment(ctx->stream, ctx->K, ctx->fem, ctx->seg, ctx->wear, ctx->tool_dev, ctx->K.dt);
+    ctx->launches += 5;
+    ctx->counts_valid = false;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+int sph_download_wear(sph_ctx *ctx, sph_wear_state *h) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    if (!h) return SPH_ERR_INVALID;
+    const ToolModelHost &M = ctx->tool_host;
+    h->n_elements = M.n_elements;
+    h->n_seg = ctx->seg.n;
+    const size_t ne = (size_t)M.n_elements, ns = (size_t)ctx->seg.n, nn = (size_t)ctx->fem.n_nodes;
+    if (h->elements) std::memcpy(h->elements, M.elements.data(), sizeof(int32_t) * 4 * ne);
+    if (h->layer)
+        for (size_t e = 0; e < ne; e++) {
+            h->layer[2 * e] = M.layer[e].x;
+            h->layer[2 * e + 1] = M.layer[e].y;
+        }
+    const bool dev = ctx->wear_ready;
+    if (h->M) {
+        if (dev) CK(cudaMemcpyAsync(h->M, ctx->fem.M, sizeof(double) * nn, cudaMemcpyDeviceToHost, ctx->stream));
+        else std::memcpy(h->M, M.M.data(), sizeof(double) * nn);
+    }
+    if (h->phys_para) {
+        if (dev) CK(cudaMemcpyAsync(h->phys_para, ctx->wear_pp, sizeof(dbl4) * ns, cudaMemcpyDeviceToHost, ctx->stream));
+        else std::memset(h->phys_para, 0, sizeof(double) * 4 * ns);
+    }
+    if (h->sliding_force) {
+        if (dev) CK(cudaMemcpyAsync(h->sliding_force, ctx->wear_sf, sizeof(double) * ns, cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+        else std::memset(h->sliding_force, 0, sizeof(double) * ns);
+    }
+    if (h->wear_nodes) {
+        if (dev) CK(cudaMemcpyAsync(h->wear_nodes, ctx->seg.wear_rate, sizeof(double) * ns, cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+        else std::memset(h->wear_nodes, 0, sizeof(double) * ns);
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SPH_OK;
+}
+
+int sph_upload_wear(sph_ctx *ctx, const sph_wear_state *h) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    if (!h) return SPH_ERR_INVALID;
+    if (!ctx->wear_ready) return fail(ctx, SPH_ERR_STATE, "wear was never switched on in this context");
+    const size_t ns = (size_t)ctx->seg.n, nn = (size_t)ctx->fem.n_nodes;
+    if (h->M) {
+        CK(cudaMemcpyAsync(ctx->fem.M, h->M, sizeof(double) * nn, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    if (h->phys_para)
+        CK(cudaMemcpyAsync(ctx->wear_pp, h->phys_para, sizeof(dbl4) * ns, cudaMemcpyHostToDevice, ctx->stream));
+    if (h->sliding_force)
+        CK(cudaMemcpyAsync(ctx->wear_sf, h->sliding_force, sizeof(double) * ns, cudaMemcpyHostToDevice, ctx->stream));
+    if (h->wear_nodes)
+        CK(cudaMemcpyAsync(ctx->seg.wear_rate, h->wear_nodes, sizeof(double) * ns, cudaMemcpyHostToDevice,
+                           ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     return SPH_OK;
 }
 

@@ -102,21 +102,25 @@ __global__ void __launch_bounds__(kBlock) k_fem_temp(FemDev F, const double *__r
     F.T[i] = dt * F.k[i] + T_old[i];
 }
 
-// tool_FEM.cu:119-139 do_segments_update (flank_retreat == 0 without wear).
-__device__ __forceinline__ void segment_move(const SegDev &seg, int s, const double *vel, double dt) {
+// tool_FEM.cu:119-139 do_segments_update: y + v.y dt + flank_retreat, evaluated
+// left to right (flank_retreat is 0 without wear).
+__device__ __forceinline__ double seg_y_move(double y, double vy, double dt, double fr) {
+    return __dadd_rn(__dadd_rn(y, __dmul_rn(vy, dt)), fr);
+}
+__device__ __forceinline__ void segment_move(const SegDev &seg, int s, const double *vel, double dt, double fr) {
     double2 l = seg.left[s], r = seg.right[s];
-    double dy = __dadd_rn(__dmul_rn(vel[1], dt), 0.);
-    seg.left[s] = make_double2(add_mul_rn(l.x, vel[0], dt), __dadd_rn(l.y, dy));
-    seg.right[s] = make_double2(add_mul_rn(r.x, vel[0], dt), __dadd_rn(r.y, dy));
+    seg.left[s] = make_double2(add_mul_rn(l.x, vel[0], dt), seg_y_move(l.y, vel[1], dt, fr));
+    seg.right[s] = make_double2(add_mul_rn(r.x, vel[0], dt), seg_y_move(r.y, vel[1], dt, fr));
     seg.heat_exchange[s] = make_double2(0., 0.);
     seg.fric_heat[s] = 0.;
 }
 
 // tool_FEM.cu:109-117 do_tool_update_FEM_gpu + the host bookkeeping of
 // tool_update_FEM_gpu (tool_FEM.cu:1555-1559), kept on the device.
-__device__ __forceinline__ void node_move(const FemDev &F, int i, const double *vel, double dt) {
+// position.y += v.y dt + flank_retreat (tool_FEM.cu:115)
+__device__ __forceinline__ void node_move(const FemDev &F, int i, const double *vel, double dt, double fr) {
     double2 p = F.position[i];
-    double dy = __dadd_rn(__dmul_rn(vel[1], dt), 0.);
+    double dy = __dadd_rn(__dmul_rn(vel[1], dt), fr);
     F.position[i] = make_double2(add_mul_rn(p.x, vel[0], dt), __dadd_rn(p.y, dy));
 }
 
@@ -128,6 +132,7 @@ __device__ __forceinline__ void tool_state_move(ToolDev *tool, double dt) {
     tool->br_point[1] = add_mul_rn(tool->br_point[1], vy, dt);
     tool->lowest_point = add_mul_rn(tool->lowest_point, vy, dt);
     tool->right_point = add_mul_rn(tool->right_point, vx, dt);
+    tool->flank_contact = tool->lowest_point;   // tool_FEM.cu:1567-1569
 }
 
 // what = 1: segments only; 2: nodes + tool state only; 3: both.  With
@@ -138,18 +143,17 @@ __global__ void __launch_bounds__(kBlock) k_tool_move(KConsts K, SegDev seg, Fem
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if ((what & 1) && i < seg.n) {
         const ToolDev &tc = tool[(per_case && K.case_of_seg) ? K.case_of_seg[i] : 0];
-        segment_move(seg, i, tc.vel, per_case ? tc.dt : dt);
+        segment_move(seg, i, tc.vel, per_case ? tc.dt : dt, tc.flank_retreat);
     }
     if ((what & 2) && i < F.n_nodes) {
         const ToolDev &tc = tool[(per_case && K.case_of_node) ? K.case_of_node[i] : 0];
-        node_move(F, i, tc.vel, per_case ? tc.dt : dt);
+        node_move(F, i, tc.vel, per_case ? tc.dt : dt, tc.flank_retreat);
     }
     if ((what & 2) && i < (per_case ? K.n_cases : 1)) tool_state_move(tool + i, per_case ? tool[i].dt : dt);
     if ((what & 1) && i < (per_case ? K.n_cases : 1)) {   // the segments' y-range, with segment_move's arithmetic
         const double dtc = per_case ? tool[i].dt : dt;
-        const double dy = __dadd_rn(__dmul_rn(tool[i].vel[1], dtc), 0.);
-        tool[i].seg_ymin = __dadd_rn(tool[i].seg_ymin, dy);
-        tool[i].seg_ymax = __dadd_rn(tool[i].seg_ymax, dy);
+        tool[i].seg_ymin = seg_y_move(tool[i].seg_ymin, tool[i].vel[1], dtc, tool[i].flank_retreat);
+        tool[i].seg_ymax = seg_y_move(tool[i].seg_ymax, tool[i].vel[1], dtc, tool[i].flank_retreat);
         tool[i].seg_xmax = add_mul_rn(tool[i].seg_xmax, tool[i].vel[0], dtc);
     }
 }

@@ -112,7 +112,7 @@ __device__ __forceinline__ void fused_epilogue(int k, const KConsts &K, const So
     uint32_t st = 0;
     // friction heat (actions_gpu.cu:345-420), tool runs only
     if (K.has_tool) st |= fric_heat_one(K, K.dt, tool->vel, vel, B.ft[k], B.n[k], B.fc[k], rho, B.eps_pl[k], B.on_seg[k],
-                                        seg.n, T, blanked, seg.fric_heat);
+                                        seg.n, T, blanked, seg.fric_heat, seg.wear);
     else if (K.rigid && !is_tool && K.c.trml_wp.eta != 0.)   // actions_gpu.cu:316-343
         rigid_fric_heat_one(K, dt, K.rigid->vel, vel, B.ft[k], B.n[k], T);
     // return mapping (actions_gpu.cu:689-754)
@@ -194,7 +194,7 @@ __device__ __forceinline__ void fused_epilogue32(int k, const KConsts &K, const 
         if (on >= 0 && on < seg.n) {
             double Td = (double)T, bl = 0.;
             st |= fric_heat_one(K, dt, tc.vel, make_double2(vel.x, vel.y), B.ft[k], B.n[k], B.fc[k], rho,
-                                B.eps_pl[k], on, seg.n, Td, bl, seg.fric_heat);
+                                B.eps_pl[k], on, seg.n, Td, bl, seg.fric_heat, seg.wear);
             T = (float)Td;
             blanked = flag_is_one(bl);
         }

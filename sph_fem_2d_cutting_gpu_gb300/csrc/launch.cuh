@@ -75,6 +75,11 @@ void launch_fem_temp(cudaStream_t s, const FemDev &F, const double *T_old, doubl
 void launch_tool_move(cudaStream_t s, const KConsts &K, const SegDev &seg, const FemDev &F, ToolDev *tool, double dt,
                       int what, bool per_case);
 
+// wear.cu
+void launch_wear_reset(cudaStream_t s, const SegDev &seg);
+void launch_wear_adjustment(cudaStream_t s, const KConsts &K, const FemDev &F, const SegDev &seg, const WearDev &W,
+                            ToolDev *tool, double dt);
+
 // mlp.cu
 size_t mlp_fwd_smem();
 size_t mlp_train_smem();

@@ -162,8 +162,7 @@ __device__ __forceinline__ uint32_t plasticity_one(const KConsts &K, dbl4 &S, do
 __device__ __forceinline__ uint32_t fric_heat_one(const KConsts &K, double dt, const double *vel_tool, double2 vel,
                                                   double2 ft, double2 nrm, double2 fc, double rho, double eps_pl,
                                                   int seg, int n_seg, double &T, double &blanked,
-                                                  double *__restrict__ fric_heat) {
-    (void)fc; (void)rho;
+                                                  double *__restrict__ fric_heat, const WearAcc &wear) {
     if (blanked == 1.) return 0u;
     if (eps_pl > 20.) return 0u;
     double f_fric_mag = sqrtf_d(ft.x * ft.x + ft.y * ft.y);
@@ -182,9 +181,24 @@ __device__ __forceinline__ uint32_t fric_heat_one(const KConsts &K, double dt, c
     double T_buffer = T + value * (1 - partition_wp) * dt / K.c.trml_wp.cp / K.c.phys.mass;
     if (T_buffer > 1550.) {
         T = 1550.;
-    } else {
-        T = T_buffer;
-        atomicAdd(fric_heat + seg, value * partition_wp);
+        return 0u;
+    }
+    T = T_buffer;
+    atomicAdd(fric_heat + seg, value * partition_wp);
+    if (wear.pp) {   // WEAR_NODE_SHIFT statistics (actions_gpu.cu:401-419)
+        const int4 mk = wear.marks[seg];
+        const double T_seg = 0.5 * (wear.T_nodes[mk.z] + wear.T_nodes[mk.w]);
+        const double vel_tool_norm = sqrt(vel_tool[0] * vel_tool[0] + vel_tool[1] * vel_tool[1]);
+        if (v_rel_mag > 0.008) return 0u;
+        if (v_rel_mag > vel_tool_norm * 8.0 && fabs(nrm.y) > 0.5) return 0u;   // around the flank face
+        const double f_normal = sqrtf_d(fc.x * fc.x + fc.y * fc.y);
+        const double length = sqrtf_d(K.c.tool.slave_mass / rho);
+        const double pressure_trial = f_normal / length;
+        atomicAdd(&wear.pp[seg].x, 1.);
+        atomicAdd(&wear.pp[seg].y, pressure_trial);
+        atomicAdd(&wear.pp[seg].z, v_rel_mag);
+        atomicAdd(&wear.pp[seg].w, T_seg);
+        atomicAdd(wear.sf + seg, f_fric_mag / length);
     }
     return 0u;
 }

@@ -53,6 +53,8 @@ struct SegDev {
     int4 *marks;              // element, colour, node left, node right
     double2 *heat_exchange;   // (sum T*length, sum length)
     double *fric_heat;
+    WearAcc wear;             // wear statistics (pp == NULL: off)
+    double *wear_rate;        // wear_nodes: per-segment wear rate of the last nodal shift
 };
 
 // FEM thermal system of the tool (FEM_thermal_2D_GPU, FEM_thermal_gpu.h:35-93).
@@ -66,6 +68,22 @@ struct FemDev {
     double *K, *M_inv, *f, *T, *k;
     double *T_half;                      // T after calculate_temp(0.5 dt)
     int32_t *node_seg_ptr, *node_seg;    // segments whose left/right node is this node
+    double *M;                           // lumped mass (m_mass_matrix); allocated with wear only
+};
+
+// Wear by nodal shift: the nodes of the two cutting-edge layers, each with its
+// layer elements (x: element, y: the node's local index) and the CSR slots of
+// (node, element node b), b = 0..2, for the atomic-free retreat / resume of the
+// layers' mass and stiffness; the per-segment node shifts; the wear constants.
+struct WearDev {
+    int n_nodes;                         // nodes of layer elements
+    const int32_t *node;                 // [n_nodes] node ids
+    const int32_t *adj_ptr;              // [n_nodes + 1]
+    const int4 *adj;                     // (element, local index)
+    const int4 *slot;                    // CSR slots (x, y, z)
+    const int4 *elements;                // [n_elements] node a, b, c, colour
+    dbl4 *seg_delta;                     // [n_seg] shift of the left (x, y) and right (z, w) node
+    double A, B, C, D;                   // wear constants (constants_structs.h:113-119)
 };
 
 struct StepScratch {

@@ -10,6 +10,7 @@
 //    inverse: FEM_thermal_gpu.cu:71-109,126-225,234-332, executed in the
 //    reference's colour-by-colour order on one host thread.
 #include "toolsetup.h"
+#include "p1elem.h"
 
 #include <algorithm>
 #include <cfloat>
@@ -158,7 +159,6 @@ int build_tool_model(const sph_tool_mesh &mesh, const sph_tool_constants &tc, To
     M.K.assign(NZ, 0.);
     M.M.assign(NN, 0.);
     M.f.assign(NN, 0.);
-    const double weights = 1. / 3. * 0.5;
     auto csr_add = [&](int row, int col, double v) {
         for (int j = M.row_ptr[row]; j < M.row_ptr[row + 1]; j++)
             if (M.col_ind[j] == col) {
@@ -171,25 +171,8 @@ int build_tool_model(const sph_tool_mesh &mesh, const sph_tool_constants &tc, To
             const Int4 el = M.elements[e];
             if (el.w != colour) continue;
             V2 p0 = node(el.x), p1 = node(el.y), p2 = node(el.z);
-            // jacobian columns: x1 - x0, x2 - x0
-            double j00 = p1.x - p0.x, j01 = p1.y - p0.y, j10 = p2.x - p0.x, j11 = p2.y - p0.y;
-            double det_signed = j00 * j11 - j10 * j01;
-            double determinant = std::fabs(det_signed);
-            // lumped mass (do_mass_ele_matrix_construction_p1q3)
-            double mvalue = weights * tc.cp * tc.rho * determinant;
-            // physical gradients of (1-xi-eta, xi, eta): J^-T * grad_ref
-            double inv = 1.0 / det_signed;
-            // J = [[j00, j10], [j01, j11]] (rows x, y; columns xi, eta); J^-T = inv*[[j11, -j01], [-j10, j00]]
-            double gref[3][2] = {{-1., -1.}, {1., 0.}, {0., 1.}};
-            double g[3][2];
-            for (int a = 0; a < 3; a++) {
-                g[a][0] = inv * (j11 * gref[a][0] - j01 * gref[a][1]);
-                g[a][1] = inv * (-j10 * gref[a][0] + j00 * gref[a][1]);
-            }
-            double s = weights * 3. * (tc.k * determinant);
-            double ke[3][3];
-            for (int a = 0; a < 3; a++)
-                for (int b = 0; b < 3; b++) ke[a][b] = s * (g[a][0] * g[b][0] + g[a][1] * g[b][1]);
+            double mvalue, ke[3][3];
+            p1_element(p0.x, p0.y, p1.x, p1.y, p2.x, p2.y, tc.cp, tc.rho, tc.k, mvalue, ke);
             M.M[el.x] += mvalue;
             M.M[el.y] += mvalue;
             M.M[el.z] += mvalue;
@@ -383,6 +366,46 @@ int build_tool_model(const sph_tool_mesh &mesh, const sph_tool_constants &tc, To
     for (int i = 0; i < NN; i++) {
         for (int s : ns[i]) M.node_seg.push_back(s);
         M.node_seg_ptr[i + 1] = (int)M.node_seg.size();
+    }
+    // ---- wear layers (mesh_structure_GPU.cu:1063-1148): layer 1 = elements with a
+    // cutting edge; layer 2 = the other elements that share a node with layer 1
+    // (a node on the cutting edge is always such a node) -------------------------
+    M.layer.assign(NE, Int4{0, 0, 0, 0});
+    std::vector<char> near_cut(NN, 0);
+    for (int e : cut_elems) {
+        M.layer[e].x = 1;
+        near_cut[M.elements[e].x] = near_cut[M.elements[e].y] = near_cut[M.elements[e].z] = 1;
+    }
+    for (int e = 0; e < NE; e++) {
+        const Int4 el = M.elements[e];
+        if (!M.layer[e].x && (near_cut[el.x] || near_cut[el.y] || near_cut[el.z])) M.layer[e].y = 1;
+    }
+    // per node of a layer element: its layer elements (ascending), the node's
+    // local index there and the CSR slots of (node, node_b), b = 0..2
+    M.wear_node.clear();
+    M.wear_adj_ptr.assign(1, 0);
+    M.wear_adj.clear();
+    M.wear_slot.clear();
+    auto slot_of = [&](int row, int col) {
+        for (int t = M.row_ptr[row]; t < M.row_ptr[row + 1]; t++)
+            if (M.col_ind[t] == col) return t;
+        return -1;
+    };
+    for (int i = 0; i < NN; i++) {
+        bool any = false;
+        for (int e : node_elems[i]) {
+            if (!M.layer[e].x && !M.layer[e].y) continue;
+            const Int4 el = M.elements[e];
+            const int nd[3] = {el.x, el.y, el.z};
+            const int a = (nd[0] == i) ? 0 : (nd[1] == i ? 1 : 2);
+            M.wear_adj.push_back(Int4{e, a, 0, 0});
+            M.wear_slot.push_back(Int4{slot_of(i, nd[0]), slot_of(i, nd[1]), slot_of(i, nd[2]), 0});
+            any = true;
+        }
+        if (any) {
+            M.wear_node.push_back(i);
+            M.wear_adj_ptr.push_back((int)M.wear_adj.size());
+        }
     }
     return SPH_OK;
 }

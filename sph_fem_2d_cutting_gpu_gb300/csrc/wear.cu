@@ -1,0 +1,166 @@
+// wear.cu -- tool wear by nodal shift (WEAR_NODE_SHIFT): wear_adjustment of the
+// reference (actions_gpu.cu:1009-1020) on the device.
+//
+// The reference adds and removes the element matrices of the two cutting-edge
+// layers colour by colour (do_mesh_adjustment_wear, FEM_thermal_gpu.cu:476-577)
+// and shifts the nodes with atomics (tool_FEM.cu:423-430).  Here every node of
+// a layer element gathers the contributions of its own layer elements into its
+// own mass entry and CSR row, and every cutting-edge node adds the shifts of
+// the segments ending on it in segment order: the same sums, without atomics
+// or colour launches, in a fixed order.
+#include "launch.cuh"
+#include "p1elem.h"
+
+namespace sphfem {
+
+// Element e's lumped mass and stiffness at the current node positions.
+__device__ __forceinline__ void layer_element(const KConsts &K, const FemDev &F, const WearDev &W, int e, double &m,
+                                              double ke[3][3]) {
+    const int4 el = W.elements[e];
+    const double2 p0 = F.position[el.x], p1 = F.position[el.y], p2 = F.position[el.z];
+    p1_element(p0.x, p0.y, p1.x, p1.y, p2.x, p2.y, K.c.tool.cp, K.c.tool.rho, K.c.tool.k, m, ke);
+}
+
+// mesh_retreat_wear (sign -1) / mesh_resume_wear (sign +1) for the layer nodes
+// (FEM_thermal_gpu.cu:923-950); the resume also rebuilds the lumped inverse
+// mass of the node (do_inverse_mass_matrix_lumped, FEM_thermal_gpu.cu:326-331:
+// the other nodes' entries do not change).
+__global__ void __launch_bounds__(kBlock) k_wear_layers(KConsts K, FemDev F, WearDev W, double sign, int resume) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= W.n_nodes) return;
+    const int i = W.node[idx];
+    double Mi = F.M[i];
+    for (int t = W.adj_ptr[idx]; t < W.adj_ptr[idx + 1]; t++) {
+        const int4 ad = W.adj[t];
+        double m, ke[3][3];
+        layer_element(K, F, W, ad.x, m, ke);
+        Mi += sign * m;
+        const int4 sl = W.slot[t];
+        const int a = ad.y;
+        F.K[sl.x] += sign * ke[a][0];
+        F.K[sl.y] += sign * ke[a][1];
+        F.K[sl.z] += sign * ke[a][2];
+    }
+    F.M[i] = Mi;
+    if (resume) F.M_inv[i] = 1. / Mi;
+}
+
+// do_nodal_shift_wear_smooth_temp (tool_FEM.cu:299-432) with RESTRICT_WEAR_TEMP and
+// USE_USUI_RAKE_FLANK, one segment per thread: the wear depth of its left and
+// right node from the segment's mean pressure and sliding speed and the nodal
+// temperatures, and the shift along the segment normal (nodal_shift,
+// tool_FEM.cu:49-55).  The shift is applied by k_wear_node_shift.
+__global__ void __launch_bounds__(kBlock) k_wear_segment_shift(FemDev F, SegDev seg, WearDev W, double dt) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= seg.n) return;
+    W.seg_delta[s] = mk4(0., 0., 0., 0.);
+    const dbl4 w = seg.wear.pp[s];
+    if (w.x == 0.) return;
+    const int4 mk = seg.marks[s];
+    double pressure = w.y / w.x;
+    double vel = w.z / w.x;
+    double Tl = F.T[mk.z], Tr = F.T[mk.w];
+    if (vel > 0.008) return;
+    Tl = fmin(Tl, 1350.);
+    Tr = fmin(Tr, 1350.);
+    vel = fmin(vel, 0.008);
+    pressure = fmin(pressure, 0.04);
+    const double2 n = seg.normal[s];
+    double wl, wr;
+    if (fabs(n.x) > 0.85) {   // rake face
+        wl = dt * W.C * pressure * vel * exp(-W.D / Tl);
+        wr = dt * W.C * pressure * vel * exp(-W.D / Tr);
+    } else {                  // flank face
+        wl = dt * W.A * pressure * vel * exp(-W.B / Tl);
+        wr = dt * W.A * pressure * vel * exp(-W.B / Tr);
+    }
+    seg.wear_rate[s] = (wl + wr) / dt;
+    W.seg_delta[s] = mk4(n.x * wl, n.y * wl, n.x * wr, n.y * wr);
+}
+
+// Each node adds the shifts of the segments ending on it, in segment order.
+__global__ void __launch_bounds__(kBlock) k_wear_node_shift(FemDev F, SegDev seg, WearDev W) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F.n_nodes) return;
+    const int t0 = F.node_seg_ptr[i], t1 = F.node_seg_ptr[i + 1];
+    if (t0 == t1) return;
+    double2 p = F.position[i];
+    for (int t = t0; t < t1; t++) {
+        const int s = F.node_seg[t];
+        const int4 mk = seg.marks[s];
+        const dbl4 d = W.seg_delta[s];
+        if (mk.z == i) {
+            p.x += d.x;
+            p.y += d.y;
+        }
+        if (mk.w == i) {
+            p.x += d.z;
+            p.y += d.w;
+        }
+    }
+    F.position[i] = p;
+}
+
+// do_segment_wear_update (tool_FEM.cu:520-545): segments follow their nodes;
+// do_correct_flank_contact (tool_FEM.cu:559-587): flank_retreat = flank_contact
+// - the lowest left end among the first 512 segments (the reference reduces
+// over one block of 512 threads); and the segments' bounds that the contact
+// search's exact prefilters use.  One block.
+constexpr int kFlankSegments = 512;
+__global__ void __launch_bounds__(1024) k_wear_segments_flank(FemDev F, SegDev seg, ToolDev *tool) {
+    __shared__ double s_min[1024], s_ymin[1024], s_ymax[1024], s_xmax[1024], s_dxdy[1024];
+    double mn = 3.402823466385288598e38, ymin = INFINITY, ymax = -INFINITY, xmax = -INFINITY, dxdy = 0.;
+    for (int s = threadIdx.x; s < seg.n; s += blockDim.x) {
+        const int4 mk = seg.marks[s];
+        const double2 l = F.position[mk.z], r = F.position[mk.w];
+        seg.left[s] = l;
+        seg.right[s] = r;
+        const double dx = r.x - l.x, dy = r.y - l.y;
+        const double inv = 1. / sqrt(dy * dy + dx * dx);   // glm::normalize(vec2(dy, -dx))
+        seg.normal[s] = make_double2(dy * inv, -dx * inv);
+        if (s < kFlankSegments) mn = fmin(mn, l.y);
+        ymin = fmin(ymin, fmin(l.y, r.y));
+        ymax = fmax(ymax, fmax(l.y, r.y));
+        xmax = fmax(xmax, fmax(l.x, r.x));
+        if (l.y != r.y) dxdy = fmax(dxdy, 1.01 * fabs(l.x - r.x) / fabs(l.y - r.y));
+    }
+    const int t = threadIdx.x;
+    s_min[t] = mn; s_ymin[t] = ymin; s_ymax[t] = ymax; s_xmax[t] = xmax; s_dxdy[t] = dxdy;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (t < o) {
+            s_min[t] = fmin(s_min[t], s_min[t + o]);
+            s_ymin[t] = fmin(s_ymin[t], s_ymin[t + o]);
+            s_ymax[t] = fmax(s_ymax[t], s_ymax[t + o]);
+            s_xmax[t] = fmax(s_xmax[t], s_xmax[t + o]);
+            s_dxdy[t] = fmax(s_dxdy[t], s_dxdy[t + o]);
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        tool->flank_retreat = tool->flank_contact - s_min[0];
+        tool->seg_ymin = s_ymin[0];
+        tool->seg_ymax = s_ymax[0];
+        tool->seg_xmax = s_xmax[0];
+        tool->seg_dxdy = s_dxdy[0];
+    }
+}
+
+// ---- host launchers -------------------------------------------------------------------------------
+void launch_wear_reset(cudaStream_t s, const SegDev &seg) {
+    cudaMemsetAsync(seg.wear.pp, 0, sizeof(dbl4) * (size_t)seg.n, s);
+    cudaMemsetAsync(seg.wear.sf, 0, sizeof(double) * (size_t)seg.n, s);
+    cudaMemsetAsync(seg.wear_rate, 0, sizeof(double) * (size_t)seg.n, s);
+}
+
+void launch_wear_adjustment(cudaStream_t s, const KConsts &K, const FemDev &F, const SegDev &seg, const WearDev &W,
+                            ToolDev *tool, double dt) {
+    const int gl = div_up(W.n_nodes > 0 ? W.n_nodes : 1, kBlock);
+    k_wear_layers<<<gl, kBlock, 0, s>>>(K, F, W, -1., 0);
+    k_wear_segment_shift<<<div_up(seg.n > 0 ? seg.n : 1, kBlock), kBlock, 0, s>>>(F, seg, W, dt);
+    k_wear_node_shift<<<div_up(F.n_nodes, kBlock), kBlock, 0, s>>>(F, seg, W);
+    k_wear_layers<<<gl, kBlock, 0, s>>>(K, F, W, 1., 1);
+    k_wear_segments_flank<<<1, 1024, 0, s>>>(F, seg, tool);
+}
+
+}  // namespace sphfem

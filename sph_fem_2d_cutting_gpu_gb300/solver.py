@@ -215,6 +215,25 @@ class Solver:
         self._ck(self.lib.sph_get_rigid_tool(self.ctx, C.byref(t)), "sph_get_rigid_tool")
         return t
 
+    # ---- tool wear by nodal shift (WEAR_NODE_SHIFT) ------------------------------------------
+    def set_wear(self, mode: int, constants: abi.WearConstants | None = None):
+        self._ck(self.lib.sph_set_wear(self.ctx, int(mode), C.byref(constants) if constants is not None else None),
+                 "sph_set_wear")
+
+    def wear_state(self) -> dict:
+        seg_n = self.tool_state().n_segments
+        f = abi.Fem()
+        self._ck(self.lib.sph_get_fem(self.ctx, C.byref(f)), "sph_get_fem")
+        nn = f.n_nodes
+        ne = self.case.tool_mesh["elements"].shape[0] if self.case.tool_mesh is not None else 0
+        out = dict(elements=np.zeros((ne, 4), np.int32), layer=np.zeros((ne, 2), np.int32), M=np.zeros(nn),
+                   phys_para=np.zeros((seg_n, 4)), sliding_force=np.zeros(seg_n), wear_nodes=np.zeros(seg_n))
+        w = abi.WearState()
+        for k, v in out.items():
+            setattr(w, k, abi.ptr(v))
+        self._ck(self.lib.sph_download_wear(self.ctx, C.byref(w)), "sph_download_wear")
+        return out
+
     def set_thermal_model(self, model: int):
         self._ck(self.lib.sph_set_thermal_model(self.ctx, int(model)), "sph_set_thermal_model")
 
