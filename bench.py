@@ -268,6 +268,19 @@ def run_small_cut(args, local):
         ms = e0.elapsed_time(e1) / steps
         row[name] = {"ms_per_step": ms, "value": case.N / (ms * 1e-3),
                      "launches_per_step": (s.launch_count() - n0) / steps, "status": s.status()}
+        # the same step with tool wear by nodal shift (WEAR_NODE_SHIFT, after wear_pro)
+        s.set_wear(abi.SPH_WEAR_SHIFT, abi.WearConstants(10.0, 300.0, 10.0, 300.0))
+        s.step(args.warmup)
+        s.sync()
+        n0 = s.launch_count()
+        e0.record(ext)
+        s.step(steps)
+        e1.record(ext)
+        e1.synchronize()
+        msw = e0.elapsed_time(e1) / steps
+        row[name + "_wear"] = {"ms_per_step": msw, "value": case.N / (msw * 1e-3),
+                               "launches_per_step": (s.launch_count() - n0) / steps, "status": s.status()}
+        s.set_wear(abi.SPH_WEAR_OFF, None)
         if prec == abi.SPH_PREC_FP64 and not args.no_cpu:
             P = s.download()
             ts = s.tool_state()

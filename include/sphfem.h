@@ -347,6 +347,9 @@ int sph_eval_usui(sph_ctx *ctx, double K_usui, double alpha, const double tool_v
  * "%.9g %.9g\n" of sph_reduce_force (mfree_gpu.cpp:336-338). */
 int sph_write_vtk_particles(sph_ctx *ctx, const char *path);
 int sph_write_vtk_tool(sph_ctx *ctx, const char *path, const double *tl_ref);
+/* vtk_writer.cu:368-516 (WEAR_NODE_SHIFT builds): the contact segments with
+ * the wear statistics of the last step (see sph_set_wear). */
+int sph_write_vtk_segments(sph_ctx *ctx, const char *path);
 int sph_append_force_log(sph_ctx *ctx, const char *path);
 
 /* ---- pipelined host I/O ------------------------------------------------------------

@@ -255,6 +255,7 @@ def load() -> C.CDLL:
         "sph_upload_particles_async": ([P, C.POINTER(Particles)], C.c_int),
         "sph_write_vtk_particles": ([P, C.c_char_p], C.c_int),
         "sph_write_vtk_tool": ([P, C.c_char_p, PD], C.c_int),
+        "sph_write_vtk_segments": ([P, C.c_char_p], C.c_int),
         "sph_append_force_log": ([P, C.c_char_p], C.c_int),
         "sph_eval_usui": ([P, D, D, PD, D, PD, PD], C.c_int),
         "sph_download_particles_async": ([P, C.POINTER(Particles)], C.c_int),

@@ -384,7 +384,7 @@ int issue_fused_body(sph_ctx *ctx, int64_t &n, int w) {
         n += 1;
         if (ctx->wear_mode == SPH_WEAR_SHIFT) {   // wear_adjustment (leap_frog.cu:224-229)
             launch_wear_adjustment(s, ctx->K, ctx->fem, ctx->seg, ctx->wear, ctx->tool_dev, ctx->K.dt);
-            n += 5;
+            n += 6;
         }
         launch_tool_move(s, ctx->K, ctx->seg, ctx->fem, ctx->tool_dev, ctx->K.dt, 3, true);
         n += 1;
@@ -1898,6 +1898,60 @@ int sph_write_vtk_tool(sph_ctx *ctx, const char *path, const double *tl_ref) {
     return SPH_OK;
 }
 
+// vtk_writer.cu:368-516 vtk_writer_write_FEM_segments: every contact segment as a
+// triangle (left, right, and right + |segment| n), with the wear statistics on
+// the third point: mean pressure (GPa), sliding speed (m/s), segment
+// temperature, frictional stress and wear rate (1e10 x).  Without gathered
+// statistics the wear fields are zero.
+int sph_write_vtk_segments(sph_ctx *ctx, const char *path) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    if (!path) return SPH_ERR_INVALID;
+    const int ns = ctx->seg.n;
+    std::vector<double> left(2 * (size_t)ns), right(2 * (size_t)ns), n(2 * (size_t)ns), wear(4 * (size_t)ns, 0.),
+        sf(ns, 0.), wr(ns, 0.);
+    CK(cudaMemcpyAsync(left.data(), ctx->seg.left, 16 * (size_t)ns, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(right.data(), ctx->seg.right, 16 * (size_t)ns, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(n.data(), ctx->seg.normal, 16 * (size_t)ns, cudaMemcpyDeviceToHost, ctx->stream));
+    if (ctx->wear_ready) {
+        CK(cudaMemcpyAsync(wear.data(), ctx->wear_pp, 32 * (size_t)ns, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(sf.data(), ctx->wear_sf, 8 * (size_t)ns, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(wr.data(), ctx->seg.wear_rate, 8 * (size_t)ns, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    FILE *fp = fopen(path, "w");
+    if (!fp) return fail(ctx, SPH_ERR_INVALID, std::string("cannot open ") + path);
+    fprintf(fp, "# vtk DataFile Version 2.0\nmfree iwf\nASCII\n\nDATASET UNSTRUCTURED_GRID\nPOINTS %d float\n", 3 * ns);
+    for (int i = 0; i < ns; i++) {
+        const double lx = left[2 * i], ly = left[2 * i + 1], rx = right[2 * i], ry = right[2 * i + 1];
+        fprintf(fp, "%f %f %f\n", lx, ly, 0.);
+        fprintf(fp, "%f %f %f\n", rx, ry, 0.);
+        const double dis = sqrt((lx - rx) * (lx - rx) + (ly - ry) * (ly - ry));
+        fprintf(fp, "%f %f %f\n", rx + dis * n[2 * i], ry + dis * n[2 * i + 1], 0.);
+    }
+    fprintf(fp, "\nCELLS %d %d\n", ns, 4 * ns);
+    for (int i = 0; i < ns; i++) fprintf(fp, "3 %d %d %d \n", 3 * i, 3 * i + 1, 3 * i + 2);
+    fprintf(fp, "\nCELL_TYPES %d\n", ns);
+    for (int i = 0; i < ns; i++) fprintf(fp, "5\n");
+    fprintf(fp, "POINT_DATA %d\n", 3 * ns);
+    // a segment's value on its third point, 0 where no particle contributed
+    auto field = [&](const char *name, auto value) {
+        fprintf(fp, "SCALARS %s float 1\nLOOKUP_TABLE default\n", name);
+        for (int i = 0; i < ns; i++) {
+            fprintf(fp, "%f\n%f\n", 0., 0.);
+            fprintf(fp, "%f\n", wear[4 * i] != 0. ? value(i) : 0.);
+        }
+        fprintf(fp, "\n");
+    };
+    field("PressureGPa", [&](int i) { return wear[4 * i + 1] / wear[4 * i] * 100.; });
+    field("Velocity", [&](int i) { return wear[4 * i + 2] / wear[4 * i] * 10000.; });
+    field("Temperature", [&](int i) { return wear[4 * i + 3] / wear[4 * i]; });
+    field("Frictional_stress", [&](int i) { return sf[i] / wear[4 * i] * 100.; });
+    field("Wear_rate", [&](int i) { return wr[i] * 1e10; });
+    if (fclose(fp) != 0) return fail(ctx, SPH_ERR_INVALID, std::string("cannot write ") + path);
+    return SPH_OK;
+}
+
 int sph_append_force_log(sph_ctx *ctx, const char *path) {
     REQUIRE_CTX();
     if (!path) return SPH_ERR_INVALID;
@@ -2068,6 +2122,13 @@ int wear_setup(sph_ctx *ctx) {
     DALLOC(slot, M.wear_slot.size());
     DALLOC(elements, M.elements.size());
     DALLOC(W.seg_delta, S.n);
+    int32_t *elem = nullptr;
+    DALLOC(elem, M.wear_elem.size());
+    DALLOC(W.mat_old, 10 * M.wear_elem.size());
+    DALLOC(W.mat_new, 10 * M.wear_elem.size());
+    if (!M.wear_elem.empty())
+        CK(cudaMemcpyAsync(elem, M.wear_elem.data(), sizeof(int32_t) * M.wear_elem.size(), cudaMemcpyHostToDevice,
+                           ctx->stream));
     CK(cudaMemsetAsync(ctx->wear_pp, 0, sizeof(dbl4) * S.n, ctx->stream));
     CK(cudaMemsetAsync(ctx->wear_sf, 0, sizeof(double) * S.n, ctx->stream));
     CK(cudaMemsetAsync(S.wear_rate, 0, sizeof(double) * S.n, ctx->stream));
@@ -2086,6 +2147,8 @@ int wear_setup(sph_ctx *ctx) {
     CK(cudaMemcpyAsync(elements, M.elements.data(), sizeof(int4) * M.elements.size(), cudaMemcpyHostToDevice,
                        ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    W.n_elem = (int)M.wear_elem.size();
+    W.elem = elem;
     W.n_nodes = (int)M.wear_node.size();
     W.node = node;
     W.adj_ptr = adj_ptr;
@@ -2138,7 +2201,7 @@ int sph_wear_adjustment(sph_ctx *ctx) {
     REQUIRE_TOOL();
     if (ctx->wear_mode != SPH_WEAR_SHIFT) return fail(ctx, SPH_ERR_STATE, "nodal-shift wear is off");
     launch_wear_adjustment(ctx->stream, ctx->K, ctx->fem, ctx->seg, ctx->wear, ctx->tool_dev, ctx->K.dt);
-    ctx->launches += 5;
+    ctx->launches += 6;
     ctx->counts_valid = false;
     CK_LAUNCH();
     return SPH_OK;

@@ -76,10 +76,13 @@ struct FemDev {
 // (node, element node b), b = 0..2, for the atomic-free retreat / resume of the
 // layers' mass and stiffness; the per-segment node shifts; the wear constants.
 struct WearDev {
+    int n_elem;                          // layer elements
+    const int32_t *elem;                 // [n_elem] element ids
+    double *mat_old, *mat_new;           // [n_elem][10]: lumped mass, stiffness (row-major) before / after the shift
     int n_nodes;                         // nodes of layer elements
     const int32_t *node;                 // [n_nodes] node ids
     const int32_t *adj_ptr;              // [n_nodes + 1]
-    const int4 *adj;                     // (element, local index)
+    const int4 *adj;                     // (layer element index, local index)
     const int4 *slot;                    // CSR slots (x, y, z)
     const int4 *elements;                // [n_elements] node a, b, c, colour
     dbl4 *seg_delta;                     // [n_seg] shift of the left (x, y) and right (z, w) node

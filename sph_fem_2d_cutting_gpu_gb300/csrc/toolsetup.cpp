@@ -380,8 +380,16 @@ int build_tool_model(const sph_tool_mesh &mesh, const sph_tool_constants &tc, To
         const Int4 el = M.elements[e];
         if (!M.layer[e].x && (near_cut[el.x] || near_cut[el.y] || near_cut[el.z])) M.layer[e].y = 1;
     }
-    // per node of a layer element: its layer elements (ascending), the node's
-    // local index there and the CSR slots of (node, node_b), b = 0..2
+    // the layer elements (ascending) and, per node of a layer element, its layer
+    // elements (index into that list), the node's local index there and the CSR
+    // slots of (node, node_b), b = 0..2
+    M.wear_elem.clear();
+    std::vector<int> compact(NE, -1);
+    for (int e = 0; e < NE; e++)
+        if (M.layer[e].x || M.layer[e].y) {
+            compact[e] = (int)M.wear_elem.size();
+            M.wear_elem.push_back(e);
+        }
     M.wear_node.clear();
     M.wear_adj_ptr.assign(1, 0);
     M.wear_adj.clear();
@@ -398,7 +406,7 @@ int build_tool_model(const sph_tool_mesh &mesh, const sph_tool_constants &tc, To
             const Int4 el = M.elements[e];
             const int nd[3] = {el.x, el.y, el.z};
             const int a = (nd[0] == i) ? 0 : (nd[1] == i ? 1 : 2);
-            M.wear_adj.push_back(Int4{e, a, 0, 0});
+            M.wear_adj.push_back(Int4{compact[e], a, 0, 0});
             M.wear_slot.push_back(Int4{slot_of(i, nd[0]), slot_of(i, nd[1]), slot_of(i, nd[2]), 0});
             any = true;
         }

@@ -24,11 +24,12 @@ struct ToolModelHost {
     std::vector<double> left, right, normal;   // [n_seg][2]
     std::vector<Int4> marks;                   // element, colour, node left, node right
     std::vector<int> node_seg_ptr, node_seg;   // segments ending on each node
-    // wear (WEAR_NODE_SHIFT): layer flags per element (x: layer 1, y: layer 2) and,
-    // per node of a layer element, its layer elements (x: element, y: local index)
-    // with the CSR slots of (node, element node b), b = 0..2 (x, y, z)
+    // wear (WEAR_NODE_SHIFT): layer flags per element (x: layer 1, y: layer 2), the
+    // layer elements, and per node of a layer element its layer elements
+    // (x: index into wear_elem, y: local index) with the CSR slots of
+    // (node, element node b), b = 0..2 (x, y, z)
     std::vector<Int4> layer;
-    std::vector<int> wear_node, wear_adj_ptr;
+    std::vector<int> wear_elem, wear_node, wear_adj_ptr;
     std::vector<Int4> wear_adj, wear_slot;
     // tool kinematics
     double tl_point_ref[2] = {0, 0}, br_point[2] = {0, 0};

@@ -13,36 +13,49 @@
 
 namespace sphfem {
 
-// Element e's lumped mass and stiffness at the current node positions.
-__device__ __forceinline__ void layer_element(const KConsts &K, const FemDev &F, const WearDev &W, int e, double &m,
-                                              double ke[3][3]) {
-    const int4 el = W.elements[e];
+// Lumped mass and stiffness of every layer element at the current node
+// positions (do_mass_ele_matrix_construction_p1q3 /
+// do_stiffness_ele_matrix_construction_p1q3), one element per thread.
+__global__ void __launch_bounds__(kBlock) k_wear_elements(KConsts K, FemDev F, WearDev W, double *__restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= W.n_elem) return;
+    const int4 el = W.elements[W.elem[k]];
     const double2 p0 = F.position[el.x], p1 = F.position[el.y], p2 = F.position[el.z];
+    double m, ke[3][3];
     p1_element(p0.x, p0.y, p1.x, p1.y, p2.x, p2.y, K.c.tool.cp, K.c.tool.rho, K.c.tool.k, m, ke);
+    double *o = out + 10 * (size_t)k;
+    o[0] = m;
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) o[1 + 3 * a + b] = ke[a][b];
 }
 
-// mesh_retreat_wear (sign -1) / mesh_resume_wear (sign +1) for the layer nodes
-// (FEM_thermal_gpu.cu:923-950); the resume also rebuilds the lumped inverse
-// mass of the node (do_inverse_mass_matrix_lumped, FEM_thermal_gpu.cu:326-331:
-// the other nodes' entries do not change).
-__global__ void __launch_bounds__(kBlock) k_wear_layers(KConsts K, FemDev F, WearDev W, double sign, int resume) {
+// mesh_retreat_wear then mesh_resume_wear (FEM_thermal_gpu.cu:923-950) for the
+// layer nodes: each node takes its layer elements' contributions at the old
+// positions out of its mass entry and CSR row, then puts them back at the new
+// positions, and rebuilds its lumped inverse mass (do_inverse_mass_matrix_lumped,
+// FEM_thermal_gpu.cu:326-331; the other nodes' entries do not change).
+__global__ void __launch_bounds__(kBlock) k_wear_layers(FemDev F, WearDev W) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= W.n_nodes) return;
     const int i = W.node[idx];
+    const int t0 = W.adj_ptr[idx], t1 = W.adj_ptr[idx + 1];
     double Mi = F.M[i];
-    for (int t = W.adj_ptr[idx]; t < W.adj_ptr[idx + 1]; t++) {
-        const int4 ad = W.adj[t];
-        double m, ke[3][3];
-        layer_element(K, F, W, ad.x, m, ke);
-        Mi += sign * m;
-        const int4 sl = W.slot[t];
-        const int a = ad.y;
-        F.K[sl.x] += sign * ke[a][0];
-        F.K[sl.y] += sign * ke[a][1];
-        F.K[sl.z] += sign * ke[a][2];
+    for (int pass = 0; pass < 2; pass++) {
+        const double sign = pass ? 1. : -1.;
+        const double *mat = pass ? W.mat_new : W.mat_old;
+        for (int t = t0; t < t1; t++) {
+            const int4 ad = W.adj[t];
+            const double *o = mat + 10 * (size_t)ad.x;
+            Mi += sign * o[0];
+            const int4 sl = W.slot[t];
+            const int a = ad.y;
+            F.K[sl.x] += sign * o[1 + 3 * a + 0];
+            F.K[sl.y] += sign * o[1 + 3 * a + 1];
+            F.K[sl.z] += sign * o[1 + 3 * a + 2];
+        }
     }
     F.M[i] = Mi;
-    if (resume) F.M_inv[i] = 1. / Mi;
+    F.M_inv[i] = 1. / Mi;
 }
 
 // do_nodal_shift_wear_smooth_temp (tool_FEM.cu:299-432) with RESTRICT_WEAR_TEMP and
@@ -107,8 +120,10 @@ __global__ void __launch_bounds__(kBlock) k_wear_node_shift(FemDev F, SegDev seg
 // over one block of 512 threads); and the segments' bounds that the contact
 // search's exact prefilters use.  One block.
 constexpr int kFlankSegments = 512;
-__global__ void __launch_bounds__(1024) k_wear_segments_flank(FemDev F, SegDev seg, ToolDev *tool) {
-    __shared__ double s_min[1024], s_ymin[1024], s_ymax[1024], s_xmax[1024], s_dxdy[1024];
+constexpr int kFlankThreads = 256;
+__global__ void __launch_bounds__(kFlankThreads) k_wear_segments_flank(FemDev F, SegDev seg, ToolDev *tool) {
+    __shared__ double s_min[kFlankThreads], s_ymin[kFlankThreads], s_ymax[kFlankThreads], s_xmax[kFlankThreads],
+        s_dxdy[kFlankThreads];
     double mn = 3.402823466385288598e38, ymin = INFINITY, ymax = -INFINITY, xmax = -INFINITY, dxdy = 0.;
     for (int s = threadIdx.x; s < seg.n; s += blockDim.x) {
         const int4 mk = seg.marks[s];
@@ -153,14 +168,18 @@ void launch_wear_reset(cudaStream_t s, const SegDev &seg) {
     cudaMemsetAsync(seg.wear_rate, 0, sizeof(double) * (size_t)seg.n, s);
 }
 
+// Few hundred threads of FP64 element work: blocks as small as needed to
+// spread them over the SMs (fp64_block).
 void launch_wear_adjustment(cudaStream_t s, const KConsts &K, const FemDev &F, const SegDev &seg, const WearDev &W,
                             ToolDev *tool, double dt) {
-    const int gl = div_up(W.n_nodes > 0 ? W.n_nodes : 1, kBlock);
-    k_wear_layers<<<gl, kBlock, 0, s>>>(K, F, W, -1., 0);
-    k_wear_segment_shift<<<div_up(seg.n > 0 ? seg.n : 1, kBlock), kBlock, 0, s>>>(F, seg, W, dt);
-    k_wear_node_shift<<<div_up(F.n_nodes, kBlock), kBlock, 0, s>>>(F, seg, W);
-    k_wear_layers<<<gl, kBlock, 0, s>>>(K, F, W, 1., 1);
-    k_wear_segments_flank<<<1, 1024, 0, s>>>(F, seg, tool);
+    const int ne = W.n_elem > 0 ? W.n_elem : 1, nl = W.n_nodes > 0 ? W.n_nodes : 1, ns = seg.n > 0 ? seg.n : 1;
+    const int be = fp64_block(ne), bl = fp64_block(nl), bs = fp64_block(ns), bn = fp64_block(F.n_nodes);
+    k_wear_elements<<<div_up(ne, be), be, 0, s>>>(K, F, W, W.mat_old);
+    k_wear_segment_shift<<<div_up(ns, bs), bs, 0, s>>>(F, seg, W, dt);
+    k_wear_node_shift<<<div_up(F.n_nodes, bn), bn, 0, s>>>(F, seg, W);
+    k_wear_elements<<<div_up(ne, be), be, 0, s>>>(K, F, W, W.mat_new);
+    k_wear_layers<<<div_up(nl, bl), bl, 0, s>>>(F, W);
+    k_wear_segments_flank<<<1, kFlankThreads, 0, s>>>(F, seg, tool);
 }
 
 }  // namespace sphfem

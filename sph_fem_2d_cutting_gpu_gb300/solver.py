@@ -122,6 +122,10 @@ class Solver:
         ref = None if tl_ref is None else np.ascontiguousarray(tl_ref, np.float64)
         self._ck(self.lib.sph_write_vtk_tool(self.ctx, str(path).encode(), abi.ptr(ref)), "sph_write_vtk_tool")
 
+    def write_vtk_segments(self, path: str):
+        """The contact segments with their wear statistics (vtk_writer_write_FEM_segments)."""
+        self._ck(self.lib.sph_write_vtk_segments(self.ctx, str(path).encode()), "sph_write_vtk_segments")
+
     def append_force_log(self, path: str):
         """One line 'fx fy' of the cutting force (the reference's force log)."""
         self._ck(self.lib.sph_append_force_log(self.ctx, str(path).encode()), "sph_append_force_log")

@@ -181,3 +181,35 @@ def test_wear_api_errors(lib):
     s.set_wear(abi.SPH_WEAR_ACCUMULATE, None)    # statistics need no constants
     with pytest.raises(SphError):
         s.wear_adjustment()                      # only in the shift mode
+
+
+def test_segment_vtk_carries_wear_fields(lib, tmp_path):
+    """vtk_writer_write_FEM_segments (vtk_writer.cu:368-516): each segment as a
+    triangle left, right, right + |segment| n; the wear fields on its third point."""
+    c, s, o = wear_pair(abi.SPH_WEAR_SHIFT)
+    s.step(5)
+    path = tmp_path / "seg.vtk"
+    s.write_vtk_segments(path)
+    seg, w = s.segments(), s.wear_state()
+    ns = len(seg["left"])
+    lines = path.read_text().splitlines()
+    i = lines.index(f"POINTS {3 * ns} float")
+    pts = np.array([[float(v) for v in lines[i + 1 + k].split()] for k in range(3 * ns)])
+    np.testing.assert_allclose(pts[0::3, :2], seg["left"], atol=1e-6)
+    np.testing.assert_allclose(pts[1::3, :2], seg["right"], atol=1e-6)
+    length = np.linalg.norm(seg["left"] - seg["right"], axis=1)
+    np.testing.assert_allclose(pts[2::3, :2], seg["right"] + length[:, None] * seg["normal"], atol=1e-6)
+
+    def field(name):
+        j = lines.index(f"SCALARS {name} float 1")
+        return np.array([float(v) for v in lines[j + 2:j + 2 + 3 * ns]])
+
+    pp = w["phys_para"]
+    hit = pp[:, 0] != 0
+    assert hit.any()
+    p = field("PressureGPa")
+    assert np.all(p[0::3] == 0) and np.all(p[1::3] == 0)
+    np.testing.assert_allclose(p[2::3][hit], pp[hit, 1] / pp[hit, 0] * 100.0, rtol=1e-5, atol=1e-6)
+    assert np.all(p[2::3][~hit] == 0)
+    np.testing.assert_allclose(field("Temperature")[2::3][hit], pp[hit, 3] / pp[hit, 0], rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(field("Wear_rate")[2::3][hit], w["wear_nodes"][hit] * 1e10, rtol=1e-5, atol=1e-6)
