@@ -641,11 +641,12 @@ def run_product(args):
 
             pipelined(max(2, args.warmup))
             barrier()
-            t0 = time.perf_counter()
-            pipelined(args.steps)
+            n_e2e = max(args.steps, args.e2e_steps)   # a stream of requests: the first upload and
+            t0 = time.perf_counter()                  # the last download are not overlapped
+            pipelined(n_e2e)
             el = max_over_ranks(time.perf_counter() - t0)
-            res["e2e"] = dict(value=world * case.N * args.steps / el, unit=UNIT, h2d_bytes_per_step=nbytes,
-                              d2h_bytes_per_step=nbytes,
+            res["e2e"] = dict(value=world * case.N * n_e2e / el, unit=UNIT, h2d_bytes_per_step=nbytes,
+                              d2h_bytes_per_step=nbytes, requests=n_e2e,
                               api="sph_upload_particles_async + sph_step + sph_download_particles_async")
             res["e2e_sync"] = e2e_sync
         res["clocks"] = clocks.stop() if clocks else None
@@ -781,6 +782,8 @@ def main():
     ap.add_argument("--ref-side", type=int, default=1024)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=40,
+                    help="requests in the timed pipelined end-to-end stream (at least --steps)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--batched-cases", type=int, default=64, help="cases of the batched sweep (0: skip)")

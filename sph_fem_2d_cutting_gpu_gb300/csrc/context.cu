@@ -14,13 +14,19 @@
 
 using namespace sphfem;
 
+// Particle-state buffers: two for stepping; four once pipelined host I/O is
+// used, so that the upload of the next request, the current step and the
+// download of the last result each have a buffer of their own and the two copy
+// directions run at the same time.
+constexpr int kBufs = 4;
+
 struct sph_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     int N = 0;
     KConsts K{};
     sph_grid_params grid{};
-    SortedFields buf[3]{};               // the third only once pipelined I/O is used
+    SortedFields buf[kBufs]{};           // the third and fourth only once pipelined I/O is used
     int nbuf = 2;
     int cur = 0;                         // buf[cur] holds the particle state
     int last_in = -1;                    // the buffer the last step read
@@ -36,8 +42,8 @@ struct sph_ctx {
     ToolDev *tool_dev = nullptr;
     double *fem_T_old = nullptr, *fem_f_temp = nullptr, *fem_K_temp = nullptr;
     // graphs, one per buffer parity
-    cudaGraphExec_t graph[3][3] = {};    // [input buffer][output buffer]
-    int64_t graph_launches[3][3] = {};
+    cudaGraphExec_t graph[kBufs][kBufs] = {};    // [input buffer][output buffer]
+    int64_t graph_launches[kBufs][kBufs] = {};
     bool use_graph = true;
     int64_t launches = 0;
     double *h_reduce = nullptr;          // pinned
@@ -73,8 +79,9 @@ struct sph_ctx {
     // their own streams, ordered per buffer by events; a step waits only for the
     // copies into its input and out of its output buffer
     cudaStream_t io_up = nullptr, io_down = nullptr;
-    cudaEvent_t ev_used[3] = {}, ev_up[3] = {}, ev_down[3] = {}, ev_fixed = nullptr;
-    bool up_pending[3] = {}, down_pending[3] = {}, fixed_pending = false;
+    cudaEvent_t ev_used[kBufs] = {}, ev_up[kBufs] = {}, ev_down[kBufs] = {}, ev_fixed = nullptr;
+    bool up_pending[kBufs] = {}, down_pending[kBufs] = {}, fixed_pending = false;
+    int64_t down_seq[kBufs] = {}, n_downloads = 0;   // issue order of each buffer's last download
     std::vector<void *> allocs;
     std::string err;
 };
@@ -114,7 +121,7 @@ int dalloc(sph_ctx *ctx, T **p, size_t count) {
 // Makes the compute stream wait for the pending copies into (upload) / out of
 // (download) buffer b, or for every pending copy with b < 0.
 int wait_io(sph_ctx *ctx, int b) {
-    for (int i = 0; i < 3; i++) {
+    for (int i = 0; i < kBufs; i++) {
         if (b >= 0 && i != b) continue;
         if (ctx->up_pending[i]) {
             CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_up[i], 0));
@@ -222,8 +229,8 @@ void set_case_dt(ToolDev &td, double dt) {
 }
 
 void invalidate_graphs(sph_ctx *ctx) {
-    for (int a = 0; a < 3; a++)
-        for (int b = 0; b < 3; b++)
+    for (int a = 0; a < kBufs; a++)
+        for (int b = 0; b < kBufs; b++)
             if (ctx->graph[a][b]) {
                 cudaGraphExecDestroy(ctx->graph[a][b]);
                 ctx->graph[a][b] = nullptr;
@@ -294,22 +301,25 @@ int zero_all(sph_ctx *ctx) {
     return SPH_OK;
 }
 
-// Copy streams, per-buffer events and the third particle buffer of pipelined I/O.
+// Copy streams, per-buffer events and the third and fourth particle buffers of
+// pipelined I/O.
 int ensure_io(sph_ctx *ctx) {
     if (ctx->io_up) return SPH_OK;
-    int r = alloc_sorted(ctx, ctx->buf[2], ctx->N);
-    if (r) return r;
-    ctx->nbuf = 3;
+    for (int b = 2; b < kBufs; b++) {
+        int r = alloc_sorted(ctx, ctx->buf[b], ctx->N);
+        if (r) return r;
+    }
+    ctx->nbuf = kBufs;
     CK(cudaStreamCreateWithFlags(&ctx->io_up, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&ctx->io_down, cudaStreamNonBlocking));
-    for (int b = 0; b < 3; b++) {
+    for (int b = 0; b < kBufs; b++) {
         CK(cudaEventCreateWithFlags(&ctx->ev_used[b], cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&ctx->ev_up[b], cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&ctx->ev_down[b], cudaEventDisableTiming));
     }
     CK(cudaEventCreateWithFlags(&ctx->ev_fixed, cudaEventDisableTiming));
     // the buffers' last users are whatever the compute stream has queued so far
-    for (int b = 0; b < 3; b++) CK(cudaEventRecord(ctx->ev_used[b], ctx->stream));
+    for (int b = 0; b < kBufs; b++) CK(cudaEventRecord(ctx->ev_used[b], ctx->stream));
     return SPH_OK;
 }
 
@@ -497,7 +507,7 @@ int sph_ctx_destroy(sph_ctx *ctx) {
         cudaStreamSynchronize(ctx->io_down);
         cudaStreamDestroy(ctx->io_up);
         cudaStreamDestroy(ctx->io_down);
-        for (int b = 0; b < 3; b++) {
+        for (int b = 0; b < kBufs; b++) {
             cudaEventDestroy(ctx->ev_used[b]);
             cudaEventDestroy(ctx->ev_up[b]);
             cudaEventDestroy(ctx->ev_down[b]);
@@ -854,10 +864,19 @@ int sph_upload_particles_async(sph_ctx *ctx, const sph_particles *host) {
         return fail(ctx, SPH_ERR_INVALID, "async upload: p, R, S_der, v_der, idx are recomputed by the step");
     int r = ensure_io(ctx);
     if (r) return r;
-    // a buffer neither holding the current state nor read by the last queued step
+    // a buffer neither holding the current state nor read by the last queued step:
+    // one no download reads, else the one whose download was issued first (the
+    // upload then waits for the oldest download, not the one just queued)
     int t = -1;
-    for (int b = 0; b < 3 && t < 0; b++)
-        if (b != ctx->cur && b != ctx->last_in) t = b;
+    for (int b = 0; b < kBufs; b++) {
+        if (b == ctx->cur || b == ctx->last_in) continue;
+        if (t < 0) {
+            t = b;
+            continue;
+        }
+        const bool tb = ctx->down_pending[t], bb = ctx->down_pending[b];
+        if ((tb && !bb) || (tb && bb && ctx->down_seq[b] < ctx->down_seq[t])) t = b;
+    }
     CK(cudaStreamWaitEvent(ctx->io_up, ctx->ev_used[t], 0));                  // its last compute user
     if (ctx->down_pending[t]) CK(cudaStreamWaitEvent(ctx->io_up, ctx->ev_down[t], 0));   // a download out of it
     const sph_particles v = view_of_buf(ctx, t);
@@ -899,6 +918,7 @@ int sph_download_particles_async(sph_ctx *ctx, sph_particles *host) {
     }
     CK(cudaEventRecord(ctx->ev_down[src_b], ctx->io_down));
     ctx->down_pending[src_b] = true;
+    ctx->down_seq[src_b] = ++ctx->n_downloads;
     if (fixed) {
         CK(cudaEventRecord(ctx->ev_fixed, ctx->io_down));
         ctx->fixed_pending = true;
