@@ -124,6 +124,32 @@ def dist_env():
     return world, rank, local
 
 
+def rank_collectives(dist, device):
+    """The two collectives of the replica runs: a barrier around the timed
+    region and the max over ranks of a time (the slowest replica sets the
+    whole job's time).  dist = None for one process."""
+    import torch
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    return barrier, max_over_ranks
+
+
+def replica_value(world: int, particles_per_rank: int, ms_per_step: float) -> float:
+    """Whole-job particle-steps/s of `world` replicas of `particles_per_rank`
+    particles each, from the slowest rank's time per step."""
+    return world * particles_per_rank / (ms_per_step * 1e-3)
+
+
 def cpu_sample(case, max_seconds=15.0, min_steps=1):
     """Time whole oracle steps of the workload (all host threads)."""
     from oracle.oracle import OracleSim, num_threads
@@ -521,16 +547,7 @@ def run_product(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x: float) -> float:
-        if dist is None:
-            return x
-        t = torch.tensor([x], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    barrier, max_over_ranks = rank_collectives(dist, torch.device("cuda", local))
 
     # cells of 2h with a 3x3 stencil, as the micro-benchmark specifies
     case = setups.micro(n_side=args.n_side, seed=args.seed + rank, cell_factor=args.cell_factor,
@@ -715,7 +732,7 @@ def run_product(args):
         return 0
     head_name = "fp32k" if "fp32k" in results else "fp64"
     head = results[head_name]
-    value = world * case.N / (head["ms"] * 1e-3)
+    value = replica_value(world, case.N, head["ms"])
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak",
@@ -771,7 +788,7 @@ def run_product(args):
     return 0
 
 
-def main():
+def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -801,9 +818,14 @@ def main():
     ap.add_argument("--no-small", action="store_true", help="skip the 12,000-particle Ti6Al4V cut line")
     ap.add_argument("--rigid-ny", type=int, nargs="*", default=[30, 240],
                     help="rows of the rigid-tool cut sizes to time (none: skip)")
-    args = ap.parse_args()
+    args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
+    return args
+
+
+def main():
+    args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
     return run_product(args)
