@@ -333,7 +333,7 @@ def run_rigid(args, local):
     arguments: rake 0, clearance 4.5 deg, edge radius 3.5 um, uncut chip 100 um,
     300 in the reference's speed unit) at ny = 30 rows -- the reference's own
     size -- and at larger ny: leap_frog::step(particles, grid) with the rigid
-    tool, the Brookshaw build, FP64 and FP32K, plus the PSE build in FP64; the
+    tool, the Brookshaw build and the PSE build, each in FP64 and FP32K; the
     CPU oracle's whole-step time beside each size."""
     import ctypes as C
 
@@ -349,7 +349,7 @@ def run_rigid(args, local):
         case = setups.ref_cut(ny=ny, rake=0.0, clear=4.5, chamfer=0.00035, speed=speed, feed=0.01)
         row = {"ny": ny, "particles": case.N, "workpiece": case.info["n_workpiece"], "tool": case.info["n_tool"]}
         for name, prec, pse in (("fp64", abi.SPH_PREC_FP64, False), ("fp32k", abi.SPH_PREC_FP32K, False),
-                                ("fp64_pse", abi.SPH_PREC_FP64, True)):
+                                ("fp64_pse", abi.SPH_PREC_FP64, True), ("fp32k_pse", abi.SPH_PREC_FP32K, True)):
             s = Solver(case, prec, device=local)
             if pse:
                 s.set_thermal_model(abi.SPH_THERMAL_PSE)

@@ -321,7 +321,8 @@ int sph_material_fric_heat_gen(sph_ctx *ctx);
 
 /* Thermal conduction model of the neighbour sums: SPH_THERMAL_BROOKSHAW (the
  * reference's default, interactions_gpu.cu:143-379) or SPH_THERMAL_PSE
- * (do_interactions_heat_pse, interactions_gpu.cu:84-140; FP64 contexts only). */
+ * (do_interactions_heat_pse, interactions_gpu.cu:84-140; contexts on cells of edge h,
+ * FP64 or FP32K). */
 #define SPH_THERMAL_BROOKSHAW 0
 #define SPH_THERMAL_PSE 1
 int sph_set_thermal_model(sph_ctx *ctx, int32_t model);

@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused32(int N, const int32_t 
         R = make_float4((float)Rd.x, (float)Rd.y, (float)Rd.z, 0.f);
     }
     const float thermal_alpha = is_tool ? K.f.alpha_tool_sph : K.f.alpha_wp;
-    const float Tn = (thermal_alpha != 0.f) ? Tp : 0.f;
+    const float Tn = (thermal_alpha != 0.f || K.thermal_pse) ? Tp : 0.f;   // PSE reads every neighbour's T
     // record: (xr, yr, flags|row, h) (vx, vy, rho, c) (sA, sB, sC, m/rho) (Rxx, Rxy, Ryy, T)
     const sph_geom_constants &g = K.g;
     int ci = 0, cj = 0;

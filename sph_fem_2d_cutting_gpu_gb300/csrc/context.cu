@@ -2089,14 +2089,13 @@ int sph_material_fric_heat_gen(sph_ctx *ctx) {
 
 // types.h:11-13,122-123: the thermal solver of the build, Brookshaw or PSE.  PSE
 // sums over the reference's 5x5 block of cells of edge h, so it needs the
-// reference's cell geometry (cell_factor 1), and is evaluated in FP64.
+// reference's cell geometry (cell_factor 1).
 int sph_set_thermal_model(sph_ctx *ctx, int32_t model) {
     REQUIRE_CTX();
     if (model != SPH_THERMAL_BROOKSHAW && model != SPH_THERMAL_PSE)
         return fail(ctx, SPH_ERR_INVALID, "unknown thermal model");
     const int32_t pse = model == SPH_THERMAL_PSE ? 1 : 0;
     if (pse) {
-        if (ctx->K.precision != SPH_PREC_FP64) return fail(ctx, SPH_ERR_STATE, "PSE conduction needs an FP64 context");
         if (ctx->grid.cell_factor != 1) return fail(ctx, SPH_ERR_STATE, "PSE conduction needs cells of edge h");
         if (ctx->K.n_cases > 1) return fail(ctx, SPH_ERR_STATE, "PSE conduction: single-case contexts only");
     }

@@ -167,8 +167,14 @@ __device__ __forceinline__ void fused_epilogue32(int k, const KConsts &K, const 
         const dbl4 Sto = B.S_t[k];
         St = make_float4((float)Sto.x, (float)Sto.y, (float)Sto.z, (float)Sto.w);
         rho_t = B.rho_t[k];
-        vel_t = vt;
-        pos_t = xt;
+        if (K.thermal_pse) {   // PSE build: tool particles leave the sums unwritten
+            const double2 vto = B.vel_t[k], pto = B.pos_t[k];
+            vel_t = make_float2((float)vto.x, (float)vto.y);
+            pos_t = make_float2((float)pto.x, (float)pto.y);
+        } else {
+            vel_t = vt;
+            pos_t = xt;
+        }
     }
     const float T_t = thermal ? T_t_new : (float)B.T_t[k];
     const double2 pos_t_d = make_double2(pos_t.x, pos_t.y);
@@ -474,7 +480,8 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
     const float sAi = i2.x, sBi = i2.y, sCi = i2.z;
     const float Rxxi = i3.x, Rxyi = i3.y, Ryyi = i3.z, Ti = i3.w;
     const float thermal_alpha = (!tool_i) ? K.f.alpha_wp : K.f.alpha_tool_sph;
-    const bool thermal = thermal_alpha != 0.f;
+    const bool thermal = thermal_alpha != 0.f && !K.thermal_pse;   // Brookshaw build only
+    const bool pse_tool = K.thermal_pse && tool_i;                  // PSE build: tool particles return at once
     const float h1 = 1.f / hi;
     const float fourh2 = 4.f * hi * hi;
     const float fac = (float)kPiFac * h1 * h1;
@@ -489,7 +496,7 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
     int gi = 0, gj = 0, ii = 0, hi_i = 0, lo_j = 0, hi_j = 0, j = 0, j1 = 0;
     const int R = g.stencil;
     bool done = true;
-    if (hash >= 0 && hash < g.num_cell) {
+    if (hash >= 0 && hash < g.num_cell && !pse_tool) {
         gi = hash / g.ny;
         gj = hash - gi * g.ny;
         ii = max(gi - R, 0);
@@ -635,6 +642,7 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
     const float2 xt = make_float2(xs * xt0.s, xs * xt1.s);
     const float T_t = thermal_alpha * (2.0f * tl.s);
     if (!kFused) {
+        if (pse_tool) return;
         F.S_der[k] = mk4(sd.x, sd.y, sd.z, sd.w);
         F.v_der[k] = mk4(vd.x, vd.y, vd.z, vd.w);
         B.pos_t[k] = make_double2(xt.x, xt.y);
@@ -740,8 +748,52 @@ __global__ void __launch_bounds__(kB) k_heat_pse64(int N, KConsts K, const int32
     T_t[k] = alpha * sum;
 }
 
+// FP32-compensated form of the PSE sum over the FP32 records: positions as
+// offsets from the cell corners (cells of edge h), the Gaussian with expf, the
+// sum Kahan-compensated; T_t written in FP64.
+__global__ void __launch_bounds__(kBlock) k_heat_pse32(int N, KConsts K, const int32_t *__restrict__ offsets,
+                                                       const float4 *__restrict__ rec,
+                                                       const int32_t *__restrict__ hashes, double *__restrict__ T_t) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    const float4 i0 = rec[4 * k + 0];
+    const int fi = __float_as_int(i0.z);
+    if (fi & kFlagBlanked) return;
+    const float xri = i0.x, yri = i0.y, hi = i0.w, Ti = rec[4 * k + 3].w;
+    const double alpha = (fi & kFlagTool) ? K.c.trml_tool_sph.alpha : K.c.trml_wp.alpha;
+    const float h2 = hi * hi;
+    const float c = 4.f / (h2 * h2 * (float)kRigidPi);
+    const float inv_h2 = 1.f / h2;
+    const float cell = K.f.cell;
+    KahanF sum = {};
+    const int hash = hashes[k];
+    const sph_geom_constants &g = K.g;
+    if (hash >= 0 && hash < g.num_cell) {
+        const int gi = hash / g.ny, gj = hash - gi * g.ny;
+        const int lo_i = max(gi - 2, 0), hi_i = min(gi + 3, g.nx);
+        const int lo_j = max(gj - 2, 0), hi_j = min(gj + 3, g.ny);
+        for (int ii = lo_i; ii < hi_i; ii++) {
+            const float dxc = (float)(gi - ii) * cell;
+            const int j1 = __ldg(offsets + ii * g.ny + hi_j);
+            for (int j = __ldg(offsets + ii * g.ny + lo_j); j < j1; j++) {
+                const float4 n0 = rec[4 * j + 0];
+                const float dx = dxc + (xri - n0.x);
+                const float dy = (float)(gj - (__float_as_int(n0.z) & kRowMask)) * cell + (yri - n0.y);
+                const float w2 = c * expf(-(dx * dx + dy * dy) * inv_h2);
+                sum.add((rec[4 * j + 3].w - Ti) * w2 * rec[4 * j + 2].w);
+            }
+        }
+    }
+    T_t[k] = alpha * (double)sum.s;
+}
+
 void launch_heat_pse(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const StepScratch &W,
                      const SortedFields &B) {
+    if (K.precision == SPH_PREC_FP32K) {
+        const int tb = fp64_block(N);
+        k_heat_pse32<<<div_up(N, tb), tb, 0, s>>>(N, K, offsets, W.rec32, B.hash, B.T_t);
+        return;
+    }
     switch (fp64_block(N)) {
         case 32: k_heat_pse64<32><<<div_up(N, 32), 32, 0, s>>>(N, K, offsets, W.rec64, B.hash, B.T_t); break;
         case 64: k_heat_pse64<64><<<div_up(N, 64), 64, 0, s>>>(N, K, offsets, W.rec64, B.hash, B.T_t); break;

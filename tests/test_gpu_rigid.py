@@ -185,6 +185,29 @@ def test_rigid_fp32k_error_bound(lib):
         assert e < 2e-5, f"FP32K rigid {f}: {e:.2e}"
 
 
+def test_rigid_pse_fp32k_error_bound(lib):
+    """The FP32K form of the PSE build (FP32 records, expf, Kahan sum) against the
+    FP64 oracle of the same build."""
+    c = rigid_case()
+    s32 = Solver(c, precision=abi.SPH_PREC_FP32K)
+    s32.set_thermal_model(abi.SPH_THERMAL_PSE)
+    _, o = rigid_pair(c, pse=True)
+    for _ in range(3):
+        s32.step()
+        o.step()
+    G = s32.download()
+    for f in ["hash", "idx", "blanked"]:
+        assert np.array_equal(G[f], o.P[f]), f
+    act = o.P["blanked"] != 1
+    for f in ["pos", "vel", "S", "rho", "T", "fc", "ft"]:
+        e = rel_err(G[f][act], o.P[f][act])
+        assert e < 2e-5, f"FP32K rigid PSE {f}: {e:.2e}"
+    # the conduction rate itself, on the particles where heat flows
+    e = rel_err(G["T_t"][act], o.P["T_t"][act])
+    assert e < 1e-3, f"FP32K PSE T_t: {e:.2e}"
+    assert np.max(np.abs(o.P["T_t"][act])) > 0
+
+
 def test_rigid_api_errors(lib):
     c = rigid_case()
     s = Solver(c)
@@ -202,10 +225,9 @@ def test_rigid_api_errors(lib):
         s.compute_contact_forces()
     s.set_rigid_tool(t)
     s.compute_contact_forces()
-    # PSE needs FP64 and cells of edge h
+    # PSE needs cells of edge h (FP64 or FP32K)
     s32 = Solver(c, precision=abi.SPH_PREC_FP32K)
-    with pytest.raises(SphError):
-        s32.set_thermal_model(abi.SPH_THERMAL_PSE)
+    s32.set_thermal_model(abi.SPH_THERMAL_PSE)
     c2 = rigid_case(cell_factor=2, stencil=1)
     s2 = Solver(c2)
     with pytest.raises(SphError):
