@@ -775,6 +775,7 @@ __global__ void __launch_bounds__(kBlock) k_heat_pse32(int N, KConsts K, const i
         for (int ii = lo_i; ii < hi_i; ii++) {
             const float dxc = (float)(gi - ii) * cell;
             const int j1 = __ldg(offsets + ii * g.ny + hi_j);
+#pragma unroll 4   // several neighbours' loads in flight (the kernel waits on loads, not on math)
             for (int j = __ldg(offsets + ii * g.ny + lo_j); j < j1; j++) {
                 const float4 n0 = rec[4 * j + 0];
                 const float dx = dxc + (xri - n0.x);
