@@ -62,8 +62,9 @@ NCU_FLOPS_PER_PARTICLE = {"fp64": 1_401_475_197 / 262_144, "fp32k": 1_454_251_76
 # Nominal GB300 rates (no measured figure exists for these pipes): FP64 1.25 TFLOP/s;
 # FP32 152 SMs x 128 lanes x 2 flops x 2.07 GHz = 80.5 TFLOP/s.
 NOMINAL_TFLOPS = {"fp64": 1.25, "fp32k": 80.5}
-STAGES = ["hash+histogram", "scan+scatter+rank", "reorder+predict+eos+artstress+records", "fem half step",
-          "neighbour sums+epilogue", "fem update+tool move", "contact/bc/invalidate tail"]
+# the seven stages of sph_profile_steps (the solver's PROFILE_STAGES)
+STAGES = ["hash+histogram", "scan+scatter+rank", "reorder+predict+eos+artstress+records", "fem half step+pse",
+          "neighbour sums+epilogue", "fem update+wear+tool move", "contact/bc/invalidate tail"]
 # fields a caller moves per step in the end-to-end arm (the persistent state)
 E2E_FIELDS = ["pos", "vel", "h", "rho", "S", "fc", "ft", "n", "fixed", "blanked", "tool_particle", "eps_pl",
               "eps_pl_dot", "T", "pos_t", "vel_t", "rho_t", "S_t", "T_t", "on_seg", "hash"]

@@ -478,9 +478,11 @@ int sph_get_launch_config(const sph_ctx *ctx, sph_launch_config *cfg);
  * context stream between the stages; stage_ms[k] receives the summed device
  * time of stage k over the steps: 0 histogram/hash (previous step's tail when
  * chained), 1 scan+scatter+rank, 2 reorder gather (+predict, EOS, artificial
- * stress, records), 3 FEM half step, 4 neighbour sums + fused epilogue,
- * 5 FEM rate/update + tool move, 6 contact/BC/invalidate tail (+ next
- * histogram).  n_stages receives 7. */
+ * stress, records), 3 FEM half step (+ PSE conduction), 4 neighbour sums +
+ * fused epilogue (+ wear statistics reset, warm-started return mapping),
+ * 5 FEM rate/update (+ wear adjustment) + tool move (+ rigid tool move),
+ * 6 contact/BC/invalidate tail (+ next histogram).  The steps are the same
+ * as those of sph_step_fused.  n_stages receives 7. */
 int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_stages);
 
 /* ---- tool wear by nodal shift (WEAR_NODE_SHIFT) --------------------------------

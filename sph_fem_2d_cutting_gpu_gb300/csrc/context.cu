@@ -1316,6 +1316,12 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
     for (int k = 0; k < kStages; k++) stage_ms[k] = 0.f;
     for (int step = 0; step < nsteps; step++) {
         const int w = pick_out(ctx);
+        int r0 = wait_io(ctx, ctx->cur);
+        if (r0 == SPH_OK) r0 = wait_io(ctx, w);
+        if (r0) {
+            for (auto &e : ev) cudaEventDestroy(e);
+            return r0;
+        }
         SortedFields &A = ctx->buf[ctx->cur];
         SortedFields &B = ctx->buf[w];
         CK(cudaEventRecord(ev[0], s));
@@ -1331,8 +1337,13 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
         if (ctx->has_tool) launch_fem_half(s, ctx->K, ctx->fem, ctx->tool_dev);
         if (pse_active(ctx)) launch_heat_pse(s, N, ctx->K, ctx->X.offsets, ctx->W, B);
         CK(cudaEventRecord(ev[4], s));
+        SegDev sw = ctx->seg;
+        if (ctx->wear_mode != SPH_WEAR_OFF) {
+            launch_wear_reset(s, ctx->seg);
+            sw.wear.T_nodes = ctx->fem.T_half;
+        }
         if (ctx->mlp_on) CK(cudaMemsetAsync(ctx->jc_list_count, 0, sizeof(int32_t), s));
-        launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, ctx->seg, ctx->tool_dev, true,
+        launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, sw, ctx->tool_dev, true,
                             ctx->interact_variant);
         if (ctx->mlp_on) {
             launch_jc_warm(s, jc_warm_grid(ctx), ctx->K, B, ctx->F, ctx->tool_dev, ctx->mlp, ctx->W.secant_iters,
@@ -1342,6 +1353,10 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
         CK(cudaEventRecord(ev[5], s));
         if (ctx->has_tool) {
             launch_fem_rate_update(s, ctx->K, ctx->fem, ctx->seg, ctx->tool_dev);
+            if (ctx->wear_mode == SPH_WEAR_SHIFT) {
+                launch_wear_adjustment(s, ctx->K, ctx->fem, ctx->seg, ctx->wear, ctx->tool_dev, ctx->K.dt);
+                ctx->launches += 6;
+            }
             launch_tool_move(s, ctx->K, ctx->seg, ctx->fem, ctx->tool_dev, ctx->K.dt, 3, true);
         }
         if (ctx->K.rigid) launch_rigid_move(s, ctx->K.rigid, ctx->K.dt);

@@ -15,6 +15,11 @@ import numpy as np
 from . import abi
 from .setups import Case
 
+# the seven stages of sph_profile_steps, in order
+PROFILE_STAGES = ("hash+histogram", "scan+scatter+rank", "reorder+predict+eos+artstress+records",
+                  "fem half step+pse", "neighbour sums+epilogue", "fem update+wear+tool move",
+                  "contact/bc/invalidate tail")
+
 
 class SphError(RuntimeError):
     pass
@@ -247,6 +252,14 @@ class Solver:
             self.call("sph_step")
         else:
             self._ck(self.lib.sph_run(self.ctx, n), "sph_run")
+
+    def profile_steps(self, n: int = 1) -> dict:
+        """n fused steps issued stage by stage with CUDA events between the
+        stages (no graph); returns the summed device ms per stage."""
+        ms = (C.c_float * 7)()
+        ns = abi.I32()
+        self._ck(self.lib.sph_profile_steps(self.ctx, n, ms, C.byref(ns)), "sph_profile_steps")
+        return dict(zip(PROFILE_STAGES, list(ms)[:ns.value]))
 
     def step_staged(self):
         """leap_frog::step issued as the reference's separate calls."""
