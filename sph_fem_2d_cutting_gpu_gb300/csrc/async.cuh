@@ -54,4 +54,13 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst_smem, const void *src, uin
                  : "memory");
 }
 
+// Hint to the bulk-copy engine: bring [p, p + bytes) into L2.  No completion,
+// nothing to wait for.  Skipped unless p is non-null and 16-byte aligned; bytes
+// rounded down to a multiple of 16.
+__device__ __forceinline__ void prefetch_l2_bulk(const void *p, uint32_t bytes) {
+    bytes &= ~15u;
+    if (!p || bytes == 0 || ((uintptr_t)p & 15u)) return;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 }  // namespace sphfem

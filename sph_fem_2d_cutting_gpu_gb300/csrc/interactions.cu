@@ -432,6 +432,40 @@ __device__ __forceinline__ void stage_issue(int N, int kB, const KConsts &K, con
     h.c_lo = c_lo;
 }
 
+// L2 prefetch by one thread at block start, overlapped with the neighbour loops:
+// the block's slice of the start-of-step state its epilogue reads, and, when
+// the block lies in one grid column, the neighbour records of its stencil
+// (one contiguous run of rows per column).  Hints only: every range lies
+// inside its array.
+__device__ __forceinline__ void block_prefetch_l2(int N, int kB, const KConsts &K, const int32_t *__restrict__ offsets,
+                                                  const float4 *__restrict__ rec, const SortedFields &B,
+                                                  const FixedFields &F) {
+    const int b0 = blockIdx.x * kB;
+    const uint32_t n = (uint32_t)min(kB, N - b0);
+    prefetch_l2_bulk(B.S + b0, n * 32u);
+    prefetch_l2_bulk(B.S_t + b0, n * 32u);
+    prefetch_l2_bulk(B.pos + b0, n * 16u);
+    prefetch_l2_bulk(B.vel + b0, n * 16u);
+    prefetch_l2_bulk(B.fc + b0, n * 16u);
+    prefetch_l2_bulk(B.ft + b0, n * 16u);
+    prefetch_l2_bulk(B.rho + b0, n * 8u);
+    prefetch_l2_bulk(B.T + b0, n * 8u);
+    prefetch_l2_bulk(B.eps_pl + b0, n * 8u);
+    prefetch_l2_bulk(B.eps_pl_dot + b0, n * 8u);
+    prefetch_l2_bulk(F.p + b0, n * 8u);
+    const sph_geom_constants &g = K.g;
+    const int R = g.stencil;
+    const int hf = B.hash[b0], hl = B.hash[b0 + (int)n - 1];
+    if (hf < 0 || hl >= g.num_cell || hl < hf) return;
+    const int ix = hf / g.ny;
+    if (hl / g.ny != ix) return;
+    const int r_lo = max(hf - ix * g.ny - R, 0), r_hi = min(hl - ix * g.ny + R, g.ny - 1);
+    for (int c = max(ix - R, 0); c <= min(ix + R, g.nx - 1); c++) {
+        const int s0 = __ldg(offsets + c * g.ny + r_lo), s1 = __ldg(offsets + c * g.ny + r_hi + 1);
+        if (s1 > s0) prefetch_l2_bulk(rec + 4 * (size_t)s0, (uint32_t)(s1 - s0) * 64u);
+    }
+}
+
 // kB threads per block, at least kMinB resident blocks per SM (a register
 // budget for the compiler): the launch shapes the autotuner chooses from.
 // kStaged: neighbour records from shared memory (dynamic: cap records + the
@@ -443,6 +477,7 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
                                                        int32_t *__restrict__ secant_iters, uint32_t *status,
                                                        int cap) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kFused && threadIdx.x == 0) block_prefetch_l2(N, kB, K, offsets, rec, B, F);
     int (*s_list)[kB];
     const float4 *nrec = rec;   // where the neighbour records are read from
     __shared__ StageHdr s_hdr;
@@ -561,23 +596,13 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
                 }
             }
         }
-        // phase 2: the pair body over the collected list, lanes in step; the
-        // next neighbour's record is fetched while the current one is computed
-        float4 p0, p1, p2, p3;
-        int pe = 0;
-        if (cnt > 0) {
-            pe = s_list[0][threadIdx.x];
-            const int jp = pe >> 3;
-            p0 = nb[4 * jp + 0]; p1 = nb[4 * jp + 1]; p2 = nb[4 * jp + 2]; p3 = nb[4 * jp + 3];
-        }
+        // phase 2: the pair body over the collected list, lanes in step.  No
+        // software prefetch of the next record: the 32 registers it holds cost
+        // more resident warps than it hides latency.
         for (int t = 0; t < cnt; t++) {
-            const int e = pe;
-            const float4 n0 = p0, n1 = p1, n2 = p2, n3 = p3;
-            if (t + 1 < cnt) {
-                pe = s_list[t + 1][threadIdx.x];
-                const int jp = pe >> 3;
-                p0 = nb[4 * jp + 0]; p1 = nb[4 * jp + 1]; p2 = nb[4 * jp + 2]; p3 = nb[4 * jp + 3];
-            }
+            const int e = s_list[t][threadIdx.x];
+            const int jn = e >> 3;
+            const float4 n0 = nb[4 * jn + 0], n1 = nb[4 * jn + 1], n2 = nb[4 * jn + 2], n3 = nb[4 * jn + 3];
             {
                 const int fj = __float_as_int(n0.z);
                 const float dx = (float)((e & 7) - R) * cell + (xri - n0.x);
@@ -658,8 +683,8 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
 // Launch shapes of the fused FP32K neighbour-sum kernel: (threads per block,
 // minimum resident blocks per SM, staged records: 0 = global loads).
 // Variant 0 is the default.
-const int kInteractVariants[][3] = {{256, 1, 0},   {256, 3, 0},   {128, 4, 0},  {128, 6, 0},  {512, 1, 0},
-                                    {64, 8, 0},    {128, 3, 640}, {128, 2, 1024}, {64, 6, 384}, {256, 2, 1024}};
+const int kInteractVariants[][3] = {{128, 6, 0},   {64, 12, 0},   {64, 8, 0},     {128, 4, 0},  {256, 3, 0},
+                                    {256, 1, 0},   {128, 3, 640}, {128, 2, 1024}, {64, 6, 384}, {256, 2, 1024}};
 
 int interact_variant_count() { return (int)(sizeof(kInteractVariants) / sizeof(kInteractVariants[0])); }
 void interact_variant_shape(int v, int *block, int *min_blocks, int *staged) {
@@ -810,16 +835,16 @@ void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t 
     if (K.precision == SPH_PREC_FP32K) {
         if (fused) {
             switch (variant) {
-                case 1: launch_i32<256, 3, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
-                case 2: launch_i32<128, 4, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
-                case 3: launch_i32<128, 6, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
-                case 4: launch_i32<512, 1, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
-                case 5: launch_i32<64, 8, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+                case 1: launch_i32<64, 12, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+                case 2: launch_i32<64, 8, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+                case 3: launch_i32<128, 4, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+                case 4: launch_i32<256, 3, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+                case 5: launch_i32<256, 1, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
                 case 6: launch_i32<128, 3, true>(s, N, K, offsets, B, F, W, seg, tool, 640); break;
                 case 7: launch_i32<128, 2, true>(s, N, K, offsets, B, F, W, seg, tool, 1024); break;
                 case 8: launch_i32<64, 6, true>(s, N, K, offsets, B, F, W, seg, tool, 384); break;
                 case 9: launch_i32<256, 2, true>(s, N, K, offsets, B, F, W, seg, tool, 1024); break;
-                default: launch_i32<256, 1, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+                default: launch_i32<128, 6, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
             }
         } else
             k_interact32<false><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec32, B, F, seg, tool, W.secant_iters, W.status,
