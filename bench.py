@@ -51,9 +51,9 @@ ALGO_BYTES = {
 }
 # DRAM bytes (read + write) per particle of one full-size launch of the fused
 # neighbour sums, from ncu on the 2048x2048 micro workload with 2h cells
-# (dram__bytes_read.sum 991,403,264 + dram__bytes_write.sum 706,622,464 for
-# 4,194,304 particles, k_interact32<fused, 64x8>; one-pass capture).
-NCU_TRAFFIC_PER_PARTICLE = {"fp32k": (991_403_264 + 706_622_464) / 4_194_304}
+# (dram__bytes_read.sum 997,552,640 + dram__bytes_write.sum 706,785,024 for
+# 4,194,304 particles, k_interact32<fused, 128x6>; one-pass capture).
+NCU_TRAFFIC_PER_PARTICLE = {"fp32k": (997_552_640 + 706_785_024) / 4_194_304}
 # Floating-point work per particle of the fused neighbour sums, from ncu's SASS
 # instruction counters (dadd + dmul + 2 dfma; fadd + fmul + 2 ffma) on the
 # 512x512 micro workload with 2h cells (262,144 particles): k_interact64 executes
