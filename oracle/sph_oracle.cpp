@@ -650,8 +650,11 @@ int orc_plasticity_johnson_cook(sph_particles *P, const sph_constants *C, double
                                            norm_Strial, eps_pl, T, dt, C->phys.G, &it);
         if (it < 0) { capped++; it = -it; }
         its += it;
-        double eps_pl_new = eps_pl + sqrtf_d(2.0 / 3.0) * fmaxf_d(delta_lambda, 0.);
-        double eps_pl_dot_new = sqrtf_d(2.0 / 3.0) * fmaxf_d(delta_lambda, 0.) / dt;
+        // sqrtf(2.0/3.0) * fmaxf(delta_lambda, 0.): both calls return float, so the
+        // reference multiplies in float (actions_gpu.cu:728-729)
+        const float inc = sqrtf((float)(2.0 / 3.0)) * fmaxf((float)delta_lambda, 0.f);
+        double eps_pl_new = eps_pl + (double)inc;
+        double eps_pl_dot_new = (double)inc / dt;
         P->eps_pl[pidx] = eps_pl_new;
         P->eps_pl_dot[pidx] = eps_pl_dot_new;
         P->S[4 * pidx + 0] = Sxx - Sxx / norm_Strial * delta_lambda * 2. * mu;

@@ -132,8 +132,11 @@ __device__ __forceinline__ uint32_t plasticity_one(const KConsts &K, dbl4 &S, do
     jc_log_record(K, (float)svm, (float)eps_pl, (float)eps_pl_dot, (float)T, (float)norm_Strial, (float)delta_lambda,
                   it, (float)dt);
     jc_count(K, it);
-    double eps_pl_new = eps_pl + sqrtf_d(2.0 / 3.0) * fmaxf_d(delta_lambda, 0.);
-    double eps_pl_dot_new = sqrtf_d(2.0 / 3.0) * fmaxf_d(delta_lambda, 0.) / dt;
+    // sqrtf(2.0/3.0) * fmaxf(delta_lambda, 0.): both calls return float, so the
+    // reference multiplies in float (actions_gpu.cu:728-729)
+    const float inc = sqrtf((float)(2.0 / 3.0)) * fmaxf((float)delta_lambda, 0.f);
+    double eps_pl_new = eps_pl + (double)inc;
+    double eps_pl_dot_new = (double)inc / dt;
     double eps_old = eps_pl;
     eps_pl = eps_pl_new;
     eps_pl_dot = eps_pl_dot_new;

@@ -1,0 +1,269 @@
+"""Parity pinned to the reference's own CUDA code.
+
+The reference's actions_gpu.cu, leap_frog.cu and grid.cu are compiled,
+unmodified, into cubins (oracle/Makefile target ``ref_gpu``; built where the
+reference tree is present and carried to the GPU host with the other built
+files).  Each test uploads one seeded state to the product, runs one staged
+call through the C ABI, runs the reference kernel that call replaces on a
+copy of the same state (oracle/ref_gpu.py, CUDA driver API) and compares:
+  - every field bit for bit (EOS, continuity, momentum, advection, the
+    Johnson-Cook return mapping, boundary conditions, invalidation,
+    predictor / corrector, cell hashes), except
+  - the Jaumann rate within 1e-13 relative, norm-wise: the reference forms it
+    with GLM 3x3 matrix products, the product with the expanded 2-D terms, and
+    the compiler contracts them into FMAs differently;
+  - the artificial stress R within 1e-6: the reference evaluates the stress
+    angle's atan2f / cosf / sinf with CUDA's float functions, the product
+    evaluates them in double and rounds once to float (so that the CPU oracle
+    reproduces it), and the two agree to a few float ULPs (2^-23 relative).
+The state is a small cut after 15 fused steps with the tool in contact, then
+spread out so every branch of the kernels runs: random velocity and stress
+gradients, stresses beyond yield, temperatures above melting, tool, fixed and
+blanked particles, NaN / Inf rates for the invalidation.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from sph_fem_2d_cutting_gpu_gb300 import abi, setups
+from sph_fem_2d_cutting_gpu_gb300.solver import Solver
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 0.0   # bit for bit
+RTOL_JAUMANN = 1e-13
+RTOL_FLOAT_TRIG = 1e-6   # R: CUDA's float atan2f / cosf / sinf against double-evaluated, once-rounded
+torch = pytest.importorskip("torch")
+ref_gpu = pytest.importorskip("oracle.ref_gpu")
+
+
+def module(which):
+    try:
+        return ref_gpu.RefModule(which)
+    except FileNotFoundError as e:
+        pytest.skip(f"reference cubin not built here: {e}")
+
+
+@pytest.fixture(scope="module")
+def base():
+    c = setups.small_cut()
+    s = Solver(c)
+    s.move_tool(0.3 * c.info["dx"] / c.tool_speed)
+    s.step(15)
+    H = s.download()
+    s.close()
+    return c, spread(H)
+
+
+def spread(H, seed=5):
+    rng = np.random.default_rng(seed)
+    H = {k: v.copy() for k, v in H.items()}
+    N = len(H["rho"])
+
+    def noise(a, scale):
+        return a + rng.normal(0.0, 1.0, a.shape) * scale
+
+    for f in ("v_der", "S_der"):
+        H[f] = noise(H[f], 3.0 * np.abs(H[f]).std() + 1e-6)
+    for f in ("fc", "ft", "n"):
+        H[f] = noise(H[f], np.abs(H[f]).std() + 1e-9)
+    sel = rng.random(N) < 0.3                          # beyond yield
+    H["S"][sel] *= rng.uniform(1.5, 4.0, (sel.sum(), 1))
+    H["S"] = noise(H["S"], 0.05 * np.abs(H["S"]).std())
+    H["eps_pl"] = np.abs(noise(H["eps_pl"], 0.05))
+    H["eps_pl_dot"] = np.abs(noise(H["eps_pl_dot"], 1e-3))
+    hot = rng.random(N) < 0.1                          # some above melting
+    H["T"][hot] += rng.uniform(0.0, 2000.0, hot.sum())
+    H["rho"] = H["rho"] * rng.uniform(0.97, 1.03, N)
+    for f, frac in (("tool_particle", 0.05), ("fixed", 0.05), ("blanked", 0.03)):
+        H[f] = (rng.random(N) < frac).astype(np.float64)
+    for f in ("pos_t", "vel_t", "S_t", "rho_t", "T_t"):
+        H[f] = noise(H[f], np.abs(H[f]).std() + 1e-9)
+    return H
+
+
+def device(H):
+    return {k: torch.tensor(np.ascontiguousarray(v), device="cuda") for k, v in H.items()}
+
+
+def particle_struct(T, N):
+    pg = ref_gpu.ParticleGPU()
+    for f, _, _ in abi.PARTICLE_FIELDS:
+        setattr(pg, f, ref_gpu.ptr(T[f]))
+    pg.N = N
+    return pg
+
+
+@pytest.fixture(scope="module")
+def actions(lib, base):
+    m = module("actions")
+    c = base[0].constants
+    m.launch("ref_set_actions_constants", 1, c.phys, c.corr, c.joco, c.trml_wp, c.trml_tool, c.tool,
+             abi.WearConstants(0.0, 0.0, 0.0, 0.0), block=1)
+    return m
+
+
+def product_after(case, H, calls):
+    s = Solver(case)
+    s.upload(H)
+    for name, *args in calls:
+        s.call(name, *args)
+    G = s.download()
+    s.close()
+    return G
+
+
+def check(G, R, fields, exact=(), rtol=RTOL):
+    for f in fields:
+        a, b = G[f], R[f]
+        if f in exact:
+            assert np.array_equal(a, b, equal_nan=True), f"{f}: {np.count_nonzero(a != b)} entries differ"
+        else:
+            fin = np.isfinite(b)
+            assert np.array_equal(np.isfinite(a), fin), f"{f}: non-finite entries differ"
+            if rtol == 0.0:
+                assert np.array_equal(a, b, equal_nan=True), f"{f}: {np.count_nonzero(a != b)} entries differ"
+            else:
+                e = rel_err(a[fin], b[fin])
+                assert e <= rtol, f"{f}: relative error {e:.3e}"
+
+
+def ref_run(H, launch):
+    T = device(H)
+    N = len(H["rho"])
+    launch(T, particle_struct(T, N), N)
+    return {k: v.cpu().numpy() for k, v in T.items()}
+
+
+P = ref_gpu.ptr if ref_gpu else None
+
+
+def test_eos(actions, base):
+    c, H = base
+    G = product_after(c, H, [("sph_material_eos",)])
+    R = ref_run(H, lambda T, pg, N: actions.launch("do_material_eos", N, P(T["rho"]), P(T["p"]),
+                                                    P(T["tool_particle"]), C.c_int32(N)))
+    check(G, R, ["p"])
+
+
+def test_artificial_stress(actions, base):
+    c, H = base
+    G = product_after(c, H, [("sph_corrector_artificial_stress",)])
+    R = ref_run(H, lambda T, pg, N: actions.launch("do_corrector_artificial_stress", N, P(T["rho"]), P(T["p"]),
+                                                    P(T["S"]), P(T["tool_particle"]), P(T["R"]), C.c_int32(N)))
+    check(G, R, ["R"], rtol=RTOL_FLOAT_TRIG)
+
+
+def test_jaumann(actions, base):
+    c, H = base
+    G = product_after(c, H, [("sph_material_stress_rate_jaumann",)])
+    R = ref_run(H, lambda T, pg, N: actions.launch("do_material_stress_rate_jaumann", N, P(T["v_der"]), P(T["S"]),
+                                                    P(T["tool_particle"]), P(T["S_t"]), C.c_int32(N)))
+    check(G, R, ["S_t"], rtol=RTOL_JAUMANN)
+
+
+def test_continuity_momentum_advection(actions, base):
+    c, H = base
+    G = product_after(c, H, [("sph_contmech_continuity",), ("sph_contmech_momentum",), ("sph_contmech_advection",)])
+
+    def launch(T, pg, N):
+        actions.launch("do_contmech_continuity", N, P(T["rho"]), P(T["v_der"]), P(T["tool_particle"]),
+                       P(T["rho_t"]), C.c_int32(N))
+        actions.launch("do_contmech_momentum", N, P(T["S_der"]), P(T["fc"]), P(T["ft"]), P(T["tool_particle"]),
+                       P(T["vel_t"]), C.c_int32(N))
+        actions.launch("do_contmech_advection", N, P(T["vel"]), P(T["tool_particle"]), P(T["pos_t"]), C.c_int32(N))
+
+    R = ref_run(H, launch)
+    check(G, R, ["rho_t", "vel_t", "pos_t"])
+
+
+def test_plasticity(actions, base):
+    c, H = base
+    assert c.constants.plastic
+    G = product_after(c, H, [("sph_material_eos",), ("sph_plasticity_johnson_cook",)])
+
+    def launch(T, pg, N):
+        actions.launch("do_material_eos", N, P(T["rho"]), P(T["p"]), P(T["tool_particle"]), C.c_int32(N))
+        actions.launch("do_plasticity_johnson_cook", N, pg, C.c_double(c.dt))
+
+    R = ref_run(H, launch)
+    check(G, R, ["S", "eps_pl", "eps_pl_dot", "T", "blanked"], exact=["blanked"])
+    yielded = R["eps_pl_dot"] > 0
+    assert yielded.sum() > 50, "the state exercises the return mapping"
+    assert np.count_nonzero(R["blanked"] != H["blanked"]) > 0, "and the melting cap"
+
+
+def test_boundary_conditions(actions, base):
+    c, H = base
+    calls = [("sph_perform_boundary_conditions",)]
+    thermal = c.constants.trml_tool.alpha != 0.0
+    if thermal:
+        calls.append(("sph_perform_boundary_conditions_thermal",))
+    G = product_after(c, H, calls)
+
+    def launch(T, pg, N):
+        actions.launch("do_boundary_conditions", N, pg)
+        if thermal:
+            actions.launch("do_boundary_conditions_thermal", N, pg)
+
+    R = ref_run(H, launch)
+    check(G, R, ["vel", "fc", "pos_t", "vel_t", "T"])
+
+
+def test_invalidate(actions, base):
+    c, H = base
+    H = {k: v.copy() for k, v in H.items()}
+    rng = np.random.default_rng(9)
+    N = len(H["rho"])
+    for f, bad in (("pos_t", np.nan), ("vel_t", np.inf), ("S_t", -np.inf), ("rho_t", np.nan), ("T_t", np.inf)):
+        idx = rng.choice(N, 3, replace=False)
+        H[f][idx] = bad
+    G = product_after(c, H, [("sph_debug_invalidate",)])
+    R = ref_run(H, lambda T, pg, N: actions.launch("do_invalidate", N, pg, C.c_int32(0)))
+    check(G, R, ["blanked"], exact=["blanked"])
+    assert np.count_nonzero(R["blanked"] != H["blanked"]) >= 10
+
+
+@pytest.mark.parametrize("stage", ["predict", "correct"])
+def test_leap_frog(lib, base, stage):
+    m = module("leap_frog")
+    c, H = base
+    G = product_after(c, H, [("sph_init",), ("sph_" + stage,)])
+    N = len(H["rho"])
+    ini = {"pos_init": (N, 2), "vel_init": (N, 2), "S_init": (N, 4), "rho_init": (N,), "T_init": (N,),
+           "T_init_tool": (1,)}
+    I = {k: torch.zeros(v, dtype=torch.float64, device="cuda") for k, v in ini.items()}
+    st = ref_gpu.IniState(**{k: ref_gpu.ptr(v) for k, v in I.items()})
+
+    def launch(T, pg, N):
+        m.launch("init", N, pg, st)
+        m.launch(stage, N, pg, st, C.c_double(c.dt))
+
+    R = ref_run(H, launch)
+    check(G, R, ["pos", "vel", "S", "rho", "T"])
+
+
+def test_compute_hashes(lib, base):
+    """compute_hashes (grid.cu:25-42) against the product's FP32-first cell index:
+    positions on, next to and between cell edges, blanked particles keep a stale hash."""
+    m = module("grid")
+    c, H = base
+    s = Solver(c)
+    g = s.geometry()
+    s.close()
+    rng = np.random.default_rng(17)
+    N = len(H["rho"])
+    ix = rng.integers(0, g.nx, N)
+    iy = rng.integers(0, g.ny, N)
+    frac = rng.choice([0.0, 1e-15, 0.5, 1 - 1e-15, 1 - 2.2e-16], (N, 2))
+    H = {k: v.copy() for k, v in H.items()}
+    H["pos"][:, 0] = g.bbmin_x + (ix + frac[:, 0]) * g.dx
+    H["pos"][:, 1] = g.bbmin_y + (iy + frac[:, 1]) * g.dx
+    H["hash"] = rng.integers(-5, 5, N).astype(np.int32)   # stale values the blanked particles keep
+    G = product_after(c, H, [("sph_assign_hashes",)])
+    R = ref_run(H, lambda T, pg, N: m.launch("compute_hashes", N, P(T["blanked"]), P(T["pos"]), P(T["hash"]),
+                                              C.c_int32(N), C.c_double(g.dx), C.c_int32(g.ny),
+                                              C.c_double(g.bbmin_x), C.c_double(g.bbmin_y)))
+    check(G, R, ["hash"], exact=["hash"])
