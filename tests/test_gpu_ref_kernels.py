@@ -267,3 +267,89 @@ def test_compute_hashes(lib, base):
                                               C.c_int32(N), C.c_double(g.dx), C.c_int32(g.ny),
                                               C.c_double(g.bbmin_x), C.c_double(g.bbmin_y)))
     check(G, R, ["hash"], exact=["hash"])
+
+
+# ---- contact and friction heat with the FEM tool (live tool state) -------------------------------
+@pytest.fixture(scope="module")
+def cut(lib):
+    """The 12,000-particle Ti6Al4V cut with the tool pushed 0.3 dx into the
+    workpiece, after 40 fused steps (about 15 particles in contact; a deeper
+    push blanks the penetrated particles instead); the solver stays open."""
+    c = setups.ti64_cut()
+    s = Solver(c)
+    s.move_tool(0.3 * c.info["dx"] / c.tool_speed)
+    s.step(40)
+    yield c, s
+    s.close()
+
+
+def segment_struct(seg, n, wear=None):
+    T = {k: torch.tensor(np.ascontiguousarray(v), device="cuda") for k, v in seg.items()}
+    W = wear or dict(wear_rate=np.zeros((n, 2)), wear_nodes=np.zeros(n), physical_para=np.zeros((n, 4)),
+                     sliding_force=np.zeros(n))
+    T.update({k: torch.tensor(np.ascontiguousarray(v), device="cuda") for k, v in W.items()})
+    sg = ref_gpu.SegmentFEMGPU()
+    sg.segment_num = n
+    for k, src in (("left", "left"), ("right", "right"), ("n", "normal"), ("marks", "marks"),
+                   ("heat_exchange", "heat_exchange"), ("fric_heat", "fric_heat"), ("wear_rate", "wear_rate"),
+                   ("wear_nodes", "wear_nodes"), ("physical_para", "physical_para"), ("sliding_force", "sliding_force")):
+        setattr(sg, k, ref_gpu.ptr(T[src]))
+    return T, sg
+
+
+def test_contact_forces(actions, cut):
+    """compute_contact_forces_FEM_tool_v3 (actions_gpu.cu:983-999 -> :423-617): penalty
+    normal force, friction, segment ids, penetration blanking, the particle-segment
+    heat exchange (FP64 atomics: sums within 1e-13).  Both reference kernels call
+    __syncthreads() after their early returns, so they run here one thread per
+    block: no thread of a block can have left before the barrier."""
+    c, s = cut
+    H, seg, ts, fem = s.download(), s.segments(), s.tool_state(), s.fem()
+    n = ts.n_segments
+    s.call("sph_compute_contact_forces_fem")
+    G, Gseg = s.download(), s.segments()
+    S, sg = segment_struct(seg, n)
+    Tn = torch.tensor(fem["T"], device="cuda")
+
+    def launch(T, pg, N):
+        actions.launch("do_compute_contact_forces_FEM_tool_v3_s1", N, C.c_int32(N), pg, sg,
+                       ref_gpu.Vec2(*ts.tl_point_ref), C.c_double(ts.ref_dist), ref_gpu.Vec2(*ts.vel),
+                       C.c_double(c.dt), C.c_int32(n), block=1)
+        actions.launch("do_compute_contact_forces_FEM_tool_v3_s2", N, C.c_int32(N), pg, sg, P(Tn),
+                       C.c_double(c.dt), block=1)
+
+    R = ref_run(H, launch)
+    check(G, R, ["on_seg", "blanked", "fc", "ft", "n", "T"], exact=["on_seg", "blanked"])
+    assert np.count_nonzero(R["on_seg"] >= 0) >= 8, "particles in contact"
+    e = rel_err(Gseg["heat_exchange"], S["heat_exchange"].cpu().numpy())
+    assert e <= 1e-13, f"heat_exchange: {e:.3e}"
+
+
+@pytest.mark.parametrize("wear", [False, True], ids=["plain", "wear_statistics"])
+def test_friction_heat(actions, cut, wear):
+    """material_fric_heat_gen_FEM_v2 (actions_gpu.cu:967-981 -> :345-420): particle
+    heating, the tool's share per segment and, with WEAR_NODE_SHIFT, the segment
+    statistics (FP64 atomics: sums within 1e-13)."""
+    c, s = cut
+    if wear:
+        s.set_wear(abi.SPH_WEAR_ACCUMULATE, abi.WearConstants(10.0, 300.0, 10.0, 300.0))
+        s.call("sph_segments_wear_rate_reset")
+    H, seg, ts, fem = s.download(), s.segments(), s.tool_state(), s.fem()
+    n = ts.n_segments
+    s.call("sph_material_fric_heat_gen_fem")
+    G, Gseg = s.download(), s.segments()
+    S, sg = segment_struct(seg, n)
+    Tn = torch.tensor(fem["T"], device="cuda")
+    R = ref_run(H, lambda T, pg, N: actions.launch("do_material_fric_heat_gen_FEM_v21", N, pg, sg,
+                                                    ref_gpu.Vec2(*ts.vel), P(Tn), C.c_double(c.dt), C.c_int32(N)))
+    check(G, R, ["T", "blanked"], exact=["blanked"])
+    assert np.count_nonzero(G["T"] != H["T"]) >= 4, "particles heated by friction"
+    e = rel_err(Gseg["fric_heat"], S["fric_heat"].cpu().numpy())
+    assert e <= 1e-13, f"fric_heat: {e:.3e}"
+    if wear:
+        w = s.wear_state()
+        for k, src in (("phys_para", "physical_para"), ("sliding_force", "sliding_force")):
+            e = rel_err(w[k], S[src].cpu().numpy())
+            assert e <= 1e-13, f"{k}: {e:.3e}"
+        assert w["phys_para"][:, 0].sum() > 0
+        s.set_wear(abi.SPH_WEAR_OFF)
