@@ -2,9 +2,10 @@
 parity pin.
 
 ``oracle/Makefile`` (target ``ref_gpu``) compiles the reference's
-actions_gpu.cu, leap_frog.cu and grid.cu, unmodified, from the read-only
-reference tree into cubins for sm_103a under ``oracle/_ref/`` (with the
-stand-in GLM and gmsh headers of ``oracle/ref_shim``).  This module loads them
+actions_gpu.cu, leap_frog.cu, grid.cu and interactions_gpu.cu, unmodified,
+from the read-only reference tree into cubins for sm_103a under
+``oracle/_ref/`` (with the stand-in GLM, gmsh and texture-reference headers of
+``oracle/ref_shim``).  This module loads them
 through the CUDA driver API (``libcuda``, via ctypes), finds each kernel by its
 name and launches it on device buffers the caller owns (torch tensors).  It is
 never part of the product; only the GPU tests import it.
@@ -21,7 +22,8 @@ import re
 from pathlib import Path
 
 REF_DIR = Path(__file__).resolve().parent / "_ref"
-CUBINS = {"actions": "ref_gpu_actions.cubin", "leap_frog": "ref_gpu_leapfrog.cubin", "grid": "ref_gpu_grid.cubin"}
+CUBINS = {"actions": "ref_gpu_actions.cubin", "leap_frog": "ref_gpu_leapfrog.cubin", "grid": "ref_gpu_grid.cubin",
+          "interactions": "ref_gpu_interactions.cubin"}
 BLOCK_SIZE = 256   # the reference's BLOCK_SIZE (types.h)
 
 P = C.c_uint64     # device pointer
@@ -45,6 +47,12 @@ class SegmentFEMGPU(C.Structure):
     _fields_ = [("vptr", P), ("segment_num", C.c_int32), ("pad", C.c_int32)] + \
         [(n, P) for n in ("left", "right", "n", "marks", "heat_exchange", "fric_heat", "wear_rate", "wear_nodes",
                           "physical_para", "sliding_force")]
+
+
+class GeomConstants(C.Structure):
+    """geom_constants (constants_structs.h:70-76)."""
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("bbmin_x", C.c_double), ("bbmin_y", C.c_double),
+                ("dx", C.c_double)]
 
 
 class Vec2(C.Structure):

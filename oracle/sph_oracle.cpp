@@ -1316,9 +1316,9 @@ void orc_fric_heat_rigid(sph_particles *P, const sph_constants *C, const double 
 
 // interactions_gpu.cu:84-140 do_interactions_heat_pse with kernels.cuh:67-84
 // lapl_pse, over the 5x5 block of cells of edge h (launched only when
-// thermals_workpiece.alpha != 0, :434-435).  alpha by the tool flag (the
-// reference binds its tool-flag texture over N ints of an N-double array, so
-// its second half of particles reads flag 0; the intended flag is used here).
+// thermals_workpiece.alpha != 0, :434-435).  alpha by the tool flag as the
+// reference reads it: its tool-flag texture is bound over N ints of an N-double
+// array (:448), so from index N/2 on the fetch reads flag 0 (workpiece alpha).
 void orc_interactions_heat_pse(sph_particles *P, const int32_t *cell_start, const int32_t *cell_end,
                                const sph_geom_constants *g, const sph_constants *C) {
     if (C->trml_wp.alpha == 0.) return;
@@ -1329,7 +1329,7 @@ void orc_interactions_heat_pse(sph_particles *P, const int32_t *cell_start, cons
         if (P->blanked[pidx] == 1.) continue;
         double pix = P->pos[2 * pidx], piy = P->pos[2 * pidx + 1], hi = P->h[pidx], Ti = P->T[pidx];
         int hashi = P->hash[pidx];
-        double alpha = (P->tool_particle[pidx] == 1.) ? C->trml_tool_sph.alpha : C->trml_wp.alpha;
+        double alpha = (pidx < N / 2 && P->tool_particle[pidx] == 1.) ? C->trml_tool_sph.alpha : C->trml_wp.alpha;
         double T_ti = 0.;
         if (hashi >= 0 && hashi < g->num_cell) {
             int gi = hashi / ny, gj = hashi - gi * ny;

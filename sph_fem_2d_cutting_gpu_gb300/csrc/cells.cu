@@ -244,8 +244,11 @@ __global__ void __launch_bounds__(kBlock) k_build_records(int N, KConsts K, Sort
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= N) return;
     double tool = A.tool_particle[k];
-    double thermal_alpha = (tool == 0.) ? K.c.trml_wp.alpha : K.c.trml_tool_sph.alpha;
-    double T = (thermal_alpha != 0. || K.thermal_pse) ? A.T[k] : 0.;   // PSE reads every neighbour's T
+    // every record carries T: a particle whose own diffusivity is zero (a tool
+    // particle of a non-conducting tool) still passes its temperature to the
+    // conducting neighbours that sum over it (interactions_gpu.cu:242-247 gate
+    // the fetch on the summing particle's alpha, not the neighbour's)
+    double T = A.T[k];
     int hash = A.hash[k];
     if (rec64) {
         int row = 0;
@@ -325,8 +328,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused(int N, const int32_t *_
         F.p[k] = p;
         F.R[k] = R;
     }
-    double thermal_alpha = (tool == 0.) ? K.c.trml_wp.alpha : K.c.trml_tool_sph.alpha;
-    double Tn = (thermal_alpha != 0. || K.thermal_pse) ? T : 0.;   // PSE reads every neighbour's T
+    double Tn = T;   // every record carries T (k_build_records)
     if (!kF32) {
         int row = 0;
         if (hash >= 0 && hash < K.g.num_cell) row = hash - (hash / K.g.ny) * K.g.ny;
@@ -409,8 +411,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused32(int N, const int32_t 
         dbl4 Rd = F.R[k];
         R = make_float4((float)Rd.x, (float)Rd.y, (float)Rd.z, 0.f);
     }
-    const float thermal_alpha = is_tool ? K.f.alpha_tool_sph : K.f.alpha_wp;
-    const float Tn = (thermal_alpha != 0.f || K.thermal_pse) ? Tp : 0.f;   // PSE reads every neighbour's T
+    const float Tn = Tp;   // every record carries T (k_build_records)
     // record: (xr, yr, flags|row, h) (vx, vy, rho, c) (sA, sB, sC, m/rho) (Rxx, Rxy, Ryy, T)
     const sph_geom_constants &g = K.g;
     int ci = 0, cj = 0;

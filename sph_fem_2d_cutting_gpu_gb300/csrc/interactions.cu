@@ -746,7 +746,9 @@ __global__ void __launch_bounds__(kB) k_heat_pse64(int N, KConsts K, const int32
     if (fi & kFlagBlanked) return;
     const dbl4 i0 = rec[4 * k + 0], i2 = rec[4 * k + 2];
     const double xi = i0.x, yi = i0.y, hi = i2.z, Ti = i3.z;
-    const double alpha = (fi & kFlagTool) ? K.c.trml_tool_sph.alpha : K.c.trml_wp.alpha;
+    // the reference binds the tool flags (doubles) for N ints, half the array
+    // (interactions_gpu.cu:448): from index N/2 on its fetch reads zero
+    const double alpha = ((fi & kFlagTool) && k < N / 2) ? K.c.trml_tool_sph.alpha : K.c.trml_wp.alpha;
     const double h2 = hi * hi, h4 = h2 * h2;
     const double c = 4. / (h4 * kRigidPi);
     const double inv_h2 = 1. / h2;
@@ -785,7 +787,7 @@ __global__ void __launch_bounds__(kBlock) k_heat_pse32(int N, KConsts K, const i
     const int fi = __float_as_int(i0.z);
     if (fi & kFlagBlanked) return;
     const float xri = i0.x, yri = i0.y, hi = i0.w, Ti = rec[4 * k + 3].w;
-    const double alpha = (fi & kFlagTool) ? K.c.trml_tool_sph.alpha : K.c.trml_wp.alpha;
+    const double alpha = ((fi & kFlagTool) && k < N / 2) ? K.c.trml_tool_sph.alpha : K.c.trml_wp.alpha;
     const float h2 = hi * hi;
     const float c = 4.f / (h2 * h2 * (float)kRigidPi);
     const float inv_h2 = 1.f / h2;

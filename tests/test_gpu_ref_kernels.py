@@ -1,6 +1,6 @@
 """Parity pinned to the reference's own CUDA code.
 
-The reference's actions_gpu.cu, leap_frog.cu and grid.cu are compiled,
+The reference's actions_gpu.cu, leap_frog.cu, grid.cu and interactions_gpu.cu are compiled,
 unmodified, into cubins (oracle/Makefile target ``ref_gpu``; built where the
 reference tree is present and carried to the GPU host with the other built
 files).  Each test uploads one seeded state to the product, runs one staged
@@ -353,3 +353,84 @@ def test_friction_heat(actions, cut, wear):
             assert e <= 1e-13, f"{k}: {e:.3e}"
         assert w["phys_para"][:, 0].sum() > 0
         s.set_wear(abi.SPH_WEAR_OFF)
+
+
+# ---- neighbour sums: do_interactions_monaghan and do_interactions_heat_pse -----------------------
+# interactions_gpu.cu with its texture references served by ref_shim/texture_ref.h.
+# The product visits the same cells in the same order but skips out-of-support
+# candidates (the reference adds exact zeros for them) and folds per-neighbour
+# quotients into its records (reassociation at the 1e-16 level per term), so the
+# sums are compared within 1e-12 relative, norm-wise.
+RTOL_SUMS = 1e-12
+
+
+def interactions_module(c, geom):
+    m = module("interactions")
+    k = c.constants
+    ge = ref_gpu.GeomConstants(geom.nx, geom.ny, geom.bbmin_x, geom.bbmin_y, geom.dx)
+    m.launch("ref_set_interactions_constants", 1, k.phys, k.corr, ge, k.trml_wp, k.trml_tool_sph, k.tool, block=1)
+    return m
+
+
+def sorted_product(c, H, pse=False):
+    """The product on state H, sorted into cells, with pressure and artificial stress."""
+    s = Solver(c)
+    if pse:
+        s.set_thermal_model(abi.SPH_THERMAL_PSE)
+    s.upload(H)
+    for name in ("sph_assign_hashes", "sph_sort", "sph_material_eos", "sph_corrector_artificial_stress"):
+        s.call(name)
+    return s
+
+
+def test_interactions_monaghan(lib, base):
+    c, H = base
+    s = sorted_product(c, H)
+    H2, (cs, ce), g = s.download(), s.cells(), s.geometry()
+    assert c.grid.cell_factor == 1 and c.grid.stencil == 2      # the reference's cells of h, 5x5
+    s.call("sph_interactions_monaghan")
+    G = s.download()
+    s.close()
+    m = interactions_module(c, g)
+    N = len(H2["rho"])
+    T = device(H2)
+    CS, CE = torch.tensor(cs, device="cuda"), torch.tensor(ce, device="cuda")
+    m.launch("ref_bind_interactions", 1, P(T["pos"]), P(T["vel"]), P(T["S"]), P(T["R"]), P(T["h"]), P(T["rho"]),
+             P(T["p"]), P(T["T"]), P(T["hash"]), P(T["tool_particle"]), P(T["fc"]), P(CS), P(CE), C.c_int32(N),
+             C.c_int32(g.num_cell), block=1)
+    m.launch("do_interactions_monaghan", N, P(T["blanked"]), P(T["v_der"]), P(T["S_der"]), P(T["pos_t"]),
+             P(T["vel_t"]), P(T["T_t"]), C.c_uint32(N))
+    R = {k: v.cpu().numpy() for k, v in T.items()}
+    check(G, R, ["v_der", "S_der", "pos_t", "vel_t", "T_t"], rtol=RTOL_SUMS)
+    assert np.abs(R["S_der"]).max() > 0 and np.abs(R["T_t"]).max() > 0
+
+
+def test_interactions_heat_pse(lib, base):
+    """do_interactions_heat_pse with the reference's bindings: its tool-flag
+    texture covers N ints of the N-double array, so particles from index N/2 on
+    take the workpiece diffusivity; the product keeps that."""
+    c, H = base
+    k = c.constants
+    saved = k.trml_tool_sph.alpha
+    k.trml_tool_sph.alpha = 2.5 * k.trml_wp.alpha          # tool particles of both halves matter
+    try:
+        s = sorted_product(c, H, pse=True)
+        H2, (cs, ce), g = s.download(), s.cells(), s.geometry()
+        s.call("sph_interactions_heat_pse")
+        G = s.download()
+        s.close()
+        m = interactions_module(c, g)
+    finally:
+        k.trml_tool_sph.alpha = saved
+    N = len(H2["rho"])
+    T = device(H2)
+    CS, CE = torch.tensor(cs, device="cuda"), torch.tensor(ce, device="cuda")
+    m.launch("ref_bind_interactions_pse", 1, P(T["pos"]), P(T["h"]), P(T["rho"]), P(T["T"]), P(T["hash"]),
+             P(T["tool_particle"]), P(CS), P(CE), C.c_int32(N), C.c_int32(g.num_cell), block=1)
+    m.launch("do_interactions_heat_pse", N, P(T["blanked"]), P(T["T_t"]), C.c_int32(N),
+             C.c_double(c.constants.trml_wp.alpha), C.c_double(2.5 * c.constants.trml_wp.alpha))
+    R = {k: v.cpu().numpy() for k, v in T.items()}
+    check(G, R, ["T_t"], rtol=RTOL_SUMS)
+    tool = H2["tool_particle"] == 1.0
+    idx = np.arange(N)
+    assert tool[idx < N // 2].any() and tool[idx >= N // 2].any()
