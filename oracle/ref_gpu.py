@@ -2,7 +2,7 @@
 parity pin.
 
 ``oracle/Makefile`` (target ``ref_gpu``) compiles the reference's
-actions_gpu.cu, leap_frog.cu, grid.cu and interactions_gpu.cu, unmodified,
+actions_gpu.cu, leap_frog.cu, grid.cu, grid_gpu_green.cu and interactions_gpu.cu, unmodified,
 from the read-only reference tree into cubins for sm_103a under
 ``oracle/_ref/`` (with the stand-in GLM, gmsh and texture-reference headers of
 ``oracle/ref_shim``).  This module loads them
@@ -13,7 +13,8 @@ never part of the product; only the GPU tests import it.
 Kernel arguments are ctypes values: ``ptr(tensor)`` for a device pointer,
 ``C.c_int32`` / ``C.c_double`` scalars, and the ctypes structures below,
 which restate the reference's by-value parameter types (particle_gpu.h:22-79,
-leap_frog.cu:13-23, segment_FEM_gpu.h:31-48) field for field.
+leap_frog.cu:13-23, segment_FEM_gpu.h:31-48, grid_gpu_green.h:33-63) field for
+field.
 """
 from __future__ import annotations
 
@@ -23,7 +24,7 @@ from pathlib import Path
 
 REF_DIR = Path(__file__).resolve().parent / "_ref"
 CUBINS = {"actions": "ref_gpu_actions.cubin", "leap_frog": "ref_gpu_leapfrog.cubin", "grid": "ref_gpu_grid.cubin",
-          "interactions": "ref_gpu_interactions.cubin"}
+          "interactions": "ref_gpu_interactions.cubin", "green": "ref_gpu_green.cubin"}
 BLOCK_SIZE = 256   # the reference's BLOCK_SIZE (types.h)
 
 P = C.c_uint64     # device pointer
@@ -47,6 +48,13 @@ class SegmentFEMGPU(C.Structure):
     _fields_ = [("vptr", P), ("segment_num", C.c_int32), ("pad", C.c_int32)] + \
         [(n, P) for n in ("left", "right", "n", "marks", "heat_exchange", "fric_heat", "wear_rate", "wear_nodes",
                           "physical_para", "sliding_force")]
+
+
+class DeviceBuffer(C.Structure):
+    """grid_gpu_green::device_buffer (grid_gpu_green.h:33-63) with USE_FEM_TOOL."""
+    _fields_ = [(n, P) for n in ("pos", "vel", "fc", "ft", "h", "n", "rho", "S", "eps_pl", "eps_pl_dot", "T",
+                                 "fixed", "blanked", "tool_particle", "pos_t", "vel_t", "rho_t", "S_t", "T_t",
+                                 "on_seg")]
 
 
 class GeomConstants(C.Structure):
@@ -109,11 +117,12 @@ class RefModule:
             raise KeyError(f"{name}: {hits or 'not found'} among {sorted(self.names)}")
         return self.names[hits[0]]
 
-    def launch(self, name: str, n_threads: int, *args, block: int = BLOCK_SIZE):
-        """Launches ``name`` over n_threads (the reference's 1-D grids) and waits."""
+    def launch(self, name: str, n_threads: int, *args, block: int = BLOCK_SIZE, shared: int = 0):
+        """Launches ``name`` over n_threads (the reference's 1-D grids, ``shared``
+        bytes of dynamic shared memory) and waits."""
         f = self.func(name)
         grid = max(1, (n_threads + block - 1) // block)
         holders = list(args)
         argv = (C.c_void_p * max(1, len(holders)))(*[C.cast(C.pointer(a), C.c_void_p) for a in holders])
-        self.d.ck(self.d.cu.cuLaunchKernel(f, grid, 1, 1, block, 1, 1, 0, None, argv, None), f"launch {name}")
+        self.d.ck(self.d.cu.cuLaunchKernel(f, grid, 1, 1, block, 1, 1, shared, None, argv, None), f"launch {name}")
         self.d.ck(self.d.cu.cuCtxSynchronize(), f"sync {name}")

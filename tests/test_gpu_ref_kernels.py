@@ -434,3 +434,47 @@ def test_interactions_heat_pse(lib, base):
     tool = H2["tool_particle"] == 1.0
     idx = np.arange(N)
     assert tool[idx < N // 2].any() and tool[idx >= N // 2].any()
+
+
+# ---- cell list: grid_gpu_green::sort ----------------------------------------------------------
+def test_sort_and_cell_tables(lib, base):
+    """grid_gpu_green::sort (grid_gpu_green.cu:185-209) on a shuffled state:
+    compute_hashes, thrust::sort_by_key of the int hashes (a stable radix sort;
+    numpy's stable argsort stands in for it here), then the reference's own
+    reorder_data_and_find_cell_start; permutation, sorted hashes, every
+    reordered field and the cell tables bit for bit (cell_end where the cell is
+    occupied: the reference leaves it stale elsewhere)."""
+    grid, green = module("grid"), module("green")
+    c, H = base
+    rng = np.random.default_rng(23)
+    perm = rng.permutation(len(H["rho"]))
+    H = {k: np.ascontiguousarray(v[perm]) for k, v in H.items()}
+    s = Solver(c)
+    g = s.geometry()
+    s.upload(H)
+    s.call("sph_assign_hashes")
+    s.call("sph_sort")
+    G, (cs, ce) = s.download(), s.cells()
+    s.close()
+    N = len(H["rho"])
+    T = device(H)
+    grid.launch("compute_hashes", N, P(T["blanked"]), P(T["pos"]), P(T["hash"]), C.c_int32(N), C.c_double(g.dx),
+                C.c_int32(g.ny), C.c_double(g.bbmin_x), C.c_double(g.bbmin_y))
+    hashes = T["hash"].cpu().numpy()
+    assert hashes.min() >= 0 and hashes.max() < g.num_cell, "the reorder kernel indexes its cell tables by hash"
+    order = np.argsort(hashes, kind="stable").astype(np.int32)
+    T["hash"] = torch.tensor(hashes[order], device="cuda")
+    T["idx"] = torch.tensor(order, device="cuda")
+    Bf = {k: torch.empty_like(T[k]) for k, _, _ in abi.PARTICLE_FIELDS if k in [f for f, _ in ref_gpu.DeviceBuffer._fields_]}
+    buf = ref_gpu.DeviceBuffer(**{k: ref_gpu.ptr(v) for k, v in Bf.items()})
+    CS = torch.full((g.num_cell,), -1, dtype=torch.int32, device="cuda")
+    CE = torch.full((g.num_cell,), -7, dtype=torch.int32, device="cuda")
+    green.launch("reorder_data_and_find_cell_start", N, particle_struct(T, N), buf, P(CS), P(CE), C.c_int32(N),
+                 block=512, shared=(512 + 1) * 4)
+    assert np.array_equal(G["idx"], order) and np.array_equal(G["hash"], hashes[order])
+    for k, v in Bf.items():
+        assert np.array_equal(G[k], v.cpu().numpy(), equal_nan=True), k
+    rcs, rce = CS.cpu().numpy(), CE.cpu().numpy()
+    assert np.array_equal(cs, rcs)
+    occ = rcs != -1
+    assert np.array_equal(ce[occ], rce[occ]) and occ.sum() > 100
