@@ -2,7 +2,8 @@
 parity pin.
 
 ``oracle/Makefile`` (target ``ref_gpu``) compiles the reference's
-actions_gpu.cu, leap_frog.cu, grid.cu, grid_gpu_green.cu and interactions_gpu.cu, unmodified,
+actions_gpu.cu, leap_frog.cu, grid.cu, grid_gpu_green.cu, interactions_gpu.cu,
+FEM_thermal_gpu.cu and tool_FEM.cu, unmodified,
 from the read-only reference tree into cubins for sm_103a under
 ``oracle/_ref/`` (with the stand-in GLM, gmsh and texture-reference headers of
 ``oracle/ref_shim``).  This module loads them
@@ -24,7 +25,8 @@ from pathlib import Path
 
 REF_DIR = Path(__file__).resolve().parent / "_ref"
 CUBINS = {"actions": "ref_gpu_actions.cubin", "leap_frog": "ref_gpu_leapfrog.cubin", "grid": "ref_gpu_grid.cubin",
-          "interactions": "ref_gpu_interactions.cubin", "green": "ref_gpu_green.cubin"}
+          "interactions": "ref_gpu_interactions.cubin", "green": "ref_gpu_green.cubin", "fem": "ref_gpu_fem.cubin",
+          "tool": "ref_gpu_tool.cubin"}
 BLOCK_SIZE = 256   # the reference's BLOCK_SIZE (types.h)
 
 P = C.c_uint64     # device pointer

@@ -2,7 +2,8 @@
 // only).  GLM is a third-party dependency of the reference that this image
 // does not have.  This header provides the GLM types and functions the
 // reference's host geometry (tool.cpp, geometric_primitives.cpp) and its
-// device code (actions_gpu.cu, leap_frog.cu, grid.cu) use, written from
+// device code (actions_gpu.cu, leap_frog.cu, grid.cu, FEM_thermal_gpu.cu,
+// tool_FEM.cu) use, written from
 // GLM's documented semantics:
 //   - vectors with component-wise +, -, *, / and scalar forms;
 //   - column-major matrices built column by column (m[c][r] is column c, row
@@ -10,8 +11,9 @@
 //   - matrix + - matrix and scalar * matrix component-wise; matrix * matrix
 //     the linear-algebra product, column c of the result being
 //     a[0] * b[c][0] + a[1] * b[c][1] (+ a[2] * b[c][2]);
-//   - transpose; row vector * matrix is the vector's dot product with each
-//     column;
+//   - transpose; the inverse of a 2x2 as its adjugate over its determinant;
+//     row vector * matrix is the vector's dot product with each column;
+//   - == / != of vectors component-wise;
 //   - dot(a, b) = (a * b).x + (a * b).y; length(v) = sqrt(dot(v, v));
 //     distance(a, b) = length(b - a); normalize(v) = v * inversesqrt(dot(v, v))
 //     with inversesqrt(x) = 1 / sqrt(x);
@@ -95,8 +97,69 @@ struct tmat3x3 {
     GLMS_HD const tvec3<T> &operator[](int i) const { return c[i]; }
 };
 
-template <class T> struct tmat3x2 { tvec2<T> c[3]; };
-template <class T> struct tmat2x3 { tvec3<T> c[2]; };
+// 3 columns of 2 rows
+template <class T>
+struct tmat3x2 {
+    tvec2<T> c[3];
+    GLMS_HD tmat3x2() : c{tvec2<T>(1, 0), tvec2<T>(0, 1), tvec2<T>(0, 0)} {}
+    GLMS_HD explicit tmat3x2(T s) : c{tvec2<T>(s, 0), tvec2<T>(0, s), tvec2<T>(0, 0)} {}
+    GLMS_HD tmat3x2(T x0, T y0, T x1, T y1, T x2, T y2) : c{tvec2<T>(x0, y0), tvec2<T>(x1, y1), tvec2<T>(x2, y2)} {}
+    GLMS_HD tvec2<T> &operator[](int i) { return c[i]; }
+    GLMS_HD const tvec2<T> &operator[](int i) const { return c[i]; }
+};
+
+// 2 columns of 3 rows
+template <class T>
+struct tmat2x3 {
+    tvec3<T> c[2];
+    GLMS_HD tmat2x3() : c{tvec3<T>(1, 0, 0), tvec3<T>(0, 1, 0)} {}
+    GLMS_HD explicit tmat2x3(T s) : c{tvec3<T>(s, 0, 0), tvec3<T>(0, s, 0)} {}
+    GLMS_HD tmat2x3(T x0, T y0, T z0, T x1, T y1, T z1) : c{tvec3<T>(x0, y0, z0), tvec3<T>(x1, y1, z1)} {}
+    GLMS_HD tvec3<T> &operator[](int i) { return c[i]; }
+    GLMS_HD const tvec3<T> &operator[](int i) const { return c[i]; }
+};
+
+template <class T> GLMS_HD bool operator==(const tvec2<T> &a, const tvec2<T> &b) { return a.x == b.x && a.y == b.y; }
+template <class T> GLMS_HD bool operator!=(const tvec2<T> &a, const tvec2<T> &b) { return !(a == b); }
+template <class T> GLMS_HD bool operator==(const tvec3<T> &a, const tvec3<T> &b) {
+    return a.x == b.x && a.y == b.y && a.z == b.z;
+}
+template <class T> GLMS_HD bool operator!=(const tvec3<T> &a, const tvec3<T> &b) { return !(a == b); }
+
+// transposes
+template <class T> GLMS_HD tmat2x2<T> transpose(const tmat2x2<T> &m) {
+    return tmat2x2<T>(m[0][0], m[1][0], m[0][1], m[1][1]);
+}
+template <class T> GLMS_HD tmat3x2<T> transpose(const tmat2x3<T> &m) {
+    return tmat3x2<T>(m[0][0], m[1][0], m[0][1], m[1][1], m[0][2], m[1][2]);
+}
+template <class T> GLMS_HD tmat2x3<T> transpose(const tmat3x2<T> &m) {
+    return tmat2x3<T>(m[0][0], m[1][0], m[2][0], m[0][1], m[1][1], m[2][1]);
+}
+
+// inverse of a 2x2: the adjugate over the determinant
+template <class T> GLMS_HD tmat2x2<T> inverse(const tmat2x2<T> &m) {
+    const T one_over_det = static_cast<T>(1) / (m[0][0] * m[1][1] - m[1][0] * m[0][1]);
+    return tmat2x2<T>(m[1][1] * one_over_det, -m[0][1] * one_over_det, -m[1][0] * one_over_det,
+                      m[0][0] * one_over_det);
+}
+
+// products: column c of a * b is the sum over k of a's column k times b[c][k]
+template <class T> GLMS_HD tmat3x2<T> operator*(const tmat2x2<T> &a, const tmat3x2<T> &b) {
+    tmat3x2<T> r;
+    for (int c = 0; c < 3; c++) r[c] = a[0] * b[c][0] + a[1] * b[c][1];
+    return r;
+}
+template <class T> GLMS_HD tmat3x3<T> operator*(const tmat2x3<T> &a, const tmat3x2<T> &b) {
+    tmat3x3<T> r;
+    for (int c = 0; c < 3; c++) r[c] = a[0] * b[c][0] + a[1] * b[c][1];
+    return r;
+}
+template <class T> GLMS_HD tmat2x3<T> operator*(T s, const tmat2x3<T> &m) {
+    tmat2x3<T> r;
+    for (int i = 0; i < 2; i++) r[i] = s * m[i];
+    return r;
+}
 
 template <class T> GLMS_HD T dot(const tvec2<T> &a, const tvec2<T> &b) {
     tvec2<T> t = a * b;
@@ -136,6 +199,10 @@ template <class T> GLMS_HD tmat3x3<T> operator*(const tmat3x3<T> &a, const tmat3
     tmat3x3<T> r;
     for (int c = 0; c < 3; c++) r[c] = a[0] * b[c][0] + a[1] * b[c][1] + a[2] * b[c][2];
     return r;
+}
+template <class T> GLMS_HD tmat3x3<T> &operator+=(tmat3x3<T> &a, const tmat3x3<T> &b) {
+    for (int i = 0; i < 3; i++) a[i] = a[i] + b[i];
+    return a;
 }
 template <class T> GLMS_HD tmat3x3<T> transpose(const tmat3x3<T> &m) {
     return tmat3x3<T>(m[0][0], m[1][0], m[2][0], m[0][1], m[1][1], m[2][1], m[0][2], m[1][2], m[2][2]);

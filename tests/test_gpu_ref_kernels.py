@@ -478,3 +478,71 @@ def test_sort_and_cell_tables(lib, base):
     assert np.array_equal(cs, rcs)
     occ = rcs != -1
     assert np.array_equal(ce[occ], rce[occ]) and occ.sum() > 100
+
+
+# ---- the tool's FEM heat step and the tool / segment moves -----------------------------------------
+def test_fem_heat_step(actions, cut):
+    """reset_FEM_server, apply_robin_bdc over the cutting-edge colours,
+    calculate_temp_rate and calculate_temp (FEM_thermal_gpu.cu:443-468,865-921)
+    after a contact and friction pass has filled the segments' heat exchange:
+    temperature rate and temperature of every node within 1e-13 relative,
+    norm-wise.  The product adds the Robin terms to each node in one fixed
+    order; the reference adds them colour by colour with FP64 atomics, so the
+    diagonal and right-hand side can round differently."""
+    c, s = cut
+    fem_m = module("fem")
+    fem_m.launch("ref_set_fem_constants", 1, c.constants.tool, block=1)
+    s.call("sph_compute_contact_forces_fem")
+    s.call("sph_material_fric_heat_gen_fem")
+    seg, fem, ts = s.segments(), s.fem(), s.tool_state()
+    assert np.abs(seg["heat_exchange"][:, 1]).sum() > 0, "segments in contact"
+    s.call("sph_fem_reset_server")
+    s.call("sph_fem_apply_robin")
+    s.call("sph_fem_calculate_temp_rate")
+    k_prod = s.fem()["k"]
+    s.call("sph_fem_calculate_temp", C.c_double(c.dt))
+    T_prod = s.fem()["T"]
+    D = {k: torch.tensor(np.ascontiguousarray(v), device="cuda") for k, v in fem.items()}
+    Sg = {k: torch.tensor(np.ascontiguousarray(v), device="cuda") for k, v in seg.items()}
+    nn, nz, ns = len(fem["T"]), len(fem["K"]), ts.n_segments
+    K_temp, f_temp, T_old = torch.empty_like(D["K"]), torch.empty_like(D["f"]), torch.empty_like(D["T"])
+    fem_m.launch("do_copy_vector", nn, C.c_int32(nn), P(D["T"]), P(T_old))
+    fem_m.launch("do_copy_vector", nn, C.c_int32(nn), P(D["f"]), P(f_temp))
+    fem_m.launch("do_copy_vector", nz, C.c_int32(nz), P(D["K"]), P(K_temp))
+    for colour in range(1, ts.n_cut_colors + 1):
+        fem_m.launch("do_apply_heat_boundary_condition", ns, C.c_int32(colour), C.c_int32(ns), P(Sg["marks"]),
+                     P(Sg["heat_exchange"]), P(Sg["fric_heat"]), P(Sg["left"]), P(Sg["right"]), P(D["row_ptr"]),
+                     P(D["col_ind"]), P(K_temp), P(f_temp), block=16)
+    fem_m.launch("do_calculate_temp_rate", nn, C.c_int32(nn), P(D["M_inv"]), P(K_temp), P(D["row_ptr"]),
+                 P(D["col_ind"]), P(f_temp), P(D["k"]), P(D["T"]))
+    e = rel_err(k_prod, D["k"].cpu().numpy())
+    assert e <= 1e-13, f"FEM temperature rate: {e:.3e}"
+    fem_m.launch("do_calculate_temp", nn, C.c_int32(nn), P(D["k"]), P(D["T"]), P(T_old), C.c_double(c.dt))
+    e = rel_err(T_prod, D["T"].cpu().numpy())
+    assert e <= 1e-13, f"FEM temperature: {e:.3e}"
+    assert np.abs(k_prod).max() > 0
+
+
+def test_tool_and_segment_move(cut):
+    """tool_update_FEM_gpu and segments_update (tool_FEM.cu:109-139,1552-1582):
+    node positions, segment end points (with the flank retreat) and the reset
+    of the segments' heat exchange and friction heat, bit for bit."""
+    c, s = cut
+    tool_m = module("tool")
+    seg, fem, ts = s.segments(), s.fem(), s.tool_state()
+    dt = 7.0 * c.dt
+    s.call("sph_segments_update", C.c_double(dt))
+    s.call("sph_tool_update_fem", C.c_double(dt))
+    seg2, pos2 = s.segments(), s.fem()["position"]
+    tool_m.launch("ref_set_flank", 1, C.c_double(ts.flank_retreat), C.c_double(ts.flank_contact), block=1)
+    Sg = {k: torch.tensor(np.ascontiguousarray(v), device="cuda") for k, v in seg.items()}
+    X = torch.tensor(fem["position"], device="cuda")
+    vel = ref_gpu.Vec2(*ts.vel)
+    n, nn = ts.n_segments, len(fem["T"])
+    tool_m.launch("do_segments_update", n, C.c_int32(n), P(Sg["left"]), P(Sg["right"]), P(Sg["heat_exchange"]),
+                  P(Sg["fric_heat"]), vel, C.c_double(dt))
+    tool_m.launch("do_tool_update_FEM_gpu", nn, C.c_int32(nn), P(X), vel, C.c_double(dt))
+    for k in ("left", "right", "heat_exchange", "fric_heat"):
+        assert np.array_equal(seg2[k], Sg[k].cpu().numpy()), k
+    assert np.array_equal(pos2, X.cpu().numpy())
+    assert np.any(pos2 != fem["position"])
