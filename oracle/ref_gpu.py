@@ -128,3 +128,155 @@ class RefModule:
         argv = (C.c_void_p * max(1, len(holders)))(*[C.cast(C.pointer(a), C.c_void_p) for a in holders])
         self.d.ck(self.d.cu.cuLaunchKernel(f, grid, 1, 1, block, 1, 1, shared, None, argv, None), f"launch {name}")
         self.d.ck(self.d.cu.cuCtxSynchronize(), f"sync {name}")
+
+
+# ---- the reference's FEM-tool step, composed from its own kernels -----------------------------------
+SORTED = [n for n, _ in DeviceBuffer._fields_]          # the fields grid_gpu_green reorders
+
+
+class RefFemStep:
+    """leap_frog::step(particles, grid, tool_FEM) (leap_frog.cu:162-248) run as
+    the reference runs it: every kernel launch of the step, in its order, from
+    the reference's own cubins, with the host side of the step restated here
+    (the sort's thrust::sort_by_key of the int hashes as a stable argsort, the
+    double-buffer swap of grid_gpu_green, the tool's host reference points,
+    the colour loop of apply_robin_bdc).  State lives in torch tensors:
+    ``P`` particles (particle_gpu fields), ``F`` the FEM system (position,
+    row_ptr, col_ind, K, M_inv, f, T, k and the step's K_temp, f_temp, T_old),
+    ``S`` segments.  No wear (wear_pro off)."""
+
+    def __init__(self, constants, geom, dt, particles: dict, fem: dict, segments: dict, tool_state):
+        import numpy as np
+        import torch
+        self.torch, self.np = torch, np
+        self.c, self.g, self.dt = constants, geom, float(dt)
+        self.m = {k: RefModule(k) for k in ("actions", "leap_frog", "grid", "green", "interactions", "fem", "tool")}
+        zero_wear = (C.c_double * 4)()
+        k = constants
+        self.m["actions"].launch("ref_set_actions_constants", 1, k.phys, k.corr, k.joco, k.trml_wp, k.trml_tool,
+                                 k.tool, zero_wear, block=1)
+        ge = GeomConstants(geom.nx, geom.ny, geom.bbmin_x, geom.bbmin_y, geom.dx)
+        self.m["interactions"].launch("ref_set_interactions_constants", 1, k.phys, k.corr, ge, k.trml_wp,
+                                      k.trml_tool_sph, k.tool, block=1)
+        self.m["fem"].launch("ref_set_fem_constants", 1, k.tool, block=1)
+        dev = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+        self.P = {f: dev(v) for f, v in particles.items()}
+        self.N = len(particles["rho"])
+        self.F = {f: dev(v) for f, v in fem.items()}
+        self.F["K_temp"], self.F["f_temp"], self.F["T_old"] = (torch.empty_like(self.F["K"]),
+                                                               torch.empty_like(self.F["f"]),
+                                                               torch.empty_like(self.F["T"]))
+        n = len(segments["left"])
+        self.S = {f: dev(v) for f, v in segments.items()}
+        for f, shape in (("wear_rate", (n, 2)), ("wear_nodes", (n,)), ("physical_para", (n, 4)),
+                         ("sliding_force", (n,))):
+            self.S[f] = torch.zeros(shape, dtype=torch.float64, device="cuda")
+        self.n_seg, self.n_colors = n, tool_state.n_cut_colors
+        self.vel = (tool_state.vel[0], tool_state.vel[1])
+        self.tl_ref = [tool_state.tl_point_ref[0], tool_state.tl_point_ref[1]]
+        self.ref_dist = tool_state.ref_dist
+        self.lowest = tool_state.lowest_point
+        self.cell_start = torch.full((geom.num_cell,), -1, dtype=torch.int32, device="cuda")
+        self.cell_end = torch.zeros(geom.num_cell, dtype=torch.int32, device="cuda")
+        ini = {"pos_init": (self.N, 2), "vel_init": (self.N, 2), "S_init": (self.N, 4), "rho_init": (self.N,),
+               "T_init": (self.N,), "T_init_tool": (1,)}
+        self.I = {f: torch.zeros(s, dtype=torch.float64, device="cuda") for f, s in ini.items()}
+
+    def particles(self):
+        st = ParticleGPU()
+        for f, _ in ParticleGPU._fields_[:-1]:
+            setattr(st, f, ptr(self.P[f]))
+        st.N = self.N
+        return st
+
+    def segments(self):
+        sg = SegmentFEMGPU()
+        sg.segment_num = self.n_seg
+        for f, src in (("left", "left"), ("right", "right"), ("n", "normal"), ("marks", "marks"),
+                       ("heat_exchange", "heat_exchange"), ("fric_heat", "fric_heat"), ("wear_rate", "wear_rate"),
+                       ("wear_nodes", "wear_nodes"), ("physical_para", "physical_para"),
+                       ("sliding_force", "sliding_force")):
+            setattr(sg, f, ptr(self.S[src]))
+        return sg
+
+    def _sort(self):
+        """grid_base::assign_hashes + grid_gpu_green::sort (grid.cu:25-42,80-86;
+        grid_gpu_green.cu:185-209)."""
+        torch, np, g, N = self.torch, self.np, self.g, self.N
+        P = self.P
+        self.m["grid"].launch("compute_hashes", N, ptr(P["blanked"]), ptr(P["pos"]), ptr(P["hash"]), C.c_int32(N),
+                              C.c_double(g.dx), C.c_int32(g.ny), C.c_double(g.bbmin_x), C.c_double(g.bbmin_y))
+        h = P["hash"].cpu().numpy()
+        if h.min() < 0 or h.max() >= g.num_cell:
+            raise ValueError("a particle hashed outside the grid: the reference's reorder kernel would index "
+                             "its cell tables out of range")
+        order = np.argsort(h, kind="stable").astype(np.int32)
+        P["hash"] = torch.tensor(h[order], device="cuda")
+        P["idx"] = torch.tensor(order, device="cuda")
+        buf = {f: torch.empty_like(P[f]) for f in SORTED}
+        self.cell_start.fill_(-1)
+        self.m["green"].launch("reorder_data_and_find_cell_start", N, self.particles(),
+                               DeviceBuffer(**{f: ptr(v) for f, v in buf.items()}), ptr(self.cell_start),
+                               ptr(self.cell_end), C.c_int32(N), block=512, shared=(512 + 1) * 4)
+        P.update(buf)   # the double-buffer swap
+
+    def step(self):
+        a, lf, it, fm, tl = (self.m[k] for k in ("actions", "leap_frog", "interactions", "fem", "tool"))
+        P, F, S, N, dt, k = self.P, self.F, self.S, self.N, self.dt, self.c
+        I = IniState(**{f: ptr(v) for f, v in self.I.items()})
+        nn, nz = len(self.F["T"]), len(self.F["K"])
+        self._sort()
+        lf.launch("init", N, self.particles(), I)
+        fm.launch("do_copy_vector", nn, C.c_int32(nn), ptr(F["T"]), ptr(F["T_old"]))           # reset_FEM_server
+        fm.launch("do_copy_vector", nn, C.c_int32(nn), ptr(F["f"]), ptr(F["f_temp"]))
+        fm.launch("do_copy_vector", nz, C.c_int32(nz), ptr(F["K"]), ptr(F["K_temp"]))
+        lf.launch("predict", N, self.particles(), I, C.c_double(dt))
+        fm.launch("do_calculate_temp", nn, C.c_int32(nn), ptr(F["k"]), ptr(F["T"]), ptr(F["T_old"]),
+                  C.c_double(0.5 * dt))
+        a.launch("do_material_eos", N, ptr(P["rho"]), ptr(P["p"]), ptr(P["tool_particle"]), C.c_int32(N))
+        a.launch("do_corrector_artificial_stress", N, ptr(P["rho"]), ptr(P["p"]), ptr(P["S"]),
+                 ptr(P["tool_particle"]), ptr(P["R"]), C.c_int32(N))
+        it.launch("ref_bind_interactions", 1, ptr(P["pos"]), ptr(P["vel"]), ptr(P["S"]), ptr(P["R"]), ptr(P["h"]),
+                  ptr(P["rho"]), ptr(P["p"]), ptr(P["T"]), ptr(P["hash"]), ptr(P["tool_particle"]), ptr(P["fc"]),
+                  ptr(self.cell_start), ptr(self.cell_end), C.c_int32(N), C.c_int32(self.g.num_cell), block=1)
+        it.launch("do_interactions_monaghan", N, ptr(P["blanked"]), ptr(P["v_der"]), ptr(P["S_der"]),
+                  ptr(P["pos_t"]), ptr(P["vel_t"]), ptr(P["T_t"]), C.c_uint32(N))
+        a.launch("do_material_stress_rate_jaumann", N, ptr(P["v_der"]), ptr(P["S"]), ptr(P["tool_particle"]),
+                 ptr(P["S_t"]), C.c_int32(N))
+        a.launch("do_contmech_continuity", N, ptr(P["rho"]), ptr(P["v_der"]), ptr(P["tool_particle"]),
+                 ptr(P["rho_t"]), C.c_int32(N))
+        a.launch("do_contmech_momentum", N, ptr(P["S_der"]), ptr(P["fc"]), ptr(P["ft"]), ptr(P["tool_particle"]),
+                 ptr(P["vel_t"]), C.c_int32(N))
+        a.launch("do_contmech_advection", N, ptr(P["vel"]), ptr(P["tool_particle"]), ptr(P["pos_t"]), C.c_int32(N))
+        lf.launch("correct", N, self.particles(), I, C.c_double(dt))
+        vel2 = Vec2(*self.vel)
+        a.launch("do_material_fric_heat_gen_FEM_v21", N, self.particles(), self.segments(), vel2, ptr(F["T"]),
+                 C.c_double(dt), C.c_int32(N))
+        for colour in range(1, self.n_colors + 1):                                             # apply_robin_bdc
+            fm.launch("do_apply_heat_boundary_condition", self.n_seg, C.c_int32(colour), C.c_int32(self.n_seg),
+                      ptr(S["marks"]), ptr(S["heat_exchange"]), ptr(S["fric_heat"]), ptr(S["left"]),
+                      ptr(S["right"]), ptr(F["row_ptr"]), ptr(F["col_ind"]), ptr(F["K_temp"]), ptr(F["f_temp"]),
+                      block=16)
+        fm.launch("do_calculate_temp_rate", nn, C.c_int32(nn), ptr(F["M_inv"]), ptr(F["K_temp"]), ptr(F["row_ptr"]),
+                  ptr(F["col_ind"]), ptr(F["f_temp"]), ptr(F["k"]), ptr(F["T"]))
+        fm.launch("do_calculate_temp", nn, C.c_int32(nn), ptr(F["k"]), ptr(F["T"]), ptr(F["T_old"]), C.c_double(dt))
+        if k.plastic:
+            a.launch("do_plasticity_johnson_cook", N, self.particles(), C.c_double(dt))
+        tl.launch("ref_set_flank", 1, C.c_double(0.0), C.c_double(self.lowest), block=1)
+        tl.launch("do_segments_update", self.n_seg, C.c_int32(self.n_seg), ptr(S["left"]), ptr(S["right"]),
+                  ptr(S["heat_exchange"]), ptr(S["fric_heat"]), vel2, C.c_double(dt))
+        tl.launch("do_tool_update_FEM_gpu", nn, C.c_int32(nn), ptr(F["position"]), vel2, C.c_double(dt))
+        self.tl_ref = [self.tl_ref[0] + self.vel[0] * dt, self.tl_ref[1] + self.vel[1] * dt]   # tool_update_FEM_gpu
+        self.lowest = self.lowest + self.vel[1] * dt
+        a.launch("do_compute_contact_forces_FEM_tool_v3_s1", N, C.c_int32(N), self.particles(), self.segments(),
+                 Vec2(*self.tl_ref), C.c_double(self.ref_dist), vel2, C.c_double(dt), C.c_int32(self.n_seg), block=1)
+        a.launch("do_compute_contact_forces_FEM_tool_v3_s2", N, C.c_int32(N), self.particles(), self.segments(),
+                 ptr(F["T"]), C.c_double(dt), block=1)
+        a.launch("do_boundary_conditions", N, self.particles())
+        if k.trml_tool.alpha != 0.0:
+            a.launch("do_boundary_conditions_thermal", N, self.particles())
+        a.launch("do_invalidate", N, self.particles(), C.c_int32(0))
+
+    def host(self):
+        return ({f: v.cpu().numpy() for f, v in self.P.items()}, {f: v.cpu().numpy() for f, v in self.F.items()},
+                {f: v.cpu().numpy() for f, v in self.S.items()})

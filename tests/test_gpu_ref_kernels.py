@@ -546,3 +546,49 @@ def test_tool_and_segment_move(cut):
         assert np.array_equal(seg2[k], Sg[k].cpu().numpy()), k
     assert np.array_equal(pos2, X.cpu().numpy())
     assert np.any(pos2 != fem["position"])
+
+
+# ---- the whole step ------------------------------------------------------------------------------------
+@pytest.mark.parametrize("art_stress", [True, False], ids=["art_stress", "no_art_stress"])
+def test_fused_step_against_reference_step(lib, art_stress):
+    """Three fused, graph-replayed steps of the product against three
+    leap_frog::step(particles, grid, tool_FEM) (leap_frog.cu:162-248) composed
+    from the reference's own kernels (oracle/ref_gpu.RefFemStep), on the
+    Ti6Al4V cut with the tool in contact: cell list, permutation, segment ids
+    and blanking bit for bit; particle state, rates, FEM temperatures and the
+    segments norm-wise within
+      - 1e-12 without artificial stress: only the neighbour sums' 1e-16
+        reassociations, carried through three steps;
+      - 1e-8 with it: the stress angle's float trigonometry (CUDA's atan2f /
+        cosf / sinf in the reference, double-evaluated and rounded once here)
+        differs by float ULPs in R, and R enters the momentum sums."""
+    c = setups.ti64_cut()
+    if not art_stress:
+        c.constants.corr.stresseps = 0.0
+    tol = 1e-8 if art_stress else 1e-12
+    s = Solver(c)
+    s.move_tool(0.3 * c.info["dx"] / c.tool_speed)
+    s.step(20)
+    ref = ref_gpu.RefFemStep(c.constants, s.geometry(), c.dt, s.download(), s.fem(), s.segments(), s.tool_state())
+    for _ in range(3):
+        s.step()
+        ref.step()
+    G, Gf, Gs = s.download(), s.fem(), s.segments()
+    s.close()
+    R, Rf, Rs = ref.host()
+    for f in ("hash", "idx", "on_seg", "blanked", "fixed", "tool_particle"):
+        assert np.array_equal(G[f], R[f]), f"{f}: {np.count_nonzero(G[f] != R[f])} entries differ"
+    act = R["blanked"] != 1.0
+    for f in ("pos", "vel", "rho", "S", "T", "eps_pl", "eps_pl_dot", "p", "R", "fc", "ft", "n", "h"):
+        e = rel_err(G[f], R[f])
+        assert e <= (RTOL_FLOAT_TRIG if f == "R" else tol), f"{f}: {e:.3e}"
+    for f in ("pos_t", "vel_t", "rho_t", "S_t", "T_t"):
+        e = rel_err(G[f][act], R[f][act])
+        assert e <= tol, f"{f}: {e:.3e}"
+    for f in ("T", "k", "position"):
+        e = rel_err(Gf[f], Rf[f])
+        assert e <= tol, f"FEM {f}: {e:.3e}"
+    for f in ("left", "right", "heat_exchange", "fric_heat"):
+        e = rel_err(Gs[f], Rs[f]) if np.abs(Rs[f]).max() > 0 else float(np.abs(Gs[f]).max())
+        assert e <= tol, f"segments {f}: {e:.3e}"
+    assert np.count_nonzero(R["on_seg"] >= 0) >= 8
