@@ -3,7 +3,7 @@ parity pin.
 
 ``oracle/Makefile`` (target ``ref_gpu``) compiles the reference's
 actions_gpu.cu, leap_frog.cu, grid.cu, grid_gpu_green.cu, interactions_gpu.cu,
-FEM_thermal_gpu.cu and tool_FEM.cu, unmodified,
+FEM_thermal_gpu.cu, tool_FEM.cu and tool_gpu.cu, unmodified,
 from the read-only reference tree into cubins for sm_103a under
 ``oracle/_ref/`` (with the stand-in GLM, gmsh and texture-reference headers of
 ``oracle/ref_shim``).  This module loads them
@@ -26,7 +26,7 @@ from pathlib import Path
 REF_DIR = Path(__file__).resolve().parent / "_ref"
 CUBINS = {"actions": "ref_gpu_actions.cubin", "leap_frog": "ref_gpu_leapfrog.cubin", "grid": "ref_gpu_grid.cubin",
           "interactions": "ref_gpu_interactions.cubin", "green": "ref_gpu_green.cubin", "fem": "ref_gpu_fem.cubin",
-          "tool": "ref_gpu_tool.cubin"}
+          "tool": "ref_gpu_tool.cubin", "toolgpu": "ref_gpu_toolgpu.cubin"}
 BLOCK_SIZE = 256   # the reference's BLOCK_SIZE (types.h)
 
 P = C.c_uint64     # device pointer
@@ -63,6 +63,41 @@ class GeomConstants(C.Structure):
     """geom_constants (constants_structs.h:70-76)."""
     _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("bbmin_x", C.c_double), ("bbmin_y", C.c_double),
                 ("dx", C.c_double)]
+
+
+class LineGPU(C.Structure):
+    """line_gpu (tool_gpu.cuh:23-27)."""
+    _fields_ = [("a", C.c_double), ("b", C.c_double), ("vertical", C.c_bool)]
+
+
+class SegmentGPU(C.Structure):
+    """segment_gpu (tool_gpu.cuh:29-34): double2 members are 16-byte aligned."""
+    _fields_ = [("left", C.c_double * 2), ("right", C.c_double * 2), ("l", LineGPU), ("pad", C.c_double),
+                ("n", C.c_double * 2)]
+
+
+class CircleSegmentGPU(C.Structure):
+    """circle_segment_gpu (tool_gpu.cuh:36-41)."""
+    _fields_ = [("r", C.c_double), ("t1", C.c_double), ("t2", C.c_double), ("pad", C.c_double),
+                ("p", C.c_double * 2)]
+
+
+def rigid_tool_args(tool, contact_alpha: float, mass: float):
+    """The setter arguments of ref_set_rigid_tool for a product sph_rigid_tool:
+    (device buffer of segment_gpu, its torch tensor, count, fillet, has_fillet,
+    mu, alpha, mass, velocity)."""
+    import torch
+    segs = (SegmentGPU * max(1, tool.n_seg))()
+    for i in range(tool.n_seg):
+        s = segs[i]
+        s.left[:] = list(tool.left[i])
+        s.right[:] = list(tool.right[i])
+        s.n[:] = list(tool.n[i])
+        s.l.a, s.l.b, s.l.vertical = tool.la[i], tool.lb[i], bool(tool.vertical[i])
+    raw = torch.tensor(list(bytes(segs)), dtype=torch.uint8, device="cuda")
+    fil = CircleSegmentGPU(tool.fillet_r, tool.fillet_t1, tool.fillet_t2, 0.0, (C.c_double * 2)(*tool.fillet_p))
+    return raw, (ptr(raw), C.c_int32(tool.n_seg), fil, C.c_int32(tool.has_fillet), C.c_double(tool.mu),
+                 C.c_double(contact_alpha), C.c_double(mass), Vec2(*tool.vel))
 
 
 class Vec2(C.Structure):

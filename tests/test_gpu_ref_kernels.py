@@ -592,3 +592,72 @@ def test_fused_step_against_reference_step(lib, art_stress):
         e = rel_err(Gs[f], Rs[f]) if np.abs(Rs[f]).max() > 0 else float(np.abs(Gs[f]).max())
         assert e <= tol, f"segments {f}: {e:.3e}"
     assert np.count_nonzero(R["on_seg"] >= 0) >= 8
+
+
+# ---- the rigid (SPH-particle) tool: tool_gpu.cu ------------------------------------------------------------
+@pytest.fixture(scope="module")
+def rigid(lib):
+    """setup_ref_cut (benchmarks.cpp:247-530) at 30 rows, the tool 0.8 dx into the
+    workpiece, after 5 fused steps (about 10 particles in contact); the solver
+    stays open."""
+    c = setups.ref_cut(ny=30, length=0.04, preload_dx=0.8)
+    s = Solver(c)
+    s.step(5)
+    m = module("toolgpu")
+    yield c, s, m
+    s.close()
+
+
+def set_rigid(m, c, s):
+    raw, args = ref_gpu.rigid_tool_args(s.rigid_tool(), c.constants.tool.contact_alpha, c.constants.phys.mass)
+    m.launch("ref_set_rigid_tool", 1, *args, block=1)
+    return raw
+
+
+def test_rigid_contact_forces(rigid):
+    """compute_contact_forces (tool_gpu.cu:146-203): penalty normal force and
+    LS-DYNA friction against the rigid outline and its fillet, within 1e-13
+    relative, norm-wise: the product keeps the host geometry's uncontracted
+    roundings (it is pinned bit for bit to tool.cpp), the reference's device
+    code lets the compiler contract them into FMAs (1e-16 seen on other states)."""
+    c, s, m = rigid
+    raw = set_rigid(m, c, s)
+    H = s.download()
+    s.call("sph_compute_contact_forces")
+    G = s.download()
+    R = ref_run(H, lambda T, pg, N: m.launch("do_compute_contact_forces", N, pg, C.c_double(c.dt)))
+    check(G, R, ["fc", "ft", "n"], rtol=1e-13)
+    assert np.count_nonzero(np.abs(R["fc"]).sum(1) > 0) >= 5, "particles in contact"
+    del raw
+
+
+def test_rigid_friction_heat(actions, rigid):
+    """material_fric_heat_gen (actions_gpu.cu:316-343, :956-965), bit for bit."""
+    c, s, m = rigid
+    k = c.constants
+    actions.launch("ref_set_actions_constants", 1, k.phys, k.corr, k.joco, k.trml_wp, k.trml_tool, k.tool,
+                   abi.WearConstants(0.0, 0.0, 0.0, 0.0), block=1)
+    assert k.trml_wp.eta != 0.0
+    H = s.download()
+    s.call("sph_material_fric_heat_gen")
+    G = s.download()
+    vt = s.rigid_tool().vel
+    R = ref_run(H, lambda T, pg, N: actions.launch("do_material_fric_heat_gen", N, P(T["vel"]), P(T["ft"]), P(T["n"]),
+                                                    P(T["tool_particle"]), P(T["T"]), ref_gpu.Vec2(*vt),
+                                                    C.c_double(c.dt), C.c_int32(N)))
+    check(G, R, ["T"])
+    assert np.count_nonzero(G["T"] != H["T"]) >= 3, "particles heated by friction"
+
+
+def test_rigid_tool_particle_move(rigid):
+    """update_tool_particles (tool_gpu.cu:205-216) inside tool_gpu_update_tool:
+    the tool particles move by vel * dt, bit for bit."""
+    c, s, m = rigid
+    H = s.download()
+    vt = s.rigid_tool().vel
+    s.call("sph_rigid_tool_update")
+    G = s.download()
+    R = ref_run(H, lambda T, pg, N: m.launch("update_tool_particles", N, pg, ref_gpu.Vec2(*vt), C.c_double(c.dt)))
+    check(G, R, ["pos"])
+    tool = H["tool_particle"] == 1.0
+    assert tool.sum() > 100 and np.all(np.any(G["pos"][tool] != H["pos"][tool], axis=1))
