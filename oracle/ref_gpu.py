@@ -165,52 +165,32 @@ class RefModule:
         self.d.ck(self.d.cu.cuCtxSynchronize(), f"sync {name}")
 
 
-# ---- the reference's FEM-tool step, composed from its own kernels -----------------------------------
+# ---- the reference's steps, composed from its own kernels -------------------------------------------
 SORTED = [n for n, _ in DeviceBuffer._fields_]          # the fields grid_gpu_green reorders
 
 
-class RefFemStep:
-    """leap_frog::step(particles, grid, tool_FEM) (leap_frog.cu:162-248) run as
-    the reference runs it: every kernel launch of the step, in its order, from
-    the reference's own cubins, with the host side of the step restated here
-    (the sort's thrust::sort_by_key of the int hashes as a stable argsort, the
-    double-buffer swap of grid_gpu_green, the tool's host reference points,
-    the colour loop of apply_robin_bdc).  State lives in torch tensors:
-    ``P`` particles (particle_gpu fields), ``F`` the FEM system (position,
-    row_ptr, col_ind, K, M_inv, f, T, k and the step's K_temp, f_temp, T_old),
-    ``S`` segments.  No wear (wear_pro off)."""
+class _RefStep:
+    """What leap_frog::step's two forms share: the sort, the predictor, EOS,
+    artificial stress, the neighbour sums, the rates and the corrector, each a
+    launch of the reference's own kernel in the reference's order.  Particle
+    state lives in torch tensors ``P`` (particle_gpu fields)."""
 
-    def __init__(self, constants, geom, dt, particles: dict, fem: dict, segments: dict, tool_state):
+    MODULES = ("actions", "leap_frog", "grid", "green", "interactions")
+
+    def __init__(self, constants, geom, dt, particles: dict):
         import numpy as np
         import torch
         self.torch, self.np = torch, np
         self.c, self.g, self.dt = constants, geom, float(dt)
-        self.m = {k: RefModule(k) for k in ("actions", "leap_frog", "grid", "green", "interactions", "fem", "tool")}
-        zero_wear = (C.c_double * 4)()
+        self.m = {k: RefModule(k) for k in self.MODULES}
         k = constants
         self.m["actions"].launch("ref_set_actions_constants", 1, k.phys, k.corr, k.joco, k.trml_wp, k.trml_tool,
-                                 k.tool, zero_wear, block=1)
+                                 k.tool, (C.c_double * 4)(), block=1)
         ge = GeomConstants(geom.nx, geom.ny, geom.bbmin_x, geom.bbmin_y, geom.dx)
         self.m["interactions"].launch("ref_set_interactions_constants", 1, k.phys, k.corr, ge, k.trml_wp,
                                       k.trml_tool_sph, k.tool, block=1)
-        self.m["fem"].launch("ref_set_fem_constants", 1, k.tool, block=1)
-        dev = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
-        self.P = {f: dev(v) for f, v in particles.items()}
+        self.P = {f: torch.tensor(np.ascontiguousarray(v), device="cuda") for f, v in particles.items()}
         self.N = len(particles["rho"])
-        self.F = {f: dev(v) for f, v in fem.items()}
-        self.F["K_temp"], self.F["f_temp"], self.F["T_old"] = (torch.empty_like(self.F["K"]),
-                                                               torch.empty_like(self.F["f"]),
-                                                               torch.empty_like(self.F["T"]))
-        n = len(segments["left"])
-        self.S = {f: dev(v) for f, v in segments.items()}
-        for f, shape in (("wear_rate", (n, 2)), ("wear_nodes", (n,)), ("physical_para", (n, 4)),
-                         ("sliding_force", (n,))):
-            self.S[f] = torch.zeros(shape, dtype=torch.float64, device="cuda")
-        self.n_seg, self.n_colors = n, tool_state.n_cut_colors
-        self.vel = (tool_state.vel[0], tool_state.vel[1])
-        self.tl_ref = [tool_state.tl_point_ref[0], tool_state.tl_point_ref[1]]
-        self.ref_dist = tool_state.ref_dist
-        self.lowest = tool_state.lowest_point
         self.cell_start = torch.full((geom.num_cell,), -1, dtype=torch.int32, device="cuda")
         self.cell_end = torch.zeros(geom.num_cell, dtype=torch.int32, device="cuda")
         ini = {"pos_init": (self.N, 2), "vel_init": (self.N, 2), "S_init": (self.N, 4), "rho_init": (self.N,),
@@ -224,19 +204,14 @@ class RefFemStep:
         st.N = self.N
         return st
 
-    def segments(self):
-        sg = SegmentFEMGPU()
-        sg.segment_num = self.n_seg
-        for f, src in (("left", "left"), ("right", "right"), ("n", "normal"), ("marks", "marks"),
-                       ("heat_exchange", "heat_exchange"), ("fric_heat", "fric_heat"), ("wear_rate", "wear_rate"),
-                       ("wear_nodes", "wear_nodes"), ("physical_para", "physical_para"),
-                       ("sliding_force", "sliding_force")):
-            setattr(sg, f, ptr(self.S[src]))
-        return sg
+    def inistate(self):
+        return IniState(**{f: ptr(v) for f, v in self.I.items()})
 
-    def _sort(self):
+    def sort(self):
         """grid_base::assign_hashes + grid_gpu_green::sort (grid.cu:25-42,80-86;
-        grid_gpu_green.cu:185-209)."""
+        grid_gpu_green.cu:185-209): compute_hashes, thrust::sort_by_key of the int
+        hashes (a stable radix sort; a stable argsort here), the reorder kernel and
+        the double-buffer swap."""
         torch, np, g, N = self.torch, self.np, self.g, self.N
         P = self.P
         self.m["grid"].launch("compute_hashes", N, ptr(P["blanked"]), ptr(P["pos"]), ptr(P["hash"]), C.c_int32(N),
@@ -253,21 +228,12 @@ class RefFemStep:
         self.m["green"].launch("reorder_data_and_find_cell_start", N, self.particles(),
                                DeviceBuffer(**{f: ptr(v) for f, v in buf.items()}), ptr(self.cell_start),
                                ptr(self.cell_end), C.c_int32(N), block=512, shared=(512 + 1) * 4)
-        P.update(buf)   # the double-buffer swap
+        P.update(buf)
 
-    def step(self):
-        a, lf, it, fm, tl = (self.m[k] for k in ("actions", "leap_frog", "interactions", "fem", "tool"))
-        P, F, S, N, dt, k = self.P, self.F, self.S, self.N, self.dt, self.c
-        I = IniState(**{f: ptr(v) for f, v in self.I.items()})
-        nn, nz = len(self.F["T"]), len(self.F["K"])
-        self._sort()
-        lf.launch("init", N, self.particles(), I)
-        fm.launch("do_copy_vector", nn, C.c_int32(nn), ptr(F["T"]), ptr(F["T_old"]))           # reset_FEM_server
-        fm.launch("do_copy_vector", nn, C.c_int32(nn), ptr(F["f"]), ptr(F["f_temp"]))
-        fm.launch("do_copy_vector", nz, C.c_int32(nz), ptr(F["K"]), ptr(F["K_temp"]))
-        lf.launch("predict", N, self.particles(), I, C.c_double(dt))
-        fm.launch("do_calculate_temp", nn, C.c_int32(nn), ptr(F["k"]), ptr(F["T"]), ptr(F["T_old"]),
-                  C.c_double(0.5 * dt))
+    def sums_and_rates(self):
+        """material_eos .. contmech_advection (leap_frog.cu:119-134 / :191-206)."""
+        a, it = self.m["actions"], self.m["interactions"]
+        P, N = self.P, self.N
         a.launch("do_material_eos", N, ptr(P["rho"]), ptr(P["p"]), ptr(P["tool_particle"]), C.c_int32(N))
         a.launch("do_corrector_artificial_stress", N, ptr(P["rho"]), ptr(P["p"]), ptr(P["S"]),
                  ptr(P["tool_particle"]), ptr(P["R"]), C.c_int32(N))
@@ -283,6 +249,74 @@ class RefFemStep:
         a.launch("do_contmech_momentum", N, ptr(P["S_der"]), ptr(P["fc"]), ptr(P["ft"]), ptr(P["tool_particle"]),
                  ptr(P["vel_t"]), C.c_int32(N))
         a.launch("do_contmech_advection", N, ptr(P["vel"]), ptr(P["tool_particle"]), ptr(P["pos_t"]), C.c_int32(N))
+
+    def finish(self):
+        """perform_boundary_conditions(_thermal) and debug_invalidate."""
+        a, N = self.m["actions"], self.N
+        a.launch("do_boundary_conditions", N, self.particles())
+        if self.c.trml_tool.alpha != 0.0:
+            a.launch("do_boundary_conditions_thermal", N, self.particles())
+        a.launch("do_invalidate", N, self.particles(), C.c_int32(0))
+
+    def host_particles(self):
+        return {f: v.cpu().numpy() for f, v in self.P.items()}
+
+
+class RefFemStep(_RefStep):
+    """leap_frog::step(particles, grid, tool_FEM) (leap_frog.cu:162-248) run as
+    the reference runs it: every kernel launch of the step, in its order, from
+    the reference's own cubins, with the host side restated (the sort's
+    argsort, the buffer swap, the tool's host reference points, the colour loop
+    of apply_robin_bdc).  ``F`` holds the FEM system (position, row_ptr,
+    col_ind, K, M_inv, f, T, k and the step's K_temp, f_temp, T_old), ``S`` the
+    segments.  No wear (wear_pro off)."""
+
+    MODULES = _RefStep.MODULES + ("fem", "tool")
+
+    def __init__(self, constants, geom, dt, particles: dict, fem: dict, segments: dict, tool_state):
+        super().__init__(constants, geom, dt, particles)
+        torch, np = self.torch, self.np
+        self.m["fem"].launch("ref_set_fem_constants", 1, constants.tool, block=1)
+        dev = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+        self.F = {f: dev(v) for f, v in fem.items()}
+        self.F["K_temp"], self.F["f_temp"], self.F["T_old"] = (torch.empty_like(self.F["K"]),
+                                                               torch.empty_like(self.F["f"]),
+                                                               torch.empty_like(self.F["T"]))
+        n = len(segments["left"])
+        self.S = {f: dev(v) for f, v in segments.items()}
+        for f, shape in (("wear_rate", (n, 2)), ("wear_nodes", (n,)), ("physical_para", (n, 4)),
+                         ("sliding_force", (n,))):
+            self.S[f] = torch.zeros(shape, dtype=torch.float64, device="cuda")
+        self.n_seg, self.n_colors = n, tool_state.n_cut_colors
+        self.vel = (tool_state.vel[0], tool_state.vel[1])
+        self.tl_ref = [tool_state.tl_point_ref[0], tool_state.tl_point_ref[1]]
+        self.ref_dist = tool_state.ref_dist
+        self.lowest = tool_state.lowest_point
+
+    def segments(self):
+        sg = SegmentFEMGPU()
+        sg.segment_num = self.n_seg
+        for f, src in (("left", "left"), ("right", "right"), ("n", "normal"), ("marks", "marks"),
+                       ("heat_exchange", "heat_exchange"), ("fric_heat", "fric_heat"), ("wear_rate", "wear_rate"),
+                       ("wear_nodes", "wear_nodes"), ("physical_para", "physical_para"),
+                       ("sliding_force", "sliding_force")):
+            setattr(sg, f, ptr(self.S[src]))
+        return sg
+
+    def step(self):
+        a, lf, fm, tl = (self.m[k] for k in ("actions", "leap_frog", "fem", "tool"))
+        P, F, S, N, dt, k = self.P, self.F, self.S, self.N, self.dt, self.c
+        I = self.inistate()
+        nn, nz = len(self.F["T"]), len(self.F["K"])
+        self.sort()
+        lf.launch("init", N, self.particles(), I)
+        fm.launch("do_copy_vector", nn, C.c_int32(nn), ptr(F["T"]), ptr(F["T_old"]))           # reset_FEM_server
+        fm.launch("do_copy_vector", nn, C.c_int32(nn), ptr(F["f"]), ptr(F["f_temp"]))
+        fm.launch("do_copy_vector", nz, C.c_int32(nz), ptr(F["K"]), ptr(F["K_temp"]))
+        lf.launch("predict", N, self.particles(), I, C.c_double(dt))
+        fm.launch("do_calculate_temp", nn, C.c_int32(nn), ptr(F["k"]), ptr(F["T"]), ptr(F["T_old"]),
+                  C.c_double(0.5 * dt))
+        self.sums_and_rates()
         lf.launch("correct", N, self.particles(), I, C.c_double(dt))
         vel2 = Vec2(*self.vel)
         a.launch("do_material_fric_heat_gen_FEM_v21", N, self.particles(), self.segments(), vel2, ptr(F["T"]),
@@ -303,15 +337,54 @@ class RefFemStep:
         tl.launch("do_tool_update_FEM_gpu", nn, C.c_int32(nn), ptr(F["position"]), vel2, C.c_double(dt))
         self.tl_ref = [self.tl_ref[0] + self.vel[0] * dt, self.tl_ref[1] + self.vel[1] * dt]   # tool_update_FEM_gpu
         self.lowest = self.lowest + self.vel[1] * dt
+        # contact s1/s2 call __syncthreads() after early returns: one thread per block
         a.launch("do_compute_contact_forces_FEM_tool_v3_s1", N, C.c_int32(N), self.particles(), self.segments(),
                  Vec2(*self.tl_ref), C.c_double(self.ref_dist), vel2, C.c_double(dt), C.c_int32(self.n_seg), block=1)
         a.launch("do_compute_contact_forces_FEM_tool_v3_s2", N, C.c_int32(N), self.particles(), self.segments(),
                  ptr(F["T"]), C.c_double(dt), block=1)
-        a.launch("do_boundary_conditions", N, self.particles())
-        if k.trml_tool.alpha != 0.0:
-            a.launch("do_boundary_conditions_thermal", N, self.particles())
-        a.launch("do_invalidate", N, self.particles(), C.c_int32(0))
+        self.finish()
 
     def host(self):
-        return ({f: v.cpu().numpy() for f, v in self.P.items()}, {f: v.cpu().numpy() for f, v in self.F.items()},
+        return (self.host_particles(), {f: v.cpu().numpy() for f, v in self.F.items()},
                 {f: v.cpu().numpy() for f, v in self.S.items()})
+
+
+class RefRigidStep(_RefStep):
+    """leap_frog::step(particles, grid) with a rigid tool (leap_frog.cu:99-160),
+    Brookshaw build: the reference's kernels in its order.  The tool outline
+    moves on the host in the reference (tool::update_tool, tool.cpp:202-212);
+    here ``move_tool(tool, dt)`` does it (the tests pass the CPU oracle's
+    restatement, pinned bit for bit to tool.cpp), and the moved outline is
+    installed as tool_gpu_update_tool does."""
+
+    MODULES = _RefStep.MODULES + ("toolgpu",)
+
+    def __init__(self, constants, geom, dt, particles: dict, tool, move_tool):
+        super().__init__(constants, geom, dt, particles)
+        self.tool, self.move_tool = tool, move_tool
+        self._install()
+
+    def _install(self):
+        self._raw, args = rigid_tool_args(self.tool, self.c.tool.contact_alpha, self.c.phys.mass)
+        self.m["toolgpu"].launch("ref_set_rigid_tool", 1, *args, block=1)
+
+    def step(self):
+        a, lf, tg = self.m["actions"], self.m["leap_frog"], self.m["toolgpu"]
+        P, N, dt, k = self.P, self.N, self.dt, self.c
+        I = self.inistate()
+        self.sort()
+        lf.launch("init", N, self.particles(), I)
+        lf.launch("predict", N, self.particles(), I, C.c_double(dt))
+        self.sums_and_rates()
+        lf.launch("correct", N, self.particles(), I, C.c_double(dt))
+        vel = Vec2(*self.tool.vel)
+        if k.trml_wp.eta != 0.0:                                                 # material_fric_heat_gen
+            a.launch("do_material_fric_heat_gen", N, ptr(P["vel"]), ptr(P["ft"]), ptr(P["n"]),
+                     ptr(P["tool_particle"]), ptr(P["T"]), vel, C.c_double(dt), C.c_int32(N))
+        if k.plastic:
+            a.launch("do_plasticity_johnson_cook", N, self.particles(), C.c_double(dt))
+        self.move_tool(self.tool, dt)                                            # tool_gpu_update_tool
+        self._install()
+        tg.launch("update_tool_particles", N, self.particles(), vel, C.c_double(dt))
+        tg.launch("do_compute_contact_forces", N, self.particles(), C.c_double(dt))
+        self.finish()

@@ -661,3 +661,40 @@ def test_rigid_tool_particle_move(rigid):
     check(G, R, ["pos"])
     tool = H["tool_particle"] == 1.0
     assert tool.sum() > 100 and np.all(np.any(G["pos"][tool] != H["pos"][tool], axis=1))
+
+
+@pytest.mark.parametrize("art_stress", [True, False], ids=["art_stress", "no_art_stress"])
+def test_fused_rigid_step_against_reference_step(lib, oracle_lib, art_stress):
+    """Three fused product steps with the rigid tool against three
+    leap_frog::step(particles, grid) (leap_frog.cu:99-160) composed from the
+    reference's own kernels (oracle/ref_gpu.RefRigidStep; the outline moved by
+    the oracle's restatement of tool::update_tool, pinned bit for bit to
+    tool.cpp).  Cell list, permutation and blanking bit for bit; the state
+    within 1e-12 without artificial stress and 1e-8 with it (R itself 1e-6:
+    the float trigonometry of the stress angle)."""
+    c = setups.ref_cut(ny=30, length=0.04, preload_dx=0.8)
+    if not art_stress:
+        c.constants.corr.stresseps = 0.0
+    tol = 1e-8 if art_stress else 1e-12
+    s = Solver(c)
+    s.step(5)
+    ref = ref_gpu.RefRigidStep(c.constants, s.geometry(), c.dt, s.download(), s.rigid_tool(),
+                               lambda t, dt: oracle_lib.orc_rigid_move(C.byref(t), dt))
+    for _ in range(3):
+        s.step()
+        ref.step()
+    G, tool = s.download(), s.rigid_tool()
+    s.close()
+    R = ref.host_particles()
+    for f in ("hash", "idx", "blanked", "fixed", "tool_particle"):
+        assert np.array_equal(G[f], R[f]), f"{f}: {np.count_nonzero(G[f] != R[f])} entries differ"
+    act = R["blanked"] != 1.0
+    for f in ("pos", "vel", "rho", "S", "T", "eps_pl", "eps_pl_dot", "p", "R", "fc", "ft", "n", "h"):
+        e = rel_err(G[f], R[f])
+        assert e <= (RTOL_FLOAT_TRIG if f == "R" else tol), f"{f}: {e:.3e}"
+    for f in ("pos_t", "vel_t", "rho_t", "S_t", "T_t"):
+        e = rel_err(G[f][act], R[f][act])
+        assert e <= tol, f"{f}: {e:.3e}"
+    for i in range(tool.n_seg):
+        assert list(tool.left[i]) == list(ref.tool.left[i]) and list(tool.right[i]) == list(ref.tool.right[i])
+    assert np.count_nonzero(np.abs(R["fc"]).sum(1) > 0) >= 5
