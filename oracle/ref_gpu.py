@@ -26,7 +26,8 @@ from pathlib import Path
 REF_DIR = Path(__file__).resolve().parent / "_ref"
 CUBINS = {"actions": "ref_gpu_actions.cubin", "leap_frog": "ref_gpu_leapfrog.cubin", "grid": "ref_gpu_grid.cubin",
           "interactions": "ref_gpu_interactions.cubin", "green": "ref_gpu_green.cubin", "fem": "ref_gpu_fem.cubin",
-          "tool": "ref_gpu_tool.cubin", "toolgpu": "ref_gpu_toolgpu.cubin"}
+          "tool": "ref_gpu_tool.cubin", "toolgpu": "ref_gpu_toolgpu.cubin",
+          "interactions_pse": "ref_gpu_interactions_pse.cubin"}
 BLOCK_SIZE = 256   # the reference's BLOCK_SIZE (types.h)
 
 P = C.c_uint64     # device pointer
@@ -240,8 +241,18 @@ class _RefStep:
         it.launch("ref_bind_interactions", 1, ptr(P["pos"]), ptr(P["vel"]), ptr(P["S"]), ptr(P["R"]), ptr(P["h"]),
                   ptr(P["rho"]), ptr(P["p"]), ptr(P["T"]), ptr(P["hash"]), ptr(P["tool_particle"]), ptr(P["fc"]),
                   ptr(self.cell_start), ptr(self.cell_end), C.c_int32(N), C.c_int32(self.g.num_cell), block=1)
-        it.launch("do_interactions_monaghan", N, ptr(P["blanked"]), ptr(P["v_der"]), ptr(P["S_der"]),
-                  ptr(P["pos_t"]), ptr(P["vel_t"]), ptr(P["T_t"]), C.c_uint32(N))
+        if not getattr(self, "pse", False):
+            it.launch("do_interactions_monaghan", N, ptr(P["blanked"]), ptr(P["v_der"]), ptr(P["S_der"]),
+                      ptr(P["pos_t"]), ptr(P["vel_t"]), ptr(P["T_t"]), C.c_uint32(N))
+        else:   # PSE build: no Brookshaw term, then interactions_heat_pse (:434-463) when alpha_wp != 0
+            it.launch("do_interactions_monaghan", N, ptr(P["blanked"]), ptr(P["v_der"]), ptr(P["S_der"]),
+                      ptr(P["pos_t"]), ptr(P["vel_t"]), C.c_uint32(N))
+            if self.c.trml_wp.alpha != 0.0:
+                it.launch("ref_bind_interactions_pse", 1, ptr(P["pos"]), ptr(P["h"]), ptr(P["rho"]), ptr(P["T"]),
+                          ptr(P["hash"]), ptr(P["tool_particle"]), ptr(self.cell_start), ptr(self.cell_end),
+                          C.c_int32(N), C.c_int32(self.g.num_cell), block=1)
+                it.launch("do_interactions_heat_pse", N, ptr(P["blanked"]), ptr(P["T_t"]), C.c_int32(N),
+                          C.c_double(self.c.trml_wp.alpha), C.c_double(self.c.trml_tool_sph.alpha))
         a.launch("do_material_stress_rate_jaumann", N, ptr(P["v_der"]), ptr(P["S"]), ptr(P["tool_particle"]),
                  ptr(P["S_t"]), C.c_int32(N))
         a.launch("do_contmech_continuity", N, ptr(P["rho"]), ptr(P["v_der"]), ptr(P["tool_particle"]),
@@ -351,7 +362,8 @@ class RefFemStep(_RefStep):
 
 class RefRigidStep(_RefStep):
     """leap_frog::step(particles, grid) with a rigid tool (leap_frog.cu:99-160),
-    Brookshaw build: the reference's kernels in its order.  The tool outline
+    Brookshaw build, or with ``pse`` the Thermal_Conduction_PSE build: the
+    reference's kernels in its order.  The tool outline
     moves on the host in the reference (tool::update_tool, tool.cpp:202-212);
     here ``move_tool(tool, dt)`` does it (the tests pass the CPU oracle's
     restatement, pinned bit for bit to tool.cpp), and the moved outline is
@@ -359,8 +371,17 @@ class RefRigidStep(_RefStep):
 
     MODULES = _RefStep.MODULES + ("toolgpu",)
 
-    def __init__(self, constants, geom, dt, particles: dict, tool, move_tool):
+    def __init__(self, constants, geom, dt, particles: dict, tool, move_tool, pse: bool = False):
+        self.pse = pse
+        if pse:   # the Thermal_Conduction_PSE build of interactions_gpu.cu
+            self.MODULES = self.MODULES + ("interactions_pse",)
         super().__init__(constants, geom, dt, particles)
+        if pse:
+            self.m["interactions"] = self.m.pop("interactions_pse")
+            k = constants
+            ge = GeomConstants(geom.nx, geom.ny, geom.bbmin_x, geom.bbmin_y, geom.dx)
+            self.m["interactions"].launch("ref_set_interactions_constants", 1, k.phys, k.corr, ge, k.trml_wp,
+                                          k.trml_tool_sph, k.tool, block=1)
         self.tool, self.move_tool = tool, move_tool
         self._install()
 

@@ -663,23 +663,27 @@ def test_rigid_tool_particle_move(rigid):
     assert tool.sum() > 100 and np.all(np.any(G["pos"][tool] != H["pos"][tool], axis=1))
 
 
-@pytest.mark.parametrize("art_stress", [True, False], ids=["art_stress", "no_art_stress"])
-def test_fused_rigid_step_against_reference_step(lib, oracle_lib, art_stress):
+@pytest.mark.parametrize("art_stress,pse", [(True, False), (False, False), (True, True), (False, True)],
+                         ids=["brookshaw", "brookshaw_no_art_stress", "pse", "pse_no_art_stress"])
+def test_fused_rigid_step_against_reference_step(lib, oracle_lib, art_stress, pse):
     """Three fused product steps with the rigid tool against three
     leap_frog::step(particles, grid) (leap_frog.cu:99-160) composed from the
     reference's own kernels (oracle/ref_gpu.RefRigidStep; the outline moved by
     the oracle's restatement of tool::update_tool, pinned bit for bit to
-    tool.cpp).  Cell list, permutation and blanking bit for bit; the state
-    within 1e-12 without artificial stress and 1e-8 with it (R itself 1e-6:
-    the float trigonometry of the stress angle)."""
+    tool.cpp), in the Brookshaw and in the Thermal_Conduction_PSE build.  Cell
+    list, permutation and blanking bit for bit; the state within 1e-12 without
+    artificial stress and 1e-8 with it (R itself 1e-6: the float trigonometry
+    of the stress angle)."""
     c = setups.ref_cut(ny=30, length=0.04, preload_dx=0.8)
     if not art_stress:
         c.constants.corr.stresseps = 0.0
     tol = 1e-8 if art_stress else 1e-12
     s = Solver(c)
+    if pse:
+        s.set_thermal_model(abi.SPH_THERMAL_PSE)
     s.step(5)
     ref = ref_gpu.RefRigidStep(c.constants, s.geometry(), c.dt, s.download(), s.rigid_tool(),
-                               lambda t, dt: oracle_lib.orc_rigid_move(C.byref(t), dt))
+                               lambda t, dt: oracle_lib.orc_rigid_move(C.byref(t), dt), pse=pse)
     for _ in range(3):
         s.step()
         ref.step()
