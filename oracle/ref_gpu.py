@@ -60,6 +60,13 @@ class DeviceBuffer(C.Structure):
                                  "on_seg")]
 
 
+class MeshGPU(C.Structure):
+    """mesh_GPU_m (mesh_structure_GPU.h:80-125), 160 bytes, with only its node
+    positions at offset 80 set: the wear kernels that take it by value
+    (do_nodal_shift_wear_smooth_temp, do_segment_wear_update) read nothing else."""
+    _fields_ = [("head", C.c_uint8 * 80), ("position", P), ("tail", C.c_uint8 * 72)]
+
+
 class GeomConstants(C.Structure):
     """geom_constants (constants_structs.h:70-76)."""
     _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("bbmin_x", C.c_double), ("bbmin_y", C.c_double),

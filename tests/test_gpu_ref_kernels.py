@@ -702,3 +702,65 @@ def test_fused_rigid_step_against_reference_step(lib, oracle_lib, art_stress, ps
     for i in range(tool.n_seg):
         assert list(tool.left[i]) == list(ref.tool.left[i]) and list(tool.right[i]) == list(ref.tool.right[i])
     assert np.count_nonzero(np.abs(R["fc"]).sum(1) > 0) >= 5
+
+
+# ---- wear by nodal shift (WEAR_NODE_SHIFT) ---------------------------------------------------------
+def test_wear_adjustment(actions, cut):
+    """wear_adjustment (actions_gpu.cu:1009-1020) as the reference runs it:
+    mesh_retreat_wear and mesh_resume_wear over the element colours
+    (do_mesh_adjustment_wear, one thread per block: it calls __syncthreads()
+    after its early returns), the Usui rake/flank nodal shift
+    (do_nodal_shift_wear_smooth_temp), do_segment_wear_update,
+    do_correct_flank_contact and the lumped inverse mass, after a contact and
+    friction pass has gathered the segment statistics.  Node positions (FP64
+    atomics in the reference), lumped mass, stiffness, segments and the flank
+    retreat within 1e-13 relative, norm-wise; the per-segment wear rate bit for
+    bit."""
+    c, s = cut
+    fem_m, tool_m = module("fem"), module("tool")
+    wc = abi.WearConstants(10.0, 300.0, 10.0, 300.0)
+    fem_m.launch("ref_set_fem_constants", 1, c.constants.tool, block=1)
+    s.set_wear(abi.SPH_WEAR_SHIFT, wc)
+    s.call("sph_segments_wear_rate_reset")
+    s.call("sph_compute_contact_forces_fem")
+    s.call("sph_material_fric_heat_gen_fem")
+    fem, seg, ts, w = s.fem(), s.segments(), s.tool_state(), s.wear_state()
+    assert w["phys_para"][:, 0].sum() > 0, "segments with wear statistics"
+    s.call("sph_wear_adjustment")
+    Gf, Gs, Gt, Gw = s.fem(), s.segments(), s.tool_state(), s.wear_state()
+    s.set_wear(abi.SPH_WEAR_OFF)
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+    n, ne, nn = ts.n_segments, len(w["elements"]), len(fem["T"])
+    assert n <= 512, "do_correct_flank_contact reduces in one block of 512"
+    X, K, Mi, Tn = dev(fem["position"]), dev(fem["K"]), dev(fem["M_inv"]), dev(fem["T"])
+    M, layer, elem = dev(w["M"]), dev(w["layer"]), dev(w["elements"])
+    rp, ci = dev(fem["row_ptr"]), dev(fem["col_ind"])
+    Sg, sg = segment_struct(seg, n, wear=dict(wear_rate=np.zeros((n, 2)), wear_nodes=np.zeros(n),
+                                              physical_para=w["phys_para"], sliding_force=w["sliding_force"]))
+    mesh = ref_gpu.MeshGPU()
+    mesh.position = ref_gpu.ptr(X)
+    colours = int(w["elements"][:, 3].max())
+    tool_m.launch("ref_set_wear", 1, C.c_double(ts.flank_retreat), C.c_double(ts.flank_contact), wc, block=1)
+
+    def adjust(sign):
+        for colour in range(1, colours + 1):
+            fem_m.launch("do_mesh_adjustment_wear", ne, C.c_int32(colour), C.c_int32(ne), P(layer), P(X), P(elem),
+                         P(rp), P(ci), C.c_int32(colours), P(M), P(K), C.c_int32(sign), block=1)
+
+    adjust(-1)
+    tool_m.launch("do_nodal_shift_wear_smooth_temp", n, C.c_int32(n), C.c_double(c.dt), sg, mesh, P(Tn))
+    adjust(+1)
+    tool_m.launch("do_segment_wear_update", n, C.c_int32(n), sg, mesh, block=512)
+    tool_m.launch("do_correct_flank_contact", 512, C.c_int32(n), P(Sg["left"]), block=512)
+    fem_m.launch("do_inverse_mass_matrix_lumped", nn, C.c_int32(nn), P(Mi), P(M))
+    flank = torch.zeros(2, dtype=torch.float64, device="cuda")
+    tool_m.launch("ref_get_flank", 1, P(flank), block=1)
+    for name, a, b in (("position", Gf["position"], X), ("K", Gf["K"], K), ("M_inv", Gf["M_inv"], Mi),
+                       ("M", Gw["M"], M), ("left", Gs["left"], Sg["left"]), ("right", Gs["right"], Sg["right"]),
+                       ("normal", Gs["normal"], Sg["normal"])):
+        e = rel_err(a, b.cpu().numpy())
+        assert e <= 1e-13, f"{name}: {e:.3e}"
+    assert np.array_equal(Gw["wear_nodes"], Sg["wear_nodes"].cpu().numpy())
+    assert np.max(Gw["wear_nodes"]) > 0 and np.any(Gf["position"] != fem["position"])
+    fr = flank.cpu().numpy()
+    assert Gt.flank_retreat == pytest.approx(fr[0], rel=1e-13, abs=1e-18)
