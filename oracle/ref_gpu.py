@@ -416,3 +416,66 @@ class RefRigidStep(_RefStep):
         tg.launch("update_tool_particles", N, self.particles(), vel, C.c_double(dt))
         tg.launch("do_compute_contact_forces", N, self.particles(), C.c_double(dt))
         self.finish()
+
+
+class RefPlainStep(_RefStep):
+    """leap_frog::step(particles, grid) without a tool (leap_frog.cu:99-160 with
+    global_tool null): the reference's kernels in its order.  With ``timed``,
+    ``kernel_ms`` accumulates the device time of the step's kernels (CUDA
+    events on the default stream); the host-side argsort standing in for
+    thrust::sort_by_key is left out of it."""
+
+    def __init__(self, constants, geom, dt, particles: dict, timed: bool = False):
+        super().__init__(constants, geom, dt, particles)
+        self.timed, self.kernel_ms = timed, 0.0
+
+    def _span(self):
+        ev = self.torch.cuda.Event(enable_timing=True)
+        ev.record()
+        return ev
+
+    def sort(self):
+        if not self.timed:
+            return super().sort()
+        # time compute_hashes and the reorder kernel, not the host argsort between them
+        torch, np, g, N, P = self.torch, self.np, self.g, self.N, self.P
+        e0 = self._span()
+        self.m["grid"].launch("compute_hashes", N, ptr(P["blanked"]), ptr(P["pos"]), ptr(P["hash"]), C.c_int32(N),
+                              C.c_double(g.dx), C.c_int32(g.ny), C.c_double(g.bbmin_x), C.c_double(g.bbmin_y))
+        e1 = self._span()
+        e1.synchronize()
+        self.kernel_ms += e0.elapsed_time(e1)
+        h = P["hash"].cpu().numpy()
+        if h.min() < 0 or h.max() >= g.num_cell:
+            raise ValueError("a particle hashed outside the grid")
+        order = np.argsort(h, kind="stable").astype(np.int32)
+        P["hash"] = torch.tensor(h[order], device="cuda")
+        P["idx"] = torch.tensor(order, device="cuda")
+        buf = {f: torch.empty_like(P[f]) for f in SORTED}
+        self.cell_start.fill_(-1)
+        e0 = self._span()
+        self.m["green"].launch("reorder_data_and_find_cell_start", N, self.particles(),
+                               DeviceBuffer(**{f: ptr(v) for f, v in buf.items()}), ptr(self.cell_start),
+                               ptr(self.cell_end), C.c_int32(N), block=512, shared=(512 + 1) * 4)
+        e1 = self._span()
+        e1.synchronize()
+        self.kernel_ms += e0.elapsed_time(e1)
+        P.update(buf)
+
+    def step(self):
+        a, lf = self.m["actions"], self.m["leap_frog"]
+        N, dt = self.N, self.dt
+        I = self.inistate()
+        self.sort()
+        e0 = self._span() if self.timed else None
+        lf.launch("init", N, self.particles(), I)
+        lf.launch("predict", N, self.particles(), I, C.c_double(dt))
+        self.sums_and_rates()
+        lf.launch("correct", N, self.particles(), I, C.c_double(dt))
+        if self.c.plastic:
+            a.launch("do_plasticity_johnson_cook", N, self.particles(), C.c_double(dt))
+        self.finish()
+        if self.timed:
+            e1 = self._span()
+            e1.synchronize()
+            self.kernel_ms += e0.elapsed_time(e1)

@@ -764,3 +764,91 @@ def test_wear_adjustment(actions, cut):
     assert np.max(Gw["wear_nodes"]) > 0 and np.any(Gf["position"] != fem["position"])
     fr = flank.cpu().numpy()
     assert Gt.flank_retreat == pytest.approx(fr[0], rel=1e-13, abs=1e-18)
+
+
+# ---- full size: the neighbour sums on the 4.19 M-particle micro workload -----------------------------------
+def test_interactions_full_size(lib, capsys):
+    """do_interactions_monaghan on the 2048 x 2048 micro workload (4,194,304
+    particles, cells of h, the reference's geometry): the product's FP64 sums
+    against the reference's own kernel at full size, within 1e-12 relative,
+    norm-wise.  The device times of both launches are printed (CUDA events,
+    after a warm-up launch); the reference's texture fetches are served by the
+    stand-in's bounds-checked loads, so its time is indicative only."""
+    c = setups.micro(n_side=2048, cell_factor=1, stencil=2)
+    s = Solver(c)
+    for name in ("sph_assign_hashes", "sph_sort", "sph_material_eos", "sph_corrector_artificial_stress"):
+        s.call(name)
+    H, (cs, ce), g = s.download(), s.cells(), s.geometry()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    s.call("sph_interactions_monaghan")
+    s.sync()
+    ev[0].record()
+    s.call("sph_interactions_monaghan")
+    s.sync()
+    ev[1].record()
+    G = s.download()
+    s.close()
+    m = interactions_module(c, g)
+    N = len(H["rho"])
+    T = device(H)
+    CS, CE = torch.tensor(cs, device="cuda"), torch.tensor(ce, device="cuda")
+    m.launch("ref_bind_interactions", 1, P(T["pos"]), P(T["vel"]), P(T["S"]), P(T["R"]), P(T["h"]), P(T["rho"]),
+             P(T["p"]), P(T["T"]), P(T["hash"]), P(T["tool_particle"]), P(T["fc"]), P(CS), P(CE), C.c_int32(N),
+             C.c_int32(g.num_cell), block=1)
+    args = (P(T["blanked"]), P(T["v_der"]), P(T["S_der"]), P(T["pos_t"]), P(T["vel_t"]), P(T["T_t"]), C.c_uint32(N))
+    m.launch("do_interactions_monaghan", N, *args)
+    torch.cuda.synchronize()
+    ev[2].record()
+    m.launch("do_interactions_monaghan", N, *args)
+    ev[3].record()
+    torch.cuda.synchronize()
+    R = {k: v.cpu().numpy() for k, v in T.items()}
+    check(G, R, ["v_der", "S_der", "pos_t", "vel_t", "T_t"], rtol=RTOL_SUMS)
+    with capsys.disabled():
+        print(f"\n[micro 2048x2048 FP64 neighbour sums] product {ev[0].elapsed_time(ev[1]):.2f} ms "
+              f"(staged call, records + sums), reference kernel {ev[2].elapsed_time(ev[3]):.2f} ms")
+
+
+def test_plain_step_full_size(lib, capsys):
+    """leap_frog::step(particles, grid) without a tool, composed from the
+    reference's own kernels (oracle/ref_gpu.RefPlainStep), against the
+    product's fused FP64 step on the 2048 x 2048 micro workload (4,194,304
+    particles, the reference's cells of h), with the artificial-stress
+    coefficient set to zero: the workload's random stresses make the
+    artificial stress large, and the stress angle's float trigonometry (CUDA's
+    atan2f / cosf / sinf in the reference) would reach the velocities at 2e-8
+    and, through the float-rounded plastic increment, eps_pl at 2e-7 after two
+    steps (the kernels still run in full; R comes out zero).  Two steps: cell
+    list and permutation bit for bit, state and rates within 1e-11.  The device
+    time of the reference's kernels
+    per step (its sort's thrust::sort_by_key left out) and of the product's
+    fused step are printed."""
+    c = setups.micro(n_side=2048, cell_factor=1, stencil=2)
+    c.constants.corr.stresseps = 0.0
+    s = Solver(c)
+    ref = ref_gpu.RefPlainStep(c.constants, s.geometry(), c.dt, s.download(), timed=True)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    s.step()
+    s.sync()
+    e[0].record()
+    s.step()
+    s.sync()
+    e[1].record()
+    e[1].synchronize()
+    for _ in range(2):
+        ref.step()
+    G = s.download()
+    s.close()
+    R = ref.host_particles()
+    for f in ("hash", "idx", "blanked"):
+        assert np.array_equal(G[f], R[f]), f
+    act = R["blanked"] != 1.0
+    for f in ("pos", "vel", "rho", "S", "T", "eps_pl", "eps_pl_dot", "p"):
+        e_ = rel_err(G[f], R[f])
+        assert e_ <= 1e-11, f"{f}: {e_:.3e}"
+    for f in ("pos_t", "vel_t", "rho_t", "S_t"):
+        e_ = rel_err(G[f][act], R[f][act])
+        assert e_ <= 1e-11, f"{f}: {e_:.3e}"
+    with capsys.disabled():
+        print(f"\n[micro 2048x2048 FP64 step] product fused step {e[0].elapsed_time(e[1]):.2f} ms, "
+              f"reference kernels {ref.kernel_ms / 2:.2f} ms per step (sort excluded)")
