@@ -116,8 +116,65 @@ __global__ void __launch_bounds__(kBlock) k_fric_heat(int N, KConsts K, SortedFi
     if (st) set_status(status, st);
 }
 
+// ---- y-bins of the interface segments for the contact's ray casting ----------------------------
+// A segment adds a crossing for a particle only if the particle's y lies in the
+// segment's float-rounded y-range [lo, hi] (on_segment_mesh).  Each case's range
+// [y0, y1] of those rounded values is cut into kSegBins bins, and every segment is
+// listed in the bins its [lo, hi] overlaps (one more on each side).  The bin of a
+// y is floor((y - y0) * scale); subtraction, the product and floor are monotone
+// in y, so a particle's bin lies between the bins of lo and hi of any segment
+// that can cross it.  Counting crossings over the particle's bin alone therefore
+// gives the full scan's count (an integer sum: order does not matter).  A bin
+// holding more than kSegBinCap segments is marked -1 and its particles scan all.
+__device__ __forceinline__ int seg_bin_of(double y, double y0, double scale) {
+    const double t = floor((y - y0) * scale);
+    return t < 0. ? 0 : (t >= (double)(kSegBins - 1) ? kSegBins - 1 : (int)t);
+}
+
+__global__ void __launch_bounds__(256) k_seg_bins(SegDev seg, ToolDev *tool) {
+    const int c = blockIdx.x;
+    ToolDev &t = tool[c];
+    __shared__ int cnt[kSegBins];
+    for (int b = threadIdx.x; b < kSegBins; b += blockDim.x) cnt[b] = 0;
+    const double y0 = (double)(float)t.seg_ymin, y1 = (double)(float)t.seg_ymax;
+    const double scale = (y1 > y0) ? (double)kSegBins / (y1 - y0) : 0.;
+    int32_t *list = seg.bin_list + (size_t)c * kSegBins * kSegBinCap;
+    __syncthreads();
+    for (int i = threadIdx.x; i < t.seg_count; i += blockDim.x) {
+        const double2 L = seg.left[t.seg_first + i], R = seg.right[t.seg_first + i];
+        const int b0 = max(seg_bin_of(fminf_d(L.y, R.y), y0, scale) - 1, 0);
+        const int b1 = min(seg_bin_of(fmaxf_d(L.y, R.y), y0, scale) + 1, kSegBins - 1);
+        for (int b = b0; b <= b1; b++) {
+            const int slot = atomicAdd(&cnt[b], 1);
+            if (slot < kSegBinCap) list[b * kSegBinCap + slot] = i;
+        }
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < kSegBins; b += blockDim.x)
+        seg.bin_count[c * kSegBins + b] = cnt[b] <= kSegBinCap ? cnt[b] : -1;
+    if (threadIdx.x == 0) {
+        t.bin_y0 = y0;
+        t.bin_scale = scale;
+    }
+}
+
+// inside_judgement over the particle's y-bin (the full scan when it overflowed)
+__device__ __forceinline__ int inside_binned(double2 qp, const SegDev &seg, const ToolDev &tool) {
+    const int b = seg_bin_of(qp.y, tool.bin_y0, tool.bin_scale);
+    const int n = seg.bin_count[b];
+    if (n < 0) return inside_judgement(qp, seg.left, seg.right, seg.n);
+    const int32_t *list = seg.bin_list + b * kSegBinCap;
+    int crossings = 0;
+    for (int k = 0; k < n; k++) {
+        const int i = list[k];
+        crossings += on_segment_mesh(__ldg(seg.left + i), __ldg(seg.right + i), qp);
+    }
+    return crossings & 1;
+}
+
 // ---- contact, one particle: actions_gpu.cu:423-583 (s1) ------------------------------------------
-// seg: the segments of the particle's case; on_seg comes back as an index into them.
+// seg: the segments of the particle's case (and their y-bins); on_seg comes back
+// as an index into them.
 __device__ __forceinline__ uint32_t contact_s1_one(const KConsts &K, double dt, const SegDev &seg, const ToolDev &tool,
                                                    double2 pos, double2 vel, double2 &fc, double2 &ft, double2 &nrm,
                                                    int &on_seg, double &blanked) {
@@ -135,7 +192,7 @@ __device__ __forceinline__ uint32_t contact_s1_one(const KConsts &K, double dt, 
         pos.x <= tool.seg_xmax + tool.seg_dxdy * fmax(fabs(tool.seg_ymin), fabs(tool.seg_ymax)) * 2.384185791015625e-7 +
                      1e-12 &&
         sqrt(ddx * ddx + ddy * ddy) < 1.05 * tool.ref_dist)
-        inside = inside_judgement(pos, seg.left, seg.right, seg.n);
+        inside = seg.bin_count ? inside_binned(pos, seg, tool) : inside_judgement(pos, seg.left, seg.right, seg.n);
     if (inside == 0) {
         fc = make_double2(0., 0.); ft = make_double2(0., 0.); nrm = make_double2(0., 0.);
         on_seg = -1;
@@ -305,12 +362,17 @@ __global__ void __launch_bounds__(kBlock) k_step_tail(int N, KConsts K, SortedFi
     double2 pos = A.pos[i];
     if (kMode == 1 && !blanked) {
         // the particle's case: its tool, time step and interface segments
-        const ToolDev &tc = tool[case_of_hash(K, A.hash[i])];
+        const int c = case_of_hash(K, A.hash[i]);
+        const ToolDev &tc = tool[c];
         SegDev cs = seg;
         cs.left += tc.seg_first;
         cs.right += tc.seg_first;
         cs.normal += tc.seg_first;
         cs.n = tc.seg_count;
+        if (cs.bin_count) {
+            cs.bin_count += c * kSegBins;
+            cs.bin_list += (size_t)c * kSegBins * kSegBinCap;
+        }
         double2 fc = A.fc[i], ft = A.ft[i], nrm = A.n[i];
         int on = A.on_seg[i];
         double bl = 0.;
@@ -517,8 +579,12 @@ void launch_fric_heat(cudaStream_t s, int N, const KConsts &K, const SortedField
                       const ToolDev *tool, uint32_t *status) {
     k_fric_heat<<<GRID>>>(N, K, A, seg, tool, status);
 }
+void launch_seg_bins(cudaStream_t s, int n_cases, const SegDev &seg, ToolDev *tool) {
+    if (seg.bin_count) k_seg_bins<<<n_cases, 256, 0, s>>>(seg, tool);
+}
 void launch_contact(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
-                    const ToolDev *tool, const double *T_nodes, uint32_t *status) {
+                    ToolDev *tool, const double *T_nodes, uint32_t *status) {
+    launch_seg_bins(s, 1, seg, tool);
     k_contact_s1<<<GRID>>>(N, K, A, seg, tool, status);
     k_contact_s2<<<GRID>>>(N, K, A, seg, T_nodes);
 }
@@ -530,9 +596,10 @@ void launch_invalidate(cudaStream_t s, int N, const SortedFields &A, uint32_t *s
     k_invalidate<<<GRID>>>(N, A, status);
 }
 void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
-                      const ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
+                      ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
                       bool next_hash) {
     const int tb = fp64_block(N);   // the contact search is FP64 work: spread small systems over all SMs
+    if (K.has_tool) launch_seg_bins(s, K.n_cases, seg, tool);
 #undef GRID
 #define GRID div_up(N, tb), tb, 0, s
     if (K.has_tool) {

@@ -152,6 +152,7 @@ struct ToolDev {
     double seg_dxdy;                // largest |dx/dy| of a non-horizontal segment
     double flank_retreat;           // wear: added to the y motion of nodes and segments (tool_FEM.cu:19)
     double flank_contact;           // wear: lowest_point after the last tool update (tool_FEM.cu:20)
+    double bin_y0, bin_scale;       // segment y-bins: bin = floor((y - bin_y0) * bin_scale) (k_seg_bins)
 };
 
 // Per-segment wear statistics gathered by the friction-heat kernel

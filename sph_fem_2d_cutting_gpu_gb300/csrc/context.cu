@@ -405,7 +405,7 @@ int issue_fused_body(sph_ctx *ctx, int64_t &n, int w) {
     }
     CK(cudaMemsetAsync(ctx->X.counts, 0, sizeof(int32_t) * (size_t)(ctx->K.g.num_cell + 1), s));
     launch_step_tail(s, N, ctx->K, B, ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->X, ctx->W.status, true);
-    n += 1;
+    n += ctx->has_tool ? 2 : 1;   // with the FEM tool: the segment y-bins, then the tail
     CK_LAUNCH();
     return SPH_OK;
 }
@@ -616,6 +616,8 @@ int ctx_upload_tool(sph_ctx *ctx, bool with_model, const std::vector<ToolDev> &t
         S.n = M.n_seg;
         DALLOC(S.left, M.n_seg); DALLOC(S.right, M.n_seg); DALLOC(S.normal, M.n_seg); DALLOC(S.marks, M.n_seg);
         DALLOC(S.heat_exchange, M.n_seg); DALLOC(S.fric_heat, M.n_seg);
+        DALLOC(S.bin_count, (size_t)kSegBins * tds.size());
+        DALLOC(S.bin_list, (size_t)kSegBins * kSegBinCap * tds.size());
         CK(cudaMemcpy(S.left, M.left.data(), sizeof(double) * 2 * M.n_seg, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(S.right, M.right.data(), sizeof(double) * 2 * M.n_seg, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(S.normal, M.normal.data(), sizeof(double) * 2 * M.n_seg, cudaMemcpyHostToDevice));
@@ -1077,7 +1079,7 @@ int sph_compute_contact_forces_fem(sph_ctx *ctx) {
     REQUIRE_SINGLE_CASE();
     REQUIRE_TOOL();
     launch_contact(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->W.status);
-    ctx->launches += 2;
+    ctx->launches += 3;   // segment y-bins, s1, s2
     ctx->counts_valid = false;
     CK_LAUNCH();
     return SPH_OK;
@@ -1365,7 +1367,7 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
         launch_step_tail(s, N, ctx->K, B, ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->X, ctx->W.status, true);
         CK(cudaEventRecord(ev[7], s));
         CK_LAUNCH();
-        ctx->launches += 8 + (ctx->has_tool ? 3 : 0) + (pse_active(ctx) ? 1 : 0) + (ctx->K.rigid ? 1 : 0);
+        ctx->launches += 8 + (ctx->has_tool ? 4 : 0) + (pse_active(ctx) ? 1 : 0) + (ctx->K.rigid ? 1 : 0);
         CK(cudaEventSynchronize(ev[7]));
         for (int k = 0; k < kStages; k++) {
             float ms = 0.f;

@@ -44,13 +44,17 @@ void launch_plasticity(cudaStream_t s, int N, const KConsts &K, const SortedFiel
                        const StepScratch &W);
 void launch_fric_heat(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
                       const ToolDev *tool, uint32_t *status);
+// the contact's segment y-bins of every case (k_seg_bins); a no-op without bins
+void launch_seg_bins(cudaStream_t s, int n_cases, const SegDev &seg, ToolDev *tool);
+// builds the bins first (the tool state moves), then contact s1 / s2
 void launch_contact(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
-                    const ToolDev *tool, const double *T_nodes, uint32_t *status);
+                    ToolDev *tool, const double *T_nodes, uint32_t *status);
 void launch_bc(cudaStream_t s, int N, const SortedFields &A);
 void launch_bc_thermal(cudaStream_t s, int N, const KConsts &K, const SortedFields &A);
 void launch_invalidate(cudaStream_t s, int N, const SortedFields &A, uint32_t *status);
+// with the FEM tool: builds the segment y-bins first (one more launch)
 void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
-                      const ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
+                      ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
                       bool next_hash);
 void launch_rigid_move(cudaStream_t s, sph_rigid_tool *t, double dt);
 void launch_rigid_move_particles(cudaStream_t s, int N, const SortedFields &A, const sph_rigid_tool *t, double dt);

@@ -55,7 +55,15 @@ struct SegDev {
     double *fric_heat;
     WearAcc wear;             // wear statistics (pp == NULL: off)
     double *wear_rate;        // wear_nodes: per-segment wear rate of the last nodal shift
+    // y-bins of each case's segments for the contact's ray casting (k_seg_bins):
+    // bin_count[case * kSegBins + b] segments listed, -1 when the bin overflowed
+    // (then the full scan runs); bin_list[(case * kSegBins + b) * kSegBinCap + k]
+    // the case-local segment index.  NULL: no bins, full scan.
+    int32_t *bin_count;
+    int32_t *bin_list;
 };
+constexpr int kSegBins = 64;
+constexpr int kSegBinCap = 64;
 
 // FEM thermal system of the tool (FEM_thermal_2D_GPU, FEM_thermal_gpu.h:35-93).
 // K, f are the assembled (post-Dirichlet) m_stiffness_matrix / m_f; the Robin
