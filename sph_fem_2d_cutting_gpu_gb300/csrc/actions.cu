@@ -155,6 +155,10 @@ __global__ void __launch_bounds__(256) k_seg_bins(SegDev seg, ToolDev *tool) {
     if (threadIdx.x == 0) {
         t.bin_y0 = y0;
         t.bin_scale = scale;
+        t.key_y0 = order_key(y0);
+        t.key_y1 = order_key(y1);
+        t.key_x1 = order_key(t.seg_xmax + t.seg_dxdy * fmax(fabs(t.seg_ymin), fabs(t.seg_ymax)) *
+                                              2.384185791015625e-7 + 1e-12);
     }
 }
 
@@ -179,7 +183,6 @@ __device__ __forceinline__ uint32_t contact_s1_one(const KConsts &K, double dt, 
                                                    double2 pos, double2 vel, double2 &fc, double2 &ft, double2 &nrm,
                                                    int &on_seg, double &blanked) {
     int inside = 0;
-    double ddx = pos.x - tool.tl_point_ref[0], ddy = pos.y - tool.tl_point_ref[1];
     // A segment counts a crossing only if the particle's y lies in its float-rounded
     // y-range (on_segment_mesh); float rounding is monotone, so a particle outside the
     // rounded y-range of all segments has no crossing and the scan is skipped.
@@ -188,11 +191,22 @@ __device__ __forceinline__ uint32_t contact_s1_one(const KConsts &K, double dt, 
     // crossing by at most |dx/dy| * |y| * 2^-24 (bounded here with 2^-22 and an
     // absolute 1e-12).  (These tests first: all tests are pure, and they spare most
     // particles the FP64 sqrt.)
-    if (pos.y <= (double)(float)tool.seg_ymax && pos.y >= (double)(float)tool.seg_ymin &&
-        pos.x <= tool.seg_xmax + tool.seg_dxdy * fmax(fabs(tool.seg_ymin), fabs(tool.seg_ymax)) * 2.384185791015625e-7 +
-                     1e-12 &&
-        sqrt(ddx * ddx + ddy * ddy) < 1.05 * tool.ref_dist)
-        inside = seg.bin_count ? inside_binned(pos, seg, tool) : inside_judgement(pos, seg.left, seg.right, seg.n);
+    // With the y-bins built (k_seg_bins), the two bounds come as order keys and the
+    // tests run on the integer pipe.
+    bool near;
+    if (seg.bin_count) {
+        const long long ky = order_key(pos.y);
+        near = ky <= tool.key_y1 && ky >= tool.key_y0 && order_key(pos.x) <= tool.key_x1;
+    } else {
+        near = pos.y <= (double)(float)tool.seg_ymax && pos.y >= (double)(float)tool.seg_ymin &&
+               pos.x <= tool.seg_xmax + tool.seg_dxdy * fmax(fabs(tool.seg_ymin), fabs(tool.seg_ymax)) *
+                                           2.384185791015625e-7 + 1e-12;
+    }
+    if (near) {
+        const double ddx = pos.x - tool.tl_point_ref[0], ddy = pos.y - tool.tl_point_ref[1];
+        if (sqrt(ddx * ddx + ddy * ddy) < 1.05 * tool.ref_dist)
+            inside = seg.bin_count ? inside_binned(pos, seg, tool) : inside_judgement(pos, seg.left, seg.right, seg.n);
+    }
     if (inside == 0) {
         fc = make_double2(0., 0.); ft = make_double2(0., 0.); nrm = make_double2(0., 0.);
         on_seg = -1;

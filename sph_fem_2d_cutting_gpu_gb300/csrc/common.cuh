@@ -153,7 +153,21 @@ struct ToolDev {
     double flank_retreat;           // wear: added to the y motion of nodes and segments (tool_FEM.cu:19)
     double flank_contact;           // wear: lowest_point after the last tool update (tool_FEM.cu:20)
     double bin_y0, bin_scale;       // segment y-bins: bin = floor((y - bin_y0) * bin_scale) (k_seg_bins)
+    // the contact pre-filter's bounds as order keys (k_seg_bins): float-rounded
+    // segment y-range and the x bound right of which no crossing can lie
+    long long key_y0, key_y1, key_x1;
 };
+
+// Order key of a double: for non-NaN a, b, a <= b exactly when key(a) <= key(b)
+// as signed integers (sign-magnitude bits made two's-complement ordered; -0
+// taken as +0).  NaN keys sort outside every finite range, so a NaN fails a
+// two-sided range test as the IEEE comparisons do.  Compares on the integer
+// pipe: GB300's FP64 pipe is narrow.
+__device__ __forceinline__ long long order_key(double x) {
+    long long b = __double_as_longlong(x);
+    if (b == (long long)0x8000000000000000ull) b = 0;
+    return b ^ ((b >> 63) & 0x7fffffffffffffffll);
+}
 
 // Per-segment wear statistics gathered by the friction-heat kernel
 // (WEAR_NODE_SHIFT, actions_gpu.cu:401-419); pp == NULL: not gathered.
