@@ -37,6 +37,9 @@ RTOL_JAUMANN = 1e-13
 RTOL_FLOAT_TRIG = 1e-6   # R: CUDA's float atan2f / cosf / sinf against double-evaluated, once-rounded
 torch = pytest.importorskip("torch")
 ref_gpu = pytest.importorskip("oracle.ref_gpu")
+if not all((ref_gpu.REF_DIR / f).exists() for f in ref_gpu.CUBINS.values()):
+    pytest.skip("the reference cubins are not built here (oracle/Makefile target ref_gpu needs the "
+                "reference tree at build time)", allow_module_level=True)
 
 
 def module(which):
