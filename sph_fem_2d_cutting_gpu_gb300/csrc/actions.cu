@@ -356,25 +356,20 @@ __global__ void __launch_bounds__(kBlock) k_fric_heat_rigid(int N, KConsts K, So
     if (T != A.T[i]) A.T[i] = T;
 }
 
-// ---- fused tail of the step ----------------------------------------------------------------------
-// The tool's contact for one particle -- kMode 1: FEM tool, contact s1 + s2
-// (actions_gpu.cu:423-617); kMode 2: rigid tool, update_tool_particles and
-// do_compute_contact_forces (tool_gpu.cu:146-216); kMode 0: no tool -- then
-// do_boundary_conditions, do_boundary_conditions_thermal, do_invalidate
-// (actions_gpu.cu:756-824) and (kNextHash) the next step's compute_hashes and
-// the counting-sort histogram (grid.cu:25-42) on the final state.
-template <int kMode, bool kNextHash>
-__global__ void __launch_bounds__(kBlock) k_step_tail(int N, KConsts K, SortedFields A, SegDev seg,
-                                                      const ToolDev *__restrict__ tool,
-                                                      const double *__restrict__ T_nodes, SortScratch X,
-                                                      uint32_t *status) {
+// ---- the FEM tool's contact of the fused step: actions_gpu.cu:423-617 (s1 + s2) -----------------------
+// Its own pass before the tail: the contact search's registers would otherwise
+// hold down the occupancy of the memory-bound tail for every particle, although
+// only the particles near a tool reach it.  The tail that follows sees the
+// contact's results (forces, segment id, blanking, temperature) in memory, in the
+// order of the reference's step.
+__global__ void __launch_bounds__(kBlock) k_contact_fem(int N, KConsts K, SortedFields A, SegDev seg,
+                                                        const ToolDev *__restrict__ tool,
+                                                        const double *__restrict__ T_nodes, uint32_t *status) {
     PARTICLE_LOOP_HEAD
-    bool blanked = flag_is_one(A.blanked[i]);
-    const bool bc_fixed = !flag_nonzero(A.tool_particle[i]) && flag_nonzero(A.fixed[i]);   // do_boundary_conditions
-    const bool bc_thermal = K.thermal_bc && flag_is_one(A.fixed[i]);                         // ..._thermal
+    if (flag_is_one(A.blanked[i])) return;
+    const double2 pos = A.pos[i];
     uint32_t st = 0;
-    double2 pos = A.pos[i];
-    if (kMode == 1 && !blanked) {
+    {
         // the particle's case: its tool, time step and interface segments
         const int c = case_of_hash(K, A.hash[i]);
         const ToolDev &tc = tool[c];
@@ -392,18 +387,40 @@ __global__ void __launch_bounds__(kBlock) k_step_tail(int N, KConsts K, SortedFi
         double bl = 0.;
         st |= contact_s1_one(K, tc.dt, cs, tc, pos, A.vel[i], fc, ft, nrm, on, bl);
         if (on >= 0) on += tc.seg_first;   // global segment id
-        if (flag_is_one(bl)) { blanked = true; A.blanked[i] = 1.; }
+        const bool blanked = flag_is_one(bl);
+        if (blanked) A.blanked[i] = 1.;
         A.ft[i] = ft;
         A.n[i] = nrm;
         A.on_seg[i] = on;
-        if (bc_fixed) fc = make_double2(0., 0.);
-        A.fc[i] = fc;
+        A.fc[i] = fc;   // zeroed for fixed particles by the tail (do_boundary_conditions)
         if (!blanked && on >= 0 && on < seg.n) {
             double T = A.T[i];
             contact_s2_one(K, tc.dt, seg, T_nodes, on, A.rho[i], T);
             A.T[i] = T;
         }
-    } else if (kMode == 2) {
+    }
+    if (st) set_status(status, st);
+}
+
+// ---- fused tail of the step ----------------------------------------------------------------------
+// The tool's contact for one particle -- kMode 2: rigid tool, update_tool_particles
+// and do_compute_contact_forces (tool_gpu.cu:146-216); kMode 0: no tool, or the
+// FEM tool whose contact k_contact_fem has applied just before -- then
+// do_boundary_conditions, do_boundary_conditions_thermal, do_invalidate
+// (actions_gpu.cu:756-824) and (kNextHash) the next step's compute_hashes and
+// the counting-sort histogram (grid.cu:25-42) on the final state.
+template <int kMode, bool kNextHash>
+__global__ void __launch_bounds__(kBlock) k_step_tail(int N, KConsts K, SortedFields A, SegDev seg,
+                                                      const ToolDev *__restrict__ tool,
+                                                      const double *__restrict__ T_nodes, SortScratch X,
+                                                      uint32_t *status) {
+    PARTICLE_LOOP_HEAD
+    bool blanked = flag_is_one(A.blanked[i]);
+    const bool bc_fixed = !flag_nonzero(A.tool_particle[i]) && flag_nonzero(A.fixed[i]);   // do_boundary_conditions
+    const bool bc_thermal = K.thermal_bc && flag_is_one(A.fixed[i]);                         // ..._thermal
+    uint32_t st = 0;
+    double2 pos = A.pos[i];
+    if (kMode == 2) {
         const sph_rigid_tool &rt = *K.rigid;
         if (flag_nonzero(A.tool_particle[i])) {   // update_tool_particles, blanked or not
             pos.x += K.dt * rt.vel[0];
@@ -616,9 +633,10 @@ void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedField
     if (K.has_tool) launch_seg_bins(s, K.n_cases, seg, tool);
 #undef GRID
 #define GRID div_up(N, tb), tb, 0, s
-    if (K.has_tool) {
-        if (next_hash) k_step_tail<1, true><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
-        else k_step_tail<1, false><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
+    if (K.has_tool) {   // the contact pass, then the tail of a step without tool
+        k_contact_fem<<<GRID>>>(N, K, A, seg, tool, T_nodes, status);
+        if (next_hash) k_step_tail<0, true><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
+        else k_step_tail<0, false><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
     } else if (K.rigid) {
         if (next_hash) k_step_tail<2, true><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
         else k_step_tail<2, false><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);

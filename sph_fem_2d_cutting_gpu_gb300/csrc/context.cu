@@ -405,7 +405,7 @@ int issue_fused_body(sph_ctx *ctx, int64_t &n, int w) {
     }
     CK(cudaMemsetAsync(ctx->X.counts, 0, sizeof(int32_t) * (size_t)(ctx->K.g.num_cell + 1), s));
     launch_step_tail(s, N, ctx->K, B, ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->X, ctx->W.status, true);
-    n += ctx->has_tool ? 2 : 1;   // with the FEM tool: the segment y-bins, then the tail
+    n += ctx->has_tool ? 3 : 1;   // with the FEM tool: the segment y-bins and the contact pass, then the tail
     CK_LAUNCH();
     return SPH_OK;
 }
@@ -1367,7 +1367,7 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
         launch_step_tail(s, N, ctx->K, B, ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->X, ctx->W.status, true);
         CK(cudaEventRecord(ev[7], s));
         CK_LAUNCH();
-        ctx->launches += 8 + (ctx->has_tool ? 4 : 0) + (pse_active(ctx) ? 1 : 0) + (ctx->K.rigid ? 1 : 0);
+        ctx->launches += 8 + (ctx->has_tool ? 5 : 0) + (pse_active(ctx) ? 1 : 0) + (ctx->K.rigid ? 1 : 0);
         CK(cudaEventSynchronize(ev[7]));
         for (int k = 0; k < kStages; k++) {
             float ms = 0.f;

@@ -52,7 +52,7 @@ void launch_contact(cudaStream_t s, int N, const KConsts &K, const SortedFields 
 void launch_bc(cudaStream_t s, int N, const SortedFields &A);
 void launch_bc_thermal(cudaStream_t s, int N, const KConsts &K, const SortedFields &A);
 void launch_invalidate(cudaStream_t s, int N, const SortedFields &A, uint32_t *status);
-// with the FEM tool: builds the segment y-bins first (one more launch)
+// with the FEM tool: the segment y-bins and the contact pass (k_contact_fem) first (two more launches)
 void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
                       ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
                       bool next_hash);
