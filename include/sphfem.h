@@ -549,11 +549,20 @@ int sph_wear_adjustment(sph_ctx *ctx);
  *  - hash_sorted [n]: optional (NULL to skip);
  *  - cell_start / cell_end [g->num_cell]: cell_end is left untouched for
  *    empty cells.
+ * Particles outside the grid (and blanked particles whose stale hash lies
+ * outside [0, num_cell)) go to one trailing bucket after every cell, in
+ * original-index order, exactly as in the allocating path; unlike that path,
+ * this call raises no status bit for them (SPH_STATUS_OUT_OF_GRID) nor for
+ * crowded cells (SPH_STATUS_CELL_OVERFLOW).  The in-cell ranking costs the
+ * square of a bucket's size, so many out-of-grid particles make it slow.
  * Scratch is a fixed file-scope device array (about 5.2 MB held by every GPU
  * that loads the library).  Limits: n <= 262144 particles and
  * g->num_cell <= 262143 cells; larger sizes return SPH_ERR_INVALID with a
- * message in err (err_len bytes, may be NULL).  The first call on a device
- * looks up the array's address there; make it before any stream capture.
+ * message in err (err_len bytes, may be NULL).  The first call in each CUDA
+ * context (the device's primary context, or one the caller created with the
+ * driver API and made current) looks up the array's address in that context;
+ * make it before any stream capture.  The lookup is cached per context, so a
+ * context created later (also after cudaDeviceReset) gets its own.
  * All calls share the scratch, so calls that overlap on the GPU race:
  * serialise them.  Work is queued on `stream` (cudaStream_t, NULL = default
  * stream); the call does not synchronise. */

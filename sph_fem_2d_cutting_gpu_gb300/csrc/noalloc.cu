@@ -17,8 +17,11 @@
 // Contract:
 //  - Each GPU that loads the library holds this array until the process
 //    exits: about 5.2 MB per device.
-//  - The first call on a device looks up the array's device address on that
-//    device.  Make that first call before any stream capture.
+//  - The first call in each CUDA context (a device's primary context, or a
+//    context the application created with the driver API) looks up the
+//    array's address in that context.  Make that first call before any
+//    stream capture.  A context created later (after cudaDeviceReset, say)
+//    gets its own lookup on its first call.
 //  - Every call shares the same array.  Calls that overlap on the GPU (two
 //    streams, or two host threads, in flight at once) race on it, so
 //    serialise them.
@@ -146,31 +149,84 @@ __global__ void __launch_bounds__(kBlock) k_na_rank(int n, ScratchView X, const 
     if (hash_sorted) hash_sorted[cs + rank] = hash[i];
 }
 
-// Per-device address of g_cells_scratch, looked up once with that device current.
-constexpr int kMaxDevices = 64;
-int32_t *g_scratch_addr[kMaxDevices] = {};
+// Address of g_cells_scratch in the CUDA context current at the call.  A
+// module's __device__ array has one copy per context: the device's primary
+// context (what the runtime API uses by default) and every context an
+// application creates itself with the driver API (cuCtxCreate) each hold
+// their own.  The cache is therefore keyed on the context's unique id
+// (cuCtxGetId, never reused within a process), not on the device ordinal:
+// after cudaDeviceReset the primary context is a new one with a new id, and
+// the lookup runs again.
+typedef int (*PFN_ctx_current)(void **ctx);
+typedef int (*PFN_ctx_id)(void *ctx, unsigned long long *id);
+constexpr int kCacheSlots = 64;
+struct ScratchSlot {
+    unsigned long long ctx_id;
+    int32_t *addr;
+};
+ScratchSlot g_scratch_cache[kCacheSlots] = {};
+int g_scratch_next = 0;
+PFN_ctx_current g_ctx_current = nullptr;
+PFN_ctx_id g_ctx_id = nullptr;
 std::mutex g_scratch_mu;
 
-int scratch_for_current_device(int32_t **out, char *err, int err_len) {
+int current_context_id(unsigned long long *id, char *err, int err_len) {
+    if (!g_ctx_current || !g_ctx_id) {
+        void *f1 = nullptr, *f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+        cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+            q2 != cudaDriverEntryPointSuccess || !f1 || !f2) {
+            if (err && err_len > 0)
+                snprintf(err, err_len, "driver entry points cuCtxGetCurrent / cuCtxGetId unavailable: %s",
+                         cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+            return SPH_ERR_NO_DEVICE;
+        }
+        g_ctx_current = (PFN_ctx_current)f1;
+        g_ctx_id = (PFN_ctx_id)f2;
+    }
+    void *ctx = nullptr;
+    if (g_ctx_current(&ctx) == 0 && !ctx) {
+        // no context current yet: make the device's primary context current (no
+        // allocation); with a context of the caller's current this is not reached
+        int dev = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaSetDevice(dev) == cudaSuccess) g_ctx_current(&ctx);
+    }
+    if (!ctx || g_ctx_id(ctx, id) != 0) {
+        if (err && err_len > 0) snprintf(err, err_len, "no current CUDA context");
+        return SPH_ERR_NO_DEVICE;
+    }
+    return SPH_OK;
+}
+
+int scratch_for_current_context(int32_t **out, char *err, int err_len) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    if (e != cudaSuccess || dev < 0) {
         if (err && err_len > 0) snprintf(err, err_len, "cudaGetDevice failed: %s", cudaGetErrorString(e));
         return SPH_ERR_NO_DEVICE;
     }
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_cells_scratch);
-        if (e != cudaSuccess || !p) {
-            if (err && err_len > 0)
-                snprintf(err, err_len, "cudaGetSymbolAddress(g_cells_scratch) failed on device %d: %s", dev,
-                         cudaGetErrorString(e));
-            return SPH_ERR_CUDA;
+    unsigned long long id = 0;
+    int r = current_context_id(&id, err, err_len);
+    if (r != SPH_OK) return r;
+    for (const ScratchSlot &s : g_scratch_cache)
+        if (s.addr && s.ctx_id == id) {
+            *out = s.addr;
+            return SPH_OK;
         }
-        g_scratch_addr[dev] = (int32_t *)p;
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_cells_scratch);
+    if (e != cudaSuccess || !p) {
+        if (err && err_len > 0)
+            snprintf(err, err_len, "cudaGetSymbolAddress(g_cells_scratch) failed on device %d: %s", dev,
+                     cudaGetErrorString(e));
+        return SPH_ERR_CUDA;
     }
-    *out = g_scratch_addr[dev];
+    g_scratch_cache[g_scratch_next] = {id, (int32_t *)p};   // oldest entry replaced when full
+    g_scratch_next = (g_scratch_next + 1) % kCacheSlots;
+    *out = (int32_t *)p;
     return SPH_OK;
 }
 
@@ -197,7 +253,7 @@ extern "C" int sph_cells_build_noalloc(const double *pos, const double *blanked,
         return SPH_ERR_INVALID;
     }
     int32_t *base = nullptr;
-    int r = scratch_for_current_device(&base, err, err_len);
+    int r = scratch_for_current_context(&base, err, err_len);
     if (r != SPH_OK) return r;
     ScratchView X = carve(base);
     cudaStream_t s = (cudaStream_t)stream;

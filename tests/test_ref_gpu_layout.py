@@ -4,6 +4,7 @@ the reference cubins read them that way.  Checked where the reference tree and
 nvcc are present (this test compiles static_asserts against the reference's
 own headers; no GPU): sizes and every named member's offset."""
 import ctypes as C
+import os
 import shutil
 import subprocess
 from pathlib import Path
@@ -13,7 +14,7 @@ import pytest
 from oracle import ref_gpu
 
 ROOT = Path(__file__).resolve().parents[1]
-REF = Path("/root/reference")
+REF = Path(os.environ.get("SPH_REFERENCE_DIR", "/root/reference"))
 NVCC = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
 
 # (ctypes class, C++ type, members to check: ctypes name -> C++ member)

@@ -15,21 +15,18 @@ from sph_fem_2d_cutting_gpu_gb300.solver import Solver
 pytestmark = pytest.mark.gpu
 
 
-def test_noalloc_cell_build_matches_context_sort(lib):
+def _compare_with_context_sort(lib, c):
+    """Run the allocating path (sph_assign_hashes + sph_sort on a context) and
+    sph_cells_build_noalloc twice on the same particles; both calls must give
+    its permutation, sorted hashes and cell tables bit for bit."""
     torch = pytest.importorskip("torch")
-    c = setups.micro(n_side=160, seed=21)
-    rng = np.random.default_rng(3)
-    perm_in = rng.permutation(c.N)
-    c.particles = {k: np.ascontiguousarray(v[perm_in]) for k, v in c.particles.items()}
-    c.particles["blanked"][::11] = 1.0
-    c.particles["hash"][::11] = 7          # stale hash of blanked particles
     s = Solver(c)
     g = s.geometry()
     assert c.N <= 262144 and g.num_cell <= 262143
     host = s.download(["pos", "blanked", "hash"])
-    # reference result from the allocating path
     s.assign_hashes()
     s.sort()
+    s.status()      # out-of-grid particles raise a status bit on the allocating path
     ref = s.download(["idx", "hash"])
     ref_start, ref_end = s.cells()
     dev = torch.device("cuda", 0)
@@ -56,6 +53,55 @@ def test_noalloc_cell_build_matches_context_sort(lib):
         ne = cs != -1
         assert np.array_equal(cend.cpu().numpy()[ne], ref_end[ne]), f"call {call}: cell_end differs"
         assert np.all(cend.cpu().numpy()[~ne] == -7), "cell_end of empty cells must stay untouched"
+    s.close()
+    return g
+
+
+def _shuffled_micro(n_side, seed):
+    c = setups.micro(n_side=n_side, seed=seed)
+    rng = np.random.default_rng(seed + 100)
+    perm_in = rng.permutation(c.N)
+    c.particles = {k: np.ascontiguousarray(v[perm_in]) for k, v in c.particles.items()}
+    return c, rng
+
+
+def test_noalloc_cell_build_matches_context_sort(lib):
+    c, _ = _shuffled_micro(160, 21)
+    c.particles["blanked"][::11] = 1.0
+    c.particles["hash"][::11] = 7          # stale hash of blanked particles (a valid cell)
+    _compare_with_context_sort(lib, c)
+
+
+def test_noalloc_out_of_grid_and_stale_hashes(lib):
+    """Particles outside the grid and blanked particles whose stale hash lies
+    outside the cell range all go to the trailing bucket, in original-index
+    order, on both paths."""
+    c, rng = _shuffled_micro(160, 22)
+    P = c.particles
+    g = c.grid
+    out = rng.choice(c.N, 300, replace=False)
+    P["pos"][out[:100], 0] = g.bbmin[0] - rng.uniform(1e-3, 1e-2, 100)     # left of the grid
+    P["pos"][out[100:200], 1] = g.bbmin[1] - rng.uniform(1e-3, 1e-2, 100)  # below it
+    P["blanked"][out[200:250]] = 1.0
+    P["hash"][out[200:250]] = -1                                            # stale, below the range
+    P["blanked"][out[250:]] = 1.0
+    P["hash"][out[250:]] = 10 ** 7                                          # stale, above the range
+    _compare_with_context_sort(lib, c)
+
+
+def test_noalloc_at_the_size_limits(lib):
+    """262,144 particles (the maximum) on a grid of just under 262,143 cells,
+    so the single-block scan covers its last buckets."""
+    c, rng = _shuffled_micro(512, 23)
+    g = c.grid
+    edge = g.h * g.cell_factor
+    nx = int(np.ceil((g.bbmax[0] - g.bbmin[0] + 2e-6) / edge))
+    ny = 262143 // nx
+    g.bbmax[1] = g.bbmin[1] + (ny - 0.5) * edge - 2e-6     # ceil gives ny rows
+    c.particles["blanked"][::97] = 1.0
+    c.particles["hash"][::97] = nx * ny + 5                 # stale, outside the range
+    geo = _compare_with_context_sort(lib, c)
+    assert geo.num_cell > 262143 - nx, geo.num_cell
 
 
 def test_noalloc_rejects_sizes_beyond_the_scratch(lib):
