@@ -16,7 +16,6 @@ __host__ __device__ __forceinline__ dbl4 mk4(double x, double y, double z, doubl
 }
 
 constexpr int kBlock = 256;          // particle kernels
-constexpr int kPairChunk = 32;       // in-support neighbours collected per pass of the pair loops
 constexpr int kMaxStencil = 3;       // the pair list packs the column offset in 3 bits
 constexpr int kCellRankCap = 4096;   // cells larger than this are ranked by the slow path
 constexpr double kPiFac = 0.454728408833987;   // PI_FAC, kernels.cuh:19 (10/(7 pi))

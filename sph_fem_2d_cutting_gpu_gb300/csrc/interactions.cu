@@ -50,6 +50,23 @@ struct KahanF {
     }
 };
 
+// In-support neighbours collected per pass of the pair loops.  With h = 1.7 dx
+// a particle has about 36 (a disc of radius 2h): 48 covers nearly all of them
+// in one pass.  A second, short pass costs more than its share: the lanes of a
+// warp hold 0 to 10 pairs in it, and it re-enters the candidate scan.  Larger
+// lists take shared memory from the L1 that serves the neighbour records.
+constexpr int kChunk32 = 48;
+constexpr int kChunk64 = 48;   // FP64: 48 x 256 threads x 4 B = the 48 KB static limit
+
+// Sums of the fused FP32 pair loop, each Kahan-compensated.  The epilogue needs
+// the stress divergence and the artificial viscosity only through the
+// acceleration (actions_gpu.cu:641-671: vel_t = visc + (S_der.x + S_der.y) +
+// forces / m), so both go into one sum per component: nine sums instead of
+// the staged form's thirteen.
+struct Acc32Fused {
+    KahanF vd0, vd1, vd2, vd3, ax, ay, xt0, xt1, tl;
+};
+
 // A particle blanked before the step skips the neighbour sums, the corrector and
 // the return mapping, but the rigid tool's do_material_fric_heat_gen
 // (actions_gpu.cu:316-343) has no blanked test and still heats it.
@@ -272,7 +289,7 @@ __global__ void __launch_bounds__(kB) k_interact64(int N, KConsts K, const int32
     Sums64 a = {};
     const int hash = B.hash[k];
     const sph_geom_constants &g = K.g;
-    __shared__ int s_list[kPairChunk][kB];
+    __shared__ int s_list[kChunk64][kB];
     int ii = 0, hi_i = 0, lo_j = 0, hi_j = 0, jc = 0, j1 = 0;
     bool done = true;
     if (hash >= 0 && hash < g.num_cell && !pse_tool) {
@@ -288,7 +305,7 @@ __global__ void __launch_bounds__(kB) k_interact64(int N, KConsts K, const int32
     while (!done) {
         // phase 1: collect the next in-support candidates (columns ii, cells lo_j..hi_j)
         int cnt = 0;
-        while (cnt < kPairChunk) {
+        while (cnt < kChunk64) {
             if (jc < j1) {
                 const dbl4 n0 = rec[4 * jc + 0];
                 const double dx = xi - n0.x, dy = yi - n0.y;
@@ -498,7 +515,7 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
             }
         }
     } else {
-        __shared__ int s_list_st[kPairChunk][kB];
+        __shared__ int s_list_st[kChunk32][kB];
         s_list = s_list_st;
     }
     if (k >= N) return;
@@ -526,6 +543,13 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
 
     KahanF vd0 = {}, vd1 = {}, vd2 = {}, vd3 = {}, sd0 = {}, sd1 = {}, sd2 = {}, sd3 = {};
     KahanF vt0 = {}, vt1 = {}, xt0 = {}, xt1 = {}, tl = {};
+    Acc32Fused af = {};
+    // cubic spline (kernels.cuh:25-65) with the per-particle factors folded:
+    // q > 1: W = fac/4 (2-q)^6, dW/(r dr) = -3/4 fac h1 (2-q)^2 / r;
+    // q <= 1: W = fac (1 - 3/2 q^2 + 3/4 q^3), dW/(r dr) = fac h1^2 (-3 + 9/4 q)
+    const float kwa = 0.25f * fac, kda = -0.75f * fac * h1;
+    const float kwc = -1.5f * fac, kwd = 0.75f * fac;
+    const float kde = -3.f * fac * h1 * h1, kdf = 2.25f * fac * h1 * h1;
     const int hash = B.hash[k];
     const sph_geom_constants &g = K.g;
     int gi = 0, gj = 0, ii = 0, hi_i = 0, lo_j = 0, hi_j = 0, j = 0, j1 = 0;
@@ -557,8 +581,8 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
         // phase 1: collect the next in-support, active neighbours (column offset packed in 3 bits);
         // four candidates per round keep four loads in flight
         int cnt = 0;
-        while (cnt < kPairChunk) {
-            if (j + 4 <= j1 && cnt <= kPairChunk - 4) {
+        while (cnt < kChunk32) {
+            if (j + 4 <= j1 && cnt <= kChunk32 - 4) {
                 float4 n[4];
 #pragma unroll
                 for (int u = 0; u < 4; u++) n[u] = nb[4 * (j + u)];
@@ -603,14 +627,56 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
             const int e = s_list[t][threadIdx.x];
             const int jn = e >> 3;
             const float4 n0 = nb[4 * jn + 0], n1 = nb[4 * jn + 1], n2 = nb[4 * jn + 2], n3 = nb[4 * jn + 3];
-            {
-                const int fj = __float_as_int(n0.z);
-                const float dx = (float)((e & 7) - R) * cell + (xri - n0.x);
-                const float dy = (float)(gj - (fj & kRowMask)) * cell + (yri - n0.y);
-                const float rr2 = dx * dx + dy * dy;
-                // FP32 form: hardware reciprocal square root instead of sqrt and division
-                const float inv_r = rsqrtf(rr2);
-                const float q = rr2 * inv_r * h1;
+            const int fj = __float_as_int(n0.z);
+            const float dx = (float)((e & 7) - R) * cell + (xri - n0.x);
+            const float dy = (float)(gj - (fj & kRowMask)) * cell + (yri - n0.y);
+            const float rr2 = dx * dx + dy * dy;
+            // FP32 form: hardware reciprocal square root instead of sqrt and division
+            const float inv_r = rsqrtf(rr2);
+            const float q = rr2 * inv_r * h1;
+            if constexpr (kFused) {
+                float w, dwf;
+                if (q > 1.f) {
+                    const float tq = 2.f - q, t2 = tq * tq;
+                    w = kwa * (t2 * t2 * t2);
+                    dwf = kda * t2 * inv_r;
+                } else {
+                    w = fmaf(q * q, fmaf(kwd, q, kwc), fac);
+                    dwf = fmaf(kdf, q, kde);
+                }
+                const float wx = dwf * dx, wy = dwf * dy;
+                const float volj = n2.w;
+                if (!tool_i && !(fj & kFlagTool)) {
+                    const float dvx = n1.x - vix, dvy = n1.y - viy;
+                    const float tx = wx * volj, ty = wy * volj;
+                    af.vd0.add(dvx * tx);
+                    af.vd1.add(dvx * ty);
+                    af.vd2.add(dvy * tx);
+                    af.vd3.add(dvy * ty);
+                    float fab = w * inv_wdp;
+                    fab *= fab;
+                    fab *= fab;
+                    const float sxx = (sAi + n2.x) + fab * (Rxxi + n3.x);
+                    const float sxy = (sBi + n2.y) + fab * (Rxyi + n3.y);
+                    const float syy = (sCi + n2.z) + fab * (Ryyi + n3.z);
+                    const float vijposij = -(dvx * dx + dvy * dy);
+                    const float irho = __fdividef(2.f, rhoi + n1.z);
+                    float piij = 0.f;
+                    if (vijposij < 0.f) {
+                        const float cij = 0.5f * (ci + n1.w);
+                        const float hij = 0.5f * (hi + n0.w);
+                        const float muij = __fdividef(hij * vijposij, rr2 + eta2 * hij * hij);
+                        piij = (-alpha * cij * muij + beta * muij * muij) * irho;
+                    }
+                    // acceleration / mass: (stress terms - viscosity) . grad W
+                    af.ax.add(fmaf(sxx - piij, wx, sxy * wy));
+                    af.ay.add(fmaf(sxy, wx, (syy - piij) * wy));
+                    const float wr = w * irho;
+                    af.xt0.add(wr * dvx);
+                    af.xt1.add(wr * dvy);
+                }
+                if (thermal) af.tl.add(volj * (Ti - n3.w) * dwf);
+            } else {
                 float val, der;
                 if (q > 1.f) {
                     const float t = 2.f - q, t2 = t * t;
@@ -659,6 +725,19 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
             }
         }
     }
+    if constexpr (kFused) {
+        const float mass = K.f.mass;
+        const float xs = K.f.xs_mass;
+        const float4 vd = make_float4(af.vd0.s, af.vd1.s, af.vd2.s, af.vd3.s);
+        // the whole acceleration sum rides in sd.x / sd.z (vt zero): the epilogue adds sd.x + sd.y + vt.x
+        const float4 sd = make_float4(mass * af.ax.s, 0.f, mass * af.ay.s, 0.f);
+        const float2 xt = make_float2(xs * af.xt0.s, xs * af.xt1.s);
+        const float T_t = thermal_alpha * (2.0f * af.tl.s);
+        // predicted velocity and density from this particle's record
+        fused_epilogue32(k, K, B, F, seg, tool, secant_iters, status, tool_i, make_float2(vix, viy), rhoi, vd, sd,
+                         make_float2(0.f, 0.f), xt, thermal, T_t);
+        return;
+    }
     const float mass = K.f.mass;
     const float xs = K.f.xs_mass;
     const float4 vd = make_float4(vd0.s, vd1.s, vd2.s, vd3.s);
@@ -666,18 +745,12 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
     const float2 vt = make_float2(-mass * vt0.s, -mass * vt1.s);
     const float2 xt = make_float2(xs * xt0.s, xs * xt1.s);
     const float T_t = thermal_alpha * (2.0f * tl.s);
-    if (!kFused) {
-        if (pse_tool) return;
-        F.S_der[k] = mk4(sd.x, sd.y, sd.z, sd.w);
-        F.v_der[k] = mk4(vd.x, vd.y, vd.z, vd.w);
-        B.pos_t[k] = make_double2(xt.x, xt.y);
-        B.vel_t[k] = make_double2(vt.x, vt.y);
-        if (thermal) B.T_t[k] = (double)T_t;
-    } else {
-        // predicted velocity and density from this particle's record
-        fused_epilogue32(k, K, B, F, seg, tool, secant_iters, status, tool_i, make_float2(vix, viy), rhoi, vd, sd,
-                         vt, xt, thermal, T_t);
-    }
+    if (pse_tool) return;
+    F.S_der[k] = mk4(sd.x, sd.y, sd.z, sd.w);
+    F.v_der[k] = mk4(vd.x, vd.y, vd.z, vd.w);
+    B.pos_t[k] = make_double2(xt.x, xt.y);
+    B.vel_t[k] = make_double2(vt.x, vt.y);
+    if (thermal) B.T_t[k] = (double)T_t;
 }
 
 // Launch shapes of the fused FP32K neighbour-sum kernel: (threads per block,
@@ -698,7 +771,7 @@ static void launch_i32(cudaStream_t s, int N, const KConsts &K, const int32_t *o
                        const FixedFields &F, const StepScratch &W, const SegDev &seg, const ToolDev *tool, int cap) {
     size_t smem = 0;
     if (kStaged) {
-        smem = (size_t)cap * 64 + sizeof(int) * kPairChunk * kB;
+        smem = (size_t)cap * 64 + sizeof(int) * kChunk32 * kB;
         static bool configured = false;   // opt in above 48 KB of dynamic shared memory, once
         if (!configured) {
             cudaFuncSetAttribute(k_interact32<true, kB, kMinB, kStaged>, cudaFuncAttributeMaxDynamicSharedMemorySize,
