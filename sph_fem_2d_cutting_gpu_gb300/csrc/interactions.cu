@@ -50,6 +50,14 @@ struct KahanF {
     }
 };
 
+// One 32-byte-aligned 256-bit load (two float4) through the non-coherent path:
+// the neighbour records are read-only while the pair loops run.
+__device__ __forceinline__ void ld_nc_256(const float4 *p, float4 &a, float4 &b) {
+    asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+                 : "l"(p));
+}
+
 // In-support neighbours collected per pass of the pair loops.  With h = 1.7 dx
 // a particle has about 36 (a disc of radius 2h): 48 covers nearly all of them
 // in one pass.  A second, short pass costs more than its share: the lanes of a
@@ -626,7 +634,18 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
         for (int t = 0; t < cnt; t++) {
             const int e = s_list[t][threadIdx.x];
             const int jn = e >> 3;
-            const float4 n0 = nb[4 * jn + 0], n1 = nb[4 * jn + 1], n2 = nb[4 * jn + 2], n3 = nb[4 * jn + 3];
+            // the 64-byte record of an in-support neighbour: two 256-bit loads (the
+            // kernel is bound by L1 wavefronts, and one request per 32 bytes halves them)
+            float4 n0, n1, n2, n3;
+            if (use_s) {
+                n0 = nb[4 * jn + 0];
+                n1 = nb[4 * jn + 1];
+                n2 = nb[4 * jn + 2];
+                n3 = nb[4 * jn + 3];
+            } else {
+                ld_nc_256(rec + 4 * jn, n0, n1);
+                ld_nc_256(rec + 4 * jn + 2, n2, n3);
+            }
             const int fj = __float_as_int(n0.z);
             const float dx = (float)((e & 7) - R) * cell + (xri - n0.x);
             const float dy = (float)(gj - (fj & kRowMask)) * cell + (yri - n0.y);
