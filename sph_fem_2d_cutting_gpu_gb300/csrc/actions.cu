@@ -309,6 +309,12 @@ __device__ __forceinline__ bool invalid_rates(double2 pt, double2 vt, dbl4 St, d
     return isnaninf(pt.x) || isnaninf(pt.y) || isnaninf(vt.x) || isnaninf(vt.y) || isnaninf(St.x) ||
            isnaninf(St.y) || isnaninf(St.z) || isnaninf(St.w) || isnaninf(rho_t) || isnaninf(T_t);
 }
+// the compact FP32 state: the same test on its FP32 rates
+__device__ __forceinline__ bool invalid_rates(float2 pt, float2 vt, float4 St, float rho_t, float T_t) {
+    return is_nan_or_inf(pt.x) || is_nan_or_inf(pt.y) || is_nan_or_inf(vt.x) || is_nan_or_inf(vt.y) ||
+           is_nan_or_inf(St.x) || is_nan_or_inf(St.y) || is_nan_or_inf(St.z) || is_nan_or_inf(St.w) ||
+           is_nan_or_inf(rho_t) || is_nan_or_inf(T_t);
+}
 
 __global__ void __launch_bounds__(kBlock) k_invalidate(int N, SortedFields A, uint32_t *status) {
     PARTICLE_LOOP_HEAD
@@ -362,7 +368,10 @@ __global__ void __launch_bounds__(kBlock) k_fric_heat_rigid(int N, KConsts K, So
 // only the particles near a tool reach it.  The tail that follows sees the
 // contact's results (forces, segment id, blanking, temperature) in memory, in the
 // order of the reference's step.
-__global__ void __launch_bounds__(kBlock) k_contact_fem(int N, KConsts K, SortedFields A, SegDev seg,
+// SF: SortedFields (FP64 state) or SortedFields32 (the compact state of FP32K
+// contexts); the contact search runs in FP64 either way.
+template <class SF>
+__global__ void __launch_bounds__(kBlock) k_contact_fem(int N, KConsts K, SF A, SegDev seg,
                                                         const ToolDev *__restrict__ tool,
                                                         const double *__restrict__ T_nodes, uint32_t *status) {
     PARTICLE_LOOP_HEAD
@@ -382,21 +391,21 @@ __global__ void __launch_bounds__(kBlock) k_contact_fem(int N, KConsts K, Sorted
             cs.bin_count += c * kSegBins;
             cs.bin_list += (size_t)c * kSegBins * kSegBinCap;
         }
-        double2 fc = A.fc[i], ft = A.ft[i], nrm = A.n[i];
+        double2 fc = d2(A.fc[i]), ft = d2(A.ft[i]), nrm = d2(A.n[i]);
         int on = A.on_seg[i];
         double bl = 0.;
-        st |= contact_s1_one(K, tc.dt, cs, tc, pos, A.vel[i], fc, ft, nrm, on, bl);
+        st |= contact_s1_one(K, tc.dt, cs, tc, pos, d2(A.vel[i]), fc, ft, nrm, on, bl);
         if (on >= 0) on += tc.seg_first;   // global segment id
         const bool blanked = flag_is_one(bl);
-        if (blanked) A.blanked[i] = 1.;
-        A.ft[i] = ft;
-        A.n[i] = nrm;
+        if (blanked) put(A.blanked[i], 1.);
+        put(A.ft[i], ft);
+        put(A.n[i], nrm);
         A.on_seg[i] = on;
-        A.fc[i] = fc;   // zeroed for fixed particles by the tail (do_boundary_conditions)
+        put(A.fc[i], fc);   // zeroed for fixed particles by the tail (do_boundary_conditions)
         if (!blanked && on >= 0 && on < seg.n) {
             double T = A.T[i];
             contact_s2_one(K, tc.dt, seg, T_nodes, on, A.rho[i], T);
-            A.T[i] = T;
+            put(A.T[i], T);
         }
     }
     if (st) set_status(status, st);
@@ -409,8 +418,8 @@ __global__ void __launch_bounds__(kBlock) k_contact_fem(int N, KConsts K, Sorted
 // do_boundary_conditions, do_boundary_conditions_thermal, do_invalidate
 // (actions_gpu.cu:756-824) and (kNextHash) the next step's compute_hashes and
 // the counting-sort histogram (grid.cu:25-42) on the final state.
-template <int kMode, bool kNextHash>
-__global__ void __launch_bounds__(kBlock) k_step_tail(int N, KConsts K, SortedFields A, SegDev seg,
+template <int kMode, bool kNextHash, class SF>
+__global__ void __launch_bounds__(kBlock) k_step_tail(int N, KConsts K, SF A, SegDev seg,
                                                       const ToolDev *__restrict__ tool,
                                                       const double *__restrict__ T_nodes, SortScratch X,
                                                       uint32_t *status) {
@@ -427,26 +436,26 @@ __global__ void __launch_bounds__(kBlock) k_step_tail(int N, KConsts K, SortedFi
             pos.y += K.dt * rt.vel[1];
             A.pos[i] = pos;
         } else {                                  // contact, blanked or not
-            double2 fc, ft = A.ft[i], nrm;
-            rigid_contact_one(K, rt, K.dt, pos, A.vel[i], fc, ft, nrm);
-            A.ft[i] = ft;
-            A.n[i] = nrm;
+            double2 fc, ft = d2(A.ft[i]), nrm;
+            rigid_contact_one(K, rt, K.dt, pos, d2(A.vel[i]), fc, ft, nrm);
+            put(A.ft[i], ft);
+            put(A.n[i], nrm);
             if (bc_fixed) fc = make_double2(0., 0.);
-            A.fc[i] = fc;
+            put(A.fc[i], fc);
         }
     } else if (bc_fixed) {
-        A.fc[i] = make_double2(0., 0.);
+        put(A.fc[i], make_double2(0., 0.));
     }
     if (bc_fixed) {
-        A.vel[i] = make_double2(0., 0.);
-        A.pos_t[i] = make_double2(0., 0.);
-        A.vel_t[i] = make_double2(0., 0.);
+        put(A.vel[i], make_double2(0., 0.));
+        put(A.pos_t[i], make_double2(0., 0.));
+        put(A.vel_t[i], make_double2(0., 0.));
     }
-    if (bc_thermal) A.T[i] = K.c.trml_wp.T_init;
+    if (bc_thermal) put(A.T[i], K.c.trml_wp.T_init);
     if (!blanked) {
         if (invalid_rates(A.pos_t[i], A.vel_t[i], A.S_t[i], A.rho_t[i], A.T_t[i])) {
             blanked = true;
-            A.blanked[i] = 1.;
+            put(A.blanked[i], 1.);
             st |= SPH_STATUS_NAN_BLANKED;
         }
     }
@@ -626,9 +635,9 @@ void launch_bc_thermal(cudaStream_t s, int N, const KConsts &K, const SortedFiel
 void launch_invalidate(cudaStream_t s, int N, const SortedFields &A, uint32_t *status) {
     k_invalidate<<<GRID>>>(N, A, status);
 }
-void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
-                      ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
-                      bool next_hash) {
+template <class SF>
+static void step_tail(cudaStream_t s, int N, const KConsts &K, const SF &A, const SegDev &seg, ToolDev *tool,
+                      const double *T_nodes, const SortScratch &X, uint32_t *status, bool next_hash) {
     const int tb = fp64_block(N);   // the contact search is FP64 work: spread small systems over all SMs
     if (K.has_tool) launch_seg_bins(s, K.n_cases, seg, tool);
 #undef GRID
@@ -644,6 +653,16 @@ void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedField
         if (next_hash) k_step_tail<0, true><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
         else k_step_tail<0, false><<<GRID>>>(N, K, A, seg, tool, T_nodes, X, status);
     }
+}
+void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
+                      ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
+                      bool next_hash) {
+    step_tail(s, N, K, A, seg, tool, T_nodes, X, status, next_hash);
+}
+void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedFields32 &A, const SegDev &seg,
+                      ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
+                      bool next_hash) {
+    step_tail(s, N, K, A, seg, tool, T_nodes, X, status, next_hash);
 }
 #undef GRID
 #define GRID div_up(N, kBlock), kBlock, 0, s

@@ -15,16 +15,16 @@ namespace sphfem {
 // ---- hashing: grid.cu:25-42 compute_hashes --------------------------------------
 // kHash: write hash for non-blanked particles (blanked keep their stale hash).
 // kCount: derive the sort key and take an arrival slot in the key's bucket.
-template <bool kHash, bool kCount>
+template <bool kHash, bool kCount, class Bl>
 __global__ void __launch_bounds__(kBlock) k_hash_count(int N, const double2 *__restrict__ pos,
-                                                       const double *__restrict__ blanked, int32_t *__restrict__ hash,
+                                                       const Bl *__restrict__ blanked, int32_t *__restrict__ hash,
                                                        int32_t *__restrict__ key, int32_t *__restrict__ arrival,
                                                        int32_t *__restrict__ counts, int32_t *__restrict__ hash_next,
                                                        sph_geom_constants g, float inv_dxf, uint32_t *status) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     int h;
-    if (kHash && blanked[i] != 1.) {
+    if (kHash && !flag_is_one(blanked[i])) {
         double2 p = pos[i];
         int ix = cell_coord(p.x, g.bbmin_x, g.dx, inv_dxf);
         int iy = cell_coord(p.y, g.bbmin_y, g.dx, inv_dxf);
@@ -338,35 +338,48 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused(int N, const int32_t *_
     }
 }
 
-// FP32-compensated form of the fused reorder: the same gather, with the
-// predictor, EOS and artificial stress of the predicted state evaluated in
-// FP32 (positions and density stay FP64: rho - rho0 is a small difference,
-// FP32 would lose its leading digits) and written into the FP32 record.
-__global__ void __launch_bounds__(kBlock) k_gather_fused32(int N, const int32_t *__restrict__ perm, KConsts K,
-                                                           SortedFields A, SortedFields B, FixedFields F,
+__device__ __forceinline__ float2 f2(double2 v) { return make_float2((float)v.x, (float)v.y); }
+__device__ __forceinline__ float2 f2(float2 v) { return v; }
+__device__ __forceinline__ float4 f4(dbl4 v) { return make_float4((float)v.x, (float)v.y, (float)v.z, (float)v.w); }
+__device__ __forceinline__ float4 f4(float4 v) { return v; }
+
+// FP32-compensated form of the fused reorder: the same gather into the compact
+// FP32 state (SortedFields32), with the predictor, EOS and artificial stress of
+// the predicted state evaluated in FP32 (positions and density stay FP64: rho -
+// rho0 is a small difference, FP32 would lose its leading digits) and written
+// into the FP32 record.  SF / FF: the state the step starts from -- the FP64
+// arrays after an upload or a staged call, the compact arrays after a fused
+// step.  p and R of tool particles are kept from FF at the sorted position, as
+// the reference leaves them (they are not part of the Green sort's buffer).
+template <class SF, class FF>
+__global__ void __launch_bounds__(kBlock) k_gather_fused32(int N, const int32_t *__restrict__ perm, KConsts K, SF A,
+                                                           FF Fsrc, SortedFields32 B, FixedFields32 F,
+                                                           int32_t *__restrict__ idx,
                                                            const int32_t *__restrict__ hash_src,
                                                            float4 *__restrict__ rec, const ToolDev *__restrict__ tools) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= N) return;
     int i = perm[k];
-    F.idx[k] = i;
-    const double2 pos = A.pos[i], vel = A.vel[i], pos_t = A.pos_t[i], vel_t = A.vel_t[i];
-    const dbl4 S = A.S[i], S_t = A.S_t[i];
-    const double rho = A.rho[i], T = A.T[i], h = A.h[i], rho_t = A.rho_t[i], T_t = A.T_t[i];
-    const double blanked = A.blanked[i], tool = A.tool_particle[i];
+    idx[k] = i;
+    const double2 pos = A.pos[i];
+    const float2 vel = f2(A.vel[i]), pos_t = f2(A.pos_t[i]), vel_t = f2(A.vel_t[i]);
+    const float4 S = f4(A.S[i]), S_t = f4(A.S_t[i]);
+    const double rho = A.rho[i];
+    const float T = (float)A.T[i], h = (float)A.h[i], rho_t = (float)A.rho_t[i], T_t = (float)A.T_t[i];
+    const float blanked = (float)A.blanked[i], tool = (float)A.tool_particle[i];
     const int hash = hash_src[i];
     B.pos[k] = pos;
     B.vel[k] = vel;
-    B.fc[k] = A.fc[i];
-    B.ft[k] = A.ft[i];
+    B.fc[k] = f2(A.fc[i]);
+    B.ft[k] = f2(A.ft[i]);
     B.h[k] = h;
-    B.n[k] = A.n[i];
+    B.n[k] = f2(A.n[i]);
     B.rho[k] = rho;
     B.S[k] = S;
-    B.eps_pl[k] = A.eps_pl[i];
-    B.eps_pl_dot[k] = A.eps_pl_dot[i];
+    B.eps_pl[k] = (float)A.eps_pl[i];
+    B.eps_pl_dot[k] = (float)A.eps_pl_dot[i];
     B.T[k] = T;
-    B.fixed[k] = A.fixed[i];
+    B.fixed[k] = (float)A.fixed[i];
     B.blanked[k] = blanked;
     B.tool_particle[k] = tool;
     B.pos_t[k] = pos_t;
@@ -380,23 +393,23 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused32(int N, const int32_t 
     // predictor (leap_frog.cu:45-69)
     double2 pp = pos;
     double rp = rho;
-    float vx = (float)vel.x, vy = (float)vel.y;
-    float4 Sp = make_float4((float)S.x, (float)S.y, (float)S.z, (float)S.w);
-    float Tp = (float)T;
+    float vx = vel.x, vy = vel.y;
+    float4 Sp = S;
+    float Tp = T;
     if (!is_blanked) {
         const ToolDev &tc = tools[case_of_hash(K, hash)];   // time step of the particle's case
         const double hdt = tc.hdt;
         const float hdtf = tc.hdtf;
-        pp.x = pos.x + hdt * pos_t.x;
-        pp.y = pos.y + hdt * pos_t.y;
-        rp = rho + hdt * rho_t;
-        vx = fmaf(hdtf, (float)vel_t.x, vx);
-        vy = fmaf(hdtf, (float)vel_t.y, vy);
-        Sp.x = fmaf(hdtf, (float)S_t.x, Sp.x);
-        Sp.y = fmaf(hdtf, (float)S_t.y, Sp.y);
-        Sp.z = fmaf(hdtf, (float)S_t.z, Sp.z);
-        Sp.w = fmaf(hdtf, (float)S_t.w, Sp.w);
-        Tp = fmaf(hdtf, (float)T_t, Tp);
+        pp.x = pos.x + hdt * (double)pos_t.x;
+        pp.y = pos.y + hdt * (double)pos_t.y;
+        rp = rho + hdt * (double)rho_t;
+        vx = fmaf(hdtf, vel_t.x, vx);
+        vy = fmaf(hdtf, vel_t.y, vy);
+        Sp.x = fmaf(hdtf, S_t.x, Sp.x);
+        Sp.y = fmaf(hdtf, S_t.y, Sp.y);
+        Sp.z = fmaf(hdtf, S_t.z, Sp.z);
+        Sp.w = fmaf(hdtf, S_t.w, Sp.w);
+        Tp = fmaf(hdtf, T_t, Tp);
     }
     const float rhof = (float)rp;
     float p;
@@ -404,13 +417,13 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused32(int N, const int32_t 
     if (!is_tool) {
         p = (float)(K.c0sq * (rp - K.c.phys.rho0));                 // do_material_eos
         R = artificial_stress_f32(K.f.stresseps, rhof, p, Sp);
-        F.p[k] = (double)p;
-        F.R[k] = mk4(R.x, R.y, R.z, 0.);
+        R.w = 0.f;
     } else {
-        p = (float)F.p[k];
-        dbl4 Rd = F.R[k];
-        R = make_float4((float)Rd.x, (float)Rd.y, (float)Rd.z, 0.f);
+        p = (float)Fsrc.p[k];
+        R = f4(Fsrc.R[k]);
     }
+    F.p[k] = p;
+    F.R[k] = R;
     const float Tn = Tp;   // every record carries T (k_build_records)
     // record: (xr, yr, flags|row, h) (vx, vy, rho, c) (sA, sB, sC, m/rho) (Rxx, Rxy, Ryy, T)
     const sph_geom_constants &g = K.g;
@@ -420,10 +433,45 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused32(int N, const int32_t 
     const float yr = (float)(pp.y - (g.bbmin_y + (double)cj * g.dx));
     const int flags = (cj & kRowMask) | (is_blanked ? kFlagBlanked : 0) | (is_tool ? kFlagTool : 0);
     const float rho21 = 1.f / (rhof * rhof);
-    rec[4 * k + 0] = make_float4(xr, yr, __int_as_float(flags), (float)h);
+    rec[4 * k + 0] = make_float4(xr, yr, __int_as_float(flags), h);
     rec[4 * k + 1] = make_float4(vx, vy, rhof, sqrtf(K.f.K_bulk / rhof));
     rec[4 * k + 2] = make_float4((Sp.x - p) * rho21, Sp.y * rho21, (Sp.z - p) * rho21, K.f.mass / rhof);
     rec[4 * k + 3] = make_float4(R.x, R.y, R.z, Tn);
+}
+
+// The compact FP32 state (state) and its p, R (pr) widened into the FP64
+// arrays: exact.
+__global__ void __launch_bounds__(kBlock) k_state_to64(int N, SortedFields32 A, FixedFields32 Fa, SortedFields B,
+                                                       FixedFields F, bool state, bool pr) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    if (pr) {
+        F.p[k] = Fa.p[k];
+        const float4 R = Fa.R[k];
+        F.R[k] = mk4(R.x, R.y, R.z, 0.);
+    }
+    if (!state) return;
+    B.pos[k] = A.pos[k];
+    B.vel[k] = d2(A.vel[k]);
+    B.fc[k] = d2(A.fc[k]);
+    B.ft[k] = d2(A.ft[k]);
+    B.n[k] = d2(A.n[k]);
+    B.h[k] = A.h[k];
+    B.rho[k] = A.rho[k];
+    B.eps_pl[k] = A.eps_pl[k];
+    B.eps_pl_dot[k] = A.eps_pl_dot[k];
+    B.T[k] = A.T[k];
+    B.fixed[k] = A.fixed[k];
+    B.blanked[k] = A.blanked[k];
+    B.tool_particle[k] = A.tool_particle[k];
+    B.S[k] = d4(A.S[k]);
+    B.pos_t[k] = d2(A.pos_t[k]);
+    B.vel_t[k] = d2(A.vel_t[k]);
+    B.rho_t[k] = A.rho_t[k];
+    B.T_t[k] = A.T_t[k];
+    B.S_t[k] = d4(A.S_t[k]);
+    B.on_seg[k] = A.on_seg[k];
+    B.hash[k] = A.hash[k];
 }
 
 // ---- host launchers ---------------------------------------------------------------------
@@ -433,8 +481,9 @@ void launch_hash(cudaStream_t s, int N, const SortedFields &A, sph_geom_constant
                                                                      nullptr);
 }
 
-void launch_count(cudaStream_t s, int N, const SortedFields &A, const SortScratch &X, sph_geom_constants g,
-                  uint32_t *status, bool with_hash) {
+template <class SF>
+static void count(cudaStream_t s, int N, const SF &A, const SortScratch &X, sph_geom_constants g, uint32_t *status,
+                  bool with_hash) {
     cudaMemsetAsync(X.counts, 0, sizeof(int32_t) * (size_t)(g.num_cell + 1), s);
     if (with_hash)
         k_hash_count<true, true><<<div_up(N, kBlock), kBlock, 0, s>>>(N, A.pos, A.blanked, A.hash, X.key, X.arrival,
@@ -442,6 +491,14 @@ void launch_count(cudaStream_t s, int N, const SortedFields &A, const SortScratc
     else
         k_hash_count<false, true><<<div_up(N, kBlock), kBlock, 0, s>>>(N, A.pos, A.blanked, A.hash, X.key, X.arrival,
                                                                         X.counts, X.hash_next, g, (float)(1.0 / g.dx), status);
+}
+void launch_count(cudaStream_t s, int N, const SortedFields &A, const SortScratch &X, sph_geom_constants g,
+                  uint32_t *status, bool with_hash) {
+    count(s, N, A, X, g, status, with_hash);
+}
+void launch_count(cudaStream_t s, int N, const SortedFields32 &A, const SortScratch &X, sph_geom_constants g,
+                  uint32_t *status, bool with_hash) {
+    count(s, N, A, X, g, status, with_hash);
 }
 
 int scan_blocks(int num_cell) { return div_up(num_cell + 1, kScanTile); }
@@ -465,10 +522,27 @@ void launch_gather_fused(cudaStream_t s, int N, const int32_t *perm, const KCons
                          const SortedFields &B, const FixedFields &F, const StepScratch &W, const int32_t *hash_src,
                          const ToolDev *tool) {
     const int tb = fp64_block(N);   // EOS and artificial stress per particle: spread small systems
-    if (K.precision == SPH_PREC_FP32K)
-        k_gather_fused32<<<div_up(N, tb), tb, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec32, tool);
+    k_gather_fused<false><<<div_up(N, tb), tb, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec64, W.rec32);
+}
+
+void launch_gather_fused32(cudaStream_t s, int N, const int32_t *perm, const KConsts &K, const SortedFields *A64,
+                           const SortedFields32 *A32, bool pr32, const FixedFields &F, const FixedFields32 &F32,
+                           const SortedFields32 &B, int32_t *idx, const StepScratch &W, const int32_t *hash_src,
+                           const ToolDev *tool) {
+    const int tb = fp64_block(N), g = div_up(N, tb);
+    if (A32 && pr32)
+        k_gather_fused32<<<g, tb, 0, s>>>(N, perm, K, *A32, F32, B, F32, idx, hash_src, W.rec32, tool);
+    else if (A32)
+        k_gather_fused32<<<g, tb, 0, s>>>(N, perm, K, *A32, F, B, F32, idx, hash_src, W.rec32, tool);
+    else if (pr32)
+        k_gather_fused32<<<g, tb, 0, s>>>(N, perm, K, *A64, F32, B, F32, idx, hash_src, W.rec32, tool);
     else
-        k_gather_fused<false><<<div_up(N, tb), tb, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec64, W.rec32);
+        k_gather_fused32<<<g, tb, 0, s>>>(N, perm, K, *A64, F, B, F32, idx, hash_src, W.rec32, tool);
+}
+
+void launch_state_to64(cudaStream_t s, int N, const SortedFields32 &A, const FixedFields32 &Fa, const SortedFields &B,
+                       const FixedFields &F, bool state, bool pr) {
+    k_state_to64<<<div_up(N, kBlock), kBlock, 0, s>>>(N, A, Fa, B, F, state, pr);
 }
 
 void launch_build_records(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F,

@@ -113,6 +113,26 @@ __device__ __forceinline__ bool is_nan_or_inf(double v) {          // isnan(v) |
     return (__double_as_longlong(v) & 0x7FF0000000000000LL) == 0x7FF0000000000000LL;
 }
 
+// The same tests on the 0/1 flags of the compact FP32 state.
+__device__ __forceinline__ bool flag_is_one(float v) { return __float_as_int(v) == 0x3F800000; }
+__device__ __forceinline__ bool flag_nonzero(float v) { return (__float_as_int(v) << 1) != 0; }
+__device__ __forceinline__ bool is_nan_or_inf(float v) { return (__float_as_int(v) & 0x7F800000) == 0x7F800000; }
+
+// Values of either state form widened to FP64, and FP64 values stored into
+// either form (rounded once to FP32 in the compact form).
+__device__ __forceinline__ double2 d2(double2 v) { return v; }
+__device__ __forceinline__ double2 d2(float2 v) { return make_double2(v.x, v.y); }
+__device__ __forceinline__ dbl4 d4(dbl4 v) { return v; }
+__device__ __forceinline__ dbl4 d4(float4 v) { return mk4(v.x, v.y, v.z, v.w); }
+__device__ __forceinline__ void put(double2 &dst, double2 v) { dst = v; }
+__device__ __forceinline__ void put(float2 &dst, double2 v) { dst = make_float2((float)v.x, (float)v.y); }
+__device__ __forceinline__ void put(dbl4 &dst, dbl4 v) { dst = v; }
+__device__ __forceinline__ void put(float4 &dst, dbl4 v) {
+    dst = make_float4((float)v.x, (float)v.y, (float)v.z, (float)v.w);
+}
+__device__ __forceinline__ void put(double &dst, double v) { dst = v; }
+__device__ __forceinline__ void put(float &dst, double v) { dst = (float)v; }
+
 // compute_hashes' cell index (int)((x - bbmin)/dx) (grid.cu:36-39), bit for bit.
 // The quotient is first formed in FP32 with inv_dxf = (float)(1/dx): against the
 // FP64 quotient its error is below 3*2^-24 relative (three FP32 roundings and the

@@ -31,6 +31,15 @@ struct sph_ctx {
     int cur = 0;                         // buf[cur] holds the particle state
     int last_in = -1;                    // the buffer the last step read
     FixedFields F{};
+    // FP32K contexts: the compact FP32 state the fused step reads and writes, one
+    // per particle buffer, and which form of each buffer holds its state.  The
+    // FP64 arrays (the caller-visible particle_gpu layout) are filled from the
+    // compact ones on demand (sync64) before any call that reads or writes them.
+    SortedFields32 c32[kBufs]{};
+    FixedFields32 F32{};
+    bool v64[kBufs] = {true, true, true, true};   // buf[b] holds buffer b's state
+    bool v32[kBufs] = {};                          // c32[b] holds it
+    bool pr64 = true, pr32 = false;                // F / F32 hold the newest p and R
     SortScratch X{};
     StepScratch W{};
     bool counts_valid = false;           // X.key/arrival/counts match the current state
@@ -42,8 +51,9 @@ struct sph_ctx {
     ToolDev *tool_dev = nullptr;
     double *fem_T_old = nullptr, *fem_f_temp = nullptr, *fem_K_temp = nullptr;
     // graphs, one per buffer parity
-    cudaGraphExec_t graph[kBufs][kBufs] = {};    // [input buffer][output buffer]
-    int64_t graph_launches[kBufs][kBufs] = {};
+    // [input buffer][output buffer][FP32K: input in the compact form][FP32K: p, R from F32]
+    cudaGraphExec_t graph[kBufs][kBufs][2][2] = {};
+    int64_t graph_launches[kBufs][kBufs][2][2] = {};
     bool use_graph = true;
     int64_t launches = 0;
     double *h_reduce = nullptr;          // pinned
@@ -231,10 +241,12 @@ void set_case_dt(ToolDev &td, double dt) {
 void invalidate_graphs(sph_ctx *ctx) {
     for (int a = 0; a < kBufs; a++)
         for (int b = 0; b < kBufs; b++)
-            if (ctx->graph[a][b]) {
-                cudaGraphExecDestroy(ctx->graph[a][b]);
-                ctx->graph[a][b] = nullptr;
-            }
+            for (int c = 0; c < 2; c++)
+                for (int d = 0; d < 2; d++)
+                    if (ctx->graph[a][b][c][d]) {
+                        cudaGraphExecDestroy(ctx->graph[a][b][c][d]);
+                        ctx->graph[a][b][c][d] = nullptr;
+                    }
 }
 
 // Field descriptors for upload/download of the caller-visible view.
@@ -291,6 +303,39 @@ int alloc_sorted(sph_ctx *ctx, SortedFields &S, int N) {
     return SPH_OK;
 }
 
+int alloc_sorted32(sph_ctx *ctx, SortedFields32 &S, int N) {
+    DALLOC(S.pos, N); DALLOC(S.vel, N); DALLOC(S.fc, N); DALLOC(S.ft, N); DALLOC(S.n, N);
+    DALLOC(S.h, N); DALLOC(S.rho, N); DALLOC(S.eps_pl, N); DALLOC(S.eps_pl_dot, N); DALLOC(S.T, N);
+    DALLOC(S.fixed, N); DALLOC(S.blanked, N); DALLOC(S.tool_particle, N); DALLOC(S.S, N);
+    DALLOC(S.pos_t, N); DALLOC(S.vel_t, N); DALLOC(S.rho_t, N); DALLOC(S.T_t, N); DALLOC(S.S_t, N);
+    DALLOC(S.on_seg, N); DALLOC(S.hash, N);
+    return SPH_OK;
+}
+
+// FP32K contexts: makes the FP64 arrays of the current buffer (and F.p, F.R)
+// hold the state, widening the compact form into them if a fused step left it
+// there.  `modify`: the caller may change the FP64 state, so the compact form
+// (and F32's p, R) no longer count and the next fused step starts from FP64.
+int sync64(sph_ctx *ctx, bool modify) {
+    if (ctx->K.precision != SPH_PREC_FP32K) return SPH_OK;
+    const int b = ctx->cur;
+    if (!ctx->v64[b] || !ctx->pr64) {
+        int r = wait_io(ctx, b);   // copies into or out of buf[b] still in flight
+        if (r) return r;
+        launch_state_to64(ctx->stream, ctx->N, ctx->c32[b], ctx->F32, ctx->buf[b], ctx->F, !ctx->v64[b],
+                          !ctx->pr64);
+        ctx->launches++;
+        CK_LAUNCH();
+        ctx->v64[b] = true;
+        ctx->pr64 = true;
+    }
+    if (modify) {
+        ctx->v32[b] = false;
+        ctx->pr32 = false;
+    }
+    return SPH_OK;
+}
+
 int zero_all(sph_ctx *ctx) {
     sph_particles v = view_of(ctx);
     for (const FieldDesc &fd : kFields) {
@@ -307,6 +352,7 @@ int ensure_io(sph_ctx *ctx) {
     if (ctx->io_up) return SPH_OK;
     for (int b = 2; b < kBufs; b++) {
         int r = alloc_sorted(ctx, ctx->buf[b], ctx->N);
+        if (!r && ctx->K.precision == SPH_PREC_FP32K) r = alloc_sorted32(ctx, ctx->c32[b], ctx->N);
         if (r) return r;
     }
     ctx->nbuf = kBufs;
@@ -338,6 +384,13 @@ int ensure_fem_temp(sph_ctx *ctx) {
         int jr_ = join_io(ctx);                  \
         if (jr_ != SPH_OK) return jr_;           \
     }
+// Calls that read (modify false) or may write (modify true) the particle state
+// through the FP64 arrays.
+#define REQUIRE_STATE(modify)                    \
+    {                                            \
+        int sr_ = sync64(ctx, modify);           \
+        if (sr_ != SPH_OK) return sr_;           \
+    }
 #define REQUIRE_TOOL() \
     if (!ctx->has_tool) return fail(ctx, SPH_ERR_STATE, "context has no tool");
 // Calls that take one time step or one tool for the whole context.
@@ -357,38 +410,58 @@ int jc_warm_grid(const sph_ctx *ctx) {
 bool pse_active(const sph_ctx *ctx) { return ctx->K.thermal_pse && ctx->K.c.trml_wp.alpha != 0.; }
 
 // The fused step body (everything after the histogram of the current state),
-// reading buf[cur] and writing buf[w].
-int issue_fused_body(sph_ctx *ctx, int64_t &n, int w) {
+// reading buf[cur] and writing buf[w] -- in FP32K contexts the compact form
+// c32[w], from c32[cur] when it holds the state (v32) and buf[cur] otherwise.
+// ev (profiling, may be null): events recorded after the sort, the reorder, the
+// FEM half step + PSE, the neighbour sums, the tool updates and the tail
+// (ev[0..5]).
+int issue_fused_body(sph_ctx *ctx, int64_t &n, int w, cudaEvent_t *ev = nullptr) {
     const int N = ctx->N;
     cudaStream_t s = ctx->stream;
+    const bool f32 = ctx->K.precision == SPH_PREC_FP32K;
     SortedFields &A = ctx->buf[ctx->cur];
     SortedFields &B = ctx->buf[w];
+    SortedFields32 &B32 = ctx->c32[w];
     launch_sort_rest(s, N, ctx->X, ctx->K.g, ctx->F.idx, ctx->W.status);
     n += 5;
-    launch_gather_fused(s, N, ctx->F.idx, ctx->K, A, B, ctx->F, ctx->W, ctx->X.hash_next, ctx->tool_dev);
+    if (ev) CK(cudaEventRecord(ev[0], s));
+    if (f32)
+        launch_gather_fused32(s, N, ctx->F.idx, ctx->K, ctx->v32[ctx->cur] ? nullptr : &A,
+                              ctx->v32[ctx->cur] ? &ctx->c32[ctx->cur] : nullptr, ctx->pr32, ctx->F, ctx->F32, B32,
+                              ctx->F.idx, ctx->W, ctx->X.hash_next, ctx->tool_dev);
+    else
+        launch_gather_fused(s, N, ctx->F.idx, ctx->K, A, B, ctx->F, ctx->W, ctx->X.hash_next, ctx->tool_dev);
     n += 1;
+    if (ev) CK(cudaEventRecord(ev[1], s));
     if (ctx->has_tool) {
         launch_fem_half(s, ctx->K, ctx->fem, ctx->tool_dev);
         n += 1;
     }
     if (pse_active(ctx)) {
-        launch_heat_pse(s, N, ctx->K, ctx->X.offsets, ctx->W, B);
+        if (f32) launch_heat_pse(s, N, ctx->K, ctx->X.offsets, ctx->W, B32);
+        else launch_heat_pse(s, N, ctx->K, ctx->X.offsets, ctx->W, B);
         n += 1;
     }
+    if (ev) CK(cudaEventRecord(ev[2], s));
     SegDev sw = ctx->seg;
     if (ctx->wear_mode != SPH_WEAR_OFF) {   // segments_wear_rate_reset (leap_frog.cu:183-186)
         launch_wear_reset(s, ctx->seg);
         sw.wear.T_nodes = ctx->fem.T_half;  // the friction heat sees the half-step FEM temperature
     }
     if (ctx->mlp_on) CK(cudaMemsetAsync(ctx->jc_list_count, 0, sizeof(int32_t), s));
-    launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, sw, ctx->tool_dev, true,
-                        ctx->interact_variant);
+    if (f32)
+        launch_interactions32_fused(s, N, ctx->K, ctx->X.offsets, B32, ctx->F32, ctx->W, sw, ctx->tool_dev,
+                                    ctx->interact_variant);
+    else
+        launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, sw, ctx->tool_dev, true,
+                            ctx->interact_variant);
     n += 1;
-    if (ctx->mlp_on) {
-        launch_jc_warm(s, jc_warm_grid(ctx), ctx->K, B, ctx->F, ctx->tool_dev, ctx->mlp, ctx->W.secant_iters,
+    if (ctx->mlp_on) {   // FP32K only (sph_mlp_attach)
+        launch_jc_warm(s, jc_warm_grid(ctx), ctx->K, B32, ctx->F32, ctx->tool_dev, ctx->mlp, ctx->W.secant_iters,
                        ctx->W.status);
         n += 1;
     }
+    if (ev) CK(cudaEventRecord(ev[3], s));
     if (ctx->has_tool) {
         launch_fem_rate_update(s, ctx->K, ctx->fem, ctx->seg, ctx->tool_dev);
         n += 1;
@@ -403,11 +476,40 @@ int issue_fused_body(sph_ctx *ctx, int64_t &n, int w) {
         launch_rigid_move(s, ctx->K.rigid, ctx->K.dt);
         n += 1;
     }
+    if (ev) CK(cudaEventRecord(ev[4], s));
     CK(cudaMemsetAsync(ctx->X.counts, 0, sizeof(int32_t) * (size_t)(ctx->K.g.num_cell + 1), s));
-    launch_step_tail(s, N, ctx->K, B, ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->X, ctx->W.status, true);
+    if (f32) launch_step_tail(s, N, ctx->K, B32, ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->X, ctx->W.status, true);
+    else launch_step_tail(s, N, ctx->K, B, ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->X, ctx->W.status, true);
     n += ctx->has_tool ? 3 : 1;   // with the FEM tool: the segment y-bins and the contact pass, then the tail
+    if (ev) CK(cudaEventRecord(ev[5], s));
     CK_LAUNCH();
     return SPH_OK;
+}
+
+// The histogram of the current state, when the last call left it stale.
+int count_current(sph_ctx *ctx) {
+    if (ctx->counts_valid) return SPH_OK;
+    if (ctx->K.precision == SPH_PREC_FP32K && ctx->v32[ctx->cur])
+        launch_count(ctx->stream, ctx->N, ctx->c32[ctx->cur], ctx->X, ctx->K.g, ctx->W.status, true);
+    else
+        launch_count(ctx->stream, ctx->N, ctx->buf[ctx->cur], ctx->X, ctx->K.g, ctx->W.status, true);
+    ctx->launches += 1;
+    CK_LAUNCH();
+    return SPH_OK;
+}
+
+// After a fused step from buffer p into w: the bookkeeping of both forms.
+void finish_step(sph_ctx *ctx, int p, int w) {
+    if (ctx->K.precision == SPH_PREC_FP32K) {
+        ctx->v32[w] = true;
+        ctx->v64[w] = false;
+        ctx->pr32 = true;
+        ctx->pr64 = false;
+    }
+    ctx->last_in = p;
+    ctx->cur = w;
+    ctx->counts_valid = true;
+    ctx->in_cell_order = true;
 }
 
 }  // namespace
@@ -571,7 +673,12 @@ int ctx_begin(const sph_constants *c, const sph_grid_params *g, const sph_geom_c
     // particle arrays (particle_gpu ctor, particle_gpu.cu:11-104) and the Green buffer
     for (int b = 0; b < 2; b++) {
         int r = alloc_sorted(ctx, ctx->buf[b], N);
+        if (!r && precision == SPH_PREC_FP32K) r = alloc_sorted32(ctx, ctx->c32[b], N);
         if (r) return r;
+    }
+    if (precision == SPH_PREC_FP32K) {
+        DALLOC(ctx->F32.p, N);
+        DALLOC(ctx->F32.R, N);
     }
     DALLOC(ctx->F.p, N); DALLOC(ctx->F.R, N); DALLOC(ctx->F.S_der, N); DALLOC(ctx->F.v_der, N); DALLOC(ctx->F.idx, N);
     const int nc = ctx->K.g.num_cell;
@@ -821,6 +928,7 @@ int sph_launch_count(const sph_ctx *ctx, int64_t *count) {
 
 int sph_get_particles(sph_ctx *ctx, sph_particles *dev_view) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     if (!dev_view) return SPH_ERR_INVALID;
     *dev_view = view_of(ctx);
     return SPH_OK;
@@ -828,6 +936,7 @@ int sph_get_particles(sph_ctx *ctx, sph_particles *dev_view) {
 
 int sph_upload_particles(sph_ctx *ctx, const sph_particles *host) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     if (!host || host->N != ctx->N) return fail(ctx, SPH_ERR_INVALID, "upload: particle count mismatch");
     sph_particles v = view_of(ctx);
     for (const FieldDesc &fd : kFields) {
@@ -845,6 +954,7 @@ int sph_upload_particles(sph_ctx *ctx, const sph_particles *host) {
 
 int sph_download_particles(sph_ctx *ctx, sph_particles *host) {
     REQUIRE_CTX();
+    REQUIRE_STATE(false);
     if (!host || host->N != ctx->N) return fail(ctx, SPH_ERR_INVALID, "download: particle count mismatch");
     sph_particles v = view_of(ctx);
     for (const FieldDesc &fd : kFields) {
@@ -892,6 +1002,8 @@ int sph_upload_particles_async(sph_ctx *ctx, const sph_particles *host) {
     CK(cudaEventRecord(ctx->ev_up[t], ctx->io_up));
     ctx->up_pending[t] = true;
     ctx->cur = t;
+    ctx->v64[t] = true;    // the next step reads the uploaded FP64 arrays
+    ctx->v32[t] = false;
     ctx->counts_valid = false;
     ctx->in_cell_order = false;
     return SPH_OK;
@@ -904,6 +1016,19 @@ int sph_download_particles_async(sph_ctx *ctx, sph_particles *host) {
     if (r) return r;
     const int src_b = ctx->cur;
     const bool fixed = host->p || host->R || host->S_der || host->v_der || host->idx;
+    if (ctx->K.precision == SPH_PREC_FP32K && (!ctx->v64[src_b] || (fixed && !ctx->pr64))) {
+        // the step left the state in the compact form: widen it into buf[src_b] on the
+        // compute stream, after the copies of buf[src_b] still in flight
+        r = wait_io(ctx, src_b);
+        if (r) return r;
+        launch_state_to64(ctx->stream, ctx->N, ctx->c32[src_b], ctx->F32, ctx->buf[src_b], ctx->F,
+                          !ctx->v64[src_b], fixed && !ctx->pr64);
+        ctx->launches++;
+        CK_LAUNCH();
+        ctx->v64[src_b] = true;
+        if (fixed) ctx->pr64 = true;
+        CK(cudaEventRecord(ctx->ev_used[src_b], ctx->stream));
+    }
     CK(cudaStreamWaitEvent(ctx->io_down, ctx->ev_used[src_b], 0));            // the step that wrote it
     if (fixed) {                                                              // p, R, ...: the last step
         CK(cudaEventRecord(ctx->ev_fixed, ctx->stream));
@@ -953,6 +1078,7 @@ int sph_update_geometry(sph_ctx *ctx) {
 
 int sph_assign_hashes(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     launch_hash(ctx->stream, ctx->N, CUR(ctx), ctx->K.g);
     ctx->launches += 1;
     ctx->counts_valid = false;
@@ -962,6 +1088,7 @@ int sph_assign_hashes(sph_ctx *ctx) {
 
 int sph_sort(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     const int N = ctx->N;
     launch_count(ctx->stream, N, CUR(ctx), ctx->X, ctx->K.g, ctx->W.status, false);
     launch_sort_rest(ctx->stream, N, ctx->X, ctx->K.g, ctx->F.idx, ctx->W.status);
@@ -981,6 +1108,7 @@ int sph_sort(sph_ctx *ctx) {
 // ---- leap frog --------------------------------------------------------------------------------
 int sph_init(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     launch_init(ctx->stream, ctx->N, CUR(ctx), ctx->W);
     ctx->launches++;
     CK_LAUNCH();
@@ -989,6 +1117,7 @@ int sph_init(sph_ctx *ctx) {
 
 int sph_predict(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     REQUIRE_SINGLE_CASE();
     launch_predict_correct(ctx->stream, ctx->N, CUR(ctx), ctx->W, 0.5 * ctx->K.dt);
     ctx->launches++;
@@ -999,6 +1128,7 @@ int sph_predict(sph_ctx *ctx) {
 
 int sph_correct(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     REQUIRE_SINGLE_CASE();
     launch_predict_correct(ctx->stream, ctx->N, CUR(ctx), ctx->W, ctx->K.dt);
     ctx->launches++;
@@ -1011,6 +1141,7 @@ int sph_correct(sph_ctx *ctx) {
 #define STAGE(name, call)                 \
     int name(sph_ctx *ctx) {              \
         REQUIRE_CTX();                    \
+        REQUIRE_STATE(true);              \
         call;                             \
         ctx->launches++;                  \
         ctx->counts_valid = false;        \
@@ -1029,6 +1160,7 @@ STAGE(sph_debug_invalidate, launch_invalidate(ctx->stream, ctx->N, CUR(ctx), ctx
 
 int sph_perform_boundary_conditions_thermal(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     if (ctx->K.c.trml_tool.alpha == 0.) return SPH_OK;   // m_thermal off (actions_gpu.cu:881-886)
     launch_bc_thermal(ctx->stream, ctx->N, ctx->K, CUR(ctx));
     ctx->launches++;
@@ -1039,6 +1171,7 @@ int sph_perform_boundary_conditions_thermal(sph_ctx *ctx) {
 
 int sph_plasticity_johnson_cook(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     REQUIRE_SINGLE_CASE();
     if (!ctx->K.c.plastic) return SPH_OK;   // m_plastic off (actions_gpu.cu:874-879)
     launch_plasticity(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->F, ctx->W);
@@ -1050,6 +1183,7 @@ int sph_plasticity_johnson_cook(sph_ctx *ctx) {
 
 int sph_interactions_monaghan(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     REQUIRE_SINGLE_CASE();
     launch_build_records(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->F, ctx->W);
     launch_interactions(ctx->stream, ctx->N, ctx->K, ctx->X.offsets, CUR(ctx), ctx->F, ctx->W, ctx->seg,
@@ -1063,6 +1197,7 @@ int sph_interactions_monaghan(sph_ctx *ctx) {
 // ---- tool -------------------------------------------------------------------------------------
 int sph_material_fric_heat_gen_fem(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     REQUIRE_SINGLE_CASE();
     REQUIRE_TOOL();
     SegDev sw = ctx->seg;
@@ -1076,6 +1211,7 @@ int sph_material_fric_heat_gen_fem(sph_ctx *ctx) {
 
 int sph_compute_contact_forces_fem(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     REQUIRE_SINGLE_CASE();
     REQUIRE_TOOL();
     launch_contact(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->W.status);
@@ -1266,14 +1402,17 @@ int sph_step(sph_ctx *ctx) {
     int r0 = wait_io(ctx, ctx->cur);
     if (r0 == SPH_OK) r0 = wait_io(ctx, w);
     if (r0) return r0;
-    if (!ctx->counts_valid) {
-        launch_count(s, ctx->N, CUR(ctx), ctx->X, ctx->K.g, ctx->W.status, true);
-        ctx->launches += 1;
-        CK_LAUNCH();
+    {
+        int rc = count_current(ctx);
+        if (rc) return rc;
     }
     const int p = ctx->cur;
+    const bool f32 = ctx->K.precision == SPH_PREC_FP32K;
+    const int src32 = f32 && ctx->v32[p] ? 1 : 0, pr32 = f32 && ctx->pr32 ? 1 : 0;
+    cudaGraphExec_t &gexec = ctx->graph[p][w][src32][pr32];
+    int64_t &glaunch = ctx->graph_launches[p][w][src32][pr32];
     if (ctx->use_graph) {
-        if (!ctx->graph[p][w]) {
+        if (!gexec) {
             cudaGraph_t g = nullptr;
             CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
             int64_t n = 0;
@@ -1284,13 +1423,13 @@ int sph_step(sph_ctx *ctx) {
                 return r;
             }
             if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
-            e = cudaGraphInstantiate(&ctx->graph[p][w], g, 0);
+            e = cudaGraphInstantiate(&gexec, g, 0);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) return fail(ctx, SPH_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e));
-            ctx->graph_launches[p][w] = n;
+            glaunch = n;
         }
-        CK(cudaGraphLaunch(ctx->graph[p][w], s));
-        ctx->launches += ctx->graph_launches[p][w];
+        CK(cudaGraphLaunch(gexec, s));
+        ctx->launches += glaunch;
     } else {
         int64_t n = 0;
         int r = issue_fused_body(ctx, n, w);
@@ -1299,10 +1438,7 @@ int sph_step(sph_ctx *ctx) {
     }
     int r1 = mark_used(ctx, p, w);
     if (r1) return r1;
-    ctx->last_in = p;
-    ctx->cur = w;
-    ctx->counts_valid = true;
-    ctx->in_cell_order = true;
+    finish_step(ctx, p, w);
     return SPH_OK;
 }
 
@@ -1312,7 +1448,6 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
     if (!stage_ms || nsteps < 1) return SPH_ERR_INVALID;
     if (n_stages) *n_stages = kStages;
     cudaStream_t s = ctx->stream;
-    const int N = ctx->N;
     cudaEvent_t ev[kStages + 1];
     for (auto &e : ev) CK(cudaEventCreate(&e));
     for (int k = 0; k < kStages; k++) stage_ms[k] = 0.f;
@@ -1324,50 +1459,14 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
             for (auto &e : ev) cudaEventDestroy(e);
             return r0;
         }
-        SortedFields &A = ctx->buf[ctx->cur];
-        SortedFields &B = ctx->buf[w];
         CK(cudaEventRecord(ev[0], s));
-        if (!ctx->counts_valid) {
-            launch_count(s, N, A, ctx->X, ctx->K.g, ctx->W.status, true);
-            ctx->launches++;
-        }
+        int r1 = count_current(ctx);
+        if (r1) return r1;
         CK(cudaEventRecord(ev[1], s));
-        launch_sort_rest(s, N, ctx->X, ctx->K.g, ctx->F.idx, ctx->W.status);
-        CK(cudaEventRecord(ev[2], s));
-        launch_gather_fused(s, N, ctx->F.idx, ctx->K, A, B, ctx->F, ctx->W, ctx->X.hash_next, ctx->tool_dev);
-        CK(cudaEventRecord(ev[3], s));
-        if (ctx->has_tool) launch_fem_half(s, ctx->K, ctx->fem, ctx->tool_dev);
-        if (pse_active(ctx)) launch_heat_pse(s, N, ctx->K, ctx->X.offsets, ctx->W, B);
-        CK(cudaEventRecord(ev[4], s));
-        SegDev sw = ctx->seg;
-        if (ctx->wear_mode != SPH_WEAR_OFF) {
-            launch_wear_reset(s, ctx->seg);
-            sw.wear.T_nodes = ctx->fem.T_half;
-        }
-        if (ctx->mlp_on) CK(cudaMemsetAsync(ctx->jc_list_count, 0, sizeof(int32_t), s));
-        launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, sw, ctx->tool_dev, true,
-                            ctx->interact_variant);
-        if (ctx->mlp_on) {
-            launch_jc_warm(s, jc_warm_grid(ctx), ctx->K, B, ctx->F, ctx->tool_dev, ctx->mlp, ctx->W.secant_iters,
-                           ctx->W.status);
-            ctx->launches++;
-        }
-        CK(cudaEventRecord(ev[5], s));
-        if (ctx->has_tool) {
-            launch_fem_rate_update(s, ctx->K, ctx->fem, ctx->seg, ctx->tool_dev);
-            if (ctx->wear_mode == SPH_WEAR_SHIFT) {
-                launch_wear_adjustment(s, ctx->K, ctx->fem, ctx->seg, ctx->wear, ctx->tool_dev, ctx->K.dt);
-                ctx->launches += 6;
-            }
-            launch_tool_move(s, ctx->K, ctx->seg, ctx->fem, ctx->tool_dev, ctx->K.dt, 3, true);
-        }
-        if (ctx->K.rigid) launch_rigid_move(s, ctx->K.rigid, ctx->K.dt);
-        CK(cudaEventRecord(ev[6], s));
-        CK(cudaMemsetAsync(ctx->X.counts, 0, sizeof(int32_t) * (size_t)(ctx->K.g.num_cell + 1), s));
-        launch_step_tail(s, N, ctx->K, B, ctx->seg, ctx->tool_dev, ctx->fem.T, ctx->X, ctx->W.status, true);
-        CK(cudaEventRecord(ev[7], s));
-        CK_LAUNCH();
-        ctx->launches += 8 + (ctx->has_tool ? 5 : 0) + (pse_active(ctx) ? 1 : 0) + (ctx->K.rigid ? 1 : 0);
+        int64_t n = 0;
+        r1 = issue_fused_body(ctx, n, w, ev + 2);
+        if (r1) return r1;
+        ctx->launches += n;
         CK(cudaEventSynchronize(ev[7]));
         for (int k = 0; k < kStages; k++) {
             float ms = 0.f;
@@ -1376,10 +1475,7 @@ int sph_profile_steps(sph_ctx *ctx, int32_t nsteps, float *stage_ms, int32_t *n_
         }
         int rm = mark_used(ctx, ctx->cur, w);
         if (rm) return rm;
-        ctx->last_in = ctx->cur;
-        ctx->cur = w;
-        ctx->counts_valid = true;
-        ctx->in_cell_order = true;
+        finish_step(ctx, ctx->cur, w);
     }
     for (auto &e : ev) cudaEventDestroy(e);
     return SPH_OK;
@@ -1396,6 +1492,7 @@ int sph_run(sph_ctx *ctx, int32_t nsteps) {
 
 int sph_step_staged(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     REQUIRE_SINGLE_CASE();
     int r;
 #define RUN(x)            \
@@ -1445,6 +1542,7 @@ int sph_step_staged(sph_ctx *ctx) {
 
 // ---- measurement hooks --------------------------------------------------------------------------
 static int reduce_force_T(sph_ctx *ctx, double out[3]) {
+    REQUIRE_STATE(false);
     launch_reduce_force_T(ctx->stream, ctx->N, CUR(ctx), ctx->W.reduce);
     ctx->launches++;
     CK_LAUNCH();
@@ -1680,6 +1778,7 @@ int sph_batch_case_info(const sph_ctx *ctx, int32_t k, int32_t *first, int32_t *
 
 int sph_batch_reduce(sph_ctx *ctx, double *out) {
     REQUIRE_CTX();
+    REQUIRE_STATE(false);
     if (!out) return SPH_ERR_INVALID;
     const int n = (int)ctx->case_first.size();
     launch_reduce_cases(ctx->stream, n, CUR(ctx), ctx->in_cell_order ? ctx->X.offsets : nullptr,
@@ -1693,6 +1792,7 @@ int sph_batch_reduce(sph_ctx *ctx, double *out) {
 
 int sph_batch_case_of_particles(sph_ctx *ctx, int32_t *case_of) {
     REQUIRE_CTX();
+    REQUIRE_STATE(false);
     if (!case_of) return SPH_ERR_INVALID;
     const int n = (int)ctx->case_first.size();
     if (!ctx->in_cell_order || n == 1) {
@@ -2006,6 +2106,7 @@ int sph_append_force_log(sph_ctx *ctx, const char *path) {
 int sph_eval_usui(sph_ctx *ctx, double K_usui, double alpha, const double tool_vel[2], double dt, double out[3],
                   double *accum_wear) {
     REQUIRE_CTX();
+    REQUIRE_STATE(false);
     if (!tool_vel || !out) return SPH_ERR_INVALID;
     const int nb = reduce_blocks();
     std::vector<double> h(4 * (size_t)nb);
@@ -2072,6 +2173,7 @@ int sph_get_rigid_tool(sph_ctx *ctx, sph_rigid_tool *tool) {
 // then the tool particles (update_tool_particles), by the context's time step.
 int sph_rigid_tool_update(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     if (!ctx->K.rigid) return fail(ctx, SPH_ERR_STATE, "context has no rigid tool");
     launch_rigid_move(ctx->stream, ctx->K.rigid, ctx->K.dt);
     launch_rigid_move_particles(ctx->stream, ctx->N, CUR(ctx), ctx->K.rigid, ctx->K.dt);
@@ -2084,6 +2186,7 @@ int sph_rigid_tool_update(sph_ctx *ctx) {
 // tool_gpu.cu:307-313 compute_contact_forces
 int sph_compute_contact_forces(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     if (!ctx->K.rigid) return fail(ctx, SPH_ERR_STATE, "context has no rigid tool");
     launch_contact_rigid(ctx->stream, ctx->N, ctx->K, CUR(ctx));
     ctx->launches++;
@@ -2095,6 +2198,7 @@ int sph_compute_contact_forces(sph_ctx *ctx) {
 // actions_gpu.cu:955-965 material_fric_heat_gen (off while thermals_wp.eta == 0)
 int sph_material_fric_heat_gen(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     if (!ctx->K.rigid) return fail(ctx, SPH_ERR_STATE, "context has no rigid tool");
     if (ctx->K.c.trml_wp.eta == 0.) return SPH_OK;
     launch_fric_heat_rigid(ctx->stream, ctx->N, ctx->K, CUR(ctx));
@@ -2126,6 +2230,7 @@ int sph_set_thermal_model(sph_ctx *ctx, int32_t model) {
 // interactions_gpu.cu:434-462 interactions_heat_pse on the current state
 int sph_interactions_heat_pse(sph_ctx *ctx) {
     REQUIRE_CTX();
+    REQUIRE_STATE(true);
     if (!ctx->K.thermal_pse) return fail(ctx, SPH_ERR_STATE, "thermal model is not PSE");
     if (ctx->K.c.trml_wp.alpha == 0.) return SPH_OK;
     launch_build_records(ctx->stream, ctx->N, ctx->K, CUR(ctx), ctx->F, ctx->W);

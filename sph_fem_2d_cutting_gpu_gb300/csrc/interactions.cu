@@ -25,6 +25,8 @@
 // (actions_gpu.cu:689-754).  Correct writes the start-of-step arrays in
 // place (only this thread touches them); neighbours read the predicted state
 // from the records, so there is no read/write race.
+#include <type_traits>
+
 #include "async.cuh"
 #include "launch.cuh"
 #include "rigid.cuh"
@@ -78,11 +80,13 @@ struct Acc32Fused {
 // A particle blanked before the step skips the neighbour sums, the corrector and
 // the return mapping, but the rigid tool's do_material_fric_heat_gen
 // (actions_gpu.cu:316-343) has no blanked test and still heats it.
-__device__ __forceinline__ void rigid_heat_blanked(int k, const KConsts &K, const SortedFields &B) {
+template <class SF>
+__device__ __forceinline__ void rigid_heat_blanked(int k, const KConsts &K, const SF &B) {
     if (!K.rigid || K.c.trml_wp.eta == 0. || flag_nonzero(B.tool_particle[k])) return;
-    double T = B.T[k];
-    rigid_fric_heat_one(K, K.dt, K.rigid->vel, B.vel[k], B.ft[k], B.n[k], T);
-    if (T != B.T[k]) B.T[k] = T;
+    const double T0 = B.T[k];
+    double T = T0;
+    rigid_fric_heat_one(K, K.dt, K.rigid->vel, d2(B.vel[k]), d2(B.ft[k]), d2(B.n[k]), T);
+    if (T != T0) put(B.T[k], T);
 }
 
 // ---- per-particle epilogue shared by both precisions (fused mode) ---------------------
@@ -158,11 +162,12 @@ __device__ __forceinline__ void fused_epilogue(int k, const KConsts &K, const So
     if (st) set_status(status, st);
 }
 
-// FP32-compensated epilogue: the rates (Jaumann, continuity, momentum,
-// advection) and the return mapping in FP32; the corrector keeps positions
-// and density in FP64.  vd, sd, vt, xt as in the FP64 epilogue.
-__device__ __forceinline__ void fused_epilogue32(int k, const KConsts &K, const SortedFields &B,
-                                                 const FixedFields &F, const SegDev &seg,
+// FP32-compensated epilogue on the compact FP32 state: the rates (Jaumann,
+// continuity, momentum, advection) and the return mapping in FP32; the
+// corrector keeps positions and density in FP64.  vd, sd, vt, xt as in the
+// FP64 epilogue.
+__device__ __forceinline__ void fused_epilogue32(int k, const KConsts &K, const SortedFields32 &B,
+                                                 const FixedFields32 &F, const SegDev &seg,
                                                  const ToolDev *__restrict__ tool, int32_t *__restrict__ secant_iters,
                                                  uint32_t *status, bool is_tool, float2 vel_pred, float rho_pred,
                                                  float4 vd, float4 sd, float2 vt, float2 xt, bool thermal, float T_t_new) {
@@ -170,79 +175,75 @@ __device__ __forceinline__ void fused_epilogue32(int k, const KConsts &K, const 
     const double dt = tc.dt;
     const float dtf = tc.dtf, hdtf = tc.hdtf;
     const float inv_mass = K.f.inv_mass;
-    const dbl4 S0d = B.S[k];
-    float4 S0 = make_float4((float)S0d.x, (float)S0d.y, (float)S0d.z, (float)S0d.w);
+    const float4 S0 = B.S[k];
     float4 St;
     float2 pos_t, vel_t;
-    double rho_t;
+    float rho_t;
     if (!is_tool) {
-        const dbl4 Sto = B.S_t[k];
-        float4 Sp = make_float4(fmaf(hdtf, (float)Sto.x, S0.x), fmaf(hdtf, (float)Sto.y, S0.y),
-                                fmaf(hdtf, (float)Sto.z, S0.z), fmaf(hdtf, (float)Sto.w, S0.w));
+        const float4 Sto = B.S_t[k];
+        float4 Sp = make_float4(fmaf(hdtf, Sto.x, S0.x), fmaf(hdtf, Sto.y, S0.y), fmaf(hdtf, Sto.z, S0.z),
+                                fmaf(hdtf, Sto.w, S0.w));
         St = jaumann_f32(K.f.G, vd, Sp);
-        rho_t = (double)(-rho_pred * (vd.x + vd.w));
-        const double2 fc = B.fc[k], ft = B.ft[k];
-        vel_t.x = vt.x + ((sd.x + sd.y) + ((float)fc.x + (float)ft.x) * inv_mass);
-        vel_t.y = vt.y + ((sd.z + sd.w) + ((float)fc.y + (float)ft.y) * inv_mass);
+        rho_t = -rho_pred * (vd.x + vd.w);
+        const float2 fc = B.fc[k], ft = B.ft[k];
+        vel_t.x = vt.x + ((sd.x + sd.y) + (fc.x + ft.x) * inv_mass);
+        vel_t.y = vt.y + ((sd.z + sd.w) + (fc.y + ft.y) * inv_mass);
         pos_t.x = xt.x + vel_pred.x;
         pos_t.y = xt.y + vel_pred.y;
-        B.S_t[k] = mk4(St.x, St.y, St.z, St.w);
+        B.S_t[k] = St;
         B.rho_t[k] = rho_t;
     } else {
-        const dbl4 Sto = B.S_t[k];
-        St = make_float4((float)Sto.x, (float)Sto.y, (float)Sto.z, (float)Sto.w);
+        St = B.S_t[k];
         rho_t = B.rho_t[k];
         if (K.thermal_pse) {   // PSE build: tool particles leave the sums unwritten
-            const double2 vto = B.vel_t[k], pto = B.pos_t[k];
-            vel_t = make_float2((float)vto.x, (float)vto.y);
-            pos_t = make_float2((float)pto.x, (float)pto.y);
+            vel_t = B.vel_t[k];
+            pos_t = B.pos_t[k];
         } else {
             vel_t = vt;
             pos_t = xt;
         }
     }
-    const float T_t = thermal ? T_t_new : (float)B.T_t[k];
-    const double2 pos_t_d = make_double2(pos_t.x, pos_t.y);
-    B.pos_t[k] = pos_t_d;
-    B.vel_t[k] = make_double2(vel_t.x, vel_t.y);
-    if (thermal) B.T_t[k] = (double)T_t;
+    const float T_t = thermal ? T_t_new : B.T_t[k];
+    B.pos_t[k] = pos_t;
+    B.vel_t[k] = vel_t;
+    if (thermal) B.T_t[k] = T_t;
     // corrector (leap_frog.cu:71-96)
     double2 pos = B.pos[k];
-    pos.x = pos.x + dt * pos_t_d.x;
-    pos.y = pos.y + dt * pos_t_d.y;
+    pos.x = pos.x + dt * (double)pos_t.x;
+    pos.y = pos.y + dt * (double)pos_t.y;
     B.pos[k] = pos;
-    const double2 v0 = B.vel[k];
-    const float2 vel = make_float2(fmaf(dtf, vel_t.x, (float)v0.x), fmaf(dtf, vel_t.y, (float)v0.y));
-    B.vel[k] = make_double2(vel.x, vel.y);
+    const float2 v0 = B.vel[k];
+    const float2 vel = make_float2(fmaf(dtf, vel_t.x, v0.x), fmaf(dtf, vel_t.y, v0.y));
+    B.vel[k] = vel;
     float4 S = make_float4(fmaf(dtf, St.x, S0.x), fmaf(dtf, St.y, S0.y), fmaf(dtf, St.z, S0.z), fmaf(dtf, St.w, S0.w));
-    const double rho = B.rho[k] + dt * rho_t;
+    const double rho = B.rho[k] + dt * (double)rho_t;
     B.rho[k] = rho;
-    float T = fmaf(dtf, T_t, (float)B.T[k]);
+    float T = fmaf(dtf, T_t, B.T[k]);
     uint32_t st = 0;
     bool blanked = false;
     if (K.has_tool) {   // friction heat (actions_gpu.cu:345-420) for particles in contact
         const int on = B.on_seg[k];
         if (on >= 0 && on < seg.n) {
             double Td = (double)T, bl = 0.;
-            st |= fric_heat_one(K, dt, tc.vel, make_double2(vel.x, vel.y), B.ft[k], B.n[k], B.fc[k], rho,
-                                B.eps_pl[k], on, seg.n, Td, bl, seg.fric_heat, seg.wear);
+            st |= fric_heat_one(K, dt, tc.vel, make_double2(vel.x, vel.y), d2(B.ft[k]), d2(B.n[k]), d2(B.fc[k]), rho,
+                                (double)B.eps_pl[k], on, seg.n, Td, bl, seg.fric_heat, seg.wear);
             T = (float)Td;
             blanked = flag_is_one(bl);
         }
     } else if (K.rigid && !is_tool && K.c.trml_wp.eta != 0.) {   // actions_gpu.cu:316-343
         double Td = (double)T;
-        rigid_fric_heat_one(K, dt, K.rigid->vel, make_double2(vel.x, vel.y), B.ft[k], B.n[k], Td);
+        rigid_fric_heat_one(K, dt, K.rigid->vel, make_double2(vel.x, vel.y), d2(B.ft[k]), d2(B.n[k]), Td);
         T = (float)Td;
     }
     if (K.c.plastic && !is_tool && !blanked) {   // return mapping (actions_gpu.cu:689-754)
         const JcF32 &j = K.f.jc;
-        float eps_pl = (float)B.eps_pl[k], eps_pl_dot = (float)B.eps_pl_dot[k];
+        float eps_pl = B.eps_pl[k], eps_pl_dot = B.eps_pl_dot[k];
         int it = 0;
         if (K.jc_list) {
             // learned warm start: the trial state is stored below and a yielding
             // particle finishes its return mapping in k_jc_warm
             JcTrial tr;
-            if (jc_trial_f32(j, S, (float)F.p[k], eps_pl, eps_pl_dot, T, tr)) {
+            if (jc_trial_f32(j, S, F.p[k], eps_pl, eps_pl_dot, T, tr)) {
                 const unsigned mask = __activemask();
                 const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
                 int base = 0;
@@ -250,19 +251,18 @@ __device__ __forceinline__ void fused_epilogue32(int k, const KConsts &K, const 
                 base = __shfl_sync(mask, base, leader);
                 K.jc_list[base + __popc(mask & ((1u << lane) - 1u))] = k;
             } else {
-                B.eps_pl_dot[k] = 0.;
+                B.eps_pl_dot[k] = 0.f;
             }
         } else {
-            st |= plasticity_f32(K, j, dtf, tc.inv_dtf, S, (float)F.p[k], (float)rho, eps_pl, eps_pl_dot, T,
-                                 blanked, &it);
-            B.eps_pl[k] = (double)eps_pl;
-            B.eps_pl_dot[k] = (double)eps_pl_dot;
+            st |= plasticity_f32(K, j, dtf, tc.inv_dtf, S, F.p[k], (float)rho, eps_pl, eps_pl_dot, T, blanked, &it);
+            B.eps_pl[k] = eps_pl;
+            B.eps_pl_dot[k] = eps_pl_dot;
         }
         if (secant_iters) secant_iters[k] = it;
     }
-    B.S[k] = mk4(S.x, S.y, S.z, S.w);
-    B.T[k] = (double)T;
-    if (blanked) B.blanked[k] = 1.;
+    B.S[k] = S;
+    B.T[k] = T;
+    if (blanked) B.blanked[k] = 1.f;
     if (st) set_status(status, st);
 }
 
@@ -423,8 +423,9 @@ struct StageHdr {
     int delta[2 * kMaxStencil + 1];   // shared slot minus global record index, per column
 };
 
+template <class SF>
 __device__ __forceinline__ void stage_issue(int N, int kB, const KConsts &K, const int32_t *__restrict__ offsets,
-                                            const float4 *__restrict__ rec, const SortedFields &B, int cap,
+                                            const float4 *__restrict__ rec, const SF &B, int cap,
                                             float4 *srec, StageHdr &h, uint32_t mbar) {
     const sph_geom_constants &g = K.g;
     const int R = g.stencil;
@@ -462,22 +463,22 @@ __device__ __forceinline__ void stage_issue(int N, int kB, const KConsts &K, con
 // the block lies in one grid column, the neighbour records of its stencil
 // (one contiguous run of rows per column).  Hints only: every range lies
 // inside its array.
+template <class SF, class FF>
 __device__ __forceinline__ void block_prefetch_l2(int N, int kB, const KConsts &K, const int32_t *__restrict__ offsets,
-                                                  const float4 *__restrict__ rec, const SortedFields &B,
-                                                  const FixedFields &F) {
+                                                  const float4 *__restrict__ rec, const SF &B, const FF &F) {
     const int b0 = blockIdx.x * kB;
     const uint32_t n = (uint32_t)min(kB, N - b0);
-    prefetch_l2_bulk(B.S + b0, n * 32u);
-    prefetch_l2_bulk(B.S_t + b0, n * 32u);
+    prefetch_l2_bulk(B.S + b0, n * (uint32_t)sizeof(B.S[0]));
+    prefetch_l2_bulk(B.S_t + b0, n * (uint32_t)sizeof(B.S_t[0]));
     prefetch_l2_bulk(B.pos + b0, n * 16u);
-    prefetch_l2_bulk(B.vel + b0, n * 16u);
-    prefetch_l2_bulk(B.fc + b0, n * 16u);
-    prefetch_l2_bulk(B.ft + b0, n * 16u);
+    prefetch_l2_bulk(B.vel + b0, n * (uint32_t)sizeof(B.vel[0]));
+    prefetch_l2_bulk(B.fc + b0, n * (uint32_t)sizeof(B.fc[0]));
+    prefetch_l2_bulk(B.ft + b0, n * (uint32_t)sizeof(B.ft[0]));
     prefetch_l2_bulk(B.rho + b0, n * 8u);
-    prefetch_l2_bulk(B.T + b0, n * 8u);
-    prefetch_l2_bulk(B.eps_pl + b0, n * 8u);
-    prefetch_l2_bulk(B.eps_pl_dot + b0, n * 8u);
-    prefetch_l2_bulk(F.p + b0, n * 8u);
+    prefetch_l2_bulk(B.T + b0, n * (uint32_t)sizeof(B.T[0]));
+    prefetch_l2_bulk(B.eps_pl + b0, n * (uint32_t)sizeof(B.eps_pl[0]));
+    prefetch_l2_bulk(B.eps_pl_dot + b0, n * (uint32_t)sizeof(B.eps_pl_dot[0]));
+    prefetch_l2_bulk(F.p + b0, n * (uint32_t)sizeof(F.p[0]));
     const sph_geom_constants &g = K.g;
     const int R = g.stencil;
     const int hf = B.hash[b0], hl = B.hash[b0 + (int)n - 1];
@@ -495,10 +496,18 @@ __device__ __forceinline__ void block_prefetch_l2(int N, int kB, const KConsts &
 // budget for the compiler): the launch shapes the autotuner chooses from.
 // kStaged: neighbour records from shared memory (dynamic: cap records + the
 // pair lists).
+// The fused form works on the compact FP32 state (SortedFields32 / FixedFields32);
+// the staged form (sph_interactions_monaghan) on the FP64 arrays.
+template <bool kFused>
+using Sorted32Of = std::conditional_t<kFused, SortedFields32, SortedFields>;
+template <bool kFused>
+using Fixed32Of = std::conditional_t<kFused, FixedFields32, FixedFields>;
+
 template <bool kFused, int kB = kBlock, int kMinB = 1, bool kStaged = false>
 __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, const int32_t *__restrict__ offsets,
-                                                       const float4 *__restrict__ rec, SortedFields B, FixedFields F,
-                                                       SegDev seg, const ToolDev *__restrict__ tool,
+                                                       const float4 *__restrict__ rec, Sorted32Of<kFused> B,
+                                                       Fixed32Of<kFused> F, SegDev seg,
+                                                       const ToolDev *__restrict__ tool,
                                                        int32_t *__restrict__ secant_iters, uint32_t *status,
                                                        int cap) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -755,21 +764,21 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
         // predicted velocity and density from this particle's record
         fused_epilogue32(k, K, B, F, seg, tool, secant_iters, status, tool_i, make_float2(vix, viy), rhoi, vd, sd,
                          make_float2(0.f, 0.f), xt, thermal, T_t);
-        return;
+    } else {
+        const float mass = K.f.mass;
+        const float xs = K.f.xs_mass;
+        const float4 vd = make_float4(vd0.s, vd1.s, vd2.s, vd3.s);
+        const float4 sd = make_float4(mass * sd0.s, mass * sd1.s, mass * sd2.s, mass * sd3.s);
+        const float2 vt = make_float2(-mass * vt0.s, -mass * vt1.s);
+        const float2 xt = make_float2(xs * xt0.s, xs * xt1.s);
+        const float T_t = thermal_alpha * (2.0f * tl.s);
+        if (pse_tool) return;
+        F.S_der[k] = mk4(sd.x, sd.y, sd.z, sd.w);
+        F.v_der[k] = mk4(vd.x, vd.y, vd.z, vd.w);
+        B.pos_t[k] = make_double2(xt.x, xt.y);
+        B.vel_t[k] = make_double2(vt.x, vt.y);
+        if (thermal) B.T_t[k] = (double)T_t;
     }
-    const float mass = K.f.mass;
-    const float xs = K.f.xs_mass;
-    const float4 vd = make_float4(vd0.s, vd1.s, vd2.s, vd3.s);
-    const float4 sd = make_float4(mass * sd0.s, mass * sd1.s, mass * sd2.s, mass * sd3.s);
-    const float2 vt = make_float2(-mass * vt0.s, -mass * vt1.s);
-    const float2 xt = make_float2(xs * xt0.s, xs * xt1.s);
-    const float T_t = thermal_alpha * (2.0f * tl.s);
-    if (pse_tool) return;
-    F.S_der[k] = mk4(sd.x, sd.y, sd.z, sd.w);
-    F.v_der[k] = mk4(vd.x, vd.y, vd.z, vd.w);
-    B.pos_t[k] = make_double2(xt.x, xt.y);
-    B.vel_t[k] = make_double2(vt.x, vt.y);
-    if (thermal) B.T_t[k] = (double)T_t;
 }
 
 // Launch shapes of the fused FP32K neighbour-sum kernel: (threads per block,
@@ -786,8 +795,8 @@ void interact_variant_shape(int v, int *block, int *min_blocks, int *staged) {
 }
 
 template <int kB, int kMinB, bool kStaged>
-static void launch_i32(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const SortedFields &B,
-                       const FixedFields &F, const StepScratch &W, const SegDev &seg, const ToolDev *tool, int cap) {
+static void launch_i32(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const SortedFields32 &B,
+                       const FixedFields32 &F, const StepScratch &W, const SegDev &seg, const ToolDev *tool, int cap) {
     size_t smem = 0;
     if (kStaged) {
         smem = (size_t)cap * 64 + sizeof(int) * kChunk32 * kB;
@@ -870,9 +879,10 @@ __global__ void __launch_bounds__(kB) k_heat_pse64(int N, KConsts K, const int32
 // FP32-compensated form of the PSE sum over the FP32 records: positions as
 // offsets from the cell corners (cells of edge h), the Gaussian with expf, the
 // sum Kahan-compensated; T_t written in FP64.
+template <class TT>   // T_t: double (staged call, FP64 arrays) or float (the compact state)
 __global__ void __launch_bounds__(kBlock) k_heat_pse32(int N, KConsts K, const int32_t *__restrict__ offsets,
                                                        const float4 *__restrict__ rec,
-                                                       const int32_t *__restrict__ hashes, double *__restrict__ T_t) {
+                                                       const int32_t *__restrict__ hashes, TT *__restrict__ T_t) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= N) return;
     const float4 i0 = rec[4 * k + 0];
@@ -908,6 +918,12 @@ __global__ void __launch_bounds__(kBlock) k_heat_pse32(int N, KConsts K, const i
 }
 
 void launch_heat_pse(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const StepScratch &W,
+                     const SortedFields32 &B) {
+    const int tb = fp64_block(N);
+    k_heat_pse32<<<div_up(N, tb), tb, 0, s>>>(N, K, offsets, W.rec32, B.hash, B.T_t);
+}
+
+void launch_heat_pse(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const StepScratch &W,
                      const SortedFields &B) {
     if (K.precision == SPH_PREC_FP32K) {
         const int tb = fp64_block(N);
@@ -922,27 +938,31 @@ void launch_heat_pse(cudaStream_t s, int N, const KConsts &K, const int32_t *off
     }
 }
 
+void launch_interactions32_fused(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets,
+                                 const SortedFields32 &B, const FixedFields32 &F, const StepScratch &W,
+                                 const SegDev &seg, const ToolDev *tool, int variant) {
+    switch (variant) {
+        case 1: launch_i32<64, 12, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+        case 2: launch_i32<64, 8, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+        case 3: launch_i32<128, 4, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+        case 4: launch_i32<256, 3, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+        case 5: launch_i32<256, 1, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+        case 6: launch_i32<128, 3, true>(s, N, K, offsets, B, F, W, seg, tool, 640); break;
+        case 7: launch_i32<128, 2, true>(s, N, K, offsets, B, F, W, seg, tool, 1024); break;
+        case 8: launch_i32<64, 6, true>(s, N, K, offsets, B, F, W, seg, tool, 384); break;
+        case 9: launch_i32<256, 2, true>(s, N, K, offsets, B, F, W, seg, tool, 1024); break;
+        default: launch_i32<128, 6, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
+    }
+}
+
 void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const SortedFields &B,
                          const FixedFields &F, const StepScratch &W, const SegDev &seg, const ToolDev *tool,
                          bool fused, int variant) {
     const int grid = div_up(N, kBlock);
     if (K.precision == SPH_PREC_FP32K) {
-        if (fused) {
-            switch (variant) {
-                case 1: launch_i32<64, 12, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
-                case 2: launch_i32<64, 8, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
-                case 3: launch_i32<128, 4, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
-                case 4: launch_i32<256, 3, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
-                case 5: launch_i32<256, 1, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
-                case 6: launch_i32<128, 3, true>(s, N, K, offsets, B, F, W, seg, tool, 640); break;
-                case 7: launch_i32<128, 2, true>(s, N, K, offsets, B, F, W, seg, tool, 1024); break;
-                case 8: launch_i32<64, 6, true>(s, N, K, offsets, B, F, W, seg, tool, 384); break;
-                case 9: launch_i32<256, 2, true>(s, N, K, offsets, B, F, W, seg, tool, 1024); break;
-                default: launch_i32<128, 6, false>(s, N, K, offsets, B, F, W, seg, tool, 0); break;
-            }
-        } else
-            k_interact32<false><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec32, B, F, seg, tool, W.secant_iters, W.status,
-                                                        0);
+        // the fused FP32K step runs on the compact state (launch_interactions32_fused)
+        k_interact32<false><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec32, B, F, seg, tool, W.secant_iters, W.status,
+                                                    0);
     } else {
         const int kb = fp64_block(N);
         const int g64 = div_up(N, kb);

@@ -11,6 +11,8 @@ namespace sphfem {
 void launch_hash(cudaStream_t s, int N, const SortedFields &A, sph_geom_constants g);
 void launch_count(cudaStream_t s, int N, const SortedFields &A, const SortScratch &X, sph_geom_constants g,
                   uint32_t *status, bool with_hash);
+void launch_count(cudaStream_t s, int N, const SortedFields32 &A, const SortScratch &X, sph_geom_constants g,
+                  uint32_t *status, bool with_hash);
 int scan_blocks(int num_cell);
 void launch_sort_rest(cudaStream_t s, int N, const SortScratch &X, sph_geom_constants g, int32_t *perm,
                       uint32_t *status);
@@ -20,13 +22,29 @@ void launch_gather_fused(cudaStream_t s, int N, const int32_t *perm, const KCons
                          const ToolDev *tool);
 void launch_build_records(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F,
                           const StepScratch &W);
+// FP32K fused reorder into the compact state B, from the FP64 state (A64) or the
+// compact one (A32, exactly one of the two non-null); the p, R that tool
+// particles keep come from F32 (pr32) or F
+void launch_gather_fused32(cudaStream_t s, int N, const int32_t *perm, const KConsts &K, const SortedFields *A64,
+                           const SortedFields32 *A32, bool pr32, const FixedFields &F, const FixedFields32 &F32,
+                           const SortedFields32 &B, int32_t *idx, const StepScratch &W, const int32_t *hash_src,
+                           const ToolDev *tool);
+// the compact state (state) and F32's p, R (pr) widened into the FP64 arrays
+void launch_state_to64(cudaStream_t s, int N, const SortedFields32 &A, const FixedFields32 &Fa, const SortedFields &B,
+                       const FixedFields &F, bool state, bool pr);
 
 // interactions.cu
 void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const SortedFields &B,
                          const FixedFields &F, const StepScratch &W, const SegDev &seg, const ToolDev *tool,
                          bool fused, int variant = 0);
+// the fused FP32K neighbour sums and epilogue on the compact state
+void launch_interactions32_fused(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets,
+                                 const SortedFields32 &B, const FixedFields32 &F, const StepScratch &W,
+                                 const SegDev &seg, const ToolDev *tool, int variant);
 void launch_heat_pse(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const StepScratch &W,
                      const SortedFields &B);
+void launch_heat_pse(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const StepScratch &W,
+                     const SortedFields32 &B);
 int interact_variant_count();
 int fp64_block(int N);   // threads per block of the FP64 per-particle kernels for N particles
 void interact_variant_shape(int v, int *block, int *min_blocks, int *staged);
@@ -54,6 +72,9 @@ void launch_bc_thermal(cudaStream_t s, int N, const KConsts &K, const SortedFiel
 void launch_invalidate(cudaStream_t s, int N, const SortedFields &A, uint32_t *status);
 // with the FEM tool: the segment y-bins and the contact pass (k_contact_fem) first (two more launches)
 void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const SegDev &seg,
+                      ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
+                      bool next_hash);
+void launch_step_tail(cudaStream_t s, int N, const KConsts &K, const SortedFields32 &A, const SegDev &seg,
                       ToolDev *tool, const double *T_nodes, const SortScratch &X, uint32_t *status,
                       bool next_hash);
 void launch_rigid_move(cudaStream_t s, sph_rigid_tool *t, double dt);
@@ -90,7 +111,7 @@ size_t mlp_train_smem();
 cudaError_t mlp_configure();
 void launch_mlp_predict(cudaStream_t s, const MlpDev &m, const float *x, int64_t n, float *y, uint32_t *status,
                         int grid);
-void launch_jc_warm(cudaStream_t s, int grid, const KConsts &K, const SortedFields &B, const FixedFields &F,
+void launch_jc_warm(cudaStream_t s, int grid, const KConsts &K, const SortedFields32 &B, const FixedFields32 &F,
                     const ToolDev *tool, const MlpDev &m, int32_t *secant_iters, uint32_t *status);
 void launch_mlp_grad(cudaStream_t s, int grid, const MlpDev &m, const float *x, const float *t, const int32_t *idx,
                      int64_t nb, float *part, uint32_t *status);

@@ -339,7 +339,7 @@ __device__ __forceinline__ void jc_features(const JcF32 &j, float svm, float eps
 }
 
 __global__ void __launch_bounds__(kTile, 1)
-    k_jc_warm(KConsts K, SortedFields B, FixedFields F, const ToolDev *__restrict__ tool, MlpDev m,
+    k_jc_warm(KConsts K, SortedFields32 B, FixedFields32 F, const ToolDev *__restrict__ tool, MlpDev m,
               int32_t *__restrict__ secant_iters, uint32_t *status) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     FwdSmem &sh = *(FwdSmem *)smem_raw;
@@ -359,13 +359,12 @@ __global__ void __launch_bounds__(kTile, 1)
         JcTrial tr{1.f, 1.f, 1.f};
         float x[kMlpIn] = {0.f, 0.f, 0.f, 0.f}, xn[kMlpIn];
         if (valid) {
-            const dbl4 Sd = B.S[k];
-            S = make_float4((float)Sd.x, (float)Sd.y, (float)Sd.z, (float)Sd.w);
-            p = (float)F.p[k];
+            S = B.S[k];
+            p = F.p[k];
             rho = (float)B.rho[k];
-            eps = (float)B.eps_pl[k];
-            epsd = (float)B.eps_pl_dot[k];
-            T = (float)B.T[k];
+            eps = B.eps_pl[k];
+            epsd = B.eps_pl_dot[k];
+            T = B.T[k];
             jc_trial_f32(j, S, p, eps, epsd, T, tr);
             jc_features(j, tr.svm, eps, epsd, T, x);
         }
@@ -385,11 +384,11 @@ __global__ void __launch_bounds__(kTile, 1)
         int it = 0;
         bool blanked = false;
         uint32_t st = jc_return_f32(K, j, tc.dtf, tc.inv_dtf, S, rho, eps, epsd, T, blanked, &it, tr, dl0);
-        B.S[k] = mk4(S.x, S.y, S.z, S.w);
-        B.T[k] = (double)T;
-        B.eps_pl[k] = (double)eps;
-        B.eps_pl_dot[k] = (double)epsd;
-        if (blanked) B.blanked[k] = 1.;
+        B.S[k] = S;
+        B.T[k] = T;
+        B.eps_pl[k] = eps;
+        B.eps_pl_dot[k] = epsd;
+        if (blanked) B.blanked[k] = 1.f;
         if (secant_iters) secant_iters[k] = it;
         if (st) set_status(status, st);
     }
@@ -694,7 +693,7 @@ void launch_mlp_predict(cudaStream_t s, const MlpDev &m, const float *x, int64_t
     k_mlp_predict<<<grid, kTile, sizeof(FwdSmem), s>>>(m, x, n, y, status);
 }
 
-void launch_jc_warm(cudaStream_t s, int grid, const KConsts &K, const SortedFields &B, const FixedFields &F,
+void launch_jc_warm(cudaStream_t s, int grid, const KConsts &K, const SortedFields32 &B, const FixedFields32 &F,
                     const ToolDev *tool, const MlpDev &m, int32_t *secant_iters, uint32_t *status) {
     k_jc_warm<<<grid, kTile, sizeof(FwdSmem), s>>>(K, B, F, tool, m, secant_iters, status);
 }

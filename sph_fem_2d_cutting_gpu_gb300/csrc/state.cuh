@@ -18,6 +18,27 @@ struct SortedFields {
     int32_t *hash;
 };
 
+// The same fields in the compact form of FP32K contexts: positions and density
+// in FP64 (the corrector's x + dt*x_t and rho + dt*rho_t, where FP32 would lose
+// the small increments), everything else in FP32; the 0/1 flags as floats.
+// 148 bytes per particle instead of 284.  Every value the FP32K step computes
+// for these fields is an FP32 value already, so storing them in FP32 changes
+// no result of the step except the contact forces and normals, which the
+// contact search still computes in FP64 and now rounds once to FP32.
+struct SortedFields32 {
+    double2 *pos;
+    float2 *vel, *fc, *ft, *n;
+    float *h;
+    double *rho;
+    float *eps_pl, *eps_pl_dot, *T, *fixed, *blanked, *tool_particle;
+    float4 *S;
+    float2 *pos_t, *vel_t;
+    float *rho_t, *T_t;
+    float4 *S_t;
+    int32_t *on_seg;
+    int32_t *hash;
+};
+
 // Arrays that are not reordered by the sort (particle_gpu fields the Green
 // buffer does not carry: p, R, S_der, v_der, idx).
 struct FixedFields {
@@ -25,6 +46,12 @@ struct FixedFields {
     dbl4 *R;
     dbl4 *S_der, *v_der;
     int32_t *idx;
+};
+
+// p and R of the FP32K step (R.w unused); S_der, v_der and idx stay in FixedFields.
+struct FixedFields32 {
+    float *p;
+    float4 *R;
 };
 
 // Scratch of the counting sort.
