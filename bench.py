@@ -206,7 +206,111 @@ def run_reference(args):
     return 0
 
 
-def run_batched(args, local, max_over_ranks, barrier):
+def stream_of(obj, local):
+    """The library stream of a context, as a torch stream (for CUDA events on it)."""
+    import ctypes as C
+
+    import torch
+    stream_ptr = C.c_void_p()
+    obj.lib.sph_get_stream(obj.ctx, C.byref(stream_ptr))
+    return torch.cuda.ExternalStream(stream_ptr.value, device=torch.device("cuda", local))
+
+
+def time_batch(b, local, warmup, steps):
+    """Device ms per step of `steps` fused steps of a batch (CUDA events on its stream)."""
+    import torch
+    ext = stream_of(b, local)
+    b.step(warmup)
+    b.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    b.step(steps)
+    e1.record(ext)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps, ext
+
+
+def run_sweep_full(args, local, cases, variant, mlp):
+    """The batched sweep at its stated length: all cases for `sweep_steps` steps
+    in FP32K (force and peak temperature of every case every `sweep_every`
+    steps, status after the run), three of them (smallest, median, largest) run
+    alone in plain FP64 as the reference of their error curves; then the same
+    batch timed in plain FP64 and in FP32K with the learned warm start."""
+    import numpy as np
+    import torch
+
+    from sph_fem_2d_cutting_gpu_gb300 import abi, tune
+    from sph_fem_2d_cutting_gpu_gb300.solver import Batch, Solver
+
+    steps, every = args.sweep_steps, args.sweep_every
+    b = Batch(cases, abi.SPH_PREC_FP32K, device=local)
+    if variant is not None:
+        tune.set_variant(b, variant)
+    ext = stream_of(b, local)
+    hist, ms = [], 0.0
+    for _ in range(steps // every):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        b.step(every)
+        e1.record(ext)
+        e1.synchronize()
+        ms += e0.elapsed_time(e1)
+        hist.append(b.reduce())
+    status = b.status()
+    b.close()
+    torch.cuda.empty_cache()
+    H = np.stack(hist)                    # [checkpoints, cases, 3]
+    order = sorted(range(len(cases)), key=lambda k: cases[k].N)
+    picks = {"smallest": order[0], "median": order[len(order) // 2], "largest": order[-1]}
+    per_case = {}
+    for label, k in picks.items():
+        s = Solver(cases[k], abi.SPH_PREC_FP64, device=local, place_tool=False)
+        h64 = []
+        for _ in range(steps // every):
+            s.step(every)
+            h64.append((*s.reduce_force(), s.max_T()))
+        st64 = s.status()
+        s.close()
+        errs = curve_errors(h64, [tuple(H[c, k]) for c in range(len(h64))])
+        per_case[label] = dict(case=k, particles=cases[k].N, fem_nodes=cases[k].info["nodes"],
+                               speed_mpmin=cases[k].info.get("speed_mpmin"), status_fp64=st64,
+                               peak_force_fp64=float(max(np.hypot(h[0], h[1]) for h in h64)),
+                               T_rise_fp64=float(max(h[2] for h in h64) - 300.0), **errs,
+                               curve_fp64=[list(map(float, h)) for h in h64],
+                               curve_batched=[list(map(float, H[c, k])) for c in range(len(h64))])
+        torch.cuda.empty_cache()
+    n_total = sum(c.N for c in cases)
+    out = {"steps": steps, "every": every, "status": status, "ms_per_step": ms / steps,
+           "value": n_total / (ms / steps * 1e-3), "unit": UNIT,
+           "peak_T_max": float(H[:, :, 2].max()), "peak_T_rise_max": float(H[:, :, 2].max() - 300.0),
+           "reference_runs": per_case,
+           "max_errors_vs_fp64": {"force_err_of_peak": max(v["force_err_of_peak"] for v in per_case.values()),
+                                  "peak_T_err_of_rise": max(v["peak_T_err_of_rise"] for v in per_case.values())}}
+    # the same batch in plain FP64, and in FP32K with the learned warm start
+    forms = {}
+    b = Batch(cases, abi.SPH_PREC_FP64, device=local)
+    ms64, _ = time_batch(b, local, args.warmup, max(3, args.steps // 2))
+    forms["fp64"] = {"ms_per_step": ms64, "value": n_total / (ms64 * 1e-3), "status": b.status()}
+    b.close()
+    torch.cuda.empty_cache()
+    if mlp is not None:
+        b = Batch(cases, abi.SPH_PREC_FP32K, device=local)
+        if variant is not None:
+            tune.set_variant(b, variant)
+        msp, _ = time_batch(b, local, args.warmup, args.steps)
+        b.attach_mlp(mlp)
+        msm, _ = time_batch(b, local, args.warmup, args.steps)
+        forms["fp32k"] = {"ms_per_step": msp, "value": n_total / (msp * 1e-3)}
+        forms["fp32k_mlp"] = {"ms_per_step": msm, "value": n_total / (msm * 1e-3), "status": b.status()}
+        forms["speedup_fp32k_mlp_vs_fp64"] = ms64 / msm
+        forms["speedup_fp32k_vs_fp64"] = ms64 / msp
+        b.close()
+        torch.cuda.empty_cache()
+    out["forms"] = forms
+    return out
+
+
+def run_batched(args, local, max_over_ranks, barrier, mlp=None):
     """The batched sweep: independent AISI 1045 cuts of uneven sizes advanced
     by one fused, graph-replayed step over all cases (FP32-compensated)."""
     import ctypes as C
@@ -260,6 +364,9 @@ def run_batched(args, local, max_over_ranks, barrier):
                        "speed U(30,300) m/min, uncut chip U(20,150) um, rake U(-10,15) deg, own FEM tool each; "
                        "one fused step over all cases, CUDA-graph replay"}
     b.close()
+    torch.cuda.empty_cache()
+    if args.sweep_steps > 0:
+        out["sweep_run"] = run_sweep_full(args, local, cases, None if tuned is None else tuned["variant"], mlp)
     return out
 
 
@@ -388,47 +495,71 @@ def run_rigid(args, local):
                         "with thermal tool particles, 1.25e-3 cm/us; ny rows (30: the reference's size)"}
 
 
-def run_accuracy(case, mlp, steps, every, local):
-    """Cutting force (sum of fc + ft) and peak temperature of the FP32K form, with
-    and without the warm start, against the plain FP64 form over `steps` steps of
-    the same run (checkpoints every `every` steps).  The FP64 form is the oracle
-    here: it matches the CPU restatement of the reference to 1e-10 per step."""
+def curve_run(s, steps, every, ext, log_records=0):
+    """Advance `s` by `steps` fused steps in chunks of `every`, recording the
+    cutting force (sum of fc + ft) and the peak temperature after each chunk.
+    Device time is taken with CUDA events around the chunks (the reductions
+    between chunks are outside it).  With log_records, return mappings are
+    logged until that many states are held; those chunks are timed apart."""
+    import torch
+
+    hist, ms_run, ms_log, n_run, n_log = [], 0.0, 0.0, 0, 0
+    logging = log_records > 0
+    if logging:
+        s.jc_log_enable(log_records)
+    s.jc_stats(True, reset=True)
+    rec = None
+    for _ in range(steps // every):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        s.step(every)
+        e1.record(ext)
+        e1.synchronize()
+        if logging:
+            ms_log += e0.elapsed_time(e1)
+            n_log += every
+            if s.jc_log_read(0)[1] >= log_records:
+                rec = s.jc_log_read()
+                s.jc_log_enable(0)
+                logging = False
+        else:
+            ms_run += e0.elapsed_time(e1)
+            n_run += every
+        F = s.reduce_force()
+        hist.append((float(F[0]), float(F[1]), s.max_T()))
+    if logging:
+        rec = s.jc_log_read()
+        s.jc_log_enable(0)
+    calls, iters = s.jc_stats(True, reset=True)
+    # a run that logged throughout has only its logging chunks to time
+    return dict(hist=hist, ms_per_step=(ms_run / n_run) if n_run else ms_log / max(n_log, 1),
+                ms_per_step_logging=(ms_log / n_log) if n_log else None, steps_logging=n_log,
+                returns=calls, iters_per_return=iters / max(calls, 1), status=s.status()), rec
+
+
+def curve_errors(ref, other):
+    """Force error relative to the reference run's peak force, peak-temperature
+    error relative to its rise above 300 K, over all checkpoints."""
     import numpy as np
-
-    from sph_fem_2d_cutting_gpu_gb300 import abi
-    from sph_fem_2d_cutting_gpu_gb300.solver import Solver
-
-    hist = {}
-    for name, prec, net in (("fp64", abi.SPH_PREC_FP64, None), ("fp32k", abi.SPH_PREC_FP32K, None),
-                            ("fp32k_mlp", abi.SPH_PREC_FP32K, mlp)):
-        s = Solver(case, prec, device=local, place_tool=False)
-        if net is not None:
-            s.attach_mlp(net)
-        h = []
-        for _ in range(steps // every):
-            s.step(every)
-            h.append((s.reduce_force(), s.max_T()))
-        hist[name] = h
-        s.close()
-    F0 = np.array([f for f, _ in hist["fp64"]])
-    T0 = np.array([t for _, t in hist["fp64"]])
+    F0 = np.array([h[:2] for h in ref])
+    T0 = np.array([h[2] for h in ref])
+    F = np.array([h[:2] for h in other])
+    T = np.array([h[2] for h in other])
     fmax = float(np.linalg.norm(F0, axis=1).max())
     rise = max(float(T0.max()) - 300.0, 1.0)
-    out = {"steps": steps, "every": every, "peak_force_fp64": fmax, "peak_T_fp64": float(T0.max())}
-    for name in ("fp32k", "fp32k_mlp"):
-        F = np.array([f for f, _ in hist[name]])
-        T = np.array([t for _, t in hist[name]])
-        out[name] = {"force_err_of_peak": float(np.linalg.norm(F - F0, axis=1).max() / fmax),
-                     "peak_T_err_of_rise": float(np.abs(T - T0).max() / rise)}
-    return out
+    return {"force_err_of_peak": float(np.linalg.norm(F - F0, axis=1).max() / max(fmax, 1e-300)),
+            "peak_T_err_of_rise": float(np.abs(T - T0).max() / rise)}
 
 
-def run_learned(args, local):
-    """The learned warm start on the AISI 1045 cut (640,000 particles, tool of
-    about 13,000 nodes, edge placement): log the plain FP32K return mappings
-    until `learned_records` states, train the MLP on 90 % of them, score it on
-    the held-out 10 %, then time the plain and the warm-started FP32K step and
-    the plain FP64 step from the logged state."""
+def run_config3(args, local):
+    """The AISI 1045 cut at its stated size and length (640,000 particles, tool
+    of about 20,000 nodes, 20,000 steps): the plain FP64 form, the FP32K form
+    (logging its return mappings until `learned_records` states), then the MLP
+    trained on the logged states (90 %, scored on the held-out 10 %) and the
+    FP32K + MLP form, each over the whole run from the same start.  Cutting
+    force and peak temperature every `config3_every` steps; the FP64 form is the
+    reference of the error curves (it matches the CPU restatement of the
+    reference to 1e-10 per step)."""
     import ctypes as C
 
     import numpy as np
@@ -437,34 +568,24 @@ def run_learned(args, local):
     from sph_fem_2d_cutting_gpu_gb300 import abi, learned, setups
     from sph_fem_2d_cutting_gpu_gb300.solver import Solver
 
-    def timed(s, steps):
+    def solver(prec):
+        s = Solver(case, prec, device=local, place_tool=False)
         stream_ptr = C.c_void_p()
         s.lib.sph_get_stream(s.ctx, C.byref(stream_ptr))
-        ext = torch.cuda.ExternalStream(stream_ptr.value, device=torch.device("cuda", local))
-        s.step(args.warmup)
-        s.sync()
-        s.jc_stats(True, reset=True)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(ext)
-        s.step(steps)
-        e1.record(ext)
-        e1.synchronize()
-        calls, iters = s.jc_stats(True, reset=True)
-        return e0.elapsed_time(e1) / steps, calls, iters
+        return s, torch.cuda.ExternalStream(stream_ptr.value, device=torch.device("cuda", local))
 
-    case = setups.placed(setups.aisi1045_cut(), mode="edge")
-    s = Solver(case, abi.SPH_PREC_FP32K, device=local, place_tool=False)
-    s.jc_log_enable(args.learned_records)
+    steps, every = args.config3_steps, args.config3_every
+    case = setups.placed(setups.aisi1045_cut(steps=steps), mode="edge")
+    runs = {}
+    s, ext = solver(abi.SPH_PREC_FP64)
+    runs["fp64"], _ = curve_run(s, steps, every, ext)
+    s.close()
+    torch.cuda.empty_cache()
+    s, ext = solver(abi.SPH_PREC_FP32K)
     t0 = time.perf_counter()
-    logged = 0
-    while logged < args.learned_max_steps:
-        s.step(500)
-        logged += 500
-        if s.jc_log_read(0)[1] >= args.learned_records:
-            break
-    rec, offered = s.jc_log_read()
-    log_s = time.perf_counter() - t0
-    s.jc_log_enable(0)
+    runs["fp32k"], logged = curve_run(s, steps, every, ext, log_records=args.learned_records)
+    s.close()
+    rec, offered = logged
     n_logged = len(rec)
     rec = learned.valid_records(rec)
     x, t = learned.features(rec, case.constants)
@@ -484,35 +605,35 @@ def run_learned(args, local):
                         np.float32(1e-8))
     err_mlp = np.abs(dl_mlp - dl_true) / dl_true
     err_ref = np.abs(dl_ref - dl_true) / dl_true
-    # timed windows from the logged state: plain FP32K, warm-started FP32K
-    ms_plain, c_plain, it_plain = timed(s, args.steps)
+    s, ext = solver(abi.SPH_PREC_FP32K)
     s.attach_mlp(m)
-    ms_warm, c_warm, it_warm = timed(s, args.steps)
-    F32, T32 = s.reduce_force(), s.max_T()
-    P = s.download()
-    fem_T = s.fem()
-    steps_done = logged + 2 * (args.warmup + args.steps)
+    runs["fp32k_mlp"], _ = curve_run(s, steps, every, ext)
     s.close()
-    # plain FP64 from the same state (tool translated by the distance it moved)
-    c64 = setups.moved(case, case.tool_speed * case.dt * steps_done)
-    s64 = Solver(c64, abi.SPH_PREC_FP64, device=local, place_tool=False)
-    s64.upload(P)
-    s64.upload_fem_state(T=fem_T["T"], k=fem_T["k"])
-    ms_64, c_64, it_64 = timed(s64, args.steps)
-    s64.close()
     torch.cuda.empty_cache()
-    accuracy = None
-    if args.accuracy_steps > 0:
-        accuracy = run_accuracy(case, m, args.accuracy_steps, args.accuracy_every, local)
-    m.close()
-    torch.cuda.empty_cache()
-    return {
-        "accuracy_vs_fp64": accuracy,
-        "workload": "AISI 1045 cut 1600x400 (640,000 particles), tool of "
-                    f"{case.info['nodes']} nodes, rake -6 deg, 120 m/min, edge placement",
+    ms64 = runs["fp64"]["ms_per_step"]
+    curve = [{"step": (k + 1) * every, **{f"{n}": {"force": list(r["hist"][k][:2]), "peak_T": r["hist"][k][2]}
+                                         for n, r in runs.items()}} for k in range(steps // every)]
+    T64 = [h[2] for h in runs["fp64"]["hist"]]
+    config3 = {
+        "workload": f"AISI 1045 cut 1600x400 ({case.N} particles), tool of {case.info['nodes']} nodes (rake -6 deg, "
+                    f"clearance 5 deg, edge radius 20 um), 120 m/min, uncut chip 100 um, edge placement, "
+                    f"{steps} steps of dt {case.dt:.4g} us",
+        "steps": steps, "every": every, "particles": case.N, "tool_nodes": case.info["nodes"],
+        "peak_T_fp64": float(max(T64)), "T_rise_fp64": float(max(T64) - 300.0),
+        "peak_force_fp64": float(max(np.hypot(h[0], h[1]) for h in runs["fp64"]["hist"])),
+        "errors_vs_fp64": {n: curve_errors(runs["fp64"]["hist"], runs[n]["hist"]) for n in ("fp32k", "fp32k_mlp")},
+        "ms_per_step": {n: r["ms_per_step"] for n, r in runs.items()},
+        "iters_per_return": {n: r["iters_per_return"] for n, r in runs.items()},
+        "status": {n: r["status"] for n, r in runs.items()},
+        "speedup_vs_fp64": {n: ms64 / runs[n]["ms_per_step"] for n in ("fp32k", "fp32k_mlp")},
+        "curve": curve,
+    }
+    learned_line = {
+        "workload": config3["workload"],
         "records_logged": int(n_logged), "records_offered": int(offered), "records_usable": int(len(rec)),
-        "steps_logged": logged,
-        "log_s": log_s, "train_samples": int(len(tr)), "train_epochs": args.learned_epochs,
+        "steps_logged": runs["fp32k"]["steps_logging"],
+        "ms_per_step_while_logging": runs["fp32k"]["ms_per_step_logging"],
+        "train_samples": int(len(tr)), "train_epochs": args.learned_epochs,
         "train_s": train_s, "train_loss": [float(v) for v in losses],
         "heldout": {"samples": int(n_ho),
                     "median_rel_err_mlp": float(np.median(err_mlp)),
@@ -520,16 +641,19 @@ def run_learned(args, local):
                     "median_rel_err_reference_start": float(np.median(err_ref)),
                     "p90_rel_err_reference_start": float(np.quantile(err_ref, 0.9)),
                     "logged_iters_per_return": float(rec[:, learned.ITERS].mean())},
-        "timed_steps": args.steps,
-        "fp32k_plain": {"value": case.N / (ms_plain * 1e-3), "ms_per_step": ms_plain, "returns": c_plain,
-                        "iters_per_return": it_plain / max(c_plain, 1)},
-        "fp32k_mlp": {"value": case.N / (ms_warm * 1e-3), "ms_per_step": ms_warm, "returns": c_warm,
-                      "iters_per_return": it_warm / max(c_warm, 1)},
-        "fp64_plain": {"value": case.N / (ms_64 * 1e-3), "ms_per_step": ms_64, "returns": c_64,
-                       "iters_per_return": it_64 / max(c_64, 1)},
-        "speedup_mlp_vs_fp64": ms_64 / ms_warm,
+        "fp32k_plain": {"value": case.N / (runs["fp32k"]["ms_per_step"] * 1e-3),
+                        "ms_per_step": runs["fp32k"]["ms_per_step"], "returns": runs["fp32k"]["returns"],
+                        "iters_per_return": runs["fp32k"]["iters_per_return"],
+                        "timed_steps": steps - runs["fp32k"]["steps_logging"]},
+        "fp32k_mlp": {"value": case.N / (runs["fp32k_mlp"]["ms_per_step"] * 1e-3),
+                      "ms_per_step": runs["fp32k_mlp"]["ms_per_step"], "returns": runs["fp32k_mlp"]["returns"],
+                      "iters_per_return": runs["fp32k_mlp"]["iters_per_return"], "timed_steps": steps},
+        "fp64_plain": {"value": case.N / (ms64 * 1e-3), "ms_per_step": ms64, "returns": runs["fp64"]["returns"],
+                       "iters_per_return": runs["fp64"]["iters_per_return"], "timed_steps": steps},
+        "speedup_mlp_vs_fp64": ms64 / runs["fp32k_mlp"]["ms_per_step"],
         "unit": UNIT,
     }
+    return config3, learned_line, m
 
 
 def run_product(args):
@@ -711,13 +835,16 @@ def run_product(args):
             alt[prec_name] = {"value": world * hc.N / (ms * 1e-3), "ms_per_step": ms}
             s.close()
             torch.cuda.empty_cache()
+    learned_line, config3_line, mlp = None, None, None
+    if args.config3_steps > 0 and args.learned_records > 0 and rank == 0:
+        config3_line, learned_line, mlp = run_config3(args, local)
+        torch.cuda.empty_cache()
     batched = None
     if args.batched_cases > 0:
-        batched = run_batched(args, local, max_over_ranks, barrier)
+        batched = run_batched(args, local, max_over_ranks, barrier, mlp)
         torch.cuda.empty_cache()
-    learned_line = None
-    if args.learned_records > 0 and rank == 0:
-        learned_line = run_learned(args, local)
+    if mlp is not None:
+        mlp.close()
     small_line = None
     if not args.no_small and rank == 0:
         small_line = run_small_cut(args, local)
@@ -774,6 +901,8 @@ def run_product(args):
         line["batched_sweep"] = batched
     if learned_line is not None:
         line["learned_warm_start"] = learned_line
+    if config3_line is not None:
+        line["config3_run"] = config3_line
     if rigid_line is not None:
         line["rigid_tool_cut"] = rigid_line
     if small_line is not None:
@@ -809,9 +938,12 @@ def parse_args(argv=None):
                     help="return-mapping states logged for the learned warm start (0: skip)")
     ap.add_argument("--learned-max-steps", type=int, default=20_000)
     ap.add_argument("--learned-epochs", type=int, default=3)
-    ap.add_argument("--accuracy-steps", type=int, default=4000,
-                    help="AISI 1045 cut: FP32K (+ warm start) against FP64 over this many steps (0: skip)")
-    ap.add_argument("--accuracy-every", type=int, default=500)
+    ap.add_argument("--config3-steps", type=int, default=20000,
+                    help="AISI 1045 cut (640,000 particles): steps of the FP64 / FP32K / FP32K+MLP runs (0: skip)")
+    ap.add_argument("--config3-every", type=int, default=500, help="checkpoint interval of the config-3 runs")
+    ap.add_argument("--sweep-steps", type=int, default=5000,
+                    help="batched sweep: steps of the full-length run with FP64 reference cases (0: skip)")
+    ap.add_argument("--sweep-every", type=int, default=500, help="checkpoint interval of the sweep run")
     ap.add_argument("--no-tune", action="store_true", help="no launch-shape / cell-geometry autotuning")
     ap.add_argument("--cell-factor", type=int, default=2, help="micro workload: cell edge in h")
     ap.add_argument("--no-alt-geometry", action="store_true", help="skip the cells-of-h micro line")

@@ -374,7 +374,7 @@ int sph_reduce_max_T(sph_ctx *ctx, double *out);       /* max over non-blanked p
  * Many independent cutting cases advanced together: every case keeps its own
  * particles, FEM tool, tool velocity and time step; they share the material
  * and corrector constants, the smoothing length (cell geometry) and the
- * precision form, which must be SPH_PREC_FP32K.  Each case is moved to its own
+ * precision form (SPH_PREC_FP32K or SPH_PREC_FP64).  Each case is moved to its own
  * strip of one global cell grid (x offset, gaps wider than the stencil), so
  * every step stage runs as one launch over all cases and one CUDA graph per
  * step replays them all.  The tool of each case must already be placed

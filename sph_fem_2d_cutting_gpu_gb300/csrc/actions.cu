@@ -93,8 +93,8 @@ __global__ void __launch_bounds__(kBlock) k_plasticity(int N, KConsts K, SortedF
     double eps_pl = A.eps_pl[i], eps_pl_dot = A.eps_pl_dot[i], T = A.T[i], blanked = 0.;
     int it = 0;
     uint32_t st = (K.precision == SPH_PREC_FP32K)
-                      ? plasticity_one<true>(K, S, F.p[i], A.rho[i], eps_pl, eps_pl_dot, T, blanked, &it)
-                      : plasticity_one<false>(K, S, F.p[i], A.rho[i], eps_pl, eps_pl_dot, T, blanked, &it);
+                      ? plasticity_one<true>(K, K.dt, S, F.p[i], A.rho[i], eps_pl, eps_pl_dot, T, blanked, &it)
+                      : plasticity_one<false>(K, K.dt, S, F.p[i], A.rho[i], eps_pl, eps_pl_dot, T, blanked, &it);
     if (secant_iters) secant_iters[i] = it;
     A.S[i] = S;
     A.eps_pl[i] = eps_pl;

@@ -272,7 +272,8 @@ template <bool kF32>
 __global__ void __launch_bounds__(kBlock) k_gather_fused(int N, const int32_t *__restrict__ perm, KConsts K,
                                                          SortedFields A, SortedFields B, FixedFields F,
                                                          const int32_t *__restrict__ hash_src,
-                                                         dbl4 *__restrict__ rec64, float4 *__restrict__ rec32) {
+                                                         dbl4 *__restrict__ rec64, float4 *__restrict__ rec32,
+                                                         const ToolDev *__restrict__ tools) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= N) return;
     int i = perm[k];
@@ -308,7 +309,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused(int N, const int32_t *_
     B.hash[k] = hash;
     // predict (half step) for active particles
     if (blanked != 1.) {
-        const double hdt = 0.5 * K.dt;
+        const double hdt = tools[case_of_hash(K, hash)].hdt;   // half the time step of the particle's case
         pos.x = pos.x + hdt * pos_t.x;
         pos.y = pos.y + hdt * pos_t.y;
         vel.x = vel.x + hdt * vel_t.x;
@@ -522,7 +523,7 @@ void launch_gather_fused(cudaStream_t s, int N, const int32_t *perm, const KCons
                          const SortedFields &B, const FixedFields &F, const StepScratch &W, const int32_t *hash_src,
                          const ToolDev *tool) {
     const int tb = fp64_block(N);   // EOS and artificial stress per particle: spread small systems
-    k_gather_fused<false><<<div_up(N, tb), tb, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec64, W.rec32);
+    k_gather_fused<false><<<div_up(N, tb), tb, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec64, W.rec32, tool);
 }
 
 void launch_gather_fused32(cudaStream_t s, int N, const int32_t *perm, const KConsts &K, const SortedFields *A64,

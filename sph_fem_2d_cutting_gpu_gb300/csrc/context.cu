@@ -1587,7 +1587,7 @@ int sph_batch_create(const sph_constants *c, const sph_grid_params *cell, int32_
                      const sph_case_desc *cases, int32_t precision, int32_t device, sph_ctx **out) {
     if (!c || !cell || !cases || !out || n_cases < 1 || n_cases > 65535) return SPH_ERR_INVALID;
     *out = nullptr;
-    if (precision != SPH_PREC_FP32K) return SPH_ERR_INVALID;   // per-case time steps live in the FP32K path
+    if (precision != SPH_PREC_FP32K && precision != SPH_PREC_FP64) return SPH_ERR_INVALID;
     if (check_cell_params(cell)) return SPH_ERR_INVALID;
     const bool with_tool = cases[0].tool != nullptr;
     int64_t n_total = 0;

@@ -96,7 +96,8 @@ __device__ __forceinline__ void fused_epilogue(int k, const KConsts &K, const So
                                                int32_t *__restrict__ secant_iters, uint32_t *status, bool is_tool,
                                                double2 vel_pred, double rho_pred, dbl4 vd, dbl4 sd,
                                                double2 vt, double2 xt, bool thermal, double T_t_new) {
-    const double dt = K.dt;
+    const ToolDev &tc = tool[case_of_hash(K, B.hash[k])];   // the particle's case (time step, tool)
+    const double dt = tc.dt;
     const double mass = K.c.phys.mass;
     dbl4 S0 = B.S[k];
     dbl4 St = B.S_t[k];
@@ -140,7 +141,7 @@ __device__ __forceinline__ void fused_epilogue(int k, const KConsts &K, const So
     double blanked = 0.;
     uint32_t st = 0;
     // friction heat (actions_gpu.cu:345-420), tool runs only
-    if (K.has_tool) st |= fric_heat_one(K, K.dt, tool->vel, vel, B.ft[k], B.n[k], B.fc[k], rho, B.eps_pl[k], B.on_seg[k],
+    if (K.has_tool) st |= fric_heat_one(K, dt, tc.vel, vel, B.ft[k], B.n[k], B.fc[k], rho, B.eps_pl[k], B.on_seg[k],
                                         seg.n, T, blanked, seg.fric_heat, seg.wear);
     else if (K.rigid && !is_tool && K.c.trml_wp.eta != 0.)   // actions_gpu.cu:316-343
         rigid_fric_heat_one(K, dt, K.rigid->vel, vel, B.ft[k], B.n[k], T);
@@ -149,9 +150,9 @@ __device__ __forceinline__ void fused_epilogue(int k, const KConsts &K, const So
         double eps_pl = B.eps_pl[k], eps_pl_dot = B.eps_pl_dot[k];
         int it = 0;
         if (K.precision == SPH_PREC_FP32K)
-            st |= plasticity_one<true>(K, S, F.p[k], rho, eps_pl, eps_pl_dot, T, blanked, &it);
+            st |= plasticity_one<true>(K, dt, S, F.p[k], rho, eps_pl, eps_pl_dot, T, blanked, &it);
         else
-            st |= plasticity_one<false>(K, S, F.p[k], rho, eps_pl, eps_pl_dot, T, blanked, &it);
+            st |= plasticity_one<false>(K, dt, S, F.p[k], rho, eps_pl, eps_pl_dot, T, blanked, &it);
         B.eps_pl[k] = eps_pl;
         B.eps_pl_dot[k] = eps_pl_dot;
         if (secant_iters) secant_iters[k] = it;

@@ -104,13 +104,13 @@ __device__ __forceinline__ double solve_secant(const sph_joco_constants &jc, dou
 // ---- actions_gpu.cu:689-754 do_plasticity_johnson_cook (one particle) --------
 // Reads/writes the particle's S, eps_pl, eps_pl_dot, T, blanked.  Returns
 // status bits.  `iters_out` receives the secant iteration count (0 if elastic).
+// dt: the time step of the particle's case.
 template <bool kF32Yield>
-__device__ __forceinline__ uint32_t plasticity_one(const KConsts &K, dbl4 &S, double p, double rho,
+__device__ __forceinline__ uint32_t plasticity_one(const KConsts &K, double dt, dbl4 &S, double p, double rho,
                                                    double &eps_pl, double &eps_pl_dot, double &T, double &blanked,
                                                    int *iters_out) {
     const sph_joco_constants &jc = K.c.joco;
     const double mu = K.c.phys.G;
-    const double dt = K.dt;
     double Sxx = S.x, Syy = S.z, Szz = S.w, Sxy = S.y;
     double norm_Strial = sqrtf_d(Sxx * Sxx + Syy * Syy + Szz * Szz + 2. * Sxy * Sxy);
     double cxx = Sxx - p, cyy = Syy - p, czz = Szz - p, cxy = Sxy;

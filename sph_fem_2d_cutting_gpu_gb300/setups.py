@@ -218,7 +218,7 @@ def ti64_cut(steps: int = 2000, **kw) -> Case:
 
 def aisi1045_cut(steps: int = 20000, **kw) -> Case:
     return cutting("aisi1045_cut", AISI1045, 1600, 400, 2.5e-4, 1.7, 120.0, 0.01, -6.0, 5.0, 2e-3, 0.35,
-                   s_min=7e-5, s_max=2.5e-3, tool_size=0.2, steps=steps, **kw)
+                   s_min=5.5e-5, s_max=2.5e-3, tool_size=0.2, steps=steps, **kw)
 
 
 def small_cut(nx: int = 40, ny: int = 16, steps: int = 20, **kw) -> Case:

@@ -392,6 +392,10 @@ class Batch:
         self._ck(self.lib.sph_status(self.ctx, C.byref(s), 1 if clear else 0), "sph_status")
         return s.value
 
+    def attach_mlp(self, mlp):
+        """Start the FP32K return mappings of every case from the network's prediction (None detaches)."""
+        self._ck(self.lib.sph_mlp_attach(self.ctx, mlp.h if mlp is not None else None), "sph_mlp_attach")
+
     def reduce(self) -> np.ndarray:
         """[n_cases, 3]: force x, force y (sum of fc + ft), max T of non-blanked particles."""
         out = np.zeros((self.n_cases, 3))

@@ -37,8 +37,11 @@ def small_cases():
     return cases
 
 
-def single_run(case, steps):
-    s = Solver(case, abi.SPH_PREC_FP32K, place_tool=False)
+PRECISIONS = pytest.mark.parametrize("prec", [abi.SPH_PREC_FP32K, abi.SPH_PREC_FP64], ids=["fp32k", "fp64"])
+
+
+def single_run(case, steps, prec=abi.SPH_PREC_FP32K):
+    s = Solver(case, prec, place_tool=False)
     s.step(steps)
     P = s.download(STATE + EXACT)
     red = np.concatenate([s.reduce_force(), [s.max_T()]])
@@ -47,24 +50,27 @@ def single_run(case, steps):
     return P, red, T
 
 
-def test_batch_of_one_is_bit_identical(lib):
+@PRECISIONS
+def test_batch_of_one_is_bit_identical(lib, prec):
     case = small_cases()[0]
-    b = Batch([case])
+    b = Batch([case], prec)
     b.step(STEPS)
     got = b.download_cases(STATE + EXACT)[0]
     red = b.reduce()[0]
     T = b.fem_T()[0]
     b.close()
-    P, red1, T1 = single_run(case, STEPS)
+    P, red1, T1 = single_run(case, STEPS, prec)
     for f in STATE + EXACT:
         assert np.array_equal(got[f], P[f]), f"{f}: {np.count_nonzero(got[f] != P[f])} entries differ"
     assert np.array_equal(T, T1)
     assert np.array_equal(red, red1)
 
 
-def test_batch_cases_match_single_runs(lib):
+@PRECISIONS
+def test_batch_cases_match_single_runs(lib, prec):
+    """Every case runs with its own time step and tool velocity (in both forms)."""
     cases = small_cases()
-    b = Batch(cases)
+    b = Batch(cases, prec)
     assert b.info[0]["offset"].tolist() == [0.0, 0.0]
     b.step(STEPS)
     assert b.status() & abi.STATUS_BITS["out_of_grid"] == 0
@@ -73,7 +79,7 @@ def test_batch_cases_match_single_runs(lib):
     Ts = b.fem_T()
     b.close()
     for k, case in enumerate(cases):
-        P, red1, T1 = single_run(case, STEPS)
+        P, red1, T1 = single_run(case, STEPS, prec)
         assert got[k]["pos"].shape == P["pos"].shape
         if k == 0:
             for f in STATE + EXACT:
