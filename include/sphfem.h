@@ -473,6 +473,23 @@ int sph_launch_variants(int32_t *n, int32_t *block, int32_t *min_blocks, int32_t
 int sph_set_launch_config(sph_ctx *ctx, const sph_launch_config *cfg);
 int sph_get_launch_config(const sph_ctx *ctx, sph_launch_config *cfg);
 
+/* ---- failure paths under test -----------------------------------------------------
+ * No counterpart in the reference.  Lets a test drive the bounded waits and the
+ * secant cap into their failure paths without a fault: with
+ * SPH_TEST_SKIP_BULK_COPY the staged neighbour sums announce their record
+ * copies but issue none, so the wait runs out after 1 s, the step reports
+ * SPH_STATUS_COPY_TIMEOUT and falls back to global loads (same results); with
+ * SPH_TEST_SKIP_MMA the learned warm start issues no tensor-core MMA, so its
+ * wait runs out, it reports SPH_STATUS_MMA_TIMEOUT, frees its TMEM and leaves
+ * the return mappings of that step undone.  secant_cap >= 0 replaces the
+ * reference's cap of the return mapping's secant iterations (it stops with
+ * SPH_STATUS_SECANT_MAXITER once the iteration counter exceeds the cap: 100
+ * in the reference, plasticity.cuh:155-158); < 0 restores it.  faults = 0 and
+ * secant_cap = -1 is normal operation. */
+#define SPH_TEST_SKIP_BULK_COPY (1u << 0)
+#define SPH_TEST_SKIP_MMA       (1u << 1)
+int sph_set_test_faults(sph_ctx *ctx, uint32_t faults, int32_t secant_cap);
+
 /* ---- per-stage timing ---------------------------------------------------------
  * Runs `nsteps` fused steps without the CUDA graph, with CUDA events on the
  * context stream between the stages; stage_ms[k] receives the summed device

@@ -260,6 +260,7 @@ def load() -> C.CDLL:
         "sph_eval_usui": ([P, D, D, PD, D, PD, PD], C.c_int),
         "sph_download_particles_async": ([P, C.POINTER(Particles)], C.c_int),
         "sph_set_launch_config": ([P, C.POINTER(LaunchConfig)], C.c_int),
+        "sph_set_test_faults": ([P, C.c_uint32, I32], C.c_int),
         "sph_get_launch_config": ([P, C.POINTER(LaunchConfig)], C.c_int),
         "sph_set_rigid_tool": ([P, C.POINTER(RigidTool)], C.c_int),
         "sph_get_rigid_tool": ([P, C.POINTER(RigidTool)], C.c_int),

@@ -199,6 +199,13 @@ __global__ void __launch_bounds__(kBlock) k_gather_plain(int N, const int32_t *_
 }
 
 // ---- neighbour records ----------------------------------------------------------------
+__device__ __forceinline__ bool nonfinite4(dbl4 v) {
+    return is_nan_or_inf(v.x) || is_nan_or_inf(v.y) || is_nan_or_inf(v.z) || is_nan_or_inf(v.w);
+}
+__device__ __forceinline__ bool nonfinite4(float4 v) {
+    return is_nan_or_inf(v.x) || is_nan_or_inf(v.y) || is_nan_or_inf(v.z) || is_nan_or_inf(v.w);
+}
+
 // FP64 record: (x, y, vx, vy) (sA, sB, sC, Rxx) (Rxy, Ryy, h, rho) (c, vol, T, flags)
 // with sA = (Sxx-p)/rho^2, sB = Sxy/rho^2, sC = (Syy-p)/rho^2 (interactions_gpu.cu:278-281),
 // c = sqrtf(K/rho) (:294-295), vol = mass/rho (:250).
@@ -210,7 +217,11 @@ __device__ __forceinline__ void write_record64(dbl4 *__restrict__ rec, int k, co
     dbl4 r1 = mk4((S.x - p) * rho21, S.y * rho21, (S.z - p) * rho21, R.x);
     dbl4 r2 = mk4(R.y, R.z, h, rho);
     int flags = (row & kRowMask) | (blanked == 1. ? kFlagBlanked : 0) | (tool == 1. ? kFlagTool : 0);
-    dbl4 r3 = mk4(sqrtf_d(K.c.phys.K / rho), K.c.phys.mass / rho, T, __longlong_as_double((long long)flags));
+    const double c = sqrtf_d(K.c.phys.K / rho), vol = K.c.phys.mass / rho;
+    if (nonfinite4(r0) || nonfinite4(r1) || nonfinite4(r2) || is_nan_or_inf(c) || is_nan_or_inf(vol) ||
+        is_nan_or_inf(T))
+        flags |= kFlagNonFinite;
+    dbl4 r3 = mk4(c, vol, T, __longlong_as_double((long long)flags));
     rec[4 * k + 0] = r0;
     rec[4 * k + 1] = r1;
     rec[4 * k + 2] = r2;
@@ -230,11 +241,17 @@ __device__ __forceinline__ void write_record32(float4 *__restrict__ rec, int k, 
     double yr = pos.y - (g.bbmin_y + (double)cj * g.dx);
     double rho21 = 1. / (rho * rho);
     int flags = (cj & kRowMask) | (blanked == 1. ? kFlagBlanked : 0) | (tool == 1. ? kFlagTool : 0);
-    rec[4 * k + 0] = make_float4((float)xr, (float)yr, __int_as_float(flags), (float)h);
-    rec[4 * k + 1] = make_float4((float)vel.x, (float)vel.y, (float)rho, sqrtf((float)(K.c.phys.K / rho)));
-    rec[4 * k + 2] = make_float4((float)((S.x - p) * rho21), (float)(S.y * rho21), (float)((S.z - p) * rho21),
-                                 (float)(K.c.phys.mass / rho));
-    rec[4 * k + 3] = make_float4((float)R.x, (float)R.y, (float)R.z, (float)T);
+    float4 r0 = make_float4((float)xr, (float)yr, 0.f, (float)h);
+    const float4 r1 = make_float4((float)vel.x, (float)vel.y, (float)rho, sqrtf((float)(K.c.phys.K / rho)));
+    const float4 r2 = make_float4((float)((S.x - p) * rho21), (float)(S.y * rho21), (float)((S.z - p) * rho21),
+                                  (float)(K.c.phys.mass / rho));
+    const float4 r3 = make_float4((float)R.x, (float)R.y, (float)R.z, (float)T);
+    if (nonfinite4(r0) || nonfinite4(r1) || nonfinite4(r2) || nonfinite4(r3)) flags |= kFlagNonFinite;
+    r0.z = __int_as_float(flags);
+    rec[4 * k + 0] = r0;
+    rec[4 * k + 1] = r1;
+    rec[4 * k + 2] = r2;
+    rec[4 * k + 3] = r3;
 }
 
 // Staged path helper: records from the particle arrays as they are now
@@ -432,12 +449,18 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused32(int N, const int32_t 
     if (hash >= 0 && hash < g.num_cell) { ci = hash / g.ny; cj = hash - ci * g.ny; }
     const float xr = (float)(pp.x - (g.bbmin_x + (double)ci * g.dx));
     const float yr = (float)(pp.y - (g.bbmin_y + (double)cj * g.dx));
-    const int flags = (cj & kRowMask) | (is_blanked ? kFlagBlanked : 0) | (is_tool ? kFlagTool : 0);
+    int flags = (cj & kRowMask) | (is_blanked ? kFlagBlanked : 0) | (is_tool ? kFlagTool : 0);
     const float rho21 = 1.f / (rhof * rhof);
-    rec[4 * k + 0] = make_float4(xr, yr, __int_as_float(flags), h);
-    rec[4 * k + 1] = make_float4(vx, vy, rhof, sqrtf(K.f.K_bulk / rhof));
-    rec[4 * k + 2] = make_float4((Sp.x - p) * rho21, Sp.y * rho21, (Sp.z - p) * rho21, K.f.mass / rhof);
-    rec[4 * k + 3] = make_float4(R.x, R.y, R.z, Tn);
+    float4 r0 = make_float4(xr, yr, 0.f, h);
+    const float4 r1 = make_float4(vx, vy, rhof, sqrtf(K.f.K_bulk / rhof));
+    const float4 r2 = make_float4((Sp.x - p) * rho21, Sp.y * rho21, (Sp.z - p) * rho21, K.f.mass / rhof);
+    const float4 r3 = make_float4(R.x, R.y, R.z, Tn);
+    if (nonfinite4(r0) || nonfinite4(r1) || nonfinite4(r2) || nonfinite4(r3)) flags |= kFlagNonFinite;
+    r0.z = __int_as_float(flags);
+    rec[4 * k + 0] = r0;
+    rec[4 * k + 1] = r1;
+    rec[4 * k + 2] = r2;
+    rec[4 * k + 3] = r3;
 }
 
 // The compact FP32 state (state) and its p, R (pr) widened into the FP64

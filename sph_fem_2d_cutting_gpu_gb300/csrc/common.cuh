@@ -64,6 +64,10 @@ struct KConsts {
     // rigid tool (device copy, moved every step) and the PSE conduction switch
     sph_rigid_tool *rigid;
     int32_t thermal_pse;
+    // secant iterations before SPH_STATUS_SECANT_MAXITER (the reference's 100;
+    // sph_set_test_faults may lower it) and the failure-path test bits (SPH_TEST_*)
+    int32_t secant_cap;
+    uint32_t test_faults;
 };
 
 // One logged return mapping: trial von Mises stress, equivalent plastic

@@ -669,6 +669,7 @@ int ctx_begin(const sph_constants *c, const sph_grid_params *g, const sph_geom_c
     ctx->K.dt = dt;
     ctx->K.precision = precision;
     ctx->K.n_cases = 1;
+    ctx->K.secant_cap = 100;   // plasticity.cuh:155-158
     derive(ctx->K);
     // particle arrays (particle_gpu ctor, particle_gpu.cu:11-104) and the Green buffer
     for (int b = 0; b < 2; b++) {
@@ -1922,6 +1923,15 @@ int sph_set_launch_config(sph_ctx *ctx, const sph_launch_config *cfg) {
         ctx->interact_variant = cfg->interact_variant;
         invalidate_graphs(ctx);
     }
+    return SPH_OK;
+}
+
+int sph_set_test_faults(sph_ctx *ctx, uint32_t faults, int32_t secant_cap) {
+    REQUIRE_CTX();
+    if (faults & ~(SPH_TEST_SKIP_BULK_COPY | SPH_TEST_SKIP_MMA)) return fail(ctx, SPH_ERR_INVALID, "unknown test fault");
+    ctx->K.test_faults = faults;
+    ctx->K.secant_cap = secant_cap >= 0 ? secant_cap : 100;
+    invalidate_graphs(ctx);   // the graphs hold the constants by value
     return SPH_OK;
 }
 

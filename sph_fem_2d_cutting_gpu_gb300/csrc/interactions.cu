@@ -299,14 +299,28 @@ __global__ void __launch_bounds__(kB) k_interact64(int N, KConsts K, const int32
     const int hash = B.hash[k];
     const sph_geom_constants &g = K.g;
     __shared__ int s_list[kChunk64][kB];
-    int ii = 0, hi_i = 0, lo_j = 0, hi_j = 0, jc = 0, j1 = 0;
+    int ii = 0, hi_i = 0, lo_j = 0, hi_j = 0, jc = 0, j1 = 0, ii0 = 0;
     bool done = true;
     if (hash >= 0 && hash < g.num_cell && !pse_tool) {
         const int gi = hash / g.ny, gj = hash - gi * g.ny, R = g.stencil;
-        ii = max(gi - R, 0);
+        ii = ii0 = max(gi - R, 0);
         hi_i = min(gi + R + 1, g.nx);
         lo_j = max(gj - R, 0);
         hi_j = min(gj + R + 1, g.ny);
+        jc = __ldg(offsets + ii * g.ny + lo_j);
+        j1 = __ldg(offsets + ii * g.ny + hi_j);
+        done = false;
+    }
+    // Pass 0 sums over the in-support neighbours; a stencil holding a record
+    // marked non-finite repeats them over every active candidate with the
+    // reference's zero weights outside the support (pass 1; see k_interact32).
+    int marks = 0;   // OR of the flags of the stencil's active candidates
+    for (int pass = 0; pass < 2; pass++) {
+    const bool all = pass == 1;
+    if (all) {
+        if (!(marks & kFlagNonFinite)) break;
+        a = Sums64{};
+        ii = ii0;
         jc = __ldg(offsets + ii * g.ny + lo_j);
         j1 = __ldg(offsets + ii * g.ny + hi_j);
         done = false;
@@ -317,9 +331,11 @@ __global__ void __launch_bounds__(kB) k_interact64(int N, KConsts K, const int32
         while (cnt < kChunk64) {
             if (jc < j1) {
                 const dbl4 n0 = rec[4 * jc + 0];
+                const int fj = (int)__double_as_longlong(rec[4 * jc + 3].w);
                 const double dx = xi - n0.x, dy = yi - n0.y;
                 const double rr2 = dx * dx + dy * dy;
-                if (rr2 < fourh2 && rr2 >= 1e-8) s_list[cnt++][threadIdx.x] = jc;
+                marks |= (fj & kFlagBlanked) ? 0 : fj;
+                if (all || (rr2 < fourh2 && rr2 >= 1e-8)) s_list[cnt++][threadIdx.x] = jc;
                 jc++;
             } else {
                 if (++ii >= hi_i) {
@@ -352,8 +368,10 @@ __global__ void __launch_bounds__(kB) k_interact64(int N, KConsts K, const int32
                     val = 1 - 1.5 * q * q * (1 - 0.5 * q);
                     der = -3.0 * q * (1 - 0.75 * q) * h1 / rad;
                 }
-                const double w = val * fac;
-                const double dwf = der * fac;
+                // pass 1: cubic_spline's zero weights outside the support (kernels.cuh:37-39)
+                const bool zero_w = all && (rr2 >= fourh2 || rr2 < 1e-8);
+                const double w = zero_w ? 0. : val * fac;
+                const double dwf = zero_w ? 0. : der * fac;
                 const double wx = dwf * dx, wy = dwf * dy;
                 const double volj = n3.y;
                 if (!tool_i && !(fj & kFlagTool)) {
@@ -389,9 +407,11 @@ __global__ void __launch_bounds__(kB) k_interact64(int N, KConsts K, const int32
                     a.xt0 += wr * dvx;
                     a.xt1 += wr * dvy;
                 }
-                if (thermal) a.tl += volj * (Ti - n3.z) * dwf;   // Brookshaw, (e.dW)/r == dW/dr
+                // Brookshaw, (e.dW)/r == dW/dr; the reference skips it at r <= 1e-8 (interactions_gpu.cu:328)
+                if (thermal && (!zero_w || rr2 > 1e-16)) a.tl += volj * (Ti - n3.z) * dwf;
             }
         }
+    }
     }
     const double mass = K.c.phys.mass;
     const dbl4 vd = mk4(a.vd0, a.vd1, a.vd2, a.vd3);
@@ -448,8 +468,9 @@ __device__ __forceinline__ void stage_issue(int N, int kB, const KConsts &K, con
     if (total <= 0 || total > cap) return;
     mbar_init(mbar);
     mbar_arrive_expect_tx(mbar, (uint32_t)total * 64u);
+    const bool issue = !(K.test_faults & SPH_TEST_SKIP_BULK_COPY);   // a test lets the wait run out
     for (int c = c_lo; c <= c_hi; c++)
-        if (len[c - c_lo] > 0)
+        if (issue && len[c - c_lo] > 0)
             bulk_g2s(smem_u32(srec + 4 * (start[c - c_lo] + h.delta[c - c_lo])), rec + 4 * (size_t)start[c - c_lo],
                      (uint32_t)len[c - c_lo] * 64u, mbar);
     h.staged = 1;
@@ -595,6 +616,30 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
         }
     }
     const float4 *__restrict__ nb = use_s ? nrec : rec;
+    // Pass 0 sums over the in-support neighbours.  In the reference every active
+    // particle of the stencil (this one included) runs the pair body, with zero
+    // kernel weights outside the support: exact zeros for finite data, but NaN
+    // when one of the factors is NaN or infinite.  So a particle whose stencil
+    // holds a record marked non-finite repeats its sums over every active
+    // candidate with the reference's zero weights (pass 1).
+    int marks = 0;   // OR of the flags of the stencil's active candidates
+    for (int pass = 0; pass < 2; pass++) {
+    const bool all = pass == 1;
+    if (all) {
+        if (!(marks & kFlagNonFinite)) break;
+        vd0 = vd1 = vd2 = vd3 = sd0 = sd1 = sd2 = sd3 = vt0 = vt1 = xt0 = xt1 = tl = KahanF{};
+        af = Acc32Fused{};
+        ii = max(gi - R, 0);
+        j = __ldg(offsets + ii * g.ny + lo_j);
+        j1 = __ldg(offsets + ii * g.ny + hi_j);
+        if constexpr (kStaged) {
+            if (use_s) {
+                j += s_hdr.delta[ii - s_hdr.c_lo];
+                j1 += s_hdr.delta[ii - s_hdr.c_lo];
+            }
+        }
+        done = false;
+    }
     while (!done) {
         // phase 1: collect the next in-support, active neighbours (column offset packed in 3 bits);
         // four candidates per round keep four loads in flight
@@ -611,7 +656,8 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
                     const float dx = dxc + (xri - n[u].x);
                     const float dy = (float)(gj - (fj & kRowMask)) * cell + (yri - n[u].y);
                     const float rr2 = dx * dx + dy * dy;
-                    if (rr2 < fourh2 && rr2 >= 1e-8f && !(fj & kFlagBlanked))
+                    marks |= (fj & kFlagBlanked) ? 0 : fj;
+                    if ((all || (rr2 < fourh2 && rr2 >= 1e-8f)) && !(fj & kFlagBlanked))
                         s_list[cnt++][threadIdx.x] = ((j + u) << 3) | (gi - ii + R);
                 }
                 j += 4;
@@ -621,7 +667,9 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
                 const float dx = (float)(gi - ii) * cell + (xri - n0.x);
                 const float dy = (float)(gj - (fj & kRowMask)) * cell + (yri - n0.y);
                 const float rr2 = dx * dx + dy * dy;
-                if (rr2 < fourh2 && rr2 >= 1e-8f && !(fj & kFlagBlanked)) s_list[cnt++][threadIdx.x] = (j << 3) | (gi - ii + R);
+                marks |= (fj & kFlagBlanked) ? 0 : fj;
+                if ((all || (rr2 < fourh2 && rr2 >= 1e-8f)) && !(fj & kFlagBlanked))
+                    s_list[cnt++][threadIdx.x] = (j << 3) | (gi - ii + R);
                 j++;
             } else {
                 if (++ii >= hi_i) {
@@ -663,6 +711,8 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
             // FP32 form: hardware reciprocal square root instead of sqrt and division
             const float inv_r = rsqrtf(rr2);
             const float q = rr2 * inv_r * h1;
+            // pass 1: cubic_spline's zero weights outside the support (kernels.cuh:37-39)
+            const bool zero_w = all && (rr2 >= fourh2 || rr2 < 1e-8f);
             if constexpr (kFused) {
                 float w, dwf;
                 if (q > 1.f) {
@@ -673,6 +723,7 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
                     w = fmaf(q * q, fmaf(kwd, q, kwc), fac);
                     dwf = fmaf(kdf, q, kde);
                 }
+                if (zero_w) w = dwf = 0.f;
                 const float wx = dwf * dx, wy = dwf * dy;
                 const float volj = n2.w;
                 if (!tool_i && !(fj & kFlagTool)) {
@@ -704,7 +755,7 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
                     af.xt0.add(wr * dvx);
                     af.xt1.add(wr * dvy);
                 }
-                if (thermal) af.tl.add(volj * (Ti - n3.w) * dwf);
+                if (thermal && (!zero_w || rr2 > 1e-16f)) af.tl.add(volj * (Ti - n3.w) * dwf);
             } else {
                 float val, der;
                 if (q > 1.f) {
@@ -715,8 +766,8 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
                     val = 1.f - 1.5f * q * q * (1.f - 0.5f * q);
                     der = -3.0f * q * (1.f - 0.75f * q) * h1 * inv_r;
                 }
-                const float w = val * fac;
-                const float dwf = der * fac;
+                const float w = zero_w ? 0.f : val * fac;
+                const float dwf = zero_w ? 0.f : der * fac;
                 const float wx = dwf * dx, wy = dwf * dy;
                 const float volj = n2.w;
                 if (!tool_i && !(fj & kFlagTool)) {
@@ -750,9 +801,10 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
                     xt0.add(wr * dvx);
                     xt1.add(wr * dvy);
                 }
-                if (thermal) tl.add(volj * (Ti - n3.w) * dwf);
+                if (thermal && (!zero_w || rr2 > 1e-16f)) tl.add(volj * (Ti - n3.w) * dwf);
             }
         }
+    }
     }
     if constexpr (kFused) {
         const float mass = K.f.mass;

@@ -221,7 +221,9 @@ __device__ __forceinline__ void store_row16(unsigned char *base, int r, int c0, 
 // activations go 16 columns at a time (TMEM load, SiLU, store) in a rolled
 // loop: the code stays small enough for the instruction cache of a short,
 // latency-bound launch.
-__device__ float forward_tile(FwdSmem &sh, uint32_t tmem, uint32_t &phase, const float *xn, bool &timeout) {
+// skip_mma (failure-path tests): issue no MMA, so the bounded wait runs out.
+__device__ float forward_tile(FwdSmem &sh, uint32_t tmem, uint32_t &phase, const float *xn, bool &timeout,
+                              bool skip_mma = false) {
     const uint32_t mbar = smem_u32(&sh.mbar);
     const int r = threadIdx.x;
     const uint32_t trow = tmem + (((uint32_t)threadIdx.x >> 5) * 32u << 16);
@@ -243,7 +245,7 @@ __device__ float forward_tile(FwdSmem &sh, uint32_t tmem, uint32_t &phase, const
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
-        if (r == 0) {
+        if (r == 0 && !skip_mma) {
             tc_fence_after();
             gemm_issue(tmem, smem_u32(sh.act), smem_u32(layer == 0 ? sh.w2 : sh.w3), 64, 64, false);
             mma_commit(mbar);
@@ -370,7 +372,7 @@ __global__ void __launch_bounds__(kTile, 1)
         }
         normalise(m, x, xn);
         bool timeout = false;
-        const float yh = forward_tile(sh, tmem, phase, xn, timeout);
+        const float yh = forward_tile(sh, tmem, phase, xn, timeout, (K.test_faults & SPH_TEST_SKIP_MMA) != 0);
         if (timeout) {
             if (threadIdx.x == 0) set_status(status, SPH_STATUS_MMA_TIMEOUT);
             break;

@@ -75,7 +75,7 @@ __device__ __forceinline__ double sigma_yield_tc_f32(const sph_joco_constants &j
 template <bool kF32Yield>
 __device__ __forceinline__ double solve_secant(const sph_joco_constants &jc, double init, double tol,
                                               double norm_Strial, double eps_pl_init, double term_c, double delta_t,
-                                              double mu, int *iters) {
+                                              double mu, int *iters, int max_iter = 100) {
     const double s23 = sqrt(2.0 / 3.0);
     auto opt_fun = [&](double dl) {
         double eq = eps_pl_init + s23 * fmax(dl, 0.);
@@ -86,7 +86,6 @@ __device__ __forceinline__ double solve_secant(const sph_joco_constants &jc, dou
     double delta_lambda = init;
     double delta_lambda_old = delta_lambda;
     int iter = 0;
-    const int max_iter = 100;
     while (true) {
         double g = opt_fun(delta_lambda);
         double delta_lambda_1 = delta_lambda * 1.01;
@@ -125,7 +124,7 @@ __device__ __forceinline__ uint32_t plasticity_one(const KConsts &K, double dt, 
     }
     int it = 0;
     double delta_lambda = solve_secant<kF32Yield>(jc, fmax(eps_pl_dot * dt * sqrt(2. / 3.), 1e-8), 1e-6, norm_Strial,
-                                                  eps_pl, term_c, dt, mu, &it);
+                                                  eps_pl, term_c, dt, mu, &it, K.secant_cap);
     uint32_t st = 0;
     if (it < 0) { st |= SPH_STATUS_SECANT_MAXITER; it = -it; }
     *iters_out = it;
@@ -340,7 +339,7 @@ __device__ __forceinline__ uint32_t jc_return_f32(const KConsts &K, const JcF32 
         dl = dl - (float)g / slope;
         if (dl < 0.f) dl = -0.1f * dl;
         if (fabsf(dl - dl_old) < 1e-6f) { iter++; break; }
-        if (iter > 100) { st |= SPH_STATUS_SECANT_MAXITER; iter++; break; }
+        if (iter > K.secant_cap) { st |= SPH_STATUS_SECANT_MAXITER; iter++; break; }
         iter++;
     }
     *iters_out = iter;

@@ -50,9 +50,8 @@ def test_batch_create_argument_checks(lib):
     ctx = C.c_void_p()
     c0 = cases[0].constants
     g = cases[0].grid
-    # FP64 is not a batched precision; zero cases; bad time step
-    assert lib.sph_batch_create(C.byref(c0), C.byref(g), 1, descs, abi.SPH_PREC_FP64, 0, C.byref(ctx)) == \
-        abi.SPH_ERR_INVALID
+    # an unknown precision form; zero cases; bad time step
+    assert lib.sph_batch_create(C.byref(c0), C.byref(g), 1, descs, 7, 0, C.byref(ctx)) == abi.SPH_ERR_INVALID
     assert lib.sph_batch_create(C.byref(c0), C.byref(g), 0, descs, abi.SPH_PREC_FP32K, 0, C.byref(ctx)) == \
         abi.SPH_ERR_INVALID
     d.dt = 0.0
