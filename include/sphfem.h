@@ -352,6 +352,18 @@ int sph_write_vtk_tool(sph_ctx *ctx, const char *path, const double *tl_ref);
  * the wear statistics of the last step (see sph_set_wear). */
 int sph_write_vtk_segments(sph_ctx *ctx, const char *path);
 int sph_append_force_log(sph_ctx *ctx, const char *path);
+/* The same three writers on host arrays (no context, no GPU): the calls above
+ * download the state and use these.  Particles: pos, vel, fc, ft, n, S, p, T,
+ * eps_pl, on_seg and blanked of *h.  Tool: nodes [n][2], nodal T, elements
+ * [n][4] (a, b, c, colour), shift (NULL, or the top-left point's travel
+ * since tl_ref).  Segments: left, right, normal [n][2]; phys_para [n][4],
+ * sliding_force and wear_rate [n], all three NULL without wear statistics. */
+int sph_vtk_write_particles_host(const sph_particles *h, const char *path);
+int sph_vtk_write_tool_host(int32_t n_nodes, const double *position, const double *T, int32_t n_elements,
+                            const int32_t *elements, const double *shift, const char *path);
+int sph_vtk_write_segments_host(int32_t n_seg, const double *left, const double *right, const double *normal,
+                                const double *phys_para, const double *sliding_force, const double *wear_rate,
+                                const char *path);
 
 /* ---- pipelined host I/O ------------------------------------------------------------
  * No counterpart in the reference.  For callers that feed a state in and read the

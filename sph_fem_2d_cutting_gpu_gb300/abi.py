@@ -261,6 +261,9 @@ def load() -> C.CDLL:
         "sph_download_particles_async": ([P, C.POINTER(Particles)], C.c_int),
         "sph_set_launch_config": ([P, C.POINTER(LaunchConfig)], C.c_int),
         "sph_set_test_faults": ([P, C.c_uint32, I32], C.c_int),
+        "sph_vtk_write_particles_host": ([C.POINTER(Particles), C.c_char_p], C.c_int),
+        "sph_vtk_write_tool_host": ([I32, PD, PD, I32, PI, PD, C.c_char_p], C.c_int),
+        "sph_vtk_write_segments_host": ([I32, PD, PD, PD, PD, PD, PD, C.c_char_p], C.c_int),
         "sph_get_launch_config": ([P, C.POINTER(LaunchConfig)], C.c_int),
         "sph_set_rigid_tool": ([P, C.POINTER(RigidTool)], C.c_int),
         "sph_get_rigid_tool": ([P, C.POINTER(RigidTool)], C.c_int),

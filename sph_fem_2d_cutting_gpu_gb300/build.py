@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
                      "-Xptxas", "-warn-spills"]
 SOURCES = ["cells.cu", "interactions.cu", "actions.cu", "fem.cu", "context.cu", "toolsetup.cpp", "noalloc.cu", "mlp.cu",
-           "mlp_host.cu", "wear.cu"]
+           "mlp_host.cu", "wear.cu", "vtk.cpp"]
 HEADERS = ["common.cuh", "physics.cuh", "state.cuh", "launch.cuh", "toolsetup.h", "mlp_host.h", "rigid.cuh", "async.cuh", "p1elem.h"]
 
 

@@ -218,9 +218,9 @@ __device__ __forceinline__ void write_record64(dbl4 *__restrict__ rec, int k, co
     dbl4 r2 = mk4(R.y, R.z, h, rho);
     int flags = (row & kRowMask) | (blanked == 1. ? kFlagBlanked : 0) | (tool == 1. ? kFlagTool : 0);
     const double c = sqrtf_d(K.c.phys.K / rho), vol = K.c.phys.mass / rho;
-    if (nonfinite4(r0) || nonfinite4(r1) || nonfinite4(r2) || is_nan_or_inf(c) || is_nan_or_inf(vol) ||
-        is_nan_or_inf(T))
-        flags |= kFlagNonFinite;
+    if (!(flags & kFlagBlanked) && (nonfinite4(r0) || nonfinite4(r1) || nonfinite4(r2) || is_nan_or_inf(c) ||
+                                    is_nan_or_inf(vol) || is_nan_or_inf(T)))
+        flags |= kFlagNonFinite;   // blanked records are skipped as neighbours: no mark
     dbl4 r3 = mk4(c, vol, T, __longlong_as_double((long long)flags));
     rec[4 * k + 0] = r0;
     rec[4 * k + 1] = r1;
@@ -246,7 +246,8 @@ __device__ __forceinline__ void write_record32(float4 *__restrict__ rec, int k, 
     const float4 r2 = make_float4((float)((S.x - p) * rho21), (float)(S.y * rho21), (float)((S.z - p) * rho21),
                                   (float)(K.c.phys.mass / rho));
     const float4 r3 = make_float4((float)R.x, (float)R.y, (float)R.z, (float)T);
-    if (nonfinite4(r0) || nonfinite4(r1) || nonfinite4(r2) || nonfinite4(r3)) flags |= kFlagNonFinite;
+    if (!(flags & kFlagBlanked) && (nonfinite4(r0) || nonfinite4(r1) || nonfinite4(r2) || nonfinite4(r3)))
+        flags |= kFlagNonFinite;   // blanked records are skipped as neighbours: no mark
     r0.z = __int_as_float(flags);
     rec[4 * k + 0] = r0;
     rec[4 * k + 1] = r1;
@@ -455,7 +456,8 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused32(int N, const int32_t 
     const float4 r1 = make_float4(vx, vy, rhof, sqrtf(K.f.K_bulk / rhof));
     const float4 r2 = make_float4((Sp.x - p) * rho21, Sp.y * rho21, (Sp.z - p) * rho21, K.f.mass / rhof);
     const float4 r3 = make_float4(R.x, R.y, R.z, Tn);
-    if (nonfinite4(r0) || nonfinite4(r1) || nonfinite4(r2) || nonfinite4(r3)) flags |= kFlagNonFinite;
+    if (!(flags & kFlagBlanked) && (nonfinite4(r0) || nonfinite4(r1) || nonfinite4(r2) || nonfinite4(r3)))
+        flags |= kFlagNonFinite;   // blanked records are skipped as neighbours: no mark
     r0.z = __int_as_float(flags);
     rec[4 * k + 0] = r0;
     rec[4 * k + 1] = r1;

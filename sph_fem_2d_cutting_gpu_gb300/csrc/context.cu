@@ -1964,49 +1964,7 @@ int sph_write_vtk_particles(sph_ctx *ctx, const char *path) {
     h.on_seg = on_seg.data();
     int r = sph_download_particles(ctx, &h);
     if (r) return r;
-    FILE *fp = fopen(path, "w");
-    if (!fp) return fail(ctx, SPH_ERR_INVALID, std::string("cannot open ") + path);
-    int m = 0;
-    for (int i = 0; i < n; i++) m += blanked[i] != 1.;
-    // vtk_writer.cu:11-220: points of the non-blanked particles, one vertex cell each
-    fprintf(fp, "# vtk DataFile Version 2.0\nmfree iwf\nASCII\n\nDATASET UNSTRUCTURED_GRID\nPOINTS %d float\n", m);
-    for (int i = 0; i < n; i++)
-        if (blanked[i] != 1.) fprintf(fp, "%f %f %f\n", pos[2 * i], pos[2 * i + 1], 0.);
-    fprintf(fp, "\nCELLS %d %d\n", m, 2 * m);
-    for (int k = 0; k < m; k++) fprintf(fp, "%d %d\n", 1, k);   // vertex k of the POINTS list
-    fprintf(fp, "\nCELL_TYPES %d\n", m);
-    for (int k = 0; k < m; k++) fprintf(fp, "%d\n", 1);
-    fprintf(fp, "\nPOINT_DATA %d\n", m);
-    fprintf(fp, "SCALARS Temperature float 1\nLOOKUP_TABLE default\n");
-    for (int i = 0; i < n; i++)
-        if (blanked[i] != 1.) fprintf(fp, "%f\n", T[i]);
-    fprintf(fp, "\nSCALARS on_seg int 1\nLOOKUP_TABLE default\n");
-    for (int i = 0; i < n; i++)
-        if (blanked[i] != 1.) fprintf(fp, "%d\n", on_seg[i]);
-    fprintf(fp, "\nSCALARS EquivAccumPlasticStrain float 1\nLOOKUP_TABLE default\n");
-    for (int i = 0; i < n; i++)
-        if (blanked[i] != 1.) fprintf(fp, "%f\n", eps[i]);
-    fprintf(fp, "\nVECTORS Velocity float\n");
-    for (int i = 0; i < n; i++)
-        if (blanked[i] != 1.) fprintf(fp, "%f %f %f\n", vel[2 * i], vel[2 * i + 1], 0.);
-    fprintf(fp, "\nVECTORS fc float\n");
-    for (int i = 0; i < n; i++)
-        if (blanked[i] != 1.) fprintf(fp, "%2f %2f %2f\n", 100000 * fc[2 * i], 100000 * fc[2 * i + 1], 0.);
-    fprintf(fp, "\nVECTORS ft float\n");
-    for (int i = 0; i < n; i++)
-        if (blanked[i] != 1.) fprintf(fp, "%f %f %f\n", 100000 * ft[2 * i], 100000 * ft[2 * i + 1], 0.);
-    fprintf(fp, "\nVECTORS normal float\n");
-    for (int i = 0; i < n; i++)
-        if (blanked[i] != 1.) fprintf(fp, "%f %f %f\n", nrm[2 * i], nrm[2 * i + 1], 0.);
-    fprintf(fp, "\nSCALARS SvM float 1\nLOOKUP_TABLE default\n");
-    for (int i = 0; i < n; i++) {
-        if (blanked[i] == 1.) continue;
-        const double cxx = S[4 * i] - p[i], cyy = S[4 * i + 2] - p[i], czz = S[4 * i + 3] - p[i], cxy = S[4 * i + 1];
-        const double svm2 = (cxx * cxx + cyy * cyy + czz * czz) - cxx * cyy - cxx * czz - cyy * czz + 3.0 * cxy * cxy;
-        fprintf(fp, "%f\n", svm2 > 0 ? std::sqrt(svm2) : 0.);
-    }
-    fprintf(fp, "\n");
-    if (fclose(fp) != 0) return fail(ctx, SPH_ERR_INVALID, std::string("cannot write ") + path);
+    if (sph_vtk_write_particles_host(&h, path) != SPH_OK) return fail(ctx, SPH_ERR_INVALID, std::string("cannot write ") + path);
     return SPH_OK;
 }
 
@@ -2028,20 +1986,16 @@ int sph_write_vtk_tool(sph_ctx *ctx, const char *path, const double *tl_ref) {
         shift[1] = td.tl_point_ref[1] - tl_ref[1];
     }
     CK(cudaStreamSynchronize(ctx->stream));
-    FILE *fp = fopen(path, "w");
-    if (!fp) return fail(ctx, SPH_ERR_INVALID, std::string("cannot open ") + path);
-    // vtk_writer.cu:304-366: nodes, triangles, nodal temperature
-    fprintf(fp, "# vtk DataFile Version 2.0\nmfree iwf\nASCII\n\nDATASET UNSTRUCTURED_GRID\nPOINTS %d float\n", nn);
-    for (int i = 0; i < nn; i++) fprintf(fp, "%f %f %f\n", position[2 * i] - shift[0], position[2 * i + 1] - shift[1], 0.);
     const int ne = M.n_elements;
-    fprintf(fp, "\nCELLS %d %d\n", ne, 4 * ne);
-    for (int e = 0; e < ne; e++) fprintf(fp, "3 %d %d %d\n", M.elements[e].x, M.elements[e].y, M.elements[e].z);
-    fprintf(fp, "\nCELL_TYPES %d\n", ne);
-    for (int e = 0; e < ne; e++) fprintf(fp, "5\n");
-    fprintf(fp, "POINT_DATA %d\nSCALARS temperature float 1\nLOOKUP_TABLE default\n", nn);
-    for (int i = 0; i < nn; i++) fprintf(fp, "%f\n", T[i]);
-    fprintf(fp, "\n");
-    if (fclose(fp) != 0) return fail(ctx, SPH_ERR_INVALID, std::string("cannot write ") + path);
+    std::vector<int32_t> el(4 * (size_t)ne);
+    for (int e = 0; e < ne; e++) {
+        el[4 * e] = M.elements[e].x;
+        el[4 * e + 1] = M.elements[e].y;
+        el[4 * e + 2] = M.elements[e].z;
+        el[4 * e + 3] = M.elements[e].w;
+    }
+    if (sph_vtk_write_tool_host(nn, position.data(), T.data(), ne, el.data(), tl_ref ? shift : nullptr, path) != SPH_OK)
+        return fail(ctx, SPH_ERR_INVALID, std::string("cannot write ") + path);
     return SPH_OK;
 }
 
@@ -2066,36 +2020,10 @@ int sph_write_vtk_segments(sph_ctx *ctx, const char *path) {
         CK(cudaMemcpyAsync(wr.data(), ctx->seg.wear_rate, 8 * (size_t)ns, cudaMemcpyDeviceToHost, ctx->stream));
     }
     CK(cudaStreamSynchronize(ctx->stream));
-    FILE *fp = fopen(path, "w");
-    if (!fp) return fail(ctx, SPH_ERR_INVALID, std::string("cannot open ") + path);
-    fprintf(fp, "# vtk DataFile Version 2.0\nmfree iwf\nASCII\n\nDATASET UNSTRUCTURED_GRID\nPOINTS %d float\n", 3 * ns);
-    for (int i = 0; i < ns; i++) {
-        const double lx = left[2 * i], ly = left[2 * i + 1], rx = right[2 * i], ry = right[2 * i + 1];
-        fprintf(fp, "%f %f %f\n", lx, ly, 0.);
-        fprintf(fp, "%f %f %f\n", rx, ry, 0.);
-        const double dis = sqrt((lx - rx) * (lx - rx) + (ly - ry) * (ly - ry));
-        fprintf(fp, "%f %f %f\n", rx + dis * n[2 * i], ry + dis * n[2 * i + 1], 0.);
-    }
-    fprintf(fp, "\nCELLS %d %d\n", ns, 4 * ns);
-    for (int i = 0; i < ns; i++) fprintf(fp, "3 %d %d %d \n", 3 * i, 3 * i + 1, 3 * i + 2);
-    fprintf(fp, "\nCELL_TYPES %d\n", ns);
-    for (int i = 0; i < ns; i++) fprintf(fp, "5\n");
-    fprintf(fp, "POINT_DATA %d\n", 3 * ns);
-    // a segment's value on its third point, 0 where no particle contributed
-    auto field = [&](const char *name, auto value) {
-        fprintf(fp, "SCALARS %s float 1\nLOOKUP_TABLE default\n", name);
-        for (int i = 0; i < ns; i++) {
-            fprintf(fp, "%f\n%f\n", 0., 0.);
-            fprintf(fp, "%f\n", wear[4 * i] != 0. ? value(i) : 0.);
-        }
-        fprintf(fp, "\n");
-    };
-    field("PressureGPa", [&](int i) { return wear[4 * i + 1] / wear[4 * i] * 100.; });
-    field("Velocity", [&](int i) { return wear[4 * i + 2] / wear[4 * i] * 10000.; });
-    field("Temperature", [&](int i) { return wear[4 * i + 3] / wear[4 * i]; });
-    field("Frictional_stress", [&](int i) { return sf[i] / wear[4 * i] * 100.; });
-    field("Wear_rate", [&](int i) { return wr[i] * 1e10; });
-    if (fclose(fp) != 0) return fail(ctx, SPH_ERR_INVALID, std::string("cannot write ") + path);
+    const bool stats = ctx->wear_ready;
+    if (sph_vtk_write_segments_host(ns, left.data(), right.data(), n.data(), stats ? wear.data() : nullptr,
+                                    stats ? sf.data() : nullptr, stats ? wr.data() : nullptr, path) != SPH_OK)
+        return fail(ctx, SPH_ERR_INVALID, std::string("cannot write ") + path);
     return SPH_OK;
 }
 

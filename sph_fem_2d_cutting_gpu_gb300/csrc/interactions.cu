@@ -314,17 +314,9 @@ __global__ void __launch_bounds__(kB) k_interact64(int N, KConsts K, const int32
     // Pass 0 sums over the in-support neighbours; a stencil holding a record
     // marked non-finite repeats them over every active candidate with the
     // reference's zero weights outside the support (pass 1; see k_interact32).
-    int marks = 0;   // OR of the flags of the stencil's active candidates
-    for (int pass = 0; pass < 2; pass++) {
-    const bool all = pass == 1;
-    if (all) {
-        if (!(marks & kFlagNonFinite)) break;
-        a = Sums64{};
-        ii = ii0;
-        jc = __ldg(offsets + ii * g.ny + lo_j);
-        j1 = __ldg(offsets + ii * g.ny + hi_j);
-        done = false;
-    }
+    int marks = 0;   // OR of the flags of the stencil's candidates (blanked ones carry no mark)
+    auto sweep = [&](auto all_tag) {
+    constexpr bool all = decltype(all_tag)::value;
     while (!done) {
         // phase 1: collect the next in-support candidates (columns ii, cells lo_j..hi_j)
         int cnt = 0;
@@ -334,7 +326,7 @@ __global__ void __launch_bounds__(kB) k_interact64(int N, KConsts K, const int32
                 const int fj = (int)__double_as_longlong(rec[4 * jc + 3].w);
                 const double dx = xi - n0.x, dy = yi - n0.y;
                 const double rr2 = dx * dx + dy * dy;
-                marks |= (fj & kFlagBlanked) ? 0 : fj;
+                if (!all) marks |= fj;
                 if (all || (rr2 < fourh2 && rr2 >= 1e-8)) s_list[cnt++][threadIdx.x] = jc;
                 jc++;
             } else {
@@ -412,6 +404,15 @@ __global__ void __launch_bounds__(kB) k_interact64(int N, KConsts K, const int32
             }
         }
     }
+    };
+    sweep(std::false_type{});
+    if (marks & kFlagNonFinite) {   // rare: the reference's full stencil with zero weights
+        a = Sums64{};
+        ii = ii0;
+        jc = __ldg(offsets + ii * g.ny + lo_j);
+        j1 = __ldg(offsets + ii * g.ny + hi_j);
+        done = false;
+        sweep(std::true_type{});
     }
     const double mass = K.c.phys.mass;
     const dbl4 vd = mk4(a.vd0, a.vd1, a.vd2, a.vd3);
@@ -622,24 +623,9 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
     // when one of the factors is NaN or infinite.  So a particle whose stencil
     // holds a record marked non-finite repeats its sums over every active
     // candidate with the reference's zero weights (pass 1).
-    int marks = 0;   // OR of the flags of the stencil's active candidates
-    for (int pass = 0; pass < 2; pass++) {
-    const bool all = pass == 1;
-    if (all) {
-        if (!(marks & kFlagNonFinite)) break;
-        vd0 = vd1 = vd2 = vd3 = sd0 = sd1 = sd2 = sd3 = vt0 = vt1 = xt0 = xt1 = tl = KahanF{};
-        af = Acc32Fused{};
-        ii = max(gi - R, 0);
-        j = __ldg(offsets + ii * g.ny + lo_j);
-        j1 = __ldg(offsets + ii * g.ny + hi_j);
-        if constexpr (kStaged) {
-            if (use_s) {
-                j += s_hdr.delta[ii - s_hdr.c_lo];
-                j1 += s_hdr.delta[ii - s_hdr.c_lo];
-            }
-        }
-        done = false;
-    }
+    int marks = 0;   // OR of the flags of the stencil's candidates (blanked ones carry no mark)
+    auto sweep = [&](auto all_tag) {
+    constexpr bool all = decltype(all_tag)::value;
     while (!done) {
         // phase 1: collect the next in-support, active neighbours (column offset packed in 3 bits);
         // four candidates per round keep four loads in flight
@@ -656,7 +642,7 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
                     const float dx = dxc + (xri - n[u].x);
                     const float dy = (float)(gj - (fj & kRowMask)) * cell + (yri - n[u].y);
                     const float rr2 = dx * dx + dy * dy;
-                    marks |= (fj & kFlagBlanked) ? 0 : fj;
+                    if (!all) marks |= fj;
                     if ((all || (rr2 < fourh2 && rr2 >= 1e-8f)) && !(fj & kFlagBlanked))
                         s_list[cnt++][threadIdx.x] = ((j + u) << 3) | (gi - ii + R);
                 }
@@ -667,7 +653,7 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
                 const float dx = (float)(gi - ii) * cell + (xri - n0.x);
                 const float dy = (float)(gj - (fj & kRowMask)) * cell + (yri - n0.y);
                 const float rr2 = dx * dx + dy * dy;
-                marks |= (fj & kFlagBlanked) ? 0 : fj;
+                if (!all) marks |= fj;
                 if ((all || (rr2 < fourh2 && rr2 >= 1e-8f)) && !(fj & kFlagBlanked))
                     s_list[cnt++][threadIdx.x] = (j << 3) | (gi - ii + R);
                 j++;
@@ -805,6 +791,22 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
             }
         }
     }
+    };
+    sweep(std::false_type{});
+    if (marks & kFlagNonFinite) {   // rare: the reference's full stencil with zero weights
+        vd0 = vd1 = vd2 = vd3 = sd0 = sd1 = sd2 = sd3 = vt0 = vt1 = xt0 = xt1 = tl = KahanF{};
+        af = Acc32Fused{};
+        ii = max(gi - R, 0);
+        j = __ldg(offsets + ii * g.ny + lo_j);
+        j1 = __ldg(offsets + ii * g.ny + hi_j);
+        if constexpr (kStaged) {
+            if (use_s) {
+                j += s_hdr.delta[ii - s_hdr.c_lo];
+                j1 += s_hdr.delta[ii - s_hdr.c_lo];
+            }
+        }
+        done = false;
+        sweep(std::true_type{});
     }
     if constexpr (kFused) {
         const float mass = K.f.mass;

@@ -71,8 +71,9 @@ struct SortScratch {
 // FP64: 16 doubles = 128 B; FP32K: 16 floats = 64 B (positions as offsets
 // from the particle's cell corner; the last word packs the cell row and flags).
 constexpr int kRecWords = 16;
-// kFlagNonFinite: a value of the record is NaN or infinite (its pair terms are
-// NaN even with the zero kernel weights outside the support).
+// kFlagNonFinite: a value of an active particle's record is NaN or infinite
+// (its pair terms are NaN even with the zero kernel weights outside the
+// support); never set on blanked records.
 enum : int { kFlagBlanked = 1 << 30, kFlagTool = 1 << 29, kFlagNonFinite = 1 << 28, kRowMask = (1 << 28) - 1 };
 
 // Interface segments (segment_FEM_gpu, segment_FEM_gpu.h:31-56).
