@@ -46,14 +46,18 @@ UNIT = "particle-steps/s"
 ALGO_BYTES = {
     "fp64": dict(read=128 + 4 + (16 + 16 + 32 + 8 + 8) + 32 + 8 + 16 + 16 + 8 + 8 + 8,
                  write=(16 + 16 + 32 + 8 + 8) + (16 + 16 + 32 + 8 + 8) + 8 + 8 + 4),
-    "fp32k": dict(read=64 + 4 + (16 + 16 + 32 + 8 + 8) + 32 + 8 + 16 + 16 + 16 + 8 + 8 + 8 + 8,
-                  write=(16 + 16 + 32 + 8 + 8) + (16 + 16 + 32 + 8 + 8) + 8 + 8 + 4),
+    # compact FP32 state: record 64, hash 4, S + S_t 32, fc + ft 16, pos 16 (FP64),
+    # vel 8, rho 8 (FP64), T + T_t 8, eps_pl + eps_pl_dot 8, p 4; writes S_t,
+    # rho_t, pos_t, vel_t (36) and the corrected pos, vel, rho, S, T, eps_pl,
+    # eps_pl_dot (60)
+    "fp32k": dict(read=64 + 4 + 32 + 16 + (16 + 8 + 8 + 8) + 8 + 4,
+                  write=(16 + 4 + 8 + 8) + (16 + 8 + 8 + 16 + 4 + 4 + 4)),
 }
 # DRAM bytes (read + write) per particle of one full-size launch of the fused
 # neighbour sums, from ncu on the 2048x2048 micro workload with 2h cells
-# (dram__bytes_read.sum 997,552,640 + dram__bytes_write.sum 706,785,024 for
+# (dram__bytes_read.sum 689,433,344 + dram__bytes_write.sum 397,072,128 for
 # 4,194,304 particles, k_interact32<fused, 128x6>; one-pass capture).
-NCU_TRAFFIC_PER_PARTICLE = {"fp32k": (997_552_640 + 706_785_024) / 4_194_304}
+NCU_TRAFFIC_PER_PARTICLE = {"fp32k": (689_433_344 + 397_072_128) / 4_194_304}
 # Floating-point work per particle of the fused neighbour sums, from ncu's SASS
 # instruction counters (dadd + dmul + 2 dfma; fadd + fmul + 2 ffma) on the
 # 512x512 micro workload with 2h cells (262,144 particles): k_interact64 executes

@@ -203,6 +203,9 @@ int sph_tool_host_export(const sph_tool_host *t, sph_segments *seg, sph_fem *fem
 /* Wear layers of the host tool model (layer[e][0]: layer 1, layer[e][1]: layer 2;
  * mesh_structure_GPU.cu:1063-1148). */
 int sph_tool_host_layers(const sph_tool_host *t, int32_t *layer);
+/* Elements of the host tool model after colouring: elements[e] = (node a, b, c,
+ * colour 1..n_colors) (mesh_GPU_m::node_num, mesh_structure_GPU.cu:596-739). */
+int sph_tool_host_elements(const sph_tool_host *t, int32_t *elements);
 int sph_tool_host_destroy(sph_tool_host *t);
 
 /* ---- context ------------------------------------------------------------ */
@@ -450,6 +453,8 @@ int sph_mlp_get_params(sph_mlp *m, float *params, sph_mlp_norm *norm);  /* NULL 
 int sph_mlp_set_params(sph_mlp *m, const float *params, const sph_mlp_norm *norm);
 int sph_mlp_fit_norm(sph_mlp *m, const float *x, const float *t, int64_t n);   /* moments of the data */
 int sph_mlp_predict(sph_mlp *m, const float *x, int64_t n, float *y);  /* host x [n][4] -> host y [n] */
+/* The same through the warp-per-sample form the fused step runs in its epilogue (SPH_MLP_WARP). */
+int sph_mlp_predict_warp(sph_mlp *m, const float *x, int64_t n, float *y);
 /* Gradient of the mean loss over the n samples (host in/out; grad [SPH_MLP_NPARAMS]). */
 int sph_mlp_gradients(sph_mlp *m, const float *x, const float *t, int64_t n, float *grad, float *loss);
 /* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the gradient of these n samples. */
@@ -469,6 +474,16 @@ int sph_jc_stats(sph_ctx *ctx, int32_t enable, int64_t *out, int32_t reset);
 /* Copies the network into the context and starts the return mappings of the
  * fused FP32K step from its prediction; NULL detaches. */
 int sph_mlp_attach(sph_ctx *ctx, const sph_mlp *m);
+/* Where the attached network runs in the fused step:
+ * SPH_MLP_WARP (default) -- inside the neighbour-sum kernel's epilogue: a warp
+ *   with yielding particles runs one warp-wide forward pass per such particle
+ *   on the CUDA cores (BF16 weights, FP32 sums), no extra launch;
+ * SPH_MLP_TENSOR -- yielding particles are queued and a second kernel runs the
+ *   hidden layers on the tensor cores, 128 particles per tile.
+ * Both then run the same secant to the reference tolerance. */
+#define SPH_MLP_WARP 0
+#define SPH_MLP_TENSOR 1
+int sph_mlp_set_inference(sph_ctx *ctx, int32_t mode);
 
 /* ---- launch shapes -------------------------------------------------------------
  * No counterpart in the reference (its launches are fixed at 256 threads).
@@ -559,6 +574,15 @@ int sph_upload_wear(sph_ctx *ctx, const sph_wear_state *host);   /* M, phys_para
 /* Stage entry points: m_tool->segments_wear_rate_reset() (leap_frog.cu:183-186)
  * and wear_adjustment(m_tool) (leap_frog.cu:224-229). */
 int sph_segments_wear_rate_reset(sph_ctx *ctx);
+/* remesh_low_level(tool_FEM*, freq) (tool_FEM.cu:1696-1705), the remesh of the
+ * worn tool without gmsh (mfree_gpu.cpp:356): the mesh nodes on neither the
+ * cutting nor the fixed edge are shifted with the flank wear (do_mesh_shift,
+ * tool_FEM.cu:589-616, scaled by freq), the thermal system is assembled again
+ * on the moved mesh (stiffness, lumped mass, Dirichlet, inverse mass), and every
+ * node's temperature is interpolated from the old mesh
+ * (do_nodal_value_interpolation_old, tool_FEM.cu:57-107,434-443).  Single-case
+ * contexts with a FEM tool. */
+int sph_remesh_low_level(sph_ctx *ctx, int32_t freq);
 int sph_wear_adjustment(sph_ctx *ctx);
 
 /* ---- cell-list build that allocates nothing ------------------------------------

@@ -61,10 +61,13 @@ class DeviceBuffer(C.Structure):
 
 
 class MeshGPU(C.Structure):
-    """mesh_GPU_m (mesh_structure_GPU.h:80-125), 160 bytes, with only its node
-    positions at offset 80 set: the wear kernels that take it by value
-    (do_nodal_shift_wear_smooth_temp, do_segment_wear_update) read nothing else."""
-    _fields_ = [("head", C.c_uint8 * 80), ("position", P), ("tail", C.c_uint8 * 72)]
+    """mesh_GPU_m (mesh_structure_GPU.h:80-125) with WEAR_NODE_SHIFT, 160 bytes:
+    the element arrays before offset 80 are left unset (the kernels that take
+    it by value -- the wear updates, do_mesh_shift, the nodal interpolation --
+    read the node arrays and the mapping copies only)."""
+    _fields_ = [("head", C.c_uint8 * 80), ("position", P), ("cutting_edge_flag", P), ("fixed_edge_flag", P),
+                ("T_nodes", P), ("f", P), ("k", P), ("position_mapping", P), ("node_num_mapping", P),
+                ("csr_row_ptr", P), ("csr_col_ind", P)]
 
 
 class GeomConstants(C.Structure):

@@ -121,6 +121,7 @@ class MlpNorm(C.Structure):
 
 
 MLP_NPARAMS = 8705
+SPH_MLP_WARP, SPH_MLP_TENSOR = 0, 1   # sph_mlp_set_inference
 JC_LOG_WIDTH = 8
 
 
@@ -244,6 +245,7 @@ def load() -> C.CDLL:
         "sph_mlp_set_params": ([P, PF, C.POINTER(MlpNorm)], C.c_int),
         "sph_mlp_fit_norm": ([P, PF, PF, C.c_int64], C.c_int),
         "sph_mlp_predict": ([P, PF, C.c_int64, PF], C.c_int),
+        "sph_mlp_predict_warp": ([P, PF, C.c_int64, PF], C.c_int),
         "sph_mlp_gradients": ([P, PF, PF, C.c_int64, PF, PF], C.c_int),
         "sph_mlp_adam_step": ([P, PF, PF, C.c_int64, C.c_float, PF], C.c_int),
         "sph_mlp_train": ([P, PF, PF, C.c_int64, I32, I32, C.c_float, C.c_uint64, PF], C.c_int),
@@ -251,6 +253,7 @@ def load() -> C.CDLL:
         "sph_jc_log_read": ([P, PF, C.c_int64, C.POINTER(C.c_int64)], C.c_int),
         "sph_jc_stats": ([P, I32, C.POINTER(C.c_int64), I32], C.c_int),
         "sph_mlp_attach": ([P, P], C.c_int),
+        "sph_mlp_set_inference": ([P, I32], C.c_int),
         "sph_launch_variants": ([PI, PI, PI, PI], C.c_int),
         "sph_upload_particles_async": ([P, C.POINTER(Particles)], C.c_int),
         "sph_write_vtk_particles": ([P, C.c_char_p], C.c_int),
@@ -272,6 +275,8 @@ def load() -> C.CDLL:
         "sph_download_wear": ([P, C.POINTER(WearState)], C.c_int),
         "sph_upload_wear": ([P, C.POINTER(WearState)], C.c_int),
         "sph_tool_host_layers": ([P, PI], C.c_int),
+        "sph_tool_host_elements": ([P, PI], C.c_int),
+        "sph_remesh_low_level": ([P, I32], C.c_int),
     }
     for name in STAGE_FUNCTIONS:
         proto.setdefault(name, ([P], C.c_int))
@@ -312,7 +317,11 @@ def tool_model_host(case) -> dict:
             setattr(f, k, ptr(v))
         if lib.sph_tool_host_export(h, C.byref(s), C.byref(f)) != SPH_OK:
             raise RuntimeError("sph_tool_host_export failed")
-        return dict(segments=seg, fem=fem, state=st, n_colors=ncol.value, n_cut_colors=st.n_cut_colors)
+        elements = np.zeros((len(case.tool_mesh["elements"]), 4), np.int32)
+        if lib.sph_tool_host_elements(h, ptr(elements)) != SPH_OK:
+            raise RuntimeError("sph_tool_host_elements failed")
+        return dict(segments=seg, fem=fem, state=st, n_colors=ncol.value, n_cut_colors=st.n_cut_colors,
+                    elements=elements)
     finally:
         if h.value:
             lib.sph_tool_host_destroy(h)

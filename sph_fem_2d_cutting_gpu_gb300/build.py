@@ -21,11 +21,13 @@ LIBDIR = PKG / "lib"
 LIB = LIBDIR / "libsphfem.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+                     "--expt-relaxed-constexpr",
                      "-Xptxas", "-warn-spills"]
-SOURCES = ["cells.cu", "interactions.cu", "actions.cu", "fem.cu", "context.cu", "toolsetup.cpp", "noalloc.cu", "mlp.cu",
-           "mlp_host.cu", "wear.cu", "vtk.cpp"]
-HEADERS = ["common.cuh", "physics.cuh", "state.cuh", "launch.cuh", "toolsetup.h", "mlp_host.h", "rigid.cuh", "async.cuh", "p1elem.h"]
+SOURCES = ["cells.cu", "interactions.cu", "interactions_mlp.cu", "actions.cu", "fem.cu", "context.cu", "toolsetup.cpp",
+           "noalloc.cu", "mlp.cu", "mlp_host.cu", "wear.cu", "vtk.cpp"]
+HEADERS = ["common.cuh", "physics.cuh", "state.cuh", "launch.cuh", "toolsetup.h", "mlp_host.h", "rigid.cuh", "async.cuh",
+           "p1elem.h", "interact32.cuh", "mlp_warp.cuh"]
 
 
 def nvcc() -> str:

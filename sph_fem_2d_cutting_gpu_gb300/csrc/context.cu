@@ -49,6 +49,13 @@ struct sph_ctx {
     SegDev seg{};
     FemDev fem{};
     ToolDev *tool_dev = nullptr;
+    int4 *fem_elements = nullptr;        // tool elements: nodes a, b, c and colour
+    int32_t *fem_dir_elems = nullptr;    // the Dirichlet elimination's order (elements, fixed-edge flags)
+    int4 *fem_dir_flags = nullptr;
+    int fem_n_dir = 0;
+    int32_t *fem_node_edge = nullptr;    // remesh: per node, on a cutting (1) / fixed (2) edge
+    double2 *fem_pos_old = nullptr;      // remesh: the mesh and temperatures before the shift
+    double *fem_T_map = nullptr;
     double *fem_T_old = nullptr, *fem_f_temp = nullptr, *fem_K_temp = nullptr;
     // graphs, one per buffer parity
     // [input buffer][output buffer][FP32K: input in the compact form][FP32K: p, R from F32]
@@ -76,6 +83,7 @@ struct sph_ctx {
     uint16_t *mlp_wb = nullptr;
     MlpDev mlp{};
     bool mlp_on = false;
+    int mlp_mode = SPH_MLP_WARP;   // sph_mlp_set_inference
     int interact_variant = 0;            // launch shape of the fused FP32K neighbour sums
     double *usui_scratch = nullptr;      // per-block partials of sph_eval_usui
     sph_rigid_tool *rigid_dev = nullptr; // the rigid tool, moved on the device every step (NULL: none)
@@ -448,15 +456,19 @@ int issue_fused_body(sph_ctx *ctx, int64_t &n, int w, cudaEvent_t *ev = nullptr)
         launch_wear_reset(s, ctx->seg);
         sw.wear.T_nodes = ctx->fem.T_half;  // the friction heat sees the half-step FEM temperature
     }
-    if (ctx->mlp_on) CK(cudaMemsetAsync(ctx->jc_list_count, 0, sizeof(int32_t), s));
-    if (f32)
+    const bool mlp_tensor = ctx->mlp_on && ctx->mlp_mode == SPH_MLP_TENSOR;
+    if (mlp_tensor) CK(cudaMemsetAsync(ctx->jc_list_count, 0, sizeof(int32_t), s));
+    if (f32 && ctx->mlp_on && !mlp_tensor)
+        launch_interactions32_fused_mlp(s, N, ctx->K, ctx->X.offsets, B32, ctx->F32, ctx->W, sw, ctx->tool_dev,
+                                        ctx->interact_variant, ctx->mlp);
+    else if (f32)
         launch_interactions32_fused(s, N, ctx->K, ctx->X.offsets, B32, ctx->F32, ctx->W, sw, ctx->tool_dev,
                                     ctx->interact_variant);
     else
         launch_interactions(s, N, ctx->K, ctx->X.offsets, B, ctx->F, ctx->W, sw, ctx->tool_dev, true,
                             ctx->interact_variant);
     n += 1;
-    if (ctx->mlp_on) {   // FP32K only (sph_mlp_attach)
+    if (mlp_tensor) {   // FP32K only (sph_mlp_attach)
         launch_jc_warm(s, jc_warm_grid(ctx), ctx->K, B32, ctx->F32, ctx->tool_dev, ctx->mlp, ctx->W.secant_iters,
                        ctx->W.status);
         n += 1;
@@ -588,6 +600,18 @@ int sph_tool_host_layers(const sph_tool_host *t, int32_t *layer) {
     for (int e = 0; e < t->m.n_elements; e++) {
         layer[2 * e] = t->m.layer[e].x;
         layer[2 * e + 1] = t->m.layer[e].y;
+    }
+    return SPH_OK;
+}
+
+int sph_tool_host_elements(const sph_tool_host *t, int32_t *elements) {
+    if (!t || !elements) return SPH_ERR_INVALID;
+    for (int e = 0; e < t->m.n_elements; e++) {
+        const Int4 &el = t->m.elements[e];
+        elements[4 * e] = el.x;
+        elements[4 * e + 1] = el.y;
+        elements[4 * e + 2] = el.z;
+        elements[4 * e + 3] = el.w;
     }
     return SPH_OK;
 }
@@ -737,15 +761,32 @@ int ctx_upload_tool(sph_ctx *ctx, bool with_model, const std::vector<ToolDev> &t
         Fm.nnz = (int)M.col_ind.size();
         DALLOC(Fm.position, M.n_nodes); DALLOC(Fm.row_ptr, M.n_nodes + 1); DALLOC(Fm.col_ind, Fm.nnz);
         DALLOC(Fm.diag, M.n_nodes); DALLOC(Fm.K, Fm.nnz); DALLOC(Fm.M_inv, M.n_nodes); DALLOC(Fm.f, M.n_nodes);
+        DALLOC(Fm.M, M.n_nodes); DALLOC(ctx->fem_elements, M.n_elements);
         DALLOC(Fm.T, M.n_nodes); DALLOC(Fm.k, M.n_nodes); DALLOC(Fm.T_half, M.n_nodes);
         DALLOC(Fm.node_seg_ptr, M.n_nodes + 1); DALLOC(Fm.node_seg, M.node_seg.size());
         CK(cudaMemcpy(Fm.position, M.pos.data(), sizeof(double) * 2 * M.n_nodes, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(Fm.row_ptr, M.row_ptr.data(), sizeof(int) * (M.n_nodes + 1), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(Fm.col_ind, M.col_ind.data(), sizeof(int) * Fm.nnz, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(Fm.diag, M.diag.data(), sizeof(int) * M.n_nodes, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(Fm.K, M.K.data(), sizeof(double) * Fm.nnz, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(Fm.M_inv, M.M_inv.data(), sizeof(double) * M.n_nodes, cudaMemcpyHostToDevice));
-        CK(cudaMemcpy(Fm.f, M.f.data(), sizeof(double) * M.n_nodes, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(ctx->fem_elements, M.elements.data(), sizeof(int4) * M.n_elements, cudaMemcpyHostToDevice));
+        {   // K, lumped M, the Dirichlet elimination (f) and M_inv assembled on the device
+            const int nd = (int)M.dirichlet_elem.size();
+            int32_t *&dir_e = ctx->fem_dir_elems;
+            int4 *&dir_f = ctx->fem_dir_flags;
+            ctx->fem_n_dir = nd;
+            DALLOC(dir_e, std::max(nd, 1));
+            DALLOC(dir_f, std::max(nd, 1));
+            if (nd) {
+                CK(cudaMemcpy(dir_e, M.dirichlet_elem.data(), sizeof(int32_t) * nd, cudaMemcpyHostToDevice));
+                CK(cudaMemcpy(dir_f, M.dirichlet_flags.data(), sizeof(int4) * nd, cudaMemcpyHostToDevice));
+            }
+            const sph_tool_constants &tc = ctx->K.c.tool;
+            launch_fem_assemble(ctx->stream, Fm, ctx->fem_elements, M.n_elements, M.n_colors, dir_e, dir_f, nd,
+                                tc.cp, tc.rho, tc.k, tc.T0, Fm.M);
+            ctx->launches += M.n_colors + 2;
+            CK_LAUNCH();
+            CK(cudaStreamSynchronize(ctx->stream));
+        }
         CK(cudaMemcpy(Fm.T, M.T.data(), sizeof(double) * M.n_nodes, cudaMemcpyHostToDevice));
         CK(cudaMemset(Fm.k, 0, sizeof(double) * M.n_nodes));
         CK(cudaMemcpy(Fm.T_half, M.T.data(), sizeof(double) * M.n_nodes, cudaMemcpyHostToDevice));
@@ -807,6 +848,10 @@ void append_tool_model(ToolModelHost &a, const ToolModelHost &b) {
     if (a.node_seg_ptr.empty()) a.node_seg_ptr.push_back(0);
     for (size_t i = 1; i < b.node_seg_ptr.size(); i++) a.node_seg_ptr.push_back(b.node_seg_ptr[i] + nsl);
     for (int s : b.node_seg) a.node_seg.push_back(s + ns);
+    a.node_edge.insert(a.node_edge.end(), b.node_edge.begin(), b.node_edge.end());
+    // one Dirichlet pass over the cases in turn: each case's rows are its own
+    for (int e : b.dirichlet_elem) a.dirichlet_elem.push_back(e + ne);
+    a.dirichlet_flags.insert(a.dirichlet_flags.end(), b.dirichlet_flags.begin(), b.dirichlet_flags.end());
     a.n_nodes += b.n_nodes;
     a.n_elements += b.n_elements;
     a.n_seg += b.n_seg;
@@ -1885,18 +1930,29 @@ int sph_mlp_attach(sph_ctx *ctx, const sph_mlp *m) {
     CK(mlp_configure());
     if (!ctx->mlp_params) {
         DALLOC(ctx->mlp_params, kMlpParams);
-        DALLOC(ctx->mlp_wb, kMlpWb);
+        DALLOC(ctx->mlp_wb, kMlpWbAll);
         DALLOC(ctx->jc_list, ctx->N);
         DALLOC(ctx->jc_list_count, 1);
     }
     CK(cudaStreamSynchronize(m->stream));
     CK(cudaMemcpy(ctx->mlp_params, m->params, sizeof(float) * kMlpParams, cudaMemcpyDeviceToDevice));
-    CK(cudaMemcpy(ctx->mlp_wb, m->wb, sizeof(uint16_t) * kMlpWb, cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(ctx->mlp_wb, m->wb, sizeof(uint16_t) * kMlpWbAll, cudaMemcpyDeviceToDevice));
     ctx->mlp = mlp_view(m, ctx->mlp_params, ctx->mlp_wb);
     ctx->mlp_on = true;
     ctx->K.jc_list = ctx->jc_list;
     ctx->K.jc_list_count = ctx->jc_list_count;
     invalidate_graphs(ctx);
+    return SPH_OK;
+}
+
+int sph_mlp_set_inference(sph_ctx *ctx, int32_t mode) {
+    REQUIRE_CTX();
+    if (mode != SPH_MLP_WARP && mode != SPH_MLP_TENSOR) return fail(ctx, SPH_ERR_INVALID, "unknown inference mode");
+    if (mode != ctx->mlp_mode) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        ctx->mlp_mode = mode;
+        invalidate_graphs(ctx);
+    }
     return SPH_OK;
 }
 
@@ -2192,14 +2248,14 @@ int wear_setup(sph_ctx *ctx) {
     DALLOC(ctx->wear_pp, S.n);
     DALLOC(ctx->wear_sf, S.n);
     DALLOC(S.wear_rate, S.n);
-    DALLOC(Fm.M, Fm.n_nodes);
+    if (!Fm.M) DALLOC(Fm.M, Fm.n_nodes);   // the device assembly's lumped mass (after Dirichlet)
     int32_t *node = nullptr, *adj_ptr = nullptr;
-    int4 *adj = nullptr, *slot = nullptr, *elements = nullptr;
+    int4 *adj = nullptr, *slot = nullptr, *elements = ctx->fem_elements;
     DALLOC(node, M.wear_node.size());
     DALLOC(adj_ptr, M.wear_adj_ptr.size());
     DALLOC(adj, M.wear_adj.size());
     DALLOC(slot, M.wear_slot.size());
-    DALLOC(elements, M.elements.size());
+    if (!elements) DALLOC(elements, M.elements.size());
     DALLOC(W.seg_delta, S.n);
     int32_t *elem = nullptr;
     DALLOC(elem, M.wear_elem.size());
@@ -2212,7 +2268,6 @@ int wear_setup(sph_ctx *ctx) {
     CK(cudaMemsetAsync(ctx->wear_sf, 0, sizeof(double) * S.n, ctx->stream));
     CK(cudaMemsetAsync(S.wear_rate, 0, sizeof(double) * S.n, ctx->stream));
     CK(cudaMemsetAsync(W.seg_delta, 0, sizeof(dbl4) * S.n, ctx->stream));
-    CK(cudaMemcpyAsync(Fm.M, M.M.data(), sizeof(double) * Fm.n_nodes, cudaMemcpyHostToDevice, ctx->stream));
     if (!M.wear_node.empty()) {
         CK(cudaMemcpyAsync(node, M.wear_node.data(), sizeof(int32_t) * M.wear_node.size(), cudaMemcpyHostToDevice,
                            ctx->stream));
@@ -2223,8 +2278,9 @@ int wear_setup(sph_ctx *ctx) {
     }
     CK(cudaMemcpyAsync(adj_ptr, M.wear_adj_ptr.data(), sizeof(int32_t) * M.wear_adj_ptr.size(),
                        cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(elements, M.elements.data(), sizeof(int4) * M.elements.size(), cudaMemcpyHostToDevice,
-                       ctx->stream));
+    if (elements != ctx->fem_elements)
+        CK(cudaMemcpyAsync(elements, M.elements.data(), sizeof(int4) * M.elements.size(), cudaMemcpyHostToDevice,
+                           ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     W.n_elem = (int)M.wear_elem.size();
     W.elem = elem;
@@ -2263,6 +2319,28 @@ int sph_set_wear(sph_ctx *ctx, int32_t mode, const sph_wear_constants *wc) {
     ctx->seg.wear.pp = on ? ctx->wear_pp : nullptr;
     ctx->seg.wear.sf = on ? ctx->wear_sf : nullptr;
     if (changed) invalidate_graphs(ctx);
+    return SPH_OK;
+}
+
+int sph_remesh_low_level(sph_ctx *ctx, int32_t freq) {
+    REQUIRE_CTX();
+    REQUIRE_TOOL();
+    REQUIRE_SINGLE_CASE();
+    const ToolModelHost &M = ctx->tool_host;
+    FemDev &Fm = ctx->fem;
+    if (!ctx->fem_node_edge) {
+        DALLOC(ctx->fem_node_edge, Fm.n_nodes);
+        DALLOC(ctx->fem_pos_old, Fm.n_nodes);
+        DALLOC(ctx->fem_T_map, Fm.n_nodes);
+        CK(cudaMemcpyAsync(ctx->fem_node_edge, M.node_edge.data(), sizeof(int32_t) * Fm.n_nodes,
+                           cudaMemcpyHostToDevice, ctx->stream));
+    }
+    launch_remesh_low_level(ctx->stream, Fm, ctx->fem_elements, M.n_elements, M.n_colors, ctx->fem_node_edge,
+                            ctx->tool_dev, freq, ctx->fem_dir_elems, ctx->fem_dir_flags, ctx->fem_n_dir, ctx->K.c.tool,
+                            ctx->fem_pos_old, ctx->fem_T_map);
+    ctx->launches += M.n_colors + 5;
+    CK_LAUNCH();
+    CK(cudaStreamSynchronize(ctx->stream));
     return SPH_OK;
 }
 

@@ -9,6 +9,7 @@
 // inside its own SpMV row: the same arithmetic without the per-step matrix
 // copy, without atomics and without the colour launches.
 #include "launch.cuh"
+#include "p1elem.h"
 
 namespace sphfem {
 
@@ -185,6 +186,94 @@ void launch_tool_move(cudaStream_t s, const KConsts &K, const SegDev &seg, const
     if ((what & 1) && seg.n > n) n = seg.n;
     if ((what & 2) && F.n_nodes > n) n = F.n_nodes;
     k_tool_move<<<div_up(n, kBlock), kBlock, 0, s>>>(K, seg, F, tool, dt, what, per_case ? 1 : 0);
+}
+
+// ---- set-up of the thermal system on the device (FEM_thermal_gpu.cu:126-332) ----------
+// do_stiffness_mass_matrix_construction_p1q3 for the elements of one colour:
+// elements of a colour share no node, so every K entry and mass slot receives
+// at most one term per launch and the colours run in order -- the sums are
+// formed in the same order as the host assembly's colour-by-colour loop.
+__global__ void __launch_bounds__(kBlock) k_fem_assemble(int colour, int n_elem, const int4 *__restrict__ elements,
+                                                         const double2 *__restrict__ pos,
+                                                         const int32_t *__restrict__ row_ptr,
+                                                         const int32_t *__restrict__ col_ind, double cp, double rho,
+                                                         double k, double *__restrict__ K, double *__restrict__ M) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n_elem) return;
+    const int4 el = elements[e];
+    if (el.w != colour) return;
+    const double2 p0 = pos[el.x], p1 = pos[el.y], p2 = pos[el.z];
+    double m, ke[3][3];
+    p1_element(p0.x, p0.y, p1.x, p1.y, p2.x, p2.y, cp, rho, k, m, ke);
+    const int nd[3] = {el.x, el.y, el.z};
+    for (int a = 0; a < 3; a++) {
+        M[nd[a]] = __dadd_rn(M[nd[a]], m);
+        for (int b = 0; b < 3; b++)
+            for (int j = row_ptr[nd[a]]; j < row_ptr[nd[a] + 1]; j++)
+                if (col_ind[j] == nd[b]) {
+                    K[j] = __dadd_rn(K[j], ke[a][b]);
+                    break;
+                }
+    }
+}
+
+// do_dirichlet_bdc_p1q3 (FEM_thermal_gpu.cu:234-324) in the reference's
+// processing order -- colour by colour, then element order -- by one thread:
+// the reference's threads of one colour read and zero each other's symmetric
+// entries, so only a fixed order gives one answer.  The fixed boundary holds
+// a few hundred elements; this runs once per context.
+__global__ void k_fem_dirichlet(int n, const int32_t *__restrict__ elems, const int4 *__restrict__ flags,
+                                const int4 *__restrict__ elements, const int32_t *__restrict__ row_ptr,
+                                const int32_t *__restrict__ col_ind, double T0, double *__restrict__ K,
+                                double *__restrict__ M, double *__restrict__ f) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    auto node = [&](int nd) {
+        for (int i = row_ptr[nd]; i < row_ptr[nd + 1]; i++) {
+            const int local_no = col_ind[i];
+            f[local_no] = __dadd_rn(f[local_no], -__dmul_rn(K[i], T0));
+            K[i] = 0.;
+            for (int t = row_ptr[local_no]; t < row_ptr[local_no + 1]; t++)   // find_location
+                if (col_ind[t] == nd) {
+                    K[t] = 0.;
+                    break;
+                }
+            if (local_no == nd) K[i] = 1.0;
+        }
+        M[nd] = 1.0;
+        f[nd] = T0;
+    };
+    for (int q = 0; q < n; q++) {
+        const int4 el = elements[elems[q]];
+        const int4 ff = flags[q];
+        bool fx = false, fy = false, fz = false;
+        if (ff.x) fx = fy = true;
+        if (ff.y) fy = fz = true;
+        if (ff.z) fz = fx = true;
+        if (fx) node(el.x);
+        if (fy) node(el.y);
+        if (fz) node(el.z);
+    }
+}
+
+// do_inverse_mass_matrix_lumped (FEM_thermal_gpu.cu:326-332)
+__global__ void __launch_bounds__(kBlock) k_fem_inverse_mass(int n, const double *__restrict__ M,
+                                                             double *__restrict__ M_inv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) M_inv[i] = 1. / M[i];
+}
+
+void launch_fem_assemble(cudaStream_t s, const FemDev &F, const int4 *elements, int n_elem, int n_colors,
+                         const int32_t *dir_elems, const int4 *dir_flags, int n_dir, double cp, double rho, double k,
+                         double T0, double *M) {
+    cudaMemsetAsync(F.K, 0, sizeof(double) * (size_t)F.nnz, s);
+    cudaMemsetAsync(M, 0, sizeof(double) * (size_t)F.n_nodes, s);
+    cudaMemsetAsync(F.f, 0, sizeof(double) * (size_t)F.n_nodes, s);
+    for (int c = 1; c <= n_colors; c++)
+        k_fem_assemble<<<div_up(n_elem, kBlock), kBlock, 0, s>>>(c, n_elem, elements, F.position, F.row_ptr,
+                                                                 F.col_ind, cp, rho, k, F.K, M);
+    if (n_dir > 0)
+        k_fem_dirichlet<<<1, 1, 0, s>>>(n_dir, dir_elems, dir_flags, elements, F.row_ptr, F.col_ind, T0, F.K, M, F.f);
+    k_fem_inverse_mass<<<div_up(F.n_nodes, kBlock), kBlock, 0, s>>>(F.n_nodes, M, F.M_inv);
 }
 
 }  // namespace sphfem

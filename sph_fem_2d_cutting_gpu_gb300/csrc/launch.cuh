@@ -41,6 +41,10 @@ void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t 
 void launch_interactions32_fused(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets,
                                  const SortedFields32 &B, const FixedFields32 &F, const StepScratch &W,
                                  const SegDev &seg, const ToolDev *tool, int variant);
+// the same with the learned warm start folded into the epilogue (interactions_mlp.cu)
+void launch_interactions32_fused_mlp(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets,
+                                     const SortedFields32 &B, const FixedFields32 &F, const StepScratch &W,
+                                     const SegDev &seg, const ToolDev *tool, int variant, const MlpDev &mlp);
 void launch_heat_pse(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const StepScratch &W,
                      const SortedFields &B);
 void launch_heat_pse(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const StepScratch &W,
@@ -97,6 +101,11 @@ void launch_fem_robin(cudaStream_t s, const KConsts &K, const FemDev &F, const S
                       double *K_temp);
 void launch_fem_rate(cudaStream_t s, const FemDev &F, const double *f_temp, const double *K_temp);
 void launch_fem_temp(cudaStream_t s, const FemDev &F, const double *T_old, double dt);
+// the tool's thermal system assembled on the device: K, lumped M (into M), the
+// Dirichlet elimination in the given order (f) and M_inv
+void launch_fem_assemble(cudaStream_t s, const FemDev &F, const int4 *elements, int n_elem, int n_colors,
+                         const int32_t *dir_elems, const int4 *dir_flags, int n_dir, double cp, double rho, double k,
+                         double T0, double *M);
 void launch_tool_move(cudaStream_t s, const KConsts &K, const SegDev &seg, const FemDev &F, ToolDev *tool, double dt,
                       int what, bool per_case);
 
@@ -104,6 +113,13 @@ void launch_tool_move(cudaStream_t s, const KConsts &K, const SegDev &seg, const
 void launch_wear_reset(cudaStream_t s, const SegDev &seg);
 void launch_wear_adjustment(cudaStream_t s, const KConsts &K, const FemDev &F, const SegDev &seg, const WearDev &W,
                             ToolDev *tool, double dt);
+// remesh_low_level (tool_FEM.cu:1696-1705): interior nodes shifted, the
+// thermal system re-assembled, nodal temperatures interpolated from the old
+// mesh (pos_old, T_old: scratch of n_nodes)
+void launch_remesh_low_level(cudaStream_t s, const FemDev &F, const int4 *elements, int n_elem, int n_colors,
+                             const int32_t *node_edge, const ToolDev *tool, int freq, const int32_t *dir_elems,
+                             const int4 *dir_flags, int n_dir, const sph_tool_constants &tc, double2 *pos_old,
+                             double *T_old);
 
 // mlp.cu
 size_t mlp_fwd_smem();
@@ -111,6 +127,8 @@ size_t mlp_train_smem();
 cudaError_t mlp_configure();
 void launch_mlp_predict(cudaStream_t s, const MlpDev &m, const float *x, int64_t n, float *y, uint32_t *status,
                         int grid);
+// one warp per sample, the fused step's in-epilogue form (grid: blocks of 256)
+void launch_mlp_predict_warp(cudaStream_t s, const MlpDev &m, const float *x, int64_t n, float *y, int grid);
 void launch_jc_warm(cudaStream_t s, int grid, const KConsts &K, const SortedFields32 &B, const FixedFields32 &F,
                     const ToolDev *tool, const MlpDev &m, int32_t *secant_iters, uint32_t *status);
 void launch_mlp_grad(cudaStream_t s, int grid, const MlpDev &m, const float *x, const float *t, const int32_t *idx,

@@ -19,6 +19,7 @@
 
 #include "async.cuh"
 #include "launch.cuh"
+#include "mlp_warp.cuh"
 
 namespace sphfem {
 namespace {
@@ -112,18 +113,11 @@ __device__ __forceinline__ void tmem_row64(uint32_t tmem, uint32_t col, float *v
     tmem_ld16(a + 48, v + 48);
 }
 
-__device__ __forceinline__ float sigmoidf_(float z) { return 1.f / (1.f + expf(-z)); }
-__device__ __forceinline__ float siluf_(float z) { return z * sigmoidf_(z); }
 __device__ __forceinline__ float dsiluf_(float z) {
     float s = sigmoidf_(z);
     return s * (1.f + z * (1.f - s));
 }
 __device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
-__device__ __forceinline__ float bf16_bits_to_f(uint16_t b) { return __uint_as_float((uint32_t)b << 16); }
-__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
-    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
-           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(hi)) << 16);
-}
 
 // Row r of a K-major 64-column operand from 64 floats (rounded to BF16).
 __device__ __forceinline__ void store_row64(unsigned char *base, int r, const float *v) {
@@ -176,10 +170,6 @@ __device__ void load_weight(unsigned char *dst, const uint16_t *w, bool transpos
     }
 }
 
-__device__ __forceinline__ void normalise(const MlpDev &m, const float *x, float *xn) {
-#pragma unroll
-    for (int c = 0; c < kMlpIn; c++) xn[c] = (x[c] - m.x_mean[c]) * m.x_inv_std[c];
-}
 
 __device__ __forceinline__ void layer1(const MlpSmall &s, const float *xn, float *a, float *z) {
 #pragma unroll
@@ -330,16 +320,21 @@ __global__ void __launch_bounds__(kTile, 1) k_mlp_predict(MlpDev m, const float 
     fwd_teardown(sh, tmem);
 }
 
-// ---- warm-started return mapping of the fused FP32 step ------------------------------------------
-// Features of a yielding trial state: log(svm / A), eps_pl, log(1 + eps_pl_dot
-// / eps_dot_ref), homologous temperature.  Target: log(2 mu dl / |dev S|).
-__device__ __forceinline__ void jc_features(const JcF32 &j, float svm, float eps, float epsd, float T, float *x) {
-    x[0] = logf(svm / j.A);
-    x[1] = eps;
-    x[2] = log1pf(epsd * j.inv_epsdot_ref);
-    x[3] = (T - j.Tref) * j.inv_dT;
+// ---- batch inference, one warp per sample (the fused step's in-epilogue form) ----------------------
+__global__ void __launch_bounds__(256) k_mlp_predict_warp(MlpDev m, const float *__restrict__ x, int64_t n,
+                                                         float *__restrict__ y) {
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
+        const float4 q = __ldg((const float4 *)x + i);   // the same sample in every lane: warp-uniform loop
+        const float xr[kMlpIn] = {q.x, q.y, q.z, q.w};
+        float xn[kMlpIn];
+        normalise(m, xr, xn);
+        const float yh = mlp_forward_warp(m, xn);
+        if ((threadIdx.x & 31) == 0) y[i] = yh * m.y_std + m.y_mean;
+    }
 }
 
+// ---- warm-started return mapping of the fused FP32 step (tensor-core form) -----------------------
 __global__ void __launch_bounds__(kTile, 1)
     k_jc_warm(KConsts K, SortedFields32 B, FixedFields32 F, const ToolDev *__restrict__ tool, MlpDev m,
               int32_t *__restrict__ secant_iters, uint32_t *status) {
@@ -351,25 +346,13 @@ __global__ void __launch_bounds__(kTile, 1)
     uint32_t tmem;
     fwd_setup(sh, m, tmem);
     uint32_t phase = 0;
-    const JcF32 &j = K.f.jc;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int e = t * kTile + threadIdx.x;
         const bool valid = e < count;
         const int k = valid ? K.jc_list[e] : 0;
-        float4 S = make_float4(0.f, 0.f, 0.f, 0.f);
-        float p = 0.f, rho = 1.f, eps = 0.f, epsd = 0.f, T = 0.f;
-        JcTrial tr{1.f, 1.f, 1.f};
+        JcWarmState st{};
         float x[kMlpIn] = {0.f, 0.f, 0.f, 0.f}, xn[kMlpIn];
-        if (valid) {
-            S = B.S[k];
-            p = F.p[k];
-            rho = (float)B.rho[k];
-            eps = B.eps_pl[k];
-            epsd = B.eps_pl_dot[k];
-            T = B.T[k];
-            jc_trial_f32(j, S, p, eps, epsd, T, tr);
-            jc_features(j, tr.svm, eps, epsd, T, x);
-        }
+        if (valid) jc_warm_load(K, B, F, k, st, x);
         normalise(m, x, xn);
         bool timeout = false;
         const float yh = forward_tile(sh, tmem, phase, xn, timeout, (K.test_faults & SPH_TEST_SKIP_MMA) != 0);
@@ -377,22 +360,7 @@ __global__ void __launch_bounds__(kTile, 1)
             if (threadIdx.x == 0) set_status(status, SPH_STATUS_MMA_TIMEOUT);
             break;
         }
-        if (!valid) continue;
-        const ToolDev &tc = tool[case_of_hash(K, B.hash[k])];
-        // predicted increment, kept inside (0, |dev S| / 2 mu] (a full return)
-        const float dl_max = tr.norm / (2.f * K.f.G);
-        float dl0 = expf(yh * m.y_std + m.y_mean) * dl_max;
-        dl0 = (dl0 == dl0) ? fminf(fmaxf(dl0, 1e-8f), dl_max) : jc_default_start(epsd, tc.dtf);
-        int it = 0;
-        bool blanked = false;
-        uint32_t st = jc_return_f32(K, j, tc.dtf, tc.inv_dtf, S, rho, eps, epsd, T, blanked, &it, tr, dl0);
-        B.S[k] = S;
-        B.T[k] = T;
-        B.eps_pl[k] = eps;
-        B.eps_pl_dot[k] = epsd;
-        if (blanked) B.blanked[k] = 1.f;
-        if (secant_iters) secant_iters[k] = it;
-        if (st) set_status(status, st);
+        if (valid) jc_warm_finish(K, B, tool, m, k, yh, st, secant_iters, status);
     }
     fwd_teardown(sh, tmem);
 }
@@ -635,6 +603,25 @@ __global__ void __launch_bounds__(kTile, 1)
     }
 }
 
+// BF16 copy of parameter p if it is a weight, and for W2 / W3 also its slot in
+// the packed copy of the warp-per-sample forward pass.
+__device__ __forceinline__ void store_wb(uint16_t *__restrict__ wb, int p, float w) {
+    const uint16_t b = __bfloat16_as_ushort(__float2bfloat16_rn(w));
+    if (p < kMlpOffB1) {
+        wb[kMlpWbW1 + p] = b;
+    } else if (p >= kMlpOffW2 && p < kMlpOffB2) {
+        const int e = p - kMlpOffW2;
+        wb[kMlpWbW2 + e] = b;
+        wb[mlp_packed_slot(0, e / kMlpH, e % kMlpH)] = b;
+    } else if (p >= kMlpOffW3 && p < kMlpOffB3) {
+        const int e = p - kMlpOffW3;
+        wb[kMlpWbW3 + e] = b;
+        wb[mlp_packed_slot(1, e / kMlpH, e % kMlpH)] = b;
+    } else if (p >= kMlpOffW4 && p < kMlpOffB4) {
+        wb[kMlpWbW4 + (p - kMlpOffW4)] = b;
+    }
+}
+
 // Sum of the per-CTA partials in CTA order (deterministic); with `adam`, one
 // Adam step on the FP32 parameters and refreshed BF16 weight copies.
 __global__ void k_mlp_reduce_adam(const float *__restrict__ part, int nparts, float *__restrict__ grad_out,
@@ -657,23 +644,13 @@ __global__ void k_mlp_reduce_adam(const float *__restrict__ part, int nparts, fl
     m2[p] = b;
     const float w = params[p] - lr * (a * c1) / (sqrtf(b * c2) + eps);
     params[p] = w;
-    int q = -1;
-    if (p < kMlpOffB1) q = kMlpWbW1 + p;
-    else if (p >= kMlpOffW2 && p < kMlpOffB2) q = kMlpWbW2 + (p - kMlpOffW2);
-    else if (p >= kMlpOffW3 && p < kMlpOffB3) q = kMlpWbW3 + (p - kMlpOffW3);
-    else if (p >= kMlpOffW4 && p < kMlpOffB4) q = kMlpWbW4 + (p - kMlpOffW4);
-    if (q >= 0) wb[q] = __bfloat16_as_ushort(__float2bfloat16_rn(w));
+    store_wb(wb, p, w);
 }
 
 __global__ void k_mlp_refresh_wb(const float *__restrict__ params, uint16_t *__restrict__ wb) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= kMlpParams) return;
-    int q = -1;
-    if (p < kMlpOffB1) q = kMlpWbW1 + p;
-    else if (p >= kMlpOffW2 && p < kMlpOffB2) q = kMlpWbW2 + (p - kMlpOffW2);
-    else if (p >= kMlpOffW3 && p < kMlpOffB3) q = kMlpWbW3 + (p - kMlpOffW3);
-    else if (p >= kMlpOffW4 && p < kMlpOffB4) q = kMlpWbW4 + (p - kMlpOffW4);
-    if (q >= 0) wb[q] = __bfloat16_as_ushort(__float2bfloat16_rn(params[p]));
+    store_wb(wb, p, params[p]);
 }
 
 }  // namespace
@@ -693,6 +670,10 @@ cudaError_t mlp_configure() {
 void launch_mlp_predict(cudaStream_t s, const MlpDev &m, const float *x, int64_t n, float *y, uint32_t *status,
                         int grid) {
     k_mlp_predict<<<grid, kTile, sizeof(FwdSmem), s>>>(m, x, n, y, status);
+}
+
+void launch_mlp_predict_warp(cudaStream_t s, const MlpDev &m, const float *x, int64_t n, float *y, int grid) {
+    k_mlp_predict_warp<<<grid, 256, 0, s>>>(m, x, n, y);
 }
 
 void launch_jc_warm(cudaStream_t s, int grid, const KConsts &K, const SortedFields32 &B, const FixedFields32 &F,

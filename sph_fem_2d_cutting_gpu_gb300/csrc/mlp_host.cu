@@ -150,7 +150,7 @@ int sph_mlp_create(int32_t device, uint64_t seed, sph_mlp **out) {
     MALLOC(m->params, kMlpParams);
     MALLOC(m->m1, kMlpParams);
     MALLOC(m->m2, kMlpParams);
-    MALLOC(m->wb, kMlpWb);
+    MALLOC(m->wb, kMlpWbAll);
     MALLOC(m->grad, kMlpParams + 1);
     MALLOC(m->status, 1);
     MCK(cudaMemset(m->status, 0, sizeof(uint32_t)));
@@ -253,6 +253,21 @@ int sph_mlp_predict(sph_mlp *m, const float *x, int64_t n, float *y) {
     MlpDev d = mlp_view(m, m->params, m->wb);
     const int grid = (int)std::min<int64_t>((n + 127) / 128, 4 * (int64_t)m->num_sms);
     launch_mlp_predict(m->stream, d, b.x, n, b.t, m->status, grid);
+    MCK(cudaGetLastError());
+    MCK(cudaMemcpyAsync(y, b.t, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, m->stream));
+    free_batch(m, b);
+    return check_status(m);
+}
+
+int sph_mlp_predict_warp(sph_mlp *m, const float *x, int64_t n, float *y) {
+    if (!m || !x || !y || n < 0) return SPH_ERR_INVALID;
+    if (n == 0) return SPH_OK;
+    MCK(cudaSetDevice(m->device));
+    Batch b;
+    int r = upload_batch(m, x, nullptr, n, b);
+    if (r) return r;
+    MlpDev d = mlp_view(m, m->params, m->wb);
+    launch_mlp_predict_warp(m->stream, d, b.x, n, b.t, 8 * m->num_sms);
     MCK(cudaGetLastError());
     MCK(cudaMemcpyAsync(y, b.t, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, m->stream));
     free_batch(m, b);

@@ -106,6 +106,15 @@ int build_tool_model(const sph_tool_mesh &mesh, const sph_tool_constants &tc, To
         node_elems[M.elements[e].y].push_back(e);
         node_elems[M.elements[e].z].push_back(e);
     }
+    // ---- node flags: end points of cutting-edge and fixed-edge element edges ----
+    M.node_edge.assign(NN, 0);
+    for (int e = 0; e < NE; e++) {
+        const int nd[3] = {M.elements[e].x, M.elements[e].y, M.elements[e].z};
+        for (int a = 0; a < 3; a++) {   // edge a: nodes a and a + 1
+            if (mesh.cutting_flags[3 * e + a]) M.node_edge[nd[a]] |= 1, M.node_edge[nd[(a + 1) % 3]] |= 1;
+            if (mesh.fixed_flags[3 * e + a]) M.node_edge[nd[a]] |= 2, M.node_edge[nd[(a + 1) % 3]] |= 2;
+        }
+    }
     // ---- colouring: cutting-boundary elements (6 colours), then the rest (18) ----
     std::vector<int> cut_elems, fixed_elems, rest;
     for (int e = 0; e < NE; e++) {
@@ -216,6 +225,8 @@ int build_tool_model(const sph_tool_mesh &mesh, const sph_tool_constants &tc, To
             if (fx) dirichlet_node(el.x);
             if (fy) dirichlet_node(el.y);
             if (fz) dirichlet_node(el.z);
+            M.dirichlet_elem.push_back(e);
+            M.dirichlet_flags.push_back({ff[0], ff[1], ff[2], 0});
         }
     }
     M.M_inv.resize(NN);

@@ -19,6 +19,13 @@ struct ToolModelHost {
     // CSR (zero-based, columns ascending per row)
     std::vector<int> row_ptr, col_ind, diag;
     std::vector<double> K, M, M_inv, f, T;
+    // the Dirichlet elimination's processing order (colour by colour, then
+    // element order): element and its fixed-edge flags (x, y, z; w unused)
+    std::vector<int> dirichlet_elem;
+    std::vector<Int4> dirichlet_flags;
+    // per node: bit 0 on a cutting edge, bit 1 on a fixed edge (the mesh
+    // reader's cutting_edge_flag / fixed_edge_flag, mesh_structure_GPU.cu:430-471)
+    std::vector<int> node_edge;
     // interface segments
     int n_seg = 0;
     std::vector<double> left, right, normal;   // [n_seg][2]

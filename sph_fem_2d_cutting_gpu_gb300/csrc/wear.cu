@@ -182,4 +182,83 @@ void launch_wear_adjustment(cudaStream_t s, const KConsts &K, const FemDev &F, c
     k_wear_segments_flank<<<1, kFlankThreads, 0, s>>>(F, seg, tool);
 }
 
+// ---- remesh_low_level (tool_FEM.cu:1696-1705) -----------------------------------------------
+// do_mesh_shift (tool_FEM.cu:589-616): the nodes on neither the cutting nor the
+// fixed edge follow the flank wear -- a shift of at least 6.5e-6 cm, weighted by
+// the node's place between the tool's top-left and bottom-right points.
+__global__ void __launch_bounds__(kBlock) k_mesh_shift(int N, int freq, double2 *__restrict__ pos,
+                                                       const int32_t *__restrict__ node_edge,
+                                                       const ToolDev *__restrict__ tool) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N || node_edge[i] != 0) return;
+    const ToolDev &t = tool[0];
+    double shift_value = t.flank_retreat * 1.0 * freq;
+    shift_value = fmin(shift_value, -0.0000065);
+    const double2 p = pos[i];
+    const double tlx = t.tl_point_ref[0], tly = t.tl_point_ref[1], brx = t.br_point[0], bry = t.br_point[1];
+    const double weight_y = (p.x - tlx) / (brx - tlx);
+    const double weight_x = fmin(1.0, (p.y - tly) / (bry - tly));
+    const double center_KT = 0.94;
+    double x = p.x, y = p.y;
+    if (weight_x <= center_KT)
+        x += 1.45 * shift_value * (pow(center_KT, 0.7) - pow(fabs(weight_x - center_KT), 0.55)) * weight_y * weight_y *
+             weight_y;
+    else if (weight_x < 1.1 && weight_x > center_KT)
+        x += 1.45 * shift_value * (pow(center_KT, 0.7) - pow(fabs(weight_x - center_KT), 0.55)) * weight_y * weight_y;
+    if (weight_y < 1.01)
+        y += -0.9 * shift_value * fmin(pow(weight_y, 6), 1.) * pow(weight_x, 6);
+    else if (weight_y >= 0.99)
+        y += -0.9 * shift_value * fmin(pow(weight_y, 6), 1.) * weight_x * weight_x * weight_x * weight_x;
+    pos[i] = make_double2(x, y);
+}
+
+// do_nodal_value_interpolation_old + value_interpolation_in_layer_element
+// (tool_FEM.cu:57-107,434-443): each node's new temperature from the first
+// element of the old mesh (in element order) that holds its new position, by
+// the barycentric weights of that element; its old value when none does.
+__global__ void __launch_bounds__(kBlock) k_nodal_interpolation(int N, int n_elem, const int4 *__restrict__ elements,
+                                                                const double2 *__restrict__ pos_old,
+                                                                const double *__restrict__ T_old,
+                                                                const double2 *__restrict__ pos,
+                                                                double *__restrict__ T) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const double2 x_ = pos[i];
+    auto cross = [](double ax, double ay, double bx, double by) { return ax * by - ay * bx; };
+    for (int e = 0; e < n_elem; e++) {
+        const int4 el = elements[e];
+        const double2 xA = pos_old[el.x];
+        const double xBx = pos_old[el.y].x - xA.x, xBy = pos_old[el.y].y - xA.y;
+        const double xCx = pos_old[el.z].x - xA.x, xCy = pos_old[el.z].y - xA.y;
+        const double xPx = x_.x - xA.x, xPy = x_.y - xA.y;
+        const double xBCx = xBx - xCx, xBCy = xBy - xCy;
+        const double d = cross(xBx, xBy, xCx, xCy);
+        if (fabs(d) > 1e-13) {
+            const double wA = cross(xBx, xBy, xCx, xCy) + cross(xPx, xPy, xBCx, xBCy);
+            const double wB = cross(xPx, xPy, xCx, xCy);
+            const double wC = -cross(xPx, xPy, xBx, xBy);
+            if (wA >= 0 && wB >= 0 && wC >= 0 && wA <= 1 && wB <= 1 && wC <= 1) {
+                T[i] = (T_old[el.x] * wA + T_old[el.y] * wB + T_old[el.z] * wC) / d;
+                return;
+            }
+        }
+    }
+    T[i] = T_old[i];
+}
+
+void launch_remesh_low_level(cudaStream_t s, const FemDev &F, const int4 *elements, int n_elem, int n_colors,
+                             const int32_t *node_edge, const ToolDev *tool, int freq, const int32_t *dir_elems,
+                             const int4 *dir_flags, int n_dir, const sph_tool_constants &tc, double2 *pos_old,
+                             double *T_old) {
+    // mapping_data_copy (tool_FEM.cu:1611-1622)
+    cudaMemcpyAsync(pos_old, F.position, sizeof(double2) * (size_t)F.n_nodes, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(T_old, F.T, sizeof(double) * (size_t)F.n_nodes, cudaMemcpyDeviceToDevice, s);
+    k_mesh_shift<<<div_up(F.n_nodes, kBlock), kBlock, 0, s>>>(F.n_nodes, freq, F.position, node_edge, tool);
+    // reset_FEM_matrix + stiffness_mass_matrix_construction + dirichlet_bdc + inverse_mass_matrix
+    launch_fem_assemble(s, F, elements, n_elem, n_colors, dir_elems, dir_flags, n_dir, tc.cp, tc.rho, tc.k, tc.T0,
+                        F.M);
+    k_nodal_interpolation<<<div_up(F.n_nodes, kBlock), kBlock, 0, s>>>(F.n_nodes, n_elem, elements, pos_old, T_old,
+                                                                       F.position, F.T);
+}
+
 }  // namespace sphfem

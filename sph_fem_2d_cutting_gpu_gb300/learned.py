@@ -106,6 +106,13 @@ class Mlp:
         self._ck(self.lib.sph_mlp_predict(self.h, abi.ptr(x), len(x), abi.ptr(y)), "sph_mlp_predict")
         return y
 
+    def predict_warp(self, x):
+        """predict through the warp-per-sample form of the fused step's epilogue."""
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.zeros(len(x), np.float32)
+        self._ck(self.lib.sph_mlp_predict_warp(self.h, abi.ptr(x), len(x), abi.ptr(y)), "sph_mlp_predict_warp")
+        return y
+
     def gradients(self, x, t):
         x = np.ascontiguousarray(x, np.float32)
         t = np.ascontiguousarray(t, np.float32)

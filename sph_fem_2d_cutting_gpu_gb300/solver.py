@@ -298,8 +298,11 @@ class Solver:
                  "sph_jc_stats")
         return int(out[0]), int(out[1])
 
-    def attach_mlp(self, mlp):
-        """Start the FP32K return mappings from the network's prediction (None detaches)."""
+    def attach_mlp(self, mlp, inference: int = abi.SPH_MLP_WARP):
+        """Start the FP32K return mappings from the network's prediction (None
+        detaches); `inference`: SPH_MLP_WARP (in the neighbour-sum epilogue) or
+        SPH_MLP_TENSOR (a tensor-core tile kernel after it)."""
+        self._ck(self.lib.sph_mlp_set_inference(self.ctx, inference), "sph_mlp_set_inference")
         self._ck(self.lib.sph_mlp_attach(self.ctx, mlp.h if mlp is not None else None), "sph_mlp_attach")
 
     def __getattr__(self, name):
@@ -392,8 +395,9 @@ class Batch:
         self._ck(self.lib.sph_status(self.ctx, C.byref(s), 1 if clear else 0), "sph_status")
         return s.value
 
-    def attach_mlp(self, mlp):
+    def attach_mlp(self, mlp, inference: int = abi.SPH_MLP_WARP):
         """Start the FP32K return mappings of every case from the network's prediction (None detaches)."""
+        self._ck(self.lib.sph_mlp_set_inference(self.ctx, inference), "sph_mlp_set_inference")
         self._ck(self.lib.sph_mlp_attach(self.ctx, mlp.h if mlp is not None else None), "sph_mlp_attach")
 
     def reduce(self) -> np.ndarray:

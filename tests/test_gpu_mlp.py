@@ -27,15 +27,33 @@ def net_with(p, norm):
     return m
 
 
+@pytest.mark.parametrize("form", ["tensor", "warp"])
 @pytest.mark.parametrize("n", [5, 128, 1000, 40_000])
-def test_forward_matches_oracle(lib, n):
+def test_forward_matches_oracle(lib, n, form):
+    """tensor: the tcgen05 tile kernel; warp: the warp-per-sample form the
+    fused step runs in its epilogue (the packed W2 / W3 copy included)."""
     p, norm = random_net(7)
     x, _ = data(n, 8)
     m = net_with(p, norm)
-    y = m.predict(x)
+    y = m.predict(x) if form == "tensor" else m.predict_warp(x)
     y_ref, _, _ = oracle.mlp_eval(p, norm, x, bf16=True)
     assert rel(y, y_ref) < 5e-3
     m.close()
+
+
+def test_warp_form_tracks_training(lib):
+    """The packed weight copy follows every Adam step: after training, both
+    forms agree with each other and with the oracle on the trained weights."""
+    p, norm = random_net(3)
+    x, t = data(4096, 9)
+    m = net_with(p, norm)
+    m.train(x, t, epochs=2, batch=512, lr=1e-3, seed=4)
+    p2, _ = m.params()
+    y_ref, _, _ = oracle.mlp_eval(p2.astype(np.float64), norm, x, bf16=True)
+    yt, yw = m.predict(x), m.predict_warp(x)
+    m.close()
+    assert rel(yt, y_ref) < 5e-3 and rel(yw, y_ref) < 5e-3
+    assert rel(yw, yt) < 5e-3
 
 
 @pytest.mark.parametrize("n", [100, 128 * 400 + 17])
@@ -87,8 +105,10 @@ def warm_case():
     return setups.placed(c, preload_dx=0.5)
 
 
-def test_warm_start_run(lib):
-    """Log the plain FP32K run, train on it, rerun with the warm start: fewer
+@pytest.mark.parametrize("inference", [abi.SPH_MLP_WARP, abi.SPH_MLP_TENSOR])
+def test_warm_start_run(lib, inference):
+    """Log the plain FP32K run, train on it, rerun with the warm start (in the
+    neighbour-sum epilogue, or in the tensor-core kernel after it): fewer
     secant iterations per return mapping, same results within the secant
     tolerance's effect."""
     case = warm_case()
@@ -110,7 +130,7 @@ def test_warm_start_run(lib):
     losses = m.train(x, t, epochs=30, batch=2048, lr=2e-3, seed=2)
     assert losses[-1] < 0.5 * losses[0]
     warm = Solver(case, abi.SPH_PREC_FP32K, place_tool=False)
-    warm.attach_mlp(m)
+    warm.attach_mlp(m, inference)
     warm.jc_stats(True, reset=True)
     warm.step(steps)
     assert warm.status() & abi.STATUS_BITS["secant_maxiter"] == 0

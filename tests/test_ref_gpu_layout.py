@@ -27,7 +27,9 @@ STRUCTS = [
     (ref_gpu.SegmentGPU, "segment_gpu", None),
     (ref_gpu.CircleSegmentGPU, "circle_segment_gpu", None),
     (ref_gpu.LineGPU, "line_gpu", None),
-    (ref_gpu.MeshGPU, "mesh_GPU_m", {"position": "position"}),
+    (ref_gpu.MeshGPU, "mesh_GPU_m", {f: f for f in ("position", "cutting_edge_flag", "fixed_edge_flag", "T_nodes",
+                                                    "f", "k", "position_mapping", "node_num_mapping",
+                                                    "csr_row_ptr", "csr_col_ind")}),
 ]
 SKIP_FIELDS = {"vptr", "pad", "head", "tail"}
 
