@@ -61,8 +61,8 @@ NCU_TRAFFIC_PER_PARTICLE = {"fp32k": (689_433_344 + 397_072_128) / 4_194_304}
 # Floating-point work per particle of the fused neighbour sums, from ncu's SASS
 # instruction counters (dadd + dmul + 2 dfma; fadd + fmul + 2 ffma) on the
 # 512x512 micro workload with 2h cells (262,144 particles): k_interact64 executes
-# 1,401,475,197 FP64 flops, k_interact32 1,454,251,763 FP32 flops.
-NCU_FLOPS_PER_PARTICLE = {"fp64": 1_401_475_197 / 262_144, "fp32k": 1_454_251_763 / 262_144}
+# 1,401,475,197 FP64 flops, k_interact32 (compact state, 128x6) 1,402,179,265 FP32 flops.
+NCU_FLOPS_PER_PARTICLE = {"fp64": 1_401_475_197 / 262_144, "fp32k": 1_402_179_265 / 262_144}
 # Nominal GB300 rates (no measured figure exists for these pipes): FP64 1.25 TFLOP/s;
 # FP32 152 SMs x 128 lanes x 2 flops x 2.07 GHz = 80.5 TFLOP/s.
 NOMINAL_TFLOPS = {"fp64": 1.25, "fp32k": 80.5}
@@ -181,8 +181,9 @@ def run_reference(args):
     from sph_fem_2d_cutting_gpu_gb300 import setups
     from oracle.oracle import OracleSim, num_threads
     case = setups.micro(n_side=args.n_side, seed=args.seed, cell_factor=args.cell_factor, stencil=args.stencil)
-    # bounded sample: a square sub-lattice of the workload sized for ~2 s per step
-    side = min(args.n_side, args.ref_side)
+    # the whole workload (one oracle step of the 2048 x 2048 lattice takes about 0.9 s on
+    # 16 Grace cores); --ref-side bounds it to a square sub-lattice on slower hosts
+    side = min(args.n_side, args.ref_side) if args.ref_side > 0 else args.n_side
     sub = setups.micro(n_side=side, seed=args.seed, cell_factor=args.cell_factor, stencil=args.stencil)
     o = OracleSim(sub.constants, sub.grid, sub.particles, sub.dt)
     for _ in range(args.warmup):
@@ -202,8 +203,10 @@ def run_reference(args):
                                "leap-frog step without tool", "particles": case.N,
                    "sample_particles": sub.N},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": num_threads(), "kind": "port",
-                         "sample": f"{args.steps} whole steps of a {side}x{side} sub-lattice of the workload "
-                                   f"(reference CPU restatement, OpenMP)"},
+                         "sample": (f"{args.steps} whole steps of the full workload" if side == args.n_side else
+                                    f"{args.steps} whole steps of a {side}x{side} sub-lattice of the workload")
+                                   + " (reference CPU restatement, OpenMP)"},
+        "same_config": side == args.n_side,
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -234,7 +237,7 @@ def time_batch(b, local, warmup, steps):
     return e0.elapsed_time(e1) / steps, ext
 
 
-def run_sweep_full(args, local, cases, variant, mlp):
+def run_sweep_full(args, local, cases, tuned, mlp):
     """The batched sweep at its stated length: all cases for `sweep_steps` steps
     in FP32K (force and peak temperature of every case every `sweep_every`
     steps, status after the run), three of them (smallest, median, largest) run
@@ -248,8 +251,8 @@ def run_sweep_full(args, local, cases, variant, mlp):
 
     steps, every = args.sweep_steps, args.sweep_every
     b = Batch(cases, abi.SPH_PREC_FP32K, device=local)
-    if variant is not None:
-        tune.set_variant(b, variant)
+    if tuned is not None:
+        tune.apply(b, tuned)
     ext = stream_of(b, local)
     hist, ms = [], 0.0
     for _ in range(steps // every):
@@ -299,8 +302,8 @@ def run_sweep_full(args, local, cases, variant, mlp):
     torch.cuda.empty_cache()
     if mlp is not None:
         b = Batch(cases, abi.SPH_PREC_FP32K, device=local)
-        if variant is not None:
-            tune.set_variant(b, variant)
+        if tuned is not None:
+            tune.apply(b, tuned)
         msp, _ = time_batch(b, local, args.warmup, args.steps)
         b.attach_mlp(mlp)
         msm, _ = time_batch(b, local, args.warmup, args.steps)
@@ -336,7 +339,7 @@ def run_batched(args, local, max_over_ranks, barrier, mlp=None):
         cases = [tune.with_geometry(c, tuned["cell_factor"], tuned["stencil"]) for c in cases]
     b = Batch(cases, abi.SPH_PREC_FP32K, device=local)
     if tuned is not None:
-        tune.set_variant(b, tuned["variant"])
+        tune.apply(b, tuned)
     stream_ptr = C.c_void_p()
     b.lib.sph_get_stream(b.ctx, C.byref(stream_ptr))
     ext = torch.cuda.ExternalStream(stream_ptr.value, device=torch.device("cuda", local))
@@ -370,7 +373,7 @@ def run_batched(args, local, max_over_ranks, barrier, mlp=None):
     b.close()
     torch.cuda.empty_cache()
     if args.sweep_steps > 0:
-        out["sweep_run"] = run_sweep_full(args, local, cases, None if tuned is None else tuned["variant"], mlp)
+        out["sweep_run"] = run_sweep_full(args, local, cases, tuned, mlp)
     return out
 
 
@@ -383,7 +386,7 @@ def run_small_cut(args, local):
 
     import torch
 
-    from sph_fem_2d_cutting_gpu_gb300 import abi, setups
+    from sph_fem_2d_cutting_gpu_gb300 import abi, setups, tune
     from sph_fem_2d_cutting_gpu_gb300.solver import Solver
     from oracle.oracle import OracleSim, num_threads
 
@@ -419,6 +422,19 @@ def run_small_cut(args, local):
         row[name + "_wear"] = {"ms_per_step": msw, "value": case.N / (msw * 1e-3),
                                "launches_per_step": (s.launch_count() - n0) / steps, "status": s.status()}
         s.set_wear(abi.SPH_WEAR_OFF, None)
+        if prec == abi.SPH_PREC_FP32K:   # the same step as one persistent launch
+            tune.set_step_form(s, abi.SPH_STEP_PERSISTENT)
+            s.step(args.warmup)
+            s.sync()
+            n0 = s.launch_count()
+            e0.record(ext)
+            s.step(steps)
+            e1.record(ext)
+            e1.synchronize()
+            msp = e0.elapsed_time(e1) / steps
+            row["fp32k_persistent"] = {"ms_per_step": msp, "value": case.N / (msp * 1e-3),
+                                       "launches_per_step": (s.launch_count() - n0) / steps, "status": s.status()}
+            tune.set_step_form(s, abi.SPH_STEP_LAUNCHES)
         if prec == abi.SPH_PREC_FP64 and not args.no_cpu:
             P = s.download()
             ts = s.tool_state()
@@ -438,6 +454,42 @@ def run_small_cut(args, local):
     row["workload"] = ("Ti6Al4V orthogonal cut, 200 x 60 particles (dx 5 um, h 1.7 dx), FEM tool of about 2,000 "
                        "nodes (rake 0, clearance 7 deg, r 5 um), 70 m/min, uncut chip 80 um")
     return row
+
+
+
+def run_tiny_sweep(args, local):
+    """Many tiny cases in one batched context (16 AISI 1045 cuts of 3,000 to
+    12,000 particles, each with its own FEM tool): the fused FP32K step as its
+    chain of graph-replayed launches and as one persistent launch."""
+    import torch
+
+    from sph_fem_2d_cutting_gpu_gb300 import abi, setups, tune
+    from sph_fem_2d_cutting_gpu_gb300.solver import Batch
+
+    cases = setups.batched_sweep(n_cases=16, seed=args.seed + 1, n_min=3000, n_max=12000, height=0.025)
+    b = Batch(cases, abi.SPH_PREC_FP32K, device=local)
+    ext = stream_of(b, local)
+    steps = max(args.steps, 50)
+    out = {"workload": f"{b.n_cases} AISI 1045 cuts of {min(c.N for c in cases)}-{max(c.N for c in cases)} "
+                       f"particles ({b.N} in all), own FEM tool each ({sum(i['node_count'] for i in b.info)} "
+                       "nodes in all), FP32K", "particles": b.N, "cases": b.n_cases}
+    for name, form in (("launches", abi.SPH_STEP_LAUNCHES), ("persistent", abi.SPH_STEP_PERSISTENT)):
+        tune.set_step_form(b, form)
+        b.step(args.warmup)
+        b.sync()
+        n0 = b.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        b.step(steps)
+        e1.record(ext)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out[name] = {"ms_per_step": ms, "value": b.N / (ms * 1e-3),
+                     "launches_per_step": (b.launch_count() - n0) / steps, "status": b.status()}
+    b.close()
+    torch.cuda.empty_cache()
+    out["persistent_speedup"] = out["launches"]["ms_per_step"] / out["persistent"]["ms_per_step"]
+    return out
 
 
 def run_rigid(args, local):
@@ -507,7 +559,7 @@ def curve_run(s, steps, every, ext, log_records=0):
     logged until that many states are held; those chunks are timed apart."""
     import torch
 
-    hist, ms_run, ms_log, n_run, n_log = [], 0.0, 0.0, 0, 0
+    hist, chunk_ms, ms_run, ms_log, n_run, n_log = [], [], 0.0, 0.0, 0, 0
     logging = log_records > 0
     if logging:
         s.jc_log_enable(log_records)
@@ -519,6 +571,7 @@ def curve_run(s, steps, every, ext, log_records=0):
         s.step(every)
         e1.record(ext)
         e1.synchronize()
+        chunk_ms.append(e0.elapsed_time(e1))
         if logging:
             ms_log += e0.elapsed_time(e1)
             n_log += every
@@ -536,7 +589,7 @@ def curve_run(s, steps, every, ext, log_records=0):
         s.jc_log_enable(0)
     calls, iters = s.jc_stats(True, reset=True)
     # a run that logged throughout has only its logging chunks to time
-    return dict(hist=hist, ms_per_step=(ms_run / n_run) if n_run else ms_log / max(n_log, 1),
+    return dict(hist=hist, chunk_ms=chunk_ms, ms_per_step=(ms_run / n_run) if n_run else ms_log / max(n_log, 1),
                 ms_per_step_logging=(ms_log / n_log) if n_log else None, steps_logging=n_log,
                 returns=calls, iters_per_return=iters / max(calls, 1), status=s.status()), rec
 
@@ -609,12 +662,16 @@ def run_config3(args, local):
                         np.float32(1e-8))
     err_mlp = np.abs(dl_mlp - dl_true) / dl_true
     err_ref = np.abs(dl_ref - dl_true) / dl_true
-    s, ext = solver(abi.SPH_PREC_FP32K)
-    s.attach_mlp(m)
-    runs["fp32k_mlp"], _ = curve_run(s, steps, every, ext)
-    s.close()
-    torch.cuda.empty_cache()
+    for name, mode in (("fp32k_mlp", abi.SPH_MLP_WARP), ("fp32k_mlp_tensor", abi.SPH_MLP_TENSOR)):
+        s, ext = solver(abi.SPH_PREC_FP32K)
+        s.attach_mlp(m, mode)
+        runs[name], _ = curve_run(s, steps, every, ext)
+        s.close()
+        torch.cuda.empty_cache()
     ms64 = runs["fp64"]["ms_per_step"]
+    # every form timed over the same window: the steps after the FP32K run's logging
+    w0 = runs["fp32k"]["steps_logging"] // every
+    window = {n: sum(r["chunk_ms"][w0:]) / max((len(r["chunk_ms"]) - w0) * every, 1) for n, r in runs.items()}
     curve = [{"step": (k + 1) * every, **{f"{n}": {"force": list(r["hist"][k][:2]), "peak_T": r["hist"][k][2]}
                                          for n, r in runs.items()}} for k in range(steps // every)]
     T64 = [h[2] for h in runs["fp64"]["hist"]]
@@ -625,11 +682,14 @@ def run_config3(args, local):
         "steps": steps, "every": every, "particles": case.N, "tool_nodes": case.info["nodes"],
         "peak_T_fp64": float(max(T64)), "T_rise_fp64": float(max(T64) - 300.0),
         "peak_force_fp64": float(max(np.hypot(h[0], h[1]) for h in runs["fp64"]["hist"])),
-        "errors_vs_fp64": {n: curve_errors(runs["fp64"]["hist"], runs[n]["hist"]) for n in ("fp32k", "fp32k_mlp")},
+        "errors_vs_fp64": {n: curve_errors(runs["fp64"]["hist"], runs[n]["hist"])
+                           for n in ("fp32k", "fp32k_mlp", "fp32k_mlp_tensor")},
         "ms_per_step": {n: r["ms_per_step"] for n, r in runs.items()},
+        "window_steps": [w0 * every, steps],
+        "ms_per_step_same_window": window,
         "iters_per_return": {n: r["iters_per_return"] for n, r in runs.items()},
         "status": {n: r["status"] for n, r in runs.items()},
-        "speedup_vs_fp64": {n: ms64 / runs[n]["ms_per_step"] for n in ("fp32k", "fp32k_mlp")},
+        "speedup_vs_fp64": {n: window["fp64"] / window[n] for n in ("fp32k", "fp32k_mlp", "fp32k_mlp_tensor")},
         "curve": curve,
     }
     learned_line = {
@@ -651,10 +711,17 @@ def run_config3(args, local):
                         "timed_steps": steps - runs["fp32k"]["steps_logging"]},
         "fp32k_mlp": {"value": case.N / (runs["fp32k_mlp"]["ms_per_step"] * 1e-3),
                       "ms_per_step": runs["fp32k_mlp"]["ms_per_step"], "returns": runs["fp32k_mlp"]["returns"],
-                      "iters_per_return": runs["fp32k_mlp"]["iters_per_return"], "timed_steps": steps},
+                      "iters_per_return": runs["fp32k_mlp"]["iters_per_return"], "timed_steps": steps,
+                      "inference": "warp per yielding particle, in the neighbour-sum epilogue"},
+        "fp32k_mlp_tensor": {"value": case.N / (runs["fp32k_mlp_tensor"]["ms_per_step"] * 1e-3),
+                             "ms_per_step": runs["fp32k_mlp_tensor"]["ms_per_step"],
+                             "returns": runs["fp32k_mlp_tensor"]["returns"],
+                             "iters_per_return": runs["fp32k_mlp_tensor"]["iters_per_return"], "timed_steps": steps,
+                             "inference": "tcgen05 tiles of 128 queued particles, a second kernel"},
         "fp64_plain": {"value": case.N / (ms64 * 1e-3), "ms_per_step": ms64, "returns": runs["fp64"]["returns"],
                        "iters_per_return": runs["fp64"]["iters_per_return"], "timed_steps": steps},
-        "speedup_mlp_vs_fp64": ms64 / runs["fp32k_mlp"]["ms_per_step"],
+        "same_window": {"steps": [w0 * every, steps], "ms_per_step": window},
+        "speedup_mlp_vs_fp64": window["fp64"] / window["fp32k_mlp"],
         "unit": UNIT,
     }
     return config3, learned_line, m
@@ -701,7 +768,13 @@ def run_product(args):
                 tune.set_variant(s, v)
                 variant_table.append(tune._time_steps(s, 2, 4))
             best_v = min(range(len(variant_table)), key=lambda v: variant_table[v])
-            tune.set_variant(s, best_v)
+            tune.set_variant(s, 0)
+            tune.set_step_form(s, abi.SPH_STEP_PERSISTENT)   # the one-launch step (128-particle blocks)
+            persistent_ms = tune._time_steps(s, 2, 4)
+            use_persistent = persistent_ms < variant_table[best_v]
+            if not use_persistent:
+                tune.set_step_form(s, abi.SPH_STEP_LAUNCHES)
+                tune.set_variant(s, best_v)
             s.upload(P0)
             del P0
         # clock samples (every 200 ms) span the loaded period around the timed steps:
@@ -735,10 +808,13 @@ def run_product(args):
         if variant_table is not None:
             from sph_fem_2d_cutting_gpu_gb300 import tune
             shapes = tune.launch_variants()
-            res["launch_tuning"] = {"chosen": {"block": shapes[best_v][0], "min_blocks": shapes[best_v][1],
-                                               "staged_records": shapes[best_v][2]},
+            res["launch_tuning"] = {"chosen": ({"step_form": "persistent", "block": 128, "min_blocks": 6,
+                                                "staged_records": 0} if use_persistent else
+                                               {"step_form": "launches", "block": shapes[best_v][0],
+                                                "min_blocks": shapes[best_v][1], "staged_records": shapes[best_v][2]}),
                                     "ms_per_step": {f"{b}x{m}" + (f"s{c}" if c else ""): t
-                                                    for (b, m, c), t in zip(shapes, variant_table)}}
+                                                    for (b, m, c), t in zip(shapes, variant_table)},
+                                    "persistent_ms_per_step": persistent_ms}
         # end-to-end through the C ABI with pinned host buffers
         if not args.no_e2e:
             fields = {}
@@ -849,9 +925,11 @@ def run_product(args):
         torch.cuda.empty_cache()
     if mlp is not None:
         mlp.close()
-    small_line = None
+    small_line = tiny_line = None
     if not args.no_small and rank == 0:
         small_line = run_small_cut(args, local)
+        torch.cuda.empty_cache()
+        tiny_line = run_tiny_sweep(args, local)
         torch.cuda.empty_cache()
     rigid_line = None
     if args.rigid_ny and rank == 0:
@@ -911,6 +989,8 @@ def run_product(args):
         line["rigid_tool_cut"] = rigid_line
     if small_line is not None:
         line["ti64_cut_small"] = small_line
+    if tiny_line is not None:
+        line["tiny_sweep"] = tiny_line
     if not args.no_cpu:
         v, cores, n, el = cpu_sample(case, max_seconds=args.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -930,7 +1010,7 @@ def parse_args(argv=None):
     ap.add_argument("--impl", default="product", choices=["product", "reference"])
     ap.add_argument("--precision", default="both", choices=["both", "fp32k", "fp64"])
     ap.add_argument("--n-side", type=int, default=2048)
-    ap.add_argument("--ref-side", type=int, default=1024)
+    ap.add_argument("--ref-side", type=int, default=0)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=40,

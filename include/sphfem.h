@@ -55,6 +55,7 @@ enum {
 #define SPH_STATUS_CELL_OVERFLOW  (1u << 7) /* a cell held more particles than the in-cell ranker allows  */
 #define SPH_STATUS_MMA_TIMEOUT    (1u << 8) /* a tensor-core wait of the learned warm start gave up (1 s)  */
 #define SPH_STATUS_COPY_TIMEOUT   (1u << 9) /* a staged neighbour copy did not complete in 1 s (global loads used) */
+#define SPH_STATUS_GRID_TIMEOUT   (1u << 10) /* a grid-wide barrier of the persistent step gave up (1 s)     */
 
 /* ---- precision of the particle path ------------------------------------ */
 enum {
@@ -491,9 +492,21 @@ int sph_mlp_set_inference(sph_ctx *ctx, int32_t mode);
  * (threads per block, minimum resident blocks per SM, and the number of
  * neighbour records a block stages in shared memory -- 0 for global loads);
  * an autotuner times the step with each and sets the fastest.  Variant 0 is
- * the default. */
+ * the default.
+ * step_form: SPH_STEP_LAUNCHES (default) -- the fused step as its chain of
+ * launches (scan, scatter, rank, gather, FEM, neighbour sums, tool, contact,
+ * tail), replayed from a CUDA graph; SPH_STEP_PERSISTENT -- the same stages in
+ * one cooperative launch with every block resident, separated by bounded
+ * grid-wide barriers (SPH_STATUS_GRID_TIMEOUT if one gives up), captured in the
+ * graph the same way; the same results bit for bit.  FP32K contexts only; a
+ * step it does not cover (the first one after an FP64 upload, wear, the rigid
+ * tool, PSE conduction, SPH_MLP_TENSOR) runs as launches.  The neighbour sums
+ * of the persistent form use 128-particle blocks (interact_variant is ignored). */
+#define SPH_STEP_LAUNCHES 0
+#define SPH_STEP_PERSISTENT 1
 typedef struct sph_launch_config {
     int32_t interact_variant;
+    int32_t step_form;
 } sph_launch_config;
 /* *n: in, capacity of the output arrays (each may be NULL); out, number of variants. */
 int sph_launch_variants(int32_t *n, int32_t *block, int32_t *min_blocks, int32_t *staged_records);
@@ -508,13 +521,17 @@ int sph_get_launch_config(const sph_ctx *ctx, sph_launch_config *cfg);
  * SPH_STATUS_COPY_TIMEOUT and falls back to global loads (same results); with
  * SPH_TEST_SKIP_MMA the learned warm start issues no tensor-core MMA, so its
  * wait runs out, it reports SPH_STATUS_MMA_TIMEOUT, frees its TMEM and leaves
- * the return mappings of that step undone.  secant_cap >= 0 replaces the
+ * the return mappings of that step undone; with SPH_TEST_SKIP_GRID_ARRIVAL
+ * block 0 of the persistent step does not arrive at its first grid barrier,
+ * so every block's wait runs out, the step reports SPH_STATUS_GRID_TIMEOUT
+ * and the launch ends (that step's results are not usable).  secant_cap >= 0 replaces the
  * reference's cap of the return mapping's secant iterations (it stops with
  * SPH_STATUS_SECANT_MAXITER once the iteration counter exceeds the cap: 100
  * in the reference, plasticity.cuh:155-158); < 0 restores it.  faults = 0 and
  * secant_cap = -1 is normal operation. */
 #define SPH_TEST_SKIP_BULK_COPY (1u << 0)
 #define SPH_TEST_SKIP_MMA       (1u << 1)
+#define SPH_TEST_SKIP_GRID_ARRIVAL (1u << 2)
 int sph_set_test_faults(sph_ctx *ctx, uint32_t faults, int32_t secant_cap);
 
 /* ---- per-stage timing ---------------------------------------------------------

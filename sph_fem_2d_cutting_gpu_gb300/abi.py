@@ -30,6 +30,7 @@ STATUS_BITS = {
     "cell_overflow": 1 << 7,
     "mma_timeout": 1 << 8,
     "copy_timeout": 1 << 9,
+    "grid_timeout": 1 << 10,
 }
 
 D = C.c_double
@@ -126,7 +127,12 @@ JC_LOG_WIDTH = 8
 
 
 class LaunchConfig(C.Structure):
-    _fields_ = [("interact_variant", I32)]
+    _fields_ = [("interact_variant", I32), ("step_form", I32)]
+
+
+SPH_STEP_LAUNCHES, SPH_STEP_PERSISTENT = 0, 1
+# sph_set_test_faults
+SPH_TEST_SKIP_BULK_COPY, SPH_TEST_SKIP_MMA, SPH_TEST_SKIP_GRID_ARRIVAL = 1, 2, 4
 
 
 class WearConstants(C.Structure):

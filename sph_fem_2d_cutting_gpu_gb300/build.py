@@ -25,9 +25,9 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-
                      "--expt-relaxed-constexpr",
                      "-Xptxas", "-warn-spills"]
 SOURCES = ["cells.cu", "interactions.cu", "interactions_mlp.cu", "actions.cu", "fem.cu", "context.cu", "toolsetup.cpp",
-           "noalloc.cu", "mlp.cu", "mlp_host.cu", "wear.cu", "vtk.cpp"]
+           "noalloc.cu", "mlp.cu", "mlp_host.cu", "wear.cu", "vtk.cpp", "persistent.cu"]
 HEADERS = ["common.cuh", "physics.cuh", "state.cuh", "launch.cuh", "toolsetup.h", "mlp_host.h", "rigid.cuh", "async.cuh",
-           "p1elem.h", "interact32.cuh", "mlp_warp.cuh"]
+           "p1elem.h", "interact32.cuh", "mlp_warp.cuh", "cells.cuh", "fem.cuh", "tail.cuh"]
 
 
 def nvcc() -> str:

@@ -85,6 +85,8 @@ struct sph_ctx {
     bool mlp_on = false;
     int mlp_mode = SPH_MLP_WARP;   // sph_mlp_set_inference
     int interact_variant = 0;            // launch shape of the fused FP32K neighbour sums
+    int step_form = SPH_STEP_LAUNCHES;   // the fused step as a chain of launches or one persistent launch
+    unsigned *grid_bar = nullptr;        // [4] the persistent step's grid barrier
     double *usui_scratch = nullptr;      // per-block partials of sph_eval_usui
     sph_rigid_tool *rigid_dev = nullptr; // the rigid tool, moved on the device every step (NULL: none)
     // wear by nodal shift (WEAR_NODE_SHIFT): SPH_WEAR_* mode, device layer data
@@ -423,6 +425,14 @@ bool pse_active(const sph_ctx *ctx) { return ctx->K.thermal_pse && ctx->K.c.trml
 // ev (profiling, may be null): events recorded after the sort, the reorder, the
 // FEM half step + PSE, the neighbour sums, the tool updates and the tail
 // (ev[0..5]).
+// The persistent form covers this step: FP32K from the compact state, no wear,
+// rigid tool or PSE conduction, the warm start (if any) in its in-epilogue form.
+bool persistent_step(const sph_ctx *ctx) {
+    return ctx->step_form == SPH_STEP_PERSISTENT && ctx->grid_bar && ctx->K.precision == SPH_PREC_FP32K &&
+           ctx->v32[ctx->cur] && ctx->pr32 && !ctx->K.rigid && !pse_active(ctx) && ctx->wear_mode == SPH_WEAR_OFF &&
+           !(ctx->mlp_on && ctx->mlp_mode == SPH_MLP_TENSOR);
+}
+
 int issue_fused_body(sph_ctx *ctx, int64_t &n, int w, cudaEvent_t *ev = nullptr) {
     const int N = ctx->N;
     cudaStream_t s = ctx->stream;
@@ -430,6 +440,26 @@ int issue_fused_body(sph_ctx *ctx, int64_t &n, int w, cudaEvent_t *ev = nullptr)
     SortedFields &A = ctx->buf[ctx->cur];
     SortedFields &B = ctx->buf[w];
     SortedFields32 &B32 = ctx->c32[w];
+    if (!ev && persistent_step(ctx)) {   // the per-stage profile keeps the separate launches
+        PersistArgs P;
+        P.N = N;
+        P.K = ctx->K;
+        P.X = ctx->X;
+        P.A = ctx->c32[ctx->cur];
+        P.B = B32;
+        P.F32 = ctx->F32;
+        P.perm = ctx->F.idx;
+        P.W = ctx->W;
+        P.seg = ctx->seg;
+        P.fem = ctx->fem;
+        P.tool = ctx->tool_dev;
+        P.mlp = ctx->mlp;
+        P.bar = ctx->grid_bar;
+        CK(launch_step_persistent(s, P, ctx->has_tool, ctx->mlp_on, ctx->num_sms));
+        n += 1;
+        CK_LAUNCH();
+        return SPH_OK;
+    }
     launch_sort_rest(s, N, ctx->X, ctx->K.g, ctx->F.idx, ctx->W.status);
     n += 5;
     if (ev) CK(cudaEventRecord(ev[0], s));
@@ -1930,13 +1960,13 @@ int sph_mlp_attach(sph_ctx *ctx, const sph_mlp *m) {
     CK(mlp_configure());
     if (!ctx->mlp_params) {
         DALLOC(ctx->mlp_params, kMlpParams);
-        DALLOC(ctx->mlp_wb, kMlpWbAll);
+        DALLOC(ctx->mlp_wb, kMlpWb);
         DALLOC(ctx->jc_list, ctx->N);
         DALLOC(ctx->jc_list_count, 1);
     }
     CK(cudaStreamSynchronize(m->stream));
     CK(cudaMemcpy(ctx->mlp_params, m->params, sizeof(float) * kMlpParams, cudaMemcpyDeviceToDevice));
-    CK(cudaMemcpy(ctx->mlp_wb, m->wb, sizeof(uint16_t) * kMlpWbAll, cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(ctx->mlp_wb, m->wb, sizeof(uint16_t) * kMlpWb, cudaMemcpyDeviceToDevice));
     ctx->mlp = mlp_view(m, ctx->mlp_params, ctx->mlp_wb);
     ctx->mlp_on = true;
     ctx->K.jc_list = ctx->jc_list;
@@ -1975,8 +2005,18 @@ int sph_set_launch_config(sph_ctx *ctx, const sph_launch_config *cfg) {
     REQUIRE_CTX();
     if (!cfg || cfg->interact_variant < 0 || cfg->interact_variant >= interact_variant_count())
         return fail(ctx, SPH_ERR_INVALID, "unknown launch variant");
-    if (cfg->interact_variant != ctx->interact_variant) {
+    if (cfg->step_form != SPH_STEP_LAUNCHES && cfg->step_form != SPH_STEP_PERSISTENT)
+        return fail(ctx, SPH_ERR_INVALID, "unknown step form");
+    if (cfg->step_form == SPH_STEP_PERSISTENT && ctx->K.precision != SPH_PREC_FP32K)
+        return fail(ctx, SPH_ERR_STATE, "the persistent step runs the FP32K form");
+    if (cfg->step_form == SPH_STEP_PERSISTENT && !ctx->grid_bar) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        DALLOC(ctx->grid_bar, 4);
+    }
+    if (cfg->interact_variant != ctx->interact_variant || cfg->step_form != ctx->step_form) {
+        CK(cudaStreamSynchronize(ctx->stream));
         ctx->interact_variant = cfg->interact_variant;
+        ctx->step_form = cfg->step_form;
         invalidate_graphs(ctx);
     }
     return SPH_OK;
@@ -1984,7 +2024,8 @@ int sph_set_launch_config(sph_ctx *ctx, const sph_launch_config *cfg) {
 
 int sph_set_test_faults(sph_ctx *ctx, uint32_t faults, int32_t secant_cap) {
     REQUIRE_CTX();
-    if (faults & ~(SPH_TEST_SKIP_BULK_COPY | SPH_TEST_SKIP_MMA)) return fail(ctx, SPH_ERR_INVALID, "unknown test fault");
+    if (faults & ~(SPH_TEST_SKIP_BULK_COPY | SPH_TEST_SKIP_MMA | SPH_TEST_SKIP_GRID_ARRIVAL))
+        return fail(ctx, SPH_ERR_INVALID, "unknown test fault");
     ctx->K.test_faults = faults;
     ctx->K.secant_cap = secant_cap >= 0 ? secant_cap : 100;
     invalidate_graphs(ctx);   // the graphs hold the constants by value
@@ -1994,6 +2035,7 @@ int sph_set_test_faults(sph_ctx *ctx, uint32_t faults, int32_t secant_cap) {
 int sph_get_launch_config(const sph_ctx *ctx, sph_launch_config *cfg) {
     if (!ctx || !cfg) return SPH_ERR_INVALID;
     cfg->interact_variant = ctx->interact_variant;
+    cfg->step_form = ctx->step_form;
     return SPH_OK;
 }
 

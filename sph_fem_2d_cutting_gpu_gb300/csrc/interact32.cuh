@@ -186,12 +186,12 @@ struct StageHdr {
 };
 
 template <class SF>
-__device__ __forceinline__ void stage_issue(int N, int kB, const KConsts &K, const int32_t *__restrict__ offsets,
+__device__ __forceinline__ void stage_issue(int vb, int N, int kB, const KConsts &K, const int32_t *__restrict__ offsets,
                                             const float4 *__restrict__ rec, const SF &B, int cap,
                                             float4 *srec, StageHdr &h, uint32_t mbar) {
     const sph_geom_constants &g = K.g;
     const int R = g.stencil;
-    const int b0 = blockIdx.x * kB;
+    const int b0 = vb * kB;
     const int hf = B.hash[b0], hl = B.hash[min(b0 + kB, N) - 1];
     h.staged = 0;
     if (hf < 0 || hl >= g.num_cell || hl < hf) return;
@@ -227,9 +227,10 @@ __device__ __forceinline__ void stage_issue(int N, int kB, const KConsts &K, con
 // (one contiguous run of rows per column).  Hints only: every range lies
 // inside its array.
 template <class SF, class FF>
-__device__ __forceinline__ void block_prefetch_l2(int N, int kB, const KConsts &K, const int32_t *__restrict__ offsets,
-                                                  const float4 *__restrict__ rec, const SF &B, const FF &F) {
-    const int b0 = blockIdx.x * kB;
+__device__ __forceinline__ void block_prefetch_l2(int vb, int N, int kB, const KConsts &K,
+                                                  const int32_t *__restrict__ offsets, const float4 *__restrict__ rec,
+                                                  const SF &B, const FF &F) {
+    const int b0 = vb * kB;
     const uint32_t n = (uint32_t)min(kB, N - b0);
     prefetch_l2_bulk(B.S + b0, n * (uint32_t)sizeof(B.S[0]));
     prefetch_l2_bulk(B.S_t + b0, n * (uint32_t)sizeof(B.S_t[0]));
@@ -269,16 +270,17 @@ using Fixed32Of = std::conditional_t<kFused, FixedFields32, FixedFields>;
 // kMlp (fused only): the learned warm start of the return mapping in the
 // epilogue, one warp-wide forward pass per yielding particle; every lane of a
 // warp reaches it, so the per-particle body returns from a lambda.
-template <bool kFused, int kB = kBlock, int kMinB = 1, bool kStaged = false, bool kMlp = false>
-__global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, const int32_t *__restrict__ offsets,
-                                                       const float4 *__restrict__ rec, Sorted32Of<kFused> B,
-                                                       Fixed32Of<kFused> F, SegDev seg,
-                                                       const ToolDev *__restrict__ tool,
-                                                       int32_t *__restrict__ secant_iters, uint32_t *status,
-                                                       int cap, MlpDev mlp) {
+// One block of kB particles, vb-th in sorted order (the kernel's blockIdx.x,
+// or a persistent kernel's virtual block).
+template <bool kFused, int kB, bool kStaged, bool kMlp>
+__device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K, const int32_t *__restrict__ offsets,
+                                                 const float4 *__restrict__ rec, const Sorted32Of<kFused> &B,
+                                                 const Fixed32Of<kFused> &F, const SegDev &seg,
+                                                 const ToolDev *__restrict__ tool, int32_t *__restrict__ secant_iters,
+                                                 uint32_t *status, int cap, const MlpDev &mlp) {
     static_assert(kFused || !kMlp, "the warm start is folded into the fused epilogue only");
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (kFused && threadIdx.x == 0) block_prefetch_l2(N, kB, K, offsets, rec, B, F);
+    const int k = vb * kB + threadIdx.x;
+    if (kFused && threadIdx.x == 0) block_prefetch_l2(vb, N, kB, K, offsets, rec, B, F);
     int (*s_list)[kB];
     const float4 *nrec = rec;   // where the neighbour records are read from
     __shared__ StageHdr s_hdr;
@@ -287,7 +289,7 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
     if constexpr (kStaged) {
         extern __shared__ __align__(128) float4 s_dyn[];
         s_list = (int (*)[kB])(s_dyn + 4 * cap);
-        if (threadIdx.x == 0) stage_issue(N, kB, K, offsets, rec, B, cap, s_dyn, s_hdr, smem_u32(&s_mbar));
+        if (threadIdx.x == 0) stage_issue(vb, N, kB, K, offsets, rec, B, cap, s_dyn, s_hdr, smem_u32(&s_mbar));
         __syncthreads();
         if (s_hdr.staged) {
             staged = mbar_wait(smem_u32(&s_mbar), 0);
@@ -583,6 +585,17 @@ __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, cons
     };
     particle();
     if constexpr (kMlp) jc_warm_warp(K, B, F, tool, mlp, k, pending, secant_iters, status);
+}
+
+template <bool kFused, int kB = kBlock, int kMinB = 1, bool kStaged = false, bool kMlp = false>
+__global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, const int32_t *__restrict__ offsets,
+                                                       const float4 *__restrict__ rec, Sorted32Of<kFused> B,
+                                                       Fixed32Of<kFused> F, SegDev seg,
+                                                       const ToolDev *__restrict__ tool,
+                                                       int32_t *__restrict__ secant_iters, uint32_t *status,
+                                                       int cap, MlpDev mlp) {
+    interact32_block<kFused, kB, kStaged, kMlp>(blockIdx.x, N, K, offsets, rec, B, F, seg, tool, secant_iters, status,
+                                                cap, mlp);
 }
 
 template <int kB, int kMinB, bool kStaged, bool kMlp = false>

@@ -138,4 +138,22 @@ void launch_mlp_reduce_adam(cudaStream_t s, const float *part, int nparts, float
                             float eps, float c1, float c2, bool adam);
 void launch_mlp_refresh_wb(cudaStream_t s, const float *params, uint16_t *wb);
 
+// persistent.cu: the fused FP32K step from the compact state as one cooperative
+// launch (A -> B, perm = the sort's idx array; bar: 4 words of device memory)
+struct PersistArgs {
+    int N;
+    KConsts K;
+    SortScratch X;
+    SortedFields32 A, B;
+    FixedFields32 F32;
+    int32_t *perm;
+    StepScratch W;
+    SegDev seg;
+    FemDev fem;
+    ToolDev *tool;
+    MlpDev mlp;
+    unsigned *bar;
+};
+cudaError_t launch_step_persistent(cudaStream_t s, const PersistArgs &P, bool tool, bool mlp, int num_sms);
+
 }  // namespace sphfem

@@ -320,17 +320,23 @@ __global__ void __launch_bounds__(kTile, 1) k_mlp_predict(MlpDev m, const float 
     fwd_teardown(sh, tmem);
 }
 
-// ---- batch inference, one warp per sample (the fused step's in-epilogue form) ----------------------
+// ---- batch inference, 16 samples per warp pass (the fused step's in-epilogue form) -----------------
 __global__ void __launch_bounds__(256) k_mlp_predict_warp(MlpDev m, const float *__restrict__ x, int64_t n,
                                                          float *__restrict__ y) {
+    const int lane = threadIdx.x & 31;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += warps) {
-        const float4 q = __ldg((const float4 *)x + i);   // the same sample in every lane: warp-uniform loop
-        const float xr[kMlpIn] = {q.x, q.y, q.z, q.w};
-        float xn[kMlpIn];
+    for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w * 16 < n; w += warps) {
+        const int64_t i = w * 16 + lane;   // lanes 0..15 hold the samples (warp-uniform loop)
+        const bool valid = lane < 16 && i < n;
+        float xr[kMlpIn] = {0.f, 0.f, 0.f, 0.f}, xn[kMlpIn];
+        if (valid) {
+            const float4 q = __ldg((const float4 *)x + i);
+            xr[0] = q.x; xr[1] = q.y; xr[2] = q.z; xr[3] = q.w;
+        }
         normalise(m, xr, xn);
-        const float yh = mlp_forward_warp(m, xn);
-        if ((threadIdx.x & 31) == 0) y[i] = yh * m.y_std + m.y_mean;
+        const unsigned rows = __ballot_sync(0xffffffffu, valid);
+        const float yh = mlp_forward_warp16(m, rows, xn);
+        if (valid) y[i] = yh * m.y_std + m.y_mean;
     }
 }
 
@@ -603,23 +609,14 @@ __global__ void __launch_bounds__(kTile, 1)
     }
 }
 
-// BF16 copy of parameter p if it is a weight, and for W2 / W3 also its slot in
-// the packed copy of the warp-per-sample forward pass.
+// BF16 copy of parameter p if it is a weight.
 __device__ __forceinline__ void store_wb(uint16_t *__restrict__ wb, int p, float w) {
-    const uint16_t b = __bfloat16_as_ushort(__float2bfloat16_rn(w));
-    if (p < kMlpOffB1) {
-        wb[kMlpWbW1 + p] = b;
-    } else if (p >= kMlpOffW2 && p < kMlpOffB2) {
-        const int e = p - kMlpOffW2;
-        wb[kMlpWbW2 + e] = b;
-        wb[mlp_packed_slot(0, e / kMlpH, e % kMlpH)] = b;
-    } else if (p >= kMlpOffW3 && p < kMlpOffB3) {
-        const int e = p - kMlpOffW3;
-        wb[kMlpWbW3 + e] = b;
-        wb[mlp_packed_slot(1, e / kMlpH, e % kMlpH)] = b;
-    } else if (p >= kMlpOffW4 && p < kMlpOffB4) {
-        wb[kMlpWbW4 + (p - kMlpOffW4)] = b;
-    }
+    int q = -1;
+    if (p < kMlpOffB1) q = kMlpWbW1 + p;
+    else if (p >= kMlpOffW2 && p < kMlpOffB2) q = kMlpWbW2 + (p - kMlpOffW2);
+    else if (p >= kMlpOffW3 && p < kMlpOffB3) q = kMlpWbW3 + (p - kMlpOffW3);
+    else if (p >= kMlpOffW4 && p < kMlpOffB4) q = kMlpWbW4 + (p - kMlpOffW4);
+    if (q >= 0) wb[q] = __bfloat16_as_ushort(__float2bfloat16_rn(w));
 }
 
 // Sum of the per-CTA partials in CTA order (deterministic); with `adam`, one

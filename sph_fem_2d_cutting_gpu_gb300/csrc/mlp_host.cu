@@ -150,7 +150,7 @@ int sph_mlp_create(int32_t device, uint64_t seed, sph_mlp **out) {
     MALLOC(m->params, kMlpParams);
     MALLOC(m->m1, kMlpParams);
     MALLOC(m->m2, kMlpParams);
-    MALLOC(m->wb, kMlpWbAll);
+    MALLOC(m->wb, kMlpWb);
     MALLOC(m->grad, kMlpParams + 1);
     MALLOC(m->status, 1);
     MCK(cudaMemset(m->status, 0, sizeof(uint32_t)));

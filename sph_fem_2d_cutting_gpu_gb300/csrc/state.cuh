@@ -145,15 +145,12 @@ struct StepScratch {
 constexpr int kMlpIn = 4, kMlpH = 64;
 constexpr int kMlpOffW1 = 0, kMlpOffB1 = 256, kMlpOffW2 = 320, kMlpOffB2 = 4416, kMlpOffW3 = 4480,
               kMlpOffB3 = 8576, kMlpOffW4 = 8640, kMlpOffB4 = 8704, kMlpParams = 8705;
-// BF16 weight copies: W1 [64][4], W2 [64][64], W3 [64][64], W4 [64] (kMlpWb
-// values), then W2 and W3 again, packed for the warp-per-sample forward pass
-// (mlp_packed_slot); kMlpWbAll values in all.
+// BF16 weight copies: W1 [64][4], W2 [64][64], W3 [64][64], W4 [64]
 constexpr int kMlpWbW1 = 0, kMlpWbW2 = 256, kMlpWbW3 = 4352, kMlpWbW4 = 8448, kMlpWb = 8512;
-constexpr int kMlpWbPk = 8512, kMlpWbAll = kMlpWbPk + 2 * 64 * 64;
 
 struct MlpDev {
     const float *params;      // [kMlpParams] FP32 (biases are read from here)
-    const uint16_t *wb;       // [kMlpWbAll] BF16 bit patterns of the weights (and the packed copy)
+    const uint16_t *wb;       // [kMlpWb] BF16 bit patterns of the weights
     float x_mean[4], x_inv_std[4], y_mean, y_std;
 };
 

@@ -1,0 +1,285 @@
+// tail.cuh -- per-particle bodies of the step's contact with the FEM tool and
+// of its fused tail (boundary conditions, invalidation, next histogram), and
+// the per-case segment y-bins of the contact search; shared by their kernels
+// (actions.cu) and the persistent step kernel (persistent.cu).
+#pragma once
+
+#include "launch.cuh"
+#include "rigid.cuh"
+
+namespace sphfem {
+
+// ---- actions_gpu.cu:787-824 do_invalidate: the rates tested -----------------------------------------
+__device__ __forceinline__ bool isnaninf(double v) { return is_nan_or_inf(v); }
+
+__device__ __forceinline__ bool invalid_rates(double2 pt, double2 vt, dbl4 St, double rho_t, double T_t) {
+    return isnaninf(pt.x) || isnaninf(pt.y) || isnaninf(vt.x) || isnaninf(vt.y) || isnaninf(St.x) ||
+           isnaninf(St.y) || isnaninf(St.z) || isnaninf(St.w) || isnaninf(rho_t) || isnaninf(T_t);
+}
+// the compact FP32 state: the same test on its FP32 rates
+__device__ __forceinline__ bool invalid_rates(float2 pt, float2 vt, float4 St, float rho_t, float T_t) {
+    return is_nan_or_inf(pt.x) || is_nan_or_inf(pt.y) || is_nan_or_inf(vt.x) || is_nan_or_inf(vt.y) ||
+           is_nan_or_inf(St.x) || is_nan_or_inf(St.y) || is_nan_or_inf(St.z) || is_nan_or_inf(St.w) ||
+           is_nan_or_inf(rho_t) || is_nan_or_inf(T_t);
+}
+
+// ---- y-bins of the interface segments for the contact's ray casting ----------------------------
+// A segment adds a crossing for a particle only if the particle's y lies in the
+// segment's float-rounded y-range [lo, hi] (on_segment_mesh).  Each case's range
+// [y0, y1] of those rounded values is cut into kSegBins bins, and every segment is
+// listed in the bins its [lo, hi] overlaps (one more on each side).  The bin of a
+// y is floor((y - y0) * scale); subtraction, the product and floor are monotone
+// in y, so a particle's bin lies between the bins of lo and hi of any segment
+// that can cross it.  Counting crossings over the particle's bin alone therefore
+// gives the full scan's count (an integer sum: order does not matter).  A bin
+// holding more than kSegBinCap segments is marked -1 and its particles scan all.
+__device__ __forceinline__ int seg_bin_of(double y, double y0, double scale) {
+    const double t = floor((y - y0) * scale);
+    return t < 0. ? 0 : (t >= (double)(kSegBins - 1) ? kSegBins - 1 : (int)t);
+}
+
+// Case c's bins, by the whole block (any block size).
+__device__ __forceinline__ void seg_bins_block(int c, const SegDev &seg, ToolDev *tool) {
+    ToolDev &t = tool[c];
+    __shared__ int cnt[kSegBins];
+    for (int b = threadIdx.x; b < kSegBins; b += blockDim.x) cnt[b] = 0;
+    const double y0 = (double)(float)t.seg_ymin, y1 = (double)(float)t.seg_ymax;
+    const double scale = (y1 > y0) ? (double)kSegBins / (y1 - y0) : 0.;
+    int32_t *list = seg.bin_list + (size_t)c * kSegBins * kSegBinCap;
+    __syncthreads();
+    for (int i = threadIdx.x; i < t.seg_count; i += blockDim.x) {
+        const double2 L = seg.left[t.seg_first + i], R = seg.right[t.seg_first + i];
+        const int b0 = max(seg_bin_of(fminf_d(L.y, R.y), y0, scale) - 1, 0);
+        const int b1 = min(seg_bin_of(fmaxf_d(L.y, R.y), y0, scale) + 1, kSegBins - 1);
+        for (int b = b0; b <= b1; b++) {
+            const int slot = atomicAdd(&cnt[b], 1);
+            if (slot < kSegBinCap) list[b * kSegBinCap + slot] = i;
+        }
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < kSegBins; b += blockDim.x)
+        seg.bin_count[c * kSegBins + b] = cnt[b] <= kSegBinCap ? cnt[b] : -1;
+    if (threadIdx.x == 0) {
+        t.bin_y0 = y0;
+        t.bin_scale = scale;
+        t.key_y0 = order_key(y0);
+        t.key_y1 = order_key(y1);
+        t.key_x1 = order_key(t.seg_xmax + t.seg_dxdy * fmax(fabs(t.seg_ymin), fabs(t.seg_ymax)) *
+                                              2.384185791015625e-7 + 1e-12);
+    }
+}
+
+// inside_judgement over the particle's y-bin (the full scan when it overflowed)
+__device__ __forceinline__ int inside_binned(double2 qp, const SegDev &seg, const ToolDev &tool) {
+    const int b = seg_bin_of(qp.y, tool.bin_y0, tool.bin_scale);
+    const int n = seg.bin_count[b];
+    if (n < 0) return inside_judgement(qp, seg.left, seg.right, seg.n);
+    const int32_t *list = seg.bin_list + b * kSegBinCap;
+    int crossings = 0;
+    for (int k = 0; k < n; k++) {
+        const int i = list[k];
+        crossings += on_segment_mesh(__ldg(seg.left + i), __ldg(seg.right + i), qp);
+    }
+    return crossings & 1;
+}
+
+// ---- contact, one particle: actions_gpu.cu:423-583 (s1) ------------------------------------------
+// seg: the segments of the particle's case (and their y-bins); on_seg comes back
+// as an index into them.
+__device__ __forceinline__ uint32_t contact_s1_one(const KConsts &K, double dt, const SegDev &seg, const ToolDev &tool,
+                                                   double2 pos, double2 vel, double2 &fc, double2 &ft, double2 &nrm,
+                                                   int &on_seg, double &blanked) {
+    int inside = 0;
+    // A segment counts a crossing only if the particle's y lies in its float-rounded
+    // y-range (on_segment_mesh); float rounding is monotone, so a particle outside the
+    // rounded y-range of all segments has no crossing and the scan is skipped.
+    // Likewise right of every segment: a crossing lies right of the segments' largest
+    // x only by the float rounding of the y-range, which moves the interpolated
+    // crossing by at most |dx/dy| * |y| * 2^-24 (bounded here with 2^-22 and an
+    // absolute 1e-12).  (These tests first: all tests are pure, and they spare most
+    // particles the FP64 sqrt.)
+    // With the y-bins built (k_seg_bins), the two bounds come as order keys and the
+    // tests run on the integer pipe.
+    bool near;
+    if (seg.bin_count) {
+        const long long ky = order_key(pos.y);
+        near = ky <= tool.key_y1 && ky >= tool.key_y0 && order_key(pos.x) <= tool.key_x1;
+    } else {
+        near = pos.y <= (double)(float)tool.seg_ymax && pos.y >= (double)(float)tool.seg_ymin &&
+               pos.x <= tool.seg_xmax + tool.seg_dxdy * fmax(fabs(tool.seg_ymin), fabs(tool.seg_ymax)) *
+                                           2.384185791015625e-7 + 1e-12;
+    }
+    if (near) {
+        const double ddx = pos.x - tool.tl_point_ref[0], ddy = pos.y - tool.tl_point_ref[1];
+        if (sqrt(ddx * ddx + ddy * ddy) < 1.05 * tool.ref_dist)
+            inside = seg.bin_count ? inside_binned(pos, seg, tool) : inside_judgement(pos, seg.left, seg.right, seg.n);
+    }
+    if (inside == 0) {
+        fc = make_double2(0., 0.); ft = make_double2(0., 0.); nrm = make_double2(0., 0.);
+        on_seg = -1;
+        return 0u;
+    }
+    double gN = 0.;
+    double2 n_ = make_double2(0., 0.);
+    int seg_no = find_shortest_distance_v1(pos, gN, n_, seg.left, seg.right, seg.normal, seg.n);
+    on_seg = seg_no;
+    if (seg_no == -1) {
+        fc = make_double2(0., 0.); ft = make_double2(0., 0.); nrm = make_double2(0., 0.);
+        on_seg = -1;
+        return SPH_STATUS_CONTACT_NOSEG;
+    }
+    if (gN < -0.00025) {
+        blanked = 1.;
+        fc = make_double2(0., 0.); ft = make_double2(0., 0.); nrm = make_double2(0., 0.);
+        on_seg = -1;
+        return SPH_STATUS_CONTACT_DEEP;
+    }
+    double dt2 = dt * dt;
+    double s1 = -K.c.tool.slave_mass * gN;
+    double2 fN = make_double2(s1 * n_.x / dt2 * K.c.tool.contact_alpha, s1 * n_.y / dt2 * K.c.tool.contact_alpha);
+    double vx = vel.x - tool.vel[0], vy = vel.y - tool.vel[1];
+    double vdn = vx * n_.x + vy * n_.y;
+    double vrx = vx - n_.x * vdn, vry = vy - n_.y * vdn;
+    double am = K.c.tool.contact_alpha * K.c.tool.slave_mass;
+    double kx = am * vrx / dt, ky = am * vry / dt;
+    double fy = K.c.tool.mu * sqrt(fN.x * fN.x + fN.y * fN.y);
+    double fsx = ft.x - kx, fsy = ft.y - ky;
+    double lfs = sqrt(fsx * fsx + fsy * fsy);
+    if (lfs > fy) ft = make_double2(fy * fsx / lfs, fy * fsy / lfs);
+    else ft = make_double2(fsx, fsy);
+    fc = fN;
+    nrm = n_;
+    return 0u;
+}
+
+// ---- contact, one particle: actions_gpu.cu:585-617 (s2) ------------------------------------------
+__device__ __forceinline__ void contact_s2_one(const KConsts &K, double dt, const SegDev &seg,
+                                               const double *__restrict__ T_nodes, int seg_no, double rho, double &T) {
+    int4 mk = seg.marks[seg_no];
+    double T_ = T;
+    double T_seg = 0.5 * (T_nodes[mk.z] + T_nodes[mk.w]);
+    double delta_T = T_seg - T_;
+    double length = sqrtf_d(K.c.tool.slave_mass / rho);
+    atomicAdd(&seg.heat_exchange[seg_no].x, T_ * length);
+    atomicAdd(&seg.heat_exchange[seg_no].y, length);
+    double delta_T_part = delta_T * K.c.tool.h * length / K.c.trml_wp.cp / K.c.tool.slave_mass * dt;
+    if (delta_T_part < 0) T += fmax(delta_T_part, delta_T);
+    else T += fmin(delta_T_part, delta_T);
+}
+
+// ---- the FEM tool's contact of the fused step: actions_gpu.cu:423-617 (s1 + s2) -----------------------
+// Its own pass before the tail: the contact search's registers would otherwise
+// hold down the occupancy of the memory-bound tail for every particle, although
+// only the particles near a tool reach it.  The tail that follows sees the
+// contact's results (forces, segment id, blanking, temperature) in memory, in the
+// order of the reference's step.
+// SF: SortedFields (FP64 state) or SortedFields32 (the compact state of FP32K
+// contexts); the contact search runs in FP64 either way.
+template <class SF>
+__device__ __forceinline__ void contact_fem_one(int i, const KConsts &K, const SF &A, const SegDev &seg,
+                                                const ToolDev *__restrict__ tool, const double *__restrict__ T_nodes,
+                                                uint32_t *status) {
+    if (flag_is_one(A.blanked[i])) return;
+    const double2 pos = A.pos[i];
+    uint32_t st = 0;
+    {
+        // the particle's case: its tool, time step and interface segments
+        const int c = case_of_hash(K, A.hash[i]);
+        const ToolDev &tc = tool[c];
+        SegDev cs = seg;
+        cs.left += tc.seg_first;
+        cs.right += tc.seg_first;
+        cs.normal += tc.seg_first;
+        cs.n = tc.seg_count;
+        if (cs.bin_count) {
+            cs.bin_count += c * kSegBins;
+            cs.bin_list += (size_t)c * kSegBins * kSegBinCap;
+        }
+        double2 fc = d2(A.fc[i]), ft = d2(A.ft[i]), nrm = d2(A.n[i]);
+        int on = A.on_seg[i];
+        double bl = 0.;
+        st |= contact_s1_one(K, tc.dt, cs, tc, pos, d2(A.vel[i]), fc, ft, nrm, on, bl);
+        if (on >= 0) on += tc.seg_first;   // global segment id
+        const bool blanked = flag_is_one(bl);
+        if (blanked) put(A.blanked[i], 1.);
+        put(A.ft[i], ft);
+        put(A.n[i], nrm);
+        A.on_seg[i] = on;
+        put(A.fc[i], fc);   // zeroed for fixed particles by the tail (do_boundary_conditions)
+        if (!blanked && on >= 0 && on < seg.n) {
+            double T = A.T[i];
+            contact_s2_one(K, tc.dt, seg, T_nodes, on, A.rho[i], T);
+            put(A.T[i], T);
+        }
+    }
+    if (st) set_status(status, st);
+}
+
+// ---- fused tail of the step ----------------------------------------------------------------------
+// The tool's contact for one particle -- kMode 2: rigid tool, update_tool_particles
+// and do_compute_contact_forces (tool_gpu.cu:146-216); kMode 0: no tool, or the
+// FEM tool whose contact k_contact_fem has applied just before -- then
+// do_boundary_conditions, do_boundary_conditions_thermal, do_invalidate
+// (actions_gpu.cu:756-824) and (kNextHash) the next step's compute_hashes and
+// the counting-sort histogram (grid.cu:25-42) on the final state.
+template <int kMode, bool kNextHash, class SF>
+__device__ __forceinline__ void step_tail_one(int i, const KConsts &K, const SF &A, const SortScratch &X,
+                                              uint32_t *status) {
+    bool blanked = flag_is_one(A.blanked[i]);
+    const bool bc_fixed = !flag_nonzero(A.tool_particle[i]) && flag_nonzero(A.fixed[i]);   // do_boundary_conditions
+    const bool bc_thermal = K.thermal_bc && flag_is_one(A.fixed[i]);                         // ..._thermal
+    uint32_t st = 0;
+    double2 pos = A.pos[i];
+    if (kMode == 2) {
+        const sph_rigid_tool &rt = *K.rigid;
+        if (flag_nonzero(A.tool_particle[i])) {   // update_tool_particles, blanked or not
+            pos.x += K.dt * rt.vel[0];
+            pos.y += K.dt * rt.vel[1];
+            A.pos[i] = pos;
+        } else {                                  // contact, blanked or not
+            double2 fc, ft = d2(A.ft[i]), nrm;
+            rigid_contact_one(K, rt, K.dt, pos, d2(A.vel[i]), fc, ft, nrm);
+            put(A.ft[i], ft);
+            put(A.n[i], nrm);
+            if (bc_fixed) fc = make_double2(0., 0.);
+            put(A.fc[i], fc);
+        }
+    } else if (bc_fixed) {
+        put(A.fc[i], make_double2(0., 0.));
+    }
+    if (bc_fixed) {
+        put(A.vel[i], make_double2(0., 0.));
+        put(A.pos_t[i], make_double2(0., 0.));
+        put(A.vel_t[i], make_double2(0., 0.));
+    }
+    if (bc_thermal) put(A.T[i], K.c.trml_wp.T_init);
+    if (!blanked) {
+        if (invalid_rates(A.pos_t[i], A.vel_t[i], A.S_t[i], A.rho_t[i], A.T_t[i])) {
+            blanked = true;
+            put(A.blanked[i], 1.);
+            st |= SPH_STATUS_NAN_BLANKED;
+        }
+    }
+    if (kNextHash) {
+        int h;
+        if (!blanked) {
+            const sph_geom_constants &g = K.g;
+            int ix = cell_coord(pos.x, g.bbmin_x, g.dx, K.f.inv_cell);
+            int iy = cell_coord(pos.y, g.bbmin_y, g.dx, K.f.inv_cell);
+            h = ix * g.ny + iy;
+        } else {
+            h = A.hash[i];   // blanked particles keep their stale hash
+        }
+        int key = h;
+        if (h < 0 || h >= K.g.num_cell) {
+            key = K.g.num_cell;
+            st |= SPH_STATUS_OUT_OF_GRID;
+        }
+        X.key[i] = key;
+        X.arrival[i] = atomicAdd(X.counts + key, 1);
+        X.hash_next[i] = h;   // the visible hash array changes only at the next sort
+    }
+    if (st) set_status(status, st);
+}
+
+}  // namespace sphfem

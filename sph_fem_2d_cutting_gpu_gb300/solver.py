@@ -387,6 +387,11 @@ class Batch:
     def step(self, n: int = 1):
         self._ck(self.lib.sph_run(self.ctx, n), "sph_run")
 
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        self._ck(self.lib.sph_launch_count(self.ctx, C.byref(n)), "sph_launch_count")
+        return n.value
+
     def sync(self):
         self._ck(self.lib.sph_sync(self.ctx), "sph_sync")
 

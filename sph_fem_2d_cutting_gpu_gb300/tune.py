@@ -2,8 +2,8 @@
 
 Candidates: every compiled launch shape of the FP32K neighbour-sum kernel
 (``sph_launch_variants``: threads per block, minimum resident blocks per SM,
-neighbour records staged in shared memory)
-times every cell geometry in ``CELL_GEOMETRIES`` (cell edge = h x factor,
+neighbour records staged in shared memory), and the persistent one-launch
+step (``SPH_STEP_PERSISTENT``), times every cell geometry in ``CELL_GEOMETRIES`` (cell edge = h x factor,
 stencil half-width in cells; both cover the 2h kernel support).  Each
 candidate is timed on the workload itself with CUDA events over whole fused
 steps after a warm-up; the fastest is returned with the full table.  The
@@ -34,10 +34,30 @@ def launch_variants():
     return [(blk[i], mb[i], st[i]) for i in range(n.value)]
 
 
-def set_variant(obj, v: int):
+def get_config(obj) -> abi.LaunchConfig:
     cfg = abi.LaunchConfig()
+    obj._ck(obj.lib.sph_get_launch_config(obj.ctx, C.byref(cfg)), "sph_get_launch_config")
+    return cfg
+
+
+def set_variant(obj, v: int):
+    """Launch shape of the neighbour sums (the step form is kept)."""
+    cfg = get_config(obj)
     cfg.interact_variant = v
     obj._ck(obj.lib.sph_set_launch_config(obj.ctx, C.byref(cfg)), "sph_set_launch_config")
+
+
+def set_step_form(obj, form: int):
+    """abi.SPH_STEP_LAUNCHES or abi.SPH_STEP_PERSISTENT (the launch shape is kept)."""
+    cfg = get_config(obj)
+    cfg.step_form = form
+    obj._ck(obj.lib.sph_set_launch_config(obj.ctx, C.byref(cfg)), "sph_set_launch_config")
+
+
+def apply(obj, best: dict):
+    """Set the launch shape and step form of an autotune result."""
+    set_variant(obj, best["variant"])
+    set_step_form(obj, best.get("step_form", abi.SPH_STEP_LAUNCHES))
 
 
 def _time_steps(obj, warmup: int, steps: int) -> float:
@@ -65,9 +85,10 @@ def with_geometry(case, factor: int, stencil: int):
     return c
 
 
-def autotune(make, cases, warmup: int = 3, steps: int = 10, geometries=None, variants=None):
+def autotune(make, cases, warmup: int = 3, steps: int = 10, geometries=None, variants=None, persistent=True):
     """Times every (geometry, launch variant) on contexts built by
-    ``make(cases_with_geometry)`` (a Solver or Batch factory) and returns
+    ``make(cases_with_geometry)`` (a Solver or Batch factory), and with
+    `persistent` the persistent one-launch step on each geometry, and returns
     (best dict, table).  ``cases`` is a case or a list of cases."""
     geometries = geometries or CELL_GEOMETRIES
     all_v = launch_variants()
@@ -82,7 +103,15 @@ def autotune(make, cases, warmup: int = 3, steps: int = 10, geometries=None, var
             set_variant(obj, v)
             ms = _time_steps(obj, warmup, steps)
             table.append(dict(cell_factor=factor, stencil=stencil, variant=v, block=all_v[v][0],
-                              min_blocks=all_v[v][1], staged=all_v[v][2], ms_per_step=ms))
+                              min_blocks=all_v[v][1], staged=all_v[v][2], step_form=abi.SPH_STEP_LAUNCHES,
+                              ms_per_step=ms))
+        if persistent:   # one cooperative launch per step (128-particle blocks of the neighbour sums)
+            set_variant(obj, 0)
+            set_step_form(obj, abi.SPH_STEP_PERSISTENT)
+            ms = _time_steps(obj, warmup, steps)
+            table.append(dict(cell_factor=factor, stencil=stencil, variant=0, block=128, min_blocks=6, staged=0,
+                              step_form=abi.SPH_STEP_PERSISTENT, ms_per_step=ms))
+            set_step_form(obj, abi.SPH_STEP_LAUNCHES)
         obj.close()
     best = min(table, key=lambda r: r["ms_per_step"])
     return dict(best, tune_s=time.perf_counter() - t0), table

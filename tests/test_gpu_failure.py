@@ -73,7 +73,7 @@ def test_mma_timeout_frees_tmem_and_recovers(lib):
     m.fit_norm(rng.normal(size=(4096, 4)).astype(np.float32), rng.normal(size=4096).astype(np.float32))
     s = Solver(case, abi.SPH_PREC_FP32K, place_tool=False)
     s.step(40)                                   # plastic flow under the tool
-    s.attach_mlp(m)
+    s.attach_mlp(m, abi.SPH_MLP_TENSOR)          # the tensor-core tile kernel and its bounded waits
     s.jc_stats(True, reset=True)
     s.step(2)
     calls, _ = s.jc_stats(True, reset=True)

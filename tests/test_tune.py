@@ -65,5 +65,6 @@ def test_launch_variants_agree_with_tool(lib):
 def test_autotune_returns_fastest(lib):
     case = setups.micro(n_side=256)
     best, table = tune.autotune(lambda c: Solver(c, abi.SPH_PREC_FP32K), case, warmup=3, steps=5)
-    assert len(table) == len(tune.CELL_GEOMETRIES) * len(tune.launch_variants())
+    assert len(table) == len(tune.CELL_GEOMETRIES) * (len(tune.launch_variants()) + 1)
+    assert sum(r["step_form"] == abi.SPH_STEP_PERSISTENT for r in table) == len(tune.CELL_GEOMETRIES)
     assert best["ms_per_step"] == min(r["ms_per_step"] for r in table)
