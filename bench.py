@@ -397,6 +397,22 @@ def run_small_cut(args, local):
         sp = C.c_void_p()
         s.lib.sph_get_stream(s.ctx, C.byref(sp))
         ext = torch.cuda.ExternalStream(sp.value, device=torch.device("cuda", local))
+        if prec == abi.SPH_PREC_FP32K and not args.no_tune:
+            # launch shape of the neighbour sums on this workload: each shape on a fresh
+            # context over the same steps as the timed run (the tool advances with the steps,
+            # so a reused context would time a later phase of the cut)
+            shapes = tune.launch_variants()
+            steps_t = max(args.steps, 50)
+            table = []
+            for v in range(len(shapes)):
+                t = Solver(case, prec, device=local)
+                tune.set_variant(t, v)
+                table.append(tune._time_steps(t, args.warmup, steps_t))
+                t.close()
+            best_v = min(range(len(table)), key=lambda v: table[v])
+            tune.set_variant(s, best_v)
+            row["launch_tuning"] = {"chosen": tune.shape_name(shapes[best_v]),
+                                    "ms_per_step": {tune.shape_name(sh): t for sh, t in zip(shapes, table)}}
         s.step(args.warmup)
         s.sync()
         n0 = s.launch_count()
@@ -422,19 +438,21 @@ def run_small_cut(args, local):
         row[name + "_wear"] = {"ms_per_step": msw, "value": case.N / (msw * 1e-3),
                                "launches_per_step": (s.launch_count() - n0) / steps, "status": s.status()}
         s.set_wear(abi.SPH_WEAR_OFF, None)
-        if prec == abi.SPH_PREC_FP32K:   # the same step as one persistent launch
-            tune.set_step_form(s, abi.SPH_STEP_PERSISTENT)
-            s.step(args.warmup)
-            s.sync()
-            n0 = s.launch_count()
-            e0.record(ext)
-            s.step(steps)
-            e1.record(ext)
+        if prec == abi.SPH_PREC_FP32K:   # the same steps as one persistent launch each (fresh context)
+            t = Solver(case, prec, device=local)
+            tune.set_step_form(t, abi.SPH_STEP_PERSISTENT)
+            t.step(args.warmup)
+            t.sync()
+            n0 = t.launch_count()
+            text = stream_of(t, local)
+            e0.record(text)
+            t.step(steps)
+            e1.record(text)
             e1.synchronize()
             msp = e0.elapsed_time(e1) / steps
             row["fp32k_persistent"] = {"ms_per_step": msp, "value": case.N / (msp * 1e-3),
-                                       "launches_per_step": (s.launch_count() - n0) / steps, "status": s.status()}
-            tune.set_step_form(s, abi.SPH_STEP_LAUNCHES)
+                                       "launches_per_step": (t.launch_count() - n0) / steps, "status": t.status()}
+            t.close()
         if prec == abi.SPH_PREC_FP64 and not args.no_cpu:
             P = s.download()
             ts = s.tool_state()
@@ -809,11 +827,11 @@ def run_product(args):
             from sph_fem_2d_cutting_gpu_gb300 import tune
             shapes = tune.launch_variants()
             res["launch_tuning"] = {"chosen": ({"step_form": "persistent", "block": 128, "min_blocks": 6,
-                                                "staged_records": 0} if use_persistent else
+                                                "staged_records": 0, "lanes_per_particle": 1} if use_persistent else
                                                {"step_form": "launches", "block": shapes[best_v][0],
-                                                "min_blocks": shapes[best_v][1], "staged_records": shapes[best_v][2]}),
-                                    "ms_per_step": {f"{b}x{m}" + (f"s{c}" if c else ""): t
-                                                    for (b, m, c), t in zip(shapes, variant_table)},
+                                                "min_blocks": shapes[best_v][1], "staged_records": shapes[best_v][2],
+                                                "lanes_per_particle": shapes[best_v][3]}),
+                                    "ms_per_step": {tune.shape_name(sh): t for sh, t in zip(shapes, variant_table)},
                                     "persistent_ms_per_step": persistent_ms}
         # end-to-end through the C ABI with pinned host buffers
         if not args.no_e2e:

@@ -492,7 +492,9 @@ int sph_mlp_set_inference(sph_ctx *ctx, int32_t mode);
  * (threads per block, minimum resident blocks per SM, and the number of
  * neighbour records a block stages in shared memory -- 0 for global loads);
  * an autotuner times the step with each and sets the fastest.  Variant 0 is
- * the default.
+ * the default.  Shapes with lanes_per_particle > 1 (for small systems, which
+ * leave most of the GPU idle) let that many lanes share a particle's
+ * candidates and merge their compensated sums.
  * step_form: SPH_STEP_LAUNCHES (default) -- the fused step as its chain of
  * launches (scan, scatter, rank, gather, FEM, neighbour sums, tool, contact,
  * tail), replayed from a CUDA graph; SPH_STEP_PERSISTENT -- the same stages in
@@ -509,7 +511,8 @@ typedef struct sph_launch_config {
     int32_t step_form;
 } sph_launch_config;
 /* *n: in, capacity of the output arrays (each may be NULL); out, number of variants. */
-int sph_launch_variants(int32_t *n, int32_t *block, int32_t *min_blocks, int32_t *staged_records);
+int sph_launch_variants(int32_t *n, int32_t *block, int32_t *min_blocks, int32_t *staged_records,
+                        int32_t *lanes_per_particle);
 int sph_set_launch_config(sph_ctx *ctx, const sph_launch_config *cfg);
 int sph_get_launch_config(const sph_ctx *ctx, sph_launch_config *cfg);
 

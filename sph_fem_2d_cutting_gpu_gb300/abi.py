@@ -260,7 +260,7 @@ def load() -> C.CDLL:
         "sph_jc_stats": ([P, I32, C.POINTER(C.c_int64), I32], C.c_int),
         "sph_mlp_attach": ([P, P], C.c_int),
         "sph_mlp_set_inference": ([P, I32], C.c_int),
-        "sph_launch_variants": ([PI, PI, PI, PI], C.c_int),
+        "sph_launch_variants": ([PI, PI, PI, PI, PI], C.c_int),
         "sph_upload_particles_async": ([P, C.POINTER(Particles)], C.c_int),
         "sph_write_vtk_particles": ([P, C.c_char_p], C.c_int),
         "sph_write_vtk_tool": ([P, C.c_char_p, PD], C.c_int),

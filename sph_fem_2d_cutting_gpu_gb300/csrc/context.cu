@@ -1474,9 +1474,11 @@ int sph_step(sph_ctx *ctx) {
     if (!ctx) return SPH_ERR_INVALID;
     cudaStream_t s = ctx->stream;
     const int w = pick_out(ctx);
-    // only the copies into the input, out of (or into) the output, and of the derived fields
+    // only the copies into the input, out of (or into) the output, and of the derived fields;
+    // an FP32K step writes the compact copy c32[w], which no copy touches (a download widens
+    // it into buf[w] later, after the copies of buf[w])
     int r0 = wait_io(ctx, ctx->cur);
-    if (r0 == SPH_OK) r0 = wait_io(ctx, w);
+    if (r0 == SPH_OK && ctx->K.precision != SPH_PREC_FP32K) r0 = wait_io(ctx, w);
     if (r0) return r0;
     {
         int rc = count_current(ctx);
@@ -1987,15 +1989,17 @@ int sph_mlp_set_inference(sph_ctx *ctx, int32_t mode) {
 }
 
 // ---- launch shapes (autotuning) -------------------------------------------------------------------
-int sph_launch_variants(int32_t *n, int32_t *block, int32_t *min_blocks, int32_t *staged_records) {
+int sph_launch_variants(int32_t *n, int32_t *block, int32_t *min_blocks, int32_t *staged_records,
+                        int32_t *lanes_per_particle) {
     if (!n) return SPH_ERR_INVALID;
     const int nv = interact_variant_count();
     for (int v = 0; v < nv && v < *n; v++) {
-        int b, m, st;
-        interact_variant_shape(v, &b, &m, &st);
+        int b, m, st, l;
+        interact_variant_shape(v, &b, &m, &st, &l);
         if (block) block[v] = b;
         if (min_blocks) min_blocks[v] = m;
         if (staged_records) staged_records[v] = st;
+        if (lanes_per_particle) lanes_per_particle[v] = l;
     }
     *n = nv;
     return SPH_OK;

@@ -23,6 +23,16 @@ struct KahanF {
         c = (t - s) - y;
         s = t;
     }
+    // Adds the partner lane's (s, c) (lane ^ o within mask): the two sums by an
+    // error-free two-sum, whose rounding error joins the compensations.
+    __device__ __forceinline__ void merge(unsigned mask, int o) {
+        const float so = __shfl_xor_sync(mask, s, o), co = __shfl_xor_sync(mask, c, o);
+        const float t = s + so;
+        const float bp = t - s;
+        const float e = (s - (t - bp)) + (so - bp);
+        c = (c + co) - e;
+        s = t;
+    }
 };
 
 // One 32-byte-aligned 256-bit load (two float4) through the non-coherent path:
@@ -270,17 +280,24 @@ using Fixed32Of = std::conditional_t<kFused, FixedFields32, FixedFields>;
 // kMlp (fused only): the learned warm start of the return mapping in the
 // epilogue, one warp-wide forward pass per yielding particle; every lane of a
 // warp reaches it, so the per-particle body returns from a lambda.
-// One block of kB particles, vb-th in sorted order (the kernel's blockIdx.x,
-// or a persistent kernel's virtual block).
-template <bool kFused, int kB, bool kStaged, bool kMlp>
+// One block of kB / kSplit particles, vb-th in sorted order (the kernel's
+// blockIdx.x, or a persistent kernel's virtual block).  kSplit > 1 (small
+// systems, fused form): kSplit consecutive lanes share a particle, each
+// scanning every kSplit-th candidate of each stencil column; their sums are
+// merged (compensated) before the epilogue, which the first lane runs.
+template <bool kFused, int kB, bool kStaged, bool kMlp, int kSplit = 1>
 __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K, const int32_t *__restrict__ offsets,
                                                  const float4 *__restrict__ rec, const Sorted32Of<kFused> &B,
                                                  const Fixed32Of<kFused> &F, const SegDev &seg,
                                                  const ToolDev *__restrict__ tool, int32_t *__restrict__ secant_iters,
                                                  uint32_t *status, int cap, const MlpDev &mlp) {
     static_assert(kFused || !kMlp, "the warm start is folded into the fused epilogue only");
-    const int k = vb * kB + threadIdx.x;
-    if (kFused && threadIdx.x == 0) block_prefetch_l2(vb, N, kB, K, offsets, rec, B, F);
+    static_assert(kSplit == 1 || (kFused && !kStaged && 32 % kSplit == 0), "split lanes: fused, unstaged");
+    constexpr int kPPB = kB / kSplit;   // particles per block
+    const int k = vb * kPPB + (int)threadIdx.x / kSplit;
+    const int sub = (int)threadIdx.x % kSplit;
+    const unsigned gmask = ((1u << kSplit) - 1u) << ((threadIdx.x & 31u) & ~(unsigned)(kSplit - 1));
+    if (kFused && threadIdx.x == 0) block_prefetch_l2(vb, N, kPPB, K, offsets, rec, B, F);
     int (*s_list)[kB];
     const float4 *nrec = rec;   // where the neighbour records are read from
     __shared__ StageHdr s_hdr;
@@ -310,7 +327,7 @@ __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K
     const float4 i0 = rec[4 * k + 0];
     const int fi = __float_as_int(i0.z);
     if (fi & kFlagBlanked) {
-        if (kFused) rigid_heat_blanked(k, K, B);
+        if (kFused && sub == 0) rigid_heat_blanked(k, K, B);   // one lane per particle
         return;
     }
     const bool tool_i = (fi & kFlagTool) != 0;
@@ -350,7 +367,7 @@ __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K
         hi_i = min(gi + R + 1, g.nx);
         lo_j = max(gj - R, 0);
         hi_j = min(gj + R + 1, g.ny);
-        j = __ldg(offsets + ii * g.ny + lo_j);
+        j = __ldg(offsets + ii * g.ny + lo_j) + sub;
         j1 = __ldg(offsets + ii * g.ny + hi_j);
         done = false;
     }
@@ -379,10 +396,10 @@ __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K
         // four candidates per round keep four loads in flight
         int cnt = 0;
         while (cnt < kChunk32) {
-            if (j + 4 <= j1 && cnt <= kChunk32 - 4) {
+            if (j + 4 * kSplit - (kSplit - 1) <= j1 && cnt <= kChunk32 - 4) {
                 float4 n[4];
 #pragma unroll
-                for (int u = 0; u < 4; u++) n[u] = nb[4 * (j + u)];
+                for (int u = 0; u < 4; u++) n[u] = nb[4 * (j + u * kSplit)];
                 const float dxc = (float)(gi - ii) * cell;
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
@@ -392,9 +409,9 @@ __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K
                     const float rr2 = dx * dx + dy * dy;
                     if (!all) marks |= fj;
                     if ((all || (rr2 < fourh2 && rr2 >= 1e-8f)) && !(fj & kFlagBlanked))
-                        s_list[cnt++][threadIdx.x] = ((j + u) << 3) | (gi - ii + R);
+                        s_list[cnt++][threadIdx.x] = ((j + u * kSplit) << 3) | (gi - ii + R);
                 }
-                j += 4;
+                j += 4 * kSplit;
             } else if (j < j1) {
                 const float4 n0 = nb[4 * j + 0];
                 const int fj = __float_as_int(n0.z);
@@ -404,13 +421,13 @@ __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K
                 if (!all) marks |= fj;
                 if ((all || (rr2 < fourh2 && rr2 >= 1e-8f)) && !(fj & kFlagBlanked))
                     s_list[cnt++][threadIdx.x] = (j << 3) | (gi - ii + R);
-                j++;
+                j += kSplit;
             } else {
                 if (++ii >= hi_i) {
                     done = true;
                     break;
                 }
-                j = __ldg(offsets + ii * g.ny + lo_j);
+                j = __ldg(offsets + ii * g.ny + lo_j) + sub;
                 j1 = __ldg(offsets + ii * g.ny + hi_j);
                 if constexpr (kStaged) {
                     if (use_s) {
@@ -541,11 +558,15 @@ __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K
     }
     };
     sweep(std::false_type{});
+    if constexpr (kSplit > 1) {   // the particle's stencil as a whole
+#pragma unroll
+        for (int o = 1; o < kSplit; o <<= 1) marks |= __shfl_xor_sync(gmask, marks, o);
+    }
     if (marks & kFlagNonFinite) {   // rare: the reference's full stencil with zero weights
         vd0 = vd1 = vd2 = vd3 = sd0 = sd1 = sd2 = sd3 = vt0 = vt1 = xt0 = xt1 = tl = KahanF{};
         af = Acc32Fused{};
         ii = max(gi - R, 0);
-        j = __ldg(offsets + ii * g.ny + lo_j);
+        j = __ldg(offsets + ii * g.ny + lo_j) + sub;
         j1 = __ldg(offsets + ii * g.ny + hi_j);
         if constexpr (kStaged) {
             if (use_s) {
@@ -557,6 +578,21 @@ __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K
         sweep(std::true_type{});
     }
     if constexpr (kFused) {
+        if constexpr (kSplit > 1) {   // merge the lanes' compensated sums; the first lane goes on
+#pragma unroll
+            for (int o = 1; o < kSplit; o <<= 1) {
+                af.vd0.merge(gmask, o);
+                af.vd1.merge(gmask, o);
+                af.vd2.merge(gmask, o);
+                af.vd3.merge(gmask, o);
+                af.ax.merge(gmask, o);
+                af.ay.merge(gmask, o);
+                af.xt0.merge(gmask, o);
+                af.xt1.merge(gmask, o);
+                af.tl.merge(gmask, o);
+            }
+            if (sub != 0) return;
+        }
         const float mass = K.f.mass;
         const float xs = K.f.xs_mass;
         const float4 vd = make_float4(af.vd0.s, af.vd1.s, af.vd2.s, af.vd3.s);
@@ -587,18 +623,18 @@ __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K
     if constexpr (kMlp) jc_warm_warp(K, B, F, tool, mlp, k, pending, secant_iters, status);
 }
 
-template <bool kFused, int kB = kBlock, int kMinB = 1, bool kStaged = false, bool kMlp = false>
+template <bool kFused, int kB = kBlock, int kMinB = 1, bool kStaged = false, bool kMlp = false, int kSplit = 1>
 __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, const int32_t *__restrict__ offsets,
                                                        const float4 *__restrict__ rec, Sorted32Of<kFused> B,
                                                        Fixed32Of<kFused> F, SegDev seg,
                                                        const ToolDev *__restrict__ tool,
                                                        int32_t *__restrict__ secant_iters, uint32_t *status,
                                                        int cap, MlpDev mlp) {
-    interact32_block<kFused, kB, kStaged, kMlp>(blockIdx.x, N, K, offsets, rec, B, F, seg, tool, secant_iters, status,
-                                                cap, mlp);
+    interact32_block<kFused, kB, kStaged, kMlp, kSplit>(blockIdx.x, N, K, offsets, rec, B, F, seg, tool,
+                                                        secant_iters, status, cap, mlp);
 }
 
-template <int kB, int kMinB, bool kStaged, bool kMlp = false>
+template <int kB, int kMinB, bool kStaged, bool kMlp = false, int kSplit = 1>
 static void launch_i32(cudaStream_t s, int N, const KConsts &K, const int32_t *offsets, const SortedFields32 &B,
                        const FixedFields32 &F, const StepScratch &W, const SegDev &seg, const ToolDev *tool, int cap,
                        const MlpDev &mlp = MlpDev{}) {
@@ -607,12 +643,12 @@ static void launch_i32(cudaStream_t s, int N, const KConsts &K, const int32_t *o
         smem = (size_t)cap * 64 + sizeof(int) * kChunk32 * kB;
         static bool configured = false;   // opt in above 48 KB of dynamic shared memory, once
         if (!configured) {
-            cudaFuncSetAttribute(k_interact32<true, kB, kMinB, kStaged, kMlp>,
+            cudaFuncSetAttribute(k_interact32<true, kB, kMinB, kStaged, kMlp, kSplit>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             configured = true;
         }
     }
-    k_interact32<true, kB, kMinB, kStaged, kMlp><<<div_up(N, kB), kB, smem, s>>>(
+    k_interact32<true, kB, kMinB, kStaged, kMlp, kSplit><<<div_up(N, kB / kSplit), kB, smem, s>>>(
         N, K, offsets, W.rec32, B, F, seg, tool, W.secant_iters, W.status, cap, mlp);
 }
 
@@ -631,6 +667,8 @@ void launch_i32_variant(cudaStream_t s, int N, const KConsts &K, const int32_t *
         case 7: launch_i32<128, 2, true, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 1024, mlp); break;
         case 8: launch_i32<64, 6, true, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 384, mlp); break;
         case 9: launch_i32<256, 2, true, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 1024, mlp); break;
+        case 10: launch_i32<128, 6, false, kMlp, 2>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
+        case 11: launch_i32<128, 6, false, kMlp, 4>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
         default: launch_i32<128, 6, false, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
     }
 }

@@ -279,16 +279,18 @@ __global__ void __launch_bounds__(kB) k_interact64(int N, KConsts K, const int32
 }
 
 // Launch shapes of the fused FP32K neighbour-sum kernel: (threads per block,
-// minimum resident blocks per SM, staged records: 0 = global loads).
-// Variant 0 is the default.
-const int kInteractVariants[][3] = {{128, 6, 0},   {64, 12, 0},   {64, 8, 0},     {128, 4, 0},  {256, 3, 0},
-                                    {256, 1, 0},   {128, 3, 640}, {128, 2, 1024}, {64, 6, 384}, {256, 2, 1024}};
+// minimum resident blocks per SM, staged records: 0 = global loads, lanes per
+// particle).  Variant 0 is the default.
+const int kInteractVariants[][4] = {{128, 6, 0, 1},   {64, 12, 0, 1},   {64, 8, 0, 1},     {128, 4, 0, 1},
+                                    {256, 3, 0, 1},   {256, 1, 0, 1},   {128, 3, 640, 1},  {128, 2, 1024, 1},
+                                    {64, 6, 384, 1},  {256, 2, 1024, 1}, {128, 6, 0, 2},    {128, 6, 0, 4}};
 
 int interact_variant_count() { return (int)(sizeof(kInteractVariants) / sizeof(kInteractVariants[0])); }
-void interact_variant_shape(int v, int *block, int *min_blocks, int *staged) {
+void interact_variant_shape(int v, int *block, int *min_blocks, int *staged, int *lanes) {
     *block = kInteractVariants[v][0];
     *min_blocks = kInteractVariants[v][1];
     *staged = kInteractVariants[v][2];
+    *lanes = kInteractVariants[v][3];
 }
 
 // Threads per block of the FP64 per-particle kernels: the largest of 256, 128,

@@ -51,7 +51,7 @@ void launch_heat_pse(cudaStream_t s, int N, const KConsts &K, const int32_t *off
                      const SortedFields32 &B);
 int interact_variant_count();
 int fp64_block(int N);   // threads per block of the FP64 per-particle kernels for N particles
-void interact_variant_shape(int v, int *block, int *min_blocks, int *staged);
+void interact_variant_shape(int v, int *block, int *min_blocks, int *staged, int *lanes);
 
 // actions.cu
 void launch_init(cudaStream_t s, int N, const SortedFields &A, const StepScratch &W);

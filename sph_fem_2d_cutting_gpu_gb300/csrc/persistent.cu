@@ -9,7 +9,10 @@
 // grid-stride loops, and the neighbour sums over virtual blocks of 128
 // particles.  Results are those of the graph form, bit for bit: every element
 // is computed by the same code from the same inputs, and the only cross-thread
-// sums (segment heat exchange, histogram arrivals) are the same atomics.
+// sums (segment heat exchange, histogram arrivals) are the same atomics.  (With
+// the learned warm start folded in, nvcc contracts a few products of the
+// epilogue into FMAs differently in the two instantiations: the states then
+// agree to FP32 rounding.)
 //
 // Every barrier wait is bounded (1 s): a block that gives up, or sees that
 // another gave up, sets SPH_STATUS_GRID_TIMEOUT and leaves the kernel, so the
@@ -30,7 +33,7 @@ namespace {
 constexpr int kPB = 128;                     // threads per block
 constexpr int kPMinBlocks = 6;               // register budget: 6 resident blocks per SM
 constexpr int kPItems = kScanTile / kPB;     // scan buckets per thread (the separate kernels' tiles)
-constexpr int kScanOneBlockTiles = 16;       // bucket grids up to 16 tiles are scanned by one block
+constexpr int kScanOneBlockTiles = 2;        // bucket grids up to 2 tiles are scanned by one block
 
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
     unsigned v;

@@ -22,16 +22,23 @@ CELL_GEOMETRIES = [(1, 2), (2, 1)]
 
 
 def launch_variants():
-    """[(threads per block, min blocks per SM, staged records)] of the compiled shapes."""
+    """[(threads per block, min blocks per SM, staged records, lanes per particle)] of the compiled shapes."""
     lib = abi.load()
     n = C.c_int32(0)
-    lib.sph_launch_variants(C.byref(n), None, None, None)
+    lib.sph_launch_variants(C.byref(n), None, None, None, None)
     blk = (C.c_int32 * n.value)()
     mb = (C.c_int32 * n.value)()
     st = (C.c_int32 * n.value)()
+    ln = (C.c_int32 * n.value)()
     cap = C.c_int32(n.value)
-    lib.sph_launch_variants(C.byref(cap), blk, mb, st)
-    return [(blk[i], mb[i], st[i]) for i in range(n.value)]
+    lib.sph_launch_variants(C.byref(cap), blk, mb, st, ln)
+    return [(blk[i], mb[i], st[i], ln[i]) for i in range(n.value)]
+
+
+def shape_name(shape) -> str:
+    """'128x6', '128x3s640' (staged records), '128x6l4' (lanes per particle)."""
+    b, m, c, l = shape
+    return f"{b}x{m}" + (f"s{c}" if c else "") + (f"l{l}" if l > 1 else "")
 
 
 def get_config(obj) -> abi.LaunchConfig:
@@ -103,14 +110,14 @@ def autotune(make, cases, warmup: int = 3, steps: int = 10, geometries=None, var
             set_variant(obj, v)
             ms = _time_steps(obj, warmup, steps)
             table.append(dict(cell_factor=factor, stencil=stencil, variant=v, block=all_v[v][0],
-                              min_blocks=all_v[v][1], staged=all_v[v][2], step_form=abi.SPH_STEP_LAUNCHES,
-                              ms_per_step=ms))
+                              min_blocks=all_v[v][1], staged=all_v[v][2], lanes=all_v[v][3],
+                              step_form=abi.SPH_STEP_LAUNCHES, ms_per_step=ms))
         if persistent:   # one cooperative launch per step (128-particle blocks of the neighbour sums)
             set_variant(obj, 0)
             set_step_form(obj, abi.SPH_STEP_PERSISTENT)
             ms = _time_steps(obj, warmup, steps)
             table.append(dict(cell_factor=factor, stencil=stencil, variant=0, block=128, min_blocks=6, staged=0,
-                              step_form=abi.SPH_STEP_PERSISTENT, ms_per_step=ms))
+                              lanes=1, step_form=abi.SPH_STEP_PERSISTENT, ms_per_step=ms))
             set_step_form(obj, abi.SPH_STEP_LAUNCHES)
         obj.close()
     best = min(table, key=lambda r: r["ms_per_step"])

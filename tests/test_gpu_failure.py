@@ -34,7 +34,7 @@ def set_faults(s, faults, cap=-1):
 
 
 def staged_variant():
-    for v, (_, _, staged) in enumerate(tune.launch_variants()):
+    for v, (_, _, staged, _) in enumerate(tune.launch_variants()):
         if staged:
             return v
     pytest.skip("no staged launch shape compiled")
