@@ -213,6 +213,23 @@ def run_reference(args):
     return 0
 
 
+def tune_fresh(make, warmup: int, steps: int):
+    """Launch shape of the FP32K neighbour sums for a small workload: every shape
+    timed on a fresh context from make() over the same steps (a cut advances its
+    tool with the steps, so a reused context would time a later phase).
+    Returns (best variant, {shape name: ms per step})."""
+    from sph_fem_2d_cutting_gpu_gb300 import tune
+    shapes = tune.launch_variants()
+    table = []
+    for v in range(len(shapes)):
+        t = make()
+        tune.set_variant(t, v)
+        table.append(tune._time_steps(t, warmup, steps))
+        t.close()
+    best = min(range(len(table)), key=lambda v: table[v])
+    return best, {tune.shape_name(sh): ms for sh, ms in zip(shapes, table)}
+
+
 def stream_of(obj, local):
     """The library stream of a context, as a torch stream (for CUDA events on it)."""
     import ctypes as C
@@ -397,22 +414,10 @@ def run_small_cut(args, local):
         sp = C.c_void_p()
         s.lib.sph_get_stream(s.ctx, C.byref(sp))
         ext = torch.cuda.ExternalStream(sp.value, device=torch.device("cuda", local))
-        if prec == abi.SPH_PREC_FP32K and not args.no_tune:
-            # launch shape of the neighbour sums on this workload: each shape on a fresh
-            # context over the same steps as the timed run (the tool advances with the steps,
-            # so a reused context would time a later phase of the cut)
-            shapes = tune.launch_variants()
-            steps_t = max(args.steps, 50)
-            table = []
-            for v in range(len(shapes)):
-                t = Solver(case, prec, device=local)
-                tune.set_variant(t, v)
-                table.append(tune._time_steps(t, args.warmup, steps_t))
-                t.close()
-            best_v = min(range(len(table)), key=lambda v: table[v])
+        if prec == abi.SPH_PREC_FP32K and not args.no_tune:   # launch shape on this workload
+            best_v, table = tune_fresh(lambda: Solver(case, prec, device=local), args.warmup, max(args.steps, 50))
             tune.set_variant(s, best_v)
-            row["launch_tuning"] = {"chosen": tune.shape_name(shapes[best_v]),
-                                    "ms_per_step": {tune.shape_name(sh): t for sh, t in zip(shapes, table)}}
+            row["launch_tuning"] = {"chosen": list(table)[best_v], "ms_per_step": table}
         s.step(args.warmup)
         s.sync()
         n0 = s.launch_count()
@@ -485,14 +490,22 @@ def run_tiny_sweep(args, local):
     from sph_fem_2d_cutting_gpu_gb300.solver import Batch
 
     cases = setups.batched_sweep(n_cases=16, seed=args.seed + 1, n_min=3000, n_max=12000, height=0.025)
-    b = Batch(cases, abi.SPH_PREC_FP32K, device=local)
-    ext = stream_of(b, local)
     steps = max(args.steps, 50)
-    out = {"workload": f"{b.n_cases} AISI 1045 cuts of {min(c.N for c in cases)}-{max(c.N for c in cases)} "
-                       f"particles ({b.N} in all), own FEM tool each ({sum(i['node_count'] for i in b.info)} "
-                       "nodes in all), FP32K", "particles": b.N, "cases": b.n_cases}
+    best_v, table = (0, None) if args.no_tune else \
+        tune_fresh(lambda: Batch(cases, abi.SPH_PREC_FP32K, device=local), args.warmup, steps)
+    out = None
     for name, form in (("launches", abi.SPH_STEP_LAUNCHES), ("persistent", abi.SPH_STEP_PERSISTENT)):
+        b = Batch(cases, abi.SPH_PREC_FP32K, device=local)   # a fresh batch: both forms time the same steps
+        tune.set_variant(b, best_v)
         tune.set_step_form(b, form)
+        if out is None:
+            out = {"workload": f"{b.n_cases} AISI 1045 cuts of {min(c.N for c in cases)}-{max(c.N for c in cases)} "
+                               f"particles ({b.N} in all), own FEM tool each "
+                               f"({sum(i['node_count'] for i in b.info)} nodes in all), FP32K",
+                   "particles": b.N, "cases": b.n_cases}
+            if table is not None:
+                out["launch_tuning"] = {"chosen": list(table)[best_v], "ms_per_step": table}
+        ext = stream_of(b, local)
         b.step(args.warmup)
         b.sync()
         n0 = b.launch_count()
@@ -504,8 +517,8 @@ def run_tiny_sweep(args, local):
         ms = e0.elapsed_time(e1) / steps
         out[name] = {"ms_per_step": ms, "value": b.N / (ms * 1e-3),
                      "launches_per_step": (b.launch_count() - n0) / steps, "status": b.status()}
-    b.close()
-    torch.cuda.empty_cache()
+        b.close()
+        torch.cuda.empty_cache()
     out["persistent_speedup"] = out["launches"]["ms_per_step"] / out["persistent"]["ms_per_step"]
     return out
 
@@ -521,7 +534,7 @@ def run_rigid(args, local):
 
     import torch
 
-    from sph_fem_2d_cutting_gpu_gb300 import abi, setups
+    from sph_fem_2d_cutting_gpu_gb300 import abi, setups, tune
     from sph_fem_2d_cutting_gpu_gb300.solver import Solver
     from oracle.oracle import OracleSim, num_threads
 
@@ -530,11 +543,18 @@ def run_rigid(args, local):
     for ny in args.rigid_ny:
         case = setups.ref_cut(ny=ny, rake=0.0, clear=4.5, chamfer=0.00035, speed=speed, feed=0.01)
         row = {"ny": ny, "particles": case.N, "workpiece": case.info["n_workpiece"], "tool": case.info["n_tool"]}
+        best_v = 0
+        if not args.no_tune:   # launch shape of the FP32K neighbour sums (Brookshaw build)
+            best_v, table = tune_fresh(lambda: Solver(case, abi.SPH_PREC_FP32K, device=local), args.warmup,
+                                       args.steps)
+            row["launch_tuning"] = {"chosen": list(table)[best_v], "ms_per_step": table}
         for name, prec, pse in (("fp64", abi.SPH_PREC_FP64, False), ("fp32k", abi.SPH_PREC_FP32K, False),
                                 ("fp64_pse", abi.SPH_PREC_FP64, True), ("fp32k_pse", abi.SPH_PREC_FP32K, True)):
             s = Solver(case, prec, device=local)
             if pse:
                 s.set_thermal_model(abi.SPH_THERMAL_PSE)
+            if prec == abi.SPH_PREC_FP32K:
+                tune.set_variant(s, best_v)
             sp = C.c_void_p()
             s.lib.sph_get_stream(s.ctx, C.byref(sp))
             ext = torch.cuda.ExternalStream(sp.value, device=torch.device("cuda", local))

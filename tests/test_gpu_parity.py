@@ -222,6 +222,30 @@ def test_staged_step_matches_fused(lib):
         assert np.array_equal(A[f], B[f]), f
 
 
+def test_fp32_compensated_full_size_2h(lib):
+    """The headline workload itself (2048 x 2048 = 4,194,304 particles, cells of
+    2h / 3x3 stencil), one fused step in FP32K against one in FP64 (the FP64 form
+    is pinned to the oracle at 1e-10 per step): the same cell lists and sort
+    permutation, rates and state within the FP32K bound of the small case."""
+    c = setups.micro(n_side=2048, seed=9, cell_factor=2, stencil=1)
+    out = {}
+    for prec in (abi.SPH_PREC_FP64, abi.SPH_PREC_FP32K):
+        s = Solver(c, precision=prec)
+        s.step()
+        out[prec] = s.download(["hash", "idx", "blanked", "vel_t", "pos_t", "S_t", "rho_t", "vel", "S", "rho",
+                                "eps_pl"])
+        st = s.status()
+        s.close()
+        assert st & abi.STATUS_BITS["nan_blanked"] == 0
+    G, R = out[abi.SPH_PREC_FP32K], out[abi.SPH_PREC_FP64]
+    for f in ("hash", "idx", "blanked"):
+        assert np.array_equal(G[f], R[f]), f
+    assert (R["eps_pl"] > 0).sum() > 1000, "plastic flow: the return mapping runs"
+    for f in ("vel_t", "pos_t", "S_t", "rho_t", "vel", "S", "rho"):
+        e = rel_err(G[f], R[f])
+        assert e < 2e-5, f"FP32K {f}: {e:.2e}"
+
+
 def test_fp32_compensated_error_bound(lib):
     c = shuffled_micro(n=80, seed=9)
     s64, o = pair(c)
