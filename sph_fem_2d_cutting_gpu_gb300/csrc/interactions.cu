@@ -283,7 +283,8 @@ __global__ void __launch_bounds__(kB) k_interact64(int N, KConsts K, const int32
 // particle).  Variant 0 is the default.
 const int kInteractVariants[][4] = {{128, 6, 0, 1},   {64, 12, 0, 1},   {64, 8, 0, 1},     {128, 4, 0, 1},
                                     {256, 3, 0, 1},   {256, 1, 0, 1},   {128, 3, 640, 1},  {128, 2, 1024, 1},
-                                    {64, 6, 384, 1},  {256, 2, 1024, 1}, {128, 6, 0, 2},    {128, 6, 0, 4}};
+                                    {64, 6, 384, 1},  {256, 2, 1024, 1}, {128, 6, 0, 2},    {128, 6, 0, 4},
+                                    {128, 5, 0, 1},   {64, 10, 0, 1}};
 
 int interact_variant_count() { return (int)(sizeof(kInteractVariants) / sizeof(kInteractVariants[0])); }
 void interact_variant_shape(int v, int *block, int *min_blocks, int *staged, int *lanes) {
