@@ -182,7 +182,8 @@ __device__ __forceinline__ void write_record64(dbl4 *__restrict__ rec, int k, co
 // FP32 record: (xr, yr, flags|row, h) (vx, vy, rho, c) (sA, sB, sC, vol) (Rxx, Rxy, Ryy, T)
 // xr, yr = offset of the particle from its cell's lower-left corner; the first
 // 16 bytes are all the candidate test needs.
-__device__ __forceinline__ void write_record32(float4 *__restrict__ rec, int k, const KConsts &K, double2 pos,
+__device__ __forceinline__ void write_record32(float4 *__restrict__ rec, float2 *__restrict__ cand, int k,
+                                               const KConsts &K, double2 pos,
                                                double2 vel, dbl4 S, dbl4 R, double p, double h, double rho,
                                                double T, double blanked, double tool, int hash) {
     const sph_geom_constants &g = K.g;
@@ -204,12 +205,14 @@ __device__ __forceinline__ void write_record32(float4 *__restrict__ rec, int k, 
     rec[4 * k + 1] = r1;
     rec[4 * k + 2] = r2;
     rec[4 * k + 3] = r3;
+    cand[k] = cand_pack(r0.x, r0.y, flags);
 }
 
 // Staged path helper: records from the particle arrays as they are now
 // (interactions_monaghan reads pos, vel, S, R, h, rho, p, T, tool, blanked).
 __global__ void __launch_bounds__(kBlock) k_build_records(int N, KConsts K, SortedFields A, FixedFields F,
-                                                          dbl4 *__restrict__ rec64, float4 *__restrict__ rec32) {
+                                                          dbl4 *__restrict__ rec64, float4 *__restrict__ rec32,
+                                                          float2 *__restrict__ cand32) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= N) return;
     double tool = A.tool_particle[k];
@@ -225,7 +228,7 @@ __global__ void __launch_bounds__(kBlock) k_build_records(int N, KConsts K, Sort
         write_record64(rec64, k, K, A.pos[k], A.vel[k], A.S[k], F.R[k], F.p[k], A.h[k], A.rho[k], T, A.blanked[k],
                        tool, row);
     } else {
-        write_record32(rec32, k, K, A.pos[k], A.vel[k], A.S[k], F.R[k], F.p[k], A.h[k], A.rho[k], T, A.blanked[k],
+        write_record32(rec32, cand32, k, K, A.pos[k], A.vel[k], A.S[k], F.R[k], F.p[k], A.h[k], A.rho[k], T, A.blanked[k],
                        tool, hash);
     }
 }
@@ -242,7 +245,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused(int N, const int32_t *_
                                                          SortedFields A, SortedFields B, FixedFields F,
                                                          const int32_t *__restrict__ hash_src,
                                                          dbl4 *__restrict__ rec64, float4 *__restrict__ rec32,
-                                                         const ToolDev *__restrict__ tools) {
+                                                         float2 *__restrict__ cand32, const ToolDev *__restrict__ tools) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= N) return;
     int i = perm[k];
@@ -304,7 +307,7 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused(int N, const int32_t *_
         if (hash >= 0 && hash < K.g.num_cell) row = hash - (hash / K.g.ny) * K.g.ny;
         write_record64(rec64, k, K, pos, vel, S, R, p, h, rho, Tn, blanked, tool, row);
     } else {
-        write_record32(rec32, k, K, pos, vel, S, R, p, h, rho, Tn, blanked, tool, hash);
+        write_record32(rec32, cand32, k, K, pos, vel, S, R, p, h, rho, Tn, blanked, tool, hash);
     }
 }
 
@@ -314,9 +317,10 @@ __global__ void __launch_bounds__(kBlock) k_gather_fused32(int N, const int32_t 
                                                            FF Fsrc, SortedFields32 B, FixedFields32 F,
                                                            int32_t *__restrict__ idx,
                                                            const int32_t *__restrict__ hash_src,
-                                                           float4 *__restrict__ rec, const ToolDev *__restrict__ tools) {
+                                                           float4 *__restrict__ rec, float2 *__restrict__ cand,
+                                                           const ToolDev *__restrict__ tools) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < N) gather32_one(k, perm, K, A, Fsrc, B, F, idx, hash_src, rec, tools);
+    if (k < N) gather32_one(k, perm, K, A, Fsrc, B, F, idx, hash_src, rec, cand, tools);
 }
 
 // The compact FP32 state (state) and its p, R (pr) widened into the FP64
@@ -402,7 +406,7 @@ void launch_gather_fused(cudaStream_t s, int N, const int32_t *perm, const KCons
                          const SortedFields &B, const FixedFields &F, const StepScratch &W, const int32_t *hash_src,
                          const ToolDev *tool) {
     const int tb = fp64_block(N);   // EOS and artificial stress per particle: spread small systems
-    k_gather_fused<false><<<div_up(N, tb), tb, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec64, W.rec32, tool);
+    k_gather_fused<false><<<div_up(N, tb), tb, 0, s>>>(N, perm, K, A, B, F, hash_src, W.rec64, W.rec32, W.cand32, tool);
 }
 
 void launch_gather_fused32(cudaStream_t s, int N, const int32_t *perm, const KConsts &K, const SortedFields *A64,
@@ -411,13 +415,13 @@ void launch_gather_fused32(cudaStream_t s, int N, const int32_t *perm, const KCo
                            const ToolDev *tool) {
     const int tb = fp64_block(N), g = div_up(N, tb);
     if (A32 && pr32)
-        k_gather_fused32<<<g, tb, 0, s>>>(N, perm, K, *A32, F32, B, F32, idx, hash_src, W.rec32, tool);
+        k_gather_fused32<<<g, tb, 0, s>>>(N, perm, K, *A32, F32, B, F32, idx, hash_src, W.rec32, W.cand32, tool);
     else if (A32)
-        k_gather_fused32<<<g, tb, 0, s>>>(N, perm, K, *A32, F, B, F32, idx, hash_src, W.rec32, tool);
+        k_gather_fused32<<<g, tb, 0, s>>>(N, perm, K, *A32, F, B, F32, idx, hash_src, W.rec32, W.cand32, tool);
     else if (pr32)
-        k_gather_fused32<<<g, tb, 0, s>>>(N, perm, K, *A64, F32, B, F32, idx, hash_src, W.rec32, tool);
+        k_gather_fused32<<<g, tb, 0, s>>>(N, perm, K, *A64, F32, B, F32, idx, hash_src, W.rec32, W.cand32, tool);
     else
-        k_gather_fused32<<<g, tb, 0, s>>>(N, perm, K, *A64, F, B, F32, idx, hash_src, W.rec32, tool);
+        k_gather_fused32<<<g, tb, 0, s>>>(N, perm, K, *A64, F, B, F32, idx, hash_src, W.rec32, W.cand32, tool);
 }
 
 void launch_state_to64(cudaStream_t s, int N, const SortedFields32 &A, const FixedFields32 &Fa, const SortedFields &B,
@@ -428,7 +432,7 @@ void launch_state_to64(cudaStream_t s, int N, const SortedFields32 &A, const Fix
 void launch_build_records(cudaStream_t s, int N, const KConsts &K, const SortedFields &A, const FixedFields &F,
                           const StepScratch &W) {
     k_build_records<<<div_up(N, kBlock), kBlock, 0, s>>>(N, K, A, F, K.precision == SPH_PREC_FP32K ? nullptr : W.rec64,
-                                                         W.rec32);
+                                                         W.rec32, W.cand32);
 }
 
 }  // namespace sphfem

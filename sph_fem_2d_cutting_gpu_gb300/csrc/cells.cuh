@@ -79,19 +79,12 @@ __device__ __forceinline__ void rank_one(int s, const int32_t *__restrict__ key,
 // arrays after an upload or a staged call, the compact arrays after a fused
 // step.  p and R of tool particles are kept from FF at the sorted position, as
 // the reference leaves them (they are not part of the Green sort's buffer).
-// FP32-compensated form of the fused reorder: the same gather into the compact
-// FP32 state (SortedFields32), with the predictor, EOS and artificial stress of
-// the predicted state evaluated in FP32 (positions and density stay FP64: rho -
-// rho0 is a small difference, FP32 would lose its leading digits) and written
-// into the FP32 record.  SF / FF: the state the step starts from -- the FP64
-// arrays after an upload or a staged call, the compact arrays after a fused
-// step.  p and R of tool particles are kept from FF at the sorted position, as
-// the reference leaves them (they are not part of the Green sort's buffer).
 template <class SF, class FF>
 __device__ __forceinline__ void gather32_one(int k, const int32_t *__restrict__ perm, const KConsts &K, const SF &A,
                                              const FF &Fsrc, const SortedFields32 &B, const FixedFields32 &F,
                                              int32_t *__restrict__ idx, const int32_t *__restrict__ hash_src,
-                                             float4 *__restrict__ rec, const ToolDev *__restrict__ tools) {
+                                             float4 *__restrict__ rec, float2 *__restrict__ cand,
+                                             const ToolDev *__restrict__ tools) {
     int i = perm[k];
     idx[k] = i;
     const double2 pos = A.pos[i];
@@ -177,6 +170,7 @@ __device__ __forceinline__ void gather32_one(int k, const int32_t *__restrict__ 
     rec[4 * k + 1] = r1;
     rec[4 * k + 2] = r2;
     rec[4 * k + 3] = r3;
+    cand[k] = cand_pack(r0.x, r0.y, flags);
 }
 
 }  // namespace sphfem

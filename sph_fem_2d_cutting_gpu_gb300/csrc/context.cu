@@ -741,8 +741,12 @@ int ctx_begin(const sph_constants *c, const sph_grid_params *g, const sph_geom_c
     DALLOC(ctx->X.counts, (size_t)nc + 1); DALLOC(ctx->X.offsets, (size_t)nc + 2);
     DALLOC(ctx->X.block_sums, (size_t)scan_blocks(nc) + 1);
     DALLOC(ctx->X.cell_start, nc); DALLOC(ctx->X.cell_end, nc);
-    if (precision == SPH_PREC_FP32K) DALLOC(ctx->W.rec32, (size_t)4 * N);
-    else DALLOC(ctx->W.rec64, (size_t)4 * N);
+    if (precision == SPH_PREC_FP32K) {
+        DALLOC(ctx->W.rec32, (size_t)4 * N);
+        DALLOC(ctx->W.cand32, N);
+    } else {
+        DALLOC(ctx->W.rec64, (size_t)4 * N);
+    }
     DALLOC(ctx->W.pos_init, N); DALLOC(ctx->W.vel_init, N); DALLOC(ctx->W.S_init, N);
     DALLOC(ctx->W.rho_init, N); DALLOC(ctx->W.T_init, N);
     DALLOC(ctx->W.secant_iters, N); DALLOC(ctx->W.status, 1);

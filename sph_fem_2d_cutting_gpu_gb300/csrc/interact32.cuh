@@ -43,12 +43,20 @@ __device__ __forceinline__ void ld_nc_256(const float4 *p, float4 &a, float4 &b)
                  : "l"(p));
 }
 
+// The candidate flag bits (kCandBlanked, kCandNonFinite) of a record's flag word.
+__device__ __forceinline__ int rec_cand_flags(int fj) {
+    return ((fj & kFlagBlanked) ? kCandBlanked : 0) | ((fj & kFlagNonFinite) ? kCandNonFinite : 0);
+}
+
 // In-support neighbours collected per pass of the pair loops.  With h = 1.7 dx
-// a particle has about 36 (a disc of radius 2h): 48 covers nearly all of them
+// a particle has about 36 (a disc of radius 2h): 40 covers nearly all of them
 // in one pass.  A second, short pass costs more than its share: the lanes of a
-// warp hold 0 to 10 pairs in it, and it re-enters the candidate scan.  Larger
-// lists take shared memory from the L1 that serves the neighbour records.
-constexpr int kChunk32 = 48;
+// warp hold 0 to 10 pairs in it, and it re-enters the candidate scan (36 or 32
+// entries: 13-15 % slower on the 4.19 M lattice).  Larger lists take shared
+// memory from the L1 that serves the neighbour records: at 128 threads x 6
+// blocks, 40 entries take 120 KB of shared memory per SM, 48 take 144 KB and
+// were 1.3 % slower (44: the same as 48).
+constexpr int kChunk32 = 40;
 constexpr int kChunk64 = 48;   // FP64: 48 x 256 threads x 4 B = the 48 KB static limit
 
 // Sums of the fused FP32 pair loop, each Kahan-compensated.  The epilogue needs
@@ -239,7 +247,7 @@ __device__ __forceinline__ void stage_issue(int vb, int N, int kB, const KConsts
 template <class SF, class FF>
 __device__ __forceinline__ void block_prefetch_l2(int vb, int N, int kB, const KConsts &K,
                                                   const int32_t *__restrict__ offsets, const float4 *__restrict__ rec,
-                                                  const SF &B, const FF &F) {
+                                                  const float2 *__restrict__ cand, const SF &B, const FF &F) {
     const int b0 = vb * kB;
     const uint32_t n = (uint32_t)min(kB, N - b0);
     prefetch_l2_bulk(B.S + b0, n * (uint32_t)sizeof(B.S[0]));
@@ -262,7 +270,11 @@ __device__ __forceinline__ void block_prefetch_l2(int vb, int N, int kB, const K
     const int r_lo = max(hf - ix * g.ny - R, 0), r_hi = min(hl - ix * g.ny + R, g.ny - 1);
     for (int c = max(ix - R, 0); c <= min(ix + R, g.nx - 1); c++) {
         const int s0 = __ldg(offsets + c * g.ny + r_lo), s1 = __ldg(offsets + c * g.ny + r_hi + 1);
-        if (s1 > s0) prefetch_l2_bulk(rec + 4 * (size_t)s0, (uint32_t)(s1 - s0) * 64u);
+        if (s1 > s0) {
+            prefetch_l2_bulk(rec + 4 * (size_t)s0, (uint32_t)(s1 - s0) * 64u);
+            const int a0 = s0 & ~1;   // 16-byte aligned start; the size is rounded down
+            prefetch_l2_bulk(cand + a0, (uint32_t)(s1 - a0) * 8u);
+        }
     }
 }
 
@@ -287,7 +299,8 @@ using Fixed32Of = std::conditional_t<kFused, FixedFields32, FixedFields>;
 // merged (compensated) before the epilogue, which the first lane runs.
 template <bool kFused, int kB, bool kStaged, bool kMlp, int kSplit = 1>
 __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K, const int32_t *__restrict__ offsets,
-                                                 const float4 *__restrict__ rec, const Sorted32Of<kFused> &B,
+                                                 const float4 *__restrict__ rec, const float2 *__restrict__ cand,
+                                                 const Sorted32Of<kFused> &B,
                                                  const Fixed32Of<kFused> &F, const SegDev &seg,
                                                  const ToolDev *__restrict__ tool, int32_t *__restrict__ secant_iters,
                                                  uint32_t *status, int cap, const MlpDev &mlp) {
@@ -297,7 +310,7 @@ __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K
     const int k = vb * kPPB + (int)threadIdx.x / kSplit;
     const int sub = (int)threadIdx.x % kSplit;
     const unsigned gmask = ((1u << kSplit) - 1u) << ((threadIdx.x & 31u) & ~(unsigned)(kSplit - 1));
-    if (kFused && threadIdx.x == 0) block_prefetch_l2(vb, N, kPPB, K, offsets, rec, B, F);
+    if (kFused && threadIdx.x == 0) block_prefetch_l2(vb, N, kPPB, K, offsets, rec, cand, B, F);
     int (*s_list)[kB];
     const float4 *nrec = rec;   // where the neighbour records are read from
     __shared__ StageHdr s_hdr;
@@ -388,39 +401,56 @@ __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K
     // when one of the factors is NaN or infinite.  So a particle whose stencil
     // holds a record marked non-finite repeats its sums over every active
     // candidate with the reference's zero weights (pass 1).
-    int marks = 0;   // OR of the flags of the stencil's candidates (blanked ones carry no mark)
+    // OR of the candidate flags over the stencil (bit kCandNonFinite is the one
+    // read; blanked candidates carry no mark)
+    int marks = 0;
     auto sweep = [&](auto all_tag) {
     constexpr bool all = decltype(all_tag)::value;
+    // the candidate test on (xr, yr), the row difference and the flag bits
+    auto take = [&](int &cnt, int jj, float cx, float cy, int drow, int cf, float dxc) {
+        const float dx = dxc + (xri - cx);
+        const float dy = (float)drow * cell + (yri - cy);
+        const float rr2 = dx * dx + dy * dy;
+        if (!all) marks |= cf;
+        if ((all || (rr2 < fourh2 && rr2 >= 1e-8f)) && !(cf & kCandBlanked))
+            s_list[cnt++][threadIdx.x] = (jj << 3) | (gi - ii + R);
+    };
     while (!done) {
-        // phase 1: collect the next in-support, active neighbours (column offset packed in 3 bits);
-        // four candidates per round keep four loads in flight
+        // phase 1: collect the next in-support, active neighbours (column offset packed in 3 bits)
+        // from the 8-byte candidate entries (cand_pack), or from the staged records' first 16
+        // bytes; four candidates per round keep four loads in flight
         int cnt = 0;
         while (cnt < kChunk32) {
+            const float dxc = (float)(gi - ii) * cell;
             if (j + 4 * kSplit - (kSplit - 1) <= j1 && cnt <= kChunk32 - 4) {
-                float4 n[4];
+                if (!kStaged || !use_s) {
+                    float2 c[4];
 #pragma unroll
-                for (int u = 0; u < 4; u++) n[u] = nb[4 * (j + u * kSplit)];
-                const float dxc = (float)(gi - ii) * cell;
+                    for (int u = 0; u < 4; u++) c[u] = __ldg(cand + j + u * kSplit);
 #pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const int fj = __float_as_int(n[u].z);
-                    const float dx = dxc + (xri - n[u].x);
-                    const float dy = (float)(gj - (fj & kRowMask)) * cell + (yri - n[u].y);
-                    const float rr2 = dx * dx + dy * dy;
-                    if (!all) marks |= fj;
-                    if ((all || (rr2 < fourh2 && rr2 >= 1e-8f)) && !(fj & kFlagBlanked))
-                        s_list[cnt++][threadIdx.x] = ((j + u * kSplit) << 3) | (gi - ii + R);
+                    for (int u = 0; u < 4; u++)
+                        take(cnt, j + u * kSplit, c[u].x, c[u].y, ((gj - __float_as_int(c[u].y)) << 29) >> 29,
+                             __float_as_int(c[u].x), dxc);
+                } else {
+                    float4 n[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) n[u] = nb[4 * (j + u * kSplit)];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int fj = __float_as_int(n[u].z);
+                        take(cnt, j + u * kSplit, n[u].x, n[u].y, gj - (fj & kRowMask), rec_cand_flags(fj), dxc);
+                    }
                 }
                 j += 4 * kSplit;
             } else if (j < j1) {
-                const float4 n0 = nb[4 * j + 0];
-                const int fj = __float_as_int(n0.z);
-                const float dx = (float)(gi - ii) * cell + (xri - n0.x);
-                const float dy = (float)(gj - (fj & kRowMask)) * cell + (yri - n0.y);
-                const float rr2 = dx * dx + dy * dy;
-                if (!all) marks |= fj;
-                if ((all || (rr2 < fourh2 && rr2 >= 1e-8f)) && !(fj & kFlagBlanked))
-                    s_list[cnt++][threadIdx.x] = (j << 3) | (gi - ii + R);
+                if (!kStaged || !use_s) {
+                    const float2 c = __ldg(cand + j);
+                    take(cnt, j, c.x, c.y, ((gj - __float_as_int(c.y)) << 29) >> 29, __float_as_int(c.x), dxc);
+                } else {
+                    const float4 n0 = nb[4 * j + 0];
+                    const int fj = __float_as_int(n0.z);
+                    take(cnt, j, n0.x, n0.y, gj - (fj & kRowMask), rec_cand_flags(fj), dxc);
+                }
                 j += kSplit;
             } else {
                 if (++ii >= hi_i) {
@@ -562,7 +592,7 @@ __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K
 #pragma unroll
         for (int o = 1; o < kSplit; o <<= 1) marks |= __shfl_xor_sync(gmask, marks, o);
     }
-    if (marks & kFlagNonFinite) {   // rare: the reference's full stencil with zero weights
+    if (marks & kCandNonFinite) {   // rare: the reference's full stencil with zero weights
         vd0 = vd1 = vd2 = vd3 = sd0 = sd1 = sd2 = sd3 = vt0 = vt1 = xt0 = xt1 = tl = KahanF{};
         af = Acc32Fused{};
         ii = max(gi - R, 0);
@@ -625,12 +655,13 @@ __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K
 
 template <bool kFused, int kB = kBlock, int kMinB = 1, bool kStaged = false, bool kMlp = false, int kSplit = 1>
 __global__ void __launch_bounds__(kB, kMinB) k_interact32(int N, KConsts K, const int32_t *__restrict__ offsets,
-                                                       const float4 *__restrict__ rec, Sorted32Of<kFused> B,
+                                                       const float4 *__restrict__ rec,
+                                                       const float2 *__restrict__ cand, Sorted32Of<kFused> B,
                                                        Fixed32Of<kFused> F, SegDev seg,
                                                        const ToolDev *__restrict__ tool,
                                                        int32_t *__restrict__ secant_iters, uint32_t *status,
                                                        int cap, MlpDev mlp) {
-    interact32_block<kFused, kB, kStaged, kMlp, kSplit>(blockIdx.x, N, K, offsets, rec, B, F, seg, tool,
+    interact32_block<kFused, kB, kStaged, kMlp, kSplit>(blockIdx.x, N, K, offsets, rec, cand, B, F, seg, tool,
                                                         secant_iters, status, cap, mlp);
 }
 
@@ -649,7 +680,7 @@ static void launch_i32(cudaStream_t s, int N, const KConsts &K, const int32_t *o
         }
     }
     k_interact32<true, kB, kMinB, kStaged, kMlp, kSplit><<<div_up(N, kB / kSplit), kB, smem, s>>>(
-        N, K, offsets, W.rec32, B, F, seg, tool, W.secant_iters, W.status, cap, mlp);
+        N, K, offsets, W.rec32, W.cand32, B, F, seg, tool, W.secant_iters, W.status, cap, mlp);
 }
 
 // The launch shapes of kInteractVariants (interactions.cu), in its order.
@@ -669,9 +700,9 @@ void launch_i32_variant(cudaStream_t s, int N, const KConsts &K, const int32_t *
         case 9: launch_i32<256, 2, true, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 1024, mlp); break;
         case 10: launch_i32<128, 6, false, kMlp, 2>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
         case 11: launch_i32<128, 6, false, kMlp, 4>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
-        case 12: launch_i32<128, 5, false, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
+        case 12: launch_i32<128, 6, false, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
         case 13: launch_i32<64, 10, false, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
-        default: launch_i32<128, 6, false, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
+        default: launch_i32<128, 5, false, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
     }
 }
 

@@ -280,11 +280,14 @@ __global__ void __launch_bounds__(kB) k_interact64(int N, KConsts K, const int32
 
 // Launch shapes of the fused FP32K neighbour-sum kernel: (threads per block,
 // minimum resident blocks per SM, staged records: 0 = global loads, lanes per
-// particle).  Variant 0 is the default.
-const int kInteractVariants[][4] = {{128, 6, 0, 1},   {64, 12, 0, 1},   {64, 8, 0, 1},     {128, 4, 0, 1},
+// particle).  Variant 0 is the default: a minimum of 5 blocks lets the compiler
+// keep 80 registers, which still fits 6 blocks (24 warps) per SM; a minimum of
+// 6 caps it at 77 and ran 4 % slower on the 4.19 M lattice, a free choice
+// (88 registers, 20 warps) 4 % slower too.
+const int kInteractVariants[][4] = {{128, 5, 0, 1},   {64, 12, 0, 1},   {64, 8, 0, 1},     {128, 4, 0, 1},
                                     {256, 3, 0, 1},   {256, 1, 0, 1},   {128, 3, 640, 1},  {128, 2, 1024, 1},
                                     {64, 6, 384, 1},  {256, 2, 1024, 1}, {128, 6, 0, 2},    {128, 6, 0, 4},
-                                    {128, 5, 0, 1},   {64, 10, 0, 1}};
+                                    {128, 6, 0, 1},   {64, 10, 0, 1}};
 
 int interact_variant_count() { return (int)(sizeof(kInteractVariants) / sizeof(kInteractVariants[0])); }
 void interact_variant_shape(int v, int *block, int *min_blocks, int *staged, int *lanes) {
@@ -433,8 +436,8 @@ void launch_interactions(cudaStream_t s, int N, const KConsts &K, const int32_t 
     const int grid = div_up(N, kBlock);
     if (K.precision == SPH_PREC_FP32K) {
         // the fused FP32K step runs on the compact state (launch_interactions32_fused)
-        k_interact32<false><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec32, B, F, seg, tool, W.secant_iters, W.status,
-                                                    0, MlpDev{});
+        k_interact32<false><<<grid, kBlock, 0, s>>>(N, K, offsets, W.rec32, W.cand32, B, F, seg, tool, W.secant_iters,
+                                                    W.status, 0, MlpDev{});
     } else {
         const int kb = fp64_block(N);
         const int g64 = div_up(N, kb);

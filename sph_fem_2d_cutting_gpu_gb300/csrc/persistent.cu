@@ -183,13 +183,13 @@ __global__ void __launch_bounds__(kPB, kPMinBlocks) k_step_persistent(PersistArg
     if (!grid_barrier(P.bar, status)) return;
     // reorder + predictor + EOS + artificial stress + records
     for (int k = gtid; k < N; k += gstride)
-        gather32_one(k, P.perm, K, P.A, P.F32, P.B, P.F32, P.perm, P.X.hash_next, P.W.rec32, P.tool);
+        gather32_one(k, P.perm, K, P.A, P.F32, P.B, P.F32, P.perm, P.X.hash_next, P.W.rec32, P.W.cand32, P.tool);
     if (!grid_barrier(P.bar, status)) return;
     // neighbour sums + epilogue, 128 particles per virtual block
     const int n_vb = (N + kPB - 1) / kPB;
     for (int vb = blockIdx.x; vb < n_vb; vb += gridDim.x)
-        interact32_block<true, kPB, false, kMlp>(vb, N, K, P.X.offsets, P.W.rec32, P.B, P.F32, P.seg, P.tool,
-                                                  P.W.secant_iters, status, 0, P.mlp);
+        interact32_block<true, kPB, false, kMlp>(vb, N, K, P.X.offsets, P.W.rec32, P.W.cand32, P.B, P.F32, P.seg,
+                                                  P.tool, P.W.secant_iters, status, 0, P.mlp);
     if (!grid_barrier(P.bar, status)) return;
     if (kTool) {
         for (int i = gtid; i < P.fem.n_nodes; i += gstride) fem_rate_update_one(i, K, P.fem, P.seg, P.tool);

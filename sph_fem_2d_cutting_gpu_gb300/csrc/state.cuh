@@ -76,6 +76,23 @@ constexpr int kRecWords = 16;
 // support); never set on blanked records.
 enum : int { kFlagBlanked = 1 << 30, kFlagTool = 1 << 29, kFlagNonFinite = 1 << 28, kRowMask = (1 << 28) - 1 };
 
+// FP32K candidate entry, one float2 per record in the same order: the record's
+// (xr, yr) for the in-support test of the candidate scan, 8 bytes instead of
+// the record's first 16.  The flags ride in the low mantissa bits: xr's two
+// lowest bits hold kCandBlanked / kCandNonFinite, yr's three lowest bits the
+// cell row modulo 8 (the row difference to the summing particle is at most the
+// stencil half-width, 3).  Each coordinate moves by at most 7 units in the
+// last place of a value below a cell edge, so the test's support boundary
+// moves by at most 2^-20 of a cell, where the kernel and its gradient vanish to
+// third and second order; the pair terms themselves use the full record.
+enum : int { kCandBlanked = 1, kCandNonFinite = 2 };
+__device__ __forceinline__ float2 cand_pack(float xr, float yr, int flags) {
+    const int bx = (__float_as_int(xr) & ~3) | ((flags & kFlagBlanked) ? kCandBlanked : 0) |
+                   ((flags & kFlagNonFinite) ? kCandNonFinite : 0);
+    const int by = (__float_as_int(yr) & ~7) | (flags & 7);
+    return make_float2(__int_as_float(bx), __int_as_float(by));
+}
+
 // Interface segments (segment_FEM_gpu, segment_FEM_gpu.h:31-56).
 struct SegDev {
     int n;
@@ -130,6 +147,7 @@ struct WearDev {
 struct StepScratch {
     dbl4 *rec64;      // [N][4] FP64 records
     float4 *rec32;       // [N][4] FP32 records
+    float2 *cand32;      // [N] candidate entries of the FP32 records (cand_pack)
     double2 *pos_init, *vel_init;   // leap_frog snapshots (staged path)
     dbl4 *S_init;
     double *rho_init, *T_init;
