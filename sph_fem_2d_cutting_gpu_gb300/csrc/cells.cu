@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(kBlock) k_hash_count(int N, const double2 *__r
             set_status(status, SPH_STATUS_OUT_OF_GRID);
         }
         key[i] = k;
-        arrival[i] = atomicAdd(counts + k, 1);
+        arrival[i] = histogram_slot(counts, k);
         hash_next[i] = h;
     }
 }

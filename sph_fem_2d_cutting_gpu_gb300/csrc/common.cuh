@@ -156,6 +156,22 @@ __device__ __forceinline__ int cell_coord(double x, double bbmin, double dx, flo
     return __double2int_rz(a / dx);
 }
 
+// A slot in bucket `key` of a histogram (the counting sort's arrival index):
+// the lanes of a warp with the same key -- consecutive particles mostly share
+// a cell -- take their slots with one atomic, in lane order.  Any order inside
+// a bucket is valid: the rank pass orders each cell by original index.
+// One-dimensional blocks (lane = threadIdx.x % 32).
+__device__ __forceinline__ int histogram_slot(int32_t *counts, int key) {
+    const unsigned active = __activemask();
+    const unsigned peers = __match_any_sync(active, key);
+    const int lane = (int)(threadIdx.x & 31u);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counts + key, __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
 // Device copy of the rigid tool kinematics that tool_FEM keeps on the host
 // (tool_FEM.h:57-77); updated by the tool-move kernel so a captured CUDA graph
 // needs no host round trip.

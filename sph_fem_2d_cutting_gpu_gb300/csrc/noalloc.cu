@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kBlock) k_na_hash_count(int n, const double2 *
     }
     int k = (h < 0 || h >= g.num_cell) ? g.num_cell : h;
     X.key[i] = k;
-    X.arrival[i] = atomicAdd(X.counts + k, 1);
+    X.arrival[i] = histogram_slot(X.counts, k);
 }
 
 // exclusive scan of the buckets in one block; also writes cell_start /

@@ -276,7 +276,7 @@ __device__ __forceinline__ void step_tail_one(int i, const KConsts &K, const SF 
             st |= SPH_STATUS_OUT_OF_GRID;
         }
         X.key[i] = key;
-        X.arrival[i] = atomicAdd(X.counts + key, 1);
+        X.arrival[i] = histogram_slot(X.counts, key);
         X.hash_next[i] = h;   // the visible hash array changes only at the next sort
     }
     if (st) set_status(status, st);
