@@ -700,9 +700,9 @@ void launch_i32_variant(cudaStream_t s, int N, const KConsts &K, const int32_t *
         case 9: launch_i32<256, 2, true, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 1024, mlp); break;
         case 10: launch_i32<128, 6, false, kMlp, 2>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
         case 11: launch_i32<128, 6, false, kMlp, 4>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
-        case 12: launch_i32<128, 6, false, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
+        case 12: launch_i32<128, 5, false, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
         case 13: launch_i32<64, 10, false, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
-        default: launch_i32<128, 5, false, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
+        default: launch_i32<128, 6, false, kMlp>(s, N, K, offsets, B, F, W, seg, tool, 0, mlp); break;
     }
 }
 

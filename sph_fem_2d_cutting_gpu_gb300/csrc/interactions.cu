@@ -280,14 +280,16 @@ __global__ void __launch_bounds__(kB) k_interact64(int N, KConsts K, const int32
 
 // Launch shapes of the fused FP32K neighbour-sum kernel: (threads per block,
 // minimum resident blocks per SM, staged records: 0 = global loads, lanes per
-// particle).  Variant 0 is the default: a minimum of 5 blocks lets the compiler
-// keep 80 registers, which still fits 6 blocks (24 warps) per SM; a minimum of
-// 6 caps it at 77 and ran 4 % slower on the 4.19 M lattice, a free choice
-// (88 registers, 20 warps) 4 % slower too.
-const int kInteractVariants[][4] = {{128, 5, 0, 1},   {64, 12, 0, 1},   {64, 8, 0, 1},     {128, 4, 0, 1},
+// particle).  Variant 0 is the default: 6 blocks (24 warps) per SM at 76
+// registers (80 with the learned warm start in the epilogue).  A minimum of 5
+// blocks of 128 (or 10 of 64) lets the compiler keep 80 registers at the same
+// 24 warps; a free choice (91 registers) drops to 20 warps.  On the 4.19 M
+// lattice 64x10, 128x6 and 256x3 lie within 2 % of each other, 128x5 4 % behind;
+// with the warm start 128x5 and 64x10 need 96 registers (20 warps).
+const int kInteractVariants[][4] = {{128, 6, 0, 1},   {64, 12, 0, 1},   {64, 8, 0, 1},     {128, 4, 0, 1},
                                     {256, 3, 0, 1},   {256, 1, 0, 1},   {128, 3, 640, 1},  {128, 2, 1024, 1},
                                     {64, 6, 384, 1},  {256, 2, 1024, 1}, {128, 6, 0, 2},    {128, 6, 0, 4},
-                                    {128, 6, 0, 1},   {64, 10, 0, 1}};
+                                    {128, 5, 0, 1},   {64, 10, 0, 1}};
 
 int interact_variant_count() { return (int)(sizeof(kInteractVariants) / sizeof(kInteractVariants[0])); }
 void interact_variant_shape(int v, int *block, int *min_blocks, int *staged, int *lanes) {

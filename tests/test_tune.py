@@ -9,7 +9,7 @@ from conftest import rel_err
 
 def test_launch_variants_listed(lib):
     v = tune.launch_variants()
-    assert v[0] == (128, 5, 0, 1)     # the default: 80 registers, still 24 resident warps per SM, no spills
+    assert v[0] == (128, 6, 0, 1)     # the default: 24 resident warps per SM, no spills
     assert len(v) >= 4 and len(set(v)) == len(v)
     assert any(c > 0 for _, _, c, _ in v) and any(l > 1 for _, _, _, l in v)
     for block, min_blocks, staged, lanes in v:
