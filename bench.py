@@ -55,9 +55,9 @@ ALGO_BYTES = {
 }
 # DRAM bytes (read + write) per particle of one full-size launch of the fused
 # neighbour sums, from ncu on the 2048x2048 micro workload with 2h cells
-# (dram__bytes_read.sum 723,047,424 + dram__bytes_write.sum 397,837,312 for
-# 4,194,304 particles, k_interact32<fused, 128x5>; one-pass capture).
-NCU_TRAFFIC_PER_PARTICLE = {"fp32k": (723_047_424 + 397_837_312) / 4_194_304}
+# (dram__bytes_read.sum 723,139,584 + dram__bytes_write.sum 398,211,584 for
+# 4,194,304 particles, k_interact32<fused, 128x6>; one-pass capture).
+NCU_TRAFFIC_PER_PARTICLE = {"fp32k": (723_139_584 + 398_211_584) / 4_194_304}
 # Floating-point work per particle of the fused neighbour sums, from ncu's SASS
 # instruction counters (dadd + dmul + 2 dfma; fadd + fmul + 2 ffma) on the
 # 512x512 micro workload with 2h cells (262,144 particles): k_interact64 executes
