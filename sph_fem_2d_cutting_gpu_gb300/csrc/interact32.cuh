@@ -48,6 +48,13 @@ __device__ __forceinline__ int rec_cand_flags(int fj) {
     return ((fj & kFlagBlanked) ? kCandBlanked : 0) | ((fj & kFlagNonFinite) ? kCandNonFinite : 0);
 }
 
+// The row difference gj - row of a candidate entry (cand_pack): its y carries the
+// row modulo 8 in the three lowest bits, and |gj - row| <= kMaxStencil = 3, so the
+// low three bits of the difference, sign-extended, are the difference.
+__device__ __forceinline__ int cand_row_diff(int gj, float cy) {
+    return (int)(((unsigned)gj - (unsigned)__float_as_int(cy)) << 29) >> 29;
+}
+
 // In-support neighbours collected per pass of the pair loops.  With h = 1.7 dx
 // a particle has about 36 (a disc of radius 2h): 40 covers nearly all of them
 // in one pass.  A second, short pass costs more than its share: the lanes of a
@@ -429,7 +436,7 @@ __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K
                     for (int u = 0; u < 4; u++) c[u] = __ldg(cand + j + u * kSplit);
 #pragma unroll
                     for (int u = 0; u < 4; u++)
-                        take(cnt, j + u * kSplit, c[u].x, c[u].y, ((gj - __float_as_int(c[u].y)) << 29) >> 29,
+                        take(cnt, j + u * kSplit, c[u].x, c[u].y, cand_row_diff(gj, c[u].y),
                              __float_as_int(c[u].x), dxc);
                 } else {
                     float4 n[4];
@@ -445,7 +452,7 @@ __device__ __forceinline__ void interact32_block(int vb, int N, const KConsts &K
             } else if (j < j1) {
                 if (!kStaged || !use_s) {
                     const float2 c = __ldg(cand + j);
-                    take(cnt, j, c.x, c.y, ((gj - __float_as_int(c.y)) << 29) >> 29, __float_as_int(c.x), dxc);
+                    take(cnt, j, c.x, c.y, cand_row_diff(gj, c.y), __float_as_int(c.x), dxc);
                 } else {
                     const float4 n0 = nb[4 * j + 0];
                     const int fj = __float_as_int(n0.z);
