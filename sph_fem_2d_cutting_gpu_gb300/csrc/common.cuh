@@ -207,6 +207,10 @@ __device__ __forceinline__ long long order_key(double x) {
     if (b == (long long)0x8000000000000000ull) b = 0;
     return b ^ ((b >> 63) & 0x7fffffffffffffffll);
 }
+// The double of an order key (the inverse map; -0 comes back as +0).
+__device__ __forceinline__ double order_key_value(long long k) {
+    return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffll));
+}
 
 // Per-segment wear statistics gathered by the friction-heat kernel
 // (WEAR_NODE_SHIFT, actions_gpu.cu:401-419); pp == NULL: not gathered.

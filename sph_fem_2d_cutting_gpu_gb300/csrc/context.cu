@@ -784,6 +784,8 @@ int ctx_upload_tool(sph_ctx *ctx, bool with_model, const std::vector<ToolDev> &t
         DALLOC(S.heat_exchange, M.n_seg); DALLOC(S.fric_heat, M.n_seg);
         DALLOC(S.bin_count, (size_t)kSegBins * tds.size());
         DALLOC(S.bin_list, (size_t)kSegBins * kSegBinCap * tds.size());
+        DALLOC(S.geo, M.n_seg);
+        DALLOC(S.bin_xkey, (size_t)kSegBins * tds.size());
         CK(cudaMemcpy(S.left, M.left.data(), sizeof(double) * 2 * M.n_seg, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(S.right, M.right.data(), sizeof(double) * 2 * M.n_seg, cudaMemcpyHostToDevice));
         CK(cudaMemcpy(S.normal, M.normal.data(), sizeof(double) * 2 * M.n_seg, cudaMemcpyHostToDevice));

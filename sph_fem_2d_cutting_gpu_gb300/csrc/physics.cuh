@@ -413,6 +413,38 @@ __device__ __forceinline__ int inside_judgement(double2 qp, const double2 *__res
 }
 
 // ---- actions_gpu.cu:139-220 find_shortest_distance_v1 ------------------------------
+// The branch for no segment within limit_value (:182-219): the nearest right end
+// point, its normal averaged with the next segment's.  seg: the first loop's
+// result, kept when no end point is nearer than FLT_MAX (as the reference).
+__device__ __forceinline__ int shortest_distance_fallback(double2 qp, double &dN, double2 &n_re,
+                                                          const double2 *__restrict__ left,
+                                                          const double2 *__restrict__ right,
+                                                          const double2 *__restrict__ n, int num_seg, int seg) {
+    double depth = FLT_MAX;
+    for (int i = 0; i < num_seg; i++) {
+        double2 Rr = __ldg(right + i);
+        double d_trial = sqrtf_d((qp.x - Rr.x) * (qp.x - Rr.x) + (qp.y - Rr.y) * (qp.y - Rr.y));
+        if (d_trial < depth) { depth = d_trial; seg = i; }
+    }
+    if (seg == -1) return seg;
+    double2 ns = __ldg(n + seg);
+    double2 rs = __ldg(right + seg);
+    double nsx = ns.x, nsy = ns.y;
+    for (int j = 0; j < num_seg; j++) {
+        double2 Lj = __ldg(left + j);
+        if (Lj.y == rs.y && Lj.x == rs.x) {
+            double2 nj = __ldg(n + j);
+            nsx = (nj.x + ns.x) / 2.;
+            nsy = (nj.y + ns.y) / 2.;
+            break;
+        }
+    }
+    double n_length = sqrtf_d(nsx * nsx + nsy * nsy);
+    n_re = make_double2(-nsx / n_length, -nsy / n_length);
+    dN = -1.0 * depth;
+    return seg;
+}
+
 __device__ __forceinline__ int find_shortest_distance_v1(double2 qp, double &dN, double2 &n_re,
                                                          const double2 *__restrict__ left,
                                                          const double2 *__restrict__ right,
@@ -441,31 +473,9 @@ __device__ __forceinline__ int find_shortest_distance_v1(double2 qp, double &dN,
         double2 ns = __ldg(n + seg);
         n_re = make_double2(-ns.x, -ns.y);
         dN = -depth;
-    } else {
-        depth = FLT_MAX;
-        for (int i = 0; i < num_seg; i++) {
-            double2 Rr = __ldg(right + i);
-            double d_trial = sqrtf_d((qp.x - Rr.x) * (qp.x - Rr.x) + (qp.y - Rr.y) * (qp.y - Rr.y));
-            if (d_trial < depth) { depth = d_trial; seg = i; }
-        }
-        if (seg == -1) return seg;
-        double2 ns = __ldg(n + seg);
-        double2 rs = __ldg(right + seg);
-        double nsx = ns.x, nsy = ns.y;
-        for (int j = 0; j < num_seg; j++) {
-            double2 Lj = __ldg(left + j);
-            if (Lj.y == rs.y && Lj.x == rs.x) {
-                double2 nj = __ldg(n + j);
-                nsx = (nj.x + ns.x) / 2.;
-                nsy = (nj.y + ns.y) / 2.;
-                break;
-            }
-        }
-        double n_length = sqrtf_d(nsx * nsx + nsy * nsy);
-        n_re = make_double2(-nsx / n_length, -nsy / n_length);
-        dN = -1.0 * depth;
+        return seg;
     }
-    return seg;
+    return shortest_distance_fallback(qp, dN, n_re, left, right, n, num_seg, seg);
 }
 
 }  // namespace sphfem

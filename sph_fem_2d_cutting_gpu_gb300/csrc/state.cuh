@@ -93,6 +93,18 @@ __device__ __forceinline__ float2 cand_pack(float xr, float yr, int flags) {
     return make_float2(__int_as_float(bx), __int_as_float(by));
 }
 
+// Per-segment constants of the contact search, rebuilt each step with the
+// y-bins (k_seg_bins), after the tool has moved: what on_segment_mesh and the
+// first loop of find_shortest_distance_v1 (actions_gpu.cu:51-63, :139-180)
+// form per particle from the segment alone, computed once with the same
+// operations -- so every test gives the reference's result bit for bit.
+struct __align__(64) SegGeo {
+    long long kx0, kx1, ky0, ky1;     // order keys of xmin - 0.0008, xmax + 0.0008, ymin - 0.0008, ymax + 0.0008
+    double ymin_f, ymax_f;            // fminf / fmaxf of the end points' y (float-rounded)
+    double inv_slope;                 // (left.x - right.x) / (left.y - right.y), non-horizontal segments
+    long long pad;
+};
+
 // Interface segments (segment_FEM_gpu, segment_FEM_gpu.h:31-56).
 struct SegDev {
     int n;
@@ -108,9 +120,14 @@ struct SegDev {
     // the case-local segment index.  NULL: no bins, full scan.
     int32_t *bin_count;
     int32_t *bin_list;
+    // with the bins: per segment, SegGeo; per bin, the order key of an x bound
+    // right of which no segment of the bin has a crossing (an empty bin: the
+    // lowest key)
+    SegGeo *geo;
+    long long *bin_xkey;
 };
 constexpr int kSegBins = 64;
-constexpr int kSegBinCap = 64;
+constexpr int kSegBinCap = 256;
 
 // FEM thermal system of the tool (FEM_thermal_2D_GPU, FEM_thermal_gpu.h:35-93).
 // K, f are the assembled (post-Dirichlet) m_stiffness_matrix / m_f; the Robin

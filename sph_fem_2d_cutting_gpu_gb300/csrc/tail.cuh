@@ -42,7 +42,11 @@ __device__ __forceinline__ int seg_bin_of(double y, double y0, double scale) {
 __device__ __forceinline__ void seg_bins_block(int c, const SegDev &seg, ToolDev *tool) {
     ToolDev &t = tool[c];
     __shared__ int cnt[kSegBins];
-    for (int b = threadIdx.x; b < kSegBins; b += blockDim.x) cnt[b] = 0;
+    __shared__ long long xkey[kSegBins];   // order key of the largest end-point x listed in the bin
+    for (int b = threadIdx.x; b < kSegBins; b += blockDim.x) {
+        cnt[b] = 0;
+        xkey[b] = (long long)0x8000000000000000ull;
+    }
     const double y0 = (double)(float)t.seg_ymin, y1 = (double)(float)t.seg_ymax;
     const double scale = (y1 > y0) ? (double)kSegBins / (y1 - y0) : 0.;
     int32_t *list = seg.bin_list + (size_t)c * kSegBins * kSegBinCap;
@@ -51,14 +55,46 @@ __device__ __forceinline__ void seg_bins_block(int c, const SegDev &seg, ToolDev
         const double2 L = seg.left[t.seg_first + i], R = seg.right[t.seg_first + i];
         const int b0 = max(seg_bin_of(fminf_d(L.y, R.y), y0, scale) - 1, 0);
         const int b1 = min(seg_bin_of(fmaxf_d(L.y, R.y), y0, scale) + 1, kSegBins - 1);
+        const long long kx = order_key(fmax(L.x, R.x));
         for (int b = b0; b <= b1; b++) {
             const int slot = atomicAdd(&cnt[b], 1);
             if (slot < kSegBinCap) list[b * kSegBinCap + slot] = i;
+            if (seg.bin_xkey) atomicMax(&xkey[b], kx);
+        }
+    }
+    // the per-segment constants of the contact search (SegGeo)
+    if (seg.geo) {
+        for (int i = threadIdx.x; i < t.seg_count; i += blockDim.x) {
+            const double2 L = seg.left[t.seg_first + i], R = seg.right[t.seg_first + i];
+            SegGeo g;
+            g.ymin_f = fminf_d(L.y, R.y);
+            g.ymax_f = fmaxf_d(L.y, R.y);
+            g.inv_slope = fabs(L.y - R.y) != 0 ? (L.x - R.x) / (L.y - R.y) : 0.;
+            const double xmax = find_max(L.x, R.x), xmin = find_min(L.x, R.x);
+            const double ymax = find_max(L.y, R.y), ymin = find_min(L.y, R.y);
+            g.kx0 = order_key(xmin - 0.0008);
+            g.kx1 = order_key(xmax + 0.0008);
+            g.ky0 = order_key(ymin - 0.0008);
+            g.ky1 = order_key(ymax + 0.0008);
+            g.pad = 0;
+            seg.geo[t.seg_first + i] = g;
         }
     }
     __syncthreads();
-    for (int b = threadIdx.x; b < kSegBins; b += blockDim.x)
+    for (int b = threadIdx.x; b < kSegBins; b += blockDim.x) {
         seg.bin_count[c * kSegBins + b] = cnt[b] <= kSegBinCap ? cnt[b] : -1;
+        if (seg.bin_xkey) {
+            // A crossing of a segment lies within its x-range but for the float rounding
+            // of its y-range (the pre-filter's bound below): right of the bin's largest
+            // x by more than that, no segment of the bin counts.  An overflowed bin
+            // takes the bound of all the case's segments.
+            const double xm = cnt[b] > kSegBinCap ? t.seg_xmax : order_key_value(xkey[b]);
+            seg.bin_xkey[c * kSegBins + b] =
+                cnt[b] == 0 ? (long long)0x8000000000000000ull
+                            : order_key(xm + t.seg_dxdy * fmax(fabs(t.seg_ymin), fabs(t.seg_ymax)) *
+                                                 2.384185791015625e-7 + 1e-12);
+        }
+    }
     if (threadIdx.x == 0) {
         t.bin_y0 = y0;
         t.bin_scale = scale;
@@ -69,18 +105,131 @@ __device__ __forceinline__ void seg_bins_block(int c, const SegDev &seg, ToolDev
     }
 }
 
-// inside_judgement over the particle's y-bin (the full scan when it overflowed)
+// on_segment_mesh (actions_gpu.cu:51-63) with the segment's float-rounded y-range
+// and inverse slope from SegGeo: the same operations on the same values.
+__device__ __forceinline__ int on_segment_mesh_geo(double2 left, double2 right, const SegGeo &g, double2 point) {
+    if (point.y <= g.ymax_f && point.y >= g.ymin_f) {
+        if (left.x == right.x && point.x < left.x) return 1;
+        if (fabs(left.y - right.y) != 0) {
+            double x_on_seg = right.x + g.inv_slope * (point.y - right.y);
+            if (x_on_seg > point.x && x_on_seg != left.x) return 1;
+        } else {
+            if (point.x <= fmax(left.x, right.x)) return 1;
+        }
+    }
+    return 0;
+}
+
+// inside_judgement over the particle's y-bin (the full scan when it overflowed);
+// a particle right of the bin's x bound crosses none of its segments
 __device__ __forceinline__ int inside_binned(double2 qp, const SegDev &seg, const ToolDev &tool) {
     const int b = seg_bin_of(qp.y, tool.bin_y0, tool.bin_scale);
+    if (seg.bin_xkey && order_key(qp.x) > seg.bin_xkey[b]) return 0;
     const int n = seg.bin_count[b];
-    if (n < 0) return inside_judgement(qp, seg.left, seg.right, seg.n);
-    const int32_t *list = seg.bin_list + b * kSegBinCap;
     int crossings = 0;
-    for (int k = 0; k < n; k++) {
+    if (n < 0) {
+        if (!seg.geo) return inside_judgement(qp, seg.left, seg.right, seg.n);
+        for (int i = 0; i < seg.n; i++)
+            crossings += on_segment_mesh_geo(__ldg(seg.left + i), __ldg(seg.right + i), seg.geo[i], qp);
+        return crossings & 1;
+    }
+    const int32_t *list = seg.bin_list + b * kSegBinCap;
+    int k = 0;
+    if (seg.geo) {   // two segments' loads in flight (the count is an integer sum: order-free)
+        for (; k + 2 <= n; k += 2) {
+            const int2 i2 = *reinterpret_cast<const int2 *>(list + k);
+            const int ii[2] = {i2.x, i2.y};
+            double2 L[2], R[2], Y[2];
+            double Q[2];
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                L[u] = __ldg(seg.left + ii[u]);
+                R[u] = __ldg(seg.right + ii[u]);
+                Y[u] = *reinterpret_cast<const double2 *>(&seg.geo[ii[u]].ymin_f);
+                Q[u] = seg.geo[ii[u]].inv_slope;
+            }
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                SegGeo g;
+                g.ymin_f = Y[u].x;
+                g.ymax_f = Y[u].y;
+                g.inv_slope = Q[u];
+                crossings += on_segment_mesh_geo(L[u], R[u], g, qp);
+            }
+        }
+    }
+    for (; k < n; k++) {
         const int i = list[k];
-        crossings += on_segment_mesh(__ldg(seg.left + i), __ldg(seg.right + i), qp);
+        crossings += seg.geo ? on_segment_mesh_geo(__ldg(seg.left + i), __ldg(seg.right + i), seg.geo[i], qp)
+                             : on_segment_mesh(__ldg(seg.left + i), __ldg(seg.right + i), qp);
     }
     return crossings & 1;
+}
+
+// find_shortest_distance_v1 (actions_gpu.cu:139-220) with its first loop's
+// bounding-box test on SegGeo's order keys (integer compares, exact for every
+// non-NaN value and false for NaN, as the FP64 compares); the rest as the
+// reference.
+__device__ __forceinline__ int find_shortest_distance_geo(double2 qp, double &dN, double2 &n_re, const SegDev &seg) {
+    const SegGeo *__restrict__ geo = seg.geo;
+    const long long kx = order_key(qp.x), ky = order_key(qp.y);
+    int sg = -1;
+    double depth = FLT_MAX;
+    const double limit_value = 2.5e-4;
+    // the box tests of four segments per round (their keys loaded together), the
+    // candidates then taken in index order as the reference's loop does
+    for (int i0 = 0; i0 < seg.n; i0 += 4) {
+      bool hit[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+          const int i = i0 + u;
+          hit[u] = false;
+          if (i < seg.n) {
+              const longlong2 ka = reinterpret_cast<const longlong2 *>(geo + i)[0];   // kx0, kx1
+              const longlong2 kb = reinterpret_cast<const longlong2 *>(geo + i)[1];   // ky0, ky1
+              hit[u] = kx > ka.x && kx < ka.y && ky > kb.x && ky < kb.y;
+          }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int i = i0 + u;
+        if (!hit[u]) continue;
+        {
+            const double2 L = __ldg(seg.left + i), Rr = __ldg(seg.right + i);
+            const double ymax = find_max(L.y, Rr.y), ymin = find_min(L.y, Rr.y);
+            const double xmax = find_max(L.x, Rr.x), xmin = find_min(L.x, Rr.x);
+            const double2 ni = __ldg(seg.normal + i);
+            const double d = (qp.x - L.x) * ni.x + (qp.y - L.y) * ni.y;
+            if (d >= 0. && d < depth) {
+                const double intersec_x = qp.x - d * ni.x;
+                const double intersec_y = qp.y - d * ni.y;
+                if (intersec_y <= ymax && intersec_y >= ymin && intersec_x <= xmax && intersec_x >= xmin) {
+                    depth = d;
+                    sg = i;
+                }
+            }
+        }
+      }
+    }
+    if (sg != -1 && depth <= limit_value) {
+        const double2 ns = __ldg(seg.normal + sg);
+        n_re = make_double2(-ns.x, -ns.y);
+        dN = -depth;
+        return sg;
+    }
+    return shortest_distance_fallback(qp, dN, n_re, seg.left, seg.right, seg.normal, seg.n, sg);
+}
+
+// The contact search's pre-filter (see contact_s1_one): false means no crossing,
+// so the particle is outside the tool and out of contact.
+__device__ __forceinline__ bool contact_near(double2 pos, const SegDev &seg, const ToolDev &tool) {
+    if (seg.bin_count) {
+        const long long ky = order_key(pos.y);
+        return ky <= tool.key_y1 && ky >= tool.key_y0 && order_key(pos.x) <= tool.key_x1;
+    }
+    return pos.y <= (double)(float)tool.seg_ymax && pos.y >= (double)(float)tool.seg_ymin &&
+           pos.x <= tool.seg_xmax + tool.seg_dxdy * fmax(fabs(tool.seg_ymin), fabs(tool.seg_ymax)) *
+                                       2.384185791015625e-7 + 1e-12;
 }
 
 // ---- contact, one particle: actions_gpu.cu:423-583 (s1) ------------------------------------------
@@ -100,16 +249,7 @@ __device__ __forceinline__ uint32_t contact_s1_one(const KConsts &K, double dt, 
     // particles the FP64 sqrt.)
     // With the y-bins built (k_seg_bins), the two bounds come as order keys and the
     // tests run on the integer pipe.
-    bool near;
-    if (seg.bin_count) {
-        const long long ky = order_key(pos.y);
-        near = ky <= tool.key_y1 && ky >= tool.key_y0 && order_key(pos.x) <= tool.key_x1;
-    } else {
-        near = pos.y <= (double)(float)tool.seg_ymax && pos.y >= (double)(float)tool.seg_ymin &&
-               pos.x <= tool.seg_xmax + tool.seg_dxdy * fmax(fabs(tool.seg_ymin), fabs(tool.seg_ymax)) *
-                                           2.384185791015625e-7 + 1e-12;
-    }
-    if (near) {
+    if (contact_near(pos, seg, tool)) {
         const double ddx = pos.x - tool.tl_point_ref[0], ddy = pos.y - tool.tl_point_ref[1];
         if (sqrt(ddx * ddx + ddy * ddy) < 1.05 * tool.ref_dist)
             inside = seg.bin_count ? inside_binned(pos, seg, tool) : inside_judgement(pos, seg.left, seg.right, seg.n);
@@ -121,7 +261,8 @@ __device__ __forceinline__ uint32_t contact_s1_one(const KConsts &K, double dt, 
     }
     double gN = 0.;
     double2 n_ = make_double2(0., 0.);
-    int seg_no = find_shortest_distance_v1(pos, gN, n_, seg.left, seg.right, seg.normal, seg.n);
+    int seg_no = seg.geo ? find_shortest_distance_geo(pos, gN, n_, seg)
+                         : find_shortest_distance_v1(pos, gN, n_, seg.left, seg.right, seg.normal, seg.n);
     on_seg = seg_no;
     if (seg_no == -1) {
         fc = make_double2(0., 0.); ft = make_double2(0., 0.); nrm = make_double2(0., 0.);
@@ -194,6 +335,15 @@ __device__ __forceinline__ void contact_fem_one(int i, const KConsts &K, const S
         if (cs.bin_count) {
             cs.bin_count += c * kSegBins;
             cs.bin_list += (size_t)c * kSegBins * kSegBinCap;
+        }
+        if (cs.geo) cs.geo += tc.seg_first;
+        if (cs.bin_xkey) cs.bin_xkey += c * kSegBins;
+        if (!contact_near(pos, cs, tc)) {   // the common case: out of contact, no FP64 work
+            put(A.ft[i], make_double2(0., 0.));
+            put(A.n[i], make_double2(0., 0.));
+            A.on_seg[i] = -1;
+            put(A.fc[i], make_double2(0., 0.));
+            return;
         }
         double2 fc = d2(A.fc[i]), ft = d2(A.ft[i]), nrm = d2(A.n[i]);
         int on = A.on_seg[i];
