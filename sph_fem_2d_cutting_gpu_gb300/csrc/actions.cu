@@ -246,6 +246,10 @@ __global__ void __launch_bounds__(kBlock) k_contact_fem(int N, KConsts K, SF A, 
             prefetch_range_l1(seg.geo + tc.seg_first, tc.seg_count);
         }
     }
+    if (seg.geo && seg.bin_xkey && (blockDim.x & 31u) == 0) {   // every lane takes part in the warp searches
+        contact_fem_warp(i, N, K, A, seg, tool, T_nodes, status);
+        return;
+    }
     if (i >= N) return;
     contact_fem_one(i, K, A, seg, tool, T_nodes, status);
 }

@@ -232,6 +232,10 @@ __device__ __forceinline__ bool contact_near(double2 pos, const SegDev &seg, con
                                        2.384185791015625e-7 + 1e-12;
 }
 
+__device__ __forceinline__ uint32_t contact_s1_forces(const KConsts &K, double dt, const ToolDev &tool, double2 vel,
+                                                      int seg_no, double gN, double2 n_, double2 &fc, double2 &ft,
+                                                      double2 &nrm, int &on_seg, double &blanked);
+
 // ---- contact, one particle: actions_gpu.cu:423-583 (s1) ------------------------------------------
 // seg: the segments of the particle's case (and their y-bins); on_seg comes back
 // as an index into them.
@@ -263,6 +267,13 @@ __device__ __forceinline__ uint32_t contact_s1_one(const KConsts &K, double dt, 
     double2 n_ = make_double2(0., 0.);
     int seg_no = seg.geo ? find_shortest_distance_geo(pos, gN, n_, seg)
                          : find_shortest_distance_v1(pos, gN, n_, seg.left, seg.right, seg.normal, seg.n);
+    return contact_s1_forces(K, dt, tool, vel, seg_no, gN, n_, fc, ft, nrm, on_seg, blanked);
+}
+
+// The rest of s1 once the nearest segment is known (actions_gpu.cu:545-583).
+__device__ __forceinline__ uint32_t contact_s1_forces(const KConsts &K, double dt, const ToolDev &tool, double2 vel,
+                                                      int seg_no, double gN, double2 n_, double2 &fc, double2 &ft,
+                                                      double2 &nrm, int &on_seg, double &blanked) {
     on_seg = seg_no;
     if (seg_no == -1) {
         fc = make_double2(0., 0.); ft = make_double2(0., 0.); nrm = make_double2(0., 0.);
@@ -316,6 +327,22 @@ __device__ __forceinline__ void contact_s2_one(const KConsts &K, double dt, cons
 // order of the reference's step.
 // SF: SortedFields (FP64 state) or SortedFields32 (the compact state of FP32K
 // contexts); the contact search runs in FP64 either way.
+// The segments of case c (indices case-local) and its y-bins.
+__device__ __forceinline__ SegDev case_segments(const SegDev &seg, const ToolDev &tc, int c) {
+    SegDev cs = seg;
+    cs.left += tc.seg_first;
+    cs.right += tc.seg_first;
+    cs.normal += tc.seg_first;
+    cs.n = tc.seg_count;
+    if (cs.bin_count) {
+        cs.bin_count += c * kSegBins;
+        cs.bin_list += (size_t)c * kSegBins * kSegBinCap;
+    }
+    if (cs.geo) cs.geo += tc.seg_first;
+    if (cs.bin_xkey) cs.bin_xkey += c * kSegBins;
+    return cs;
+}
+
 template <class SF>
 __device__ __forceinline__ void contact_fem_one(int i, const KConsts &K, const SF &A, const SegDev &seg,
                                                 const ToolDev *__restrict__ tool, const double *__restrict__ T_nodes,
@@ -327,17 +354,7 @@ __device__ __forceinline__ void contact_fem_one(int i, const KConsts &K, const S
         // the particle's case: its tool, time step and interface segments
         const int c = case_of_hash(K, A.hash[i]);
         const ToolDev &tc = tool[c];
-        SegDev cs = seg;
-        cs.left += tc.seg_first;
-        cs.right += tc.seg_first;
-        cs.normal += tc.seg_first;
-        cs.n = tc.seg_count;
-        if (cs.bin_count) {
-            cs.bin_count += c * kSegBins;
-            cs.bin_list += (size_t)c * kSegBins * kSegBinCap;
-        }
-        if (cs.geo) cs.geo += tc.seg_first;
-        if (cs.bin_xkey) cs.bin_xkey += c * kSegBins;
+        const SegDev cs = case_segments(seg, tc, c);
         if (!contact_near(pos, cs, tc)) {   // the common case: out of contact, no FP64 work
             put(A.ft[i], make_double2(0., 0.));
             put(A.n[i], make_double2(0., 0.));
@@ -361,6 +378,196 @@ __device__ __forceinline__ void contact_fem_one(int i, const KConsts &K, const S
             contact_s2_one(K, tc.dt, seg, T_nodes, on, A.rho[i], T);
             put(A.T[i], T);
         }
+    }
+    if (st) set_status(status, st);
+}
+
+// ---- the same contact with the few particles at the tool searched by their whole warp --------------
+// contact_fem_one's results, bit for bit: each segment test and distance is the
+// reference's expression; the loops over a case's segments are spread over the
+// 32 lanes (lane k takes segments k, k + 32, ...) and combined in the reference's
+// order of preference -- the crossing count as a sum, the nearest segment as the
+// smallest (distance, index), the first matching neighbour as the smallest index.
+// Called by every lane of every warp (no lane may have left): 1-D blocks, a
+// multiple of 32 threads.  Needs the y-bins and SegGeo (k_seg_bins).
+constexpr unsigned kFullMask = 0xffffffffu;
+
+__device__ __forceinline__ void warp_argmin(double &d, int &idx) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double d2 = __shfl_xor_sync(kFullMask, d, o);
+        const int i2 = __shfl_xor_sync(kFullMask, idx, o);
+        if (d2 < d || (d2 == d && i2 < idx)) {
+            d = d2;
+            idx = i2;
+        }
+    }
+}
+
+// inside_binned's crossing count over this lane's share of the segments
+__device__ __forceinline__ int crossings_lanes(double2 qp, const SegDev &seg, const ToolDev &tool, int lane) {
+    const int b = seg_bin_of(qp.y, tool.bin_y0, tool.bin_scale);
+    if (order_key(qp.x) > seg.bin_xkey[b]) return 0;
+    const int n = seg.bin_count[b];
+    int crossings = 0;
+    if (n < 0) {
+        for (int i = lane; i < seg.n; i += 32)
+            crossings += on_segment_mesh_geo(__ldg(seg.left + i), __ldg(seg.right + i), seg.geo[i], qp);
+    } else {
+        const int32_t *list = seg.bin_list + b * kSegBinCap;
+        for (int k = lane; k < n; k += 32) {
+            const int i = list[k];
+            crossings += on_segment_mesh_geo(__ldg(seg.left + i), __ldg(seg.right + i), seg.geo[i], qp);
+        }
+    }
+    return crossings;
+}
+
+// find_shortest_distance_v1 by the warp (every lane gets the result)
+__device__ __forceinline__ int shortest_distance_lanes(double2 qp, double &dN, double2 &n_re, const SegDev &seg,
+                                                       int lane) {
+    const long long kx = order_key(qp.x), ky = order_key(qp.y);
+    double best = FLT_MAX;
+    int bi = 0x7fffffff;
+    for (int i = lane; i < seg.n; i += 32) {
+        const SegGeo &g = seg.geo[i];
+        if (kx > g.kx0 && kx < g.kx1 && ky > g.ky0 && ky < g.ky1) {
+            const double2 L = __ldg(seg.left + i), Rr = __ldg(seg.right + i);
+            const double ymax = find_max(L.y, Rr.y), ymin = find_min(L.y, Rr.y);
+            const double xmax = find_max(L.x, Rr.x), xmin = find_min(L.x, Rr.x);
+            const double2 ni = __ldg(seg.normal + i);
+            const double d = (qp.x - L.x) * ni.x + (qp.y - L.y) * ni.y;
+            if (d >= 0. && d < best) {
+                const double intersec_x = qp.x - d * ni.x;
+                const double intersec_y = qp.y - d * ni.y;
+                if (intersec_y <= ymax && intersec_y >= ymin && intersec_x <= xmax && intersec_x >= xmin) {
+                    best = d;
+                    bi = i;
+                }
+            }
+        }
+    }
+    warp_argmin(best, bi);
+    const int sg = bi == 0x7fffffff ? -1 : bi;
+    const double depth = sg == -1 ? (double)FLT_MAX : best;
+    if (sg != -1 && depth <= 2.5e-4) {
+        const double2 ns = __ldg(seg.normal + sg);
+        n_re = make_double2(-ns.x, -ns.y);
+        dN = -depth;
+        return sg;
+    }
+    // the fallback: the nearest right end point (strict <, so the first of equals)
+    double bd = FLT_MAX;
+    int bj = 0x7fffffff;
+    for (int i = lane; i < seg.n; i += 32) {
+        const double2 Rr = __ldg(seg.right + i);
+        const double d_trial = sqrtf_d((qp.x - Rr.x) * (qp.x - Rr.x) + (qp.y - Rr.y) * (qp.y - Rr.y));
+        if (d_trial < bd) {
+            bd = d_trial;
+            bj = i;
+        }
+    }
+    warp_argmin(bd, bj);
+    const int s_near = bj == 0x7fffffff ? sg : bj;
+    const double dep = bj == 0x7fffffff ? (double)FLT_MAX : bd;
+    if (s_near == -1) return -1;
+    const double2 ns = __ldg(seg.normal + s_near);
+    const double2 rs = __ldg(seg.right + s_near);
+    int jm = 0x7fffffff;
+    for (int j = lane; j < seg.n; j += 32) {
+        const double2 Lj = __ldg(seg.left + j);
+        if (Lj.y == rs.y && Lj.x == rs.x) {
+            jm = j;
+            break;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) jm = min(jm, __shfl_xor_sync(kFullMask, jm, o));
+    double nsx = ns.x, nsy = ns.y;
+    if (jm != 0x7fffffff) {
+        const double2 nj = __ldg(seg.normal + jm);
+        nsx = (nj.x + ns.x) / 2.;
+        nsy = (nj.y + ns.y) / 2.;
+    }
+    const double n_length = sqrtf_d(nsx * nsx + nsy * nsy);
+    n_re = make_double2(-nsx / n_length, -nsy / n_length);
+    dN = -1.0 * dep;
+    return s_near;
+}
+
+template <class SF>
+__device__ __forceinline__ void contact_fem_warp(int i, int N, const KConsts &K, const SF &A, const SegDev &seg,
+                                                 const ToolDev *__restrict__ tool,
+                                                 const double *__restrict__ T_nodes, uint32_t *status) {
+    const int lane = (int)(threadIdx.x & 31u);
+    const bool live = i < N && !flag_is_one(A.blanked[i]);
+    double2 pos = make_double2(0., 0.);
+    int c = 0;
+    bool near = false, probe = false;
+    if (live) {
+        pos = A.pos[i];
+        c = case_of_hash(K, A.hash[i]);
+        const ToolDev &tc = tool[c];
+        near = contact_near(pos, case_segments(seg, tc, c), tc);
+        if (!near) {   // out of contact: zeros, no FP64 work
+            put(A.ft[i], make_double2(0., 0.));
+            put(A.n[i], make_double2(0., 0.));
+            A.on_seg[i] = -1;
+            put(A.fc[i], make_double2(0., 0.));
+        } else {
+            const double ddx = pos.x - tc.tl_point_ref[0], ddy = pos.y - tc.tl_point_ref[1];
+            probe = sqrt(ddx * ddx + ddy * ddy) < 1.05 * tc.ref_dist;
+        }
+    }
+    // the ray casting of each probing lane, by the warp
+    int inside = 0;
+    for (unsigned pend = __ballot_sync(kFullMask, probe); pend; pend &= pend - 1) {
+        const int src = __ffs(pend) - 1;
+        const double2 qp = make_double2(__shfl_sync(kFullMask, pos.x, src), __shfl_sync(kFullMask, pos.y, src));
+        const int cc = __shfl_sync(kFullMask, c, src);
+        const int cr = __reduce_add_sync(kFullMask, crossings_lanes(qp, case_segments(seg, tool[cc], cc), tool[cc], lane));
+        if (lane == src) inside = cr & 1;
+    }
+    // the nearest segment of each lane inside the tool, by the warp
+    int seg_no = -1;
+    double gN = 0.;
+    double2 n_ = make_double2(0., 0.);
+    for (unsigned pend = __ballot_sync(kFullMask, inside != 0); pend; pend &= pend - 1) {
+        const int src = __ffs(pend) - 1;
+        const double2 qp = make_double2(__shfl_sync(kFullMask, pos.x, src), __shfl_sync(kFullMask, pos.y, src));
+        const int cc = __shfl_sync(kFullMask, c, src);
+        double dN;
+        double2 nr;
+        const int r = shortest_distance_lanes(qp, dN, nr, case_segments(seg, tool[cc], cc), lane);
+        if (lane == src) {
+            seg_no = r;
+            gN = dN;
+            n_ = nr;
+        }
+    }
+    if (!near) return;
+    const ToolDev &tc = tool[c];
+    double2 fc = d2(A.fc[i]), ft = d2(A.ft[i]), nrm = d2(A.n[i]);
+    int on = A.on_seg[i];
+    double bl = 0.;
+    uint32_t st = 0;
+    if (inside == 0) {
+        fc = make_double2(0., 0.); ft = make_double2(0., 0.); nrm = make_double2(0., 0.);
+        on = -1;
+    } else {
+        st = contact_s1_forces(K, tc.dt, tc, d2(A.vel[i]), seg_no, gN, n_, fc, ft, nrm, on, bl);
+    }
+    if (on >= 0) on += tc.seg_first;   // global segment id
+    const bool blanked = flag_is_one(bl);
+    if (blanked) put(A.blanked[i], 1.);
+    put(A.ft[i], ft);
+    put(A.n[i], nrm);
+    A.on_seg[i] = on;
+    put(A.fc[i], fc);
+    if (!blanked && on >= 0 && on < seg.n) {
+        double T = A.T[i];
+        contact_s2_one(K, tc.dt, seg, T_nodes, on, A.rho[i], T);
+        put(A.T[i], T);
     }
     if (st) set_status(status, st);
 }
