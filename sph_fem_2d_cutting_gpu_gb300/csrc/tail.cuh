@@ -516,7 +516,9 @@ __device__ __forceinline__ void contact_fem_warp(int i, int N, const KConsts &K,
             put(A.fc[i], make_double2(0., 0.));
         } else {
             const double ddx = pos.x - tc.tl_point_ref[0], ddy = pos.y - tc.tl_point_ref[1];
-            probe = sqrt(ddx * ddx + ddy * ddy) < 1.05 * tc.ref_dist;
+            // right of every segment of its y-bin a particle crosses none (no scan needed)
+            probe = sqrt(ddx * ddx + ddy * ddy) < 1.05 * tc.ref_dist &&
+                    order_key(pos.x) <= seg.bin_xkey[c * kSegBins + seg_bin_of(pos.y, tc.bin_y0, tc.bin_scale)];
         }
     }
     // the ray casting of each probing lane, by the warp
