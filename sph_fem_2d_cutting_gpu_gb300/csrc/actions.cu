@@ -208,44 +208,11 @@ __global__ void __launch_bounds__(kBlock) k_fric_heat_rigid(int N, KConsts K, So
 }
 
 // ---- the FEM tool's contact of the fused step and the fused tail (tail.cuh) ---------------------------
-// A block holding a particle inside its case's pre-filter bounds first pulls that
-// case's segments (end points, normals, SegGeo) into L1: the few particles near
-// the tool then run their segment loops on L1 hits instead of a chain of L2
-// round trips (a hint only; every result is computed as before).
-__device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
-template <class T>
-__device__ __forceinline__ void prefetch_range_l1(const T *p, int n) {
-    const char *b = reinterpret_cast<const char *>(p);
-    const int bytes = n * (int)sizeof(T);
-    for (int o = (int)threadIdx.x * 128; o < bytes; o += (int)blockDim.x * 128) prefetch_l1(b + o);
-}
-
 template <class SF>
 __global__ void __launch_bounds__(kBlock) k_contact_fem(int N, KConsts K, SF A, SegDev seg,
                                                         const ToolDev *__restrict__ tool,
                                                         const double *__restrict__ T_nodes, uint32_t *status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (seg.geo) {   // block-uniform
-        __shared__ int s_case;
-        if (threadIdx.x == 0) s_case = -1;
-        __syncthreads();
-        if (i < N && !flag_is_one(A.blanked[i])) {
-            const int c = case_of_hash(K, A.hash[i]);
-            const ToolDev &tc = tool[c];
-            const double2 pos = A.pos[i];
-            const long long ky = order_key(pos.y);
-            if (ky <= tc.key_y1 && ky >= tc.key_y0 && order_key(pos.x) <= tc.key_x1) atomicMax(&s_case, c);
-        }
-        __syncthreads();
-        const int c = s_case;
-        if (c >= 0) {
-            const ToolDev &tc = tool[c];
-            prefetch_range_l1(seg.left + tc.seg_first, tc.seg_count);
-            prefetch_range_l1(seg.right + tc.seg_first, tc.seg_count);
-            prefetch_range_l1(seg.normal + tc.seg_first, tc.seg_count);
-            prefetch_range_l1(seg.geo + tc.seg_first, tc.seg_count);
-        }
-    }
     if (seg.geo && seg.bin_xkey && (blockDim.x & 31u) == 0) {   // every lane takes part in the warp searches
         contact_fem_warp(i, N, K, A, seg, tool, T_nodes, status);
         return;
